@@ -1,0 +1,270 @@
+/*
+ * ref_driver -- runs the UNMODIFIED Object-MD reference force path on one
+ * rank and writes what the parity tests compare against.  Test
+ * infrastructure only: it is built (by oracle/ref/Makefile) from the
+ * reference's own sources and links nothing of this project's product.
+ *
+ * The program is an ordinary Object-MD application, written the way the
+ * reference's own test programs are (test/example/example.cpp:5-34): an
+ * MDSystemGrid subclass whose CreateSystem/CreateGadget/SystemSetting pick a
+ * potential, an iterator and the periodic box.  Everything else - the
+ * linked-cell Verlet list, the periodic ghost images, the force loop, the
+ * velocity-Verlet integrator - is the reference's code.
+ *
+ * usage: ref_driver <outdir> key value ...     (keys below; all values text)
+ *   import      <file>   atoms in the reference Import format (container.cpp:290)
+ *   kind        eam|pair|sw        force kernel family
+ *   table       <name>   table / parameter name searched in $OMD_TABLE
+ *   pair2       <name>   optional projectile-target pair table (two-species inputs)
+ *   steps       <n>      0 = one static force evaluation (system.cpp:1034 RunStatic)
+ *   dt          <ps>     time step
+ *   skin        <A>      comm.tolerance (absolute)
+ *   refresh     <n>      comm.refresh (0 = every step)
+ *   tcontrol    <T> <tau>  Berendsen TempController (TempController.h:78-91)
+ *   dump_nbr    0|1      write the neighbour tuples of the final list
+ *   time_only   0|1      only print the RunKernel wall time
+ *
+ * Outputs in <outdir>: atoms.txt (nid x y z vx vy vz fx fy fz potential virial
+ * for local atoms sorted by nid), nbr.txt (nid_i nid_j sx sy sz), ledger.txt
+ * (step kinetic potential energy), summary.txt.
+ */
+#include <omd/systemgrid.h>
+#include <omd/integrator.h>
+#include <potential/team.h>
+/* tpair.h names omd types unqualified, as it does inside the reference's omd.h */
+using namespace omd;
+#include <potential/tpair.h>
+#include <potential/sw.h>
+#include <modify/VerletList.h>
+#include <modify/VerletListFull.h>
+#include <modify/TempController.h>
+
+#include <sys/time.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+
+using namespace omd;
+
+static double wall_now() {
+    struct timeval tv;
+    gettimeofday(&tv, 0);
+    return tv.tv_sec + 1e-6 * tv.tv_usec;
+}
+
+struct NbrTuple {
+    int i, j, sx, sy, sz;
+    bool operator<(const NbrTuple& o) const {
+        if (i != o.i) return i < o.i;
+        if (j != o.j) return j < o.j;
+        if (sx != o.sx) return sx < o.sx;
+        if (sy != o.sy) return sy < o.sy;
+        return sz < o.sz;
+    }
+};
+
+class OracleSim;
+
+/* Records every (at,to) pair the iterator visits in its half loop. */
+class PairRecorder : public MDGadget {
+public:
+    std::vector<std::pair<int, int> > pairs;
+    bool PreIterationNode(int) { return true; }
+    void IterationNode(int at, int to) { pairs.push_back(std::make_pair(at, to)); }
+};
+
+class OracleSim : public MDSystemGrid {
+public:
+    std::map<std::string, std::vector<std::string> > opt;
+    std::string outdir;
+    int nsteps;
+    double t_begin, t_end;
+    FILE* ledger;
+
+    OracleSim(int& argc, char**& argv, const std::string& od,
+              const std::map<std::string, std::vector<std::string> >& o)
+        : MDSystemGrid(argc, argv), opt(o), outdir(od), nsteps(0), t_begin(0), t_end(0), ledger(0) {
+        nsteps = atoi(get("steps", "0").c_str());
+    }
+
+    std::string get(const std::string& k, const std::string& def, int idx = 0) {
+        std::map<std::string, std::vector<std::string> >::iterator it = opt.find(k);
+        if (it == opt.end() || (int)it->second.size() <= idx) return def;
+        return it->second[idx];
+    }
+
+    void CreateSystem() { Import(get("import", "")); }
+
+    void CreateGadget() {
+        SetIntegrator(new MDIntegrator(atof(get("dt", "0.001").c_str())));
+        std::string kind = get("kind", "eam");
+        std::string table = get("table", "aluminum");
+        std::string pair2 = get("pair2", "");
+        ForceKernel* k = 0;
+        if (kind == "eam") {
+            k = new TForceEAM(table);
+            AddModify(new VerletList);
+        } else if (kind == "pair") {
+            k = new TForcePair(table);
+            AddModify(new VerletList);
+        } else if (kind == "sw") {
+            k = new StillingerWeber(table);
+            AddModify(new VerletListFull);
+        } else {
+            die("unknown kind " + kind);
+        }
+        /* Two-species inputs name their containers "target" and "projectile"
+           (the convention of test/si-impact/atom.dat). */
+        if (pair2.empty()) {
+            AddForce(k);
+        } else {
+            AddForce(k, "target", "target");
+            AddForce(new TForcePair(pair2), "projectile", "target");
+        }
+        if (opt.count("tcontrol"))
+            AddModify(new TempController(atof(get("tcontrol", "300", 0).c_str()),
+                                         atof(get("tcontrol", "0.1", 1).c_str())));
+    }
+
+    void SystemSetting() {}
+
+    bool CheckRun() {
+        bool base = MDSystemGrid::CheckRun();
+        if (ledger && Step > 0)
+            fprintf(ledger, "%d %.17g %.17g %.17g\n", Step, Kinetic, Potential, Energy);
+        return base && Step < nsteps;
+    }
+
+    void BeforeRun() {
+        if (get("time_only", "0") == "0") {
+            ledger = fopen((outdir + "/ledger.txt").c_str(), "w");
+            if (ledger)
+                fprintf(ledger, "%d %.17g %.17g %.17g\n", 0, Kinetic, BasePotential, 0.0);
+        }
+        t_begin = wall_now();
+    }
+
+    void AfterRun() {
+        t_end = wall_now();
+        int nloc = GetLocalAtomNumber();
+        FILE* s = fopen((outdir + "/summary.txt").c_str(), "w");
+        if (s) {
+            fprintf(s, "local_atoms %d\nall_atoms %d\nsteps %d\nseconds %.9g\n", nloc, GetNAtom(), Step,
+                    t_end - t_begin);
+            fprintf(s, "potential %.17g\nkinetic %.17g\nbase_potential %.17g\nvirial %.17g\n", Potential,
+                    Kinetic, BasePotential, Virial);
+            fprintf(s, "box %.17g %.17g %.17g %.17g %.17g %.17g\n", Box.x0, Box.y0, Box.z0, Box.x1, Box.y1,
+                    Box.z1);
+            fprintf(s, "max_cut_radius %.17g\n", GetMaxCutRadius());
+            fclose(s);
+        }
+        if (ledger) {
+            fprintf(ledger, "%d %.17g %.17g %.17g\n", Step, Kinetic, Potential, Energy);
+            fclose(ledger);
+            ledger = 0;
+        }
+        if (get("time_only", "0") != "0") {
+            printf("atom_steps_per_s %.6g local_atoms %d steps %d seconds %.6f\n",
+                   (double)nloc * Step / (t_end - t_begin), nloc, Step, t_end - t_begin);
+            return;
+        }
+        std::vector<int> order(nloc);
+        for (int i = 0; i < nloc; i++) order[i] = i;
+        std::sort(order.begin(), order.end(), CompareNid(this));
+        FILE* f = fopen((outdir + "/atoms.txt").c_str(), "w");
+        for (int k = 0; k < nloc; k++) {
+            Atom& a = Atoms(order[k]);
+            fprintf(f, "%d %d %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", a.nid, a.tid,
+                    a.x, a.y, a.z, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz, a.potential, a.virial);
+        }
+        fclose(f);
+        if (get("dump_nbr", "0") != "0") DumpNeighbours();
+    }
+
+    struct CompareNid {
+        OracleSim* s;
+        CompareNid(OracleSim* ss) : s(ss) {}
+        bool operator()(int a, int b) const { return s->Atoms(a).nid < s->Atoms(b).nid; }
+    };
+
+    /* Image vector of atom idx relative to its owner, in box lengths. */
+    void ImageOf(int idx, const std::map<int, int>& owner, int& sx, int& sy, int& sz) {
+        Atom& g = Atoms(idx);
+        Atom& o = Atoms(owner.find(g.nid)->second);
+        sx = (int)lround((g.x - o.x) / Box.lx);
+        sy = (int)lround((g.y - o.y) / Box.ly);
+        sz = (int)lround((g.z - o.z) / Box.lz);
+    }
+
+    void DumpNeighbours() {
+        int nloc = GetLocalAtomNumber();
+        std::map<int, int> owner;
+        for (int i = 0; i < nloc; i++) owner[Atoms(i).nid] = i;
+        PairRecorder rec;
+        GetIterator()->IterateHalf(&rec);
+        std::vector<NbrTuple> t;
+        for (size_t k = 0; k < rec.pairs.size(); k++) {
+            int at = rec.pairs[k].first, to = rec.pairs[k].second;
+            bool gat = at >= nloc, gto = to >= nloc;
+            int sx, sy, sz;
+            if (!gat && !gto) {
+                NbrTuple a = {Atoms(at).nid, Atoms(to).nid, 0, 0, 0};
+                NbrTuple b = {Atoms(to).nid, Atoms(at).nid, 0, 0, 0};
+                t.push_back(a);
+                t.push_back(b);
+            } else if (!gat && gto) {
+                ImageOf(to, owner, sx, sy, sz);
+                NbrTuple a = {Atoms(at).nid, Atoms(to).nid, sx, sy, sz};
+                t.push_back(a);
+            } else if (gat && !gto) {
+                ImageOf(at, owner, sx, sy, sz);
+                NbrTuple a = {Atoms(to).nid, Atoms(at).nid, sx, sy, sz};
+                t.push_back(a);
+            }
+        }
+        std::sort(t.begin(), t.end());
+        FILE* f = fopen((outdir + "/nbr.txt").c_str(), "w");
+        for (size_t k = 0; k < t.size(); k++)
+            fprintf(f, "%d %d %d %d %d\n", t[k].i, t[k].j, t[k].sx, t[k].sy, t[k].sz);
+        fclose(f);
+    }
+};
+
+int main(int argc, char** argv) {
+    if (argc < 2) {
+        fprintf(stderr, "usage: ref_driver <outdir> key value ...\n");
+        return 2;
+    }
+    std::string outdir = argv[1];
+    std::map<std::string, std::vector<std::string> > opt;
+    for (int i = 2; i < argc;) {
+        std::string key = argv[i++];
+        int nval = (key == "tcontrol") ? 2 : 1;
+        for (int k = 0; k < nval && i < argc; k++) opt[key].push_back(argv[i++]);
+    }
+    /* Reference parameters go through the reference's own ParamHandler argv path. */
+    std::vector<std::string> args;
+    args.push_back(argv[0]);
+    args.push_back("comm.tolerance");
+    args.push_back(opt.count("skin") ? opt["skin"][0] : std::string("0.3"));
+    if (opt.count("refresh") && atoi(opt["refresh"][0].c_str()) > 0) {
+        args.push_back("comm.refresh");
+        args.push_back(opt["refresh"][0]);
+    }
+    args.push_back("time.step");
+    args.push_back(opt.count("dt") ? opt["dt"][0] : std::string("0.001"));
+    args.push_back("time.max");
+    args.push_back("1e30");
+    args.push_back("--silent");
+    if (!opt.count("steps") || atoi(opt["steps"][0].c_str()) == 0) args.push_back("mode.static");
+    std::vector<char*> cargs;
+    for (size_t i = 0; i < args.size(); i++) cargs.push_back(const_cast<char*>(args[i].c_str()));
+    cargs.push_back(0);
+    int cargc = (int)args.size();
+    char** cargv = &cargs[0];
+    OracleSim sim(cargc, cargv, outdir, opt);
+    return sim.Run();
+}

@@ -1,0 +1,155 @@
+/*
+ * omdg.h -- C ABI of libomdg, the GB300 (sm_103a) force-evaluation engine for
+ * Object-MD.  Plain C types only; every call returns an int status
+ * (OMDG_OK = 0, negative OMDG_E* on failure; omdg_last_error() gives text).
+ *
+ * One context owns one simulation box on one GPU: atoms, tables, neighbour
+ * list and integrator state live in device memory; the caller owns every host
+ * buffer it passes.  A context is used by one host thread at a time and all
+ * its work is ordered on the context's CUDA stream.
+ *
+ * Atom order: the library keeps atoms sorted by linked cell internally; every
+ * array passed in or out is in the caller's order (the order of
+ * omdg_set_atoms), which for an Object-MD application is the enumeration
+ * order nid (system.cpp:389-397).
+ *
+ * Each entry point names the reference interface it replaces.  Paths are
+ * relative to the Object-MD source tree.
+ */
+#ifndef OMDG_H
+#define OMDG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OMDG_OK 0
+#define OMDG_EINVAL (-1)        /* bad argument */
+#define OMDG_ECUDA (-2)         /* CUDA runtime error */
+#define OMDG_ERANGE (-3)        /* table read outside its range: TableReader::read dies (treader.cpp:199-218) */
+#define OMDG_EOVERLAP (-4)      /* r^2 < 1e-6: CalcSqrDistance dies (gadget.cpp:149-159) */
+#define OMDG_ENOMEM (-5)        /* device allocation failed */
+#define OMDG_ESTATE (-6)        /* call out of order (e.g. no atoms yet) */
+#define OMDG_EFILE (-7)         /* table / parameter file missing or malformed */
+#define OMDG_ENONFINITE (-8)    /* NaN or Inf in positions or forces */
+
+typedef struct omdg_ctx omdg_ctx;
+
+/* ---------------------------------------------------------------- context */
+
+/* Replaces MDSystem construction (system.h:257) for the force path. */
+int omdg_create(omdg_ctx** ctx, int device);
+int omdg_destroy(omdg_ctx* ctx);
+const char* omdg_last_error(omdg_ctx* ctx);
+/* The context's cudaStream_t, for callers that record events on it. */
+int omdg_get_stream(omdg_ctx* ctx, void** stream);
+
+/* ------------------------------------------------------------- atoms, box */
+
+/* MDSystem::SetBox (system.cpp:849-858) + boundary.periodic (system.cpp:228-237). */
+int omdg_set_box(omdg_ctx* ctx, const double lo[3], const double hi[3], const int periodic[3]);
+
+/*
+ * Atoms as the reference's Import/AtomContainer holds them (base.h:114-125):
+ * x, v are n*3 FP64 (A, A/ps); type is the container id tid (0..ntypes-1);
+ * mass_by_type in simulation units (amu / 9648.53397731809, container.cpp:94);
+ * z_by_type the atomic numbers (used by ZBL cores).  v may be NULL (zero).
+ */
+int omdg_set_atoms(omdg_ctx* ctx, int n, const double* x, const double* v, const int* type, int ntypes,
+                   const double* mass_by_type, const double* z_by_type);
+int omdg_num_atoms(omdg_ctx* ctx, int* n);
+
+/* Copies device state to host arrays in caller order; any pointer may be NULL.
+   x, v, f are n*3; pot, vir are n (per-atom potential and virial as Atom::potential/virial). */
+int omdg_get_state(omdg_ctx* ctx, double* x, double* v, double* f, double* pot, double* vir);
+/* Overwrites positions / velocities (n*3 FP64, caller order); marks the list dirty. */
+int omdg_set_positions(omdg_ctx* ctx, const double* x);
+int omdg_set_velocities(omdg_ctx* ctx, const double* v);
+
+/* --------------------------------------------------------- force kernels */
+
+/*
+ * TForceEAM(table) + its auto-created TEmbedding (team.cpp:166-237, :37-145):
+ * reads the PAIR, EDENS and EMBED sections of the Object-MD table file with
+ * TableReader semantics (treader.cpp:37-264).  type_a == type_b only.
+ */
+int omdg_add_eam(omdg_ctx* ctx, int type_a, int type_b, const char* table_file);
+
+/* TForcePair(table) (tpair.h:38-71); fp64 != 0 evaluates it in FP64 end to end. */
+int omdg_add_pair_table(omdg_ctx* ctx, int type_a, int type_b, const char* table_file, int fp64);
+
+/* StillingerWeber(material) (sw.cpp:35-273), parameters from an sw.* file.
+   Every triplet is evaluated (the reference's sw.cpp:261 guard is not reproduced). */
+int omdg_add_sw(omdg_ctx* ctx, int type_a, int type_b, const char* param_file);
+
+/* Tersoff(material) (include/potential/tersoff.h:104), tersoff.* keys;
+   the bond-order form of Tersoff, PRB 37, 6991 (1988). */
+int omdg_add_tersoff(omdg_ctx* ctx, int type_a, int type_b, const char* param_file);
+
+/* Universal ZBL screened Coulomb pair (sw.cpp:118-146 form) between two types,
+   cut at rc with a smoothing switch over [rc - width, rc]. */
+int omdg_add_zbl(omdg_ctx* ctx, int type_a, int type_b, double rc, double width);
+
+/* Max cut radius over all kernels (integrator.cpp:108-113). */
+int omdg_max_cut_radius(omdg_ctx* ctx, double* rc);
+
+/* --------------------------------------------------------- neighbour list */
+
+/*
+ * VerletList / VerletListFull with comm.tolerance `skin` (absolute) as the
+ * MDSystemGrid radius tolerance (systemgrid.cpp:610-617): Rv = rc_max + skin.
+ * rebuild_every > 0 rebuilds every that many steps (comm.refresh);
+ * rebuild_every == 0 rebuilds when any atom moved more than skin/2 since the
+ * last build (displacement trigger).
+ */
+int omdg_set_neighbor(omdg_ctx* ctx, double skin, int rebuild_every);
+int omdg_build_neighbors(omdg_ctx* ctx);
+/*
+ * Canonical neighbour tuples of the current list, caller order: for atom i
+ * the entries (j, code) with code = (sx+1) + 3(sy+1) + 9(sz+1) the image of
+ * j.  offsets has n+1 entries; j/code have capacity `cap`; *count receives
+ * the number of tuples (also when cap is too small, then OMDG_EINVAL).
+ */
+int omdg_get_neighbors(omdg_ctx* ctx, int* offsets, int* nbr_j, int* nbr_code, long cap, long* count);
+
+/* ----------------------------------------------------- force / integration */
+
+/* MDIntegrator::Iterate (integrator.cpp:203-216): one force evaluation. */
+int omdg_compute_forces(omdg_ctx* ctx);
+
+/* MDIntegrator(dt) / time.step (integrator.cpp:116-122). */
+int omdg_set_timestep(omdg_ctx* ctx, double dt);
+
+/*
+ * nsteps of RunKernel (system.cpp:964-983): Integrate (integrator.cpp:225-259),
+ * MeasurePotential/MeasureKinetic, POST_INTEGRATION modifies.  The first call
+ * runs FirstRun (system.cpp:860-873) first; with reference_first_step != 0 it
+ * zeroes the forces afterwards as the reference does.
+ */
+int omdg_step(omdg_ctx* ctx, int nsteps);
+int omdg_set_first_step_mode(omdg_ctx* ctx, int reference_first_step);
+
+/*
+ * Energy ledger of the last completed step: kinetic, potential (non-ghost,
+ * active atoms), base potential of FirstRun and virial/2
+ * (system.cpp:1060-1094, :971).  Energy = kinetic + potential - base.
+ */
+int omdg_ledger(omdg_ctx* ctx, double* kinetic, double* potential, double* base_potential, double* virial);
+/* Per-step ledger rows (kinetic, potential) of the last omdg_step call, up to cap rows. */
+int omdg_ledger_history(omdg_ctx* ctx, double* kinetic, double* potential, int cap, int* rows);
+
+/* TempController(T, tau) (TempController.h:51-91); tau <= 0 removes it. */
+int omdg_set_thermostat(omdg_ctx* ctx, double temperature, double tau);
+
+/* Number of neighbour-list builds so far and of kernel launches issued by the last omdg_step. */
+int omdg_stats(omdg_ctx* ctx, long* rebuilds, long* launches);
+
+/* Per-kernel CUDA-event timing of subsequent omdg_step calls (tracing). */
+int omdg_set_profiling(omdg_ctx* ctx, int on);
+/* name_buf receives "name;name;..."; ms[] the summed milliseconds, calls[] the launch counts. */
+int omdg_kernel_times(omdg_ctx* ctx, char* name_buf, int name_cap, double* ms, long* calls, int cap, int* nkern);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

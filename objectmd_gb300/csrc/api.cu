@@ -1,0 +1,1099 @@
+// C ABI of libomdg (include/omdg.h): context lifetime, atom/box upload,
+// potential registration, neighbour list control, the step driver (eager or
+// a captured CUDA graph with a conditional rebuild node) and read-back.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+
+#include "device_common.cuh"
+
+namespace omdg {
+
+size_t step_state_bytes();
+int step_state_init(Context* c);
+int step_state_reset(Context* c, int reset_row, int rebuild_every);
+int step_state_read(Context* c, long long* step, int* row, int* rebuild);
+int step_clear_rebuild(Context* c);
+int launch_set_rebuild_cond(Context* c, cudaGraphConditionalHandle h);
+int threebody_prepare(Context* c);
+
+int set_error(Context* c, int code, const std::string& msg) {
+    if (c) c->last_error = msg;
+    return code;
+}
+
+int check_cuda(Context* c, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return OMDG_OK;
+    return set_error(c, e == cudaErrorMemoryAllocation ? OMDG_ENOMEM : OMDG_ECUDA,
+                     std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int check_status(Context* c) {
+    unsigned st = 0;
+    cudaError_t e = cudaMemcpyAsync(&st, c->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "status read");
+    if (!st) return OMDG_OK;
+    unsigned zero = 0;
+    cudaMemcpyAsync(c->d_status, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, c->stream);
+    cudaStreamSynchronize(c->stream);
+    if (st & ERR_TABLE_RANGE)
+        return set_error(c, OMDG_ERANGE, "table read outside its range (the reference dies here: treader.cpp:199-218)");
+    if (st & ERR_OVERLAP) return set_error(c, OMDG_EOVERLAP, "overlapping atoms: r^2 < 1e-6 (gadget.cpp:149)");
+    if (st & ERR_NONFINITE) return set_error(c, OMDG_ENONFINITE, "non-finite position or force");
+    if (st & ERR_NBR_OVERFLOW) return set_error(c, OMDG_ESTATE, "neighbour capacity exceeded");
+    return set_error(c, OMDG_ECUDA, "device status word set");
+}
+
+// ------------------------------------------------------------- profiling
+static cudaEvent_t take_event(Context* c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+static int timer_index(Context* c, const char* name) {
+    for (size_t k = 0; k < c->timers.size(); k++)
+        if (c->timers[k].name == name) return (int)k;
+    c->timers.push_back(KernelTimer{name, 0.0, 0});
+    return (int)c->timers.size() - 1;
+}
+
+static int g_open_timer = -1;
+static cudaEvent_t g_open_event = nullptr;
+
+void prof_begin(Context* c, const char* name) {
+    if (!c->profiling) return;
+    g_open_timer = timer_index(c, name);
+    g_open_event = take_event(c);
+    cudaEventRecord(g_open_event, c->stream);
+}
+
+void prof_end(Context* c) {
+    if (!c->profiling || g_open_timer < 0) return;
+    cudaEvent_t e = take_event(c);
+    cudaEventRecord(e, c->stream);
+    c->pending.push_back(std::make_pair(g_open_timer, std::make_pair(g_open_event, e)));
+    g_open_timer = -1;
+}
+
+void prof_collect(Context* c) {
+    if (c->pending.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    for (auto& p : c->pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+        c->timers[p.first].ms += ms;
+        c->timers[p.first].calls++;
+        c->event_pool.push_back(p.second.first);
+        c->event_pool.push_back(p.second.second);
+    }
+    c->pending.clear();
+}
+
+// ------------------------------------------------------------- memory
+template <typename T>
+static bool dalloc(T*& p, size_t count) {
+    cudaFree(p);
+    p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc(&p, count * sizeof(T)) == cudaSuccess;
+}
+
+static void free_atoms(Context* c) {
+    void* ptrs[] = {c->x,    c->y,     c->z,      c->vx,     c->vy,          c->vz,          c->fx,
+                    c->fy,   c->fz,    c->pe,     c->vir,    c->pack,        c->xref,        c->type,
+                    c->id,   c->inv,   c->fp,     c->femb,   c->cell,        c->perm,        c->stage_d,
+                    c->stage_i, c->cell_sorted, c->f64, c->extra, c->stage_extra, c->nnb, c->d_red};
+    for (void* p : ptrs) cudaFree(p);
+    c->x = c->y = c->z = c->vx = c->vy = c->vz = nullptr;
+    c->fx = c->fy = c->fz = c->pe = c->vir = nullptr;
+    c->pack = nullptr;
+    c->xref = nullptr;
+    c->type = c->id = c->inv = nullptr;
+    c->fp = c->femb = nullptr;
+    c->cell = c->perm = nullptr;
+    c->stage_d = nullptr;
+    c->stage_i = nullptr;
+    c->cell_sorted = nullptr;
+    c->f64 = nullptr;
+    c->extra = c->stage_extra = nullptr;
+    c->nnb = nullptr;
+    c->d_red = nullptr;
+    c->cap = 0;
+}
+
+static int alloc_atoms(Context* c, int n) {
+    free_atoms(c);
+    int cap = n;
+    bool ok = dalloc(c->x, cap) && dalloc(c->y, cap) && dalloc(c->z, cap) && dalloc(c->vx, cap) &&
+              dalloc(c->vy, cap) && dalloc(c->vz, cap) && dalloc(c->fx, cap) && dalloc(c->fy, cap) &&
+              dalloc(c->fz, cap) && dalloc(c->pe, cap) && dalloc(c->vir, cap) && dalloc(c->pack, cap) &&
+              dalloc(c->xref, cap) && dalloc(c->type, cap) && dalloc(c->id, cap) && dalloc(c->inv, cap) &&
+              dalloc(c->fp, cap) && dalloc(c->femb, cap) && dalloc(c->cell, cap) && dalloc(c->perm, cap) &&
+              dalloc(c->stage_d, (size_t)6 * cap) && dalloc(c->stage_i, (size_t)2 * cap) &&
+              dalloc(c->cell_sorted, cap) && dalloc(c->nnb, cap);
+    int nb = grid_for(cap, 256) + 1;
+    ok = ok && dalloc(c->d_red, (size_t)3 * nb);
+    if (!ok) return set_error(c, OMDG_ENOMEM, "atom arrays");
+    c->cap = cap;
+    c->red_cap = nb;
+    cudaMemsetAsync(c->fx, 0, sizeof(float) * cap, c->stream);
+    cudaMemsetAsync(c->fy, 0, sizeof(float) * cap, c->stream);
+    cudaMemsetAsync(c->fz, 0, sizeof(float) * cap, c->stream);
+    cudaMemsetAsync(c->pe, 0, sizeof(float) * cap, c->stream);
+    cudaMemsetAsync(c->vir, 0, sizeof(float) * cap, c->stream);
+    return OMDG_OK;
+}
+
+static void invalidate_graph(Context* c);
+
+// ------------------------------------------------------------- geometry
+static void compute_frame(Context* c) {
+    BoxGeom& b = c->box;
+    double ext = 0;
+    for (int d = 0; d < 3; d++) ext = std::max(ext, b.L[d]);
+    double P = 2048.0;
+    while (P < 8.0 * ext) P *= 2.0;
+    for (int d = 0; d < 3; d++) {
+        b.org[d] = b.lo[d];
+        b.P[d] = P;
+        b.Lh[d] = (float)b.L[d];
+        b.Ll[d] = (float)(b.L[d] - (double)b.Lh[d]);
+    }
+}
+
+}  // namespace omdg
+
+using namespace omdg;
+
+struct omdg_ctx : public Context {};
+
+static Context* C(omdg_ctx* c) { return static_cast<Context*>(c); }
+
+// graph state kept beside the context
+struct GraphState {
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaStream_t side = nullptr;
+    bool valid = false;
+};
+static std::map<Context*, GraphState> g_graphs;
+
+namespace omdg {
+static void invalidate_graph(Context* c) {
+    auto it = g_graphs.find(c);
+    if (it == g_graphs.end()) return;
+    if (it->second.exec) cudaGraphExecDestroy(it->second.exec);
+    if (it->second.graph) cudaGraphDestroy(it->second.graph);
+    it->second.exec = nullptr;
+    it->second.graph = nullptr;
+    it->second.valid = false;
+}
+}  // namespace omdg
+
+extern "C" {
+
+int omdg_create(omdg_ctx** out, int device) {
+    if (!out) return OMDG_EINVAL;
+    *out = nullptr;
+    omdg_ctx* c = new omdg_ctx();
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_flags, sizeof(int) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_state, step_state_bytes());
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_mass, sizeof(double) * MAX_TYPES);
+    c->ledger_cap = 1 << 16;
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_ledger, sizeof(double) * 4 * c->ledger_cap);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_ledger, sizeof(double) * 4 * c->ledger_cap);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(unsigned) * 4, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_flags, 0, sizeof(int) * 4, c->stream);
+    if (e != cudaSuccess) {
+        delete c;
+        return OMDG_ECUDA;
+    }
+    step_state_init(c);
+    *out = c;
+    return OMDG_OK;
+}
+
+int omdg_destroy(omdg_ctx* c) {
+    if (!c) return OMDG_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    invalidate_graph(c);
+    auto it = g_graphs.find(c);
+    if (it != g_graphs.end()) {
+        if (it->second.side) cudaStreamDestroy(it->second.side);
+        g_graphs.erase(it);
+    }
+    free_atoms(c);
+    cudaFree(c->nbr);
+    cudaFree(c->rev);
+    cudaFree(c->slot_buf);
+    cudaFree(c->cell_count);
+    cudaFree(c->cell_start);
+    cudaFree(c->cell_fill);
+    cudaFree(c->d_status);
+    cudaFree(c->d_flags);
+    cudaFree(c->d_state);
+    cudaFree(c->d_mass);
+    cudaFree(c->d_ledger);
+    cudaFreeHost(c->h_ledger);
+    for (auto& p : c->pots)
+        for (int k = 0; k < 3; k++) {
+            cudaFree(p.d_coef[k]);
+            cudaFree(p.d_coef64[k]);
+        }
+    for (auto e : c->event_pool) cudaEventDestroy(e);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return OMDG_OK;
+}
+
+const char* omdg_last_error(omdg_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+
+int omdg_get_stream(omdg_ctx* c, void** stream) {
+    if (!c || !stream) return OMDG_EINVAL;
+    *stream = (void*)c->stream;
+    return OMDG_OK;
+}
+
+int omdg_set_box(omdg_ctx* c, const double lo[3], const double hi[3], const int periodic[3]) {
+    if (!c || !lo || !hi || !periodic) return OMDG_EINVAL;
+    for (int d = 0; d < 3; d++) {
+        if (!(hi[d] > lo[d])) return set_error(c, OMDG_EINVAL, "box hi must exceed lo");
+        c->box.lo[d] = lo[d];
+        c->box.hi[d] = hi[d];
+        c->box.L[d] = std::fabs(hi[d] - lo[d]);  // system.cpp:852-854
+        c->box.periodic[d] = periodic[d] ? 1 : 0;
+    }
+    c->have_box = true;
+    compute_frame(c);
+    c->list_valid = false;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_set_atoms(omdg_ctx* c, int n, const double* x, const double* v, const int* type, int ntypes,
+                   const double* mass_by_type, const double* z_by_type) {
+    if (!c || n <= 0 || !x || !type || ntypes <= 0 || ntypes > MAX_TYPES || !mass_by_type) return OMDG_EINVAL;
+    if (n > MAX_ATOMS) return set_error(c, OMDG_EINVAL, "too many atoms");
+    if (!c->have_box) return set_error(c, OMDG_ESTATE, "set the box first");
+    cudaSetDevice(c->device);
+    for (int i = 0; i < n; i++)
+        if (type[i] < 0 || type[i] >= ntypes) return set_error(c, OMDG_EINVAL, "atom type out of range");
+    int rc = alloc_atoms(c, n);
+    if (rc) return rc;
+    c->n = n;
+    c->ntypes = ntypes;
+    for (int t = 0; t < MAX_TYPES; t++) {
+        c->mass[t] = t < ntypes ? mass_by_type[t] : 0.0;
+        c->zat[t] = (t < ntypes && z_by_type) ? z_by_type[t] : 0.0;
+    }
+    std::vector<double> hx(n), hy(n), hz(n), hvx(n, 0.0), hvy(n, 0.0), hvz(n, 0.0);
+    std::vector<int> hid(n);
+    for (int i = 0; i < n; i++) {
+        hx[i] = x[3 * i];
+        hy[i] = x[3 * i + 1];
+        hz[i] = x[3 * i + 2];
+        if (v) {
+            hvx[i] = v[3 * i];
+            hvy[i] = v[3 * i + 1];
+            hvz[i] = v[3 * i + 2];
+        }
+        hid[i] = i;
+    }
+    cudaStream_t s = c->stream;
+    cudaMemcpyAsync(c->x, hx.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->y, hy.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->z, hz.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->vx, hvx.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->vy, hvy.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->vz, hvz.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->type, type, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->id, hid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->inv, hid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->d_mass, c->mass, sizeof(double) * MAX_TYPES, cudaMemcpyHostToDevice, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return check_cuda(c, e, "atom upload");
+    if (c->use_f64 && !dalloc(c->f64, (size_t)4 * n)) return set_error(c, OMDG_ENOMEM, "FP64 force arrays");
+    if (c->f64) cudaMemsetAsync(c->f64, 0, sizeof(double) * 4 * n, s);
+    c->list_valid = false;
+    c->first_run_done = false;
+    c->maxnb = 0;
+    cudaFree(c->nbr);
+    cudaFree(c->rev);
+    cudaFree(c->slot_buf);
+    c->nbr = nullptr;
+    c->rev = nullptr;
+    c->slot_buf = nullptr;
+    invalidate_graph(c);
+    return integrate_pack(c);
+}
+
+int omdg_num_atoms(omdg_ctx* c, int* n) {
+    if (!c || !n) return OMDG_EINVAL;
+    *n = c->n;
+    return OMDG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- read-back
+namespace omdg {
+static int fetch_ids(Context* c, std::vector<int>& id) {
+    id.resize(c->n);
+    cudaError_t e = cudaMemcpyAsync(id.data(), c->id, sizeof(int) * c->n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return check_cuda(c, e, "id read");
+}
+
+template <typename T>
+static int fetch(Context* c, const T* d, std::vector<T>& h, size_t count) {
+    h.resize(count);
+    cudaError_t e = cudaMemcpyAsync(h.data(), d, sizeof(T) * count, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return check_cuda(c, e, "read-back");
+}
+}  // namespace omdg
+
+extern "C" {
+
+int omdg_get_state(omdg_ctx* c, double* x, double* v, double* f, double* pot, double* vir) {
+    if (!c) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    std::vector<int> id;
+    int rc = fetch_ids(c, id);
+    if (rc) return rc;
+    int n = c->n;
+    if (x) {
+        std::vector<double> a, b, d;
+        if ((rc = fetch(c, c->x, a, n)) || (rc = fetch(c, c->y, b, n)) || (rc = fetch(c, c->z, d, n))) return rc;
+        for (int k = 0; k < n; k++) {
+            x[3 * id[k]] = a[k];
+            x[3 * id[k] + 1] = b[k];
+            x[3 * id[k] + 2] = d[k];
+        }
+    }
+    if (v) {
+        std::vector<double> a, b, d;
+        if ((rc = fetch(c, c->vx, a, n)) || (rc = fetch(c, c->vy, b, n)) || (rc = fetch(c, c->vz, d, n))) return rc;
+        for (int k = 0; k < n; k++) {
+            v[3 * id[k]] = a[k];
+            v[3 * id[k] + 1] = b[k];
+            v[3 * id[k] + 2] = d[k];
+        }
+    }
+    if (f) {
+        if (c->use_f64) {
+            std::vector<double> a;
+            if ((rc = fetch(c, c->f64, a, (size_t)3 * n))) return rc;
+            for (int k = 0; k < n; k++)
+                for (int q = 0; q < 3; q++) f[3 * id[k] + q] = a[3 * k + q];
+        } else {
+            std::vector<float> a, b, d;
+            if ((rc = fetch(c, c->fx, a, n)) || (rc = fetch(c, c->fy, b, n)) || (rc = fetch(c, c->fz, d, n)))
+                return rc;
+            for (int k = 0; k < n; k++) {
+                f[3 * id[k]] = a[k];
+                f[3 * id[k] + 1] = b[k];
+                f[3 * id[k] + 2] = d[k];
+            }
+        }
+    }
+    if (pot) {
+        if (c->use_f64) {
+            std::vector<double> a;
+            if ((rc = fetch(c, c->f64, a, (size_t)4 * n))) return rc;
+            for (int k = 0; k < n; k++) pot[id[k]] = a[3 * (size_t)n + k];
+        } else {
+            std::vector<float> a;
+            if ((rc = fetch(c, c->pe, a, n))) return rc;
+            for (int k = 0; k < n; k++) pot[id[k]] = a[k];
+        }
+    }
+    if (vir) {
+        std::vector<float> a;
+        if ((rc = fetch(c, c->vir, a, n))) return rc;
+        for (int k = 0; k < n; k++) vir[id[k]] = a[k];
+    }
+    return OMDG_OK;
+}
+
+static int upload_caller_order(omdg_ctx* c, const double* src, double* dx, double* dy, double* dz) {
+    std::vector<int> id;
+    int rc = fetch_ids(c, id);
+    if (rc) return rc;
+    int n = c->n;
+    std::vector<double> a(n), b(n), d(n);
+    for (int k = 0; k < n; k++) {
+        a[k] = src[3 * id[k]];
+        b[k] = src[3 * id[k] + 1];
+        d[k] = src[3 * id[k] + 2];
+    }
+    cudaMemcpyAsync(dx, a.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dy, b.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dz, d.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "upload");
+}
+
+int omdg_set_positions(omdg_ctx* c, const double* x) {
+    if (!c || !x) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    int rc = upload_caller_order(c, x, c->x, c->y, c->z);
+    if (rc) return rc;
+    c->list_valid = false;
+    return integrate_pack(c);
+}
+
+int omdg_set_velocities(omdg_ctx* c, const double* v) {
+    if (!c || !v) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    return upload_caller_order(c, v, c->vx, c->vy, c->vz);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- potentials
+namespace omdg {
+
+static int upload_table(Context* c, Potential& p, int k, HostTable& t, bool fp64) {
+    std::vector<float4> h(t.n);
+    for (int i = 0; i < t.n; i++) h[i] = make_float4((float)t.a[i], (float)t.b[i], (float)t.c[i], (float)t.d[i]);
+    if (cudaMalloc(&p.d_coef[k], sizeof(float4) * t.n) != cudaSuccess)
+        return set_error(c, OMDG_ENOMEM, "table upload");
+    cudaMemcpy(p.d_coef[k], h.data(), sizeof(float4) * t.n, cudaMemcpyHostToDevice);
+    DevTable& d = p.dt[k];
+    d.coef = p.d_coef[k];
+    d.coef64 = nullptr;
+    if (fp64) {
+        std::vector<double4_32a> h64(t.n);
+        for (int i = 0; i < t.n; i++) h64[i] = make_double4_32a(t.a[i], t.b[i], t.c[i], t.d[i]);
+        if (cudaMalloc(&p.d_coef64[k], sizeof(double4_32a) * t.n) != cudaSuccess)
+            return set_error(c, OMDG_ENOMEM, "table upload");
+        cudaMemcpy(p.d_coef64[k], h64.data(), sizeof(double4_32a) * t.n, cudaMemcpyHostToDevice);
+        d.coef64 = p.d_coef64[k];
+    }
+    d.off = (float)t.off;
+    d.dr = (float)t.dr;
+    d.inv_dr = (float)(1.0 / t.dr);
+    d.off64 = t.off;
+    d.dr64 = t.dr;
+    d.n = t.n;
+    d.rmult = t.rmult ? 1 : 0;
+    d.allow_lo = t.allow_lo;
+    d.allow_hi = t.allow_hi;
+    d.out_lo = (float)t.out_lo;
+    d.out_hi = (float)t.out_hi;
+    d.rc = (float)t.max_range();
+    d.rc64 = t.max_range();
+    return OMDG_OK;
+}
+
+static void update_rc(Context* c) {
+    // integrator.cpp:108-113: the largest CutRadius over all force kernels
+    double m = -1.0;
+    for (auto& p : c->pots) m = std::max(m, p.rc);
+    c->rc_max = m;
+    c->list_valid = false;
+    c->maxnb = 0;
+    invalidate_graph(c);
+}
+
+static int check_types(Context* c, int ta, int tb) {
+    if (ta < 0 || tb < 0 || ta >= MAX_TYPES || tb >= MAX_TYPES) return set_error(c, OMDG_EINVAL, "bad type id");
+    for (auto& p : c->pots)
+        if ((p.ta == ta && p.tb == tb) || (p.ta == tb && p.tb == ta))
+            return set_error(c, OMDG_EINVAL, "interaction for these types is already assigned (integrator.cpp:90-93)");
+    return OMDG_OK;
+}
+
+// whitespace 'key value...' parameter file (param.cpp:77-98)
+static bool read_params(const std::string& file, std::map<std::string, std::vector<std::string>>& kv) {
+    std::ifstream fl(file.c_str());
+    if (!fl.good()) return false;
+    std::string line;
+    while (std::getline(fl, line)) {
+        size_t h = line.find('#');
+        if (h != std::string::npos) line = line.substr(0, h);
+        std::istringstream ss(line);
+        std::string k, v;
+        if (!(ss >> k)) continue;
+        std::vector<std::string> vals;
+        while (ss >> v) vals.push_back(v);
+        kv[k] = vals;
+    }
+    return true;
+}
+
+static bool pnum(std::map<std::string, std::vector<std::string>>& kv, const char* k, double& out, int idx = 0) {
+    auto it = kv.find(k);
+    if (it == kv.end() || (int)it->second.size() <= idx) return false;
+    out = std::strtod(it->second[idx].c_str(), nullptr);
+    return true;
+}
+
+}  // namespace omdg
+
+extern "C" {
+
+int omdg_add_eam(omdg_ctx* c, int ta, int tb, const char* file) {
+    if (!c || !file) return OMDG_EINVAL;
+    if (ta != tb) return set_error(c, OMDG_EINVAL, "EAM between different types is not supported");
+    int rc = check_types(c, ta, tb);
+    if (rc) return rc;
+    if (c->use_f64) return set_error(c, OMDG_EINVAL, "EAM cannot be combined with FP64 kernels");
+    Potential p;
+    p.kind = POT_EAM;
+    p.ta = ta;
+    p.tb = tb;
+    std::string err;
+    if ((rc = table_load(file, "PAIR", p.t0, err)) || (rc = table_load(file, "EDENS", p.t1, err)) ||
+        (rc = table_load(file, "EMBED", p.t2, err)))
+        return set_error(c, rc, err);
+    if ((rc = upload_table(c, p, 0, p.t0, false)) || (rc = upload_table(c, p, 1, p.t1, false)) ||
+        (rc = upload_table(c, p, 2, p.t2, false)))
+        return rc;
+    p.rc = p.t0.max_range();  // team.cpp:212
+    c->pots.push_back(p);
+    update_rc(c);
+    return OMDG_OK;
+}
+
+int omdg_add_pair_table(omdg_ctx* c, int ta, int tb, const char* file, int fp64) {
+    if (!c || !file) return OMDG_EINVAL;
+    int rc = check_types(c, ta, tb);
+    if (rc) return rc;
+    if (fp64) {
+        for (auto& q : c->pots)
+            if (!q.fp64) return set_error(c, OMDG_EINVAL, "FP64 kernels cannot be mixed with FP32 kernels");
+    } else if (c->use_f64) {
+        return set_error(c, OMDG_EINVAL, "FP32 kernels cannot be mixed with FP64 kernels");
+    }
+    Potential p;
+    p.kind = POT_PAIR;
+    p.ta = ta;
+    p.tb = tb;
+    p.fp64 = fp64 != 0;
+    std::string err;
+    if ((rc = table_load(file, "", p.t0, err))) return set_error(c, rc, err);
+    if ((rc = upload_table(c, p, 0, p.t0, p.fp64))) return rc;
+    p.rc = p.t0.max_range();  // tpair.h:59
+    c->pots.push_back(p);
+    if (p.fp64 && !c->use_f64) {
+        c->use_f64 = true;
+        if (c->n > 0) {
+            if (!dalloc(c->f64, (size_t)4 * c->n)) return set_error(c, OMDG_ENOMEM, "FP64 force arrays");
+            cudaMemset(c->f64, 0, sizeof(double) * 4 * c->n);
+        }
+    }
+    update_rc(c);
+    return OMDG_OK;
+}
+
+int omdg_add_sw(omdg_ctx* c, int ta, int tb, const char* file) {
+    if (!c || !file) return OMDG_EINVAL;
+    int rc = check_types(c, ta, tb);
+    if (rc) return rc;
+    if (c->use_f64) return set_error(c, OMDG_EINVAL, "SW cannot be combined with FP64 kernels");
+    std::map<std::string, std::vector<std::string>> kv;
+    if (!read_params(file, kv)) return set_error(c, OMDG_EFILE, std::string("can not read ") + file);
+    Potential p;
+    p.kind = POT_SW;
+    p.ta = ta;
+    p.tb = tb;
+    SWParams& s = p.sw;
+    // sw.cpp:35-62
+    bool ok = pnum(kv, "sw.epsilon", s.eps) && pnum(kv, "sw.A", s.A) && pnum(kv, "sw.B", s.B) &&
+              pnum(kv, "sw.p", s.p) && pnum(kv, "sw.q", s.q) && pnum(kv, "sw.sigma", s.sigma) &&
+              pnum(kv, "sw.a", s.a) && pnum(kv, "sw.lambda", s.lambda) && pnum(kv, "sw.gamma", s.gamma) &&
+              pnum(kv, "sw.invers_cos0", s.icos0);
+    if (!ok) return set_error(c, OMDG_EFILE, std::string("incomplete SW parameters in ") + file);
+    s.usezbl = 0;
+    auto z = kv.find("zbl");
+    if (z != kv.end() && !z->second.empty()) {
+        std::string v = z->second[0];
+        s.usezbl = (v == "yes" || v == "true" || v == "1") ? 1 : 0;
+    }
+    if (s.usezbl) {
+        ok = pnum(kv, "spline.range", s.sx0, 0) && pnum(kv, "spline.range", s.sx1, 1) &&
+             pnum(kv, "spline.coeff", s.sa0, 0) && pnum(kv, "spline.coeff", s.sa1, 1) &&
+             pnum(kv, "spline.coeff", s.sa2, 2) && pnum(kv, "spline.coeff", s.sa3, 3);
+        if (!ok) return set_error(c, OMDG_EFILE, "incomplete SW ZBL spline parameters");
+    }
+    // sw.cpp:65-91
+    s.rc = s.a * s.sigma;
+    s.c1 = s.A * s.eps * s.p * s.B * std::pow(s.sigma, s.p);
+    s.c2 = s.A * s.eps * s.q * std::pow(s.sigma, s.q);
+    s.c3 = s.A * s.eps * s.B * std::pow(s.sigma, s.p + 1.0);
+    s.c4 = s.A * s.eps * std::pow(s.sigma, s.q + 1.0);
+    s.c5 = s.A * s.eps * s.B * std::pow(s.sigma, s.p);
+    s.c6 = s.A * s.eps * std::pow(s.sigma, s.q);
+    s.c7 = s.sigma * s.gamma;
+    s.c8 = s.lambda * s.eps;
+    s.c9 = 2.0 * s.lambda * s.eps;
+    s.c10 = 1.0 / s.icos0;
+    double z1 = c->zat[ta], z2 = c->zat[tb];
+    if (z1 <= 0 || z2 <= 0) {
+        z1 = z2 = 14.0;
+    }
+    double znor = 0.468521928 / (std::pow(z1, 0.23) + std::pow(z2, 0.23));
+    s.zc = 14.39964415 * z1 * z2;
+    s.ze0 = 3.2000 / znor;
+    s.ze1 = 0.9423 / znor;
+    s.ze2 = 0.4029 / znor;
+    s.ze3 = 0.2016 / znor;
+    p.rc = s.rc;  // sw.cpp:71
+    c->pots.push_back(p);
+    c->need_rev = true;
+    update_rc(c);
+    return OMDG_OK;
+}
+
+int omdg_add_tersoff(omdg_ctx* c, int ta, int tb, const char* file) {
+    if (!c || !file) return OMDG_EINVAL;
+    int rc = check_types(c, ta, tb);
+    if (rc) return rc;
+    if (c->use_f64) return set_error(c, OMDG_EINVAL, "Tersoff cannot be combined with FP64 kernels");
+    std::map<std::string, std::vector<std::string>> kv;
+    if (!read_params(file, kv)) return set_error(c, OMDG_EFILE, std::string("can not read ") + file);
+    Potential p;
+    p.kind = POT_TERSOFF;
+    p.ta = ta;
+    p.tb = tb;
+    TersoffParams& t = p.ters;
+    // tersoff.h:150-170 key names
+    bool ok = pnum(kv, "tersoff.A", t.A) && pnum(kv, "tersoff.B", t.B) && pnum(kv, "tersoff.lambda_1", t.lambda1) &&
+              pnum(kv, "tersoff.lambda_2", t.lambda2) && pnum(kv, "tersoff.lambda_3", t.lambda3) &&
+              pnum(kv, "tersoff.beta", t.beta) && pnum(kv, "tersoff.n", t.n) && pnum(kv, "tersoff.c", t.c) &&
+              pnum(kv, "tersoff.d", t.d) && pnum(kv, "tersoff.h", t.h) && pnum(kv, "tersoff.R", t.R) &&
+              pnum(kv, "tersoff.D", t.D);
+    if (!ok) return set_error(c, OMDG_EFILE, std::string("incomplete Tersoff parameters in ") + file);
+    auto z = kv.find("tersoff.zbl");
+    if (z != kv.end() && !z->second.empty() && z->second[0] == "true")
+        return set_error(c, OMDG_EINVAL, "tersoff.zbl true is not supported (the reference disables it: tersoff.h:402)");
+    p.rc = t.R + t.D;  // tersoff.h:183
+    c->pots.push_back(p);
+    c->need_rev = true;
+    update_rc(c);
+    return OMDG_OK;
+}
+
+int omdg_add_zbl(omdg_ctx* c, int ta, int tb, double rcut, double width) {
+    if (!c || !(rcut > 0) || width < 0 || width >= rcut) return OMDG_EINVAL;
+    int rc = check_types(c, ta, tb);
+    if (rc) return rc;
+    if (c->use_f64) return set_error(c, OMDG_EINVAL, "ZBL cannot be combined with FP64 kernels");
+    Potential p;
+    p.kind = POT_ZBL;
+    p.ta = ta;
+    p.tb = tb;
+    ZBLParams& z = p.zbl;
+    z.z1 = c->zat[ta];
+    z.z2 = c->zat[tb];
+    if (!(z.z1 > 0 && z.z2 > 0)) return set_error(c, OMDG_EINVAL, "ZBL needs atomic numbers (omdg_set_atoms z_by_type)");
+    z.rc = rcut;
+    z.width = width;
+    // sw.cpp:84-91
+    double znor = 0.468521928 / (std::pow(z.z1, 0.23) + std::pow(z.z2, 0.23));
+    z.zc = 14.39964415 * z.z1 * z.z2;
+    z.ze0 = 3.2000 / znor;
+    z.ze1 = 0.9423 / znor;
+    z.ze2 = 0.4029 / znor;
+    z.ze3 = 0.2016 / znor;
+    p.rc = rcut;
+    c->pots.push_back(p);
+    update_rc(c);
+    return OMDG_OK;
+}
+
+int omdg_max_cut_radius(omdg_ctx* c, double* rc) {
+    if (!c || !rc) return OMDG_EINVAL;
+    *rc = c->rc_max;
+    return OMDG_OK;
+}
+
+int omdg_set_neighbor(omdg_ctx* c, double skin, int rebuild_every) {
+    if (!c || skin < 0 || rebuild_every < 0) return OMDG_EINVAL;
+    c->skin = skin;
+    c->rebuild_every = rebuild_every;
+    c->list_valid = false;
+    c->maxnb = 0;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+}  // extern "C"
+
+namespace omdg {
+
+// Builds the list, sizing the per-atom capacity from the first build.
+static int build_list(Context* c) {
+    if (c->pots.empty()) return set_error(c, OMDG_ESTATE, "no force kernel (integrator.cpp:79)");
+    nlist_prepare_geometry(c);
+    if (c->maxnb == 0) {
+        // first build: estimate from the mean density, then fit to the measured maximum
+        double vol = 1.0;
+        for (int d = 0; d < 3; d++) vol *= c->box.L[d];
+        double rv = c->rc_max + c->skin;
+        double est = c->n / vol * 4.18879 * rv * rv * rv;
+        int m = (int)(2.0 * est) + 32;
+        int rc = nlist_reserve(c, m);
+        if (rc) return rc;
+    }
+    for (int attempt = 0; attempt < 4; attempt++) {
+        int zero = 0;
+        cudaMemcpyAsync(c->d_flags + 1, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+        int rc = nlist_build(c);
+        if (rc) return rc;
+        int need = 0;
+        cudaMemcpyAsync(&need, c->d_flags + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return check_cuda(c, e, "build");
+        unsigned st = 0;
+        cudaMemcpy(&st, c->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+        if (st & ERR_NBR_OVERFLOW) {
+            unsigned clr = st & ~ERR_NBR_OVERFLOW;
+            cudaMemcpy(c->d_status, &clr, sizeof(unsigned), cudaMemcpyHostToDevice);
+            int m = (int)(1.25 * std::max(need, c->maxnb)) + 16;
+            c->maxnb = 0;
+            rc = nlist_reserve(c, m);
+            if (rc) return rc;
+            invalidate_graph(c);
+            continue;
+        }
+        return check_status(c);
+    }
+    return set_error(c, OMDG_ESTATE, "neighbour list did not fit");
+}
+
+int forces_compute(Context* c) {
+    if (c->pots.empty()) return set_error(c, OMDG_ESTATE, "no force kernel");
+    bool first = true;
+    for (auto& p : c->pots) {
+        int rc = OMDG_OK;
+        switch (p.kind) {
+            case POT_EAM: rc = eam_launch(c, p, first); break;
+            case POT_PAIR: rc = pair_launch(c, p, first); break;
+            case POT_SW: rc = sw_launch(c, p, first); break;
+            case POT_TERSOFF: rc = tersoff_launch(c, p, first); break;
+            case POT_ZBL: rc = zbl_launch(c, p, first); break;
+        }
+        if (rc) return rc;
+        first = false;
+    }
+    return OMDG_OK;
+}
+
+// Eager rebuild of the list when the device asks for it (reads the flag).
+static int eager_maybe_rebuild(Context* c) {
+    int rebuild = 0;
+    int rc = step_state_read(c, nullptr, nullptr, &rebuild);
+    if (rc) return rc;
+    if (rebuild) {
+        if ((rc = step_clear_rebuild(c))) return rc;
+        if ((rc = nlist_build(c))) return rc;
+    }
+    return OMDG_OK;
+}
+
+static int capture_step(Context* c, GraphState& gs) {
+    cudaStream_t s = c->stream;
+    if (!gs.side) cudaStreamCreateWithFlags(&gs.side, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return check_cuda(c, e, "capture begin");
+    int rc = integrate_kick_drift(c, 0);
+    cudaGraph_t g = nullptr;
+    cudaStreamCaptureStatus cst;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaGraphConditionalHandle h = 0;
+    if (!rc) {
+        e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &g, nullptr, nullptr, nullptr);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+        if (e != cudaSuccess) rc = check_cuda(c, e, "conditional handle");
+    }
+    if (!rc) rc = launch_set_rebuild_cond(c, h);
+    cudaGraphNode_t cond_node = nullptr;
+    if (!rc) {
+        e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &g, &deps, nullptr, &ndeps);
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&cond_node, g, deps, nullptr, ndeps, &cp);
+        if (e == cudaSuccess)
+            e = cudaStreamUpdateCaptureDependencies(s, &cond_node, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e != cudaSuccess) rc = check_cuda(c, e, "conditional node");
+        if (!rc) {
+            // populate the body: the rebuild pipeline, captured on a side stream
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            e = cudaStreamBeginCaptureToGraph(gs.side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) rc = check_cuda(c, e, "body capture");
+            if (!rc) {
+                c->stream = gs.side;
+                rc = nlist_build(c);
+                c->stream = s;
+                cudaGraph_t body_out = nullptr;
+                e = cudaStreamEndCapture(gs.side, &body_out);
+                if (!rc && e != cudaSuccess) rc = check_cuda(c, e, "body capture end");
+            }
+        }
+    }
+    if (!rc) rc = forces_compute(c);
+    if (!rc) rc = integrate_kick(c, 0);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(s, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return check_cuda(c, e, "capture end");
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return check_cuda(c, e, "graph instantiate");
+    }
+    gs.graph = graph;
+    gs.exec = exec;
+    gs.valid = true;
+    // the rebuild count is advanced on the host only for eager builds
+    return OMDG_OK;
+}
+
+}  // namespace omdg
+
+extern "C" {
+
+int omdg_build_neighbors(omdg_ctx* c) {
+    if (!c) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    cudaSetDevice(c->device);
+    return build_list(c);
+}
+
+int omdg_get_neighbors(omdg_ctx* c, int* offsets, int* nbr_j, int* nbr_code, long cap, long* count) {
+    if (!c || !offsets || !count) return OMDG_EINVAL;
+    if (!c->list_valid) {
+        int rc = omdg_build_neighbors(c);
+        if (rc) return rc;
+    }
+    int n = c->n;
+    std::vector<int> id, nn;
+    std::vector<unsigned> nb;
+    int rc = fetch_ids(c, id);
+    if (rc) return rc;
+    if ((rc = fetch(c, c->nnb, nn, n))) return rc;
+    if ((rc = fetch(c, reinterpret_cast<const unsigned*>(c->nbr), nb, (size_t)c->maxnb * n))) return rc;
+    // rows in caller order, each sorted by (j, code)
+    std::vector<int> sorted_of(n);
+    for (int k = 0; k < n; k++) sorted_of[id[k]] = k;
+    long total = 0;
+    for (int k = 0; k < n; k++) total += nn[k];
+    *count = total;
+    if (total > cap || !nbr_j || !nbr_code) return set_error(c, OMDG_EINVAL, "neighbour output capacity too small");
+    long pos = 0;
+    std::vector<std::pair<int, int>> row;
+    for (int i = 0; i < n; i++) {
+        int k = sorted_of[i];
+        row.clear();
+        for (int s = 0; s < nn[k]; s++) {
+            unsigned e = nb[(size_t)s * n + k];
+            row.push_back(std::make_pair(id[nbr_index(e)], omdg::nbr_code(e)));
+        }
+        std::sort(row.begin(), row.end());
+        offsets[i] = (int)pos;
+        for (auto& pr : row) {
+            nbr_j[pos] = pr.first;
+            nbr_code[pos] = pr.second;
+            pos++;
+        }
+    }
+    offsets[n] = (int)pos;
+    return OMDG_OK;
+}
+
+int omdg_compute_forces(omdg_ctx* c) {
+    if (!c) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    cudaSetDevice(c->device);
+    int rc;
+    if (!c->list_valid && (rc = build_list(c))) return rc;
+    if ((rc = threebody_prepare(c))) return rc;
+    if ((rc = forces_compute(c))) return rc;
+    if ((rc = measure_energies(c, 0))) return rc;
+    prof_collect(c);
+    if ((rc = check_status(c))) return rc;
+    double row[4];
+    cudaMemcpy(row, c->d_ledger, sizeof(row), cudaMemcpyDeviceToHost);
+    c->last_kin = row[0];
+    c->last_pot = row[1];
+    c->last_vir = row[2];
+    return OMDG_OK;
+}
+
+int omdg_set_timestep(omdg_ctx* c, double dt) {
+    if (!c || !(dt > 0)) return OMDG_EINVAL;
+    c->dt = dt;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_set_first_step_mode(omdg_ctx* c, int reference_first_step) {
+    if (!c) return OMDG_EINVAL;
+    c->reference_first_step = reference_first_step != 0;
+    return OMDG_OK;
+}
+
+int omdg_set_thermostat(omdg_ctx* c, double temperature, double tau) {
+    if (!c) return OMDG_EINVAL;
+    c->thermo_T = temperature;
+    c->thermo_tau = tau;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_step(omdg_ctx* c, int nsteps) {
+    if (!c || nsteps < 0) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    cudaSetDevice(c->device);
+    int rc;
+    long launches0 = c->launches;
+    if (!c->first_run_done) {
+        // FirstRun (system.cpp:860-873): one force evaluation, energies, base potential
+        if ((rc = build_list(c))) return rc;
+        if ((rc = threebody_prepare(c))) return rc;
+        if ((rc = step_state_init(c))) return rc;
+        if ((rc = forces_compute(c))) return rc;
+        if ((rc = measure_energies(c, 0))) return rc;
+        if ((rc = check_status(c))) return rc;
+        double row[4];
+        cudaMemcpy(row, c->d_ledger, sizeof(row), cudaMemcpyDeviceToHost);
+        c->base_potential = row[1];
+        c->last_kin = row[0];
+        c->last_pot = row[1];
+        c->last_vir = row[2];
+        if (c->reference_first_step && (rc = zero_forces(c))) return rc;
+        c->first_run_done = true;
+    }
+    if ((rc = step_state_reset(c, 1, c->rebuild_every))) return rc;
+    if (!c->list_valid) {
+        if ((rc = build_list(c))) return rc;
+        if ((rc = threebody_prepare(c))) return rc;
+    }
+    if (nsteps > c->ledger_cap) return set_error(c, OMDG_EINVAL, "too many steps for one call (ledger capacity)");
+    if (c->profiling) {
+        for (int k = 0; k < nsteps; k++) {
+            if ((rc = integrate_kick_drift(c, k))) return rc;
+            if ((rc = eager_maybe_rebuild(c))) return rc;
+            if ((rc = forces_compute(c))) return rc;
+            if ((rc = integrate_kick(c, k))) return rc;
+        }
+        prof_collect(c);
+    } else {
+        GraphState& gs = g_graphs[c];
+        if (!gs.valid) {
+            if ((rc = capture_step(c, gs))) return rc;
+        }
+        for (int k = 0; k < nsteps; k++) {
+            cudaError_t e = cudaGraphLaunch(gs.exec, c->stream);
+            if (e != cudaSuccess) return check_cuda(c, e, "graph launch");
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "step");
+    if ((rc = check_status(c))) {
+        if (rc == OMDG_ESTATE) {
+            // a neighbour row overflowed during the run: grow for the next call
+            int m = (int)(1.25 * c->maxnb) + 16;
+            c->maxnb = 0;
+            nlist_reserve(c, m);
+            c->list_valid = false;
+            invalidate_graph(c);
+        }
+        return rc;
+    }
+    long long step;
+    int rows;
+    if ((rc = step_state_read(c, &step, &rows, nullptr))) return rc;
+    c->step = step;
+    int nrow = std::min(rows, c->ledger_cap);
+    if (nrow > 0) {
+        cudaMemcpy(c->h_ledger, c->d_ledger, sizeof(double) * 4 * nrow, cudaMemcpyDeviceToHost);
+        c->last_kin = c->h_ledger[4 * (nrow - 1)];
+        c->last_pot = c->h_ledger[4 * (nrow - 1) + 1];
+        c->last_vir = c->h_ledger[4 * (nrow - 1) + 2];
+    }
+    c->last_rows = nrow;
+    c->launches = c->launches - launches0;
+    return OMDG_OK;
+}
+
+int omdg_ledger(omdg_ctx* c, double* kinetic, double* potential, double* base_potential, double* virial) {
+    if (!c) return OMDG_EINVAL;
+    if (kinetic) *kinetic = c->last_kin;
+    if (potential) *potential = c->last_pot;
+    if (base_potential) *base_potential = c->base_potential;
+    if (virial) *virial = c->last_vir;
+    return OMDG_OK;
+}
+
+int omdg_ledger_history(omdg_ctx* c, double* kinetic, double* potential, int cap, int* rows) {
+    if (!c || !rows) return OMDG_EINVAL;
+    int m = std::min(cap, c->last_rows);
+    for (int k = 0; k < m; k++) {
+        if (kinetic) kinetic[k] = c->h_ledger[4 * k];
+        if (potential) potential[k] = c->h_ledger[4 * k + 1];
+    }
+    *rows = m;
+    return OMDG_OK;
+}
+
+int omdg_stats(omdg_ctx* c, long* rebuilds, long* launches) {
+    if (!c) return OMDG_EINVAL;
+    if (rebuilds) *rebuilds = c->rebuilds;
+    if (launches) *launches = c->launches;
+    return OMDG_OK;
+}
+
+int omdg_set_profiling(omdg_ctx* c, int on) {
+    if (!c) return OMDG_EINVAL;
+    c->profiling = on != 0;
+    if (on) c->timers.clear();
+    return OMDG_OK;
+}
+
+int omdg_kernel_times(omdg_ctx* c, char* name_buf, int name_cap, double* ms, long* calls, int cap, int* nkern) {
+    if (!c || !nkern) return OMDG_EINVAL;
+    prof_collect(c);
+    std::string names;
+    int m = std::min(cap, (int)c->timers.size());
+    for (int k = 0; k < m; k++) {
+        if (k) names += ";";
+        names += c->timers[k].name;
+        if (ms) ms[k] = c->timers[k].ms;
+        if (calls) calls[k] = c->timers[k].calls;
+    }
+    if (name_buf && name_cap > 0) {
+        std::strncpy(name_buf, names.c_str(), name_cap - 1);
+        name_buf[name_cap - 1] = 0;
+    }
+    *nkern = m;
+    return OMDG_OK;
+}
+
+}  // extern "C"

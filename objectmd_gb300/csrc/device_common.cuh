@@ -1,0 +1,164 @@
+// Device helpers shared by the kernels: neighbour entry encoding, the
+// mixed-precision relative vector, FP32/FP64 spline reads with TableReader
+// semantics and compensated accumulation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "omdg_internal.h"
+
+namespace omdg {
+
+// Neighbour entry: bits 0..25 atom index, then (s+1) for x, y, z in two bits each.
+__host__ __device__ __forceinline__ unsigned nbr_encode(int j, int sx, int sy, int sz) {
+    return (unsigned)j | ((unsigned)(sx + 1) << 26) | ((unsigned)(sy + 1) << 28) | ((unsigned)(sz + 1) << 30);
+}
+__host__ __device__ __forceinline__ int nbr_index(unsigned e) { return (int)(e & (unsigned)INDEX_MASK); }
+__host__ __device__ __forceinline__ int nbr_sx(unsigned e) { return (int)((e >> 26) & 3u) - 1; }
+__host__ __device__ __forceinline__ int nbr_sy(unsigned e) { return (int)((e >> 28) & 3u) - 1; }
+__host__ __device__ __forceinline__ int nbr_sz(unsigned e) { return (int)((e >> 30) & 3u) - 1; }
+// The caller-facing image code (sx+1) + 3(sy+1) + 9(sz+1).
+__host__ __device__ __forceinline__ int nbr_code(unsigned e) {
+    return (nbr_sx(e) + 1) + 3 * (nbr_sy(e) + 1) + 9 * (nbr_sz(e) + 1);
+}
+
+// Periodic lengths split into float hi + lo parts.
+struct ShiftF {
+    float hx, hy, hz, lx, ly, lz;
+};
+
+__host__ inline ShiftF make_shift(const BoxGeom& b) {
+    ShiftF s;
+    s.hx = b.Lh[0];
+    s.hy = b.Lh[1];
+    s.hz = b.Lh[2];
+    s.lx = b.Ll[0];
+    s.ly = b.Ll[1];
+    s.lz = b.Ll[2];
+    return s;
+}
+
+__device__ __forceinline__ float sel_shift(int s, float v) { return s == 0 ? 0.0f : (s > 0 ? v : -v); }
+
+// d = x_i - (x_j + s L) from the packs.  hi_i - hi_j is exact (one binade),
+// and so is subtracting the hi part of the periodic length (Sterbenz, since
+// |hi_i - hi_j| >= L/2 whenever s != 0 and L >= 2 Rv); the lo parts carry the
+// remaining bits, so d is the FP32 rounding of the FP64 difference.
+__device__ __forceinline__ float3 pair_delta(const float4& hi_i, const float4& lo_i, const float4& hi_j,
+                                             const float4& lo_j, unsigned e, const ShiftF& L) {
+    int sx = nbr_sx(e), sy = nbr_sy(e), sz = nbr_sz(e);
+    float3 d;
+    d.x = __fadd_rn(__fsub_rn(__fsub_rn(hi_i.x, hi_j.x), sel_shift(sx, L.hx)),
+                    __fsub_rn(__fsub_rn(lo_i.x, lo_j.x), sel_shift(sx, L.lx)));
+    d.y = __fadd_rn(__fsub_rn(__fsub_rn(hi_i.y, hi_j.y), sel_shift(sy, L.hy)),
+                    __fsub_rn(__fsub_rn(lo_i.y, lo_j.y), sel_shift(sy, L.ly)));
+    d.z = __fadd_rn(__fsub_rn(__fsub_rn(hi_i.z, hi_j.z), sel_shift(sz, L.hz)),
+                    __fsub_rn(__fsub_rn(lo_i.z, lo_j.z), sel_shift(sz, L.lz)));
+    return d;
+}
+
+__device__ __forceinline__ int pack_type(const float4& hi) { return __float_as_int(hi.w); }
+
+// Compensated (Kahan) accumulator; the intrinsics keep the compiler from
+// contracting or reassociating the correction.
+struct Kahan {
+    float s, c;
+    __device__ __forceinline__ Kahan() : s(0.f), c(0.f) {}
+    __device__ __forceinline__ void add(float v) {
+        float y = __fsub_rn(v, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s; }
+};
+
+// ------------------------------------------------------------ spline reads
+// TableReader::read (treader.cpp:193-229): index by truncation, the two
+// edge rules, cubic value and derivative, RMULT division.  Returns false
+// (and sets the status bit) where the reference would die.
+__device__ __forceinline__ bool tab_read(const DevTable& t, const float4* __restrict__ coef, float r, float rinv,
+                                         float& v, float& dv, unsigned* status) {
+    float rval = r - t.off;
+    int x = (int)(rval * t.inv_dr);
+    float dx = fmaf(-(float)x, t.dr, rval);
+    if (x > t.n - 1) {
+        if (t.allow_hi) {
+            v = dv = t.out_hi;
+            return true;
+        }
+        atomicOr(status, ERR_TABLE_RANGE);
+        v = dv = 0.f;
+        return false;
+    }
+    if (x < -1) {
+        if (t.allow_lo) {
+            v = dv = t.out_lo;
+            return true;
+        }
+        atomicOr(status, ERR_TABLE_RANGE);
+        v = dv = 0.f;
+        return false;
+    }
+    if (x == t.n - 1) {
+        dx += t.dr;
+        x--;
+    }
+    if (x == -1) x = 0;
+    float4 cf = coef[x];  // (a, b, c, d)
+    v = fmaf(dx, fmaf(dx, fmaf(dx, cf.x, cf.y), cf.z), cf.w);
+    dv = fmaf(dx, fmaf(3.0f * dx, cf.x, 2.0f * cf.y), cf.z);
+    if (t.rmult) {
+        v = v * rinv;
+        dv = (dv - v) * rinv;
+    }
+    return true;
+}
+
+// Value only (TableReader::read(double), treader.cpp:231-264).
+__device__ __forceinline__ bool tab_value(const DevTable& t, const float4* __restrict__ coef, float r, float& v,
+                                          float& dv, unsigned* status) {
+    float rinv = t.rmult ? 1.0f / r : 0.f;
+    return tab_read(t, coef, r, rinv, v, dv, status);
+}
+
+// FP64 variant with the reference's exact operation order.
+__device__ __forceinline__ bool tab_read64(const DevTable& t, double r, double& v, double& dv, unsigned* status) {
+    double rval = __dsub_rn(r, t.off64);
+    int x = (int)__ddiv_rn(rval, t.dr64);
+    double dx = __dsub_rn(rval, __dmul_rn((double)x, t.dr64));
+    if (x > t.n - 1) {
+        if (t.allow_hi) {
+            v = dv = t.out_hi;
+            return true;
+        }
+        atomicOr(status, ERR_TABLE_RANGE);
+        v = dv = 0.0;
+        return false;
+    }
+    if (x < -1) {
+        if (t.allow_lo) {
+            v = dv = t.out_lo;
+            return true;
+        }
+        atomicOr(status, ERR_TABLE_RANGE);
+        v = dv = 0.0;
+        return false;
+    }
+    if (x == t.n - 1) {
+        dx = __dadd_rn(dx, t.dr64);
+        x--;
+    }
+    if (x == -1) x = 0;
+    double4_32a cf = t.coef64[x];
+    v = __dadd_rn(cf.w, __dmul_rn(dx, __dadd_rn(cf.z, __dmul_rn(dx, __dadd_rn(cf.y, __dmul_rn(dx, cf.x))))));
+    dv = __dadd_rn(cf.z, __dmul_rn(dx, __dadd_rn(__dmul_rn(2.0, cf.y), __dmul_rn(__dmul_rn(3.0, dx), cf.x))));
+    if (t.rmult) {
+        v = __ddiv_rn(v, r);
+        dv = __ddiv_rn(__dsub_rn(dv, v), r);
+    }
+    return true;
+}
+
+}  // namespace omdg

@@ -1,0 +1,336 @@
+// Velocity Verlet (MDIntegrator::Integrate, integrator.cpp:225-259) in FP64,
+// the energy ledger (MeasurePotential/MeasureKinetic, system.cpp:1060-1094)
+// and the Berendsen thermostat (TempController::PostIntegration,
+// TempController.h:78-91), all driven by a device-side step state so that a
+// captured step replays without host parameters.
+//
+//   kick_drift  v = lambda v (thermostat of the previous step), v += dt/2 f/m,
+//               x += dt v, refresh the FP32 position packs, flag a rebuild
+//               when an atom moved more than skin/2 since the last build
+//   kick        v += dt/2 f/m, block partials of sum m v^2, sum potential,
+//               sum virial (FP64, fixed order)
+//   finalize    one block: ledger row, thermostat factor, step counter
+#include "device_common.cuh"
+
+namespace omdg {
+
+struct StepState {
+    long long step;      // RunKernel Step (system.cpp:979)
+    int row;             // ledger row within the current omdg_step call
+    int rebuild;         // rebuild request for the next list build
+    double lambda;       // velocity factor to apply before the next kick
+    int rebuild_every;   // >0: rebuild when step % rebuild_every == 0
+    int pad;
+};
+
+struct IntParams {
+    int n;
+    double hdtm[MAX_TYPES];  // (dt/2) / m per type
+    double dt;
+    double org[3], P[3];
+    float half_skin2;       // (skin/2)^2
+    int use_f64;
+};
+
+__device__ __forceinline__ void split_pack(double X, float& hi, float& lo) {
+    hi = __double2float_rn(X);
+    lo = __double2float_rn(__dsub_rn(X, (double)hi));
+}
+
+__global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
+                                                    double* __restrict__ z, double* __restrict__ vx,
+                                                    double* __restrict__ vy, double* __restrict__ vz,
+                                                    const float* __restrict__ fx, const float* __restrict__ fy,
+                                                    const float* __restrict__ fz, const double* __restrict__ f64,
+                                                    const int* __restrict__ type, PosPack* __restrict__ pack,
+                                                    const float4* __restrict__ xref, StepState* st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ int moved;
+    if (threadIdx.x == 0) moved = 0;
+    __syncthreads();
+    if (i < p.n) {
+        double lam = st->lambda;
+        int t = type[i];
+        double h = p.hdtm[t];
+        double ax, ay, az;
+        if (p.use_f64) {
+            ax = f64[3 * (size_t)i];
+            ay = f64[3 * (size_t)i + 1];
+            az = f64[3 * (size_t)i + 2];
+        } else {
+            ax = fx[i];
+            ay = fy[i];
+            az = fz[i];
+        }
+        double ux = fma(ax, h, vx[i] * lam);
+        double uy = fma(ay, h, vy[i] * lam);
+        double uz = fma(az, h, vz[i] * lam);
+        double X = fma(p.dt, ux, x[i]);
+        double Y = fma(p.dt, uy, y[i]);
+        double Z = fma(p.dt, uz, z[i]);
+        vx[i] = ux;
+        vy[i] = uy;
+        vz[i] = uz;
+        x[i] = X;
+        y[i] = Y;
+        z[i] = Z;
+        PosPack pk;
+        split_pack(__dadd_rn(__dsub_rn(X, p.org[0]), p.P[0]), pk.hi.x, pk.lo.x);
+        split_pack(__dadd_rn(__dsub_rn(Y, p.org[1]), p.P[1]), pk.hi.y, pk.lo.y);
+        split_pack(__dadd_rn(__dsub_rn(Z, p.org[2]), p.P[2]), pk.hi.z, pk.lo.z);
+        pk.hi.w = __int_as_float(t);
+        pk.lo.w = 0.f;
+        pack[i] = pk;
+        float4 r0 = xref[i];
+        float dx = (pk.hi.x - r0.x) + pk.lo.x, dy = (pk.hi.y - r0.y) + pk.lo.y, dz = (pk.hi.z - r0.z) + pk.lo.z;
+        if (dx * dx + dy * dy + dz * dz > p.half_skin2) moved = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && moved) st->rebuild = 1;
+}
+
+constexpr int RED_BLOCK = 256;
+
+__global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, double* __restrict__ vx, double* __restrict__ vy,
+                                                    double* __restrict__ vz, const float* __restrict__ fx,
+                                                    const float* __restrict__ fy, const float* __restrict__ fz,
+                                                    const double* __restrict__ f64, const int* __restrict__ type,
+                                                    const double* __restrict__ mass, const float* __restrict__ pe,
+                                                    const float* __restrict__ vir, double* __restrict__ partial,
+                                                    int kick) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double k = 0, e = 0, w = 0;
+    if (i < p.n) {
+        int t = type[i];
+        double ux = vx[i], uy = vy[i], uz = vz[i];
+        if (kick) {
+            double h = p.hdtm[t];
+            if (p.use_f64) {
+                ux = fma((double)f64[3 * (size_t)i], h, ux);
+                uy = fma((double)f64[3 * (size_t)i + 1], h, uy);
+                uz = fma((double)f64[3 * (size_t)i + 2], h, uz);
+            } else {
+                ux = fma((double)fx[i], h, ux);
+                uy = fma((double)fy[i], h, uy);
+                uz = fma((double)fz[i], h, uz);
+            }
+            vx[i] = ux;
+            vy[i] = uy;
+            vz[i] = uz;
+        }
+        k = mass[t] * (ux * ux + uy * uy + uz * uz);
+        e = p.use_f64 ? f64[3 * (size_t)p.n + i] : (double)pe[i];
+        w = vir[i];
+    }
+    // fixed-order block reduction
+    __shared__ double sk[RED_BLOCK], se[RED_BLOCK], sw[RED_BLOCK];
+    sk[threadIdx.x] = k;
+    se[threadIdx.x] = e;
+    sw[threadIdx.x] = w;
+    __syncthreads();
+    for (int off = RED_BLOCK / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            sk[threadIdx.x] += sk[threadIdx.x + off];
+            se[threadIdx.x] += se[threadIdx.x + off];
+            sw[threadIdx.x] += sw[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[3 * blockIdx.x + 0] = sk[0];
+        partial[3 * blockIdx.x + 1] = se[0];
+        partial[3 * blockIdx.x + 2] = sw[0];
+    }
+}
+
+struct FinParams {
+    int nblocks;
+    int natoms;
+    int ledger_cap;
+    int count_step;       // 1: this is a RunKernel step (advance Step)
+    double dt, tau, tset; // thermostat (tau <= 0: off)
+    double temp_factor;   // 2/3/k_B (unit.h:66-104)
+};
+
+__global__ void k_finalize(FinParams p, const double* __restrict__ partial, double* __restrict__ ledger,
+                           StepState* st) {
+    __shared__ double sk[256], se[256], sw[256];
+    double k = 0, e = 0, w = 0;
+    // each thread sums a contiguous run of blocks, then a fixed tree
+    int per = (p.nblocks + blockDim.x - 1) / blockDim.x;
+    int b0 = threadIdx.x * per, b1 = min(p.nblocks, b0 + per);
+    for (int b = b0; b < b1; b++) {
+        k += partial[3 * b];
+        e += partial[3 * b + 1];
+        w += partial[3 * b + 2];
+    }
+    sk[threadIdx.x] = k;
+    se[threadIdx.x] = e;
+    sw[threadIdx.x] = w;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            sk[threadIdx.x] += sk[threadIdx.x + off];
+            se[threadIdx.x] += se[threadIdx.x + off];
+            sw[threadIdx.x] += sw[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double kinetic = 0.5 * sk[0];
+        int row = st->row;
+        if (row < p.ledger_cap) {
+            ledger[4 * row + 0] = kinetic;
+            ledger[4 * row + 1] = se[0];
+            ledger[4 * row + 2] = 0.5 * sw[0];
+        }
+        double lam = 1.0;
+        if (p.count_step && p.tau > 0.0 && st->step != 0) {
+            // TempController::PostIntegration: T from the system kinetic energy
+            double T = p.temp_factor * kinetic / (double)p.natoms;
+            if (T > 0.0) lam = sqrt(1. + p.dt / p.tau * (p.tset / T - 1.));
+        }
+        if (row < p.ledger_cap) ledger[4 * row + 3] = lam;
+        st->lambda = lam;
+        if (p.count_step) {
+            st->step += 1;
+            st->row = row + 1;
+            if (st->rebuild_every > 0 && (st->step % st->rebuild_every) == 0) st->rebuild = 1;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host
+
+static IntParams int_params(Context* c) {
+    IntParams p;
+    p.n = c->n;
+    for (int t = 0; t < MAX_TYPES; t++) p.hdtm[t] = c->mass[t] > 0 ? (0.5 * c->dt) / c->mass[t] : 0.0;
+    p.dt = c->dt;
+    for (int d = 0; d < 3; d++) {
+        p.org[d] = c->box.org[d];
+        p.P[d] = c->box.P[d];
+    }
+    float hs = (float)(0.5 * c->skin);
+    p.half_skin2 = hs * hs;
+    p.use_f64 = c->use_f64 ? 1 : 0;
+    return p;
+}
+
+int integrate_kick_drift(Context* c, int) {
+    IntParams p = int_params(c);
+    prof_begin(c, "kick_drift");
+    k_kick_drift<<<grid_for(c->n, 256), 256, 0, c->stream>>>(p, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->fx, c->fy,
+                                                             c->fz, c->f64, c->type, c->pack, c->xref,
+                                                             reinterpret_cast<StepState*>(c->d_state));
+    prof_end(c);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "kick_drift");
+}
+
+static int reduce_and_finalize(Context* c, int kick, int count_step) {
+    IntParams p = int_params(c);
+    int nb = grid_for(c->n, RED_BLOCK);
+    prof_begin(c, "kick");
+    k_kick<<<nb, RED_BLOCK, 0, c->stream>>>(p, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz, c->f64, c->type, c->d_mass,
+                                            c->pe, c->vir, c->d_red, kick);
+    prof_end(c);
+    FinParams f;
+    f.nblocks = nb;
+    f.natoms = c->n;
+    f.ledger_cap = c->ledger_cap;
+    f.count_step = count_step;
+    f.dt = c->dt;
+    f.tau = c->thermo_tau;
+    f.tset = c->thermo_T;
+    f.temp_factor = 2.0 / 3.0 / 8.61734279e-05;
+    prof_begin(c, "finalize");
+    k_finalize<<<1, 256, 0, c->stream>>>(f, c->d_red, c->d_ledger, reinterpret_cast<StepState*>(c->d_state));
+    prof_end(c);
+    c->launches += 2;
+    return check_cuda(c, cudaGetLastError(), "kick/finalize");
+}
+
+int integrate_kick(Context* c, int) { return reduce_and_finalize(c, 1, 1); }
+
+int measure_energies(Context* c, int) { return reduce_and_finalize(c, 0, 0); }
+
+size_t step_state_bytes() { return sizeof(StepState); }
+
+int step_state_reset(Context* c, int reset_row, int rebuild_every) {
+    StepState h;
+    cudaError_t e = cudaMemcpyAsync(&h, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "step state");
+    if (reset_row) h.row = 0;
+    h.rebuild_every = rebuild_every;
+    e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return check_cuda(c, e, "step state");
+}
+
+int step_state_read(Context* c, long long* step, int* row, int* rebuild) {
+    StepState h;
+    cudaError_t e = cudaMemcpyAsync(&h, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "step state");
+    if (step) *step = h.step;
+    if (row) *row = h.row;
+    if (rebuild) *rebuild = h.rebuild;
+    return OMDG_OK;
+}
+
+int step_state_init(Context* c) {
+    StepState h;
+    h.step = 0;
+    h.row = 0;
+    h.rebuild = 0;
+    h.lambda = 1.0;
+    h.rebuild_every = c->rebuild_every;
+    h.pad = 0;
+    cudaError_t e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return check_cuda(c, e, "step state");
+}
+
+__global__ void k_clear_rebuild(StepState* st) { st->rebuild = 0; }
+
+int step_clear_rebuild(Context* c) {
+    k_clear_rebuild<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state));
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "clear rebuild");
+}
+
+// Graph-side rebuild predicate: copies the request into the conditional
+// handle and clears it.
+__global__ void k_set_rebuild_cond(StepState* st, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, st->rebuild ? 1u : 0u);
+    st->rebuild = 0;
+}
+
+int launch_set_rebuild_cond(Context* c, cudaGraphConditionalHandle h) {
+    k_set_rebuild_cond<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state), h);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "rebuild predicate");
+}
+
+__global__ void k_zero_f(int n, float* fx, float* fy, float* fz, double* f64) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    fx[i] = 0.f;
+    fy[i] = 0.f;
+    fz[i] = 0.f;
+    if (f64) {
+        f64[3 * (size_t)i] = 0.0;
+        f64[3 * (size_t)i + 1] = 0.0;
+        f64[3 * (size_t)i + 2] = 0.0;
+    }
+}
+
+int zero_forces(Context* c) {
+    k_zero_f<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->fx, c->fy, c->fz, c->f64);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "zero forces");
+}
+
+}  // namespace omdg

@@ -1,0 +1,477 @@
+// Linked-cell binning by counting sort and the Verlet-list build
+// (replaces VerletList::Update, VerletList.cpp:126-199, and
+// VerletListFull::Update, VerletListFull.cpp:138-230, together with the
+// periodic ghost images of comhandler.cpp:288-377).
+//
+// Rebuild pipeline, all on the context stream:
+//   1 cell_assign   wrap periodic owners into the box (systemgrid.cpp:129-151),
+//                   cell of every atom, per-cell counts
+//   2 scan          exclusive scan of the counts -> cell starts
+//   3 scatter       atom -> slot in its cell
+//   4 cell_sort     sort each cell's slots by previous index (deterministic order)
+//   5 permute       reorder every per-atom array into cell order
+//   6 pack          FP32 hi/lo position packs + displacement reference
+//   7 build         full list, slot-major nbr[s*n+i]; FP32 screen, FP64 tie-break
+//   8 reverse       (three-body kernels) slot of i in each neighbour's row
+#include <algorithm>
+#include <cmath>
+
+#include "device_common.cuh"
+
+namespace omdg {
+
+struct CellGeom {
+    int nc[3];
+    double org[3], h[3];
+    int periodic[3];
+    double lo[3], L[3];
+};
+
+static CellGeom cell_geom(const Context* c) {
+    CellGeom g;
+    for (int d = 0; d < 3; d++) {
+        g.nc[d] = c->box.nc[d];
+        g.org[d] = c->box.cell_org[d];
+        g.h[d] = c->box.cell_h[d];
+        g.periodic[d] = c->box.periodic[d];
+        g.lo[d] = c->box.lo[d];
+        g.L[d] = c->box.L[d];
+    }
+    return g;
+}
+
+__device__ __forceinline__ int cell_coord(double x, double org, double h, int nc) {
+    int k = (int)floor(__ddiv_rn(__dsub_rn(x, org), h));
+    return k < 0 ? 0 : (k >= nc ? nc - 1 : k);
+}
+
+__global__ void k_cell_assign(int n, double* __restrict__ x, double* __restrict__ y, double* __restrict__ z,
+                              CellGeom g, int* __restrict__ cell, int* __restrict__ count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double p[3] = {x[i], y[i], z[i]};
+    for (int d = 0; d < 3; d++) {
+        if (!g.periodic[d]) continue;
+        // systemgrid.cpp:132-138: owned iff floor((x - x0) / lx) == 0; the owner
+        // otherwise becomes the image x + shift (comhandler.cpp:427-432).
+        int u = (int)floor(__ddiv_rn(__dsub_rn(p[d], g.lo[d]), g.L[d]));
+        if (u < 0) p[d] = __dadd_rn(p[d], g.L[d]);
+        else if (u >= 1) p[d] = __dadd_rn(p[d], -g.L[d]);
+    }
+    x[i] = p[0];
+    y[i] = p[1];
+    z[i] = p[2];
+    int cx = cell_coord(p[0], g.org[0], g.h[0], g.nc[0]);
+    int cy = cell_coord(p[1], g.org[1], g.h[1], g.nc[1]);
+    int cz = cell_coord(p[2], g.org[2], g.h[2], g.nc[2]);
+    int c = (cz * g.nc[1] + cy) * g.nc[0] + cx;
+    cell[i] = c;
+    atomicAdd(&count[c], 1);
+}
+
+// Exclusive scan of count[0..m) into start[0..m]; one block, chunked.
+__global__ void k_scan(int m, const int* __restrict__ count, int* __restrict__ start) {
+    __shared__ int sums[1024];
+    int t = threadIdx.x, nt = blockDim.x;
+    int chunk = (m + nt - 1) / nt;
+    int b = t * chunk, e = min(m, b + chunk);
+    int s = 0;
+    for (int k = b; k < e; k++) s += count[k];
+    sums[t] = s;
+    __syncthreads();
+    for (int off = 1; off < nt; off <<= 1) {
+        int v = t >= off ? sums[t - off] : 0;
+        __syncthreads();
+        sums[t] += v;
+        __syncthreads();
+    }
+    int run = sums[t] - s;
+    for (int k = b; k < e; k++) {
+        start[k] = run;
+        run += count[k];
+    }
+    if (t == nt - 1) start[m] = sums[t];
+}
+
+__global__ void k_scatter(int n, const int* __restrict__ cell, const int* __restrict__ start, int* __restrict__ fill,
+                          int* __restrict__ perm) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = cell[i];
+    int s = start[c] + atomicAdd(&fill[c], 1);
+    perm[s] = i;
+}
+
+// Atomic slot order is arbitrary; sorting each cell by previous index makes
+// the final order (and every later floating-point sum) deterministic.
+__global__ void k_cell_sort(int m, const int* __restrict__ start, int* __restrict__ perm) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m) return;
+    int b = start[c], e = start[c + 1];
+    for (int k = b + 1; k < e; k++) {
+        int v = perm[k];
+        int q = k - 1;
+        while (q >= b && perm[q] > v) {
+            perm[q + 1] = perm[q];
+            q--;
+        }
+        perm[q + 1] = v;
+    }
+}
+
+// Per-atom state that survives a rebuild, gathered into staging and copied
+// back so every array keeps its address (a captured step graph replays the
+// same pointers).
+struct AtomArrays {
+    double *x, *y, *z, *vx, *vy, *vz;
+    int *type, *id;
+    double* extra;   // optional per-atom FP64 state (extra_n values per atom, slot-major)
+    int extra_n;
+};
+
+__global__ void k_permute_gather(int n, const int* __restrict__ perm, AtomArrays a, AtomArrays st) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int o = perm[k];
+    st.x[k] = a.x[o];
+    st.y[k] = a.y[o];
+    st.z[k] = a.z[o];
+    st.vx[k] = a.vx[o];
+    st.vy[k] = a.vy[o];
+    st.vz[k] = a.vz[o];
+    st.type[k] = a.type[o];
+    st.id[k] = a.id[o];
+    for (int q = 0; q < a.extra_n; q++) st.extra[(size_t)q * n + k] = a.extra[(size_t)q * n + o];
+}
+
+__global__ void k_permute_copyback(int n, AtomArrays st, AtomArrays a) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    a.x[k] = st.x[k];
+    a.y[k] = st.y[k];
+    a.z[k] = st.z[k];
+    a.vx[k] = st.vx[k];
+    a.vy[k] = st.vy[k];
+    a.vz[k] = st.vz[k];
+    a.type[k] = st.type[k];
+    a.id[k] = st.id[k];
+    for (int q = 0; q < a.extra_n; q++) a.extra[(size_t)q * n + k] = st.extra[(size_t)q * n + k];
+}
+
+__global__ void k_zero_ints(int m, int* __restrict__ a, int* __restrict__ b) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < m) {
+        a[k] = 0;
+        b[k] = 0;
+    }
+}
+
+__global__ void k_inverse(int n, const int* __restrict__ id, int* __restrict__ inv) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) inv[id[k]] = k;
+}
+
+// Cell of each sorted atom (cell[] is indexed by the previous order).
+__global__ void k_sorted_cell(int n, const int* __restrict__ perm, const int* __restrict__ cell_old,
+                              int* __restrict__ cell_new) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) cell_new[k] = cell_old[perm[k]];
+}
+
+struct PackFrame {
+    double org[3], P[3];
+};
+
+__device__ __forceinline__ void split(double X, float& hi, float& lo) {
+    hi = __double2float_rn(X);
+    lo = __double2float_rn(__dsub_rn(X, (double)hi));
+}
+
+__global__ void k_pack(int n, const double* __restrict__ x, const double* __restrict__ y,
+                       const double* __restrict__ z, const int* __restrict__ type, PackFrame f,
+                       PosPack* __restrict__ pack, float4* __restrict__ xref) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PosPack p;
+    double X = __dadd_rn(__dsub_rn(x[i], f.org[0]), f.P[0]);
+    double Y = __dadd_rn(__dsub_rn(y[i], f.org[1]), f.P[1]);
+    double Z = __dadd_rn(__dsub_rn(z[i], f.org[2]), f.P[2]);
+    split(X, p.hi.x, p.lo.x);
+    split(Y, p.hi.y, p.lo.y);
+    split(Z, p.hi.z, p.lo.z);
+    p.hi.w = __int_as_float(type[i]);
+    p.lo.w = 0.f;
+    pack[i] = p;
+    if (xref) xref[i] = make_float4(p.hi.x, p.hi.y, p.hi.z, 0.f);
+}
+
+struct BuildParams {
+    int n, maxnb;
+    int nc[3];
+    int periodic[3];
+    ShiftF L;
+    double L64[3];
+    double rsq;           // Rv*Rv in FP64 (VerletList.cpp:161)
+    float rsq_lo, rsq_hi; // FP32 screening band around rsq
+};
+
+// Per axis, the (cell, image) pairs a cell's neighbours live in.
+__device__ __forceinline__ int axis_candidates(int c, int nc, int periodic, int* cc, int* cs) {
+    int m = 0;
+    if (periodic) {
+        if (nc >= 3) {
+            for (int o = -1; o <= 1; o++) {
+                int k = c + o, s = 0;
+                if (k < 0) {
+                    k += nc;
+                    s = -1;
+                } else if (k >= nc) {
+                    k -= nc;
+                    s = 1;
+                }
+                cc[m] = k;
+                cs[m++] = s;
+            }
+        } else {
+            for (int k = 0; k < nc; k++)
+                for (int s = -1; s <= 1; s++) {
+                    cc[m] = k;
+                    cs[m++] = s;
+                }
+        }
+    } else {
+        for (int o = -1; o <= 1; o++) {
+            int k = c + o;
+            if (k < 0 || k >= nc) continue;
+            cc[m] = k;
+            cs[m++] = 0;
+        }
+    }
+    return m;
+}
+
+__global__ void __launch_bounds__(128) k_build(BuildParams p, const PosPack* __restrict__ pack,
+                                               const double* __restrict__ x, const double* __restrict__ y,
+                                               const double* __restrict__ z, const int* __restrict__ cell,
+                                               const int* __restrict__ start, unsigned* __restrict__ nbr,
+                                               int* __restrict__ nnb, unsigned* status, int* need) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    PosPack pi = pack[i];
+    int ci = cell[i];
+    int cx = ci % p.nc[0], cy = (ci / p.nc[0]) % p.nc[1], cz = ci / (p.nc[0] * p.nc[1]);
+    int ccx[6], csx[6], ccy[6], csy[6], ccz[6], csz[6];
+    int mx = axis_candidates(cx, p.nc[0], p.periodic[0], ccx, csx);
+    int my = axis_candidates(cy, p.nc[1], p.periodic[1], ccy, csy);
+    int mz = axis_candidates(cz, p.nc[2], p.periodic[2], ccz, csz);
+    int cnt = 0;
+    double xi = 0, yi = 0, zi = 0;
+    bool have64 = false;
+    for (int a = 0; a < mz; a++)
+        for (int b = 0; b < my; b++)
+            for (int q = 0; q < mx; q++) {
+                int c = (ccz[a] * p.nc[1] + ccy[b]) * p.nc[0] + ccx[q];
+                unsigned code = nbr_encode(0, csx[q], csy[b], csz[a]);
+                bool self_image = (csx[q] == 0 && csy[b] == 0 && csz[a] == 0);
+                int e = start[c + 1];
+                for (int k = start[c]; k < e; k++) {
+                    if (self_image && k == i) continue;
+                    PosPack pk = pack[k];
+                    float3 d = pair_delta(pi.hi, pi.lo, pk.hi, pk.lo, code, p.L);
+                    float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+                    if (r2 > p.rsq_hi) continue;
+                    bool in = r2 < p.rsq_lo;
+                    if (!in) {
+                        // Borderline: decide with the reference's FP64 arithmetic,
+                        // dx = x_i - (x_j + s), r2 = (dx*dx + dy*dy) + dz*dz.
+                        if (!have64) {
+                            xi = x[i];
+                            yi = y[i];
+                            zi = z[i];
+                            have64 = true;
+                        }
+                        double sx = csx[q] == 0 ? 0.0 : (csx[q] > 0 ? p.L64[0] : -p.L64[0]);
+                        double sy = csy[b] == 0 ? 0.0 : (csy[b] > 0 ? p.L64[1] : -p.L64[1]);
+                        double sz = csz[a] == 0 ? 0.0 : (csz[a] > 0 ? p.L64[2] : -p.L64[2]);
+                        double dx = __dsub_rn(xi, __dadd_rn(x[k], sx));
+                        double dy = __dsub_rn(yi, __dadd_rn(y[k], sy));
+                        double dz = __dsub_rn(zi, __dadd_rn(z[k], sz));
+                        double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                        in = rr <= p.rsq;
+                    }
+                    if (!in) continue;
+                    if (r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
+                    if (cnt < p.maxnb) nbr[(size_t)cnt * p.n + i] = code | (unsigned)k;
+                    cnt++;
+                }
+            }
+    if (cnt > p.maxnb) {
+        atomicOr(status, ERR_NBR_OVERFLOW);
+        atomicMax(need, cnt);
+        cnt = p.maxnb;
+    }
+    nnb[i] = cnt;
+}
+
+// rev[s*n+i]: the slot of (i, -s) in row j = nbr[s*n+i].
+__global__ void k_reverse(int n, const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                          int* __restrict__ rev, unsigned* status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int m = nnb[i];
+    for (int s = 0; s < m; s++) {
+        unsigned e = nbr[(size_t)s * n + i];
+        int j = nbr_index(e);
+        unsigned want = nbr_encode(i, -nbr_sx(e), -nbr_sy(e), -nbr_sz(e));
+        int mj = nnb[j], found = -1;
+        for (int t = 0; t < mj; t++)
+            if (nbr[(size_t)t * n + j] == want) {
+                found = t;
+                break;
+            }
+        if (found < 0) atomicOr(status, ERR_NBR_OVERFLOW);
+        rev[(size_t)s * n + i] = found < 0 ? 0 : found;
+    }
+}
+
+// ---------------------------------------------------------------- host side
+
+void nlist_prepare_geometry(Context* c) {
+    double rv = c->rc_max + c->skin;
+    BoxGeom& b = c->box;
+    for (int d = 0; d < 3; d++) {
+        if (b.periodic[d]) {
+            b.cell_org[d] = b.lo[d];
+            int nc = (int)(b.L[d] / rv);
+            b.nc[d] = nc < 1 ? 1 : nc;
+            b.cell_h[d] = b.L[d] / b.nc[d];
+        } else {
+            // free axis: a fixed grid over the box with a margin; atoms
+            // beyond it are clamped into the edge cells, which keeps the
+            // 27-cell search complete.
+            double margin = 2.0 * rv;
+            b.cell_org[d] = b.lo[d] - margin;
+            double ext = b.L[d] + 2.0 * margin;
+            int nc = (int)(ext / rv);
+            b.nc[d] = nc < 1 ? 1 : nc;
+            b.cell_h[d] = ext / b.nc[d];
+        }
+    }
+}
+
+int nlist_reserve(Context* c, int maxnb) {
+    size_t need = (size_t)maxnb * (size_t)c->cap * sizeof(unsigned);
+    if (maxnb <= c->maxnb && c->nbr) return OMDG_OK;
+    cudaFree(c->nbr);
+    cudaFree(c->rev);
+    cudaFree(c->slot_buf);
+    c->nbr = nullptr;
+    c->rev = nullptr;
+    c->slot_buf = nullptr;
+    if (cudaMalloc(&c->nbr, need) != cudaSuccess) return set_error(c, OMDG_ENOMEM, "neighbour list allocation");
+    if (c->need_rev) {
+        if (cudaMalloc(&c->rev, need) != cudaSuccess) return set_error(c, OMDG_ENOMEM, "reverse slot allocation");
+        if (cudaMalloc(&c->slot_buf, (size_t)maxnb * c->cap * sizeof(float4)) != cudaSuccess)
+            return set_error(c, OMDG_ENOMEM, "slot buffer allocation");
+    }
+    c->maxnb = maxnb;
+    c->nbr_bytes = (long)need;
+    return OMDG_OK;
+}
+
+static int ensure_cells(Context* c, int m) {
+    if (m + 1 <= c->ncell_cap) return OMDG_OK;
+    cudaFree(c->cell_count);
+    cudaFree(c->cell_start);
+    cudaFree(c->cell_fill);
+    int cap = m + 1;
+    if (cudaMalloc(&c->cell_count, cap * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&c->cell_start, (cap + 1) * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&c->cell_fill, cap * sizeof(int)) != cudaSuccess)
+        return set_error(c, OMDG_ENOMEM, "cell arrays");
+    c->ncell_cap = cap;
+    return OMDG_OK;
+}
+
+PackFrame pack_frame(const Context* c) {
+    PackFrame f;
+    for (int d = 0; d < 3; d++) {
+        f.org[d] = c->box.org[d];
+        f.P[d] = c->box.P[d];
+    }
+    return f;
+}
+
+int integrate_pack(Context* c) {
+    if (c->n == 0) return OMDG_OK;
+    k_pack<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack,
+                                                       c->xref);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "pack");
+}
+
+int nlist_build(Context* c) {
+    int n = c->n;
+    if (n == 0) return OMDG_OK;
+    CellGeom g = cell_geom(c);
+    int m = g.nc[0] * g.nc[1] * g.nc[2];
+    int rc = ensure_cells(c, m);
+    if (rc) return rc;
+    cudaStream_t s = c->stream;
+    prof_begin(c, "cell_sort");
+    k_zero_ints<<<grid_for(m + 1, 256), 256, 0, s>>>(m + 1, c->cell_count, c->cell_fill);
+    k_cell_assign<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, g, c->cell, c->cell_count);
+    k_scan<<<1, 1024, 0, s>>>(m, c->cell_count, c->cell_start);
+    k_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->cell, c->cell_start, c->cell_fill, c->perm);
+    k_cell_sort<<<grid_for(m, 128), 128, 0, s>>>(m, c->cell_start, c->perm);
+    c->launches += 5;
+    AtomArrays cur{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->extra, c->extra_n};
+    AtomArrays stg{c->stage_d, c->stage_d + c->cap, c->stage_d + 2 * (size_t)c->cap, c->stage_d + 3 * (size_t)c->cap,
+                   c->stage_d + 4 * (size_t)c->cap, c->stage_d + 5 * (size_t)c->cap, c->stage_i,
+                   c->stage_i + c->cap, c->stage_extra, c->extra_n};
+    k_permute_gather<<<grid_for(n, 256), 256, 0, s>>>(n, c->perm, cur, stg);
+    k_permute_copyback<<<grid_for(n, 256), 256, 0, s>>>(n, stg, cur);
+    c->launches += 2;
+    int* cell_sorted = c->cell_sorted;
+    k_sorted_cell<<<grid_for(n, 256), 256, 0, s>>>(n, c->perm, c->cell, cell_sorted);
+    k_inverse<<<grid_for(n, 256), 256, 0, s>>>(n, c->id, c->inv);
+    c->launches += 2;
+    prof_end(c);
+    prof_begin(c, "pack");
+    k_pack<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack, c->xref);
+    c->launches++;
+    prof_end(c);
+
+    BuildParams bp;
+    bp.n = n;
+    bp.maxnb = c->maxnb;
+    for (int d = 0; d < 3; d++) {
+        bp.nc[d] = g.nc[d];
+        bp.periodic[d] = g.periodic[d];
+        bp.L64[d] = g.L[d];
+    }
+    bp.L = make_shift(c->box);
+    double rv = c->rc_max + c->skin;
+    bp.rsq = rv * rv;
+    bp.rsq_lo = (float)(bp.rsq * (1.0 - 2e-5));
+    bp.rsq_hi = (float)(bp.rsq * (1.0 + 2e-5));
+    prof_begin(c, "nlist_build");
+    k_build<<<grid_for(n, 128), 128, 0, s>>>(bp, c->pack, c->x, c->y, c->z, cell_sorted, c->cell_start,
+                                             reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
+                                             c->d_flags + 1);
+    c->launches++;
+    prof_end(c);
+    if (c->need_rev) {
+        prof_begin(c, "nlist_reverse");
+        k_reverse<<<grid_for(n, 128), 128, 0, s>>>(n, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->rev,
+                                                   c->d_status);
+        c->launches++;
+        prof_end(c);
+    }
+    c->rebuilds++;
+    c->list_valid = true;
+    c->steps_since_build = 0;
+    return check_cuda(c, cudaGetLastError(), "neighbour build");
+}
+
+}  // namespace omdg

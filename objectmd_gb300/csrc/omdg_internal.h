@@ -1,0 +1,252 @@
+// Internal types of libomdg: device-resident state of one simulation box,
+// the mixed-precision position pack, spline tables and kernel parameter
+// blocks.  Nothing here crosses the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/omdg.h"
+
+namespace omdg {
+
+// ------------------------------------------------------------ error words
+// Device kernels never trap: they OR one of these bits into the context's
+// device status word; the host maps it to an OMDG_E* code after the launch.
+enum : unsigned {
+    ERR_TABLE_RANGE = 1u,  // TableReader would die (treader.cpp:199-218)
+    ERR_OVERLAP = 2u,      // r^2 < OMD_PROXIMITY (gadget.cpp:149)
+    ERR_NBR_OVERFLOW = 4u, // per-atom neighbour capacity exceeded (host grows and rebuilds)
+    ERR_NONFINITE = 8u,    // NaN/Inf force or position
+    ERR_CELL = 16u,        // atom outside the cell grid of a free axis (host re-grids)
+};
+
+constexpr int CODE_SHIFT = 26;                // nbr entry = j | code << 26
+constexpr int INDEX_MASK = (1 << CODE_SHIFT) - 1;
+constexpr int MAX_ATOMS = INDEX_MASK;         // 67,108,863
+constexpr int MAX_TYPES = 8;                  // MAXATOMTYPE (config.h:25)
+constexpr double OMD_PROXIMITY = 1e-6;        // config.h:31
+
+// ------------------------------------------------------------ spline table
+// One TableReader (treader.h:28-61): the coefficients are computed on the
+// host in FP64 exactly as the reference does; the device holds them as FP32
+// (a,b,c,d) per knot and, for FP64 kernels, as FP64.
+struct HostTable {
+    std::string file, name;
+    int n = 0;
+    double dr = 0, off = 0;
+    bool rmult = false, allow_lo = false, allow_hi = false;
+    double out_lo = 0, out_hi = 0;
+    std::vector<double> a, b, c, d;
+    double max_range() const { return off + (double)(n - 1) * dr; }
+};
+int table_load(const std::string& file, const std::string& name, HostTable& t, std::string& err);
+void table_coef(HostTable& t);
+// Reference evaluation (FP64) used by host-side checks.
+bool table_read(const HostTable& t, double r, double& val, double& dval);
+
+struct DevTable {
+    const float4* coef;    // (a, b, c, d) per knot
+    const double4_32a* coef64; // FP64 copy (FP64 kernels only, may be null)
+    float off, dr, inv_dr;
+    double off64, dr64;
+    int n;
+    int rmult;
+    int allow_lo, allow_hi;
+    float out_lo, out_hi;
+    float rc;      // max_range as float
+    double rc64;   // max_range
+};
+
+// ------------------------------------------------------------ box geometry
+// Positions are kept in FP64 (x, y, z).  Force kernels read a 32-byte pack
+// per atom: hi = float(X), lo = float(X - hi) with X = (x - org) + P, where
+// P is a power of two at least 4x the extent of the box.  All X then share
+// one float binade [P, 2P), so hi_i - hi_j is exact and subtracting the
+// split periodic length (Lh + Ll) keeps the relative vector accurate to the
+// final FP32 rounding (see pair_delta()).
+struct BoxGeom {
+    double lo[3], hi[3], L[3];
+    int periodic[3];
+    double org[3];  // origin of the pack frame (box lo, or free-axis minimum minus margin)
+    double P[3];    // pack offset (power of two)
+    float Lh[3], Ll[3];
+    // linked cells (rebuilt with the list)
+    int nc[3];
+    double cell_org[3], cell_h[3];
+};
+
+struct __align__(16) PosPack {
+    float4 hi;  // hx, hy, hz, type (bit pattern)
+    float4 lo;  // lx, ly, lz, 0
+};
+
+// ------------------------------------------------------------ potentials
+enum PotKind { POT_EAM = 1, POT_PAIR = 2, POT_SW = 3, POT_TERSOFF = 4, POT_ZBL = 5 };
+
+struct SWParams {
+    double eps, A, B, p, q, sigma, a, lambda, gamma, icos0;
+    int usezbl;
+    double sx0, sx1, sa0, sa1, sa2, sa3;
+    // derived constants (sw.cpp:65-91)
+    double rc, c1, c2, c3, c4, c5, c6, c7, c8, c9, c10, zc, ze0, ze1, ze2, ze3;
+};
+
+struct TersoffParams {
+    double A, B, lambda1, lambda2, lambda3, beta, n, c, d, h, R, D;
+};
+
+struct ZBLParams {
+    double z1, z2, rc, width;
+    double zc, ze0, ze1, ze2, ze3;
+};
+
+struct Potential {
+    PotKind kind;
+    int ta, tb;
+    bool fp64 = false;
+    HostTable t0, t1, t2;  // EAM: PAIR, EDENS, EMBED; PAIR: phi
+    SWParams sw{};
+    TersoffParams ters{};
+    ZBLParams zbl{};
+    double rc = 0;         // CutRadius as the reference sets it
+    // device copies
+    float4* d_coef[3] = {nullptr, nullptr, nullptr};
+    double4_32a* d_coef64[3] = {nullptr, nullptr, nullptr};
+    DevTable dt[3]{};
+};
+
+// ------------------------------------------------------------ kernel timing
+struct KernelTimer {
+    std::string name;
+    double ms = 0;
+    long calls = 0;
+};
+
+// ------------------------------------------------------------ context
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+
+    // atoms
+    int n = 0, cap = 0, ntypes = 0;
+    double mass[MAX_TYPES] = {0}, zat[MAX_TYPES] = {0};
+    BoxGeom box{};
+    bool have_box = false;
+
+    // device per-atom arrays (sorted order)
+    double *x = nullptr, *y = nullptr, *z = nullptr;
+    double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+    float *fx = nullptr, *fy = nullptr, *fz = nullptr;
+    float *pe = nullptr, *vir = nullptr;
+    PosPack* pack = nullptr;
+    float4* xref = nullptr;   // pack-frame position at the last build (FP32)
+    int* type = nullptr;
+    int* id = nullptr;        // caller index of sorted atom
+    int* inv = nullptr;       // sorted index of caller atom
+    float *fp = nullptr, *femb = nullptr;  // EAM F'(rho), F(rho)
+    // sort scratch
+    int *cell = nullptr, *perm = nullptr;
+    int *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr;
+    int ncell_cap = 0;
+    int* scan_partials = nullptr;
+    double* stage_d = nullptr;   // permutation staging: 6 FP64 arrays x cap
+    int* stage_i = nullptr;      // permutation staging: 2 int arrays x cap
+    double* extra = nullptr;     // optional per-atom FP64 state carried through sorts
+    double* stage_extra = nullptr;
+    int extra_n = 0;
+    int* cell_sorted = nullptr;
+    double* f64 = nullptr;       // FP64 forces (3n) + FP64 per-atom energy (n), FP64 kernels only
+    bool use_f64 = false;
+    double* d_mass = nullptr;    // mass per type (device)
+    void* d_state = nullptr;     // StepState (integrate.cu)
+
+    // neighbour list: nbr[s*n + i] = j | code << 26, count in nnb[i]
+    int* nbr = nullptr;
+    int* nnb = nullptr;
+    int* rev = nullptr;       // slot of i in row j (three-body kernels)
+    float4* slot_buf = nullptr;  // per-slot force contributions (three-body kernels)
+    int maxnb = 0;
+    long nbr_bytes = 0;
+    double skin = 0.3;
+    int rebuild_every = 0;
+    bool list_valid = false;
+    bool need_rev = false;
+    long rebuilds = 0;
+    int steps_since_build = 0;
+
+    // launch shapes chosen by the tuner (omdg_tune)
+    int eam_block = 128;
+    int eam_stage = 0;     // 1: stage spline knots in shared memory
+    int pair_block = 128;
+    int tb_block = 128;    // three-body kernels
+
+    // potentials
+    std::vector<Potential> pots;
+    double rc_max = 0;
+
+    // integrator
+    double dt = 0.001;
+    bool first_run_done = false;
+    bool reference_first_step = true;
+    long step = 0;
+    double thermo_T = 0, thermo_tau = 0;
+
+    // device status and reductions
+    unsigned* d_status = nullptr;   // error bits
+    int* d_flags = nullptr;         // [0] rebuild request
+    double* d_red = nullptr;        // block partials
+    int red_cap = 0;
+    double* d_ledger = nullptr;     // per step: kinetic, potential, virial, lambda
+    int ledger_cap = 0;
+    double* h_ledger = nullptr;     // pinned copy
+    double base_potential = 0;
+    double last_kin = 0, last_pot = 0, last_vir = 0;
+    int last_rows = 0;
+    long launches = 0;
+
+    // profiling
+    bool profiling = false;
+    std::vector<KernelTimer> timers;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    std::vector<cudaEvent_t> event_pool;
+};
+
+// ------------------------------------------------------------ host helpers
+int set_error(Context* c, int code, const std::string& msg);
+int check_cuda(Context* c, cudaError_t e, const char* what);
+int check_status(Context* c);  // reads and clears the device status word
+
+// profiling brackets (no-ops unless profiling)
+void prof_begin(Context* c, const char* name);
+void prof_end(Context* c);
+void prof_collect(Context* c);
+
+// neighbour list (nlist.cu)
+int nlist_build(Context* c);
+void nlist_prepare_geometry(Context* c);
+int nlist_reserve(Context* c, int maxnb);
+
+// forces (eam.cu, pair.cu, threebody.cu)
+int forces_compute(Context* c);
+int eam_launch(Context* c, Potential& p, bool first);
+int pair_launch(Context* c, Potential& p, bool first);
+int sw_launch(Context* c, Potential& p, bool first);
+int tersoff_launch(Context* c, Potential& p, bool first);
+int zbl_launch(Context* c, Potential& p, bool first);
+
+// integrator (integrate.cu)
+int integrate_kick_drift(Context* c, int step_index);
+int integrate_kick(Context* c, int step_index);
+int integrate_pack(Context* c);
+int measure_energies(Context* c, int row);
+int zero_forces(Context* c);
+
+// grid sizing
+inline int grid_for(int n, int block) { return (n + block - 1) / block; }
+
+}  // namespace omdg

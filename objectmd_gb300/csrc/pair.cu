@@ -1,0 +1,154 @@
+// Tabulated pair potential (TForcePair, tpair.h:38-71): fr = -phi'(r)/r for
+// r < rc (strict), ReturnForce on the owner side (forcekernel.h:92-110).
+// Two precisions: FP32 on the mixed-precision relative vector, and an FP64
+// path (positions, table and accumulation in FP64) for the plain FP64
+// Lennard-Jones configuration.
+#include "device_common.cuh"
+
+namespace omdg {
+
+struct PairParams {
+    int n;
+    ShiftF L;
+    double L64[3];
+    DevTable phi;
+    float rc, rc2;
+    double rc64;
+    int ta, tb, all_types;
+    int first;
+};
+
+__device__ __forceinline__ bool types_match(int a, int b, int ta, int tb) {
+    return (a == ta && b == tb) || (a == tb && b == ta);
+}
+
+__global__ void __launch_bounds__(256) k_pair32(PairParams p, const PosPack* __restrict__ pack,
+                                                const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                                float* __restrict__ fx, float* __restrict__ fy,
+                                                float* __restrict__ fz, float* __restrict__ pe,
+                                                float* __restrict__ vir, unsigned* status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    PosPack pi = pack[i];
+    int ti = pack_type(pi.hi);
+    Kahan ax, ay, az, ae, av;
+    bool any = p.all_types || ti == p.ta || ti == p.tb;
+    int m = any ? nnb[i] : 0;
+    for (int s = 0; s < m; s++) {
+        unsigned e = __ldg(&nbr[(size_t)s * p.n + i]);
+        int j = nbr_index(e);
+        const float4* pj = reinterpret_cast<const float4*>(pack + j);
+        float4 hj = __ldg(pj), lj = __ldg(pj + 1);
+        if (!p.all_types && !types_match(ti, pack_type(hj), p.ta, p.tb)) continue;
+        float3 d = pair_delta(pi.hi, pi.lo, hj, lj, e, p.L);
+        float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        if (r2 >= p.rc2) continue;
+        float rinv = rsqrtf(r2);
+        float r = r2 * rinv;
+        if (!(r < p.rc)) continue;
+        float ph, dph;
+        tab_read(p.phi, p.phi.coef, r, rinv, ph, dph, status);
+        float fr = -dph * rinv;
+        ax.add(d.x * fr);
+        ay.add(d.y * fr);
+        az.add(d.z * fr);
+        ae.add(0.5f * ph);
+        av.add(fr * r2);
+    }
+    if (p.first) {
+        fx[i] = ax.value();
+        fy[i] = ay.value();
+        fz[i] = az.value();
+        pe[i] = ae.value();
+        vir[i] = av.value();
+    } else if (m) {
+        fx[i] += ax.value();
+        fy[i] += ay.value();
+        fz[i] += az.value();
+        pe[i] += ae.value();
+        vir[i] += av.value();
+    }
+}
+
+// FP64 end to end: dx = x_i - (x_j + s), r = sqrt(r2), TableReader in FP64.
+__global__ void __launch_bounds__(256) k_pair64(PairParams p, const double* __restrict__ x,
+                                                const double* __restrict__ y, const double* __restrict__ z,
+                                                const int* __restrict__ type, const unsigned* __restrict__ nbr,
+                                                const int* __restrict__ nnb, double* __restrict__ f64,
+                                                float* __restrict__ pe, float* __restrict__ vir, unsigned* status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    int ti = type[i];
+    double xi = x[i], yi = y[i], zi = z[i];
+    double ax = 0, ay = 0, az = 0, ae = 0, av = 0;
+    bool any = p.all_types || ti == p.ta || ti == p.tb;
+    int m = any ? nnb[i] : 0;
+    for (int s = 0; s < m; s++) {
+        unsigned e = __ldg(&nbr[(size_t)s * p.n + i]);
+        int j = nbr_index(e);
+        if (!p.all_types && !types_match(ti, type[j], p.ta, p.tb)) continue;
+        int sx = nbr_sx(e), sy = nbr_sy(e), sz = nbr_sz(e);
+        double gx = __dadd_rn(x[j], sx == 0 ? 0.0 : (sx > 0 ? p.L64[0] : -p.L64[0]));
+        double gy = __dadd_rn(y[j], sy == 0 ? 0.0 : (sy > 0 ? p.L64[1] : -p.L64[1]));
+        double gz = __dadd_rn(z[j], sz == 0 ? 0.0 : (sz > 0 ? p.L64[2] : -p.L64[2]));
+        double dx = __dsub_rn(xi, gx), dy = __dsub_rn(yi, gy), dz = __dsub_rn(zi, gz);
+        double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        double r = __dsqrt_rn(r2);
+        if (!(r < p.rc64)) continue;
+        double ph, dph;
+        tab_read64(p.phi, r, ph, dph, status);
+        double fr = __ddiv_rn(-dph, r);
+        ax = __dadd_rn(ax, __dmul_rn(dx, fr));
+        ay = __dadd_rn(ay, __dmul_rn(dy, fr));
+        az = __dadd_rn(az, __dmul_rn(dz, fr));
+        ae = __dadd_rn(ae, __dmul_rn(0.5, ph));
+        av = __dadd_rn(av, __dmul_rn(fr, r2));
+    }
+    if (p.first) {
+        f64[3 * (size_t)i + 0] = ax;
+        f64[3 * (size_t)i + 1] = ay;
+        f64[3 * (size_t)i + 2] = az;
+        pe[i] = (float)ae;
+        vir[i] = (float)av;
+    } else if (m) {
+        f64[3 * (size_t)i + 0] += ax;
+        f64[3 * (size_t)i + 1] += ay;
+        f64[3 * (size_t)i + 2] += az;
+        pe[i] += (float)ae;
+        vir[i] += (float)av;
+    }
+    // FP64 potential energy per atom for the ledger
+    f64[3 * (size_t)p.n + i] = p.first ? ae : f64[3 * (size_t)p.n + i] + ae;
+}
+
+int pair_launch(Context* c, Potential& pot, bool first) {
+    PairParams p;
+    p.n = c->n;
+    p.L = make_shift(c->box);
+    for (int d = 0; d < 3; d++) p.L64[d] = c->box.L[d];
+    p.phi = pot.dt[0];
+    p.rc64 = pot.t0.max_range();
+    p.rc = (float)p.rc64;
+    p.rc2 = p.rc * p.rc * 1.0001f;
+    p.ta = pot.ta;
+    p.tb = pot.tb;
+    p.all_types = c->ntypes == 1 ? 1 : 0;
+    p.first = first ? 1 : 0;
+    int block = c->pair_block;
+    if (pot.fp64) {
+        prof_begin(c, "pair64");
+        k_pair64<<<grid_for(c->n, block), block, 0, c->stream>>>(p, c->x, c->y, c->z, c->type,
+                                                                  reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
+                                                                  c->f64, c->pe, c->vir, c->d_status);
+    } else {
+        prof_begin(c, "pair32");
+        k_pair32<<<grid_for(c->n, block), block, 0, c->stream>>>(p, c->pack,
+                                                                  reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
+                                                                  c->fx, c->fy, c->fz, c->pe, c->vir, c->d_status);
+    }
+    prof_end(c);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "pair");
+}
+
+}  // namespace omdg

@@ -1,0 +1,150 @@
+// Host-side TableReader: reads one '#$NAME'-tagged section of an Object-MD
+// table file and computes its spline coefficients in FP64 with the
+// reference's own algorithm (treader.cpp:37-136), so the device only ever
+// sees the coefficients the reference would use.
+#include <cmath>
+#include <fstream>
+#include <map>
+#include <sstream>
+
+#include "omdg_internal.h"
+
+namespace omdg {
+
+// treader.cpp:83-136 and param.cpp:106-136 (read_pseudo): collect the
+// '#$NAME key value' tokens up to the '#$NAME --' line, then read
+// NumberOfData values after it.
+int table_load(const std::string& file, const std::string& name, HostTable& t, std::string& err) {
+    std::ifstream fl(file.c_str());
+    if (!fl.good()) {
+        err = "can not open table file " + file;
+        return OMDG_EFILE;
+    }
+    std::string tag = "#$" + name;
+    std::map<std::string, std::vector<std::string>> meta;
+    std::string line;
+    bool found = false;
+    while (std::getline(fl, line)) {
+        std::istringstream ss(line);
+        std::string s, key;
+        ss >> s >> key;
+        if (s != tag) continue;
+        if (key == "--") {
+            found = true;
+            break;
+        }
+        std::vector<std::string> vals;
+        std::string v;
+        while (ss >> v) vals.push_back(v);
+        meta[key] = vals;
+    }
+    if (!found) {
+        err = "can not find table " + name + "@" + file;
+        return OMDG_EFILE;
+    }
+    auto num = [&](const char* k, double def, bool required, double& out) -> bool {
+        auto it = meta.find(k);
+        if (it == meta.end() || it->second.empty()) {
+            if (required) return false;
+            out = def;
+            return true;
+        }
+        out = std::strtod(it->second[0].c_str(), nullptr);
+        return true;
+    };
+    double nd = 0, dr = 0, off = 0;
+    if (!num("NumberOfData", 0, true, nd) || !num("Spacing", 0, true, dr)) {
+        err = "table " + name + "@" + file + " lacks NumberOfData/Spacing";
+        return OMDG_EFILE;
+    }
+    num("Offset", 0.0, false, off);
+    t.file = file;
+    t.name = name;
+    t.n = (int)nd;
+    t.dr = dr;
+    t.off = off;
+    t.rmult = false;
+    auto fit = meta.find("Format");
+    if (fit != meta.end() && !fit->second.empty()) {
+        if (fit->second[0] == "RMULT") t.rmult = true;
+        else if (fit->second[0] != "PLAIN") {
+            err = "unsupported format " + fit->second[0];
+            return OMDG_EFILE;
+        }
+    }
+    t.allow_lo = meta.count("OutOfRangeLower") > 0;
+    t.allow_hi = meta.count("OutOfRangeUpper") > 0;
+    num("OutOfRangeLower", 0.0, false, t.out_lo);
+    num("OutOfRangeUpper", 0.0, false, t.out_hi);
+    if (t.n < 4 || !(t.dr > 0)) {
+        err = "table " + name + "@" + file + " too small";
+        return OMDG_EFILE;
+    }
+    t.d.assign(t.n, 0.0);
+    for (int i = 0; i < t.n; i++) {
+        if (!(fl >> t.d[i])) {
+            err = "table " + name + "@" + file + " has fewer than NumberOfData values";
+            return OMDG_EFILE;
+        }
+    }
+    table_coef(t);
+    return OMDG_OK;
+}
+
+// treader.cpp:37-64, same operation order (the tridiagonal system with end
+// rows b=5 and S[0]=S[1], S[n+1]=S[n]).
+void table_coef(HostTable& t) {
+    int nd = t.n;
+    int n = nd - 2;
+    std::vector<double> b(n), d(n), S(nd);
+    double dr = t.dr;
+    t.a.assign(nd, 0.0);
+    t.b.assign(nd, 0.0);
+    t.c.assign(nd, 0.0);
+    for (int i = 1; i < n + 1; i++) d[i - 1] = t.d[i + 1] - 2.0 * t.d[i] + t.d[i - 1];
+    for (int i = 1; i < n - 1; i++) b[i] = 4.0;
+    b[0] = b[n - 1] = 5.0;
+    for (int k = 1; k < n; k++) {
+        double m = 1.0 / b[k - 1];
+        b[k] -= m;
+        d[k] -= m * d[k - 1];
+    }
+    S[n + 1] = S[n] = d[n - 1] / b[n - 1];
+    for (int k = n - 2; k >= 0; k--) S[k + 1] = (d[k] - 1.0 * S[k + 2]) / b[k];
+    S[0] = S[1];
+    for (int i = 0; i < nd - 1; i++) {
+        t.a[i] = (S[i + 1] - S[i]) / dr / dr / dr;
+        t.b[i] = 3.0 * S[i] / dr / dr;
+        t.c[i] = (t.d[i + 1] - t.d[i] - 2.0 * S[i] - S[i + 1]) / dr;
+    }
+}
+
+bool table_read(const HostTable& t, double r, double& val, double& dval) {
+    double rval = r - t.off;
+    int x = (int)(rval / t.dr);
+    double dx = rval - (double)x * t.dr;
+    if (x > t.n - 1) {
+        if (!t.allow_hi) return false;
+        val = dval = t.out_hi;
+        return true;
+    }
+    if (x < -1) {
+        if (!t.allow_lo) return false;
+        val = dval = t.out_lo;
+        return true;
+    }
+    if (x == t.n - 1) {
+        dx += t.dr;
+        x--;
+    }
+    if (x == -1) x = 0;
+    val = (t.d[x] + dx * (t.c[x] + dx * (t.b[x] + dx * t.a[x])));
+    dval = (t.c[x] + dx * (2.0 * t.b[x] + 3.0 * dx * t.a[x]));
+    if (t.rmult) {
+        val /= r;
+        dval = (dval - val) / r;
+    }
+    return true;
+}
+
+}  // namespace omdg

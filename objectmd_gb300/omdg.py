@@ -1,0 +1,254 @@
+"""ctypes binding of libomdg's C ABI (include/omdg.h).
+
+This is the thin host layer the Python tests, the benchmark and the plugin
+mirror (objectmd_gb300.plugin) call.  It loads the in-tree
+``objectmd_gb300/_build/libomdg.so`` and fails loudly when it is missing:
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libomdg.so")
+
+OMDG_OK = 0
+ERRORS = {
+    -1: "OMDG_EINVAL",
+    -2: "OMDG_ECUDA",
+    -3: "OMDG_ERANGE",
+    -4: "OMDG_EOVERLAP",
+    -5: "OMDG_ENOMEM",
+    -6: "OMDG_ESTATE",
+    -7: "OMDG_EFILE",
+    -8: "OMDG_ENONFINITE",
+}
+
+# every symbol include/omdg.h declares, with its ctypes signature
+_P = ctypes.POINTER
+_d, _i, _l, _vp, _cp = ctypes.c_double, ctypes.c_int, ctypes.c_long, ctypes.c_void_p, ctypes.c_char_p
+SIGNATURES = {
+    "omdg_create": [_P(_vp), _i],
+    "omdg_destroy": [_vp],
+    "omdg_last_error": [_vp],
+    "omdg_get_stream": [_vp, _P(_vp)],
+    "omdg_set_box": [_vp, _P(_d), _P(_d), _P(_i)],
+    "omdg_set_atoms": [_vp, _i, _P(_d), _P(_d), _P(_i), _i, _P(_d), _P(_d)],
+    "omdg_num_atoms": [_vp, _P(_i)],
+    "omdg_get_state": [_vp, _P(_d), _P(_d), _P(_d), _P(_d), _P(_d)],
+    "omdg_set_positions": [_vp, _P(_d)],
+    "omdg_set_velocities": [_vp, _P(_d)],
+    "omdg_add_eam": [_vp, _i, _i, _cp],
+    "omdg_add_pair_table": [_vp, _i, _i, _cp, _i],
+    "omdg_add_sw": [_vp, _i, _i, _cp],
+    "omdg_add_tersoff": [_vp, _i, _i, _cp],
+    "omdg_add_zbl": [_vp, _i, _i, _d, _d],
+    "omdg_max_cut_radius": [_vp, _P(_d)],
+    "omdg_set_neighbor": [_vp, _d, _i],
+    "omdg_build_neighbors": [_vp],
+    "omdg_get_neighbors": [_vp, _P(_i), _P(_i), _P(_i), _l, _P(_l)],
+    "omdg_compute_forces": [_vp],
+    "omdg_set_timestep": [_vp, _d],
+    "omdg_step": [_vp, _i],
+    "omdg_set_first_step_mode": [_vp, _i],
+    "omdg_ledger": [_vp, _P(_d), _P(_d), _P(_d), _P(_d)],
+    "omdg_ledger_history": [_vp, _P(_d), _P(_d), _i, _P(_i)],
+    "omdg_set_thermostat": [_vp, _d, _d],
+    "omdg_stats": [_vp, _P(_l), _P(_l)],
+    "omdg_set_profiling": [_vp, _i],
+    "omdg_kernel_times": [_vp, _cp, _i, _P(_d), _P(_l), _i, _P(_i)],
+}
+
+
+class OMDGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, str(code)), msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libomdg.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError("libomdg.so not built (%s); run objectmd_gb300/build.py" % path)
+    lib = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _cp if name == "omdg_last_error" else _i
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_P(_d))
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(_P(_i))
+
+
+class Context:
+    """One simulation box on one GPU (omdg_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.h = _vp()
+        self._check(self.lib.omdg_create(ctypes.byref(self.h), device), "omdg_create")
+        self.n = 0
+
+    def _check(self, rc, what=""):
+        if rc != OMDG_OK:
+            msg = self.lib.omdg_last_error(self.h).decode() if self.h else what
+            raise OMDGError(rc, msg or what)
+
+    def close(self):
+        if self.h:
+            self.lib.omdg_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---------------------------------------------------------------- setup
+    def set_box(self, lo, hi, periodic=(True, True, True)):
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        hi = np.ascontiguousarray(hi, dtype=np.float64)
+        p = np.ascontiguousarray([1 if q else 0 for q in periodic], dtype=np.int32)
+        self._check(self.lib.omdg_set_box(self.h, _dp(lo), _dp(hi), _ip(p)))
+
+    def set_atoms(self, x, v=None, types=None, masses=(1.0,), znum=None):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        n = len(x)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        t = np.zeros(n, dtype=np.int32) if types is None else np.ascontiguousarray(types, dtype=np.int32)
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        z = None if znum is None else np.ascontiguousarray(znum, dtype=np.float64)
+        self._check(self.lib.omdg_set_atoms(self.h, n, _dp(x), _dp(v), _ip(t), len(m), _dp(m), _dp(z)))
+        self.n = n
+
+    def get_state(self):
+        n = self.n
+        x = np.zeros((n, 3))
+        v = np.zeros((n, 3))
+        f = np.zeros((n, 3))
+        e = np.zeros(n)
+        w = np.zeros(n)
+        self._check(self.lib.omdg_get_state(self.h, _dp(x), _dp(v), _dp(f), _dp(e), _dp(w)))
+        return {"x": x, "v": v, "f": f, "pot": e, "vir": w}
+
+    def set_positions(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        self._check(self.lib.omdg_set_positions(self.h, _dp(x)))
+
+    def set_velocities(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        self._check(self.lib.omdg_set_velocities(self.h, _dp(v)))
+
+    def add_eam(self, table_file, ta=0, tb=0):
+        self._check(self.lib.omdg_add_eam(self.h, ta, tb, table_file.encode()))
+
+    def add_pair_table(self, table_file, ta=0, tb=0, fp64=False):
+        self._check(self.lib.omdg_add_pair_table(self.h, ta, tb, table_file.encode(), 1 if fp64 else 0))
+
+    def add_sw(self, param_file, ta=0, tb=0):
+        self._check(self.lib.omdg_add_sw(self.h, ta, tb, param_file.encode()))
+
+    def add_tersoff(self, param_file, ta=0, tb=0):
+        self._check(self.lib.omdg_add_tersoff(self.h, ta, tb, param_file.encode()))
+
+    def add_zbl(self, ta, tb, rc, width):
+        self._check(self.lib.omdg_add_zbl(self.h, ta, tb, float(rc), float(width)))
+
+    def max_cut_radius(self):
+        r = _d()
+        self._check(self.lib.omdg_max_cut_radius(self.h, ctypes.byref(r)))
+        return r.value
+
+    def set_neighbor(self, skin=0.3, rebuild_every=0):
+        self._check(self.lib.omdg_set_neighbor(self.h, float(skin), int(rebuild_every)))
+
+    def build_neighbors(self):
+        self._check(self.lib.omdg_build_neighbors(self.h))
+
+    def neighbors(self):
+        """Canonical tuples as CSR (offsets, j, code), rows sorted by (j, code)."""
+        n = self.n
+        off = np.zeros(n + 1, dtype=np.int32)
+        cnt = _l()
+        rc = self.lib.omdg_get_neighbors(self.h, _ip(off), None, None, 0, ctypes.byref(cnt))
+        if rc not in (OMDG_OK, -1):
+            self._check(rc)
+        j = np.zeros(max(1, cnt.value), dtype=np.int32)
+        c = np.zeros(max(1, cnt.value), dtype=np.int32)
+        self._check(self.lib.omdg_get_neighbors(self.h, _ip(off), _ip(j), _ip(c), cnt.value, ctypes.byref(cnt)))
+        return off, j[:cnt.value], c[:cnt.value]
+
+    # ----------------------------------------------------------------- run
+    def compute_forces(self):
+        self._check(self.lib.omdg_compute_forces(self.h))
+
+    def set_timestep(self, dt):
+        self._check(self.lib.omdg_set_timestep(self.h, float(dt)))
+
+    def set_first_step_mode(self, reference=True):
+        self._check(self.lib.omdg_set_first_step_mode(self.h, 1 if reference else 0))
+
+    def set_thermostat(self, temperature, tau):
+        self._check(self.lib.omdg_set_thermostat(self.h, float(temperature), float(tau)))
+
+    def step(self, nsteps=1):
+        self._check(self.lib.omdg_step(self.h, int(nsteps)))
+
+    def ledger(self):
+        k, p, b, w = _d(), _d(), _d(), _d()
+        self._check(self.lib.omdg_ledger(self.h, ctypes.byref(k), ctypes.byref(p), ctypes.byref(b), ctypes.byref(w)))
+        return {"kinetic": k.value, "potential": p.value, "base_potential": b.value, "virial": w.value,
+                "energy": k.value + p.value - b.value}
+
+    def ledger_history(self, cap=1 << 16):
+        k = np.zeros(cap)
+        p = np.zeros(cap)
+        rows = _i()
+        self._check(self.lib.omdg_ledger_history(self.h, _dp(k), _dp(p), cap, ctypes.byref(rows)))
+        return k[:rows.value].copy(), p[:rows.value].copy()
+
+    def stats(self):
+        r, l = _l(), _l()
+        self._check(self.lib.omdg_stats(self.h, ctypes.byref(r), ctypes.byref(l)))
+        return {"rebuilds": r.value, "launches": l.value}
+
+    def stream(self):
+        s = _vp()
+        self._check(self.lib.omdg_get_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def set_profiling(self, on=True):
+        self._check(self.lib.omdg_set_profiling(self.h, 1 if on else 0))
+
+    def kernel_times(self, cap=64):
+        buf = ctypes.create_string_buffer(4096)
+        ms = np.zeros(cap)
+        calls = np.zeros(cap, dtype=np.int64)
+        nk = _i()
+        self._check(self.lib.omdg_kernel_times(self.h, buf, 4096, _dp(ms), calls.ctypes.data_as(_P(_l)), cap,
+                                               ctypes.byref(nk)))
+        names = buf.value.decode().split(";") if nk.value else []
+        return {names[k]: (float(ms[k]), int(calls[k])) for k in range(nk.value)}

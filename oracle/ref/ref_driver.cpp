@@ -245,6 +245,22 @@ int main(int argc, char** argv) {
         int nval = (key == "tcontrol") ? 2 : 1;
         for (int k = 0; k < nval && i < argc; k++) opt[key].push_back(argv[i++]);
     }
+    /* Table mode: the reference TableReader itself (treader.cpp) evaluated at
+       the r values listed one per line in file `rfile`; prints r val dval. */
+    if (opt.count("tabfile")) {
+        TableReader t(opt["tabfile"][0], opt.count("tabname") ? opt["tabname"][0] : std::string(""));
+        FILE* rf = fopen(opt["rfile"][0].c_str(), "r");
+        FILE* of = fopen((outdir + "/table.txt").c_str(), "w");
+        double r;
+        while (rf && fscanf(rf, "%lf", &r) == 1) {
+            double v, dv;
+            t.read(r, v, dv);
+            fprintf(of, "%.17g %.17g %.17g\n", r, v, dv);
+        }
+        if (rf) fclose(rf);
+        fclose(of);
+        return 0;
+    }
     /* Reference parameters go through the reference's own ParamHandler argv path. */
     std::vector<std::string> args;
     args.push_back(argv[0]);

@@ -1,0 +1,186 @@
+"""Generates the golden fixtures under tests/golden/ from the REFERENCE's own code.
+
+Run here, where the Object-MD sources exist (python tests/golden/make_golden.py);
+the GPU tests only read the committed outputs.  Steps:
+
+1. Build the reference CPU path (oracle/ref/Makefile -> oracle/_ref/ref_driver*).
+2. Write the tables the configurations use into tests/golden/tables/:
+   - eam.aluminum5000: the reference's tables/eam.aluminum (PAIR, EDENS,
+     EMBED; 1000 knots each) resampled to 5000 knots over the same ranges by
+     evaluating the reference spline (TableReader::read restated in
+     oracle/omd_oracle.c, which is pinned to the reference below);
+   - pair.lj.argon: analytic 12-6 LJ (sigma 3.405, eps 0.0104, rc 2.5 sigma);
+   - sw.silicon and tersoff.silicon27 parameter files.
+3. Generate seeded atom configurations (objectmd_gb300.inputs) and run the
+   reference on them: static forces, per-atom energies, virials and the
+   neighbour tuples, plus a short NVE trajectory.
+4. Save each case as <case>.npz with its Import file.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from objectmd_gb300 import inputs  # noqa: E402
+from oracle import oracle as oc  # noqa: E402
+
+REF = os.environ.get("OMD_REFERENCE", "/root/reference")
+GOLD = os.path.join(ROOT, "tests", "golden")
+TABLES = os.path.join(GOLD, "tables")
+
+
+def resample_section(spec: dict, n_new: int):
+    """Evaluate the reference spline of one table section on a finer grid.
+
+    The stored quantity is resampled (for RMULT tables that is r*phi), so the
+    new table reads back the same function through TableReader semantics.
+    """
+    t = oc.Table(dict(spec, rmult=0))
+    lo = spec["off"]
+    hi = spec["off"] + (spec["n"] - 1) * spec["dr"]
+    dr = (hi - lo) / (n_new - 1)
+    r = lo + dr * np.arange(n_new)
+    r[-1] = min(r[-1], hi)
+    vals = np.array([t.read(x)[0] for x in r])
+    return dr, lo, vals
+
+
+def write_eam5000(path):
+    src = os.path.join(REF, "tables", "eam.aluminum")
+    out = ["# Object-MD table: tables/eam.aluminum resampled to 5000 knots per section",
+           "# (reference spline evaluated at the new knots; same ranges and formats)"]
+    for name in ("PAIR", "EDENS", "EMBED"):
+        spec = oc.parse_table(src, name)
+        dr, off, vals = resample_section(spec, 5000)
+        out.append("#$%s NumberOfData %d" % (name, 5000))
+        out.append("#$%s Spacing %.17g" % (name, dr))
+        out.append("#$%s Offset %.17g" % (name, off))
+        if spec["rmult"]:
+            out.append("#$%s Format RMULT" % name)
+        out.append("#$%s --" % name)
+        out += ["%.17g" % v for v in vals]
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")
+
+
+def table_dir():
+    """OMD_TABLE for reference runs: the reference tables plus the generated ones."""
+    d = tempfile.mkdtemp(prefix="omdtab_")
+    for f in os.listdir(os.path.join(REF, "tables")):
+        os.symlink(os.path.join(REF, "tables", f), os.path.join(d, f))
+    for f in os.listdir(TABLES):
+        dst = os.path.join(d, f)
+        if os.path.lexists(dst):
+            os.remove(dst)
+        os.symlink(os.path.join(TABLES, f), dst)
+    return d
+
+
+def save_case(name, import_file, res, **extra):
+    a = res["atoms"]
+    payload = dict(nid=a[:, 0].astype(np.int32), tid=a[:, 1].astype(np.int32), x=a[:, 2:5], v=a[:, 5:8],
+                   f=a[:, 8:11], pot=a[:, 11], vir=a[:, 12])
+    if "nbr" in res:
+        payload["nbr"] = res["nbr"].astype(np.int32)
+    if "ledger" in res:
+        payload["ledger"] = res["ledger"]
+    for k in ("potential", "kinetic", "base_potential", "virial", "max_cut_radius"):
+        if k in res["summary"]:
+            payload["summary_" + k] = np.array(res["summary"][k])
+    payload.update(extra)
+    np.savez_compressed(os.path.join(GOLD, name + ".npz"), **payload)
+    shutil.copy(import_file, os.path.join(GOLD, name + ".dat"))
+    print("wrote", name, "atoms", len(a), "tuples", len(res.get("nbr", [])))
+
+
+def main():
+    os.makedirs(TABLES, exist_ok=True)
+    if not oc.build_reference(REF):
+        raise SystemExit("reference sources not found at %s" % REF)
+    write_eam5000(os.path.join(TABLES, "eam.aluminum5000"))
+    with open(os.path.join(TABLES, "pair.lj.argon"), "w") as fh:
+        fh.write(inputs.lj_table_text())
+    with open(os.path.join(TABLES, "sw.silicon"), "w") as fh:
+        fh.write(inputs.sw_param_text())
+    with open(os.path.join(TABLES, "tersoff.silicon27"), "w") as fh:
+        fh.write(inputs.tersoff_param_text(2.7, 0.15))
+    tdir = table_dir()
+    work = tempfile.mkdtemp(prefix="omdgold_")
+
+    # EAM Al, static, two sizes
+    for name, ncell in (("eam_al_500", 5), ("eam_al_4000", 10)):
+        x, v, (lo, hi) = inputs.eam_aluminium(ncell=ncell, a=4.05, sigma=0.05, temp=300.0, seed_pos=2, seed_vel=3)
+        f = os.path.join(work, name + ".dat")
+        inputs.write_import(f, x, v, box=(lo, hi), species=("aluminum",))
+        res = oc.run_reference(f, "eam", "aluminum5000", steps=0, dump_nbr=True, table_dir=tdir)
+        save_case(name, f, res, box_lo=lo, box_hi=hi)
+
+    # EAM Al, NVE trajectory, list rebuilt every step (comm.refresh unset)
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=5, a=4.05, sigma=0.05, temp=300.0, seed_pos=12, seed_vel=13)
+    f = os.path.join(work, "eam_al_nve.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), species=("aluminum",))
+    res = oc.run_reference(f, "eam", "aluminum5000", steps=20, dt=0.002, table_dir=tdir)
+    save_case("eam_al_nve", f, res, box_lo=lo, box_hi=hi, steps=np.array(20), dt=np.array(0.002))
+
+    # table LJ Ar (analytic LJ table), static and NVE
+    x, v, (lo, hi) = inputs.lj_argon(ncell=5, a=5.26, temp=100.0, seed_vel=1)
+    x = inputs.perturb(x, 0.05, 9, lo, hi)
+    f = os.path.join(work, "lj_ar_500.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), species=("argon",))
+    res = oc.run_reference(f, "pair", "lj.argon", steps=0, dump_nbr=True, table_dir=tdir)
+    save_case("lj_ar_500", f, res, box_lo=lo, box_hi=hi)
+    res = oc.run_reference(f, "pair", "lj.argon", steps=50, dt=0.001, table_dir=tdir)
+    save_case("lj_ar_nve", f, res, box_lo=lo, box_hi=hi, steps=np.array(50), dt=np.array(0.001))
+
+    # SW Si, static: fixed reference build (every triplet) and as-is build
+    x, v, (lo, hi) = inputs.diamond_silicon(ncell=3, a=5.431, sigma=0.08, temp=1000.0, seed_pos=4, seed_vel=5)
+    f = os.path.join(work, "sw_si_216.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), species=("silicon",))
+    res = oc.run_reference(f, "sw", "silicon", steps=0, dump_nbr=True, table_dir=tdir, swfix=True)
+    asis = oc.run_reference(f, "sw", "silicon", steps=0, table_dir=tdir, swfix=False)
+    save_case("sw_si_216", f, res, box_lo=lo, box_hi=hi, f_asis=asis["atoms"][:, 8:11],
+              pot_asis=asis["atoms"][:, 11])
+    x, v, (lo, hi) = inputs.diamond_silicon(ncell=5, a=5.431, sigma=0.03, temp=1000.0, seed_pos=4, seed_vel=5)
+    f = os.path.join(work, "sw_si_1000.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), species=("silicon",))
+    res = oc.run_reference(f, "sw", "silicon", steps=0, dump_nbr=True, table_dir=tdir, swfix=True)
+    save_case("sw_si_1000", f, res, box_lo=lo, box_hi=hi)
+
+    # Berendsen thermostat on EAM Al
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=5, a=4.05, sigma=0.05, temp=600.0, seed_pos=22, seed_vel=23)
+    f = os.path.join(work, "eam_al_tc.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), species=("aluminum",))
+    res = oc.run_reference(f, "eam", "aluminum5000", steps=20, dt=0.002, tcontrol=(300.0, 0.05), table_dir=tdir)
+    save_case("eam_al_tc", f, res, box_lo=lo, box_hi=hi, steps=np.array(20), dt=np.array(0.002),
+              tcontrol=np.array([300.0, 0.05]))
+
+    # TableReader known answers from the reference's own TableReader: the
+    # 5000-knot PAIR section (RMULT) and EMBED section (PLAIN), including the
+    # edge rules just below the first knot and past the last one.
+    for sec in ("PAIR", "EMBED"):
+        spec = oc.parse_table(os.path.join(TABLES, "eam.aluminum5000"), sec)
+        top = spec["off"] + (spec["n"] - 1) * spec["dr"]
+        r = np.concatenate([np.linspace(max(spec["off"] - 0.9 * spec["dr"], 1e-3), top + 0.9 * spec["dr"], 509),
+                            spec["off"] + spec["dr"] * np.array([0.0, 1.0, 2.5, spec["n"] - 2, spec["n"] - 1.0])])
+        rfile = os.path.join(work, "r_%s.txt" % sec)
+        np.savetxt(rfile, r, fmt="%.17g")
+        out = tempfile.mkdtemp(prefix="omdtabref_")
+        import subprocess
+        subprocess.check_call([oc.REF_DRIVER, out, "tabfile", os.path.join(TABLES, "eam.aluminum5000"), "tabname",
+                               sec, "rfile", rfile], cwd=out)
+        tab = np.loadtxt(os.path.join(out, "table.txt"))
+        np.savez_compressed(os.path.join(GOLD, "table_%s.npz" % sec.lower()), r=tab[:, 0], val=tab[:, 1],
+                            dval=tab[:, 2])
+        print("wrote table_%s" % sec.lower(), len(tab))
+    print("done")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+"""EAM on the GPU against the reference's own outputs (golden) and the FP64 oracle.
+
+Tolerance (FP32 forces from FP64 positions, Kahan sums): the norm-wise
+relative force error ||f - f_ref|| / ||f_ref|| <= 1e-5, every component
+within 1e-5 * max|f_ref| + 1e-6 eV/A, per-atom energy within 2e-6 eV and the
+total potential within 5e-8 relative (per-atom energies are FP32, whose
+rounding near 3.4 eV is 1.2e-7 eV).  Neighbour sets are compared exactly.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import TABLES, load_case, nbr_set
+
+pytestmark = pytest.mark.gpu
+
+FORCE_REL = 1e-5
+EAM_TABLE = os.path.join(TABLES, "eam.aluminum5000")
+
+
+def make_eam(omdg, d, rebuild_every=1):
+    from objectmd_gb300 import inputs
+
+    ctx = omdg.Context(0)
+    ctx.set_box(d["box_lo"], d["box_hi"], (True, True, True))
+    ctx.set_atoms(d["x0"], d["v0"], masses=[inputs.md_mass("aluminum")], znum=[13.0])
+    ctx.add_eam(EAM_TABLE)
+    ctx.set_neighbor(skin=0.3, rebuild_every=rebuild_every)
+    return ctx
+
+
+def check_forces(f, fref, pot=None, potref=None):
+    rel = np.linalg.norm(f - fref) / np.linalg.norm(fref)
+    assert rel <= FORCE_REL, rel
+    assert np.abs(f - fref).max() <= FORCE_REL * np.abs(fref).max() + 1e-6
+    if pot is not None:
+        assert np.abs(pot - potref).max() <= 2e-6
+        assert abs(pot.sum() - potref.sum()) <= 5e-8 * abs(potref.sum())
+
+
+@pytest.mark.parametrize("case", ["eam_al_500", "eam_al_4000"])
+def test_eam_static_matches_reference(omdg_lib, case):
+    d = load_case(case)
+    with make_eam(omdg_lib, d) as ctx:
+        ctx.compute_forces()
+        st = ctx.get_state()
+        check_forces(st["f"], d["f"], st["pot"], d["pot"])
+        assert np.abs(st["vir"] - d["vir"]).max() <= 1e-5 * np.abs(d["vir"]).max() + 1e-5
+        led = ctx.ledger()
+        assert abs(led["potential"] - float(d["summary_potential"][0])) <= 5e-8 * abs(led["potential"])
+
+
+@pytest.mark.parametrize("case", ["eam_al_500", "eam_al_4000"])
+def test_eam_neighbour_set_bit_exact(omdg_lib, case):
+    d = load_case(case)
+    with make_eam(omdg_lib, d) as ctx:
+        ctx.build_neighbors()
+        mine = nbr_set(*ctx.neighbors())
+    ref = set(map(tuple, d["nbr"].tolist()))
+    assert mine == ref
+
+
+def test_eam_large_vs_oracle(omdg_lib, oracle_lib):
+    """32,000 atoms: forces against the FP64 C oracle on the same input."""
+    from objectmd_gb300 import inputs
+
+    oc = oracle_lib
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=20, a=4.05, sigma=0.05, temp=300.0, seed_pos=31, seed_vel=32)
+    phi = oc.Table.from_file(EAM_TABLE, "PAIR")
+    ed = oc.Table.from_file(EAM_TABLE, "EDENS")
+    em = oc.Table.from_file(EAM_TABLE, "EMBED")
+    box = oc.make_box(lo, hi, (1, 1, 1))
+    nb = oc.neighbors(box, x, phi.max_range() + 0.3)
+    fref, eref, vref, rho = oc.eam(box, x, nb, phi, ed, em)
+    ctx = omdg_lib.Context(0)
+    ctx.set_box(lo, hi)
+    ctx.set_atoms(x, v, masses=[inputs.md_mass("aluminum")], znum=[13.0])
+    ctx.add_eam(EAM_TABLE)
+    ctx.set_neighbor(0.3, 1)
+    ctx.compute_forces()
+    st = ctx.get_state()
+    check_forces(st["f"], fref, st["pot"], eref)
+    mine = nbr_set(*ctx.neighbors())
+    ref = nbr_set(*nb)
+    assert mine == ref
+    ctx.close()
+
+
+def test_eam_nve_trajectory_matches_reference(omdg_lib):
+    """20 steps of velocity Verlet (dt 2 fs) with the reference's first-step rule."""
+    d = load_case("eam_al_nve")
+    with make_eam(omdg_lib, d, rebuild_every=1) as ctx:
+        ctx.set_timestep(float(d["dt"]))
+        ctx.set_first_step_mode(True)
+        ctx.step(int(d["steps"]))
+        st = ctx.get_state()
+        kin, pot = ctx.ledger_history()
+        led = ctx.ledger()
+    L = d["box_hi"] - d["box_lo"]
+    dx = st["x"] - d["x"]
+    dx -= np.round(dx / L) * L  # the reference wraps owners at every refresh
+    assert np.abs(dx).max() < 1e-6
+    assert np.abs(st["v"] - d["v"]).max() < 1e-4 * np.abs(d["v"]).max()
+    ref = d["ledger"]  # step kinetic potential energy
+    assert len(kin) == int(d["steps"])
+    np.testing.assert_allclose(kin, ref[1:1 + len(kin), 1], rtol=1e-6)
+    np.testing.assert_allclose(pot, ref[1:1 + len(pot), 2], rtol=5e-8)
+    assert abs(led["base_potential"] - float(d["summary_base_potential"][0])) < 5e-8 * abs(led["base_potential"])
+
+
+def test_eam_graph_and_eager_agree(omdg_lib):
+    """The captured step graph and the eager launch sequence give identical state."""
+    d = load_case("eam_al_nve")
+    out = []
+    for profiling in (False, True):
+        with make_eam(omdg_lib, d, rebuild_every=0) as ctx:
+            ctx.set_timestep(0.002)
+            ctx.set_profiling(profiling)
+            ctx.step(30)
+            out.append(ctx.get_state())
+    np.testing.assert_array_equal(out[0]["x"], out[1]["x"])
+    np.testing.assert_array_equal(out[0]["f"], out[1]["f"])

@@ -1,0 +1,433 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 force-evaluation path (atom-steps/s).
+
+Default workload (one GB300): EAM aluminium, FCC 40^3 cells = 256,000 atoms,
+a = 4.05 A, Gaussian displacements 0.05 A (seed 2), Maxwell-Boltzmann
+300 K (seed 3), 5000-knot tabulated EAM (tests/golden/tables/eam.aluminum5000,
+the reference eam.aluminum resampled), Verlet skin 0.3 A with a
+displacement-triggered rebuild, velocity Verlet dt = 2 fs.  One "step" is one
+RunKernel iteration: kick-drift, (rebuild when triggered), EAM density and
+force, kick, energy ledger.
+
+Timing: W untimed warm-up steps, then K steps each bracketed by CUDA events
+on the library's stream, with an L2 flush (a 512 MB write) enqueued before
+every step outside the events.  `value` = atoms * K / sum(step times).  `e2e`
+repeats the K steps through the public C ABI with pinned host buffers: every
+step uploads positions and velocities, steps, and reads positions,
+velocities, forces and the energy ledger back.
+
+--impl reference times the oracle's CPU restatement of the same path
+(oracle/omd_oracle.c, compiled on this host) on every host core: one process
+per core, each an independent EAM box of the same shape and density (the
+reference's MPI domain decomposition at ideal scaling), rebuilding its
+neighbour list every step as the reference does by default.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TABLE = os.path.join(ROOT, "tests", "golden", "tables", "eam.aluminum5000")
+METRIC = "atom-steps/s on 1 GB300, EAM/Tersoff vs NN surrogate at <=30 meV/A force RMSE"
+UNIT = "atom-steps/s"
+
+WORKLOADS = {
+    # name: (description, ncell, a, sigma, T, dt)
+    "eam_al_256k": ("EAM Al FCC 40^3 = 256,000 atoms, 5000-knot table, skin 0.3, dt 2 fs", 40, 4.05, 0.05, 300.0,
+                    0.002),
+    "eam_al_1m": ("EAM Al FCC 64^3 = 1,048,576 atoms, 5000-knot table, skin 0.3, dt 2 fs", 64, 4.05, 0.05, 300.0,
+                  0.002),
+    "eam_al_32k": ("EAM Al FCC 20^3 = 32,000 atoms, 5000-knot table, skin 0.3, dt 2 fs", 20, 4.05, 0.05, 300.0,
+                   0.002),
+}
+
+# Algorithmic bytes per atom for one launch of each kernel (neighbour list of
+# N_f int32 entries, FP32 packs/forces, FP64 x and v):
+#   eam_density  24 (own position) + 4 N_f (list) + 4 (F' write)
+#   eam_force    24 + 4 N_f + 4 (F'_i) + 12 (f) + 4 (energy)
+#   kick_drift   read x v f, write x v + 32 B position pack
+#   kick         read v f, write v
+ALG_BYTES = {
+    "eam_density": lambda nf: 24 + 4 * nf + 4,
+    "eam_force": lambda nf: 24 + 4 * nf + 4 + 12 + 4,
+    "kick_drift": lambda nf: 108 + 32,
+    "kick": lambda nf: 24 + 12 + 24,
+}
+STEP_ALG_BYTES = lambda nf: 2 * (24 + 4 * nf) + 24 + 108  # noqa: E731  (EAM two passes + velocity Verlet)
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            t = [x.strip() for x in line.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                smax.append(float(t[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if t[5 + k].lower() == "active":
+                    reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ inputs
+def make_workload(name, ncell=None):
+    from objectmd_gb300 import inputs
+
+    desc, nc, a, sigma, temp, dt = WORKLOADS[name]
+    if ncell:
+        nc = ncell
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=nc, a=a, sigma=sigma, temp=temp, seed_pos=2, seed_vel=3)
+    return desc, x, v, lo, hi, dt
+
+
+def make_context(x, v, lo, hi, dt, device=0, tune=True):
+    from objectmd_gb300 import inputs, omdg
+
+    ctx = omdg.Context(device)
+    ctx.set_box(lo, hi)
+    ctx.set_atoms(x, v, masses=[inputs.md_mass("aluminum")], znum=[13.0])
+    ctx.add_eam(TABLE)
+    ctx.set_neighbor(skin=0.3, rebuild_every=0)
+    ctx.set_timestep(dt)
+    ctx.set_first_step_mode(True)
+    if tune:
+        ctx.autotune(3)
+    return ctx
+
+
+def mean_neighbours(ctx):
+    off, j, c = ctx.neighbors()
+    return float(len(j)) / max(1, len(off) - 1)
+
+
+# ------------------------------------------------------------------ GB300 arm
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    device = local if torch.cuda.device_count() > local else 0
+    torch.cuda.set_device(device)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    desc, x, v, lo, hi, dt = make_workload(args.workload, args.ncell)
+    n = len(x)
+    ctx = make_context(x, v, lo, hi, dt, device=device, tune=not args.no_tune)
+    if args.eager:
+        ctx.set_profiling(True)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+    flush = torch.empty(args.flush_mb * (1 << 20) // 4, dtype=torch.float32, device="cuda")
+
+    # warm-up (FirstRun, graph capture, tuning effects)
+    ctx.step(max(3, args.warmup))
+    nf = mean_neighbours(ctx)
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    st0 = ctx.stats()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(device)
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            ctx.step_async(1)
+            ends[k].record(stream)
+    ctx.sync()
+    torch.cuda.synchronize()
+    t_wall1 = time.perf_counter()
+    clk = clocks.stop()
+    st1 = ctx.stats()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * n * args.steps / (total_ms * 1e-3)
+    launches = st1["launches"] - st0["launches"]
+    rebuilds = st1["rebuilds"] - st0["rebuilds"]
+    led = ctx.ledger()
+
+    # per-kernel CUDA-event times over the same number of steps (eager launch
+    # sequence of the same kernels, L2 flushed before every step)
+    ctx.set_profiling(True)
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            ctx.step_async(1)
+    ctx.sync()
+    kt = ctx.kernel_times()
+    ctx.set_profiling(args.eager)
+    kernels = {k: {"ms_per_launch": ms / max(1, c), "launches": c} for k, (ms, c) in kt.items()}
+    dom = max(((k, v_) for k, v_ in kernels.items() if k in ALG_BYTES),
+              key=lambda kv: kv[1]["ms_per_launch"] * kv[1]["launches"])
+    dom_name, dom_t = dom[0], dom[1]["ms_per_launch"]
+    peaks = load_peaks()
+    alg = ALG_BYTES[dom_name](nf) * n
+    achieved = alg / (dom_t * 1e-3) / 1e9
+    traffic = load_traffic(dom_name)
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peaks["hbm"],
+                "unit": "GB/s", "frac": round(achieved / peaks["hbm"], 4), "traffic": traffic,
+                "peak_source": peaks["src"], "alg_bytes_per_launch": int(alg)}
+    step_alg = STEP_ALG_BYTES(nf) * n
+    mean_step = total_ms / args.steps
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(ctx, n, args.steps, torch)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args)
+
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": mean_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 forces / fp64 integration",
+        "data": "synthetic (seeded FCC lattice, Gaussian displacements, Maxwell-Boltzmann velocities)",
+        "config": {"workload": desc, "atoms_per_gpu": n, "mean_neighbours": round(nf, 2),
+                   "neighbour_rebuilds_in_timed_steps": rebuilds, "l2": "flushed before every step (%d MB write)" %
+                   args.flush_mb, "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "launch_shapes": ctx.launch_shapes()},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": roofline,
+        "step_roofline": {"alg_bytes_per_step": int(step_alg), "achieved_GBps": round(step_alg / (mean_step * 1e-3)
+                                                                                     / 1e9, 1),
+                          "frac": round(step_alg / (mean_step * 1e-3) / 1e9 / peaks["hbm"], 4)},
+        "kernels": {k: round(v_["ms_per_launch"] * 1e3, 2) for k, v_ in kernels.items()},
+        "kernels_unit": "us per launch",
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "energy": {"kinetic": led["kinetic"], "potential": led["potential"], "energy": led["energy"]},
+        "wall_s_timed_loop": t_wall1 - t_wall0,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(ctx, n, steps, torch):
+    """Per step: pinned H2D of x and v, one step, D2H of x, v, f and the ledger."""
+    pin = lambda: torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+    x, v, f = pin(), pin(), pin()
+    ctx.get_state_into(x=x, v=v)
+    ctx.step(1)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        ctx.set_positions(x)
+        ctx.set_velocities(v)
+        ctx.step(1)
+        ctx.get_state_into(x=x, v=v, f=f)
+        ctx.ledger()
+    t1 = time.perf_counter()
+    return {"value": n * steps / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": 2 * 24 * n,
+            "d2h_bytes_per_step": 3 * 24 * n + 32}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return {"hbm": float(d["hbm_gbs"]), "src": "measured (MEASURED_PEAKS.json hbm_gbs)"}
+    except Exception:
+        return {"hbm": 6800.0, "src": "fallback 6.8 TB/s"}
+
+
+def load_traffic(kernel):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        return json.load(open(p)).get(kernel)
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ CPU baselines
+def _cpu_worker(args_tuple):
+    ncell, steps, warm = args_tuple
+    sys.path.insert(0, ROOT)
+    from objectmd_gb300 import inputs
+    from oracle import oracle as oc
+
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=ncell, a=4.05, sigma=0.05, temp=300.0, seed_pos=2, seed_vel=3)
+    n = len(x)
+    phi, ed, em = (oc.Table.from_file(TABLE, s) for s in ("PAIR", "EDENS", "EMBED"))
+    box = oc.make_box(lo, hi, (1, 1, 1))
+    mass = np.full(n, inputs.md_mass("aluminum"))
+    rv = phi.max_range() + 0.3
+    x = np.ascontiguousarray(x)
+    v = np.ascontiguousarray(v)
+    f = np.zeros((n, 3))
+
+    def one_step():
+        oc.vv_kick_drift(x, v, f, mass, 0.002)
+        xw = oc.wrap(box, x)
+        x[:] = xw
+        nb = oc.neighbors(box, x, rv)
+        fr, e, vir, rho = oc.eam(box, x, nb, phi, ed, em)
+        f[:] = fr
+        oc.vv_kick(v, f, mass, 0.002)
+        return e.sum()
+
+    for _ in range(warm):
+        one_step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one_step()
+    t1 = time.perf_counter()
+    return n, steps, t1 - t0
+
+
+def cpu_baseline(args):
+    """Single-core oracle port on a bounded sample of the workload."""
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1) as pool:
+        n, steps, sec = pool.map(_cpu_worker, [(16, args.cpu_steps, 1)])[0]
+    return {"value": n * steps / sec, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "EAM Al FCC 16^3 = %d atoms, %d steps (neighbour list rebuilt every step, as the reference's "
+                      "default comm.refresh), oracle/omd_oracle.c on one host core" % (n, steps)}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    desc, nc, a, sigma, temp, dt = WORKLOADS[args.workload]
+    if args.ncell:
+        nc = args.ncell
+    n_total = 4 * nc ** 3
+    # split the box into `cores` equal sub-boxes of the same density
+    per = max(1, n_total // cores)
+    sub = max(3, int(round((per / 4) ** (1.0 / 3.0))))
+    steps = max(1, min(args.steps, 5))
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(sub, steps, max(0, min(args.warmup, 1)))] * cores)
+    t1 = time.perf_counter()
+    atoms = sum(r[0] for r in res)
+    slowest = max(r[2] for r in res)
+    value = atoms * steps / slowest
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+           "warmup": args.warmup, "ms_per_step": slowest / steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+           "config": {"workload": desc, "atoms_total": atoms, "host_processes": cores,
+                      "per_process": "EAM Al FCC %d^3 = %d atoms" % (sub, 4 * sub ** 3)},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": "%d independent EAM boxes of %d atoms, %d steps each, neighbour list rebuilt "
+                                      "every step (oracle/omd_oracle.c, the reference's algorithm restated)" %
+                                      (cores, 4 * sub ** 3, steps)},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "wall_s": t1 - t0}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="eam_al_256k", choices=sorted(WORKLOADS))
+    ap.add_argument("--ncell", type=int, default=0)
+    ap.add_argument("--flush-mb", type=int, default=512)
+    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--eager", action="store_true",
+                    help="launch the step kernels one by one instead of replaying the captured graph "
+                         "(profilers cannot see kernels inside a graph with conditional nodes)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -127,6 +127,10 @@ int omdg_set_timestep(omdg_ctx* ctx, double dt);
  * zeroes the forces afterwards as the reference does.
  */
 int omdg_step(omdg_ctx* ctx, int nsteps);
+/* omdg_step without the final wait: enqueues nsteps on the context stream.
+   omdg_sync waits for them, checks the device status and updates the ledger. */
+int omdg_step_async(omdg_ctx* ctx, int nsteps);
+int omdg_sync(omdg_ctx* ctx);
 int omdg_set_first_step_mode(omdg_ctx* ctx, int reference_first_step);
 
 /*
@@ -143,6 +147,21 @@ int omdg_set_thermostat(omdg_ctx* ctx, double temperature, double tau);
 
 /* Number of neighbour-list builds so far and of kernel launches issued by the last omdg_step. */
 int omdg_stats(omdg_ctx* ctx, long* rebuilds, long* launches);
+
+/*
+ * Launch shapes (no reference counterpart: the reference is scalar C++).
+ * Keys: "eam_block", "eam_lanes" (threads per atom), "eam_stage" (spline
+ * knots in shared memory), "eam_ctas_per_sm", "pair_block", "pair_lanes",
+ * "tb_block", "tb_lanes", "nbr_hshift" (log2 of the neighbour slice height).
+ */
+int omdg_set_launch(omdg_ctx* ctx, const char* key, int value);
+int omdg_get_launch(omdg_ctx* ctx, const char* key, int* value);
+/*
+ * Times the force kernels of the current system under candidate launch
+ * shapes (CUDA events, best of `reps` force evaluations each) and keeps the
+ * fastest.  best_ms receives its time per force evaluation.
+ */
+int omdg_autotune(omdg_ctx* ctx, int reps, double* best_ms);
 
 /* Per-kernel CUDA-event timing of subsequent omdg_step calls (tracing). */
 int omdg_set_profiling(omdg_ctx* ctx, int on);

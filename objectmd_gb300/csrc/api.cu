@@ -209,6 +209,9 @@ int omdg_create(omdg_ctx** out, int device) {
     omdg_ctx* c = new omdg_ctx();
     c->device = device;
     cudaError_t e = cudaSetDevice(device);
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (sms > 0) c->num_sms = sms;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_flags, sizeof(int) * 4);
@@ -255,6 +258,7 @@ int omdg_destroy(omdg_ctx* c) {
         for (int k = 0; k < 3; k++) {
             cudaFree(p.d_coef[k]);
             cudaFree(p.d_coef64[k]);
+            if (k == 0) cudaFree(p.d_coef2);
         }
     for (auto e : c->event_pool) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
@@ -374,94 +378,31 @@ extern "C" {
 int omdg_get_state(omdg_ctx* c, double* x, double* v, double* f, double* pot, double* vir) {
     if (!c) return OMDG_EINVAL;
     if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
-    std::vector<int> id;
-    int rc = fetch_ids(c, id);
+    cudaSetDevice(c->device);
+    int rc = io_get_state(c, x, v, f, pot, vir);
     if (rc) return rc;
-    int n = c->n;
-    if (x) {
-        std::vector<double> a, b, d;
-        if ((rc = fetch(c, c->x, a, n)) || (rc = fetch(c, c->y, b, n)) || (rc = fetch(c, c->z, d, n))) return rc;
-        for (int k = 0; k < n; k++) {
-            x[3 * id[k]] = a[k];
-            x[3 * id[k] + 1] = b[k];
-            x[3 * id[k] + 2] = d[k];
-        }
-    }
-    if (v) {
-        std::vector<double> a, b, d;
-        if ((rc = fetch(c, c->vx, a, n)) || (rc = fetch(c, c->vy, b, n)) || (rc = fetch(c, c->vz, d, n))) return rc;
-        for (int k = 0; k < n; k++) {
-            v[3 * id[k]] = a[k];
-            v[3 * id[k] + 1] = b[k];
-            v[3 * id[k] + 2] = d[k];
-        }
-    }
-    if (f) {
-        if (c->use_f64) {
-            std::vector<double> a;
-            if ((rc = fetch(c, c->f64, a, (size_t)3 * n))) return rc;
-            for (int k = 0; k < n; k++)
-                for (int q = 0; q < 3; q++) f[3 * id[k] + q] = a[3 * k + q];
-        } else {
-            std::vector<float> a, b, d;
-            if ((rc = fetch(c, c->fx, a, n)) || (rc = fetch(c, c->fy, b, n)) || (rc = fetch(c, c->fz, d, n)))
-                return rc;
-            for (int k = 0; k < n; k++) {
-                f[3 * id[k]] = a[k];
-                f[3 * id[k] + 1] = b[k];
-                f[3 * id[k] + 2] = d[k];
-            }
-        }
-    }
-    if (pot) {
-        if (c->use_f64) {
-            std::vector<double> a;
-            if ((rc = fetch(c, c->f64, a, (size_t)4 * n))) return rc;
-            for (int k = 0; k < n; k++) pot[id[k]] = a[3 * (size_t)n + k];
-        } else {
-            std::vector<float> a;
-            if ((rc = fetch(c, c->pe, a, n))) return rc;
-            for (int k = 0; k < n; k++) pot[id[k]] = a[k];
-        }
-    }
-    if (vir) {
-        std::vector<float> a;
-        if ((rc = fetch(c, c->vir, a, n))) return rc;
-        for (int k = 0; k < n; k++) vir[id[k]] = a[k];
-    }
-    return OMDG_OK;
-}
-
-static int upload_caller_order(omdg_ctx* c, const double* src, double* dx, double* dy, double* dz) {
-    std::vector<int> id;
-    int rc = fetch_ids(c, id);
-    if (rc) return rc;
-    int n = c->n;
-    std::vector<double> a(n), b(n), d(n);
-    for (int k = 0; k < n; k++) {
-        a[k] = src[3 * id[k]];
-        b[k] = src[3 * id[k] + 1];
-        d[k] = src[3 * id[k] + 2];
-    }
-    cudaMemcpyAsync(dx, a.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(dy, b.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(dz, d.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
-    return check_cuda(c, cudaStreamSynchronize(c->stream), "upload");
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "state read-back");
 }
 
 int omdg_set_positions(omdg_ctx* c, const double* x) {
     if (!c || !x) return OMDG_EINVAL;
     if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
-    int rc = upload_caller_order(c, x, c->x, c->y, c->z);
+    cudaSetDevice(c->device);
+    int rc = io_set_state(c, x, nullptr);
     if (rc) return rc;
+    // positions moved by the caller: refresh the packs and request a rebuild
+    if ((rc = integrate_pack(c))) return rc;
     c->list_valid = false;
-    return integrate_pack(c);
+    return request_rebuild(c);
 }
 
 int omdg_set_velocities(omdg_ctx* c, const double* v) {
     if (!c || !v) return OMDG_EINVAL;
     if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
-    return upload_caller_order(c, v, c->vx, c->vy, c->vz);
+    cudaSetDevice(c->device);
+    int rc = io_set_state(c, nullptr, v);
+    if (rc) return rc;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "velocity upload");
 }
 
 }  // extern "C"
@@ -814,6 +755,7 @@ static int capture_step(Context* c, GraphState& gs) {
     if (!gs.side) cudaStreamCreateWithFlags(&gs.side, cudaStreamNonBlocking);
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return check_cuda(c, e, "capture begin");
+    long l0 = c->launches, l1 = 0, l2 = 0;
     int rc = integrate_kick_drift(c, 0);
     cudaGraph_t g = nullptr;
     cudaStreamCaptureStatus cst;
@@ -826,6 +768,7 @@ static int capture_step(Context* c, GraphState& gs) {
         if (e != cudaSuccess) rc = check_cuda(c, e, "conditional handle");
     }
     if (!rc) rc = launch_set_rebuild_cond(c, h);
+    l1 = c->launches;
     cudaGraphNode_t cond_node = nullptr;
     if (!rc) {
         e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &g, &deps, nullptr, &ndeps);
@@ -853,8 +796,15 @@ static int capture_step(Context* c, GraphState& gs) {
             }
         }
     }
+    l2 = c->launches;
     if (!rc) rc = forces_compute(c);
     if (!rc) rc = integrate_kick(c, 0);
+    long l3 = c->launches;
+    // captured launches are counted when the graph replays, not here
+    c->graph_step_kernels = (l1 - l0) + (l3 - l2);
+    c->graph_body_kernels = l2 - l1;
+    c->launches = l0;
+    c->captured_builds += 1;
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(s, &graph);
     if (rc) {
@@ -898,7 +848,7 @@ int omdg_get_neighbors(omdg_ctx* c, int* offsets, int* nbr_j, int* nbr_code, lon
     int rc = fetch_ids(c, id);
     if (rc) return rc;
     if ((rc = fetch(c, c->nnb, nn, n))) return rc;
-    if ((rc = fetch(c, reinterpret_cast<const unsigned*>(c->nbr), nb, (size_t)c->maxnb * n))) return rc;
+    if ((rc = fetch(c, reinterpret_cast<const unsigned*>(c->nbr), nb, nlist_slots(c, c->maxnb)))) return rc;
     // rows in caller order, each sorted by (j, code)
     std::vector<int> sorted_of(n);
     for (int k = 0; k < n; k++) sorted_of[id[k]] = k;
@@ -912,7 +862,7 @@ int omdg_get_neighbors(omdg_ctx* c, int* offsets, int* nbr_j, int* nbr_code, lon
         int k = sorted_of[i];
         row.clear();
         for (int s = 0; s < nn[k]; s++) {
-            unsigned e = nb[(size_t)s * n + k];
+            unsigned e = nb[nbr_at(k, s, c->nbr_hshift, c->maxnb)];
             row.push_back(std::make_pair(id[nbr_index(e)], omdg::nbr_code(e)));
         }
         std::sort(row.begin(), row.end());
@@ -933,6 +883,7 @@ int omdg_compute_forces(omdg_ctx* c) {
     cudaSetDevice(c->device);
     int rc;
     if (!c->list_valid && (rc = build_list(c))) return rc;
+    if (c->first_run_done && (rc = eager_maybe_rebuild(c))) return rc;
     if ((rc = threebody_prepare(c))) return rc;
     if ((rc = forces_compute(c))) return rc;
     if ((rc = measure_energies(c, 0))) return rc;
@@ -967,12 +918,11 @@ int omdg_set_thermostat(omdg_ctx* c, double temperature, double tau) {
     return OMDG_OK;
 }
 
-int omdg_step(omdg_ctx* c, int nsteps) {
+int omdg_step_async(omdg_ctx* c, int nsteps) {
     if (!c || nsteps < 0) return OMDG_EINVAL;
     if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
     cudaSetDevice(c->device);
     int rc;
-    long launches0 = c->launches;
     if (!c->first_run_done) {
         // FirstRun (system.cpp:860-873): one force evaluation, energies, base potential
         if ((rc = build_list(c))) return rc;
@@ -988,14 +938,14 @@ int omdg_step(omdg_ctx* c, int nsteps) {
         c->last_pot = row[1];
         c->last_vir = row[2];
         if (c->reference_first_step && (rc = zero_forces(c))) return rc;
+        if ((rc = step_state_reset(c, 1, c->rebuild_every))) return rc;
         c->first_run_done = true;
     }
-    if ((rc = step_state_reset(c, 1, c->rebuild_every))) return rc;
     if (!c->list_valid) {
         if ((rc = build_list(c))) return rc;
         if ((rc = threebody_prepare(c))) return rc;
     }
-    if (nsteps > c->ledger_cap) return set_error(c, OMDG_EINVAL, "too many steps for one call (ledger capacity)");
+    if (c->async_steps == 0) c->launches_at_sync = c->launches;
     if (c->profiling) {
         for (int k = 0; k < nsteps; k++) {
             if ((rc = integrate_kick_drift(c, k))) return rc;
@@ -1013,9 +963,18 @@ int omdg_step(omdg_ctx* c, int nsteps) {
             cudaError_t e = cudaGraphLaunch(gs.exec, c->stream);
             if (e != cudaSuccess) return check_cuda(c, e, "graph launch");
         }
+        c->graph_steps += nsteps;
     }
+    c->async_steps += nsteps;
+    return OMDG_OK;
+}
+
+int omdg_sync(omdg_ctx* c) {
+    if (!c) return OMDG_EINVAL;
+    cudaSetDevice(c->device);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return check_cuda(c, e, "step");
+    int rc;
     if ((rc = check_status(c))) {
         if (rc == OMDG_ESTATE) {
             // a neighbour row overflowed during the run: grow for the next call
@@ -1025,22 +984,40 @@ int omdg_step(omdg_ctx* c, int nsteps) {
             c->list_valid = false;
             invalidate_graph(c);
         }
+        c->async_steps = 0;
         return rc;
     }
+    if (c->async_steps == 0) return OMDG_OK;
     long long step;
     int rows;
     if ((rc = step_state_read(c, &step, &rows, nullptr))) return rc;
     c->step = step;
-    int nrow = std::min(rows, c->ledger_cap);
+    int cap = c->ledger_cap;
+    int nrow = std::min(rows, cap);
     if (nrow > 0) {
-        cudaMemcpy(c->h_ledger, c->d_ledger, sizeof(double) * 4 * nrow, cudaMemcpyDeviceToHost);
+        // the device ledger is a ring: rows older than `cap` steps were overwritten
+        std::vector<double> ring(4 * (size_t)cap);
+        cudaMemcpy(ring.data(), c->d_ledger, sizeof(double) * 4 * (size_t)std::min(rows, cap),
+                   cudaMemcpyDeviceToHost);
+        int first = rows > cap ? rows % cap : 0;
+        for (int k = 0; k < nrow; k++) {
+            int slot = (first + k) % cap;
+            for (int q = 0; q < 4; q++) c->h_ledger[4 * k + q] = ring[4 * slot + q];
+        }
         c->last_kin = c->h_ledger[4 * (nrow - 1)];
         c->last_pot = c->h_ledger[4 * (nrow - 1) + 1];
         c->last_vir = c->h_ledger[4 * (nrow - 1) + 2];
     }
     c->last_rows = nrow;
-    c->launches = c->launches - launches0;
-    return OMDG_OK;
+    c->last_launches = c->launches - c->launches_at_sync;
+    c->async_steps = 0;
+    return step_state_reset(c, 1, c->rebuild_every);
+}
+
+int omdg_step(omdg_ctx* c, int nsteps) {
+    int rc = omdg_step_async(c, nsteps);
+    if (rc) return rc;
+    return omdg_sync(c);
 }
 
 int omdg_ledger(omdg_ctx* c, double* kinetic, double* potential, double* base_potential, double* virial) {
@@ -1065,8 +1042,19 @@ int omdg_ledger_history(omdg_ctx* c, double* kinetic, double* potential, int cap
 
 int omdg_stats(omdg_ctx* c, long* rebuilds, long* launches) {
     if (!c) return OMDG_EINVAL;
-    if (rebuilds) *rebuilds = c->rebuilds;
-    if (launches) *launches = c->launches;
+    int graph_builds = 0;
+    if (c->first_run_done) {
+        int rc = step_state_graph_rebuilds(c, &graph_builds);
+        if (rc) return rc;
+    }
+    // builds issued eagerly plus those the step graph's conditional node took
+    // (capturing the graph issues one build that never ran)
+    GraphState& gs = g_graphs[c];
+    long eager = c->rebuilds - c->captured_builds;
+    if (rebuilds) *rebuilds = eager + graph_builds;
+    // kernels issued so far: eager launches plus graph replays
+    if (launches) *launches = c->launches + c->graph_steps * c->graph_step_kernels + graph_builds * c->graph_body_kernels;
+    (void)gs;
     return OMDG_OK;
 }
 
@@ -1093,6 +1081,171 @@ int omdg_kernel_times(omdg_ctx* c, char* name_buf, int name_cap, double* ms, lon
         name_buf[name_cap - 1] = 0;
     }
     *nkern = m;
+    return OMDG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- launch shapes
+namespace omdg {
+static int* launch_knob(Context* c, const std::string& k) {
+    if (k == "eam_block") return &c->eam_block;
+    if (k == "eam_lanes") return &c->eam_lanes;
+    if (k == "eam_stage") return &c->eam_stage;
+    if (k == "eam_ctas_per_sm") return &c->eam_ctas_per_sm;
+    if (k == "pair_block") return &c->pair_block;
+    if (k == "pair_lanes") return &c->pair_lanes;
+    if (k == "tb_block") return &c->tb_block;
+    if (k == "tb_lanes") return &c->tb_lanes;
+    if (k == "nbr_hshift") return &c->nbr_hshift;
+    return nullptr;
+}
+
+static bool valid_knob(const std::string& k, int v) {
+    auto pow2 = [](int x) { return x > 0 && (x & (x - 1)) == 0; };
+    if (k == "eam_lanes" || k == "pair_lanes" || k == "tb_lanes") return pow2(v) && v <= 32;
+    if (k == "eam_block" || k == "pair_block" || k == "tb_block") return v >= 32 && v <= 1024 && v % 32 == 0;
+    if (k == "nbr_hshift") return v >= 0 && v <= 5;
+    if (k == "eam_ctas_per_sm") return v >= 1 && v <= 32;
+    if (k == "eam_stage") return v == 0 || v == 1;
+    return false;
+}
+
+// Time one force evaluation (best of reps) with events on the context stream.
+static int time_forces(Context* c, int reps, double& best) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    best = 1e30;
+    int rc = forces_compute(c);  // warm
+    for (int r = 0; r < reps && !rc; r++) {
+        cudaEventRecord(a, c->stream);
+        rc = forces_compute(c);
+        cudaEventRecord(b, c->stream);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best) best = ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (!rc) rc = check_status(c);
+    return rc;
+}
+}  // namespace omdg
+
+extern "C" {
+
+int omdg_set_launch(omdg_ctx* c, const char* key, int value) {
+    if (!c || !key) return OMDG_EINVAL;
+    std::string k(key);
+    int* p = launch_knob(c, k);
+    if (!p) return set_error(c, OMDG_EINVAL, "unknown launch key " + k);
+    if (!valid_knob(k, value)) return set_error(c, OMDG_EINVAL, "invalid value for " + k);
+    if (*p == value) return OMDG_OK;
+    *p = value;
+    if (k == "nbr_hshift") {
+        // the list layout changes: reallocate and rebuild before the next use
+        int m = c->maxnb;
+        c->maxnb = 0;
+        cudaFree(c->nbr);
+        cudaFree(c->rev);
+        cudaFree(c->slot_buf);
+        c->nbr = nullptr;
+        c->rev = nullptr;
+        c->slot_buf = nullptr;
+        if (m > 0) {
+            int rc = nlist_reserve(c, m);
+            if (rc) return rc;
+        }
+        c->list_valid = false;
+    }
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_get_launch(omdg_ctx* c, const char* key, int* value) {
+    if (!c || !key || !value) return OMDG_EINVAL;
+    int* p = launch_knob(c, key);
+    if (!p) return set_error(c, OMDG_EINVAL, std::string("unknown launch key ") + key);
+    *value = *p;
+    return OMDG_OK;
+}
+
+int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
+    if (!c || reps < 1) return OMDG_EINVAL;
+    if (c->n == 0 || c->pots.empty()) return set_error(c, OMDG_ESTATE, "autotune needs atoms and force kernels");
+    cudaSetDevice(c->device);
+    bool eam = false, pair = false, tb = false;
+    for (auto& p : c->pots) {
+        eam |= p.kind == POT_EAM;
+        pair |= (p.kind == POT_PAIR && !p.fp64) || p.kind == POT_ZBL;
+        tb |= p.kind == POT_SW || p.kind == POT_TERSOFF;
+    }
+    struct Cand {
+        int lanes, block, stage;
+    };
+    std::vector<Cand> cands;
+    if (eam) {
+        for (int lanes : {4, 8, 16})
+            for (int block : {256, 512})
+                for (int stage : {0, 1}) cands.push_back(Cand{lanes, block, stage});
+    } else if (pair) {
+        for (int lanes : {2, 4, 8, 16})
+            for (int block : {128, 256}) cands.push_back(Cand{lanes, block, 0});
+    } else if (tb) {
+        for (int lanes : {1, 2, 4})
+            for (int block : {64, 128, 256}) cands.push_back(Cand{lanes, block, 0});
+    } else {
+        return set_error(c, OMDG_ESTATE, "nothing to tune");
+    }
+    double best = 1e30;
+    Cand win = cands[0];
+    int rc = OMDG_OK;
+    for (auto& cd : cands) {
+        int hs = 0;
+        while ((1 << hs) * cd.lanes < 32 && hs < 5) hs++;
+        if (eam) {
+            c->eam_lanes = cd.lanes;
+            c->eam_block = cd.block;
+            c->eam_stage = cd.stage;
+            c->eam_ctas_per_sm = cd.block >= 512 ? 2 : 4;
+        } else if (pair) {
+            c->pair_lanes = cd.lanes;
+            c->pair_block = cd.block;
+        } else {
+            c->tb_lanes = cd.lanes;
+            c->tb_block = cd.block;
+        }
+        if ((rc = omdg_set_launch(c, "nbr_hshift", hs))) return rc;
+        if (!c->list_valid && (rc = build_list(c))) return rc;
+        if ((rc = threebody_prepare(c))) return rc;
+        double t;
+        if ((rc = time_forces(c, reps, t))) return rc;
+        if (t < best) {
+            best = t;
+            win = cd;
+        }
+    }
+    int hs = 0;
+    while ((1 << hs) * win.lanes < 32 && hs < 5) hs++;
+    if (eam) {
+        c->eam_lanes = win.lanes;
+        c->eam_block = win.block;
+        c->eam_stage = win.stage;
+        c->eam_ctas_per_sm = win.block >= 512 ? 2 : 4;
+    } else if (pair) {
+        c->pair_lanes = win.lanes;
+        c->pair_block = win.block;
+    } else {
+        c->tb_lanes = win.lanes;
+        c->tb_block = win.block;
+    }
+    if ((rc = omdg_set_launch(c, "nbr_hshift", hs))) return rc;
+    if (!c->list_valid && (rc = build_list(c))) return rc;
+    if ((rc = threebody_prepare(c))) return rc;
+    invalidate_graph(c);
+    if (best_ms) *best_ms = best;
     return OMDG_OK;
 }
 

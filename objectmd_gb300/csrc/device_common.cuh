@@ -23,6 +23,13 @@ __host__ __device__ __forceinline__ int nbr_code(unsigned e) {
     return (nbr_sx(e) + 1) + 3 * (nbr_sy(e) + 1) + 9 * (nbr_sz(e) + 1);
 }
 
+// Sliced-ELL neighbour layout: atoms are grouped in slices of H = 2^hshift
+// consecutive (cell-sorted) atoms and a slice stores its rows slot-major, so
+// a warp that covers 32/H slots of H atoms reads one contiguous 128-byte line.
+__host__ __device__ __forceinline__ size_t nbr_at(int i, int s, int hshift, int maxnb) {
+    return ((((size_t)(i >> hshift)) * (size_t)maxnb + (size_t)s) << hshift) + (size_t)(i & ((1 << hshift) - 1));
+}
+
 // Periodic lengths split into float hi + lo parts.
 struct ShiftF {
     float hx, hy, hz, lx, ly, lz;

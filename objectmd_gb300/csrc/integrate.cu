@@ -20,7 +20,7 @@ struct StepState {
     int rebuild;         // rebuild request for the next list build
     double lambda;       // velocity factor to apply before the next kick
     int rebuild_every;   // >0: rebuild when step % rebuild_every == 0
-    int pad;
+    int nrebuild;        // list builds taken by the graph's conditional node
 };
 
 struct IntParams {
@@ -179,18 +179,17 @@ __global__ void k_finalize(FinParams p, const double* __restrict__ partial, doub
     if (threadIdx.x == 0) {
         double kinetic = 0.5 * sk[0];
         int row = st->row;
-        if (row < p.ledger_cap) {
-            ledger[4 * row + 0] = kinetic;
-            ledger[4 * row + 1] = se[0];
-            ledger[4 * row + 2] = 0.5 * sw[0];
-        }
+        int slot = row % p.ledger_cap;  // ring buffer between host reads
+        ledger[4 * slot + 0] = kinetic;
+        ledger[4 * slot + 1] = se[0];
+        ledger[4 * slot + 2] = 0.5 * sw[0];
         double lam = 1.0;
         if (p.count_step && p.tau > 0.0 && st->step != 0) {
             // TempController::PostIntegration: T from the system kinetic energy
             double T = p.temp_factor * kinetic / (double)p.natoms;
             if (T > 0.0) lam = sqrt(1. + p.dt / p.tau * (p.tset / T - 1.));
         }
-        if (row < p.ledger_cap) ledger[4 * row + 3] = lam;
+        ledger[4 * slot + 3] = lam;
         st->lambda = lam;
         if (p.count_step) {
             st->step += 1;
@@ -269,6 +268,15 @@ int step_state_reset(Context* c, int reset_row, int rebuild_every) {
     return check_cuda(c, e, "step state");
 }
 
+int step_state_graph_rebuilds(Context* c, int* nrebuild) {
+    StepState h;
+    cudaError_t e = cudaMemcpyAsync(&h, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "step state");
+    *nrebuild = h.nrebuild;
+    return OMDG_OK;
+}
+
 int step_state_read(Context* c, long long* step, int* row, int* rebuild) {
     StepState h;
     cudaError_t e = cudaMemcpyAsync(&h, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);
@@ -287,13 +295,33 @@ int step_state_init(Context* c) {
     h.rebuild = 0;
     h.lambda = 1.0;
     h.rebuild_every = c->rebuild_every;
-    h.pad = 0;
+    h.nrebuild = 0;
     cudaError_t e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return check_cuda(c, e, "step state");
 }
 
 __global__ void k_clear_rebuild(StepState* st) { st->rebuild = 0; }
+
+// Flags a rebuild when positions written by the caller moved an atom more
+// than skin/2 from where the list was built.
+__global__ void k_check_disp(IntParams p, const PosPack* __restrict__ pack, const float4* __restrict__ xref,
+                             StepState* st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    PosPack pk = pack[i];
+    float4 r0 = xref[i];
+    float dx = (pk.hi.x - r0.x) + pk.lo.x, dy = (pk.hi.y - r0.y) + pk.lo.y, dz = (pk.hi.z - r0.z) + pk.lo.z;
+    if (dx * dx + dy * dy + dz * dz > p.half_skin2) st->rebuild = 1;
+}
+
+int request_rebuild(Context* c) {
+    IntParams p = int_params(c);
+    k_check_disp<<<grid_for(c->n, 256), 256, 0, c->stream>>>(p, c->pack, c->xref,
+                                                             reinterpret_cast<StepState*>(c->d_state));
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "displacement check");
+}
 
 int step_clear_rebuild(Context* c) {
     k_clear_rebuild<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state));
@@ -305,6 +333,7 @@ int step_clear_rebuild(Context* c) {
 // handle and clears it.
 __global__ void k_set_rebuild_cond(StepState* st, cudaGraphConditionalHandle h) {
     cudaGraphSetConditional(h, st->rebuild ? 1u : 0u);
+    if (st->rebuild) st->nrebuild += 1;
     st->rebuild = 0;
 }
 

@@ -206,7 +206,7 @@ __global__ void k_pack(int n, const double* __restrict__ x, const double* __rest
 }
 
 struct BuildParams {
-    int n, maxnb;
+    int n, maxnb, hshift;
     int nc[3];
     int periodic[3];
     ShiftF L;
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const PosPack* __r
                     }
                     if (!in) continue;
                     if (r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
-                    if (cnt < p.maxnb) nbr[(size_t)cnt * p.n + i] = code | (unsigned)k;
+                    if (cnt < p.maxnb) nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
                     cnt++;
                 }
             }
@@ -313,24 +313,24 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const PosPack* __r
     nnb[i] = cnt;
 }
 
-// rev[s*n+i]: the slot of (i, -s) in row j = nbr[s*n+i].
-__global__ void k_reverse(int n, const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
-                          int* __restrict__ rev, unsigned* status) {
+// rev at (i, s): the slot of (i, -image) in the row of j = nbr at (i, s).
+__global__ void k_reverse(int n, int hshift, int maxnb, const unsigned* __restrict__ nbr,
+                          const int* __restrict__ nnb, int* __restrict__ rev, unsigned* status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int m = nnb[i];
     for (int s = 0; s < m; s++) {
-        unsigned e = nbr[(size_t)s * n + i];
+        unsigned e = nbr[nbr_at(i, s, hshift, maxnb)];
         int j = nbr_index(e);
         unsigned want = nbr_encode(i, -nbr_sx(e), -nbr_sy(e), -nbr_sz(e));
         int mj = nnb[j], found = -1;
         for (int t = 0; t < mj; t++)
-            if (nbr[(size_t)t * n + j] == want) {
+            if (nbr[nbr_at(j, t, hshift, maxnb)] == want) {
                 found = t;
                 break;
             }
         if (found < 0) atomicOr(status, ERR_NBR_OVERFLOW);
-        rev[(size_t)s * n + i] = found < 0 ? 0 : found;
+        rev[nbr_at(i, s, hshift, maxnb)] = found < 0 ? 0 : found;
     }
 }
 
@@ -359,8 +359,14 @@ void nlist_prepare_geometry(Context* c) {
     }
 }
 
+size_t nlist_slots(const Context* c, int maxnb) {
+    size_t H = (size_t)1 << c->nbr_hshift;
+    size_t slices = ((size_t)c->cap + H - 1) / H;
+    return slices * H * (size_t)maxnb;
+}
+
 int nlist_reserve(Context* c, int maxnb) {
-    size_t need = (size_t)maxnb * (size_t)c->cap * sizeof(unsigned);
+    size_t need = nlist_slots(c, maxnb) * sizeof(unsigned);
     if (maxnb <= c->maxnb && c->nbr) return OMDG_OK;
     cudaFree(c->nbr);
     cudaFree(c->rev);
@@ -371,7 +377,7 @@ int nlist_reserve(Context* c, int maxnb) {
     if (cudaMalloc(&c->nbr, need) != cudaSuccess) return set_error(c, OMDG_ENOMEM, "neighbour list allocation");
     if (c->need_rev) {
         if (cudaMalloc(&c->rev, need) != cudaSuccess) return set_error(c, OMDG_ENOMEM, "reverse slot allocation");
-        if (cudaMalloc(&c->slot_buf, (size_t)maxnb * c->cap * sizeof(float4)) != cudaSuccess)
+        if (cudaMalloc(&c->slot_buf, nlist_slots(c, maxnb) * sizeof(float4)) != cudaSuccess)
             return set_error(c, OMDG_ENOMEM, "slot buffer allocation");
     }
     c->maxnb = maxnb;
@@ -445,6 +451,7 @@ int nlist_build(Context* c) {
     BuildParams bp;
     bp.n = n;
     bp.maxnb = c->maxnb;
+    bp.hshift = c->nbr_hshift;
     for (int d = 0; d < 3; d++) {
         bp.nc[d] = g.nc[d];
         bp.periodic[d] = g.periodic[d];
@@ -463,7 +470,8 @@ int nlist_build(Context* c) {
     prof_end(c);
     if (c->need_rev) {
         prof_begin(c, "nlist_reverse");
-        k_reverse<<<grid_for(n, 128), 128, 0, s>>>(n, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->rev,
+        k_reverse<<<grid_for(n, 128), 128, 0, s>>>(n, c->nbr_hshift, c->maxnb,
+                                                   reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->rev,
                                                    c->d_status);
         c->launches++;
         prof_end(c);

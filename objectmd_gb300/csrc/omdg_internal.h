@@ -115,6 +115,7 @@ struct Potential {
     double rc = 0;         // CutRadius as the reference sets it
     // device copies
     float4* d_coef[3] = {nullptr, nullptr, nullptr};
+    float4* d_coef2 = nullptr;  // EAM: PAIR and EDENS knots interleaved
     double4_32a* d_coef64[3] = {nullptr, nullptr, nullptr};
     DevTable dt[3]{};
 };
@@ -163,6 +164,14 @@ struct Context {
     double* f64 = nullptr;       // FP64 forces (3n) + FP64 per-atom energy (n), FP64 kernels only
     bool use_f64 = false;
     double* d_mass = nullptr;    // mass per type (device)
+    double* d_io = nullptr;      // caller-order transfer staging
+    size_t io_cap = 0;
+    long async_steps = 0;        // steps enqueued since the last omdg_sync
+    long launches_at_sync = 0, last_launches = 0;
+    long graph_steps = 0;        // graph replays issued
+    long graph_step_kernels = 0; // kernels per replay (outside the rebuild body)
+    long graph_body_kernels = 0; // kernels in the rebuild body
+    long captured_builds = 0;    // list builds issued while capturing (never ran)
     void* d_state = nullptr;     // StepState (integrate.cu)
 
     // neighbour list: nbr[s*n + i] = j | code << 26, count in nnb[i]
@@ -179,11 +188,18 @@ struct Context {
     long rebuilds = 0;
     int steps_since_build = 0;
 
-    // launch shapes chosen by the tuner (omdg_tune)
-    int eam_block = 128;
-    int eam_stage = 0;     // 1: stage spline knots in shared memory
-    int pair_block = 128;
-    int tb_block = 128;    // three-body kernels
+    // launch shapes (defaults; the tuner may change them)
+    int num_sms = 152;
+    int nbr_hshift = 2;        // sliced-ELL slice height H = 2^hshift
+    int eam_block = 256;
+    int eam_lanes = 8;         // threads per atom
+    int eam_stage = 1;         // 1: stage spline knots in shared memory
+    double eam_stage_frac = 0.35;
+    int eam_ctas_per_sm = 1;
+    int pair_block = 256;
+    int pair_lanes = 8;
+    int tb_block = 128;        // three-body kernels
+    int tb_lanes = 1;
 
     // potentials
     std::vector<Potential> pots;
@@ -230,6 +246,7 @@ void prof_collect(Context* c);
 int nlist_build(Context* c);
 void nlist_prepare_geometry(Context* c);
 int nlist_reserve(Context* c, int maxnb);
+size_t nlist_slots(const Context* c, int maxnb);
 
 // forces (eam.cu, pair.cu, threebody.cu)
 int forces_compute(Context* c);
@@ -245,6 +262,12 @@ int integrate_kick(Context* c, int step_index);
 int integrate_pack(Context* c);
 int measure_energies(Context* c, int row);
 int zero_forces(Context* c);
+int request_rebuild(Context* c);
+int step_state_graph_rebuilds(Context* c, int* nrebuild);
+
+// caller-order transfers (io.cu); asynchronous on the context stream
+int io_get_state(Context* c, double* x, double* v, double* f, double* pot, double* vir);
+int io_set_state(Context* c, const double* x, const double* v);
 
 // grid sizing
 inline int grid_for(int n, int block) { return (n + block - 1) / block; }

@@ -1,6 +1,7 @@
 // Tabulated pair potential (TForcePair, tpair.h:38-71): fr = -phi'(r)/r for
 // r < rc (strict), ReturnForce on the owner side (forcekernel.h:92-110).
-// Two precisions: FP32 on the mixed-precision relative vector, and an FP64
+// Two precisions: FP32 on the mixed-precision relative vector (LANES threads
+// per atom, Kahan partials combined by a TwoSum shuffle tree), and an FP64
 // path (positions, table and accumulation in FP64) for the plain FP64
 // Lennard-Jones configuration.
 #include "device_common.cuh"
@@ -9,6 +10,7 @@ namespace omdg {
 
 struct PairParams {
     int n;
+    int hshift, maxnb;
     ShiftF L;
     double L64[3];
     DevTable phi;
@@ -22,51 +24,82 @@ __device__ __forceinline__ bool types_match(int a, int b, int ta, int tb) {
     return (a == ta && b == tb) || (a == tb && b == ta);
 }
 
-__global__ void __launch_bounds__(256) k_pair32(PairParams p, const PosPack* __restrict__ pack,
+template <int LANES>
+__device__ __forceinline__ void lanes_twosum(float& s, float& c) {
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) {
+        float s2 = __shfl_xor_sync(0xffffffffu, s, off);
+        float c2 = __shfl_xor_sync(0xffffffffu, c, off);
+        float t = __fadd_rn(s, s2);
+        float bp = __fsub_rn(t, s);
+        float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(s2, bp));
+        c = __fsub_rn(__fadd_rn(c, c2), e);
+        s = t;
+    }
+}
+
+template <int LANES>
+__global__ void __launch_bounds__(512) k_pair32(PairParams p, const PosPack* __restrict__ pack,
                                                 const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                 float* __restrict__ fx, float* __restrict__ fy,
                                                 float* __restrict__ fz, float* __restrict__ pe,
                                                 float* __restrict__ vir, unsigned* status) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    PosPack pi = pack[i];
-    int ti = pack_type(pi.hi);
-    Kahan ax, ay, az, ae, av;
-    bool any = p.all_types || ti == p.ta || ti == p.tb;
-    int m = any ? nnb[i] : 0;
-    for (int s = 0; s < m; s++) {
-        unsigned e = __ldg(&nbr[(size_t)s * p.n + i]);
-        int j = nbr_index(e);
-        const float4* pj = reinterpret_cast<const float4*>(pack + j);
-        float4 hj = __ldg(pj), lj = __ldg(pj + 1);
-        if (!p.all_types && !types_match(ti, pack_type(hj), p.ta, p.tb)) continue;
-        float3 d = pair_delta(pi.hi, pi.lo, hj, lj, e, p.L);
-        float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-        if (r2 >= p.rc2) continue;
-        float rinv = rsqrtf(r2);
-        float r = r2 * rinv;
-        if (!(r < p.rc)) continue;
-        float ph, dph;
-        tab_read(p.phi, p.phi.coef, r, rinv, ph, dph, status);
-        float fr = -dph * rinv;
-        ax.add(d.x * fr);
-        ay.add(d.y * fr);
-        az.add(d.z * fr);
-        ae.add(0.5f * ph);
-        av.add(fr * r2);
-    }
-    if (p.first) {
-        fx[i] = ax.value();
-        fy[i] = ay.value();
-        fz[i] = az.value();
-        pe[i] = ae.value();
-        vir[i] = av.value();
-    } else if (m) {
-        fx[i] += ax.value();
-        fy[i] += ay.value();
-        fz[i] += az.value();
-        pe[i] += ae.value();
-        vir[i] += av.value();
+    const int lane = threadIdx.x & (LANES - 1);
+    const int per_block = blockDim.x / LANES;
+    for (int base = blockIdx.x * per_block; base < p.n; base += gridDim.x * per_block) {
+        int i = base + threadIdx.x / LANES;
+        bool valid = i < p.n;
+        int ii = valid ? i : p.n - 1;
+        PosPack pi = pack[ii];
+        int ti = pack_type(pi.hi);
+        bool any = valid && (p.all_types || ti == p.ta || ti == p.tb);
+        int m = any ? nnb[ii] : 0;
+        Kahan ax, ay, az, ae;
+        float av = 0.f;
+        for (int s = lane; s < m; s += LANES) {
+            unsigned e = __ldg(&nbr[nbr_at(ii, s, p.hshift, p.maxnb)]);
+            int j = nbr_index(e);
+            const float4* pj = reinterpret_cast<const float4*>(pack + j);
+            float4 hj = __ldg(pj), lj = __ldg(pj + 1);
+            if (!p.all_types && !types_match(ti, pack_type(hj), p.ta, p.tb)) continue;
+            float3 d = pair_delta(pi.hi, pi.lo, hj, lj, e, p.L);
+            float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+            if (r2 >= p.rc2) continue;
+            float rinv = rsqrtf(r2);
+            float r = r2 * rinv;
+            if (!(r < p.rc)) continue;
+            float ph, dph;
+            tab_read(p.phi, p.phi.coef, r, rinv, ph, dph, status);
+            float fr = -dph * rinv;
+            ax.add(d.x * fr);
+            ay.add(d.y * fr);
+            az.add(d.z * fr);
+            ae.add(0.5f * ph);
+            av = fmaf(fr, r2, av);
+        }
+        lanes_twosum<LANES>(ax.s, ax.c);
+        lanes_twosum<LANES>(ay.s, ay.c);
+        lanes_twosum<LANES>(az.s, az.c);
+        lanes_twosum<LANES>(ae.s, ae.c);
+#pragma unroll
+        for (int off = LANES / 2; off > 0; off >>= 1) av += __shfl_xor_sync(0xffffffffu, av, off);
+        if (lane == 0 && valid) {
+            float vfx = __fsub_rn(ax.s, ax.c), vfy = __fsub_rn(ay.s, ay.c), vfz = __fsub_rn(az.s, az.c);
+            float ve = __fsub_rn(ae.s, ae.c);
+            if (p.first) {
+                fx[i] = vfx;
+                fy[i] = vfy;
+                fz[i] = vfz;
+                pe[i] = ve;
+                vir[i] = av;
+            } else if (m) {
+                fx[i] += vfx;
+                fy[i] += vfy;
+                fz[i] += vfz;
+                pe[i] += ve;
+                vir[i] += av;
+            }
+        }
     }
 }
 
@@ -84,7 +117,7 @@ __global__ void __launch_bounds__(256) k_pair64(PairParams p, const double* __re
     bool any = p.all_types || ti == p.ta || ti == p.tb;
     int m = any ? nnb[i] : 0;
     for (int s = 0; s < m; s++) {
-        unsigned e = __ldg(&nbr[(size_t)s * p.n + i]);
+        unsigned e = __ldg(&nbr[nbr_at(i, s, p.hshift, p.maxnb)]);
         int j = nbr_index(e);
         if (!p.all_types && !types_match(ti, type[j], p.ta, p.tb)) continue;
         int sx = nbr_sx(e), sy = nbr_sy(e), sz = nbr_sz(e);
@@ -110,20 +143,30 @@ __global__ void __launch_bounds__(256) k_pair64(PairParams p, const double* __re
         f64[3 * (size_t)i + 2] = az;
         pe[i] = (float)ae;
         vir[i] = (float)av;
+        f64[3 * (size_t)p.n + i] = ae;
     } else if (m) {
         f64[3 * (size_t)i + 0] += ax;
         f64[3 * (size_t)i + 1] += ay;
         f64[3 * (size_t)i + 2] += az;
         pe[i] += (float)ae;
         vir[i] += (float)av;
+        f64[3 * (size_t)p.n + i] += ae;
     }
-    // FP64 potential energy per atom for the ledger
-    f64[3 * (size_t)p.n + i] = p.first ? ae : f64[3 * (size_t)p.n + i] + ae;
+}
+
+template <int LANES>
+static void launch32(Context* c, const PairParams& p, int block) {
+    int per_block = block / LANES;
+    k_pair32<LANES><<<grid_for(c->n, per_block), block, 0, c->stream>>>(
+        p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->fx, c->fy, c->fz, c->pe, c->vir,
+        c->d_status);
 }
 
 int pair_launch(Context* c, Potential& pot, bool first) {
     PairParams p;
     p.n = c->n;
+    p.hshift = c->nbr_hshift;
+    p.maxnb = c->maxnb;
     p.L = make_shift(c->box);
     for (int d = 0; d < 3; d++) p.L64[d] = c->box.L[d];
     p.phi = pot.dt[0];
@@ -137,14 +180,19 @@ int pair_launch(Context* c, Potential& pot, bool first) {
     int block = c->pair_block;
     if (pot.fp64) {
         prof_begin(c, "pair64");
-        k_pair64<<<grid_for(c->n, block), block, 0, c->stream>>>(p, c->x, c->y, c->z, c->type,
-                                                                  reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
-                                                                  c->f64, c->pe, c->vir, c->d_status);
+        k_pair64<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->x, c->y, c->z, c->type,
+                                                              reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
+                                                              c->f64, c->pe, c->vir, c->d_status);
     } else {
         prof_begin(c, "pair32");
-        k_pair32<<<grid_for(c->n, block), block, 0, c->stream>>>(p, c->pack,
-                                                                  reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
-                                                                  c->fx, c->fy, c->fz, c->pe, c->vir, c->d_status);
+        switch (c->pair_lanes) {
+            case 1: launch32<1>(c, p, block); break;
+            case 2: launch32<2>(c, p, block); break;
+            case 4: launch32<4>(c, p, block); break;
+            case 8: launch32<8>(c, p, block); break;
+            case 16: launch32<16>(c, p, block); break;
+            default: launch32<32>(c, p, block); break;
+        }
     }
     prof_end(c);
     c->launches++;

@@ -53,11 +53,16 @@ SIGNATURES = {
     "omdg_compute_forces": [_vp],
     "omdg_set_timestep": [_vp, _d],
     "omdg_step": [_vp, _i],
+    "omdg_step_async": [_vp, _i],
+    "omdg_sync": [_vp],
     "omdg_set_first_step_mode": [_vp, _i],
     "omdg_ledger": [_vp, _P(_d), _P(_d), _P(_d), _P(_d)],
     "omdg_ledger_history": [_vp, _P(_d), _P(_d), _i, _P(_i)],
     "omdg_set_thermostat": [_vp, _d, _d],
     "omdg_stats": [_vp, _P(_l), _P(_l)],
+    "omdg_set_launch": [_vp, _cp, _i],
+    "omdg_get_launch": [_vp, _cp, _P(_i)],
+    "omdg_autotune": [_vp, _i, _P(_d)],
     "omdg_set_profiling": [_vp, _i],
     "omdg_kernel_times": [_vp, _cp, _i, _P(_d), _P(_l), _i, _P(_i)],
 }
@@ -217,6 +222,16 @@ class Context:
     def step(self, nsteps=1):
         self._check(self.lib.omdg_step(self.h, int(nsteps)))
 
+    def step_async(self, nsteps=1):
+        self._check(self.lib.omdg_step_async(self.h, int(nsteps)))
+
+    def sync(self):
+        self._check(self.lib.omdg_sync(self.h))
+
+    def get_state_into(self, x=None, v=None, f=None, pot=None, vir=None):
+        """Read state into caller-provided float64 arrays (e.g. pinned buffers)."""
+        self._check(self.lib.omdg_get_state(self.h, _dp(x), _dp(v), _dp(f), _dp(pot), _dp(vir)))
+
     def ledger(self):
         k, p, b, w = _d(), _d(), _d(), _d()
         self._check(self.lib.omdg_ledger(self.h, ctypes.byref(k), ctypes.byref(p), ctypes.byref(b), ctypes.byref(w)))
@@ -239,6 +254,24 @@ class Context:
         s = _vp()
         self._check(self.lib.omdg_get_stream(self.h, ctypes.byref(s)))
         return s.value
+
+    def set_launch(self, key, value):
+        self._check(self.lib.omdg_set_launch(self.h, key.encode(), int(value)))
+
+    def get_launch(self, key):
+        v = _i()
+        self._check(self.lib.omdg_get_launch(self.h, key.encode(), ctypes.byref(v)))
+        return v.value
+
+    def launch_shapes(self):
+        keys = ("eam_block", "eam_lanes", "eam_stage", "eam_ctas_per_sm", "pair_block", "pair_lanes", "tb_block",
+                "tb_lanes", "nbr_hshift")
+        return {k: self.get_launch(k) for k in keys}
+
+    def autotune(self, reps=3):
+        ms = _d()
+        self._check(self.lib.omdg_autotune(self.h, int(reps), ctypes.byref(ms)))
+        return ms.value
 
     def set_profiling(self, on=True):
         self._check(self.lib.omdg_set_profiling(self.h, 1 if on else 0))

@@ -21,7 +21,8 @@ NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC", "-Xptxas",
            "-warn-spills"] + ARCH
-SOURCES = ["api.cu", "nlist.cu", "eam.cu", "pair.cu", "threebody.cu", "integrate.cu", "io.cu", "table.cpp"]
+SOURCES = ["api.cu", "nlist.cu", "eam.cu", "eam_fast.cu", "pair.cu", "threebody.cu", "integrate.cu", "io.cu",
+           "table.cpp"]
 
 
 def _newer(target, deps):

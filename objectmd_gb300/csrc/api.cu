@@ -1098,6 +1098,7 @@ static int* launch_knob(Context* c, const std::string& k) {
     if (k == "tb_block") return &c->tb_block;
     if (k == "tb_lanes") return &c->tb_lanes;
     if (k == "nbr_hshift") return &c->nbr_hshift;
+    if (k == "build_lanes") return &c->build_lanes;
     return nullptr;
 }
 
@@ -1108,6 +1109,7 @@ static bool valid_knob(const std::string& k, int v) {
     if (k == "nbr_hshift") return v >= 0 && v <= 5;
     if (k == "eam_ctas_per_sm") return v >= 1 && v <= 32;
     if (k == "eam_stage") return v == 0 || v == 1;
+    if (k == "build_lanes") return v == 0 || v == 1 || v == 4 || v == 8;
     return false;
 }
 
@@ -1144,6 +1146,7 @@ int omdg_set_launch(omdg_ctx* c, const char* key, int value) {
     if (!valid_knob(k, value)) return set_error(c, OMDG_EINVAL, "invalid value for " + k);
     if (*p == value) return OMDG_OK;
     *p = value;
+    if (k == "build_lanes") c->list_valid = false;
     if (k == "nbr_hshift") {
         // the list layout changes: reallocate and rebuild before the next use
         int m = c->maxnb;
@@ -1188,7 +1191,7 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
     std::vector<Cand> cands;
     if (eam) {
         for (int lanes : {4, 8, 16})
-            for (int block : {256, 512})
+            for (int block : {128, 256})
                 for (int stage : {0, 1}) cands.push_back(Cand{lanes, block, stage});
     } else if (pair) {
         for (int lanes : {2, 4, 8, 16})

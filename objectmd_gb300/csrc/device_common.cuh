@@ -67,6 +67,23 @@ __device__ __forceinline__ float3 pair_delta(const float4& hi_i, const float4& l
 
 __device__ __forceinline__ int pack_type(const float4& hi) { return __float_as_int(hi.w); }
 
+// One 256-bit read-only load (a whole 32-byte sector) for a neighbour's pack
+// or an interleaved pair of spline knots.  The data must not be written by
+// the same kernel.
+__device__ __forceinline__ void ldg256(const void* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
+// Coherent 256-bit load, for kernels that also write other words of the
+// same array.
+__device__ __forceinline__ void ld256(const void* p, float4& a, float4& b) {
+    asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                 : "l"(p));
+}
+
 // Compensated (Kahan) accumulator; the intrinsics keep the compiler from
 // contracting or reassociating the correction.
 struct Kahan {

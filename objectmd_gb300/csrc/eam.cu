@@ -290,9 +290,13 @@ int eam_prepare(Context* c, Potential& pot) {
     return OMDG_OK;
 }
 
+bool eam_fast_ok(const Context* c, const Potential& pot);
+int eam_fast_launch(Context* c, Potential& pot, bool first);
+
 int eam_launch(Context* c, Potential& pot, bool first) {
     int rc = eam_prepare(c, pot);
     if (rc) return rc;
+    if (eam_fast_ok(c, pot)) return eam_fast_launch(c, pot, first);
     EAMParams p;
     p.n = c->n;
     p.hshift = c->nbr_hshift;

@@ -1,0 +1,374 @@
+// Specialised EAM kernels for the common case: one atom type, PAIR and
+// EDENS tables on the same knot grid, no OutOfRange values (a read outside
+// the table is an error, as in the reference).  Same arithmetic as eam.cu
+// (team.cpp:81-92, :116-145, :224-237), arranged for the GB300 memory system:
+//   - each lane loads all of its neighbour-list entries up front (one DRAM
+//     round trip per atom instead of one per neighbour) and gathers the next
+//     neighbour's pack while it evaluates the current one,
+//   - a neighbour's position pack (with F'(rho) in its spare word) and an
+//     interleaved (phi, rho) knot are one 256-bit load each,
+//   - the periodic image comes from a 64-entry shared table of split shift
+//     vectors indexed by the entry's 6 image bits,
+//   - the knot index is clamped instead of branched (r <= rc keeps it below
+//     n-1; the reference's x == n-1 rule selects the same segment),
+//   - forces use Kahan sums, the per-pair energy and virial plain FP32 sums.
+#include "device_common.cuh"
+
+namespace omdg {
+
+struct EAMFast {
+    int n, hshift, maxnb;
+    float Lh[3], Ll[3];
+    const float4* coef2;   // (phi, rho) knot pairs
+    const float4* emb;     // EMBED knots
+    float off, dr, inv_dr;
+    int nknot;
+    float rc_phi, rc_rho, rc2;
+    int rmult_phi, rmult_rho;
+    float e_off, e_dr, e_inv_dr;
+    int e_n, e_rmult;
+    int stage_k0, stage_n;
+    int first;
+};
+
+__device__ __forceinline__ void build_shift_table(const EAMFast& p, float4* s_hi, float4* s_lo) {
+    for (int k = threadIdx.x; k < 64; k += blockDim.x) {
+        int bx = k & 3, by = (k >> 2) & 3, bz = (k >> 4) & 3;
+        float fx = (float)(bx - 1), fy = (float)(by - 1), fz = (float)(bz - 1);
+        s_hi[k] = make_float4(fx * p.Lh[0], fy * p.Lh[1], fz * p.Lh[2], 0.f);
+        s_lo[k] = make_float4(fx * p.Ll[0], fy * p.Ll[1], fz * p.Ll[2], 0.f);
+    }
+}
+
+// d = x_i - (x_j + s L) with the shift from the table (exact hi differences,
+// see pair_delta in device_common.cuh).
+__device__ __forceinline__ float3 delta_tab(const float4& hi, const float4& lo, const float4& hj, const float4& lj,
+                                            const float4& sh, const float4& sl) {
+    float3 d;
+    d.x = __fadd_rn(__fsub_rn(__fsub_rn(hi.x, hj.x), sh.x), __fsub_rn(__fsub_rn(lo.x, lj.x), sl.x));
+    d.y = __fadd_rn(__fsub_rn(__fsub_rn(hi.y, hj.y), sh.y), __fsub_rn(__fsub_rn(lo.y, lj.y), sl.y));
+    d.z = __fadd_rn(__fsub_rn(__fsub_rn(hi.z, hj.z), sh.z), __fsub_rn(__fsub_rn(lo.z, lj.z), sl.z));
+    return d;
+}
+
+template <int LANES>
+__device__ __forceinline__ void twosum_reduce(float& s, float& c) {
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) {
+        float s2 = __shfl_xor_sync(0xffffffffu, s, off);
+        float c2 = __shfl_xor_sync(0xffffffffu, c, off);
+        float t = __fadd_rn(s, s2);
+        float bp = __fsub_rn(t, s);
+        float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(s2, bp));
+        c = __fsub_rn(__fadd_rn(c, c2), e);
+        s = t;
+    }
+}
+
+template <int LANES>
+__device__ __forceinline__ float plain_reduce(float v) {
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Entries a lane prefetches into registers per pass over its row.
+template <int LANES>
+struct Prefetch {
+    static constexpr int N = LANES >= 4 ? 64 / LANES : 16;
+};
+
+template <int LANES, bool STAGED>
+__global__ void __launch_bounds__(256, 4) k_eamf_density(EAMFast p, PosPack* pack, const unsigned* __restrict__ nbr,
+                                                         const int* __restrict__ nnb, float* __restrict__ fp,
+                                                         float* __restrict__ femb, unsigned* status) {
+    constexpr int PF = Prefetch<LANES>::N;
+    __shared__ float4 s_hi[64], s_lo[64];
+    extern __shared__ float4 s_rho[];
+    build_shift_table(p, s_hi, s_lo);
+    if (STAGED)
+        for (int k = threadIdx.x; k < p.stage_n; k += blockDim.x) s_rho[k] = p.coef2[2 * (size_t)(p.stage_k0 + k) + 1];
+    __syncthreads();
+    const int lane = threadIdx.x & (LANES - 1);
+    const int per_block = blockDim.x / LANES;
+    const int step = LANES << p.hshift;
+    const float rc2 = p.rc_rho * p.rc_rho * 1.0001f;
+    const float offdr = p.off * p.inv_dr;
+    for (int base = blockIdx.x * per_block; base < p.n; base += gridDim.x * per_block) {
+        const int i = base + threadIdx.x / LANES;
+        const bool valid = i < p.n;
+        const int ii = valid ? i : p.n - 1;
+        const float4 hi = pack[ii].hi, lo = pack[ii].lo;
+        const int m = valid ? nnb[ii] : 0;
+        const unsigned* rp = nbr + nbr_at(ii, lane, p.hshift, p.maxnb);
+        Kahan acc;
+        bool bad = false;
+        for (int s0 = lane; s0 < m; s0 += PF * LANES, rp += PF * step) {
+            unsigned ent[PF];
+#pragma unroll
+            for (int k = 0; k < PF; k++) ent[k] = (s0 + k * LANES < m) ? __ldg(rp + k * step) : 0u;
+            float4 hj, lj;
+            ld256(pack + (ent[0] & (unsigned)INDEX_MASK), hj, lj);
+#pragma unroll
+            for (int k = 0; k < PF; k++) {
+                if (s0 + k * LANES >= m) break;
+                float4 hn, ln;
+                if (k + 1 < PF && s0 + (k + 1) * LANES < m) ld256(pack + (ent[k + 1] & (unsigned)INDEX_MASK), hn, ln);
+                const int code = (int)(ent[k] >> 26);
+                const float3 d = delta_tab(hi, lo, hj, lj, s_hi[code], s_lo[code]);
+                hj = hn;
+                lj = ln;
+                const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+                if (r2 > rc2) continue;
+                const float r = r2 * rsqrtf(r2);
+                if (!(r <= p.rc_rho)) continue;
+                int x = __float2int_rz(fmaf(r, p.inv_dr, -offdr));
+                if (x < 0) {
+                    bad = true;  // closer than the first knot: outside every tabulated range here
+                    continue;
+                }
+                x = min(x, p.nknot - 2);
+                const float dx = fmaf(-(float)x, p.dr, r - p.off);
+                float4 cf;
+                if (STAGED && (unsigned)(x - p.stage_k0) < (unsigned)p.stage_n) cf = s_rho[x - p.stage_k0];
+                else cf = __ldg(&p.coef2[2 * (size_t)x + 1]);
+                float v = fmaf(dx, fmaf(dx, fmaf(dx, cf.x, cf.y), cf.z), cf.w);
+                if (p.rmult_rho) v = v / r;
+                acc.add(v);
+            }
+        }
+        if (bad) atomicOr(status, ERR_TABLE_RANGE);
+        float sum = acc.s, comp = acc.c;
+        twosum_reduce<LANES>(sum, comp);
+        if (lane == 0 && valid) {
+            const float rho = __fsub_rn(sum, comp);
+            // F(rho), F'(rho): TableReader::read on the EMBED section
+            const float rval = rho - p.e_off;
+            int x = __float2int_rz(rval * p.e_inv_dr);
+            float F = 0.f, dF = 0.f;
+            if (x < -1 || x > p.e_n - 1) {
+                atomicOr(status, ERR_TABLE_RANGE);
+            } else {
+                float dx = fmaf(-(float)x, p.e_dr, rval);
+                if (x == p.e_n - 1) {
+                    dx += p.e_dr;
+                    x--;
+                }
+                if (x == -1) x = 0;
+                const float4 cf = __ldg(&p.emb[x]);
+                F = fmaf(dx, fmaf(dx, fmaf(dx, cf.x, cf.y), cf.z), cf.w);
+                dF = fmaf(dx, fmaf(3.0f * dx, cf.x, 2.0f * cf.y), cf.z);
+                if (p.e_rmult) {
+                    F = F / rho;
+                    dF = (dF - F) / rho;
+                }
+            }
+            fp[i] = dF;
+            femb[i] = F;
+            pack[i].lo.w = dF;  // F'(rho_i) travels with the position for the force pass
+        }
+    }
+}
+
+template <int LANES, bool STAGED>
+__global__ void __launch_bounds__(256, 4) k_eamf_force(EAMFast p, const PosPack* __restrict__ pack,
+                                                       const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                                       const float* __restrict__ femb, float* __restrict__ fx,
+                                                       float* __restrict__ fy, float* __restrict__ fz,
+                                                       float* __restrict__ pe, float* __restrict__ vir,
+                                                       unsigned* status) {
+    constexpr int PF = Prefetch<LANES>::N;
+    __shared__ float4 s_hi[64], s_lo[64];
+    extern __shared__ float4 s_tab[];  // (phi, rho) knot pairs [k0, k0+ns)
+    build_shift_table(p, s_hi, s_lo);
+    if (STAGED)
+        for (int k = threadIdx.x; k < 2 * p.stage_n; k += blockDim.x) s_tab[k] = p.coef2[2 * (size_t)p.stage_k0 + k];
+    __syncthreads();
+    const int lane = threadIdx.x & (LANES - 1);
+    const int per_block = blockDim.x / LANES;
+    const int step = LANES << p.hshift;
+    const float offdr = p.off * p.inv_dr;
+    for (int base = blockIdx.x * per_block; base < p.n; base += gridDim.x * per_block) {
+        const int i = base + threadIdx.x / LANES;
+        const bool valid = i < p.n;
+        const int ii = valid ? i : p.n - 1;
+        const float4 hi = pack[ii].hi, lo = pack[ii].lo;
+        const float fpi = lo.w;
+        const int m = valid ? nnb[ii] : 0;
+        const unsigned* rp = nbr + nbr_at(ii, lane, p.hshift, p.maxnb);
+        Kahan ax, ay, az;
+        float ae = 0.f, av = 0.f;
+        bool bad = false;
+        for (int s0 = lane; s0 < m; s0 += PF * LANES, rp += PF * step) {
+            unsigned ent[PF];
+#pragma unroll
+            for (int k = 0; k < PF; k++) ent[k] = (s0 + k * LANES < m) ? __ldg(rp + k * step) : 0u;
+            float4 hj, lj;
+            ldg256(pack + (ent[0] & (unsigned)INDEX_MASK), hj, lj);
+#pragma unroll
+            for (int k = 0; k < PF; k++) {
+                if (s0 + k * LANES >= m) break;
+                float4 hn, ln;
+                if (k + 1 < PF && s0 + (k + 1) * LANES < m)
+                    ldg256(pack + (ent[k + 1] & (unsigned)INDEX_MASK), hn, ln);
+                const int code = (int)(ent[k] >> 26);
+                const float3 d = delta_tab(hi, lo, hj, lj, s_hi[code], s_lo[code]);
+                const float fpj = lj.w;  // F'(rho_j) from the density pass
+                hj = hn;
+                lj = ln;
+                const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+                if (r2 > p.rc2) continue;
+                const float rinv = rsqrtf(r2);
+                const float r = r2 * rinv;
+                if (!(r <= p.rc_phi)) continue;
+                int x = __float2int_rz(fmaf(r, p.inv_dr, -offdr));
+                if (x < 0) {
+                    bad = true;
+                    continue;
+                }
+                x = min(x, p.nknot - 2);
+                const float dx = fmaf(-(float)x, p.dr, r - p.off);
+                float4 cp, cr;
+                if (STAGED && (unsigned)(x - p.stage_k0) < (unsigned)p.stage_n) {
+                    cp = s_tab[2 * (x - p.stage_k0)];
+                    cr = s_tab[2 * (x - p.stage_k0) + 1];
+                } else {
+                    ldg256(&p.coef2[2 * (size_t)x], cp, cr);
+                }
+                float ph = fmaf(dx, fmaf(dx, fmaf(dx, cp.x, cp.y), cp.z), cp.w);
+                float dph = fmaf(dx, fmaf(3.0f * dx, cp.x, 2.0f * cp.y), cp.z);
+                if (p.rmult_phi) {
+                    ph = ph * rinv;
+                    dph = (dph - ph) * rinv;
+                }
+                float drho = fmaf(dx, fmaf(3.0f * dx, cr.x, 2.0f * cr.y), cr.z);
+                if (p.rmult_rho) {
+                    const float rv = fmaf(dx, fmaf(dx, fmaf(dx, cr.x, cr.y), cr.z), cr.w);
+                    drho = (drho - rv * rinv) * rinv;
+                }
+                if (r > p.rc_rho) drho = 0.f;
+                const float fr = -fmaf(fpi + fpj, drho, dph) * rinv;
+                ax.add(d.x * fr);
+                ay.add(d.y * fr);
+                az.add(d.z * fr);
+                ae = fmaf(0.5f, ph, ae);
+                av = fmaf(fr, r2, av);
+            }
+        }
+        if (bad) atomicOr(status, ERR_TABLE_RANGE);
+        twosum_reduce<LANES>(ax.s, ax.c);
+        twosum_reduce<LANES>(ay.s, ay.c);
+        twosum_reduce<LANES>(az.s, az.c);
+        ae = plain_reduce<LANES>(ae);
+        av = plain_reduce<LANES>(av);
+        if (lane == 0 && valid) {
+            const float vfx = __fsub_rn(ax.s, ax.c), vfy = __fsub_rn(ay.s, ay.c), vfz = __fsub_rn(az.s, az.c);
+            const float ve = ae + femb[i];
+            if (p.first) {
+                fx[i] = vfx;
+                fy[i] = vfy;
+                fz[i] = vfz;
+                pe[i] = ve;
+                vir[i] = av;
+            } else {
+                fx[i] += vfx;
+                fy[i] += vfy;
+                fz[i] += vfz;
+                pe[i] += ve;
+                vir[i] += av;
+            }
+        }
+    }
+}
+
+template <int LANES, bool STAGED>
+static void launch_fast(Context* c, const EAMFast& p, int grid, int block, size_t smem1, size_t smem2) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_eamf_density<LANES, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_eamf_force<LANES, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    prof_begin(c, "eam_density");
+    k_eamf_density<LANES, STAGED><<<grid, block, smem1, c->stream>>>(
+        p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->fp, c->femb, c->d_status);
+    prof_end(c);
+    prof_begin(c, "eam_force");
+    k_eamf_force<LANES, STAGED><<<grid, block, smem2, c->stream>>>(
+        p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->femb, c->fx, c->fy, c->fz, c->pe, c->vir,
+        c->d_status);
+    prof_end(c);
+}
+
+bool eam_fast_ok(const Context* c, const Potential& pot) {
+    const HostTable &a = pot.t0, &b = pot.t1;
+    return c->ntypes == 1 && pot.d_coef2 && !a.allow_lo && !a.allow_hi && !b.allow_lo && !b.allow_hi &&
+           !pot.t2.allow_lo && !pot.t2.allow_hi && a.n >= 4;
+}
+
+int eam_fast_launch(Context* c, Potential& pot, bool first) {
+    EAMFast p;
+    p.n = c->n;
+    p.hshift = c->nbr_hshift;
+    p.maxnb = c->maxnb;
+    for (int d = 0; d < 3; d++) {
+        p.Lh[d] = c->box.Lh[d];
+        p.Ll[d] = c->box.Ll[d];
+    }
+    p.coef2 = pot.d_coef2;
+    p.emb = pot.dt[2].coef;
+    p.off = (float)pot.t0.off;
+    p.dr = (float)pot.t0.dr;
+    p.inv_dr = (float)(1.0 / pot.t0.dr);
+    p.nknot = pot.t0.n;
+    p.rc_phi = (float)pot.t0.max_range();
+    p.rc_rho = (float)pot.t1.max_range();
+    float rcm = p.rc_phi > p.rc_rho ? p.rc_phi : p.rc_rho;
+    p.rc2 = rcm * rcm * 1.0001f;
+    p.rmult_phi = pot.t0.rmult ? 1 : 0;
+    p.rmult_rho = pot.t1.rmult ? 1 : 0;
+    p.e_off = (float)pot.t2.off;
+    p.e_dr = (float)pot.t2.dr;
+    p.e_inv_dr = (float)(1.0 / pot.t2.dr);
+    p.e_n = pot.t2.n;
+    p.e_rmult = pot.t2.rmult ? 1 : 0;
+    p.first = first ? 1 : 0;
+    int k0 = 0, ns = 0;
+    if (c->eam_stage) {
+        k0 = (int)((c->eam_stage_frac * pot.t1.max_range() - pot.t1.off) / pot.t1.dr);
+        if (k0 < 0) k0 = 0;
+        ns = pot.t1.n - k0;
+        int max_stage = (180 * 1024) / (2 * (int)sizeof(float4));
+        if (ns > max_stage) {
+            k0 = pot.t1.n - max_stage;
+            ns = max_stage;
+        }
+    }
+    p.stage_k0 = k0;
+    p.stage_n = ns;
+    int block = c->eam_block > 256 ? 256 : c->eam_block, lanes = c->eam_lanes;
+    int per_block = block / lanes;
+    int grid = grid_for(c->n, per_block);
+    if (ns > 0) {
+        int cap = c->num_sms * (c->eam_ctas_per_sm > 0 ? c->eam_ctas_per_sm : 1);
+        grid = grid < cap ? grid : cap;
+    }
+    size_t smem1 = (size_t)ns * sizeof(float4), smem2 = 2 * smem1;
+    bool st = ns > 0;
+#define OMDG_EAMF(L)                                                 \
+    (st ? launch_fast<L, true>(c, p, grid, block, smem1, smem2)      \
+        : launch_fast<L, false>(c, p, grid, block, smem1, smem2))
+    switch (lanes) {
+        case 1: OMDG_EAMF(1); break;
+        case 2: OMDG_EAMF(2); break;
+        case 4: OMDG_EAMF(4); break;
+        case 8: OMDG_EAMF(8); break;
+        case 16: OMDG_EAMF(16); break;
+        default: OMDG_EAMF(32); break;
+    }
+#undef OMDG_EAMF
+    c->launches += 2;
+    return check_cuda(c, cudaGetLastError(), "eam");
+}
+
+}  // namespace omdg

@@ -30,11 +30,22 @@ struct IntParams {
     double org[3], P[3];
     float half_skin2;       // (skin/2)^2
     int use_f64;
+    int thermostat;         // apply the velocity factor of the previous step
+    double Q[3];            // P - org: the pack coordinate is X = x + Q
 };
 
+// hi = X rounded to 24 significant bits, lo = X - hi, with integer
+// operations on the FP64 bit pattern instead of FP64 arithmetic (the FP64
+// pipe is the scarce one).  Valid for positive normal X; hi and the
+// remainder are exact, lo is the FP32 rounding of the remainder.
 __device__ __forceinline__ void split_pack(double X, float& hi, float& lo) {
-    hi = __double2float_rn(X);
-    lo = __double2float_rn(__dsub_rn(X, (double)hi));
+    const long long b = __double_as_longlong(X);
+    const long long hb = (b + (1ll << 28)) & ~((1ll << 29) - 1);
+    const int eh = (int)((hb >> 52) & 0x7FF) - 1023 + 127;
+    hi = __int_as_float((eh << 23) | (int)((hb >> 29) & 0x7FFFFF));
+    const int diff = (int)(b - hb);  // in units of X's last mantissa bit, |diff| <= 2^28
+    const int ex = (int)((b >> 52) & 0x7FF) - 1023 - 52 + 127;
+    lo = __int2float_rn(diff) * __int_as_float(ex << 23);
 }
 
 __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
@@ -62,9 +73,15 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
             ay = fy[i];
             az = fz[i];
         }
-        double ux = fma(ax, h, vx[i] * lam);
-        double uy = fma(ay, h, vy[i] * lam);
-        double uz = fma(az, h, vz[i] * lam);
+        double ux = vx[i], uy = vy[i], uz = vz[i];
+        if (p.thermostat) {
+            ux *= lam;
+            uy *= lam;
+            uz *= lam;
+        }
+        ux = fma(ax, h, ux);
+        uy = fma(ay, h, uy);
+        uz = fma(az, h, uz);
         double X = fma(p.dt, ux, x[i]);
         double Y = fma(p.dt, uy, y[i]);
         double Z = fma(p.dt, uz, z[i]);
@@ -75,9 +92,9 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
         y[i] = Y;
         z[i] = Z;
         PosPack pk;
-        split_pack(__dadd_rn(__dsub_rn(X, p.org[0]), p.P[0]), pk.hi.x, pk.lo.x);
-        split_pack(__dadd_rn(__dsub_rn(Y, p.org[1]), p.P[1]), pk.hi.y, pk.lo.y);
-        split_pack(__dadd_rn(__dsub_rn(Z, p.org[2]), p.P[2]), pk.hi.z, pk.lo.z);
+        split_pack(__dadd_rn(X, p.Q[0]), pk.hi.x, pk.lo.x);
+        split_pack(__dadd_rn(Y, p.Q[1]), pk.hi.y, pk.lo.y);
+        split_pack(__dadd_rn(Z, p.Q[2]), pk.hi.z, pk.lo.z);
         pk.hi.w = __int_as_float(t);
         pk.lo.w = 0.f;
         pack[i] = pk;
@@ -90,6 +107,7 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
 }
 
 constexpr int RED_BLOCK = 256;
+constexpr int KICK_ATOMS = 4;
 
 __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, double* __restrict__ vx, double* __restrict__ vy,
                                                     double* __restrict__ vz, const float* __restrict__ fx,
@@ -98,9 +116,13 @@ __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, double* __restr
                                                     const double* __restrict__ mass, const float* __restrict__ pe,
                                                     const float* __restrict__ vir, double* __restrict__ partial,
                                                     int kick) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // each thread takes KICK_ATOMS atoms, blockDim apart (coalesced)
     double k = 0, e = 0, w = 0;
-    if (i < p.n) {
+    const int base = blockIdx.x * blockDim.x * KICK_ATOMS + threadIdx.x;
+#pragma unroll
+    for (int a = 0; a < KICK_ATOMS; a++) {
+        const int i = base + a * blockDim.x;
+        if (i >= p.n) break;
         int t = type[i];
         double ux = vx[i], uy = vy[i], uz = vz[i];
         if (kick) {
@@ -118,9 +140,9 @@ __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, double* __restr
             vy[i] = uy;
             vz[i] = uz;
         }
-        k = mass[t] * (ux * ux + uy * uy + uz * uz);
-        e = p.use_f64 ? f64[3 * (size_t)p.n + i] : (double)pe[i];
-        w = vir[i];
+        k = fma(mass[t], fma(ux, ux, fma(uy, uy, uz * uz)), k);
+        e += p.use_f64 ? f64[3 * (size_t)p.n + i] : (double)pe[i];
+        w += (double)vir[i];
     }
     // fixed-order block reduction
     __shared__ double sk[RED_BLOCK], se[RED_BLOCK], sw[RED_BLOCK];
@@ -213,6 +235,8 @@ static IntParams int_params(Context* c) {
     float hs = (float)(0.5 * c->skin);
     p.half_skin2 = hs * hs;
     p.use_f64 = c->use_f64 ? 1 : 0;
+    p.thermostat = c->thermo_tau > 0.0 ? 1 : 0;
+    for (int d = 0; d < 3; d++) p.Q[d] = c->box.P[d] - c->box.org[d];
     return p;
 }
 
@@ -229,7 +253,7 @@ int integrate_kick_drift(Context* c, int) {
 
 static int reduce_and_finalize(Context* c, int kick, int count_step) {
     IntParams p = int_params(c);
-    int nb = grid_for(c->n, RED_BLOCK);
+    int nb = grid_for(c->n, RED_BLOCK * KICK_ATOMS);
     prof_begin(c, "kick");
     k_kick<<<nb, RED_BLOCK, 0, c->stream>>>(p, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz, c->f64, c->type, c->d_mass,
                                             c->pe, c->vir, c->d_red, kick);

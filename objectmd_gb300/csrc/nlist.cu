@@ -313,6 +313,257 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const PosPack* __r
     nnb[i] = cnt;
 }
 
+// Per axis, how many (cell, image) candidates a cell has and the idx-th one
+// (the same enumeration as axis_candidates, without a local array).
+__device__ __forceinline__ int axis_count(int nc, int periodic) { return (periodic && nc < 3) ? 3 * nc : 3; }
+
+__device__ __forceinline__ bool axis_cell(int c, int nc, int periodic, int idx, int& cell, int& shift) {
+    if (periodic) {
+        if (nc >= 3) {
+            int k = c + idx - 1;
+            shift = 0;
+            if (k < 0) {
+                k += nc;
+                shift = -1;
+            } else if (k >= nc) {
+                k -= nc;
+                shift = 1;
+            }
+            cell = k;
+        } else {
+            cell = idx / 3;
+            shift = idx % 3 - 1;
+        }
+        return true;
+    }
+    const int k = c + idx - 1;
+    cell = k;
+    shift = 0;
+    return k >= 0 && k < nc;
+}
+
+// Same list as k_build with LANES threads per atom: the lanes test
+// consecutive atoms of a cell together and append the accepted ones in lane
+// order (ballot + prefix popcount), so each row keeps exactly the
+// cell-traversal order of the one-thread build.
+template <int LANES>
+__global__ void __launch_bounds__(256) k_build_lanes(BuildParams p, const PosPack* __restrict__ pack,
+                                                     const double* __restrict__ x, const double* __restrict__ y,
+                                                     const double* __restrict__ z, const int* __restrict__ cell,
+                                                     const int* __restrict__ start, unsigned* __restrict__ nbr,
+                                                     int* __restrict__ nnb, unsigned* status, int* need) {
+    const int lane = threadIdx.x & (LANES - 1);
+    const int gbase = (threadIdx.x & 31) & ~(LANES - 1);
+    const unsigned gmask = (LANES == 32 ? 0xffffffffu : ((1u << LANES) - 1u)) << gbase;
+    const int i = blockIdx.x * (blockDim.x / LANES) + threadIdx.x / LANES;
+    if (i >= p.n) return;  // whole groups leave together
+    const PosPack pi = pack[i];
+    const int ci = cell[i];
+    const int cx = ci % p.nc[0], cy = (ci / p.nc[0]) % p.nc[1], cz = ci / (p.nc[0] * p.nc[1]);
+    const int mx = axis_count(p.nc[0], p.periodic[0]);
+    const int my = axis_count(p.nc[1], p.periodic[1]);
+    const int mz = axis_count(p.nc[2], p.periodic[2]);
+    int cnt = 0;
+    for (int a = 0; a < mz; a++)
+        for (int b = 0; b < my; b++)
+            for (int q = 0; q < mx; q++) {
+                int kz, sz, ky, sy, kx, sx;
+                if (!axis_cell(cz, p.nc[2], p.periodic[2], a, kz, sz) ||
+                    !axis_cell(cy, p.nc[1], p.periodic[1], b, ky, sy) ||
+                    !axis_cell(cx, p.nc[0], p.periodic[0], q, kx, sx))
+                    continue;
+                const int c = (kz * p.nc[1] + ky) * p.nc[0] + kx;
+                const unsigned code = nbr_encode(0, sx, sy, sz);
+                const bool self_image = (sx == 0 && sy == 0 && sz == 0);
+                const int e = start[c + 1];
+                for (int k0 = start[c]; k0 < e; k0 += LANES) {
+                    const int k = k0 + lane;
+                    bool in = false;
+                    if (k < e && !(self_image && k == i)) {
+                        const PosPack pk = pack[k];
+                        const float3 d = pair_delta(pi.hi, pi.lo, pk.hi, pk.lo, code, p.L);
+                        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+                        if (r2 <= p.rsq_hi) {
+                            in = r2 < p.rsq_lo;
+                            if (!in) {
+                                // borderline: the reference's FP64 arithmetic decides
+                                double gx = sx == 0 ? 0.0 : (sx > 0 ? p.L64[0] : -p.L64[0]);
+                                double gy = sy == 0 ? 0.0 : (sy > 0 ? p.L64[1] : -p.L64[1]);
+                                double gz = sz == 0 ? 0.0 : (sz > 0 ? p.L64[2] : -p.L64[2]);
+                                double dx = __dsub_rn(x[i], __dadd_rn(x[k], gx));
+                                double dy = __dsub_rn(y[i], __dadd_rn(y[k], gy));
+                                double dz = __dsub_rn(z[i], __dadd_rn(z[k], gz));
+                                double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                      __dmul_rn(dz, dz));
+                                in = rr <= p.rsq;
+                            }
+                            if (in && r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
+                        }
+                    }
+                    const unsigned bal = __ballot_sync(gmask, in) >> gbase;
+                    if (in) {
+                        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                        if (pos < p.maxnb) nbr[nbr_at(i, pos, p.hshift, p.maxnb)] = code | (unsigned)k;
+                    }
+                    cnt += __popc(bal);
+                }
+            }
+    if (lane == 0) {
+        if (cnt > p.maxnb) {
+            atomicOr(status, ERR_NBR_OVERFLOW);
+            atomicMax(need, cnt);
+            cnt = p.maxnb;
+        }
+        nnb[i] = cnt;
+    }
+}
+
+// Cell-centric build: one CTA per cell.  The CTA copies the packs of every
+// (cell, image) of the cell's neighbourhood into shared memory in traversal
+// order (chunks of `cap` candidates when the neighbourhood is larger), and
+// groups of 8 lanes test one centre atom each against the staged candidates,
+// appending in lane order.  Rows come out identical to k_build's.
+constexpr int BUILD_CELL_THREADS = 128;
+constexpr int BUILD_GROUP = 8;
+
+// The reference's FP64 test (dx = x_i - (x_j + s), r2 = (dx*dx + dy*dy) +
+// dz*dz <= Rv^2) for the rare pairs inside the FP32 screening band.
+__device__ __noinline__ bool exact_within(double Lx, double Ly, double Lz, double rsq, const double* __restrict__ x,
+                                          const double* __restrict__ y, const double* __restrict__ z, int i, int k,
+                                          unsigned code) {
+    const int sx = nbr_sx(code), sy = nbr_sy(code), sz = nbr_sz(code);
+    double gx = sx == 0 ? 0.0 : (sx > 0 ? Lx : -Lx);
+    double gy = sy == 0 ? 0.0 : (sy > 0 ? Ly : -Ly);
+    double gz = sz == 0 ? 0.0 : (sz > 0 ? Lz : -Lz);
+    double dx = __dsub_rn(x[i], __dadd_rn(x[k], gx));
+    double dy = __dsub_rn(y[i], __dadd_rn(y[k], gy));
+    double dz = __dsub_rn(z[i], __dadd_rn(z[k], gz));
+    double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    return rr <= rsq && !(k == i && code == nbr_encode(0, 0, 0, 0));
+}
+
+__global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildParams p, const PosPack* __restrict__ pack,
+                                                                    const double* __restrict__ x,
+                                                                    const double* __restrict__ y,
+                                                                    const double* __restrict__ z,
+                                                                    const int* __restrict__ start, int cap,
+                                                                    unsigned* __restrict__ nbr, int* __restrict__ nnb,
+                                                                    unsigned* status, int* need) {
+    extern __shared__ float4 s_cand[];  // 2 float4 per candidate: hi (w = atom index), lo (w = image code)
+    __shared__ int s_cell[64], s_code[64], s_pref[65];
+    __shared__ float4 s_sh[64], s_sl[64];  // split image shift by the entry's 6 image bits
+    for (int k = threadIdx.x; k < 64; k += blockDim.x) {
+        const float fx = (float)((k & 3) - 1), fy = (float)(((k >> 2) & 3) - 1), fz = (float)(((k >> 4) & 3) - 1);
+        s_sh[k] = make_float4(fx * p.L.hx, fy * p.L.hy, fz * p.L.hz, 0.f);
+        s_sl[k] = make_float4(fx * p.L.lx, fy * p.L.ly, fz * p.L.lz, 0.f);
+    }
+    const int c = blockIdx.x;
+    const int cx = c % p.nc[0], cy = (c / p.nc[0]) % p.nc[1], cz = c / (p.nc[0] * p.nc[1]);
+    const int mx = axis_count(p.nc[0], p.periodic[0]);
+    const int my = axis_count(p.nc[1], p.periodic[1]);
+    const int mz = axis_count(p.nc[2], p.periodic[2]);
+    const int ncombo = mx * my * mz;  // <= 27 unless a periodic axis has fewer than 3 cells
+    // enumerate (cell, image) combos in traversal order (combo t = (a, b, q)
+    // with q fastest); the first two warps look up one combo each in parallel
+    if (threadIdx.x < 64) {
+        const int t = threadIdx.x;
+        int cnt = 0, cc = 0;
+        unsigned code = 0;
+        if (t < ncombo) {
+            const int q = t % mx, b = (t / mx) % my, a = t / (mx * my);
+            int kz, sz, ky, sy, kx, sx;
+            if (axis_cell(cz, p.nc[2], p.periodic[2], a, kz, sz) && axis_cell(cy, p.nc[1], p.periodic[1], b, ky, sy) &&
+                axis_cell(cx, p.nc[0], p.periodic[0], q, kx, sx)) {
+                cc = (kz * p.nc[1] + ky) * p.nc[0] + kx;
+                cnt = start[cc + 1] - start[cc];
+                code = nbr_encode(0, sx, sy, sz);
+            }
+        }
+        s_cell[t] = cc;
+        s_code[t] = (int)code;
+        s_pref[t + 1] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_pref[0] = 0;
+        for (int t = 0; t < 64; t++) s_pref[t + 1] += s_pref[t];
+    }
+    __syncthreads();
+    const int nc_used = ncombo < 64 ? ncombo : 64;
+    const int total = s_pref[nc_used];
+    const int c_begin = start[c], c_end = start[c + 1];
+    const int group = threadIdx.x / BUILD_GROUP, lane = threadIdx.x & (BUILD_GROUP - 1);
+    const int gbase = (threadIdx.x & 31) & ~(BUILD_GROUP - 1);
+    const unsigned gmask = ((1u << BUILD_GROUP) - 1u) << gbase;
+    const unsigned self_code = nbr_encode(0, 0, 0, 0);
+    for (int batch = c_begin; batch < c_end; batch += BUILD_CELL_THREADS / BUILD_GROUP) {
+        const int i = batch + group;
+        const bool active = i < c_end;
+        PosPack pi;
+        if (active) pi = pack[i];
+        int cnt = 0;
+        for (int c0 = 0; c0 < total; c0 += cap) {
+            const int c1 = min(total, c0 + cap);
+            __syncthreads();
+            for (int t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
+                int lo = 0, hi = nc_used;  // combo holding candidate t
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (s_pref[mid] <= t) lo = mid;
+                    else hi = mid;
+                }
+                const int k = start[s_cell[lo]] + (t - s_pref[lo]);
+                PosPack pk = pack[k];
+                pk.hi.w = __int_as_float(k);
+                pk.lo.w = __int_as_float(s_code[lo]);
+                s_cand[2 * (t - c0)] = pk.hi;
+                s_cand[2 * (t - c0) + 1] = pk.lo;
+            }
+            __syncthreads();
+            if (active) {
+                for (int k0 = c0; k0 < c1; k0 += BUILD_GROUP) {
+                    const int t = k0 + lane;
+                    bool in = false;
+                    unsigned entry = 0;
+                    if (t < c1) {
+                        const float4 hk = s_cand[2 * (t - c0)], lk = s_cand[2 * (t - c0) + 1];
+                        const unsigned code = __float_as_uint(lk.w);
+                        entry = code | __float_as_uint(hk.w);
+                        const float4 sh = s_sh[code >> 26], sl = s_sl[code >> 26];
+                        const float dx = __fadd_rn(__fsub_rn(__fsub_rn(pi.hi.x, hk.x), sh.x),
+                                                   __fsub_rn(__fsub_rn(pi.lo.x, lk.x), sl.x));
+                        const float dy = __fadd_rn(__fsub_rn(__fsub_rn(pi.hi.y, hk.y), sh.y),
+                                                   __fsub_rn(__fsub_rn(pi.lo.y, lk.y), sl.y));
+                        const float dz = __fadd_rn(__fsub_rn(__fsub_rn(pi.hi.z, hk.z), sh.z),
+                                                   __fsub_rn(__fsub_rn(pi.lo.z, lk.z), sl.z));
+                        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                        // the atom itself is the only candidate at exactly zero distance
+                        in = r2 < p.rsq_lo && r2 > 0.f;
+                        if (r2 >= p.rsq_lo && r2 <= p.rsq_hi)
+                            in = exact_within(p.L64[0], p.L64[1], p.L64[2], p.rsq, x, y, z, i,
+                                              (int)(entry & (unsigned)INDEX_MASK), code);
+                        if (in && r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
+                    }
+                    const unsigned bal = __ballot_sync(gmask, in) >> gbase;
+                    if (in) {
+                        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                        if (pos < p.maxnb) nbr[nbr_at(i, pos, p.hshift, p.maxnb)] = entry;
+                    }
+                    cnt += __popc(bal);
+                }
+            }
+        }
+        if (active && lane == 0) {
+            if (cnt > p.maxnb) {
+                atomicOr(status, ERR_NBR_OVERFLOW);
+                atomicMax(need, cnt);
+                cnt = p.maxnb;
+            }
+            nnb[i] = cnt;
+        }
+    }
+}
+
 // rev at (i, s): the slot of (i, -image) in the row of j = nbr at (i, s).
 __global__ void k_reverse(int n, int hshift, int maxnb, const unsigned* __restrict__ nbr,
                           const int* __restrict__ nnb, int* __restrict__ rev, unsigned* status) {
@@ -463,9 +714,26 @@ int nlist_build(Context* c) {
     bp.rsq_lo = (float)(bp.rsq * (1.0 - 2e-5));
     bp.rsq_hi = (float)(bp.rsq * (1.0 + 2e-5));
     prof_begin(c, "nlist_build");
-    k_build<<<grid_for(n, 128), 128, 0, s>>>(bp, c->pack, c->x, c->y, c->z, cell_sorted, c->cell_start,
-                                             reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
-                                             c->d_flags + 1);
+    int combos = 1;
+    for (int d = 0; d < 3; d++) combos *= (g.periodic[d] && g.nc[d] < 3) ? 3 * g.nc[d] : 3;
+    if (c->build_lanes == 0 && combos <= 64) {
+        const int cap = 1024;  // staged candidates per chunk (32 bytes each)
+        k_build_cells<<<m, BUILD_CELL_THREADS, cap * 2 * sizeof(float4), s>>>(
+            bp, c->pack, c->x, c->y, c->z, c->cell_start, cap, reinterpret_cast<unsigned*>(c->nbr), c->nnb,
+            c->d_status, c->d_flags + 1);
+    } else if (c->build_lanes == 8) {
+        k_build_lanes<8><<<grid_for(n, 256 / 8), 256, 0, s>>>(bp, c->pack, c->x, c->y, c->z, cell_sorted,
+                                                               c->cell_start, reinterpret_cast<unsigned*>(c->nbr),
+                                                               c->nnb, c->d_status, c->d_flags + 1);
+    } else if (c->build_lanes == 4) {
+        k_build_lanes<4><<<grid_for(n, 256 / 4), 256, 0, s>>>(bp, c->pack, c->x, c->y, c->z, cell_sorted,
+                                                               c->cell_start, reinterpret_cast<unsigned*>(c->nbr),
+                                                               c->nnb, c->d_status, c->d_flags + 1);
+    } else {
+        k_build<<<grid_for(n, 128), 128, 0, s>>>(bp, c->pack, c->x, c->y, c->z, cell_sorted, c->cell_start,
+                                                 reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
+                                                 c->d_flags + 1);
+    }
     c->launches++;
     prof_end(c);
     if (c->need_rev) {

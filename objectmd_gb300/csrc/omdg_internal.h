@@ -79,9 +79,9 @@ struct BoxGeom {
     double cell_org[3], cell_h[3];
 };
 
-struct __align__(16) PosPack {
+struct __align__(32) PosPack {
     float4 hi;  // hx, hy, hz, type (bit pattern)
-    float4 lo;  // lx, ly, lz, 0
+    float4 lo;  // lx, ly, lz, per-atom auxiliary (EAM: F'(rho), written by the density pass)
 };
 
 // ------------------------------------------------------------ potentials
@@ -190,10 +190,11 @@ struct Context {
 
     // launch shapes (defaults; the tuner may change them)
     int num_sms = 152;
-    int nbr_hshift = 2;        // sliced-ELL slice height H = 2^hshift
+    int build_lanes = 0;       // list build: 0 cell-centric (shared memory), else threads per atom (1, 4, 8)
+    int nbr_hshift = 3;        // sliced-ELL slice height H = 2^hshift
     int eam_block = 256;
-    int eam_lanes = 8;         // threads per atom
-    int eam_stage = 1;         // 1: stage spline knots in shared memory
+    int eam_lanes = 4;         // threads per atom
+    int eam_stage = 0;         // 1: stage spline knots in shared memory
     double eam_stage_frac = 0.35;
     int eam_ctas_per_sm = 1;
     int pair_block = 256;

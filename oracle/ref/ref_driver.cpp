@@ -248,7 +248,10 @@ int main(int argc, char** argv) {
     /* Table mode: the reference TableReader itself (treader.cpp) evaluated at
        the r values listed one per line in file `rfile`; prints r val dval. */
     if (opt.count("tabfile")) {
-        TableReader t(opt["tabfile"][0], opt.count("tabname") ? opt["tabname"][0] : std::string(""));
+        /* default-construct, then open(): the path TForceEAM::Init takes (team.cpp:211);
+           the two-argument constructor resets the format to PLAIN after opening */
+        TableReader t;
+        t.open(opt["tabfile"][0], opt.count("tabname") ? opt["tabname"][0] : std::string(""));
         FILE* rf = fopen(opt["rfile"][0].c_str(), "r");
         FILE* of = fopen((outdir + "/table.txt").c_str(), "w");
         double r;

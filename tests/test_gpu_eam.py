@@ -61,6 +61,28 @@ def test_eam_neighbour_set_bit_exact(omdg_lib, case):
     assert mine == ref
 
 
+@pytest.mark.parametrize("mode", [0, 1, 4, 8])
+def test_build_modes_give_the_reference_set(omdg_lib, mode):
+    """Cell-centric, thread-per-atom and lane-group builds all give the reference's set."""
+    d = load_case("eam_al_4000")
+    with make_eam(omdg_lib, d) as ctx:
+        ctx.set_launch("build_lanes", mode)
+        ctx.build_neighbors()
+        mine = nbr_set(*ctx.neighbors())
+    assert mine == set(map(tuple, d["nbr"].tolist()))
+
+
+@pytest.mark.parametrize("lanes,hshift", [(1, 5), (4, 3), (8, 2), (16, 1)])
+def test_eam_lane_shapes_agree(omdg_lib, lanes, hshift):
+    d = load_case("eam_al_4000")
+    with make_eam(omdg_lib, d) as ctx:
+        ctx.set_launch("eam_lanes", lanes)
+        ctx.set_launch("nbr_hshift", hshift)
+        ctx.compute_forces()
+        st = ctx.get_state()
+    check_forces(st["f"], d["f"], st["pot"], d["pot"])
+
+
 def test_eam_large_vs_oracle(omdg_lib, oracle_lib):
     """32,000 atoms: forces against the FP64 C oracle on the same input."""
     from objectmd_gb300 import inputs

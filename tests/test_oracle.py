@@ -1,0 +1,169 @@
+"""The CPU oracle against the reference's own outputs (tests/golden, made by
+tests/golden/make_golden.py from the reference's code).  No GPU needed."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLD, TABLES, load_case, nbr_set
+
+EAM_TABLE = os.path.join(TABLES, "eam.aluminum5000")
+
+
+def eam_tables(oc):
+    return tuple(oc.Table.from_file(EAM_TABLE, s) for s in ("PAIR", "EDENS", "EMBED"))
+
+
+@pytest.mark.parametrize("sec", ["PAIR", "EMBED"])
+def test_table_reader_matches_reference(oracle_lib, sec):
+    """treader.cpp:37-64 + :193-229 restated, against the reference TableReader itself."""
+    g = np.load(os.path.join(GOLD, "table_%s.npz" % sec.lower()))
+    t = oracle_lib.Table.from_file(EAM_TABLE, sec)
+    got = np.array([t.read(r) for r in g["r"]])
+    np.testing.assert_array_equal(got[:, 0], g["val"])
+    np.testing.assert_array_equal(got[:, 1], g["dval"])
+
+
+def test_table_out_of_range_is_an_error(oracle_lib):
+    t = oracle_lib.Table.from_file(EAM_TABLE, "PAIR")
+    with pytest.raises(ValueError):
+        t.read(t.max_range() + 2.5 * t.spec["dr"])
+
+
+@pytest.mark.parametrize("case", ["eam_al_500", "eam_al_4000"])
+def test_eam_oracle_matches_reference(oracle_lib, case):
+    oc = oracle_lib
+    d = load_case(case)
+    phi, ed, em = eam_tables(oc)
+    box = oc.make_box(d["box_lo"], d["box_hi"], (1, 1, 1))
+    x = oc.wrap(box, d["x0"])
+    nb = oc.neighbors(box, x, phi.max_range() + 0.3)
+    f, e, vir, rho = oc.eam(box, x, nb, phi, ed, em)
+    assert np.abs(f - d["f"]).max() < 1e-12
+    assert np.abs(e - d["pot"]).max() < 1e-12
+    assert np.abs(vir - d["vir"]).max() < 1e-10
+    assert nbr_set(*nb) == set(map(tuple, d["nbr"].tolist()))
+
+
+def test_pair_oracle_matches_reference(oracle_lib):
+    oc = oracle_lib
+    d = load_case("lj_ar_500")
+    phi = oc.Table.from_file(os.path.join(TABLES, "pair.lj.argon"), "")
+    box = oc.make_box(d["box_lo"], d["box_hi"], (1, 1, 1))
+    x = oc.wrap(box, d["x0"])
+    nb = oc.neighbors(box, x, phi.max_range() + 0.3)
+    f, e, vir = oc.pair_table(box, x, nb, phi)
+    assert np.abs(f - d["f"]).max() < 1e-14
+    assert np.abs(e - d["pot"]).max() < 1e-14
+    assert nbr_set(*nb) == set(map(tuple, d["nbr"].tolist()))
+
+
+def sw_params(oc):
+    return oc.SWParam(eps=2.1683, A=7.049556277, B=0.6022245584, p=4, q=0, sigma=2.0951, a=1.80, lam=21.0,
+                      gamma=1.2, icos0=-3.0, usezbl=1, sx0=1.2107, sx1=1.8456, sa0=335.0594, sa1=-492.3905,
+                      sa2=244.5280, sa3=-41.2347, z1=14, z2=14)
+
+
+@pytest.mark.parametrize("case", ["sw_si_216", "sw_si_1000"])
+def test_sw_oracle_matches_fixed_reference(oracle_lib, case):
+    """Every triplet evaluated: equal to the reference built without the sw.cpp:261 guard."""
+    oc = oracle_lib
+    d = load_case(case)
+    box = oc.make_box(d["box_lo"], d["box_hi"], (1, 1, 1))
+    x = oc.wrap(box, d["x0"])
+    nb = oc.neighbors(box, x, 2.0951 * 1.8 + 0.3)
+    f, e, vir = oc.sw(box, x, nb, sw_params(oc))
+    assert np.abs(f - d["f"]).max() < 1e-11
+    assert np.abs(e - d["pot"]).max() < 1e-12
+    assert nbr_set(*nb) == set(map(tuple, d["nbr"].tolist()))
+
+
+def test_sw_reference_guard_drops_triplets(oracle_lib):
+    """The unmodified reference (sw.cpp:261) differs from the full triplet sum."""
+    d = load_case("sw_si_216")
+    assert np.abs(d["f_asis"] - d["f"]).max() > 1e-3
+
+
+def test_sw_forces_are_energy_gradients(oracle_lib):
+    """Finite-difference check of the oracle's SW (away from the ZBL/spline core)."""
+    oc = oracle_lib
+    d = load_case("sw_si_216")
+    box = oc.make_box(d["box_lo"], d["box_hi"], (1, 1, 1))
+    x = oc.wrap(box, d["x0"])
+    rv = 2.0951 * 1.8 + 0.3
+    p = sw_params(oc)
+    f, e, _ = oc.sw(box, x, oc.neighbors(box, x, rv), p)
+    h = 1e-5
+    for atom in (0, 17, 101):
+        for q in range(3):
+            xp = x.copy()
+            xp[atom, q] += h
+            xm = x.copy()
+            xm[atom, q] -= h
+            ep = oc.sw(box, xp, oc.neighbors(box, xp, rv), p)[1].sum()
+            em = oc.sw(box, xm, oc.neighbors(box, xm, rv), p)[1].sum()
+            assert abs(-(ep - em) / (2 * h) - f[atom, q]) < 2e-6
+
+
+def test_tersoff_forces_are_energy_gradients(oracle_lib):
+    """Tersoff has no running reference (tersoff.h does not compile); its oracle is
+    pinned by energy-force consistency and the diamond cohesive energy."""
+    oc = oracle_lib
+    from objectmd_gb300 import inputs
+
+    p = oc.TersoffParam(A=3264.7, B=95.373, lambda1=3.2394, lambda2=1.3258, lambda3=1.3258, beta=0.33675, n=22.956,
+                        c=4.8381, d=2.0417, h=0.0, R=2.7, D=0.15)
+    x, v, (lo, hi) = inputs.diamond_silicon(ncell=3, a=5.431, sigma=0.06, temp=1000.0, seed_pos=8, seed_vel=9)
+    box = oc.make_box(lo, hi, (1, 1, 1))
+    rv = 2.85 + 0.3
+    f, e, _ = oc.tersoff(box, x, oc.neighbors(box, x, rv), p)
+    h = 1e-5
+    for atom in (0, 33, 150):
+        for q in range(3):
+            xp = x.copy()
+            xp[atom, q] += h
+            xm = x.copy()
+            xm[atom, q] -= h
+            ep = oc.tersoff(box, xp, oc.neighbors(box, xp, rv), p)[1].sum()
+            em = oc.tersoff(box, xm, oc.neighbors(box, xm, rv), p)[1].sum()
+            assert abs(-(ep - em) / (2 * h) - f[atom, q]) < 2e-6
+    # perfect diamond at a = 5.431: Tersoff (1988) Si cohesive energy 4.63 eV/atom
+    x0, lo, hi = inputs.diamond(3, 5.431)
+    box = oc.make_box(lo, hi, (1, 1, 1))
+    e0 = oc.tersoff(box, x0, oc.neighbors(box, x0, rv), p)[1]
+    assert abs(e0.mean() + 4.63) < 0.01
+
+
+def test_velocity_verlet_oracle_matches_reference_trajectory(oracle_lib):
+    """20 NVE steps with the reference's first-step rule (forces zeroed after FirstRun)."""
+    oc = oracle_lib
+    from objectmd_gb300 import inputs
+
+    d = load_case("eam_al_nve")
+    phi, ed, em = eam_tables(oc)
+    box = oc.make_box(d["box_lo"], d["box_hi"], (1, 1, 1))
+    x = oc.wrap(box, d["x0"])
+    v = d["v0"].copy()
+    n = len(x)
+    mass = np.full(n, inputs.md_mass("aluminum"))
+    rv = phi.max_range() + 0.3
+    f = np.zeros((n, 3))
+    dt = float(d["dt"])
+    kin = []
+    for step in range(int(d["steps"])):
+        oc.vv_kick_drift(x, v, f, mass, dt)
+        x = oc.wrap(box, x)
+        fr, e, vir, rho = oc.eam(box, x, oc.neighbors(box, x, rv), phi, ed, em)
+        f = fr
+        oc.vv_kick(v, f, mass, dt)
+        kin.append(oc.kinetic(v, mass))
+    L = d["box_hi"] - d["box_lo"]
+    dx = x - d["x"]
+    dx -= np.round(dx / L) * L
+    assert np.abs(dx).max() < 1e-10
+    np.testing.assert_allclose(kin, d["ledger"][1:1 + len(kin), 1], rtol=1e-10)
+
+
+def test_berendsen_factor(oracle_lib):
+    # TempController.h:86: sqrt(1 + dt/tau (T0/T - 1))
+    assert abs(oracle_lib.berendsen_factor(0.002, 0.05, 300.0, 600.0) - np.sqrt(1 + 0.04 * (0.5 - 1))) < 1e-15

@@ -142,8 +142,22 @@ int omdg_ledger(omdg_ctx* ctx, double* kinetic, double* potential, double* base_
 /* Per-step ledger rows (kinetic, potential) of the last omdg_step call, up to cap rows. */
 int omdg_ledger_history(omdg_ctx* ctx, double* kinetic, double* potential, int cap, int* rows);
 
-/* TempController(T, tau) (TempController.h:51-91); tau <= 0 removes it. */
+/* TempController(T, tau) (TempController.h:51-91); tau <= 0 removes it.
+   The temperature is 2/3 KE / (N k_B) over the box's atoms. */
 int omdg_set_thermostat(omdg_ctx* ctx, double temperature, double tau);
+
+/*
+ * Reference-compatibility switches for behaviour of the reference that this
+ * library does not take by default:
+ *   "first_step_zero_force"    FirstRun zeroes the forces it computed, so the
+ *                              first half kick uses f = 0 (system.cpp:872);
+ *                              same as omdg_set_first_step_mode; default on.
+ *   "thermostat_counts_ghosts" TempController divides the kinetic energy by
+ *                              GetTotalAtom(), which on the periodic
+ *                              MDSystemGrid counts the ghost images too
+ *                              (system.h:337); default off.
+ */
+int omdg_set_compat(omdg_ctx* ctx, const char* key, int on);
 
 /* Number of neighbour-list builds so far and of kernel launches issued by the last omdg_step. */
 int omdg_stats(omdg_ctx* ctx, long* rebuilds, long* launches);

@@ -379,7 +379,9 @@ int omdg_get_state(omdg_ctx* c, double* x, double* v, double* f, double* pot, do
     if (!c) return OMDG_EINVAL;
     if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
     cudaSetDevice(c->device);
-    int rc = io_get_state(c, x, v, f, pot, vir);
+    int rc = v ? resolve_thermostat(c) : OMDG_OK;
+    if (rc) return rc;
+    rc = io_get_state(c, x, v, f, pot, vir);
     if (rc) return rc;
     return check_cuda(c, cudaStreamSynchronize(c->stream), "state read-back");
 }
@@ -400,7 +402,10 @@ int omdg_set_velocities(omdg_ctx* c, const double* v) {
     if (!c || !v) return OMDG_EINVAL;
     if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
     cudaSetDevice(c->device);
-    int rc = io_set_state(c, nullptr, v);
+    // velocities given by the caller replace any pending thermostat factor
+    int rc = drop_thermostat_factor(c);
+    if (rc) return rc;
+    rc = io_set_state(c, nullptr, v);
     if (rc) return rc;
     return check_cuda(c, cudaStreamSynchronize(c->stream), "velocity upload");
 }
@@ -910,6 +915,16 @@ int omdg_set_first_step_mode(omdg_ctx* c, int reference_first_step) {
     return OMDG_OK;
 }
 
+int omdg_set_compat(omdg_ctx* c, const char* key, int on) {
+    if (!c || !key) return OMDG_EINVAL;
+    std::string k(key);
+    if (k == "first_step_zero_force") c->reference_first_step = on != 0;
+    else if (k == "thermostat_counts_ghosts") c->thermo_count_ghosts = on != 0;
+    else return set_error(c, OMDG_EINVAL, "unknown compatibility key " + k);
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
 int omdg_set_thermostat(omdg_ctx* c, double temperature, double tau) {
     if (!c) return OMDG_EINVAL;
     c->thermo_T = temperature;
@@ -966,6 +981,7 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         c->graph_steps += nsteps;
     }
     c->async_steps += nsteps;
+    if (nsteps > 0 && c->thermo_tau > 0.0) c->lambda_pending = true;
     return OMDG_OK;
 }
 

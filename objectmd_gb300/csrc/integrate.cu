@@ -30,7 +30,6 @@ struct IntParams {
     double org[3], P[3];
     float half_skin2;       // (skin/2)^2
     int use_f64;
-    int thermostat;         // apply the velocity factor of the previous step
     double Q[3];            // P - org: the pack coordinate is X = x + Q
 };
 
@@ -73,12 +72,8 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
             ay = fy[i];
             az = fz[i];
         }
-        double ux = vx[i], uy = vy[i], uz = vz[i];
-        if (p.thermostat) {
-            ux *= lam;
-            uy *= lam;
-            uz *= lam;
-        }
+        // pending thermostat factor (exactly 1.0 when none is pending)
+        double ux = vx[i] * lam, uy = vy[i] * lam, uz = vz[i] * lam;
         ux = fma(ax, h, ux);
         uy = fma(ay, h, uy);
         uz = fma(az, h, uz);
@@ -170,6 +165,7 @@ struct FinParams {
     int natoms;
     int ledger_cap;
     int count_step;       // 1: this is a RunKernel step (advance Step)
+    const int* ghosts;    // reference compatibility: periodic images added to the atom count (or null)
     double dt, tau, tset; // thermostat (tau <= 0: off)
     double temp_factor;   // 2/3/k_B (unit.h:66-104)
 };
@@ -208,17 +204,47 @@ __global__ void k_finalize(FinParams p, const double* __restrict__ partial, doub
         double lam = 1.0;
         if (p.count_step && p.tau > 0.0 && st->step != 0) {
             // TempController::PostIntegration: T from the system kinetic energy
-            double T = p.temp_factor * kinetic / (double)p.natoms;
+            const double count = (double)p.natoms + (p.ghosts ? (double)*p.ghosts : 0.0);
+            double T = p.temp_factor * kinetic / count;
             if (T > 0.0) lam = sqrt(1. + p.dt / p.tau * (p.tset / T - 1.));
         }
         ledger[4 * slot + 3] = lam;
-        st->lambda = lam;
         if (p.count_step) {
+            st->lambda = lam;
             st->step += 1;
             st->row = row + 1;
             if (st->rebuild_every > 0 && (st->step % st->rebuild_every) == 0) st->rebuild = 1;
         }
     }
+}
+
+struct GhostParams {
+    int n;
+    double lo[3], hi[3], L[3], rv;
+    int periodic[3];
+};
+
+__global__ void k_zero_counter(int* c) { *c = 0; }
+
+// Periodic images the reference would hold as ghosts (comhandler.cpp:647-755:
+// an atom closer than Rv to a face of a periodic axis is sent across it).
+__global__ void k_count_ghosts(GhostParams g, const double* __restrict__ x, const double* __restrict__ y,
+                               const double* __restrict__ z, int* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int images = 0;
+    if (i < g.n) {
+        const double p[3] = {x[i], y[i], z[i]};
+        int prod = 1;
+        for (int d = 0; d < 3; d++) {
+            if (!g.periodic[d]) continue;
+            double w = p[d] - floor((p[d] - g.lo[d]) / g.L[d]) * g.L[d];
+            prod *= 1 + (w < g.lo[d] + g.rv) + (w > g.hi[d] - g.rv);
+        }
+        images = prod - 1;
+    }
+    // integer sums are order independent
+    for (int off = 16; off > 0; off >>= 1) images += __shfl_xor_sync(0xffffffffu, images, off);
+    if ((threadIdx.x & 31) == 0 && images) atomicAdd(out, images);
 }
 
 // ------------------------------------------------------------------ host
@@ -235,7 +261,6 @@ static IntParams int_params(Context* c) {
     float hs = (float)(0.5 * c->skin);
     p.half_skin2 = hs * hs;
     p.use_f64 = c->use_f64 ? 1 : 0;
-    p.thermostat = c->thermo_tau > 0.0 ? 1 : 0;
     for (int d = 0; d < 3; d++) p.Q[d] = c->box.P[d] - c->box.org[d];
     return p;
 }
@@ -267,6 +292,27 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
     f.tau = c->thermo_tau;
     f.tset = c->thermo_T;
     f.temp_factor = 2.0 / 3.0 / 8.61734279e-05;
+    f.ghosts = nullptr;
+    if (c->thermo_count_ghosts && count_step && c->thermo_tau > 0.0) {
+        // TempController::GetSystemTemperature divides by GetTotalAtom(), which
+        // on MDSystemGrid is GetNAtom(): owners plus their periodic ghost images
+        // (system.h:337, TempController.h:73-76).  Count those images: per
+        // periodic axis an atom within Rv of a face has one more image.
+        GhostParams g;
+        g.n = c->n;
+        double rv = c->rc_max + c->skin;
+        for (int d = 0; d < 3; d++) {
+            g.lo[d] = c->box.lo[d];
+            g.hi[d] = c->box.hi[d];
+            g.L[d] = c->box.L[d];
+            g.periodic[d] = c->box.periodic[d];
+        }
+        g.rv = rv;
+        k_zero_counter<<<1, 1, 0, c->stream>>>(c->d_flags + 2);
+        k_count_ghosts<<<grid_for(c->n, 256), 256, 0, c->stream>>>(g, c->x, c->y, c->z, c->d_flags + 2);
+        c->launches += 2;
+        f.ghosts = c->d_flags + 2;
+    }
     prof_begin(c, "finalize");
     k_finalize<<<1, 256, 0, c->stream>>>(f, c->d_red, c->d_ledger, reinterpret_cast<StepState*>(c->d_state));
     prof_end(c);
@@ -326,6 +372,39 @@ int step_state_init(Context* c) {
 }
 
 __global__ void k_clear_rebuild(StepState* st) { st->rebuild = 0; }
+
+// The reference scales velocities at the end of the step
+// (TempController::PostIntegration); here the factor waits in the step state
+// until the next kick.  Apply it before the caller reads velocities.
+__global__ void k_apply_lambda(int n, double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
+                               const StepState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double lam = st->lambda;
+    vx[i] *= lam;
+    vy[i] *= lam;
+    vz[i] *= lam;
+}
+
+__global__ void k_reset_lambda(StepState* st) { st->lambda = 1.0; }
+
+int resolve_thermostat(Context* c) {
+    if (!c->lambda_pending) return OMDG_OK;
+    StepState* st = reinterpret_cast<StepState*>(c->d_state);
+    k_apply_lambda<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->vx, c->vy, c->vz, st);
+    k_reset_lambda<<<1, 1, 0, c->stream>>>(st);
+    c->launches += 2;
+    c->lambda_pending = false;
+    return check_cuda(c, cudaGetLastError(), "thermostat factor");
+}
+
+int drop_thermostat_factor(Context* c) {
+    if (!c->lambda_pending) return OMDG_OK;
+    k_reset_lambda<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state));
+    c->launches += 1;
+    c->lambda_pending = false;
+    return check_cuda(c, cudaGetLastError(), "thermostat factor");
+}
 
 // Flags a rebuild when positions written by the caller moved an atom more
 // than skin/2 from where the list was built.

@@ -212,6 +212,8 @@ struct Context {
     bool reference_first_step = true;
     long step = 0;
     double thermo_T = 0, thermo_tau = 0;
+    bool thermo_count_ghosts = false;  // reference compatibility (omdg_set_compat)
+    bool lambda_pending = false;       // a thermostat factor waits in the step state
 
     // device status and reductions
     unsigned* d_status = nullptr;   // error bits
@@ -264,6 +266,8 @@ int integrate_pack(Context* c);
 int measure_energies(Context* c, int row);
 int zero_forces(Context* c);
 int request_rebuild(Context* c);
+int resolve_thermostat(Context* c);
+int drop_thermostat_factor(Context* c);
 int step_state_graph_rebuilds(Context* c, int* nrebuild);
 
 // caller-order transfers (io.cu); asynchronous on the context stream

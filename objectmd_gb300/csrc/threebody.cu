@@ -1,11 +1,545 @@
-// Three-body kernels (Stillinger-Weber, Tersoff) and the ZBL pair.
+// Three-body potentials, owner-computes in two passes over the full Verlet
+// list (no atomics, deterministic):
+//
+//   pass A  for atom i: every term centred on i -- the two-body halves of
+//           i's pairs and the triplets (SW, sw.cpp:166-236) or bonds
+//           (Tersoff) whose centre is i.  The force and energy a term gives
+//           to i accumulate in registers; what it gives to a neighbour j is
+//           written to j's slot in i's row of a per-slot buffer.
+//   pass B  for atom i: own part + sum over i's slots s of the buffer entry
+//           its neighbour j wrote for i (slot rev(i,s) of j's row).
+//
+// FP32 arithmetic on relative vectors from the FP64 positions, Kahan sums in
+// pass B.  Per-atom energies follow the reference: each pair half to each
+// atom, V3/3 to each triplet member (sw.cpp:182-233); Tersoff: 1/2 V_ij to i.
 #include "device_common.cuh"
 
 namespace omdg {
 
+constexpr int TB_MAXN = 24;  // neighbours within the cutoff one atom can hold
+
+struct SWDev {
+    int n, hshift, maxnb, single_type, ta;
+    ShiftF L;
+    float rc, rc2;
+    float A, B, p, q, sigma, eps;
+    float c1, c2, c3, c4, c5, c6, c7, c8, c9, c10;
+    int usezbl;
+    float sx0, sx1, sa0, sa1, sa2, sa3;
+    float zc, ze0, ze1, ze2, ze3;
+    int first;
+};
+
+__device__ __forceinline__ void sw_two_body(const SWDev& p, float r, float& fr, float& half_e) {
+    if (p.usezbl && r < p.sx0) {
+        // sw.cpp:118-146
+        const float rinv = 1.0f / r;
+        const float f0 = 0.1818f * expf(-p.ze0 * r), f1 = 0.5099f * expf(-p.ze1 * r);
+        const float f2 = 0.2802f * expf(-p.ze2 * r), f3 = 0.02817f * expf(-p.ze3 * r);
+        const float fpot = (f0 + f1 + f2 + f3) * p.zc * rinv;
+        fr = ((rinv + p.ze0) * f0 + (rinv + p.ze1) * f1 + (rinv + p.ze2) * f2 + (rinv + p.ze3) * f3) * p.zc *
+             (rinv * rinv);
+        half_e = 0.5f * fpot;
+    } else if (p.usezbl && r < p.sx1) {
+        // sw.cpp:148-164 (force factor applied with the opposite sign)
+        const float f = p.sa1 + p.sa2 * r + p.sa3 * r * r;
+        fr = -f;
+        half_e = 0.5f * (p.sa0 + f * r);
+    } else {
+        // sw.cpp:166-189
+        const float ira = 1.0f / (r - p.rc);
+        const float rp = powf(r, -p.p), rq = powf(r, -p.q);
+        const float fex = expf(p.sigma * ira);
+        fr = (p.c1 * rp - p.c2 * rq + (p.c3 * rp - p.c4 * rq) * ira * ira * r) * fex / (r * r);
+        half_e = 0.5f * (p.c5 * rp - p.c6 * rq) * fex;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_sw_a(SWDev p, const PosPack* __restrict__ pack,
+                                              const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                              float4* __restrict__ slot, float* __restrict__ fx,
+                                              float* __restrict__ fy, float* __restrict__ fz, float* __restrict__ pe,
+                                              unsigned* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const PosPack pi = pack[i];
+    const int ti = pack_type(pi.hi);
+    const bool mine = p.single_type || ti == p.ta;
+    const int m = nnb[i];
+    // neighbours inside the cutoff, vectors from i to the neighbour
+    float vx[TB_MAXN], vy[TB_MAXN], vz[TB_MAXN], rr[TB_MAXN];
+    int sl[TB_MAXN];
+    int nc = 0;
+    float ax = 0.f, ay = 0.f, az = 0.f, ae = 0.f;
+    for (int s = 0; s < m; s++) {
+        const size_t at = nbr_at(i, s, p.hshift, p.maxnb);
+        slot[at] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!mine) continue;
+        const unsigned e = nbr[at];
+        const int j = nbr_index(e);
+        const PosPack pj = pack[j];
+        if (!p.single_type && pack_type(pj.hi) != p.ta) continue;
+        const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, p.L);  // x_i - x_j
+        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        if (!(r2 < p.rc2)) continue;
+        const float r = sqrtf(r2);
+        float fr, he;
+        sw_two_body(p, r, fr, he);
+        ax += d.x * fr;
+        ay += d.y * fr;
+        az += d.z * fr;
+        ae += he;
+        if (nc < TB_MAXN) {
+            vx[nc] = -d.x;
+            vy[nc] = -d.y;
+            vz[nc] = -d.z;
+            rr[nc] = r;
+            sl[nc] = s;
+        } else {
+            atomicOr(status, ERR_NBR_OVERFLOW);
+        }
+        nc++;
+    }
+    if (nc > TB_MAXN) nc = TB_MAXN;
+    // triplets centred on i (sw.cpp:191-236), each unordered pair (j, k) once
+    for (int a = 0; a < nc; a++) {
+        const float r1 = rr[a], dx1 = vx[a], dy1 = vy[a], dz1 = vz[a];
+        const float ira0 = 1.0f / (r1 - p.rc), fira0 = p.c7 * ira0;
+        const float ex0 = expf(fira0);
+        float gjx = 0.f, gjy = 0.f, gjz = 0.f, gje = 0.f;
+        for (int b = a + 1; b < nc; b++) {
+            const float r2_ = rr[b], dx2 = vx[b], dy2 = vy[b], dz2 = vz[b];
+            const float ira1 = 1.0f / (r2_ - p.rc), fira1 = p.c7 * ira1;
+            const float ir1r2 = 1.0f / (r1 * r2_);
+            const float fex = ex0 * expf(fira1);
+            const float cs = (dx1 * dx2 + dy1 * dy2 + dz1 * dz2) * ir1r2;
+            const float dcos = cs - p.c10;
+            const float ftheta = p.c9 * fex * dcos;
+            const float ft12 = ir1r2 * ftheta;
+            const float fpot = p.c8 * fex * dcos * dcos;
+            const float fcos = cs * ftheta;
+            const float fr0 = fpot * fira0 * ira0 / r1, fr1 = fpot * fira1 * ira1 / r2_;
+            const float ft0 = fcos / (r1 * r1), ft1 = fcos / (r2_ * r2_);
+            const float fx0 = dx1 * (fr0 + ft0) - dx2 * ft12, fx1 = dx2 * (fr1 + ft1) - dx1 * ft12;
+            const float fy0 = dy1 * (fr0 + ft0) - dy2 * ft12, fy1 = dy2 * (fr1 + ft1) - dy1 * ft12;
+            const float fz0 = dz1 * (fr0 + ft0) - dz2 * ft12, fz1 = dz2 * (fr1 + ft1) - dz1 * ft12;
+            ax -= fx0 + fx1;
+            ay -= fy0 + fy1;
+            az -= fz0 + fz1;
+            const float third = fpot * (1.0f / 3.0f);
+            ae += third;
+            gjx += fx0;
+            gjy += fy0;
+            gjz += fz0;
+            gje += third;
+            // the k member's share goes straight to its slot (it is a later slot)
+            const size_t atk = nbr_at(i, sl[b], p.hshift, p.maxnb);
+            float4 cur = slot[atk];
+            cur.x += fx1;
+            cur.y += fy1;
+            cur.z += fz1;
+            cur.w += third;
+            slot[atk] = cur;
+        }
+        const size_t atj = nbr_at(i, sl[a], p.hshift, p.maxnb);
+        float4 cur = slot[atj];
+        cur.x += gjx;
+        cur.y += gjy;
+        cur.z += gjz;
+        cur.w += gje;
+        slot[atj] = cur;
+    }
+    if (p.first) {
+        fx[i] = ax;
+        fy[i] = ay;
+        fz[i] = az;
+        pe[i] = ae;
+    } else {
+        fx[i] += ax;
+        fy[i] += ay;
+        fz[i] += az;
+        pe[i] += ae;
+    }
+}
+
+// Gathers what every neighbour's pass A left for i; clears no state.
+__global__ void __launch_bounds__(128) k_slot_gather(int n, int hshift, int maxnb, const unsigned* __restrict__ nbr,
+                                                     const int* __restrict__ nnb, const int* __restrict__ rev,
+                                                     const float4* __restrict__ slot, float* __restrict__ fx,
+                                                     float* __restrict__ fy, float* __restrict__ fz,
+                                                     float* __restrict__ pe, float* __restrict__ vir,
+                                                     int zero_virial) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Kahan gx, gy, gz, ge;
+    gx.add(fx[i]);
+    gy.add(fy[i]);
+    gz.add(fz[i]);
+    ge.add(pe[i]);
+    const int m = nnb[i];
+    for (int s = 0; s < m; s++) {
+        const size_t at = nbr_at(i, s, hshift, maxnb);
+        const int j = nbr_index(nbr[at]);
+        const float4 c = slot[nbr_at(j, rev[at], hshift, maxnb)];
+        gx.add(c.x);
+        gy.add(c.y);
+        gz.add(c.z);
+        ge.add(c.w);
+    }
+    fx[i] = gx.value();
+    fy[i] = gy.value();
+    fz[i] = gz.value();
+    pe[i] = ge.value();
+    if (zero_virial) vir[i] = 0.f;  // the reference SW does not accumulate a virial (sw.cpp:238)
+}
+
+// ------------------------------------------------------------------ Tersoff
+struct TersDev {
+    int n, hshift, maxnb, single_type, ta;
+    ShiftF L;
+    float A, B, l1, l2, l3c, beta, nn, c2, d2, h, R, D, rc, rc2;
+    int first;
+};
+
+__device__ __forceinline__ float ters_fc(const TersDev& p, float r, float& dfc) {
+    if (r < p.R - p.D) {
+        dfc = 0.f;
+        return 1.f;
+    }
+    if (r < p.R + p.D) {
+        const float arg = 1.57079632679489662f * (r - p.R) / p.D;  // pi (r-R) / (2D)
+        float sn, cs;
+        sincosf(arg, &sn, &cs);
+        dfc = -0.78539816339744831f / p.D * cs;  // -pi/(4D) cos
+        return 0.5f - 0.5f * sn;
+    }
+    dfc = 0.f;
+    return 0.f;
+}
+
+__global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __restrict__ pack,
+                                                   const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                                   float4* __restrict__ slot, float* __restrict__ fx,
+                                                   float* __restrict__ fy, float* __restrict__ fz,
+                                                   float* __restrict__ pe, float* __restrict__ vir, unsigned* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const PosPack pi = pack[i];
+    const bool mine = p.single_type || pack_type(pi.hi) == p.ta;
+    const int m = nnb[i];
+    float ux[TB_MAXN], uy[TB_MAXN], uz[TB_MAXN], rr[TB_MAXN];
+    int sl[TB_MAXN];
+    int nc = 0;
+    for (int s = 0; s < m; s++) {
+        const size_t at = nbr_at(i, s, p.hshift, p.maxnb);
+        slot[at] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!mine) continue;
+        const unsigned e = nbr[at];
+        const PosPack pj = pack[nbr_index(e)];
+        if (!p.single_type && pack_type(pj.hi) != p.ta) continue;
+        const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, p.L);
+        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        if (!(r2 < p.rc2)) continue;
+        const float r = sqrtf(r2);
+        if (!(r < p.rc)) continue;
+        if (nc < TB_MAXN) {
+            const float ri = 1.0f / r;
+            ux[nc] = -d.x * ri;  // unit vector from i to the neighbour
+            uy[nc] = -d.y * ri;
+            uz[nc] = -d.z * ri;
+            rr[nc] = r;
+            sl[nc] = s;
+        } else {
+            atomicOr(status, ERR_NBR_OVERFLOW);
+        }
+        nc++;
+    }
+    if (nc > TB_MAXN) nc = TB_MAXN;
+    float fix = 0.f, fiy = 0.f, fiz = 0.f, ei = 0.f, wi = 0.f;
+    for (int a = 0; a < nc; a++) {
+        const float rij = rr[a];
+        const float ex_ = ux[a], ey_ = uy[a], ez_ = uz[a];
+        // zeta_ij and its gradient w.r.t. x_j (the x_k parts are applied below)
+        float zeta = 0.f, gjx = 0.f, gjy = 0.f, gjz = 0.f;
+        for (int b = 0; b < nc; b++) {
+            if (b == a) continue;
+            const float rik = rr[b];
+            const float cs = ex_ * ux[b] + ey_ * uy[b] + ez_ * uz[b];
+            float dfc;
+            const float fc = ters_fc(p, rik, dfc);
+            const float hc = p.h - cs;
+            const float den = p.d2 + hc * hc;
+            const float g = 1.f + p.c2 / p.d2 - p.c2 / den;
+            const float dg = -2.f * p.c2 * hc / (den * den);
+            const float dr = rij - rik;
+            const float ex = expf(p.l3c * dr * dr * dr);
+            const float dex = 3.f * p.l3c * dr * dr * ex;
+            zeta += fc * g * ex;
+            const float cj = fc * dg * ex / rij, cu = fc * g * dex;
+            gjx += cj * (ux[b] - cs * ex_) + cu * ex_;
+            gjy += cj * (uy[b] - cs * ey_) + cu * ey_;
+            gjz += cj * (uz[b] - cs * ez_) + cu * ez_;
+        }
+        float dfc_ij;
+        const float fc_ij = ters_fc(p, rij, dfc_ij);
+        const float fR = p.A * expf(-p.l1 * rij), fA = p.B * expf(-p.l2 * rij);
+        const float bn = powf(p.beta * zeta, p.nn);
+        const float bij = powf(1.f + bn, -0.5f / p.nn);
+        const float dbdz = zeta > 0.f ? -0.5f * powf(1.f + bn, -0.5f / p.nn - 1.f) * bn / zeta : 0.f;
+        const float vij = fc_ij * (fR - bij * fA);
+        const float dv_dr = dfc_ij * (fR - bij * fA) + fc_ij * (-p.l1 * fR + bij * p.l2 * fA);
+        const float dv_dz = -fc_ij * fA * dbdz;
+        // gradient of 1/2 V_ij: x_j part
+        float sjx = 0.5f * (dv_dr * ex_ + dv_dz * gjx);
+        float sjy = 0.5f * (dv_dr * ey_ + dv_dz * gjy);
+        float sjz = 0.5f * (dv_dr * ez_ + dv_dz * gjz);
+        fix += sjx;  // the x_i gradient is minus the sum of the others
+        fiy += sjy;
+        fiz += sjz;
+        // x_k parts
+        for (int b = 0; b < nc; b++) {
+            if (b == a) continue;
+            const float rik = rr[b];
+            const float cs = ex_ * ux[b] + ey_ * uy[b] + ez_ * uz[b];
+            float dfc;
+            const float fc = ters_fc(p, rik, dfc);
+            const float hc = p.h - cs;
+            const float den = p.d2 + hc * hc;
+            const float g = 1.f + p.c2 / p.d2 - p.c2 / den;
+            const float dg = -2.f * p.c2 * hc / (den * den);
+            const float dr = rij - rik;
+            const float ex = expf(p.l3c * dr * dr * dr);
+            const float dex = 3.f * p.l3c * dr * dr * ex;
+            const float ck = dfc * g * ex - fc * g * dex, cc = fc * dg * ex / rik;
+            const float s = 0.5f * dv_dz;
+            const float kx = s * (ck * ux[b] + cc * (ex_ - cs * ux[b]));
+            const float ky = s * (ck * uy[b] + cc * (ey_ - cs * uy[b]));
+            const float kz = s * (ck * uz[b] + cc * (ez_ - cs * uz[b]));
+            fix += kx;
+            fiy += ky;
+            fiz += kz;
+            // force on k = -gradient
+            const size_t atk = nbr_at(i, sl[b], p.hshift, p.maxnb);
+            float4 cur = slot[atk];
+            cur.x -= kx;
+            cur.y -= ky;
+            cur.z -= kz;
+            slot[atk] = cur;
+        }
+        const size_t atj = nbr_at(i, sl[a], p.hshift, p.maxnb);
+        float4 cur = slot[atj];
+        cur.x -= sjx;
+        cur.y -= sjy;
+        cur.z -= sjz;
+        slot[atj] = cur;
+        ei += 0.5f * vij;
+        wi += 0.5f * dv_dr * rij;
+    }
+    if (p.first) {
+        fx[i] = fix;
+        fy[i] = fiy;
+        fz[i] = fiz;
+        pe[i] = ei;
+        vir[i] = wi;
+    } else {
+        fx[i] += fix;
+        fy[i] += fiy;
+        fz[i] += fiz;
+        pe[i] += ei;
+        vir[i] += wi;
+    }
+}
+
+// ------------------------------------------------------------------ ZBL pair
+struct ZBLDev {
+    int n, hshift, maxnb, ta, tb;
+    ShiftF L;
+    float rc, rsw, zc, ze0, ze1, ze2, ze3;
+    int first;
+};
+
+// Universal ZBL screened Coulomb (sw.cpp:118-146 form), multiplied by a
+// smooth switch S(r) that goes from 1 at rsw to 0 at rc.
+__global__ void __launch_bounds__(128) k_zbl(ZBLDev p, const PosPack* __restrict__ pack,
+                                             const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                             float* __restrict__ fx, float* __restrict__ fy, float* __restrict__ fz,
+                                             float* __restrict__ pe, float* __restrict__ vir) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const PosPack pi = pack[i];
+    const int ti = pack_type(pi.hi);
+    float ax = 0.f, ay = 0.f, az = 0.f, ae = 0.f, av = 0.f;
+    if (ti == p.ta || ti == p.tb) {
+        const int m = nnb[i];
+        for (int s = 0; s < m; s++) {
+            const unsigned e = nbr[nbr_at(i, s, p.hshift, p.maxnb)];
+            const PosPack pj = pack[nbr_index(e)];
+            const int tj = pack_type(pj.hi);
+            if (!((ti == p.ta && tj == p.tb) || (ti == p.tb && tj == p.ta))) continue;
+            const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, p.L);
+            const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+            const float r = sqrtf(r2);
+            if (!(r < p.rc)) continue;
+            const float rinv = 1.f / r;
+            const float f0 = 0.1818f * expf(-p.ze0 * r), f1 = 0.5099f * expf(-p.ze1 * r);
+            const float f2 = 0.2802f * expf(-p.ze2 * r), f3 = 0.02817f * expf(-p.ze3 * r);
+            const float phi = (f0 + f1 + f2 + f3) * p.zc * rinv;
+            const float dphi = -((rinv + p.ze0) * f0 + (rinv + p.ze1) * f1 + (rinv + p.ze2) * f2 +
+                                 (rinv + p.ze3) * f3) * p.zc * rinv;
+            float S = 1.f, dS = 0.f;
+            if (r > p.rsw) {
+                const float t = (r - p.rsw) / (p.rc - p.rsw);
+                S = 1.f - t * t * t * (10.f - 15.f * t + 6.f * t * t);
+                dS = -30.f * t * t * (1.f - t) * (1.f - t) / (p.rc - p.rsw);
+            }
+            const float v = phi * S;
+            const float dv = dphi * S + phi * dS;
+            const float fr = -dv * rinv;
+            ax += d.x * fr;
+            ay += d.y * fr;
+            az += d.z * fr;
+            ae += 0.5f * v;
+            av += fr * r2;
+        }
+    }
+    if (p.first) {
+        fx[i] = ax;
+        fy[i] = ay;
+        fz[i] = az;
+        pe[i] = ae;
+        vir[i] = av;
+    } else {
+        fx[i] += ax;
+        fy[i] += ay;
+        fz[i] += az;
+        pe[i] += ae;
+        vir[i] += av;
+    }
+}
+
+// ------------------------------------------------------------------ host
 int threebody_prepare(Context* c) { return OMDG_OK; }
-int sw_launch(Context* c, Potential&, bool) { return set_error(c, OMDG_EINVAL, "SW not built yet"); }
-int tersoff_launch(Context* c, Potential&, bool) { return set_error(c, OMDG_EINVAL, "Tersoff not built yet"); }
-int zbl_launch(Context* c, Potential&, bool) { return set_error(c, OMDG_EINVAL, "ZBL not built yet"); }
+
+static int gather_slots(Context* c, bool zero_virial) {
+    prof_begin(c, "slot_gather");
+    k_slot_gather<<<grid_for(c->n, 128), 128, 0, c->stream>>>(
+        c->n, c->nbr_hshift, c->maxnb, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->rev, c->slot_buf, c->fx,
+        c->fy, c->fz, c->pe, c->vir, zero_virial ? 1 : 0);
+    prof_end(c);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "slot gather");
+}
+
+int sw_launch(Context* c, Potential& pot, bool first) {
+    if (!c->rev || !c->slot_buf) return set_error(c, OMDG_ESTATE, "three-body buffers missing");
+    const SWParams& s = pot.sw;
+    SWDev p;
+    p.n = c->n;
+    p.hshift = c->nbr_hshift;
+    p.maxnb = c->maxnb;
+    p.single_type = c->ntypes == 1;
+    p.ta = pot.ta;
+    p.L = make_shift(c->box);
+    p.rc = (float)s.rc;
+    p.rc2 = (float)(s.rc * s.rc);
+    p.A = (float)s.A;
+    p.B = (float)s.B;
+    p.p = (float)s.p;
+    p.q = (float)s.q;
+    p.sigma = (float)s.sigma;
+    p.eps = (float)s.eps;
+    p.c1 = (float)s.c1;
+    p.c2 = (float)s.c2;
+    p.c3 = (float)s.c3;
+    p.c4 = (float)s.c4;
+    p.c5 = (float)s.c5;
+    p.c6 = (float)s.c6;
+    p.c7 = (float)s.c7;
+    p.c8 = (float)s.c8;
+    p.c9 = (float)s.c9;
+    p.c10 = (float)s.c10;
+    p.usezbl = s.usezbl;
+    p.sx0 = (float)s.sx0;
+    p.sx1 = (float)s.sx1;
+    p.sa0 = (float)s.sa0;
+    p.sa1 = (float)s.sa1;
+    p.sa2 = (float)s.sa2;
+    p.sa3 = (float)s.sa3;
+    p.zc = (float)s.zc;
+    p.ze0 = (float)s.ze0;
+    p.ze1 = (float)s.ze1;
+    p.ze2 = (float)s.ze2;
+    p.ze3 = (float)s.ze3;
+    p.first = first ? 1 : 0;
+    prof_begin(c, "sw_centre");
+    k_sw_a<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
+                                                        c->slot_buf, c->fx, c->fy, c->fz, c->pe, c->d_status);
+    prof_end(c);
+    c->launches++;
+    int rc = check_cuda(c, cudaGetLastError(), "sw");
+    if (rc) return rc;
+    return gather_slots(c, first);
+}
+
+int tersoff_launch(Context* c, Potential& pot, bool first) {
+    if (!c->rev || !c->slot_buf) return set_error(c, OMDG_ESTATE, "three-body buffers missing");
+    const TersoffParams& t = pot.ters;
+    TersDev p;
+    p.n = c->n;
+    p.hshift = c->nbr_hshift;
+    p.maxnb = c->maxnb;
+    p.single_type = c->ntypes == 1;
+    p.ta = pot.ta;
+    p.L = make_shift(c->box);
+    p.A = (float)t.A;
+    p.B = (float)t.B;
+    p.l1 = (float)t.lambda1;
+    p.l2 = (float)t.lambda2;
+    p.l3c = (float)(t.lambda3 * t.lambda3 * t.lambda3);
+    p.beta = (float)t.beta;
+    p.nn = (float)t.n;
+    p.c2 = (float)(t.c * t.c);
+    p.d2 = (float)(t.d * t.d);
+    p.h = (float)t.h;
+    p.R = (float)t.R;
+    p.D = (float)t.D;
+    p.rc = (float)(t.R + t.D);
+    p.rc2 = p.rc * p.rc * 1.0001f;
+    p.first = first ? 1 : 0;
+    prof_begin(c, "tersoff_centre");
+    k_tersoff_a<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr),
+                                                             c->nnb, c->slot_buf, c->fx, c->fy, c->fz, c->pe, c->vir,
+                                                             c->d_status);
+    prof_end(c);
+    c->launches++;
+    int rc = check_cuda(c, cudaGetLastError(), "tersoff");
+    if (rc) return rc;
+    return gather_slots(c, false);
+}
+
+int zbl_launch(Context* c, Potential& pot, bool first) {
+    const ZBLParams& z = pot.zbl;
+    ZBLDev p;
+    p.n = c->n;
+    p.hshift = c->nbr_hshift;
+    p.maxnb = c->maxnb;
+    p.ta = pot.ta;
+    p.tb = pot.tb;
+    p.L = make_shift(c->box);
+    p.rc = (float)z.rc;
+    p.rsw = (float)(z.rc - z.width);
+    p.zc = (float)z.zc;
+    p.ze0 = (float)z.ze0;
+    p.ze1 = (float)z.ze1;
+    p.ze2 = (float)z.ze2;
+    p.ze3 = (float)z.ze3;
+    p.first = first ? 1 : 0;
+    prof_begin(c, "zbl");
+    k_zbl<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
+                                                       c->fx, c->fy, c->fz, c->pe, c->vir);
+    prof_end(c);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "zbl");
+}
 
 }  // namespace omdg

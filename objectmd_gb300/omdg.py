@@ -59,6 +59,7 @@ SIGNATURES = {
     "omdg_ledger": [_vp, _P(_d), _P(_d), _P(_d), _P(_d)],
     "omdg_ledger_history": [_vp, _P(_d), _P(_d), _i, _P(_i)],
     "omdg_set_thermostat": [_vp, _d, _d],
+    "omdg_set_compat": [_vp, _cp, _i],
     "omdg_stats": [_vp, _P(_l), _P(_l)],
     "omdg_set_launch": [_vp, _cp, _i],
     "omdg_get_launch": [_vp, _cp, _P(_i)],
@@ -218,6 +219,9 @@ class Context:
 
     def set_thermostat(self, temperature, tau):
         self._check(self.lib.omdg_set_thermostat(self.h, float(temperature), float(tau)))
+
+    def set_compat(self, key, on=True):
+        self._check(self.lib.omdg_set_compat(self.h, key.encode(), 1 if on else 0))
 
     def step(self, nsteps=1):
         self._check(self.lib.omdg_step(self.h, int(nsteps)))

@@ -164,6 +164,38 @@ def test_velocity_verlet_oracle_matches_reference_trajectory(oracle_lib):
     np.testing.assert_allclose(kin, d["ledger"][1:1 + len(kin), 1], rtol=1e-10)
 
 
+def test_reference_thermostat_counts_ghost_images(oracle_lib):
+    """The reference's TempController divides by owners + periodic ghost images
+    (system.h:337 GetTotalAtom = GetNAtom on MDSystemGrid): replaying that rule
+    reproduces its kinetic-energy trace exactly."""
+    oc = oracle_lib
+    from objectmd_gb300 import inputs
+
+    d = load_case("eam_al_tc")
+    phi, ed, em = eam_tables(oc)
+    box = oc.make_box(d["box_lo"], d["box_hi"], (1, 1, 1))
+    lo, hi = d["box_lo"], d["box_hi"]
+    x = oc.wrap(box, d["x0"])
+    v = d["v0"].copy()
+    n = len(x)
+    mass = np.full(n, inputs.md_mass("aluminum"))
+    rv = phi.max_range() + 0.3
+    f = np.zeros((n, 3))
+    dt, (tset, tau) = float(d["dt"]), d["tcontrol"]
+    kin = []
+    for step in range(int(d["steps"])):
+        oc.vv_kick_drift(x, v, f, mass, dt)
+        x = oc.wrap(box, x)
+        f = oc.eam(box, x, oc.neighbors(box, x, rv), phi, ed, em)[0]
+        oc.vv_kick(v, f, mass, dt)
+        k = oc.kinetic(v, mass)
+        kin.append(k)
+        ghosts = (np.prod(1 + (x < lo + rv) + (x > hi - rv), axis=1) - 1).sum()
+        if step:
+            v *= oc.berendsen_factor(dt, tau, tset, (2.0 / 3.0) / 8.61734279e-05 * k / (n + ghosts))
+    np.testing.assert_allclose(kin, d["ledger"][1:1 + len(kin), 1], rtol=1e-12)
+
+
 def test_berendsen_factor(oracle_lib):
     # TempController.h:86: sqrt(1 + dt/tau (T0/T - 1))
     assert abs(oracle_lib.berendsen_factor(0.002, 0.05, 300.0, 600.0) - np.sqrt(1 + 0.04 * (0.5 - 1))) < 1e-15

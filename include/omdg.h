@@ -182,6 +182,42 @@ int omdg_set_profiling(omdg_ctx* ctx, int on);
 /* name_buf receives "name;name;..."; ms[] the summed milliseconds, calls[] the launch counts. */
 int omdg_kernel_times(omdg_ctx* ctx, char* name_buf, int name_cap, double* ms, long* calls, int cap, int* nkern);
 
+/* ------------------------------------------------- allocation-free counting */
+
+/*
+ * No counterpart in the reference.  Per-atom neighbour counts for positions
+ * that already live in the caller's device memory, for callers that cannot
+ * let a library allocate device memory: a host code whose own pool allocator
+ * has reserved the GPU's memory (a cudaMalloc would fail or fragment it), or
+ * one that keeps other streams busy (cudaFree synchronises the device).  This
+ * call allocates nothing: no cudaMalloc/cudaFree, no allocating library call.
+ *
+ * x: device pointer, n*3 FP64 positions (any order; periodic axes are wrapped
+ * into the box on the fly); count: device pointer, n ints.  The result equals
+ * the per-atom neighbour count of the Verlet list (owners and periodic images
+ * with r^2 <= rcut^2, computed as omdg_build_neighbors does with Rv = rcut).
+ * Work is queued on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream) of the current device and the call returns without waiting.
+ *
+ * Limits: n <= OMDG_STATIC_MAX_ATOMS; every periodic axis at least 3 rcut
+ * long; the cell grid is coarsened to OMDG_STATIC_MAX_CELLS cells when the box
+ * holds more.  Scratch is one fixed __device__ array of about 1.4 MB per
+ * device, shared by every call: calls that overlap in time (on different
+ * streams, or from several host threads at once) race on it and give wrong
+ * counts; calls queued on one stream do not.  The cell counters that must
+ * start at zero are cleared by each call itself.  The first call on a device
+ * looks the scratch address up (cudaGetSymbolAddress, which also loads the
+ * module's kernels), so make it once at setup, with that device current and
+ * before any stream capture.
+ *
+ * Returns OMDG_OK, OMDG_EINVAL (bad argument, box too small), OMDG_ERANGE
+ * (n above the limit) or OMDG_ECUDA; err (may be NULL) receives the message.
+ */
+#define OMDG_STATIC_MAX_ATOMS 131072
+#define OMDG_STATIC_MAX_CELLS 32768
+int omdg_count_neighbors_static(const double* x, int n, const double lo[3], const double hi[3], const int periodic[3],
+                                double rcut, int* count, void* stream, char* err, int err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libomdg.so")
 
 OMDG_OK = 0
+OMDG_STATIC_MAX_ATOMS = 131072  # include/omdg.h
+OMDG_STATIC_MAX_CELLS = 32768
 ERRORS = {
     -1: "OMDG_EINVAL",
     -2: "OMDG_ECUDA",
@@ -66,6 +68,7 @@ SIGNATURES = {
     "omdg_autotune": [_vp, _i, _P(_d)],
     "omdg_set_profiling": [_vp, _i],
     "omdg_kernel_times": [_vp, _cp, _i, _P(_d), _P(_l), _i, _P(_i)],
+    "omdg_count_neighbors_static": [_vp, _i, _P(_d), _P(_d), _P(_i), _d, _vp, _vp, _cp, _i],
 }
 
 
@@ -92,6 +95,21 @@ def load(path: str = LIB_PATH):
         fn.restype = _cp if name == "omdg_last_error" else _i
     _lib = lib
     return lib
+
+
+def count_neighbors_static(x_ptr, n, lo, hi, periodic, rcut, count_ptr, stream=None):
+    """omdg_count_neighbors_static: per-atom neighbour counts for n*3 FP64
+    positions at device address x_ptr into n ints at device address
+    count_ptr, queued on `stream` (a cudaStream_t address; None = default
+    stream).  Allocates no device memory; see include/omdg.h for the limits."""
+    lib = load()
+    lo3 = (_d * 3)(*[float(v) for v in lo])
+    hi3 = (_d * 3)(*[float(v) for v in hi])
+    per3 = (_i * 3)(*[1 if p else 0 for p in periodic])
+    err = ctypes.create_string_buffer(256)
+    rc = lib.omdg_count_neighbors_static(x_ptr, int(n), lo3, hi3, per3, float(rcut), count_ptr, stream, err, 256)
+    if rc != OMDG_OK:
+        raise OMDGError(rc, err.value.decode())
 
 
 def _dp(a):

@@ -43,14 +43,22 @@ TABLE = os.path.join(ROOT, "tests", "golden", "tables", "eam.aluminum5000")
 METRIC = "atom-steps/s on 1 GB300, EAM/Tersoff vs NN surrogate at <=30 meV/A force RMSE"
 UNIT = "atom-steps/s"
 
+SI_DIR = os.path.join(ROOT, "tests", "golden", "tables")
+
 WORKLOADS = {
-    # name: (description, ncell, a, sigma, T, dt)
-    "eam_al_256k": ("EAM Al FCC 40^3 = 256,000 atoms, 5000-knot table, skin 0.3, dt 2 fs", 40, 4.05, 0.05, 300.0,
-                    0.002),
-    "eam_al_1m": ("EAM Al FCC 64^3 = 1,048,576 atoms, 5000-knot table, skin 0.3, dt 2 fs", 64, 4.05, 0.05, 300.0,
-                  0.002),
-    "eam_al_32k": ("EAM Al FCC 20^3 = 32,000 atoms, 5000-knot table, skin 0.3, dt 2 fs", 20, 4.05, 0.05, 300.0,
-                   0.002),
+    # name: kind, description, lattice cells, lattice constant, Gaussian sigma, temperature, dt, seeds
+    "eam_al_256k": dict(kind="eam", desc="EAM Al FCC 40^3 = 256,000 atoms, 5000-knot table, skin 0.3, dt 2 fs",
+                        ncell=40, a=4.05, sigma=0.05, temp=300.0, dt=0.002, seeds=(2, 3)),
+    "eam_al_1m": dict(kind="eam", desc="EAM Al FCC 64^3 = 1,048,576 atoms, 5000-knot table, skin 0.3, dt 2 fs",
+                      ncell=64, a=4.05, sigma=0.05, temp=300.0, dt=0.002, seeds=(2, 3)),
+    "eam_al_32k": dict(kind="eam", desc="EAM Al FCC 20^3 = 32,000 atoms, 5000-knot table, skin 0.3, dt 2 fs",
+                       ncell=20, a=4.05, sigma=0.05, temp=300.0, dt=0.002, seeds=(2, 3)),
+    "tersoff_si_512k": dict(kind="tersoff", desc="Tersoff Si diamond 40^3 = 512,000 atoms, R 2.7 D 0.15, skin 0.3, "
+                            "1000 K, dt 1 fs", ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
+    "sw_si_512k": dict(kind="sw", desc="Stillinger-Weber Si diamond 40^3 = 512,000 atoms, rc 3.771, skin 0.3, "
+                       "1000 K, dt 1 fs", ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
+    "lj_ar_4000": dict(kind="lj", desc="LJ Ar FCC 10^3 = 4000 atoms, FP64, rc 2.5 sigma, skin 0.3, 100 K, dt 1 fs",
+                       ncell=10, a=5.26, sigma=0.0, temp=100.0, dt=0.001, seeds=(1, 1)),
 }
 
 # Algorithmic bytes per atom for one launch of each kernel (neighbour list of
@@ -62,10 +70,20 @@ WORKLOADS = {
 ALG_BYTES = {
     "eam_density": lambda nf: 24 + 4 * nf + 4,
     "eam_force": lambda nf: 24 + 4 * nf + 4 + 12 + 4,
+    "tersoff_centre": lambda nf: 24 + 4 * nf + 4,
+    "sw_centre": lambda nf: 24 + 4 * nf + 4,
+    "pair64": lambda nf: 24 + 4 * nf + 16,
+    "pair32": lambda nf: 24 + 4 * nf + 16,
     "kick_drift": lambda nf: 108 + 32,
     "kick": lambda nf: 24 + 12 + 24,
 }
-STEP_ALG_BYTES = lambda nf: 2 * (24 + 4 * nf) + 24 + 108  # noqa: E731  (EAM two passes + velocity Verlet)
+# one step: the force passes of the workload's potential + velocity Verlet (108 B)
+STEP_ALG_BYTES = {
+    "eam": lambda nf: 2 * (24 + 4 * nf) + 24 + 108,
+    "tersoff": lambda nf: 24 + 4 * nf + 16 + 108,
+    "sw": lambda nf: 24 + 4 * nf + 16 + 108,
+    "lj": lambda nf: 24 + 4 * nf + 16 + 108,
+}
 
 
 def log(*a):
@@ -137,24 +155,40 @@ class ClockSampler:
 def make_workload(name, ncell=None):
     from objectmd_gb300 import inputs
 
-    desc, nc, a, sigma, temp, dt = WORKLOADS[name]
-    if ncell:
-        nc = ncell
-    x, v, (lo, hi) = inputs.eam_aluminium(ncell=nc, a=a, sigma=sigma, temp=temp, seed_pos=2, seed_vel=3)
-    return desc, x, v, lo, hi, dt
+    w = dict(WORKLOADS[name])
+    nc = ncell or w["ncell"]
+    sp, sv = w["seeds"]
+    if w["kind"] == "eam":
+        x, v, (lo, hi) = inputs.eam_aluminium(ncell=nc, a=w["a"], sigma=w["sigma"], temp=w["temp"], seed_pos=sp,
+                                              seed_vel=sv)
+    elif w["kind"] == "lj":
+        x, v, (lo, hi) = inputs.lj_argon(ncell=nc, a=w["a"], temp=w["temp"], seed_vel=sv)
+    else:
+        x, v, (lo, hi) = inputs.diamond_silicon(ncell=nc, a=w["a"], sigma=w["sigma"], temp=w["temp"], seed_pos=sp,
+                                                seed_vel=sv)
+    return w, x, v, lo, hi
 
 
-def make_context(x, v, lo, hi, dt, device=0, tune=True):
+def make_context(w, x, v, lo, hi, device=0, tune=True):
     from objectmd_gb300 import inputs, omdg
 
     ctx = omdg.Context(device)
     ctx.set_box(lo, hi)
-    ctx.set_atoms(x, v, masses=[inputs.md_mass("aluminum")], znum=[13.0])
-    ctx.add_eam(TABLE)
+    kind = w["kind"]
+    elem, z = {"eam": ("aluminum", 13.0), "lj": ("argon", 18.0)}.get(kind, ("silicon", 14.0))
+    ctx.set_atoms(x, v, masses=[inputs.md_mass(elem)], znum=[z])
+    if kind == "eam":
+        ctx.add_eam(TABLE)
+    elif kind == "lj":
+        ctx.add_pair_table(os.path.join(SI_DIR, "pair.lj.argon"), fp64=True)
+    elif kind == "tersoff":
+        ctx.add_tersoff(os.path.join(SI_DIR, "tersoff.silicon27"))
+    else:
+        ctx.add_sw(os.path.join(SI_DIR, "sw.silicon"))
     ctx.set_neighbor(skin=0.3, rebuild_every=0)
-    ctx.set_timestep(dt)
+    ctx.set_timestep(w["dt"])
     ctx.set_first_step_mode(True)
-    if tune:
+    if tune and kind != "lj":  # the FP64 pair kernel has no launch shapes to tune
         ctx.autotune(3)
     return ctx
 
@@ -175,9 +209,10 @@ def run_gpu(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", init_method="env://")
-    desc, x, v, lo, hi, dt = make_workload(args.workload, args.ncell)
+    w, x, v, lo, hi = make_workload(args.workload, args.ncell)
+    desc = w["desc"] if not args.ncell else "%s (ncell %d)" % (w["desc"], args.ncell)
     n = len(x)
-    ctx = make_context(x, v, lo, hi, dt, device=device, tune=not args.no_tune)
+    ctx = make_context(w, x, v, lo, hi, device=device, tune=not args.no_tune)
     if args.eager:
         ctx.set_profiling(True)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
@@ -236,11 +271,11 @@ def run_gpu(args):
     peaks = load_peaks()
     alg = ALG_BYTES[dom_name](nf) * n
     achieved = alg / (dom_t * 1e-3) / 1e9
-    traffic = load_traffic(dom_name)
+    traffic = load_traffic(dom_name, n)
     roofline = {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peaks["hbm"],
                 "unit": "GB/s", "frac": round(achieved / peaks["hbm"], 4), "traffic": traffic,
                 "peak_source": peaks["src"], "alg_bytes_per_launch": int(alg)}
-    step_alg = STEP_ALG_BYTES(nf) * n
+    step_alg = STEP_ALG_BYTES[w["kind"]](nf) * n
     mean_step = total_ms / args.steps
 
     # end to end through the C ABI with host buffers
@@ -263,8 +298,9 @@ def run_gpu(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32 forces / fp64 integration",
-        "data": "synthetic (seeded FCC lattice, Gaussian displacements, Maxwell-Boltzmann velocities)",
+        "dtype": "f64" if w["kind"] == "lj" else "f32 forces, f64 integration",
+        "data": "synthetic (seeded %s lattice, Gaussian displacements, Maxwell-Boltzmann velocities)" %
+                ("diamond" if BASIS[w["kind"]] == 8 else "FCC"),
         "config": {"workload": desc, "atoms_per_gpu": n, "mean_neighbours": round(nf, 2),
                    "neighbour_rebuilds_in_timed_steps": rebuilds, "l2": "flushed before every step (%d MB write)" %
                    args.flush_mb, "parallelism": "replicas only" if world > 1 else "single GPU",
@@ -316,41 +352,69 @@ def load_peaks():
         return {"hbm": 6800.0, "src": "fallback 6.8 TB/s"}
 
 
-def load_traffic(kernel):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
-    p = os.path.join(ROOT, "profiles", "traffic.json")
+def load_traffic(kernel, n_atoms):
+    """DRAM bytes per launch: the committed ncu per-atom figure x atoms."""
+    p = os.path.join(ROOT, "profiles", "traffic_per_atom.txt")
     try:
-        return json.load(open(p)).get(kernel)
-    except Exception:
-        return None
+        for line in open(p):
+            f = line.split()
+            if len(f) == 2 and f[0] == kernel:
+                return int(float(f[1]) * n_atoms)
+    except OSError:
+        pass
+    return None
 
 
 # ------------------------------------------------------------------ CPU baselines
+SW_PARAM = dict(eps=2.1683, A=7.049556277, B=0.6022245584, p=4, q=0, sigma=2.0951, a=1.80, lam=21.0, gamma=1.2,
+                icos0=-3.0, usezbl=1, sx0=1.2107, sx1=1.8456, sa0=335.0594, sa1=-492.3905, sa2=244.5280,
+                sa3=-41.2347, z1=14, z2=14)
+TERSOFF_PARAM = dict(A=3264.7, B=95.373, lambda1=3.2394, lambda2=1.3258, lambda3=1.3258, beta=0.33675, n=22.956,
+                     c=4.8381, d=2.0417, h=0.0, R=2.7, D=0.15)
+BASIS = {"eam": 4, "lj": 4, "tersoff": 8, "sw": 8}
+CPU_SAMPLE_NCELL = {"eam": 16, "lj": 10, "tersoff": 10, "sw": 10}
+
+
 def _cpu_worker(args_tuple):
-    ncell, steps, warm = args_tuple
+    """One process: the oracle's step (kick-drift, wrap, neighbour list rebuilt
+    every step as the reference's default comm.refresh, forces, kick)."""
+    name, ncell, steps, warm = args_tuple
     sys.path.insert(0, ROOT)
     from objectmd_gb300 import inputs
     from oracle import oracle as oc
 
-    x, v, (lo, hi) = inputs.eam_aluminium(ncell=ncell, a=4.05, sigma=0.05, temp=300.0, seed_pos=2, seed_vel=3)
+    w, x, v, lo, hi = make_workload(name, ncell)
+    kind = w["kind"]
     n = len(x)
-    phi, ed, em = (oc.Table.from_file(TABLE, s) for s in ("PAIR", "EDENS", "EMBED"))
     box = oc.make_box(lo, hi, (1, 1, 1))
-    mass = np.full(n, inputs.md_mass("aluminum"))
-    rv = phi.max_range() + 0.3
+    elem = {"eam": "aluminum", "lj": "argon"}.get(kind, "silicon")
+    mass = np.full(n, inputs.md_mass(elem))
+    if kind == "eam":
+        phi, ed, em = (oc.Table.from_file(TABLE, sec) for sec in ("PAIR", "EDENS", "EMBED"))
+        rv = phi.max_range() + 0.3
+        force = lambda nb: oc.eam(box, x, nb, phi, ed, em)[0]  # noqa: E731
+    elif kind == "lj":
+        phi = oc.Table.from_file(os.path.join(SI_DIR, "pair.lj.argon"), "")
+        rv = phi.max_range() + 0.3
+        force = lambda nb: oc.pair_table(box, x, nb, phi)[0]  # noqa: E731
+    elif kind == "tersoff":
+        tp = oc.TersoffParam(**TERSOFF_PARAM)
+        rv = TERSOFF_PARAM["R"] + TERSOFF_PARAM["D"] + 0.3
+        force = lambda nb: oc.tersoff(box, x, nb, tp)[0]  # noqa: E731
+    else:
+        sp = oc.SWParam(**SW_PARAM)
+        rv = SW_PARAM["sigma"] * SW_PARAM["a"] + 0.3
+        force = lambda nb: oc.sw(box, x, nb, sp)[0]  # noqa: E731
     x = np.ascontiguousarray(x)
     v = np.ascontiguousarray(v)
     f = np.zeros((n, 3))
+    dt = w["dt"]
 
     def one_step():
-        oc.vv_kick_drift(x, v, f, mass, 0.002)
-        xw = oc.wrap(box, x)
-        x[:] = xw
-        nb = oc.neighbors(box, x, rv)
-        fr, e, vir, rho = oc.eam(box, x, nb, phi, ed, em)
-        f[:] = fr
-        oc.vv_kick(v, f, mass, 0.002)
-        return e.sum()
+        oc.vv_kick_drift(x, v, f, mass, dt)
+        x[:] = oc.wrap(box, x)
+        f[:] = force(oc.neighbors(box, x, rv))
+        oc.vv_kick(v, f, mass, dt)
 
     for _ in range(warm):
         one_step()
@@ -363,12 +427,14 @@ def _cpu_worker(args_tuple):
 
 def cpu_baseline(args):
     """Single-core oracle port on a bounded sample of the workload."""
+    kind = WORKLOADS[args.workload]["kind"]
+    nc = CPU_SAMPLE_NCELL[kind]
     ctx = mp.get_context("spawn")
     with ctx.Pool(1) as pool:
-        n, steps, sec = pool.map(_cpu_worker, [(16, args.cpu_steps, 1)])[0]
+        n, steps, sec = pool.map(_cpu_worker, [(args.workload, nc, args.cpu_steps, 1)])[0]
     return {"value": n * steps / sec, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "EAM Al FCC 16^3 = %d atoms, %d steps (neighbour list rebuilt every step, as the reference's "
-                      "default comm.refresh), oracle/omd_oracle.c on one host core" % (n, steps)}
+            "sample": "%s, lattice %d^3 = %d atoms, %d steps (neighbour list rebuilt every step, as the reference's "
+                      "default comm.refresh), oracle/omd_oracle.c on one host core" % (kind, nc, n, steps)}
 
 
 def run_reference(args):
@@ -376,31 +442,30 @@ def run_reference(args):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    desc, nc, a, sigma, temp, dt = WORKLOADS[args.workload]
-    if args.ncell:
-        nc = args.ncell
-    n_total = 4 * nc ** 3
+    w = WORKLOADS[args.workload]
+    desc, nc, basis = w["desc"], args.ncell or w["ncell"], BASIS[w["kind"]]
+    n_total = basis * nc ** 3
     # split the box into `cores` equal sub-boxes of the same density
     per = max(1, n_total // cores)
-    sub = max(3, int(round((per / 4) ** (1.0 / 3.0))))
+    sub = max(3, int(round((per / basis) ** (1.0 / 3.0))))
     steps = max(1, min(args.steps, 5))
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(sub, steps, max(0, min(args.warmup, 1)))] * cores)
+        res = pool.map(_cpu_worker, [(args.workload, sub, steps, max(0, min(args.warmup, 1)))] * cores)
     t1 = time.perf_counter()
     atoms = sum(r[0] for r in res)
     slowest = max(r[2] for r in res)
     value = atoms * steps / slowest
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
            "warmup": args.warmup, "ms_per_step": slowest / steps * 1e3, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": desc, "atoms_total": atoms, "host_processes": cores,
-                      "per_process": "EAM Al FCC %d^3 = %d atoms" % (sub, 4 * sub ** 3)},
+                      "per_process": "%s lattice %d^3 = %d atoms" % (w["kind"], sub, basis * sub ** 3)},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": "%d independent EAM boxes of %d atoms, %d steps each, neighbour list rebuilt "
+                            "sample": "%d independent %s boxes of %d atoms, %d steps each, neighbour list rebuilt "
                                       "every step (oracle/omd_oracle.c, the reference's algorithm restated)" %
-                                      (cores, 4 * sub ** 3, steps)},
+                                      (cores, w["kind"], basis * sub ** 3, steps)},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "wall_s": t1 - t0}
     print(json.dumps(out), flush=True)

@@ -166,6 +166,7 @@ struct FinParams {
     int ledger_cap;
     int count_step;       // 1: this is a RunKernel step (advance Step)
     const int* ghosts;    // reference compatibility: periodic images added to the atom count (or null)
+    unsigned* status;     // ERR_NONFINITE when a total is NaN or infinite
     double dt, tau, tset; // thermostat (tau <= 0: off)
     double temp_factor;   // 2/3/k_B (unit.h:66-104)
 };
@@ -196,6 +197,7 @@ __global__ void k_finalize(FinParams p, const double* __restrict__ partial, doub
     }
     if (threadIdx.x == 0) {
         double kinetic = 0.5 * sk[0];
+        if (!(isfinite(kinetic) && isfinite(se[0]))) atomicOr(p.status, ERR_NONFINITE);
         int row = st->row;
         int slot = row % p.ledger_cap;  // ring buffer between host reads
         ledger[4 * slot + 0] = kinetic;
@@ -293,6 +295,7 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
     f.tset = c->thermo_T;
     f.temp_factor = 2.0 / 3.0 / 8.61734279e-05;
     f.ghosts = nullptr;
+    f.status = c->d_status;
     if (c->thermo_count_ghosts && count_step && c->thermo_tau > 0.0) {
         // TempController::GetSystemTemperature divides by GetTotalAtom(), which
         // on MDSystemGrid is GetNAtom(): owners plus their periodic ghost images

@@ -46,7 +46,7 @@ __device__ __forceinline__ int cell_coord(double x, double org, double h, int nc
 }
 
 __global__ void k_cell_assign(int n, double* __restrict__ x, double* __restrict__ y, double* __restrict__ z,
-                              CellGeom g, int* __restrict__ cell, int* __restrict__ count) {
+                              CellGeom g, int* __restrict__ cell, int* __restrict__ count, unsigned* status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double p[3] = {x[i], y[i], z[i]};
@@ -65,6 +65,12 @@ __global__ void k_cell_assign(int n, double* __restrict__ x, double* __restrict_
     int cy = cell_coord(p[1], g.org[1], g.h[1], g.nc[1]);
     int cz = cell_coord(p[2], g.org[2], g.h[2], g.nc[2]);
     int c = (cz * g.nc[1] + cy) * g.nc[0] + cx;
+    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) {
+        // spread non-finite atoms over the cells so that the per-cell work stays
+        // bounded; the run is already invalid and the status word says so
+        atomicOr(status, ERR_NONFINITE);
+        c = i % (g.nc[0] * g.nc[1] * g.nc[2]);
+    }
     cell[i] = c;
     atomicAdd(&count[c], 1);
 }
@@ -104,10 +110,15 @@ __global__ void k_scatter(int n, const int* __restrict__ cell, const int* __rest
 
 // Atomic slot order is arbitrary; sorting each cell by previous index makes
 // the final order (and every later floating-point sum) deterministic.
+constexpr int CELL_SORT_MAX = 1024;
+
 __global__ void k_cell_sort(int m, const int* __restrict__ start, int* __restrict__ perm) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m) return;
     int b = start[c], e = start[c + 1];
+    // insertion sort (cells hold ~10-20 atoms); a pathological cell is left
+    // unsorted (its order is then not reproducible) rather than sorted in O(k^2)
+    if (e - b > CELL_SORT_MAX) return;
     for (int k = b + 1; k < e; k++) {
         int v = perm[k];
         int q = k - 1;
@@ -677,7 +688,7 @@ int nlist_build(Context* c) {
     cudaStream_t s = c->stream;
     prof_begin(c, "cell_sort");
     k_zero_ints<<<grid_for(m + 1, 256), 256, 0, s>>>(m + 1, c->cell_count, c->cell_fill);
-    k_cell_assign<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, g, c->cell, c->cell_count);
+    k_cell_assign<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, g, c->cell, c->cell_count, c->d_status);
     k_scan<<<1, 1024, 0, s>>>(m, c->cell_count, c->cell_start);
     k_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->cell, c->cell_start, c->cell_fill, c->perm);
     k_cell_sort<<<grid_for(m, 128), 128, 0, s>>>(m, c->cell_start, c->perm);

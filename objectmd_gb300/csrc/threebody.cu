@@ -83,6 +83,9 @@ __global__ void __launch_bounds__(128) k_sw_a(SWDev p, const PosPack* __restrict
         const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
         if (!(r2 < p.rc2)) continue;
         const float r = sqrtf(r2);
+        // r2 just below rc^2 can round to r == rc, where 1/(r - rc) is infinite
+        // and 0 * inf gives NaN; every SW term is zero there, so drop the pair
+        if (!(r < p.rc)) continue;
         float fr, he;
         sw_two_body(p, r, fr, he);
         ax += d.x * fr;

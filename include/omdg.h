@@ -182,6 +182,54 @@ int omdg_set_profiling(omdg_ctx* ctx, int on);
 /* name_buf receives "name;name;..."; ms[] the summed milliseconds, calls[] the launch counts. */
 int omdg_kernel_times(omdg_ctx* ctx, char* name_buf, int name_cap, double* ms, long* calls, int cap, int* nkern);
 
+/* ------------------------------------------------------ neural surrogate */
+
+/*
+ * No counterpart in the reference.  An atom-centred network stands in for
+ * Tersoff Si: 32 descriptors per atom (16 radial, 16 angular; cutoff from
+ * the model, 3.2 A by default), a 32-64-64-1 tanh network evaluated on the
+ * tensor cores (BF16 weights and activations, FP32 accumulation) and forces
+ * from the analytic gradient.  model_file is written by omdg_nn_save.  With
+ * tersoff_fallback (a Tersoff parameter file, as for omdg_add_tersoff) every
+ * atom whose descriptors leave the training range takes its energy and
+ * forces from Tersoff instead; NULL disables the fallback.
+ */
+int omdg_add_nn(omdg_ctx* ctx, int type_a, int type_b, const char* model_file, const char* tersoff_fallback);
+/* Atoms handed to the Tersoff fallback in the last force evaluation. */
+int omdg_nn_fallback_atoms(omdg_ctx* ctx, long* atoms);
+
+/*
+ * Training on one GPU (no reference counterpart).  A dataset is nconf
+ * periodic configurations: natoms[c] atoms each, positions x (sum natoms x 3,
+ * FP64), box lengths box_len (nconf x 3, each at least twice the cutoff),
+ * reference total energies (nconf) and forces (sum natoms x 3).  Parameters
+ * are one FP32 vector of 6337 values: W1[64x32] b1[64] W2[64x64] b2[64]
+ * w3[64] b3.  Loss: wE mean_c ((E_c - E_ref)/N_c)^2 + wF mean (F - F_ref)^2.
+ */
+typedef struct omdg_nn omdg_nn;
+int omdg_nn_create(omdg_nn** nn, int device);
+int omdg_nn_destroy(omdg_nn* nn);
+const char* omdg_nn_last_error(omdg_nn* nn);
+int omdg_nn_set_dataset(omdg_nn* nn, int nconf, const int* natoms, const double* x, const double* box_len,
+                        const double* energy, const double* forces);
+/* Raw descriptors of the dataset (sum natoms x 32). */
+int omdg_nn_descriptors(omdg_nn* nn, float* G, long count);
+/* Mean, deviation and range of the dataset's descriptors become the input scaling and the fallback range. */
+int omdg_nn_normalize_from_dataset(omdg_nn* nn);
+int omdg_nn_set_normalization(omdg_nn* nn, const float* mu, const float* sigma, const float* gmin, const float* gmax);
+int omdg_nn_get_normalization(omdg_nn* nn, float* mu, float* sigma, float* gmin, float* gmax);
+int omdg_nn_set_weights(omdg_nn* nn, const float* params, long count);
+int omdg_nn_get_weights(omdg_nn* nn, float* params, long count);
+/* Loss and dL/dparams (FP32 kernels) over configurations [conf0, conf0 + nconf). */
+int omdg_nn_gradient(omdg_nn* nn, int conf0, int nconf, double wE, double wF, double* loss, float* grad);
+/* Adam (beta 0.9/0.999) over shuffled batches of batch_confs configurations; epoch_loss (may be NULL) receives the mean batch loss of each epoch. */
+int omdg_nn_train(omdg_nn* nn, int epochs, int batch_confs, double lr, double wE, double wF, unsigned seed,
+                  double* epoch_loss);
+/* Per-atom energies and forces of configurations [conf0, conf0 + nconf) with the tensor-core network. */
+int omdg_nn_predict(omdg_nn* nn, int conf0, int nconf, double* energy_per_atom, double* forces);
+int omdg_nn_save(omdg_nn* nn, const char* path);
+int omdg_nn_load(omdg_nn* nn, const char* path);
+
 /* ------------------------------------------------- allocation-free counting */
 
 /*

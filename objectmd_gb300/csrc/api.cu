@@ -46,6 +46,7 @@ int check_status(Context* c) {
     if (st & ERR_OVERLAP) return set_error(c, OMDG_EOVERLAP, "overlapping atoms: r^2 < 1e-6 (gadget.cpp:149)");
     if (st & ERR_NONFINITE) return set_error(c, OMDG_ENONFINITE, "non-finite position or force");
     if (st & ERR_NBR_OVERFLOW) return set_error(c, OMDG_ESTATE, "neighbour capacity exceeded");
+    if (st & ERR_TIMEOUT) return set_error(c, OMDG_ECUDA, "a bounded device wait expired (tensor-core kernel)");
     return set_error(c, OMDG_ECUDA, "device status word set");
 }
 
@@ -155,7 +156,7 @@ static int alloc_atoms(Context* c, int n) {
     return OMDG_OK;
 }
 
-static void invalidate_graph(Context* c);
+void invalidate_graph(Context* c);
 
 // ------------------------------------------------------------- geometry
 static void compute_frame(Context* c) {
@@ -176,7 +177,6 @@ static void compute_frame(Context* c) {
 
 using namespace omdg;
 
-struct omdg_ctx : public Context {};
 
 static Context* C(omdg_ctx* c) { return static_cast<Context*>(c); }
 
@@ -190,7 +190,7 @@ struct GraphState {
 static std::map<Context*, GraphState> g_graphs;
 
 namespace omdg {
-static void invalidate_graph(Context* c) {
+void invalidate_graph(Context* c) {
     auto it = g_graphs.find(c);
     if (it == g_graphs.end()) return;
     if (it->second.exec) cudaGraphExecDestroy(it->second.exec);
@@ -254,12 +254,14 @@ int omdg_destroy(omdg_ctx* c) {
     cudaFree(c->d_mass);
     cudaFree(c->d_ledger);
     cudaFreeHost(c->h_ledger);
-    for (auto& p : c->pots)
+    for (auto& p : c->pots) {
         for (int k = 0; k < 3; k++) {
             cudaFree(p.d_coef[k]);
             cudaFree(p.d_coef64[k]);
             if (k == 0) cudaFree(p.d_coef2);
         }
+        nn_release(p);
+    }
     for (auto e : c->event_pool) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -448,7 +450,7 @@ static int upload_table(Context* c, Potential& p, int k, HostTable& t, bool fp64
     return OMDG_OK;
 }
 
-static void update_rc(Context* c) {
+void update_rc(Context* c) {
     // integrator.cpp:108-113: the largest CutRadius over all force kernels
     double m = -1.0;
     for (auto& p : c->pots) m = std::max(m, p.rc);
@@ -729,6 +731,7 @@ int forces_compute(Context* c) {
     if (c->pots.empty()) return set_error(c, OMDG_ESTATE, "no force kernel");
     bool first = true;
     for (auto& p : c->pots) {
+        if (p.fallback_only) continue;  // run by the potential that owns it
         int rc = OMDG_OK;
         switch (p.kind) {
             case POT_EAM: rc = eam_launch(c, p, first); break;
@@ -736,6 +739,7 @@ int forces_compute(Context* c) {
             case POT_SW: rc = sw_launch(c, p, first); break;
             case POT_TERSOFF: rc = tersoff_launch(c, p, first); break;
             case POT_ZBL: rc = zbl_launch(c, p, first); break;
+            case POT_NN: rc = nn_launch(c, p, first); break;
         }
         if (rc) return rc;
         first = false;

@@ -1,0 +1,56 @@
+// Descriptor terms of the neural surrogate (FP32), shared by the training
+// kernels (which store the Jacobian) and the MD kernels (which contract it
+// with dE/dG on the fly).  Behler-Parrinello radial G2 and angular G5 terms
+// (J. Behler, J. Chem. Phys. 134, 074106 (2011)).
+#pragma once
+
+#include "nn_internal.h"
+
+namespace omdg {
+
+__device__ __forceinline__ float nn_fc(const NNDescParams& p, float r, float& dfc) {
+    float s, c;
+    sincosf(r * p.pi_rc, &s, &c);
+    dfc = -0.5f * p.pi_rc * s;
+    return 0.5f * (c + 1.f);
+}
+
+// b^z for a small non-negative integer z (square and multiply)
+__device__ __forceinline__ float nn_ipow(float b, int z) {
+    float r = 1.f;
+    while (z > 0) {
+        if (z & 1) r *= b;
+        b *= b;
+        z >>= 1;
+    }
+    return r;
+}
+
+// Radial terms of one neighbour at distance r: value g[k] fc and dG_k/dr.
+__device__ __forceinline__ void nn_radial(const NNDescParams& p, float r, float fc, float dfc, int k, float& val,
+                                          float& ddr) {
+    const float x = r - p.rs[k];
+    const float g = expf(-p.eta_r[k] * x * x);
+    val = g * fc;
+    ddr = g * (dfc - 2.f * p.eta_r[k] * x * fc);
+}
+
+// Angular term m of the neighbour pair (a, b): the value and its derivatives
+// with respect to r_a, r_b and cos(theta).
+__device__ __forceinline__ void nn_angular(const NNDescParams& p, int m, float ra, float rb, float cs, float fa,
+                                           float dfa, float fb, float dfb, float& val, float& d_ra, float& d_rb,
+                                           float& d_cs) {
+    float base = 1.f + p.lam[m] * cs;
+    base = base > 0.f ? base : 0.f;
+    const int z = p.zeta[m];
+    const float pm1 = nn_ipow(base, z - 1);
+    const float pw = pm1 * base;
+    const float ex = p.eta_a[m] == 0.f ? 1.f : expf(-p.eta_a[m] * (ra * ra + rb * rb));
+    const float k = p.pref[m] * ex;
+    val = k * pw * fa * fb;
+    d_ra = k * pw * fb * (dfa - 2.f * p.eta_a[m] * ra * fa);
+    d_rb = k * pw * fa * (dfb - 2.f * p.eta_a[m] * rb * fb);
+    d_cs = base > 0.f ? k * (float)z * pm1 * p.lam[m] * fa * fb : 0.f;
+}
+
+}  // namespace omdg

@@ -22,6 +22,7 @@ enum : unsigned {
     ERR_NBR_OVERFLOW = 4u, // per-atom neighbour capacity exceeded (host grows and rebuilds)
     ERR_NONFINITE = 8u,    // NaN/Inf force or position
     ERR_CELL = 16u,        // atom outside the cell grid of a free axis (host re-grids)
+    ERR_TIMEOUT = 32u,     // a bounded device wait (mbarrier) expired
 };
 
 constexpr int CODE_SHIFT = 26;                // nbr entry = j | code << 26
@@ -85,7 +86,9 @@ struct __align__(32) PosPack {
 };
 
 // ------------------------------------------------------------ potentials
-enum PotKind { POT_EAM = 1, POT_PAIR = 2, POT_SW = 3, POT_TERSOFF = 4, POT_ZBL = 5 };
+enum PotKind { POT_EAM = 1, POT_PAIR = 2, POT_SW = 3, POT_TERSOFF = 4, POT_ZBL = 5, POT_NN = 6 };
+
+struct NNState;  // neural surrogate (nn_potential.cu)
 
 struct SWParams {
     double eps, A, B, p, q, sigma, a, lambda, gamma, icos0;
@@ -113,6 +116,8 @@ struct Potential {
     TersoffParams ters{};
     ZBLParams zbl{};
     double rc = 0;         // CutRadius as the reference sets it
+    NNState* nn = nullptr; // POT_NN: model, device network and per-atom buffers
+    bool fallback_only = false;  // evaluated only for the atoms a POT_NN hands over
     // device copies
     float4* d_coef[3] = {nullptr, nullptr, nullptr};
     float4* d_coef2 = nullptr;  // EAM: PAIR and EDENS knots interleaved
@@ -267,6 +272,12 @@ int measure_energies(Context* c, int row);
 int zero_forces(Context* c);
 int request_rebuild(Context* c);
 int resolve_thermostat(Context* c);
+int gather_slots(Context* c, bool zero_virial);
+int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask);
+int nn_launch(Context* c, Potential& pot, bool first);
+void update_rc(Context* c);         // largest cutoff; drops the list and the step graph
+void invalidate_graph(Context* c);
+void nn_release(Potential& pot);
 int drop_thermostat_factor(Context* c);
 int step_state_graph_rebuilds(Context* c, int* nrebuild);
 
@@ -278,3 +289,6 @@ int io_set_state(Context* c, const double* x, const double* v);
 inline int grid_for(int n, int block) { return (n + block - 1) / block; }
 
 }  // namespace omdg
+
+// The opaque handle of the C ABI is the context itself.
+struct omdg_ctx : public omdg::Context {};

@@ -224,9 +224,11 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
                                                    const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                    float4* __restrict__ slot, float* __restrict__ fx,
                                                    float* __restrict__ fy, float* __restrict__ fz,
-                                                   float* __restrict__ pe, float* __restrict__ vir, unsigned* status) {
+                                                   float* __restrict__ pe, float* __restrict__ vir, unsigned* status,
+                                                   const int* __restrict__ mask) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    if (mask && !mask[i]) return;  // centres another potential evaluates
     const PosPack pi = pack[i];
     const bool mine = p.single_type || pack_type(pi.hi) == p.ta;
     const int m = nnb[i];
@@ -423,7 +425,7 @@ __global__ void __launch_bounds__(128) k_zbl(ZBLDev p, const PosPack* __restrict
 // ------------------------------------------------------------------ host
 int threebody_prepare(Context* c) { return OMDG_OK; }
 
-static int gather_slots(Context* c, bool zero_virial) {
+int gather_slots(Context* c, bool zero_virial) {
     prof_begin(c, "slot_gather");
     k_slot_gather<<<grid_for(c->n, 128), 128, 0, c->stream>>>(
         c->n, c->nbr_hshift, c->maxnb, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->rev, c->slot_buf, c->fx,
@@ -485,6 +487,14 @@ int sw_launch(Context* c, Potential& pot, bool first) {
 }
 
 int tersoff_launch(Context* c, Potential& pot, bool first) {
+    int rc = tersoff_centre(c, pot, first, nullptr);
+    if (rc) return rc;
+    return gather_slots(c, false);
+}
+
+// Pass A of Tersoff: bond gradients of every centre (or of the centres with
+// mask[i] != 0) into the slot buffer; the caller gathers.
+int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask) {
     if (!c->rev || !c->slot_buf) return set_error(c, OMDG_ESTATE, "three-body buffers missing");
     const TersoffParams& t = pot.ters;
     TersDev p;
@@ -509,15 +519,13 @@ int tersoff_launch(Context* c, Potential& pot, bool first) {
     p.rc = (float)(t.R + t.D);
     p.rc2 = p.rc * p.rc * 1.0001f;
     p.first = first ? 1 : 0;
-    prof_begin(c, "tersoff_centre");
+    prof_begin(c, mask ? "tersoff_fallback" : "tersoff_centre");
     k_tersoff_a<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr),
                                                              c->nnb, c->slot_buf, c->fx, c->fy, c->fz, c->pe, c->vir,
-                                                             c->d_status);
+                                                             c->d_status, mask);
     prof_end(c);
     c->launches++;
-    int rc = check_cuda(c, cudaGetLastError(), "tersoff");
-    if (rc) return rc;
-    return gather_slots(c, false);
+    return check_cuda(c, cudaGetLastError(), "tersoff");
 }
 
 int zbl_launch(Context* c, Potential& pot, bool first) {

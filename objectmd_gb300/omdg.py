@@ -32,6 +32,7 @@ ERRORS = {
 # every symbol include/omdg.h declares, with its ctypes signature
 _P = ctypes.POINTER
 _d, _i, _l, _vp, _cp = ctypes.c_double, ctypes.c_int, ctypes.c_long, ctypes.c_void_p, ctypes.c_char_p
+_f = ctypes.c_float
 SIGNATURES = {
     "omdg_create": [_P(_vp), _i],
     "omdg_destroy": [_vp],
@@ -69,7 +70,25 @@ SIGNATURES = {
     "omdg_set_profiling": [_vp, _i],
     "omdg_kernel_times": [_vp, _cp, _i, _P(_d), _P(_l), _i, _P(_i)],
     "omdg_count_neighbors_static": [_vp, _i, _P(_d), _P(_d), _P(_i), _d, _vp, _vp, _cp, _i],
+    "omdg_add_nn": [_vp, _i, _i, _cp, _cp],
+    "omdg_nn_fallback_atoms": [_vp, _P(_l)],
+    "omdg_nn_create": [_P(_vp), _i],
+    "omdg_nn_destroy": [_vp],
+    "omdg_nn_last_error": [_vp],
+    "omdg_nn_set_dataset": [_vp, _i, _P(_i), _P(_d), _P(_d), _P(_d), _P(_d)],
+    "omdg_nn_descriptors": [_vp, _P(_f), _l],
+    "omdg_nn_normalize_from_dataset": [_vp],
+    "omdg_nn_set_normalization": [_vp, _P(_f), _P(_f), _P(_f), _P(_f)],
+    "omdg_nn_get_normalization": [_vp, _P(_f), _P(_f), _P(_f), _P(_f)],
+    "omdg_nn_set_weights": [_vp, _P(_f), _l],
+    "omdg_nn_get_weights": [_vp, _P(_f), _l],
+    "omdg_nn_gradient": [_vp, _i, _i, _d, _d, _P(_d), _P(_f)],
+    "omdg_nn_train": [_vp, _i, _i, _d, _d, _d, ctypes.c_uint, _P(_d)],
+    "omdg_nn_predict": [_vp, _i, _i, _P(_d), _P(_d)],
+    "omdg_nn_save": [_vp, _cp],
+    "omdg_nn_load": [_vp, _cp],
 }
+STRING_RESULT = ("omdg_last_error", "omdg_nn_last_error")
 
 
 class OMDGError(RuntimeError):
@@ -92,7 +111,7 @@ def load(path: str = LIB_PATH):
     for name, args in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = _cp if name == "omdg_last_error" else _i
+        fn.restype = _cp if name in STRING_RESULT else _i
     _lib = lib
     return lib
 
@@ -110,6 +129,105 @@ def count_neighbors_static(x_ptr, n, lo, hi, periodic, rcut, count_ptr, stream=N
     rc = lib.omdg_count_neighbors_static(x_ptr, int(n), lo3, hi3, per3, float(rcut), count_ptr, stream, err, 256)
     if rc != OMDG_OK:
         raise OMDGError(rc, err.value.decode())
+
+
+NN_PARAMS = 6337  # W1[64x32] b1[64] W2[64x64] b2[64] w3[64] b3
+NN_DESC = 32
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(_P(_f))
+
+
+class Network:
+    """The neural surrogate's trainer on one GPU (omdg_nn)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        self.h = _vp()
+        rc = self.lib.omdg_nn_create(ctypes.byref(self.h), int(device))
+        if rc != OMDG_OK:
+            raise OMDGError(rc, "omdg_nn_create failed (no usable GPU?)")
+        self.natoms = 0
+
+    def _check(self, rc):
+        if rc != OMDG_OK:
+            raise OMDGError(rc, (self.lib.omdg_nn_last_error(self.h) or b"").decode())
+
+    def close(self):
+        if self.h:
+            self.lib.omdg_nn_destroy(self.h)
+            self.h = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_dataset(self, natoms, x, box_len, energy, forces):
+        natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        box_len = np.ascontiguousarray(box_len, dtype=np.float64).reshape(-1, 3)
+        energy = np.ascontiguousarray(energy, dtype=np.float64)
+        forces = np.ascontiguousarray(forces, dtype=np.float64).reshape(-1, 3)
+        self._check(self.lib.omdg_nn_set_dataset(self.h, len(natoms), _ip(natoms), _dp(x), _dp(box_len),
+                                                 _dp(energy), _dp(forces)))
+        self.natoms = int(natoms.sum())
+        self.conf_start = np.concatenate([[0], np.cumsum(natoms)])
+
+    def descriptors(self):
+        G = np.zeros((self.natoms, NN_DESC), dtype=np.float32)
+        self._check(self.lib.omdg_nn_descriptors(self.h, _fp(G), G.size))
+        return G
+
+    def normalize_from_dataset(self):
+        self._check(self.lib.omdg_nn_normalize_from_dataset(self.h))
+
+    def set_normalization(self, mu, sigma, gmin=None, gmax=None):
+        arr = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
+        mu, sigma, gmin, gmax = arr(mu), arr(sigma), arr(gmin), arr(gmax)
+        self._check(self.lib.omdg_nn_set_normalization(self.h, _fp(mu), _fp(sigma), _fp(gmin), _fp(gmax)))
+
+    def normalization(self):
+        out = [np.zeros(NN_DESC, dtype=np.float32) for _ in range(4)]
+        self._check(self.lib.omdg_nn_get_normalization(self.h, *[_fp(a) for a in out]))
+        return dict(zip(("mu", "sigma", "gmin", "gmax"), out))
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self.lib.omdg_nn_set_weights(self.h, _fp(w), w.size))
+
+    def weights(self):
+        w = np.zeros(NN_PARAMS, dtype=np.float32)
+        self._check(self.lib.omdg_nn_get_weights(self.h, _fp(w), w.size))
+        return w
+
+    def gradient(self, conf0, nconf, wE, wF):
+        loss = _d()
+        g = np.zeros(NN_PARAMS, dtype=np.float32)
+        self._check(self.lib.omdg_nn_gradient(self.h, int(conf0), int(nconf), float(wE), float(wF),
+                                              ctypes.byref(loss), _fp(g)))
+        return loss.value, g
+
+    def train(self, epochs, batch_confs, lr, wE, wF, seed=7):
+        hist = np.zeros(int(epochs))
+        self._check(self.lib.omdg_nn_train(self.h, int(epochs), int(batch_confs), float(lr), float(wE), float(wF),
+                                           int(seed), _dp(hist)))
+        return hist
+
+    def predict(self, conf0, nconf):
+        n = int(self.conf_start[conf0 + nconf] - self.conf_start[conf0])
+        e = np.zeros(n)
+        f = np.zeros((n, 3))
+        self._check(self.lib.omdg_nn_predict(self.h, int(conf0), int(nconf), _dp(e), _dp(f)))
+        return e, f
+
+    def save(self, path):
+        self._check(self.lib.omdg_nn_save(self.h, path.encode()))
+
+    def load(self, path):
+        self._check(self.lib.omdg_nn_load(self.h, path.encode()))
 
 
 def _dp(a):
@@ -200,6 +318,15 @@ class Context:
 
     def add_zbl(self, ta, tb, rc, width):
         self._check(self.lib.omdg_add_zbl(self.h, ta, tb, float(rc), float(width)))
+
+    def add_nn(self, model_file, tersoff_fallback=None, ta=0, tb=0):
+        fb = tersoff_fallback.encode() if tersoff_fallback else None
+        self._check(self.lib.omdg_add_nn(self.h, ta, tb, model_file.encode(), fb))
+
+    def nn_fallback_atoms(self):
+        n = _l()
+        self._check(self.lib.omdg_nn_fallback_atoms(self.h, ctypes.byref(n)))
+        return n.value
 
     def max_cut_radius(self):
         r = _d()

@@ -1,0 +1,154 @@
+"""The neural surrogate on the GPU against the FP64 oracle (oracle/nn_oracle.py).
+
+- descriptors (FP32 kernels) vs the oracle: 2e-5 relative to each
+  descriptor's scale;
+- the tensor-core network (BF16 operands, FP32 accumulation): against the
+  oracle evaluated with the same BF16 rounding points, 99 % of per-atom
+  energies within 1e-4 eV (all within 2e-3: an activation at a BF16 rounding
+  boundary may round the other way) and forces within 1e-3 norm-wise; within
+  BF16 accuracy (1e-2 relative) of the plain FP64 oracle;
+- the training gradient (FP32 kernels, energy + force loss, double backward)
+  within 1e-3 norm-wise of the oracle's analytic gradient;
+- the MD force path (descriptors from the Verlet list) equal to the trainer's
+  prediction, and the Tersoff fallback equal to plain Tersoff when every atom
+  leaves the training range.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import TABLES
+
+pytestmark = pytest.mark.gpu
+
+TERSOFF = os.path.join(TABLES, "tersoff.silicon27")
+TP = dict(A=3264.7, B=95.373, lambda1=3.2394, lambda2=1.3258, lambda3=1.3258, beta=0.33675, n=22.956, c=4.8381,
+          d=2.0417, h=0.0, R=2.7, D=0.15)
+
+
+@pytest.fixture(scope="module")
+def dataset(oracle_lib):
+    """Four 64-atom diamond cells with Tersoff energies and forces from the C oracle."""
+    from objectmd_gb300 import inputs
+    from oracle import nn_oracle as nn
+
+    oc = oracle_lib
+    p = nn.descriptor_params()
+    confs = []
+    for k in range(4):
+        x, v, (lo, hi) = inputs.diamond_silicon(ncell=2, a=5.431, sigma=0.08 + 0.03 * k, temp=300.0,
+                                                seed_pos=20 + k, seed_vel=30 + k)
+        box = oc.make_box(lo, hi, (1, 1, 1))
+        f, e, _ = oc.tersoff(box, x, oc.neighbors(box, x, 3.15), oc.TersoffParam(**TP))
+        G, jac = nn.descriptors(x, lo, hi, p)
+        confs.append(dict(x=x, lo=lo, hi=hi, E=e.sum(), F=f, G=G, jac=jac))
+    return confs
+
+
+def make_network(omdg, confs, seed=3):
+    from oracle import nn_oracle as nn
+
+    net = omdg.Network(0)
+    net.set_dataset([len(c["x"]) for c in confs], np.concatenate([c["x"] for c in confs]),
+                    [np.asarray(c["hi"]) - np.asarray(c["lo"]) for c in confs], [c["E"] for c in confs],
+                    np.concatenate([c["F"] for c in confs]))
+    net.normalize_from_dataset()
+    norm = net.normalization()
+    w, _ = nn.init_model(seed, norm["mu"], norm["sigma"], -4.6)
+    net.set_weights(nn.flatten(w))
+    w = nn.unflatten(net.weights())
+    return net, w, {"mu": norm["mu"].astype(float), "sigma": norm["sigma"].astype(float)}
+
+
+def test_descriptors_match_oracle(omdg_lib, dataset):
+    net, _, _ = make_network(omdg_lib, dataset)
+    G = net.descriptors()
+    net.close()
+    ref = np.concatenate([c["G"] for c in dataset])
+    scale = np.abs(ref).max(0) + 1e-12
+    assert (np.abs(G - ref) / scale).max() < 2e-5
+
+
+def test_tensor_core_network_matches_oracle(omdg_lib, dataset):
+    from oracle import nn_oracle as nn
+
+    net, w, norm = make_network(omdg_lib, dataset)
+    E, F = net.predict(0, len(dataset))
+    net.close()
+    Et, Ft, E64, F64 = [], [], [], []
+    for c in dataset:
+        e, u = nn.forward_backward_tc(w, norm, c["G"])
+        Et.append(e)
+        Ft.append(nn.forces(c["jac"], u))
+        e, u = nn.forward_backward(w, norm, c["G"])
+        E64.append(e)
+        F64.append(nn.forces(c["jac"], u))
+    Et, Ft, E64, F64 = map(np.concatenate, (Et, Ft, E64, F64))
+    # same rounding points: agreement to FP32 accumulation order, except where
+    # an activation sits at a BF16 rounding boundary and rounds the other way
+    # (one BF16 ulp, 2^-8 relative, in one activation)
+    assert np.percentile(np.abs(E - Et), 99) < 1e-4
+    assert np.abs(E - Et).max() < 2e-3
+    assert np.linalg.norm(F - Ft) / np.linalg.norm(Ft) < 1e-3
+    assert np.abs(E - E64).max() < 1e-2 * np.abs(E64).max()
+    assert np.linalg.norm(F - F64) / np.linalg.norm(F64) < 1e-2
+
+
+def test_training_gradient_matches_oracle(omdg_lib, dataset):
+    from oracle import nn_oracle as nn
+
+    net, w, norm = make_network(omdg_lib, dataset)
+    wE, wF = 1.0, 2.0
+    loss, g = net.gradient(0, 3, wE, wF)
+    net.close()
+    batch = [(c["G"], c["jac"], c["E"], c["F"]) for c in dataset[:3]]
+    L, grad = nn.loss_and_grad(w, norm, batch, wE, wF)
+    ref = nn.flatten(grad).astype(np.float64)
+    assert abs(loss - L) < 1e-4 * abs(L)
+    assert np.linalg.norm(g - ref) / np.linalg.norm(ref) < 1e-3
+
+
+def surrogate_context(omdg, c, model, fallback):
+    from objectmd_gb300 import inputs
+
+    ctx = omdg.Context(0)
+    ctx.set_box(c["lo"], c["hi"])
+    ctx.set_atoms(c["x"], np.zeros_like(c["x"]), masses=[inputs.md_mass("silicon")], znum=[14.0])
+    if model:
+        ctx.add_nn(model, TERSOFF if fallback else None)
+    else:
+        ctx.add_tersoff(TERSOFF)
+    ctx.set_neighbor(0.3, 1)
+    ctx.compute_forces()
+    return ctx
+
+
+def test_md_path_matches_prediction(omdg_lib, dataset, tmp_path):
+    net, w, norm = make_network(omdg_lib, dataset)
+    model = str(tmp_path / "model.nn")
+    net.save(model)
+    E, F = net.predict(1, 1)
+    net.close()
+    with surrogate_context(omdg_lib, dataset[1], model, True) as ctx:
+        st = ctx.get_state()
+        assert ctx.nn_fallback_atoms() == 0
+    assert np.abs(st["pot"] - E).max() < 2e-3
+    assert np.linalg.norm(st["f"] - F) / np.linalg.norm(F) < 2e-3
+
+
+def test_fallback_is_plain_tersoff(omdg_lib, dataset, tmp_path):
+    net, w, norm = make_network(omdg_lib, dataset)
+    # a training range no atom lies in: every atom falls back
+    net.set_normalization(norm["mu"], norm["sigma"], norm["mu"] + 1e9, norm["mu"] + 2e9)
+    model = str(tmp_path / "narrow.nn")
+    net.save(model)
+    net.close()
+    c = dataset[2]
+    with surrogate_context(omdg_lib, c, model, True) as ctx:
+        st = ctx.get_state()
+        assert ctx.nn_fallback_atoms() == len(c["x"])
+    with surrogate_context(omdg_lib, c, None, False) as ctx:
+        ref = ctx.get_state()
+    np.testing.assert_array_equal(st["f"], ref["f"])
+    np.testing.assert_array_equal(st["pot"], ref["pot"])

@@ -1,0 +1,75 @@
+"""The FP64 neural-surrogate oracle pinned by finite differences (CPU only):
+descriptor Jacobian, forces = -dE/dx, and the analytic training gradient
+(energy + force loss, including the double backward through the network)."""
+import numpy as np
+import pytest
+
+from oracle import nn_oracle as nn
+
+
+@pytest.fixture(scope="module")
+def small_system():
+    from objectmd_gb300 import inputs
+
+    x, v, (lo, hi) = inputs.diamond_silicon(ncell=2, a=5.431, sigma=0.12, temp=300.0, seed_pos=11, seed_vel=12)
+    p = nn.descriptor_params()
+    G, jac = nn.descriptors(x, lo, hi, p)
+    return x, lo, hi, p, G, jac
+
+
+def test_descriptor_jacobian_matches_finite_differences(small_system):
+    x, lo, hi, p, G, jac = small_system
+    h = 1e-6
+    for atom in (0, 13):
+        for q in range(3):
+            xp = x.copy()
+            xp[atom, q] += h
+            xm = x.copy()
+            xm[atom, q] -= h
+            dG = (nn.descriptors(xp, lo, hi, p)[0] - nn.descriptors(xm, lo, hi, p)[0]) / (2 * h)
+            ana = np.zeros_like(G)
+            for i, blocks in enumerate(jac):
+                for j, B in blocks.items():
+                    if j == atom:
+                        ana[i] += B[:, q]
+                    if i == atom:
+                        ana[i] -= B[:, q]
+            assert np.abs(dG - ana).max() < 1e-6 * max(1.0, np.abs(ana).max())
+
+
+def test_forces_are_energy_gradients(small_system):
+    x, lo, hi, p, G, jac = small_system
+    w, norm = nn.init_model(3, G.mean(0), G.std(0) + 1e-3, -4.6)
+    E, F, _ = nn.predict(w, norm, x, lo, hi, p)
+    h = 1e-6
+    for atom in (2, 40):
+        for q in range(3):
+            xp = x.copy()
+            xp[atom, q] += h
+            xm = x.copy()
+            xm[atom, q] -= h
+            ep = nn.predict(w, norm, xp, lo, hi, p)[0].sum()
+            em = nn.predict(w, norm, xm, lo, hi, p)[0].sum()
+            assert abs(-(ep - em) / (2 * h) - F[atom, q]) < 1e-6
+    assert np.abs(F.sum(0)).max() < 1e-10  # no net force
+
+
+def test_training_gradient_matches_finite_differences(small_system):
+    x, lo, hi, p, G, jac = small_system
+    rng = np.random.default_rng(5)
+    w, norm = nn.init_model(4, G.mean(0), G.std(0) + 1e-3, -4.6)
+    Fref = rng.normal(0, 0.5, (len(x), 3))
+    batch = [(G, jac, -4.6 * len(x) + 0.3, Fref)]
+    wE, wF = 1.0, 10.0
+    L, grad = nn.loss_and_grad(w, norm, batch, wE, wF)
+    assert abs(L - nn.loss_only(w, norm, batch, wE, wF)) < 1e-12
+    h = 1e-6
+    for name, idx in (("W1", (5, 7)), ("W1", (60, 31)), ("b1", (9,)), ("W2", (3, 50)), ("b2", (17,)),
+                      ("w3", (11,)), ("b3", ())):
+        wp = {k: np.array(v, dtype=float, copy=True) for k, v in w.items()}
+        wm = {k: np.array(v, dtype=float, copy=True) for k, v in w.items()}
+        wp[name][idx] += h
+        wm[name][idx] -= h
+        fd = (nn.loss_only(wp, norm, batch, wE, wF) - nn.loss_only(wm, norm, batch, wE, wF)) / (2 * h)
+        ana = grad[name][idx]
+        assert abs(fd - ana) < 1e-6 * max(1.0, abs(ana)), (name, idx, fd, ana)

@@ -57,6 +57,9 @@ WORKLOADS = {
                             "1000 K, dt 1 fs", ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
     "sw_si_512k": dict(kind="sw", desc="Stillinger-Weber Si diamond 40^3 = 512,000 atoms, rc 3.771, skin 0.3, "
                        "1000 K, dt 1 fs", ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
+    "nn_si_512k": dict(kind="nn", desc="neural Tersoff surrogate (32 descriptors, 32-64-64-1 BF16 tensor-core "
+                       "network, Tersoff fallback) on Si diamond 40^3 = 512,000 atoms, 1000 K, skin 0.3, dt 1 fs",
+                       ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
     "lj_ar_4000": dict(kind="lj", desc="LJ Ar FCC 10^3 = 4000 atoms, FP64, rc 2.5 sigma, skin 0.3, 100 K, dt 1 fs",
                        ncell=10, a=5.26, sigma=0.0, temp=100.0, dt=0.001, seeds=(1, 1)),
 }
@@ -71,6 +74,8 @@ ALG_BYTES = {
     "eam_density": lambda nf: 24 + 4 * nf + 4,
     "eam_force": lambda nf: 24 + 4 * nf + 4 + 12 + 4,
     "tersoff_centre": lambda nf: 24 + 4 * nf + 4,
+    "nn_descriptors": lambda nf: 24 + 4 * nf + 128,
+    "nn_force": lambda nf: 24 + 4 * nf + 128 + 4 + 16,
     "sw_centre": lambda nf: 24 + 4 * nf + 4,
     "pair64": lambda nf: 24 + 4 * nf + 16,
     "pair32": lambda nf: 24 + 4 * nf + 16,
@@ -83,6 +88,7 @@ STEP_ALG_BYTES = {
     "tersoff": lambda nf: 24 + 4 * nf + 16 + 108,
     "sw": lambda nf: 24 + 4 * nf + 16 + 108,
     "lj": lambda nf: 24 + 4 * nf + 16 + 108,
+    "nn": lambda nf: 24 + 4 * nf + 16 + 108,
 }
 
 
@@ -183,12 +189,14 @@ def make_context(w, x, v, lo, hi, device=0, tune=True):
         ctx.add_pair_table(os.path.join(SI_DIR, "pair.lj.argon"), fp64=True)
     elif kind == "tersoff":
         ctx.add_tersoff(os.path.join(SI_DIR, "tersoff.silicon27"))
+    elif kind == "nn":
+        ctx.add_nn(NN_MODEL, os.path.join(SI_DIR, "tersoff.silicon27"))
     else:
         ctx.add_sw(os.path.join(SI_DIR, "sw.silicon"))
     ctx.set_neighbor(skin=0.3, rebuild_every=0)
     ctx.set_timestep(w["dt"])
     ctx.set_first_step_mode(True)
-    if tune and kind != "lj":  # the FP64 pair kernel has no launch shapes to tune
+    if tune and kind not in ("lj", "nn"):  # FP64 pair and surrogate kernels have no launch shapes to tune
         ctx.autotune(3)
     return ctx
 
@@ -287,6 +295,10 @@ def run_gpu(args):
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(args)
 
+    surrogate = None
+    if w["kind"] == "nn":
+        surrogate = surrogate_report(ctx, w, x, v, lo, hi, device, args, torch)
+
     out = {
         "metric": METRIC,
         "value": value,
@@ -316,6 +328,7 @@ def run_gpu(args):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "energy": {"kinetic": led["kinetic"], "potential": led["potential"], "energy": led["energy"]},
+        "surrogate": surrogate,
         "wall_s_timed_loop": t_wall1 - t_wall0,
     }
     if rank == 0:
@@ -323,6 +336,50 @@ def run_gpu(args):
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def surrogate_report(ctx, w, x0, v0, lo, hi, device, args, torch):
+    """Force RMSE of the surrogate against plain Tersoff on the starting
+    configuration and on the configuration the surrogate's MD reached, the
+    fallback count, and plain Tersoff's atom-steps/s on the same cell."""
+    from objectmd_gb300 import inputs, omdg
+
+    tersoff = os.path.join(SI_DIR, "tersoff.silicon27")
+
+    def forces(x, use_nn):
+        with omdg.Context(device) as c:
+            c.set_box(lo, hi)
+            c.set_atoms(x, np.zeros_like(x), masses=[inputs.md_mass("silicon")], znum=[14.0])
+            if use_nn:
+                c.add_nn(NN_MODEL, tersoff)
+            else:
+                c.add_tersoff(tersoff)
+            c.set_neighbor(0.3, 0)
+            c.compute_forces()
+            return c.get_state()["f"], (c.nn_fallback_atoms() if use_nn else 0)
+
+    rm = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
+    out = {}
+    for tag, xx in (("start", x0), ("after_md", ctx.get_state()["x"])):
+        fn, nfb = forces(xx, True)
+        ft, _ = forces(xx, False)
+        out[tag] = {"force_rmse_eV_per_A": rm(fn - ft), "force_rms_eV_per_A": rm(ft), "fallback_atoms": nfb}
+    # plain Tersoff on the same cell, graph-replayed steps
+    tw = dict(WORKLOADS["tersoff_si_512k"])
+    tc = make_context(tw, x0, v0, lo, hi, device=device, tune=not args.no_tune)
+    tc.step(5)
+    st = torch.cuda.ExternalStream(tc.stream(), device=device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = max(20, min(args.steps, 200))
+    with torch.cuda.stream(st):
+        e0.record(st)
+        tc.step_async(k)
+        e1.record(st)
+    tc.sync()
+    torch.cuda.synchronize()
+    out["tersoff_atom_steps_per_s"] = len(x0) * k / (e0.elapsed_time(e1) * 1e-3)
+    tc.close()
+    return out
 
 
 def run_e2e(ctx, n, steps, torch):
@@ -371,8 +428,9 @@ SW_PARAM = dict(eps=2.1683, A=7.049556277, B=0.6022245584, p=4, q=0, sigma=2.095
                 sa3=-41.2347, z1=14, z2=14)
 TERSOFF_PARAM = dict(A=3264.7, B=95.373, lambda1=3.2394, lambda2=1.3258, lambda3=1.3258, beta=0.33675, n=22.956,
                      c=4.8381, d=2.0417, h=0.0, R=2.7, D=0.15)
-BASIS = {"eam": 4, "lj": 4, "tersoff": 8, "sw": 8}
-CPU_SAMPLE_NCELL = {"eam": 16, "lj": 10, "tersoff": 10, "sw": 10}
+BASIS = {"eam": 4, "lj": 4, "tersoff": 8, "sw": 8, "nn": 8}
+CPU_SAMPLE_NCELL = {"eam": 16, "lj": 10, "tersoff": 10, "sw": 10, "nn": 10}
+NN_MODEL = os.path.join(ROOT, "objectmd_gb300", "models", "nn_tersoff_si.nn")
 
 
 def _cpu_worker(args_tuple):
@@ -397,7 +455,7 @@ def _cpu_worker(args_tuple):
         phi = oc.Table.from_file(os.path.join(SI_DIR, "pair.lj.argon"), "")
         rv = phi.max_range() + 0.3
         force = lambda nb: oc.pair_table(box, x, nb, phi)[0]  # noqa: E731
-    elif kind == "tersoff":
+    elif kind in ("tersoff", "nn"):  # the surrogate's CPU baseline is the method it replaces
         tp = oc.TersoffParam(**TERSOFF_PARAM)
         rv = TERSOFF_PARAM["R"] + TERSOFF_PARAM["D"] + 0.3
         force = lambda nb: oc.tersoff(box, x, nb, tp)[0]  # noqa: E731

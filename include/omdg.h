@@ -210,8 +210,18 @@ typedef struct omdg_nn omdg_nn;
 int omdg_nn_create(omdg_nn** nn, int device);
 int omdg_nn_destroy(omdg_nn* nn);
 const char* omdg_nn_last_error(omdg_nn* nn);
+/* Descriptor parameters (16 radial: rs, eta_r; 16 angular: zeta, lambda, eta_a), before the dataset; the defaults are
+   rs on [1.6, 3.2] A with eta_r = 1/(2 h^2), and (eta_a in {0, 0.3}) x (zeta in {1, 2, 4, 8}) x (lambda in {1, -1}). */
+int omdg_nn_set_descriptors(omdg_nn* nn, const float* rs, const float* eta_r, const int* zeta, const float* lambda,
+                            const float* eta_a);
 int omdg_nn_set_dataset(omdg_nn* nn, int nconf, const int* natoms, const double* x, const double* box_len,
                         const double* energy, const double* forces);
+/* relative != 0 weights each configuration's force residual by (mean square force of the dataset) / (its own), so
+   that every configuration counts by its relative error; 0 (the default) is the plain mean square. */
+int omdg_nn_set_force_weighting(omdg_nn* nn, int relative);
+/* Per-atom reference energies (sum natoms, e.g. a force kernel's per-atom potential): the energy term becomes
+   wE mean_i (E_i - E_i^ref)^2 over the batch atoms.  NULL restores the per-configuration total-energy term. */
+int omdg_nn_set_atom_energies(omdg_nn* nn, const double* e_atom);
 /* Raw descriptors of the dataset (sum natoms x 32). */
 int omdg_nn_descriptors(omdg_nn* nn, float* G, long count);
 /* Mean, deviation and range of the dataset's descriptors become the input scaling and the fallback range. */
@@ -222,11 +232,17 @@ int omdg_nn_set_weights(omdg_nn* nn, const float* params, long count);
 int omdg_nn_get_weights(omdg_nn* nn, float* params, long count);
 /* Loss and dL/dparams (FP32 kernels) over configurations [conf0, conf0 + nconf). */
 int omdg_nn_gradient(omdg_nn* nn, int conf0, int nconf, double wE, double wF, double* loss, float* grad);
-/* Adam (beta 0.9/0.999) over shuffled batches of batch_confs configurations; epoch_loss (may be NULL) receives the mean batch loss of each epoch. */
-int omdg_nn_train(omdg_nn* nn, int epochs, int batch_confs, double lr, double wE, double wF, unsigned seed,
-                  double* epoch_loss);
-/* Per-atom energies and forces of configurations [conf0, conf0 + nconf) with the tensor-core network. */
-int omdg_nn_predict(omdg_nn* nn, int conf0, int nconf, double* energy_per_atom, double* forces);
+/*
+ * Adam (beta 0.9/0.999) over shuffled batches of batch_confs configurations,
+ * learning rate lr in the first epoch decaying by a cosine to lr_final in the
+ * last (lr_final = lr: constant); epoch_loss (may be NULL) receives the mean
+ * batch loss of each epoch.
+ */
+int omdg_nn_train(omdg_nn* nn, int epochs, int batch_confs, double lr, double lr_final, double wE, double wF,
+                  unsigned seed, double* epoch_loss);
+/* Per-atom energies and forces of configurations [conf0, conf0 + nconf) with the tensor-core network
+   (BF16 operands), or with fp32 != 0 the FP32 kernels training uses. */
+int omdg_nn_predict(omdg_nn* nn, int conf0, int nconf, int fp32, double* energy_per_atom, double* forces);
 int omdg_nn_save(omdg_nn* nn, const char* path);
 int omdg_nn_load(omdg_nn* nn, const char* path);
 

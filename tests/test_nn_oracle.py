@@ -54,15 +54,17 @@ def test_forces_are_energy_gradients(small_system):
     assert np.abs(F.sum(0)).max() < 1e-10  # no net force
 
 
-def test_training_gradient_matches_finite_differences(small_system):
+@pytest.mark.parametrize("per_atom", [False, True])
+def test_training_gradient_matches_finite_differences(small_system, per_atom):
     x, lo, hi, p, G, jac = small_system
     rng = np.random.default_rng(5)
     w, norm = nn.init_model(4, G.mean(0), G.std(0) + 1e-3, -4.6)
     Fref = rng.normal(0, 0.5, (len(x), 3))
-    batch = [(G, jac, -4.6 * len(x) + 0.3, Fref)]
+    Eref = -4.6 + rng.normal(0, 0.1, len(x)) if per_atom else -4.6 * len(x) + 0.3
+    batch = [(G, jac, Eref, Fref)]
     wE, wF = 1.0, 10.0
-    L, grad = nn.loss_and_grad(w, norm, batch, wE, wF)
-    assert abs(L - nn.loss_only(w, norm, batch, wE, wF)) < 1e-12
+    L, grad = nn.loss_and_grad(w, norm, batch, wE, wF, per_atom)
+    assert abs(L - nn.loss_only(w, norm, batch, wE, wF, per_atom)) < 1e-12
     h = 1e-6
     for name, idx in (("W1", (5, 7)), ("W1", (60, 31)), ("b1", (9,)), ("W2", (3, 50)), ("b2", (17,)),
                       ("w3", (11,)), ("b3", ())):
@@ -70,6 +72,6 @@ def test_training_gradient_matches_finite_differences(small_system):
         wm = {k: np.array(v, dtype=float, copy=True) for k, v in w.items()}
         wp[name][idx] += h
         wm[name][idx] -= h
-        fd = (nn.loss_only(wp, norm, batch, wE, wF) - nn.loss_only(wm, norm, batch, wE, wF)) / (2 * h)
+        fd = (nn.loss_only(wp, norm, batch, wE, wF, per_atom) - nn.loss_only(wm, norm, batch, wE, wF, per_atom)) / (2 * h)
         ana = grad[name][idx]
         assert abs(fd - ana) < 1e-6 * max(1.0, abs(ana)), (name, idx, fd, ana)

@@ -196,7 +196,7 @@ def make_context(w, x, v, lo, hi, device=0, tune=True):
     ctx.set_neighbor(skin=0.3, rebuild_every=0)
     ctx.set_timestep(w["dt"])
     ctx.set_first_step_mode(True)
-    if tune and kind not in ("lj", "nn"):  # FP64 pair and surrogate kernels have no launch shapes to tune
+    if tune:
         ctx.autotune(3)
     return ctx
 

@@ -248,6 +248,7 @@ int omdg_destroy(omdg_ctx* c) {
     cudaFree(c->cell_count);
     cudaFree(c->cell_start);
     cudaFree(c->cell_fill);
+    cudaFree(c->cell_tile_sum);
     cudaFree(c->d_status);
     cudaFree(c->d_flags);
     cudaFree(c->d_state);
@@ -1154,6 +1155,27 @@ static int time_forces(Context* c, int reps, double& best) {
     if (!rc) rc = check_status(c);
     return rc;
 }
+// Best of `reps` list builds (binning, permutation, list) in milliseconds.
+static int time_build(Context* c, int reps, double& best) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    best = 1e30;
+    int rc = nlist_build(c);  // warm
+    for (int r = 0; r < reps && !rc; r++) {
+        cudaEventRecord(a, c->stream);
+        rc = nlist_build(c);
+        cudaEventRecord(b, c->stream);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best) best = ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (!rc) rc = check_status(c);
+    return rc;
+}
 }  // namespace omdg
 
 extern "C" {
@@ -1219,12 +1241,34 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
     } else if (tb) {
         for (int lanes : {1, 2, 4})
             for (int block : {64, 128, 256}) cands.push_back(Cand{lanes, block, 0});
-    } else {
-        return set_error(c, OMDG_ESTATE, "nothing to tune");
+    }
+    int rc = OMDG_OK;
+    // list build: cell-CTA, 8 or 4 lanes per atom, or one thread per atom
+    // (cells holding few atoms leave most of a cell CTA idle)
+    if (!c->list_valid && (rc = build_list(c))) return rc;
+    {
+        int best_bl = c->build_lanes;
+        double tbest = 1e30;
+        for (int bl : {0, 8, 4, 1}) {
+            c->build_lanes = bl;
+            double t;
+            if ((rc = time_build(c, reps, t))) return rc;
+            if (t < tbest) {
+                tbest = t;
+                best_bl = bl;
+            }
+        }
+        c->build_lanes = best_bl;
+        if ((rc = build_list(c))) return rc;
+        if ((rc = threebody_prepare(c))) return rc;
+    }
+    if (cands.empty()) {
+        invalidate_graph(c);
+        if (best_ms) return time_forces(c, reps, *best_ms);
+        return OMDG_OK;
     }
     double best = 1e30;
     Cand win = cands[0];
-    int rc = OMDG_OK;
     for (auto& cd : cands) {
         int hs = 0;
         while ((1 << hs) * cd.lanes < 32 && hs < 5) hs++;

@@ -75,28 +75,81 @@ __global__ void k_cell_assign(int n, double* __restrict__ x, double* __restrict_
     atomicAdd(&count[c], 1);
 }
 
-// Exclusive scan of count[0..m) into start[0..m]; one block, chunked.
-__global__ void k_scan(int m, const int* __restrict__ count, int* __restrict__ start) {
+// Exclusive scan of count[0..m) into start[0..m] in three launches: each
+// block scans a tile of SCAN_TILE cells (k_scan_tiles), one block scans the
+// tile totals (k_scan_totals), and k_scan_add adds the tile offsets.  The
+// order of every sum is fixed.
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_PER = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER;
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(int m, const int* __restrict__ count,
+                                                             int* __restrict__ start, int* __restrict__ tile_sum) {
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int base = blockIdx.x * SCAN_TILE + t * SCAN_PER;
+    int v[SCAN_PER];
+    int own = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; k++) {
+        v[k] = base + k < m ? count[base + k] : 0;
+        own += v[k];
+    }
+    int incl = own;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < SCAN_THREADS / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        if (lane < SCAN_THREADS / 32) warp_tot[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    int run = incl - own + (warp > 0 ? warp_tot[warp - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; k++) {
+        if (base + k < m) start[base + k] = run;
+        run += v[k];
+    }
+    if (t == SCAN_THREADS - 1) tile_sum[blockIdx.x] = warp_tot[SCAN_THREADS / 32 - 1];
+}
+
+// One block: tile totals -> exclusive tile offsets; start[m] = total.
+__global__ void k_scan_totals(int ntiles, int m, int* __restrict__ tile_sum, int* __restrict__ start) {
     __shared__ int sums[1024];
-    int t = threadIdx.x, nt = blockDim.x;
-    int chunk = (m + nt - 1) / nt;
-    int b = t * chunk, e = min(m, b + chunk);
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int chunk = (ntiles + nt - 1) / nt;
+    const int b = t * chunk, e = min(ntiles, b + chunk);
     int s = 0;
-    for (int k = b; k < e; k++) s += count[k];
+    for (int k = b; k < e; k++) s += tile_sum[k];
     sums[t] = s;
     __syncthreads();
     for (int off = 1; off < nt; off <<= 1) {
-        int v = t >= off ? sums[t - off] : 0;
+        const int y = t >= off ? sums[t - off] : 0;
         __syncthreads();
-        sums[t] += v;
+        sums[t] += y;
         __syncthreads();
     }
     int run = sums[t] - s;
     for (int k = b; k < e; k++) {
-        start[k] = run;
-        run += count[k];
+        const int c = tile_sum[k];
+        tile_sum[k] = run;
+        run += c;
     }
     if (t == nt - 1) start[m] = sums[t];
+}
+
+__global__ void k_scan_add(int m, int* __restrict__ start, const int* __restrict__ tile_off) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < m) start[k] += tile_off[k / SCAN_TILE];
 }
 
 __global__ void k_scatter(int n, const int* __restrict__ cell, const int* __restrict__ start, int* __restrict__ fill,
@@ -652,10 +705,12 @@ static int ensure_cells(Context* c, int m) {
     cudaFree(c->cell_count);
     cudaFree(c->cell_start);
     cudaFree(c->cell_fill);
+    cudaFree(c->cell_tile_sum);
     int cap = m + 1;
     if (cudaMalloc(&c->cell_count, cap * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&c->cell_start, (cap + 1) * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&c->cell_fill, cap * sizeof(int)) != cudaSuccess)
+        cudaMalloc(&c->cell_fill, cap * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&c->cell_tile_sum, (cap / SCAN_TILE + 2) * sizeof(int)) != cudaSuccess)
         return set_error(c, OMDG_ENOMEM, "cell arrays");
     c->ncell_cap = cap;
     return OMDG_OK;
@@ -689,10 +744,13 @@ int nlist_build(Context* c) {
     prof_begin(c, "cell_sort");
     k_zero_ints<<<grid_for(m + 1, 256), 256, 0, s>>>(m + 1, c->cell_count, c->cell_fill);
     k_cell_assign<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, g, c->cell, c->cell_count, c->d_status);
-    k_scan<<<1, 1024, 0, s>>>(m, c->cell_count, c->cell_start);
+    const int ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan_tiles<<<ntiles, SCAN_THREADS, 0, s>>>(m, c->cell_count, c->cell_start, c->cell_tile_sum);
+    k_scan_totals<<<1, 1024, 0, s>>>(ntiles, m, c->cell_tile_sum, c->cell_start);
+    k_scan_add<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->cell_tile_sum);
     k_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->cell, c->cell_start, c->cell_fill, c->perm);
     k_cell_sort<<<grid_for(m, 128), 128, 0, s>>>(m, c->cell_start, c->perm);
-    c->launches += 5;
+    c->launches += 7;
     AtomArrays cur{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->extra, c->extra_n};
     AtomArrays stg{c->stage_d, c->stage_d + c->cap, c->stage_d + 2 * (size_t)c->cap, c->stage_d + 3 * (size_t)c->cap,
                    c->stage_d + 4 * (size_t)c->cap, c->stage_d + 5 * (size_t)c->cap, c->stage_i,

@@ -158,6 +158,7 @@ struct Context {
     // sort scratch
     int *cell = nullptr, *perm = nullptr;
     int *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr;
+    int* cell_tile_sum = nullptr;  // scan tile totals / offsets
     int ncell_cap = 0;
     int* scan_partials = nullptr;
     double* stage_d = nullptr;   // permutation staging: 6 FP64 arrays x cap

@@ -60,6 +60,10 @@ WORKLOADS = {
     "nn_si_512k": dict(kind="nn", desc="neural Tersoff surrogate (32 descriptors, 32-64-64-1 BF16 tensor-core "
                        "network, Tersoff fallback) on Si diamond 40^3 = 512,000 atoms, 1000 K, skin 0.3, dt 1 fs",
                        ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
+    "impact_256": dict(kind="impact", desc="impact ensemble: 256 Si diamond slabs of 1,000-16,000 atoms (log-uniform, "
+                       "1.30M atoms), periodic x/y, free surface, 300 K, one Ar at 10-500 eV each; Tersoff + ZBL Ar-Si "
+                       "(rc 3.0 A), skin 1.0 A, dt 0.5 fs; all replicas in one context", ncell=0, a=5.431, sigma=0.03,
+                       temp=300.0, dt=0.0005, seeds=(6, 6)),
     "lj_ar_4000": dict(kind="lj", desc="LJ Ar FCC 10^3 = 4000 atoms, FP64, rc 2.5 sigma, skin 0.3, 100 K, dt 1 fs",
                        ncell=10, a=5.26, sigma=0.0, temp=100.0, dt=0.001, seeds=(1, 1)),
 }
@@ -89,6 +93,7 @@ STEP_ALG_BYTES = {
     "sw": lambda nf: 24 + 4 * nf + 16 + 108,
     "lj": lambda nf: 24 + 4 * nf + 16 + 108,
     "nn": lambda nf: 24 + 4 * nf + 16 + 108,
+    "impact": lambda nf: 24 + 4 * nf + 16 + 108,
 }
 
 
@@ -164,6 +169,17 @@ def make_workload(name, ncell=None):
     w = dict(WORKLOADS[name])
     nc = ncell or w["ncell"]
     sp, sv = w["seeds"]
+    if w["kind"] == "impact" and not ncell:
+        e = inputs.impact_ensemble(seed=w["seeds"][0], temp=w["temp"], sigma=w["sigma"], a=w["a"])
+        w["ensemble"] = e
+        return w, e["x"], e["v"], e["lo"], e["hi"]
+    if w["kind"] == "impact":  # one slab of ncell^3 cells (CPU samples), Si only
+        x, lo, hi = inputs.lattice(inputs.DIAMOND_BASIS, (nc, nc, nc), w["a"], 0.125)
+        x = inputs.perturb(x, w["sigma"], sp, lo, hi, (True, True, False))
+        v = inputs.maxwell_boltzmann(len(x), w["temp"], inputs.md_mass("silicon"), sv)
+        hi = np.array([hi[0], hi[1], hi[2] + 10.0])
+        lo = np.array([0.0, 0.0, -0.5 * w["a"]])
+        return w, x, v, lo, hi
     if w["kind"] == "eam":
         x, v, (lo, hi) = inputs.eam_aluminium(ncell=nc, a=w["a"], sigma=w["sigma"], temp=w["temp"], seed_pos=sp,
                                               seed_vel=sv)
@@ -179,8 +195,20 @@ def make_context(w, x, v, lo, hi, device=0, tune=True):
     from objectmd_gb300 import inputs, omdg
 
     ctx = omdg.Context(device)
-    ctx.set_box(lo, hi)
     kind = w["kind"]
+    if kind == "impact":
+        e = w["ensemble"]
+        ctx.set_replicas(e["natoms"], e["lo"], e["hi"], (1, 1, 0))
+        ctx.set_atoms(x, v, types=e["types"], masses=e["masses"], znum=e["znum"])
+        ctx.add_tersoff(os.path.join(SI_DIR, "tersoff.silicon27"))
+        ctx.add_zbl(1, 0, 3.0, 0.5)
+        ctx.set_neighbor(skin=1.0, rebuild_every=0)
+        ctx.set_timestep(w["dt"])
+        ctx.set_first_step_mode(True)
+        if tune:
+            ctx.autotune(3)
+        return ctx
+    ctx.set_box(lo, hi)
     elem, z = {"eam": ("aluminum", 13.0), "lj": ("argon", 18.0)}.get(kind, ("silicon", 14.0))
     ctx.set_atoms(x, v, masses=[inputs.md_mass(elem)], znum=[z])
     if kind == "eam":
@@ -428,8 +456,8 @@ SW_PARAM = dict(eps=2.1683, A=7.049556277, B=0.6022245584, p=4, q=0, sigma=2.095
                 sa3=-41.2347, z1=14, z2=14)
 TERSOFF_PARAM = dict(A=3264.7, B=95.373, lambda1=3.2394, lambda2=1.3258, lambda3=1.3258, beta=0.33675, n=22.956,
                      c=4.8381, d=2.0417, h=0.0, R=2.7, D=0.15)
-BASIS = {"eam": 4, "lj": 4, "tersoff": 8, "sw": 8, "nn": 8}
-CPU_SAMPLE_NCELL = {"eam": 16, "lj": 10, "tersoff": 10, "sw": 10, "nn": 10}
+BASIS = {"eam": 4, "lj": 4, "tersoff": 8, "sw": 8, "nn": 8, "impact": 8}
+CPU_SAMPLE_NCELL = {"eam": 16, "lj": 10, "tersoff": 10, "sw": 10, "nn": 10, "impact": 9}
 NN_MODEL = os.path.join(ROOT, "objectmd_gb300", "models", "nn_tersoff_si.nn")
 
 
@@ -444,7 +472,7 @@ def _cpu_worker(args_tuple):
     w, x, v, lo, hi = make_workload(name, ncell)
     kind = w["kind"]
     n = len(x)
-    box = oc.make_box(lo, hi, (1, 1, 1))
+    box = oc.make_box(lo, hi, (1, 1, 0) if kind == "impact" else (1, 1, 1))
     elem = {"eam": "aluminum", "lj": "argon"}.get(kind, "silicon")
     mass = np.full(n, inputs.md_mass(elem))
     if kind == "eam":
@@ -455,9 +483,9 @@ def _cpu_worker(args_tuple):
         phi = oc.Table.from_file(os.path.join(SI_DIR, "pair.lj.argon"), "")
         rv = phi.max_range() + 0.3
         force = lambda nb: oc.pair_table(box, x, nb, phi)[0]  # noqa: E731
-    elif kind in ("tersoff", "nn"):  # the surrogate's CPU baseline is the method it replaces
+    elif kind in ("tersoff", "nn", "impact"):  # the surrogate's CPU baseline is the method it replaces
         tp = oc.TersoffParam(**TERSOFF_PARAM)
-        rv = TERSOFF_PARAM["R"] + TERSOFF_PARAM["D"] + 0.3
+        rv = TERSOFF_PARAM["R"] + TERSOFF_PARAM["D"] + (1.0 if kind == "impact" else 0.3)
         force = lambda nb: oc.tersoff(box, x, nb, tp)[0]  # noqa: E731
     else:
         sp = oc.SWParam(**SW_PARAM)

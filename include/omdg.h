@@ -66,6 +66,20 @@ int omdg_get_state(omdg_ctx* ctx, double* x, double* v, double* f, double* pot, 
 int omdg_set_positions(omdg_ctx* ctx, const double* x);
 int omdg_set_velocities(omdg_ctx* ctx, const double* v);
 
+/*
+ * Replica mode (no single counterpart in the reference: each of its impact
+ * runs is one MDSystemGrid, test/si-impact/main.cpp).  nrep independent
+ * boxes in one context: replica r owns natoms[r] consecutive atoms (the
+ * order omdg_set_atoms then receives), its box lo/hi (nrep x 3 each) and the
+ * common periodic flags.  Every step kernel covers all replicas in one
+ * launch; neighbours are only found within a replica.  Replaces omdg_set_box;
+ * Tersoff and ZBL kernels.
+ */
+int omdg_set_replicas(omdg_ctx* ctx, int nrep, const int* natoms, const double* lo, const double* hi,
+                      const int periodic[3]);
+/* Kinetic and potential energy of every replica (MeasureKinetic/MeasurePotential per box). */
+int omdg_replica_ledger(omdg_ctx* ctx, int nrep, double* kinetic, double* potential);
+
 /* --------------------------------------------------------- force kernels */
 
 /*

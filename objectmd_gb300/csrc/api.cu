@@ -249,6 +249,11 @@ int omdg_destroy(omdg_ctx* c) {
     cudaFree(c->cell_start);
     cudaFree(c->cell_fill);
     cudaFree(c->cell_tile_sum);
+    cudaFree(c->d_rep_start);
+    cudaFree(c->d_rep_of);
+    cudaFree(c->d_rep_geom);
+    cudaFree(c->d_rep_shift);
+    cudaFree(c->d_rep_sums);
     cudaFree(c->d_status);
     cudaFree(c->d_flags);
     cudaFree(c->d_state);
@@ -277,8 +282,52 @@ int omdg_get_stream(omdg_ctx* c, void** stream) {
     return OMDG_OK;
 }
 
+int omdg_set_replicas(omdg_ctx* c, int nrep, const int* natoms, const double* lo, const double* hi,
+                      const int periodic[3]) {
+    if (!c || nrep <= 0 || !natoms || !lo || !hi || !periodic) return OMDG_EINVAL;
+    std::vector<int> start(nrep + 1, 0);
+    double blo[3] = {1e300, 1e300, 1e300}, bhi[3] = {-1e300, -1e300, -1e300};
+    for (int r = 0; r < nrep; r++) {
+        if (natoms[r] <= 0) return set_error(c, OMDG_EINVAL, "a replica without atoms");
+        start[r + 1] = start[r] + natoms[r];
+        for (int d = 0; d < 3; d++) {
+            if (!(hi[3 * r + d] > lo[3 * r + d])) return set_error(c, OMDG_EINVAL, "replica box hi must exceed lo");
+            blo[d] = std::min(blo[d], lo[3 * r + d]);
+            bhi[d] = std::max(bhi[d], hi[3 * r + d]);
+        }
+    }
+    c->nrep = nrep;
+    c->rep_start = start;
+    c->rep_lo.assign(lo, lo + 3 * nrep);
+    c->rep_hi.assign(hi, hi + 3 * nrep);
+    for (int d = 0; d < 3; d++) {
+        c->rep_periodic[d] = periodic[d] ? 1 : 0;
+        // the context box bounds every replica; periodicity lives in the replicas
+        c->box.lo[d] = blo[d];
+        c->box.hi[d] = bhi[d];
+        c->box.L[d] = bhi[d] - blo[d];
+        c->box.periodic[d] = 0;
+    }
+    cudaFree(c->d_rep_geom);
+    cudaFree(c->d_rep_shift);
+    cudaFree(c->d_rep_of);
+    cudaFree(c->d_rep_sums);
+    cudaFree(c->d_rep_start);
+    c->d_rep_start = nullptr;
+    c->d_rep_geom = c->d_rep_shift = nullptr;
+    c->d_rep_of = nullptr;
+    c->rep_of_cap = 0;
+    c->d_rep_sums = nullptr;
+    c->have_box = true;
+    compute_frame(c);
+    c->list_valid = false;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
 int omdg_set_box(omdg_ctx* c, const double lo[3], const double hi[3], const int periodic[3]) {
     if (!c || !lo || !hi || !periodic) return OMDG_EINVAL;
+    if (c->nrep > 0) return set_error(c, OMDG_ESTATE, "the context is in replica mode");
     for (int d = 0; d < 3; d++) {
         if (!(hi[d] > lo[d])) return set_error(c, OMDG_EINVAL, "box hi must exceed lo");
         c->box.lo[d] = lo[d];
@@ -298,6 +347,8 @@ int omdg_set_atoms(omdg_ctx* c, int n, const double* x, const double* v, const i
     if (!c || n <= 0 || !x || !type || ntypes <= 0 || ntypes > MAX_TYPES || !mass_by_type) return OMDG_EINVAL;
     if (n > MAX_ATOMS) return set_error(c, OMDG_EINVAL, "too many atoms");
     if (!c->have_box) return set_error(c, OMDG_ESTATE, "set the box first");
+    if (c->nrep > 0 && c->rep_start.back() != n)
+        return set_error(c, OMDG_EINVAL, "n differs from the sum of the replicas' atom counts");
     cudaSetDevice(c->device);
     for (int i = 0; i < n; i++)
         if (type[i] < 0 || type[i] >= ntypes) return set_error(c, OMDG_EINVAL, "atom type out of range");
@@ -692,10 +743,23 @@ namespace omdg {
 static int build_list(Context* c) {
     if (c->pots.empty()) return set_error(c, OMDG_ESTATE, "no force kernel (integrator.cpp:79)");
     nlist_prepare_geometry(c);
+    if (c->nrep > 0) {
+        if (c->rep_start.back() != c->n) return set_error(c, OMDG_ESTATE, "replica atom counts do not sum to n");
+        int rc = replica_prepare(c);
+        if (rc) return rc;
+    }
     if (c->maxnb == 0) {
         // first build: estimate from the mean density, then fit to the measured maximum
         double vol = 1.0;
         for (int d = 0; d < 3; d++) vol *= c->box.L[d];
+        if (c->nrep > 0) {
+            vol = 0.0;
+            for (int r = 0; r < c->nrep; r++) {
+                double v = 1.0;
+                for (int d = 0; d < 3; d++) v *= c->rep_hi[3 * r + d] - c->rep_lo[3 * r + d];
+                vol += v;
+            }
+        }
         double rv = c->rc_max + c->skin;
         double est = c->n / vol * 4.18879 * rv * rv * rv;
         int m = (int)(2.0 * est) + 32;
@@ -733,6 +797,8 @@ int forces_compute(Context* c) {
     bool first = true;
     for (auto& p : c->pots) {
         if (p.fallback_only) continue;  // run by the potential that owns it
+        if (c->nrep > 0 && p.kind != POT_TERSOFF && p.kind != POT_ZBL)
+            return set_error(c, OMDG_EINVAL, "replica mode evaluates Tersoff and ZBL kernels only");
         int rc = OMDG_OK;
         switch (p.kind) {
             case POT_EAM: rc = eam_launch(c, p, first); break;
@@ -899,8 +965,11 @@ int omdg_compute_forces(omdg_ctx* c) {
     if ((rc = measure_energies(c, 0))) return rc;
     prof_collect(c);
     if ((rc = check_status(c))) return rc;
+    // a non-step evaluation writes the ledger row the next step would use
+    int cur = 0;
+    if ((rc = step_state_read(c, nullptr, &cur, nullptr))) return rc;
     double row[4];
-    cudaMemcpy(row, c->d_ledger, sizeof(row), cudaMemcpyDeviceToHost);
+    cudaMemcpy(row, c->d_ledger + 4 * (size_t)(cur % c->ledger_cap), sizeof(row), cudaMemcpyDeviceToHost);
     c->last_kin = row[0];
     c->last_pot = row[1];
     c->last_vir = row[2];
@@ -1039,6 +1108,12 @@ int omdg_step(omdg_ctx* c, int nsteps) {
     int rc = omdg_step_async(c, nsteps);
     if (rc) return rc;
     return omdg_sync(c);
+}
+
+int omdg_replica_ledger(omdg_ctx* c, int nrep, double* kinetic, double* potential) {
+    if (!c || nrep != c->nrep) return c ? set_error(c, OMDG_EINVAL, "nrep differs from the context's") : OMDG_EINVAL;
+    cudaSetDevice(c->device);
+    return replica_sums(c, kinetic, potential);
 }
 
 int omdg_ledger(omdg_ctx* c, double* kinetic, double* potential, double* base_potential, double* virial) {

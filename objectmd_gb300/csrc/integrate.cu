@@ -10,6 +10,8 @@
 //   kick        v += dt/2 f/m, block partials of sum m v^2, sum potential,
 //               sum virial (FP64, fixed order)
 //   finalize    one block: ledger row, thermostat factor, step counter
+#include <vector>
+
 #include "device_common.cuh"
 
 namespace omdg {
@@ -247,6 +249,54 @@ __global__ void k_count_ghosts(GhostParams g, const double* __restrict__ x, cons
     // integer sums are order independent
     for (int off = 16; off > 0; off >>= 1) images += __shfl_xor_sync(0xffffffffu, images, off);
     if ((threadIdx.x & 31) == 0 && images) atomicAdd(out, images);
+}
+
+// One block per replica: kinetic (1/2 sum m v^2) and potential energy of the
+// replica's atom range, summed in a fixed order.
+__global__ void k_rep_sums(const int* __restrict__ start, const double* __restrict__ vx,
+                           const double* __restrict__ vy, const double* __restrict__ vz,
+                           const int* __restrict__ type, const double* __restrict__ mass,
+                           const float* __restrict__ pe, double* __restrict__ out) {
+    __shared__ double sk[256], se[256];
+    const int r = blockIdx.x;
+    double k = 0.0, e = 0.0;
+    for (int i = start[r] + threadIdx.x; i < start[r + 1]; i += blockDim.x) {
+        k = fma(mass[type[i]], fma(vx[i], vx[i], fma(vy[i], vy[i], vz[i] * vz[i])), k);
+        e += (double)pe[i];
+    }
+    sk[threadIdx.x] = k;
+    se[threadIdx.x] = e;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            sk[threadIdx.x] += sk[threadIdx.x + off];
+            se[threadIdx.x] += se[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[2 * r] = 0.5 * sk[0];
+        out[2 * r + 1] = se[0];
+    }
+}
+
+int replica_sums(Context* c, double* kinetic, double* potential) {
+    if (c->nrep == 0 || !c->d_rep_sums || !c->d_rep_start) return set_error(c, OMDG_ESTATE, "no replicas built");
+    int rc = resolve_thermostat(c);
+    if (rc) return rc;
+    k_rep_sums<<<c->nrep, 256, 0, c->stream>>>(c->d_rep_start, c->vx, c->vy, c->vz, c->type, c->d_mass, c->pe,
+                                               c->d_rep_sums);
+    std::vector<double> h(2 * (size_t)c->nrep);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h.data(), c->d_rep_sums, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "replica sums");
+    for (int r = 0; r < c->nrep; r++) {
+        if (kinetic) kinetic[r] = h[2 * r];
+        if (potential) potential[r] = h[2 * r + 1];
+    }
+    return OMDG_OK;
 }
 
 // ------------------------------------------------------------------ host

@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <climits>
+
 #include "device_common.cuh"
 
 namespace omdg {
@@ -164,6 +166,37 @@ __global__ void k_scatter(int n, const int* __restrict__ cell, const int* __rest
 // Atomic slot order is arbitrary; sorting each cell by previous index makes
 // the final order (and every later floating-point sum) deterministic.
 constexpr int CELL_SORT_MAX = 1024;
+
+// One warp per cell: for cells of up to 32 atoms each lane holds one atom
+// index and its rank (how many of the cell's indices are smaller) is counted
+// with shuffles; the lanes then write in place.  Larger cells fall back to
+// lane 0's insertion sort (bounded as in k_cell_sort).
+__global__ void k_cell_sort_warp(int m, const int* __restrict__ start, int* __restrict__ perm) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += warps) {
+        const int b = start[c], k = start[c + 1] - b;
+        if (k <= 1) continue;
+        if (k <= 32) {
+            const int v = lane < k ? perm[b + lane] : INT_MAX;
+            int r = 0;
+            for (int q = 0; q < k; q++) r += __shfl_sync(0xffffffffu, v, q) < v;
+            __syncwarp();
+            if (lane < k) perm[b + r] = v;
+        } else if (lane == 0 && k <= CELL_SORT_MAX) {
+            for (int p = b + 1; p < b + k; p++) {
+                const int v = perm[p];
+                int q = p - 1;
+                while (q >= b && perm[q] > v) {
+                    perm[q + 1] = perm[q];
+                    q--;
+                }
+                perm[q + 1] = v;
+            }
+        }
+        __syncwarp();
+    }
+}
 
 __global__ void k_cell_sort(int m, const int* __restrict__ start, int* __restrict__ perm) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -361,6 +394,103 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const PosPack* __r
                         double dy = __dsub_rn(yi, __dadd_rn(y[k], sy));
                         double dz = __dsub_rn(zi, __dadd_rn(z[k], sz));
                         double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                        in = rr <= p.rsq;
+                    }
+                    if (!in) continue;
+                    if (r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
+                    if (cnt < p.maxnb) nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
+                    cnt++;
+                }
+            }
+    if (cnt > p.maxnb) {
+        atomicOr(status, ERR_NBR_OVERFLOW);
+        atomicMax(need, cnt);
+        cnt = p.maxnb;
+    }
+    nnb[i] = cnt;
+}
+
+// ------------------------------------------------------------------ replicas
+// Replica mode: every replica has its own periodic lengths and cell grid,
+// and its cells occupy the global cell range [cell_base, cell_base + cells).
+struct RepGeom {
+    double lo[3], L[3], cell_org[3], cell_h[3];
+    int nc[3], periodic[3];
+    int cell_base;
+    ShiftF S;
+};
+
+__global__ void k_cell_assign_rep(int n, double* __restrict__ x, double* __restrict__ y, double* __restrict__ z,
+                                  const int* __restrict__ rep_of, const RepGeom* __restrict__ rg,
+                                  int* __restrict__ cell, int* __restrict__ count, unsigned* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const RepGeom& g = rg[rep_of[i]];
+    double p[3] = {x[i], y[i], z[i]};
+    for (int d = 0; d < 3; d++) {
+        if (!g.periodic[d]) continue;
+        const int u = (int)floor(__ddiv_rn(__dsub_rn(p[d], g.lo[d]), g.L[d]));
+        if (u < 0) p[d] = __dadd_rn(p[d], g.L[d]);
+        else if (u >= 1) p[d] = __dadd_rn(p[d], -g.L[d]);
+    }
+    x[i] = p[0];
+    y[i] = p[1];
+    z[i] = p[2];
+    const int cx = cell_coord(p[0], g.cell_org[0], g.cell_h[0], g.nc[0]);
+    const int cy = cell_coord(p[1], g.cell_org[1], g.cell_h[1], g.nc[1]);
+    const int cz = cell_coord(p[2], g.cell_org[2], g.cell_h[2], g.nc[2]);
+    int c = g.cell_base + (cz * g.nc[1] + cy) * g.nc[0] + cx;
+    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) {
+        atomicOr(status, ERR_NONFINITE);
+        c = g.cell_base + i % (g.nc[0] * g.nc[1] * g.nc[2]);
+    }
+    cell[i] = c;
+    atomicAdd(&count[c], 1);
+}
+
+// Thread per atom over the 27 cells of its replica's grid; the same screen
+// and FP64 tie-break as k_build, with the replica's periodic lengths.
+__global__ void __launch_bounds__(128) k_build_rep(BuildParams p, const RepGeom* __restrict__ rg,
+                                                   const int* __restrict__ rep_of, const PosPack* __restrict__ pack,
+                                                   const double* __restrict__ x, const double* __restrict__ y,
+                                                   const double* __restrict__ z, const int* __restrict__ cell,
+                                                   const int* __restrict__ start, unsigned* __restrict__ nbr,
+                                                   int* __restrict__ nnb, unsigned* status, int* need) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const RepGeom& g = rg[rep_of[i]];
+    const PosPack pi = pack[i];
+    const int ci = cell[i] - g.cell_base;
+    const int cx = ci % g.nc[0], cy = (ci / g.nc[0]) % g.nc[1], cz = ci / (g.nc[0] * g.nc[1]);
+    int ccx[6], csx[6], ccy[6], csy[6], ccz[6], csz[6];
+    const int mx = axis_candidates(cx, g.nc[0], g.periodic[0], ccx, csx);
+    const int my = axis_candidates(cy, g.nc[1], g.periodic[1], ccy, csy);
+    const int mz = axis_candidates(cz, g.nc[2], g.periodic[2], ccz, csz);
+    const ShiftF S = g.S;
+    int cnt = 0;
+    for (int a = 0; a < mz; a++)
+        for (int b = 0; b < my; b++)
+            for (int q = 0; q < mx; q++) {
+                const int c = g.cell_base + (ccz[a] * g.nc[1] + ccy[b]) * g.nc[0] + ccx[q];
+                const unsigned code = nbr_encode(0, csx[q], csy[b], csz[a]);
+                const bool self_image = (csx[q] == 0 && csy[b] == 0 && csz[a] == 0);
+                const int e = start[c + 1];
+                for (int k = start[c]; k < e; k++) {
+                    if (self_image && k == i) continue;
+                    const PosPack pk = pack[k];
+                    const float3 d = pair_delta(pi.hi, pi.lo, pk.hi, pk.lo, code, S);
+                    const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+                    if (r2 > p.rsq_hi) continue;
+                    bool in = r2 < p.rsq_lo;
+                    if (!in) {
+                        const double sx = csx[q] == 0 ? 0.0 : (csx[q] > 0 ? g.L[0] : -g.L[0]);
+                        const double sy = csy[b] == 0 ? 0.0 : (csy[b] > 0 ? g.L[1] : -g.L[1]);
+                        const double sz = csz[a] == 0 ? 0.0 : (csz[a] > 0 ? g.L[2] : -g.L[2]);
+                        const double dx = __dsub_rn(x[i], __dadd_rn(x[k], sx));
+                        const double dy = __dsub_rn(y[i], __dadd_rn(y[k], sy));
+                        const double dz = __dsub_rn(z[i], __dadd_rn(z[k], sz));
+                        const double rr =
+                            __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
                         in = rr <= p.rsq;
                     }
                     if (!in) continue;
@@ -674,6 +804,72 @@ void nlist_prepare_geometry(Context* c) {
     }
 }
 
+// Cell grids of the replicas (same rules as nlist_prepare_geometry, per
+// replica) and the replica of every atom; uploads both.
+int replica_prepare(Context* c) {
+    const double rv = c->rc_max + c->skin;
+    std::vector<RepGeom> rg(c->nrep);
+    std::vector<ShiftF> sh(c->nrep);
+    int base = 0;
+    for (int r = 0; r < c->nrep; r++) {
+        RepGeom& g = rg[r];
+        for (int d = 0; d < 3; d++) {
+            g.lo[d] = c->rep_lo[3 * r + d];
+            g.L[d] = c->rep_hi[3 * r + d] - c->rep_lo[3 * r + d];
+            g.periodic[d] = c->rep_periodic[d];
+            if (g.periodic[d]) {
+                g.cell_org[d] = g.lo[d];
+                const int nc = (int)(g.L[d] / rv);
+                g.nc[d] = nc < 1 ? 1 : nc;
+                g.cell_h[d] = g.L[d] / g.nc[d];
+            } else {
+                const double margin = 2.0 * rv;
+                g.cell_org[d] = g.lo[d] - margin;
+                const double ext = g.L[d] + 2.0 * margin;
+                const int nc = (int)(ext / rv);
+                g.nc[d] = nc < 1 ? 1 : nc;
+                g.cell_h[d] = ext / g.nc[d];
+            }
+        }
+        const float lh[3] = {(float)g.L[0], (float)g.L[1], (float)g.L[2]};
+        g.S.hx = lh[0];
+        g.S.hy = lh[1];
+        g.S.hz = lh[2];
+        g.S.lx = (float)(g.L[0] - (double)lh[0]);
+        g.S.ly = (float)(g.L[1] - (double)lh[1]);
+        g.S.lz = (float)(g.L[2] - (double)lh[2]);
+        sh[r] = g.S;
+        g.cell_base = base;
+        base += g.nc[0] * g.nc[1] * g.nc[2];
+    }
+    c->rep_cells = base;
+    // The step graph holds these pointers: allocate once (omdg_set_replicas
+    // frees them) and reallocate only for a larger atom capacity, dropping
+    // the graph then.  Contents are rewritten in place.
+    cudaError_t e = cudaSuccess;
+    if (!c->d_rep_geom) e = cudaMalloc(&c->d_rep_geom, sizeof(RepGeom) * c->nrep);
+    if (e == cudaSuccess && !c->d_rep_shift) e = cudaMalloc(&c->d_rep_shift, sizeof(ShiftF) * c->nrep);
+    if (e == cudaSuccess && !c->d_rep_start) e = cudaMalloc(&c->d_rep_start, sizeof(int) * (c->nrep + 1));
+    if (e == cudaSuccess && !c->d_rep_sums) e = cudaMalloc(&c->d_rep_sums, sizeof(double) * 2 * c->nrep);
+    if (e == cudaSuccess && (!c->d_rep_of || c->rep_of_cap < c->cap)) {
+        cudaFree(c->d_rep_of);
+        c->d_rep_of = nullptr;
+        e = cudaMalloc(&c->d_rep_of, sizeof(int) * std::max(1, c->cap));
+        c->rep_of_cap = c->cap;
+        invalidate_graph(c);
+    }
+    if (e != cudaSuccess) return set_error(c, OMDG_ENOMEM, "replica tables");
+    std::vector<int> of(c->n);
+    for (int r = 0; r < c->nrep; r++)
+        for (int i = c->rep_start[r]; i < c->rep_start[r + 1]; i++) of[i] = r;
+    cudaMemcpyAsync(c->d_rep_geom, rg.data(), sizeof(RepGeom) * c->nrep, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->d_rep_shift, sh.data(), sizeof(ShiftF) * c->nrep, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->d_rep_of, of.data(), sizeof(int) * c->n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->d_rep_start, c->rep_start.data(), sizeof(int) * (c->nrep + 1), cudaMemcpyHostToDevice,
+                    c->stream);
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "replica tables");
+}
+
 size_t nlist_slots(const Context* c, int maxnb) {
     size_t H = (size_t)1 << c->nbr_hshift;
     size_t slices = ((size_t)c->cap + H - 1) / H;
@@ -702,6 +898,10 @@ int nlist_reserve(Context* c, int maxnb) {
 
 static int ensure_cells(Context* c, int m) {
     if (m + 1 <= c->ncell_cap) return OMDG_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(c->stream, &cs);
+    if (cs != cudaStreamCaptureStatusNone) return set_error(c, OMDG_ESTATE, "cell grid grew inside a captured step");
+    invalidate_graph(c);  // a captured step holds the old cell arrays
     cudaFree(c->cell_count);
     cudaFree(c->cell_start);
     cudaFree(c->cell_fill);
@@ -737,19 +937,26 @@ int nlist_build(Context* c) {
     int n = c->n;
     if (n == 0) return OMDG_OK;
     CellGeom g = cell_geom(c);
-    int m = g.nc[0] * g.nc[1] * g.nc[2];
+    const bool reps = c->nrep > 0;
+    int m = reps ? c->rep_cells : g.nc[0] * g.nc[1] * g.nc[2];
     int rc = ensure_cells(c, m);
     if (rc) return rc;
     cudaStream_t s = c->stream;
     prof_begin(c, "cell_sort");
     k_zero_ints<<<grid_for(m + 1, 256), 256, 0, s>>>(m + 1, c->cell_count, c->cell_fill);
-    k_cell_assign<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, g, c->cell, c->cell_count, c->d_status);
+    if (reps)
+        k_cell_assign_rep<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->d_rep_of,
+                                                             static_cast<const RepGeom*>(c->d_rep_geom), c->cell,
+                                                             c->cell_count, c->d_status);
+    else
+        k_cell_assign<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, g, c->cell, c->cell_count,
+                                                         c->d_status);
     const int ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
     k_scan_tiles<<<ntiles, SCAN_THREADS, 0, s>>>(m, c->cell_count, c->cell_start, c->cell_tile_sum);
     k_scan_totals<<<1, 1024, 0, s>>>(ntiles, m, c->cell_tile_sum, c->cell_start);
     k_scan_add<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->cell_tile_sum);
     k_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->cell, c->cell_start, c->cell_fill, c->perm);
-    k_cell_sort<<<grid_for(m, 128), 128, 0, s>>>(m, c->cell_start, c->perm);
+    k_cell_sort_warp<<<grid_for(m, 8), 256, 0, s>>>(m, c->cell_start, c->perm);
     c->launches += 7;
     AtomArrays cur{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->extra, c->extra_n};
     AtomArrays stg{c->stage_d, c->stage_d + c->cap, c->stage_d + 2 * (size_t)c->cap, c->stage_d + 3 * (size_t)c->cap,
@@ -785,7 +992,12 @@ int nlist_build(Context* c) {
     prof_begin(c, "nlist_build");
     int combos = 1;
     for (int d = 0; d < 3; d++) combos *= (g.periodic[d] && g.nc[d] < 3) ? 3 * g.nc[d] : 3;
-    if (c->build_lanes == 0 && combos <= 64) {
+    if (reps) {
+        k_build_rep<<<grid_for(n, 128), 128, 0, s>>>(bp, static_cast<const RepGeom*>(c->d_rep_geom), c->d_rep_of,
+                                                     c->pack, c->x, c->y, c->z, cell_sorted, c->cell_start,
+                                                     reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
+                                                     c->d_flags + 1);
+    } else if (c->build_lanes == 0 && combos <= 64) {
         const int cap = 1024;  // staged candidates per chunk (32 bytes each)
         k_build_cells<<<m, BUILD_CELL_THREADS, cap * 2 * sizeof(float4), s>>>(
             bp, c->pack, c->x, c->y, c->z, c->cell_start, cap, reinterpret_cast<unsigned*>(c->nbr), c->nnb,

@@ -230,6 +230,7 @@ static int nn_ensure(Context* c, NNState& s) {
     if (e == cudaSuccess && !s.count) e = cudaMalloc(&s.count, sizeof(int));
     if (e != cudaSuccess) return set_error(c, OMDG_ENOMEM, "surrogate buffers");
     s.cap = (int)n;
+    invalidate_graph(c);  // a captured step holds the old buffers
     return OMDG_OK;
 }
 

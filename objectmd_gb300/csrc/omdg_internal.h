@@ -159,6 +159,20 @@ struct Context {
     int *cell = nullptr, *perm = nullptr;
     int *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr;
     int* cell_tile_sum = nullptr;  // scan tile totals / offsets
+    // replica mode (omdg_set_replicas): independent boxes in one atom array,
+    // each with its own cell grid and periodic lengths; the counting sort
+    // keeps every replica's atoms in its index range
+    int nrep = 0;
+    std::vector<int> rep_start;          // nrep + 1
+    std::vector<double> rep_lo, rep_hi;  // nrep x 3
+    int rep_periodic[3] = {1, 1, 0};
+    int rep_cells = 0;                   // cells over all replicas
+    int* d_rep_of = nullptr;             // replica of each atom (index order)
+    int rep_of_cap = 0;
+    void* d_rep_geom = nullptr;          // RepGeom[nrep] (nlist.cu)
+    void* d_rep_shift = nullptr;         // ShiftF[nrep]: periodic lengths for pair_delta
+    double* d_rep_sums = nullptr;        // per-replica ledger sums
+    int* d_rep_start = nullptr;          // nrep + 1
     int ncell_cap = 0;
     int* scan_partials = nullptr;
     double* stage_d = nullptr;   // permutation staging: 6 FP64 arrays x cap
@@ -276,6 +290,8 @@ int resolve_thermostat(Context* c);
 int gather_slots(Context* c, bool zero_virial);
 int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask);
 int nn_launch(Context* c, Potential& pot, bool first);
+int replica_prepare(Context* c);  // per-replica cell grids and shifts (host, before a build)
+int replica_sums(Context* c, double* kinetic, double* potential);  // per-replica ledger (synchronous)
 void update_rc(Context* c);         // largest cutoff; drops the list and the step graph
 void invalidate_graph(Context* c);
 void nn_release(Potential& pot);

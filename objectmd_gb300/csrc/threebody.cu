@@ -200,9 +200,33 @@ __global__ void __launch_bounds__(128) k_slot_gather(int n, int hshift, int maxn
 struct TersDev {
     int n, hshift, maxnb, single_type, ta;
     ShiftF L;
+    const ShiftF* rep_L;  // replica mode: periodic lengths of each replica (else null)
+    const int* rep_of;
     float A, B, l1, l2, l3c, beta, nn, c2, d2, h, R, D, rc, rc2;
     int first;
 };
+
+// b = (1 + (beta zeta)^n)^(-1/2n) and db/dzeta.  In a close collision the
+// exp(lambda3^3 (r_ij - r_ik)^3) factor makes zeta large enough for
+// (beta zeta)^n to overflow FP32; there b is its limit (beta zeta)^(-1/2)
+// (relative difference (beta zeta)^(-n) / 2n < 1e-26 for n ln(beta zeta) > 60).
+__device__ __forceinline__ void ters_bond_order(const TersDev& p, float zeta, float& b, float& db) {
+    if (!(zeta > 0.f)) {
+        b = 1.f;
+        db = 0.f;
+        return;
+    }
+    const float x = p.beta * zeta;
+    const float nlx = p.nn * logf(x);
+    if (nlx > 60.f) {
+        b = rsqrtf(x);
+        db = -0.5f * b / zeta;
+        return;
+    }
+    const float bn = expf(nlx);
+    b = powf(1.f + bn, -0.5f / p.nn);
+    db = -0.5f * b * bn / ((1.f + bn) * zeta);
+}
 
 __device__ __forceinline__ float ters_fc(const TersDev& p, float r, float& dfc) {
     if (r < p.R - p.D) {
@@ -231,6 +255,7 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
     if (mask && !mask[i]) return;  // centres another potential evaluates
     const PosPack pi = pack[i];
     const bool mine = p.single_type || pack_type(pi.hi) == p.ta;
+    const ShiftF L = p.rep_L ? p.rep_L[p.rep_of[i]] : p.L;
     const int m = nnb[i];
     float ux[TB_MAXN], uy[TB_MAXN], uz[TB_MAXN], rr[TB_MAXN];
     int sl[TB_MAXN];
@@ -242,7 +267,7 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
         const unsigned e = nbr[at];
         const PosPack pj = pack[nbr_index(e)];
         if (!p.single_type && pack_type(pj.hi) != p.ta) continue;
-        const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, p.L);
+        const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, L);
         const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
         if (!(r2 < p.rc2)) continue;
         const float r = sqrtf(r2);
@@ -288,9 +313,8 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
         float dfc_ij;
         const float fc_ij = ters_fc(p, rij, dfc_ij);
         const float fR = p.A * expf(-p.l1 * rij), fA = p.B * expf(-p.l2 * rij);
-        const float bn = powf(p.beta * zeta, p.nn);
-        const float bij = powf(1.f + bn, -0.5f / p.nn);
-        const float dbdz = zeta > 0.f ? -0.5f * powf(1.f + bn, -0.5f / p.nn - 1.f) * bn / zeta : 0.f;
+        float bij, dbdz;
+        ters_bond_order(p, zeta, bij, dbdz);
         const float vij = fc_ij * (fR - bij * fA);
         const float dv_dr = dfc_ij * (fR - bij * fA) + fc_ij * (-p.l1 * fR + bij * p.l2 * fA);
         const float dv_dz = -fc_ij * fA * dbdz;
@@ -359,6 +383,8 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
 struct ZBLDev {
     int n, hshift, maxnb, ta, tb;
     ShiftF L;
+    const ShiftF* rep_L;  // replica mode (else null)
+    const int* rep_of;
     float rc, rsw, zc, ze0, ze1, ze2, ze3;
     int first;
 };
@@ -373,6 +399,7 @@ __global__ void __launch_bounds__(128) k_zbl(ZBLDev p, const PosPack* __restrict
     if (i >= p.n) return;
     const PosPack pi = pack[i];
     const int ti = pack_type(pi.hi);
+    const ShiftF L = p.rep_L ? p.rep_L[p.rep_of[i]] : p.L;
     float ax = 0.f, ay = 0.f, az = 0.f, ae = 0.f, av = 0.f;
     if (ti == p.ta || ti == p.tb) {
         const int m = nnb[i];
@@ -381,7 +408,7 @@ __global__ void __launch_bounds__(128) k_zbl(ZBLDev p, const PosPack* __restrict
             const PosPack pj = pack[nbr_index(e)];
             const int tj = pack_type(pj.hi);
             if (!((ti == p.ta && tj == p.tb) || (ti == p.tb && tj == p.ta))) continue;
-            const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, p.L);
+            const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, L);
             const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
             const float r = sqrtf(r2);
             if (!(r < p.rc)) continue;
@@ -504,6 +531,8 @@ int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask) {
     p.single_type = c->ntypes == 1;
     p.ta = pot.ta;
     p.L = make_shift(c->box);
+    p.rep_L = c->nrep > 0 ? static_cast<const ShiftF*>(c->d_rep_shift) : nullptr;
+    p.rep_of = c->d_rep_of;
     p.A = (float)t.A;
     p.B = (float)t.B;
     p.l1 = (float)t.lambda1;
@@ -537,6 +566,8 @@ int zbl_launch(Context* c, Potential& pot, bool first) {
     p.ta = pot.ta;
     p.tb = pot.tb;
     p.L = make_shift(c->box);
+    p.rep_L = c->nrep > 0 ? static_cast<const ShiftF*>(c->d_rep_shift) : nullptr;
+    p.rep_of = c->d_rep_of;
     p.rc = (float)z.rc;
     p.rsw = (float)(z.rc - z.width);
     p.zc = (float)z.zc;

@@ -229,3 +229,47 @@ def projectile(target_xy, z_surface, height, theta_deg, phi_deg, energy_ev, mass
     start = np.array([target_xy[0], target_xy[1], z_surface]) + height * u
     speed = math.sqrt(2.0 * energy_ev / mass)
     return start, -speed * u
+
+
+def impact_ensemble(nrep=256, nmin=1000, nmax=16000, temp=300.0, emin=10.0, emax=500.0, theta_max=30.0,
+                    a=5.431, sigma=0.03, height=5.0, vacuum=10.0, seed=6):
+    """Independent Si diamond slabs of uneven size, each aimed at by one Ar atom.
+
+    Replica r has N_r = round(exp(U[ln nmin, ln nmax])) target atoms arranged
+    as an nx x nx x nz cell slab (nx = nz ~ (N_r / 8)^(1/3)), periodic in x
+    and y with a free surface on top, Gaussian displacements `sigma` and
+    Maxwell-Boltzmann velocities at `temp`.  The Ar atom starts `height` above
+    a uniformly drawn aim point on the surface along (theta ~ U[0, theta_max],
+    phi ~ U[0, 360)) with E = exp(U[ln emin, ln emax]) eV (Projectile.h:22-49).
+    Returns per-replica atom counts, positions, velocities, types (0 Si,
+    1 Ar), box lo/hi and the drawn energies and angles.
+    """
+    rng = np.random.default_rng(seed)
+    m_si, m_ar = md_mass("silicon"), md_mass("argon")
+    natoms, xs, vs, ts, los, his, meta = [], [], [], [], [], [], []
+    for r in range(nrep):
+        n_r = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        nx = max(2, int(round((n_r / 8.0) ** (1.0 / 3.0))))
+        nz = max(2, int(round(n_r / (8.0 * nx * nx))))
+        x, lo, hi = lattice(DIAMOND_BASIS, (nx, nx, nz), a, 0.125)
+        x = x + rng.normal(0.0, sigma, size=x.shape)
+        for d in range(2):
+            x[:, d] = np.mod(x[:, d], hi[d])
+        v = maxwell_boltzmann(len(x), temp, m_si, int(rng.integers(1 << 31)))
+        z_top = float(x[:, 2].max())
+        e = math.exp(rng.uniform(math.log(emin), math.log(emax)))
+        th = rng.uniform(0.0, theta_max)
+        ph = rng.uniform(0.0, 360.0)
+        aim = rng.uniform(0.0, 1.0, 2) * hi[:2]
+        p0, pv = projectile(aim, z_top, height, th, ph, e, m_ar)
+        p0[:2] = np.mod(p0[:2], hi[:2])
+        xs.append(np.vstack([x, p0]))
+        vs.append(np.vstack([v, pv]))
+        ts.append(np.concatenate([np.zeros(len(x), dtype=np.int32), [1]]).astype(np.int32))
+        natoms.append(len(x) + 1)
+        los.append([0.0, 0.0, -0.5 * a])
+        his.append([hi[0], hi[1], z_top + height + vacuum])
+        meta.append((e, th, ph))
+    return {"natoms": np.array(natoms), "x": np.concatenate(xs), "v": np.concatenate(vs), "types": np.concatenate(ts),
+            "lo": np.array(los), "hi": np.array(his), "energy_theta_phi": np.array(meta),
+            "masses": [m_si, m_ar], "znum": [14.0, 18.0]}

@@ -70,6 +70,8 @@ SIGNATURES = {
     "omdg_set_profiling": [_vp, _i],
     "omdg_kernel_times": [_vp, _cp, _i, _P(_d), _P(_l), _i, _P(_i)],
     "omdg_count_neighbors_static": [_vp, _i, _P(_d), _P(_d), _P(_i), _d, _vp, _vp, _cp, _i],
+    "omdg_set_replicas": [_vp, _i, _P(_i), _P(_d), _P(_d), _P(_i)],
+    "omdg_replica_ledger": [_vp, _i, _P(_d), _P(_d)],
     "omdg_add_nn": [_vp, _i, _i, _cp, _cp],
     "omdg_nn_fallback_atoms": [_vp, _P(_l)],
     "omdg_nn_create": [_P(_vp), _i],
@@ -335,6 +337,20 @@ class Context:
 
     def add_zbl(self, ta, tb, rc, width):
         self._check(self.lib.omdg_add_zbl(self.h, ta, tb, float(rc), float(width)))
+
+    def set_replicas(self, natoms, lo, hi, periodic=(1, 1, 0)):
+        natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+        lo = np.ascontiguousarray(lo, dtype=np.float64).reshape(-1, 3)
+        hi = np.ascontiguousarray(hi, dtype=np.float64).reshape(-1, 3)
+        per = (ctypes.c_int * 3)(*[1 if p else 0 for p in periodic])
+        self._check(self.lib.omdg_set_replicas(self.h, len(natoms), _ip(natoms), _dp(lo), _dp(hi), per))
+        self.nrep = len(natoms)
+
+    def replica_ledger(self):
+        k = np.zeros(self.nrep)
+        p = np.zeros(self.nrep)
+        self._check(self.lib.omdg_replica_ledger(self.h, self.nrep, _dp(k), _dp(p)))
+        return k, p
 
     def add_nn(self, model_file, tersoff_fallback=None, ta=0, tb=0):
         fb = tersoff_fallback.encode() if tersoff_fallback else None

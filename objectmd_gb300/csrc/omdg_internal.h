@@ -41,6 +41,8 @@ struct HostTable {
     double dr = 0, off = 0;
     bool rmult = false, allow_lo = false, allow_hi = false;
     double out_lo = 0, out_hi = 0;
+    double constant = 0;          // the section's 'Constant' parameter (TTM tables), if any
+    bool has_constant = false;
     std::vector<double> a, b, c, d;
     double max_range() const { return off + (double)(n - 1) * dr; }
 };

@@ -74,6 +74,8 @@ int table_load(const std::string& file, const std::string& name, HostTable& t, s
     }
     t.allow_lo = meta.count("OutOfRangeLower") > 0;
     t.allow_hi = meta.count("OutOfRangeUpper") > 0;
+    t.has_constant = meta.count("Constant") > 0;
+    num("Constant", 0.0, false, t.constant);
     num("OutOfRangeLower", 0.0, false, t.out_lo);
     num("OutOfRangeUpper", 0.0, false, t.out_hi);
     if (t.n < 4 || !(t.dr > 0)) {

@@ -273,3 +273,30 @@ def impact_ensemble(nrep=256, nmin=1000, nmax=16000, temp=300.0, emin=10.0, emax
     return {"natoms": np.array(natoms), "x": np.concatenate(xs), "v": np.concatenate(vs), "types": np.concatenate(ts),
             "lo": np.array(los), "hi": np.array(his), "energy_theta_phi": np.array(meta),
             "masses": [m_si, m_ar], "znum": [14.0, 18.0]}
+
+
+def ttm_table_text(g0=1.529e-6, c0=8.43e-10, dT=10.0, n=8001, g_slope=1.0 / 20000.0):
+    """Electron-phonon table for TTM_Homogen (TTM_Homogen_SCNA.h:176-180):
+    section ELECTRON_PHONON_COUPLING with G(T) = 1 + g_slope T and Constant
+    g0 (eV / (ps A^3 K)); section ELECTRON_HEAT_CAPACITY with Ce(T) = T and
+    Constant c0 (eV / (A^3 K^2)), so C_e = c0 T.  Knots T = 0, dT, ...
+    Defaults: aluminium, G = 2.45e17 W/(m^3 K), gamma = 135 J/(m^3 K^2)."""
+    T = np.arange(n) * dT
+    out = ["# electron-phonon coupling and electron heat capacity (objectmd_gb300.inputs)"]
+    for name, const, vals in (("ELECTRON_PHONON_COUPLING", g0, 1.0 + g_slope * T),
+                              ("ELECTRON_HEAT_CAPACITY", c0, T)):
+        out += ["#$%s Constant %.17g" % (name, const), "#$%s NumberOfData %d" % (name, n),
+                "#$%s Spacing %.17g" % (name, dT), "#$%s Offset 0" % name, "#$%s Format PLAIN" % name,
+                "#$%s --" % name]
+        out += ["%.17g" % v for v in vals]
+    return "\n".join(out) + "\n"
+
+
+def aluminium_cluster(ncell=6, a=4.05, sigma=0.05, temp=300.0, vacuum=15.0, seed_pos=12, seed_vel=13):
+    """A free FCC Al cluster (ncell^3 cells) in a non-periodic box with
+    `vacuum` A of space on every side."""
+    x, lo, hi = fcc(ncell, a)
+    rng = np.random.default_rng(seed_pos)
+    x = x + rng.normal(0.0, sigma, size=x.shape)
+    v = maxwell_boltzmann(len(x), temp, md_mass("aluminum"), seed_vel)
+    return x, v, (np.asarray(lo) - vacuum, np.asarray(hi) + vacuum)

@@ -289,7 +289,7 @@ def berendsen_factor(dt, tau, tset, tnow):
 # ------------------------------------------------------- reference executable
 
 def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh=0, dump_nbr=False,
-                  pair2=None, tcontrol=None, table_dir=None, swfix=False, time_only=False, timeout=3600):
+                  pair2=None, tcontrol=None, table_dir=None, swfix=False, time_only=False, timeout=3600, ttm=None):
     """Run the reference's own code (oracle/_ref/ref_driver) on an Import file.
 
     Returns a dict with 'atoms' (nid, tid, x, v, f, potential, virial sorted
@@ -306,6 +306,8 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
         args += ["pair2", pair2]
     if tcontrol:
         args += ["tcontrol", repr(tcontrol[0]), repr(tcontrol[1])]
+    if ttm:  # (electron-phonon table file, atom volume, initial electron temperature)
+        args += ["ttm", os.path.abspath(ttm[0]), repr(float(ttm[1])), repr(float(ttm[2]))]
     env = dict(os.environ)
     if table_dir:
         env["OMD_TABLE"] = table_dir
@@ -330,4 +332,8 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
     lp = os.path.join(out, "ledger.txt")
     if os.path.exists(lp):
         res["ledger"] = np.loadtxt(lp, ndmin=2)
+    for name in ("ttm", "thermo"):
+        fp = os.path.join(out, name + ".txt")
+        if os.path.exists(fp):
+            res[name] = np.loadtxt(fp, ndmin=2)
     return res

@@ -21,6 +21,9 @@
  *   skin        <A>      comm.tolerance (absolute)
  *   refresh     <n>      comm.refresh (0 = every step)
  *   tcontrol    <T> <tau>  Berendsen TempController (TempController.h:78-91)
+ *   ttm         <file> <atom_volume> <Te0>  TTM_Homogen (TTM_Homogen_SCNA.h) with an
+ *                        intensive ThermoDetector (ThermoDetector.h); writes ttm.txt
+ *                        (step Te int_Een int_Aen avg_temp) and thermo.txt (nid T_i n_i)
  *   dump_nbr    0|1      write the neighbour tuples of the final list
  *   time_only   0|1      only print the RunKernel wall time
  *
@@ -38,6 +41,8 @@ using namespace omd;
 #include <modify/VerletList.h>
 #include <modify/VerletListFull.h>
 #include <modify/TempController.h>
+#include <detect/ThermoDetector.h>
+#include <misc/TTM_Homogen_SCNA.h>
 
 #include <sys/time.h>
 #include <algorithm>
@@ -83,10 +88,13 @@ public:
     int nsteps;
     double t_begin, t_end;
     FILE* ledger;
+    FILE* ttmlog;
+    ThermoDetector* thermo;
 
     OracleSim(int& argc, char**& argv, const std::string& od,
               const std::map<std::string, std::vector<std::string> >& o)
-        : MDSystemGrid(argc, argv), opt(o), outdir(od), nsteps(0), t_begin(0), t_end(0), ledger(0) {
+        : MDSystemGrid(argc, argv), opt(o), outdir(od), nsteps(0), t_begin(0), t_end(0), ledger(0), ttmlog(0),
+          thermo(0) {
         nsteps = atoi(get("steps", "0").c_str());
     }
 
@@ -124,6 +132,11 @@ public:
             AddForce(k, "target", "target");
             AddForce(new TForcePair(pair2), "projectile", "target");
         }
+        if (opt.count("ttm")) {
+            thermo = new ThermoDetector(1e30);  // sample time beyond the run: no dump files
+            AddDetector(thermo);
+            AddModify(new TTM_Homogen());
+        }
         if (opt.count("tcontrol"))
             AddModify(new TempController(atof(get("tcontrol", "300", 0).c_str()),
                                          atof(get("tcontrol", "0.1", 1).c_str())));
@@ -135,6 +148,10 @@ public:
         bool base = MDSystemGrid::CheckRun();
         if (ledger && Step > 0)
             fprintf(ledger, "%d %.17g %.17g %.17g\n", Step, Kinetic, Potential, Energy);
+        if (ttmlog && Step > 0)
+            fprintf(ttmlog, "%d %.17g %.17g %.17g %.17g\n", Step, GetMessageSlot("e_temp:")->AsDouble(),
+                    GetMessageSlot("int_Een:")->AsDouble(), GetMessageSlot("int_Aen:")->AsDouble(),
+                    thermo->GetTemperatureAvg());
         return base && Step < nsteps;
     }
 
@@ -143,6 +160,7 @@ public:
             ledger = fopen((outdir + "/ledger.txt").c_str(), "w");
             if (ledger)
                 fprintf(ledger, "%d %.17g %.17g %.17g\n", 0, Kinetic, BasePotential, 0.0);
+            if (opt.count("ttm")) ttmlog = fopen((outdir + "/ttm.txt").c_str(), "w");
         }
         t_begin = wall_now();
     }
@@ -182,6 +200,19 @@ public:
         }
         fclose(f);
         if (get("dump_nbr", "0") != "0") DumpNeighbours();
+        if (ttmlog) {
+            fclose(ttmlog);
+            ttmlog = 0;
+        }
+        if (thermo) {
+            FILE* t = fopen((outdir + "/thermo.txt").c_str(), "w");
+            for (int k = 0; k < nloc; k++) {
+                Atom& a = Atoms(order[k]);
+                fprintf(t, "%d %.17g %.17g\n", a.nid, a.aux[thermo->GetAuxTempIndex()],
+                        a.aux[thermo->GetAuxDensIndex()]);
+            }
+            fclose(t);
+        }
     }
 
     struct CompareNid {
@@ -242,7 +273,7 @@ int main(int argc, char** argv) {
     std::map<std::string, std::vector<std::string> > opt;
     for (int i = 2; i < argc;) {
         std::string key = argv[i++];
-        int nval = (key == "tcontrol") ? 2 : 1;
+        int nval = (key == "tcontrol") ? 2 : (key == "ttm" ? 3 : 1);
         for (int k = 0; k < nval && i < argc; k++) opt[key].push_back(argv[i++]);
     }
     /* Table mode: the reference TableReader itself (treader.cpp) evaluated at
@@ -279,6 +310,14 @@ int main(int argc, char** argv) {
     args.push_back("1e30");
     args.push_back("--silent");
     if (!opt.count("steps") || atoi(opt["steps"][0].c_str()) == 0) args.push_back("mode.static");
+    if (opt.count("ttm")) {
+        args.push_back("ttmsc.electron-phonon_file");
+        args.push_back(opt["ttm"][0]);
+        args.push_back("ttmsc.atom_volume");
+        args.push_back(opt["ttm"][1]);
+        args.push_back("ttmsc.electron_init_temperature");
+        args.push_back(opt["ttm"][2]);
+    }
     std::vector<char*> cargs;
     for (size_t i = 0; i < args.size(); i++) cargs.push_back(const_cast<char*>(args[i].c_str()));
     cargs.push_back(0);

@@ -100,10 +100,30 @@ def save_case(name, import_file, res, **extra):
     print("wrote", name, "atoms", len(a), "tuples", len(res.get("nbr", [])))
 
 
-def main():
+def ttm_case(tdir, work):
+    """TTM_Homogen with an intensive ThermoDetector on a free EAM Al cluster
+    (no periodic images: no ghost atoms): electron temperature trace, kinetic
+    trace and the final per-atom local temperatures and densities."""
+    with open(os.path.join(TABLES, "ttm.aluminum"), "w") as fh:
+        fh.write(inputs.ttm_table_text())
+    x, v, (lo, hi) = inputs.aluminium_cluster(ncell=6, temp=300.0)
+    f = os.path.join(work, "ttm_al_cluster.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), periodic=(False, False, False), species=("aluminum",))
+    vol, te0, steps, dt = 16.6, 5000.0, 60, 0.002
+    res = oc.run_reference(f, "eam", "aluminum5000", steps=steps, dt=dt, table_dir=tdir,
+                           ttm=(os.path.join(TABLES, "ttm.aluminum"), vol, te0))
+    th = res["thermo"]
+    save_case("ttm_al_cluster", f, res, box_lo=lo, box_hi=hi, steps=np.array(steps), dt=np.array(dt),
+              atom_volume=np.array(vol), te0=np.array(te0), ttm=res["ttm"], local_temp=th[:, 1], local_dens=th[:, 2])
+
+
+def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not oc.build_reference(REF):
         raise SystemExit("reference sources not found at %s" % REF)
+    if only == "ttm":
+        ttm_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
+        return
     write_eam5000(os.path.join(TABLES, "eam.aluminum5000"))
     with open(os.path.join(TABLES, "pair.lj.argon"), "w") as fh:
         fh.write(inputs.lj_table_text())
@@ -179,8 +199,9 @@ def main():
         np.savez_compressed(os.path.join(GOLD, "table_%s.npz" % sec.lower()), r=tab[:, 0], val=tab[:, 1],
                             dval=tab[:, 2])
         print("wrote table_%s" % sec.lower(), len(tab))
+    ttm_case(tdir, work)
     print("done")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

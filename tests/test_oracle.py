@@ -199,3 +199,47 @@ def test_reference_thermostat_counts_ghost_images(oracle_lib):
 def test_berendsen_factor(oracle_lib):
     # TempController.h:86: sqrt(1 + dt/tau (T0/T - 1))
     assert abs(oracle_lib.berendsen_factor(0.002, 0.05, 300.0, 600.0) - np.sqrt(1 + 0.04 * (0.5 - 1))) < 1e-15
+
+
+def test_ttm_oracle_matches_reference(oracle_lib):
+    """TTM_Homogen + intensive ThermoDetector on a free EAM Al cluster, 60 steps:
+    the restatement (oracle/ttm_oracle.py) replays the reference's electron
+    temperature, integrated energies, mean and per-atom local temperatures."""
+    oc = oracle_lib
+    from objectmd_gb300 import inputs
+    from oracle import ttm_oracle as tt
+
+    d = load_case("ttm_al_cluster")
+    phi, ed, em = eam_tables(oc)
+    tab = os.path.join(TABLES, "ttm.aluminum")
+    G = oc.Table.from_file(tab, "ELECTRON_PHONON_COUPLING")
+    Ce = oc.Table.from_file(tab, "ELECTRON_HEAT_CAPACITY")
+    box = oc.make_box(d["box_lo"], d["box_hi"], (0, 0, 0))
+    x = d["x0"].copy()
+    v = d["v0"].copy()
+    n = len(x)
+    mass = np.full(n, inputs.md_mass("aluminum"))
+    rv = phi.max_range() + 0.3
+    dt = float(d["dt"])
+    ttm = tt.TTM(G, Ce, 1.529e-6, 8.43e-10, float(d["atom_volume"]), float(d["te0"]), dt)
+    f = np.zeros((n, 3))
+    thermo = tt.local_thermo(x, v, mass, phi.max_range())
+    kinetic = oc.kinetic(v, mass)
+    rows, kin = [], []
+    for k in range(int(d["steps"])):
+        vmax = np.sqrt((v * v).sum(1).max())
+        v = ttm.pre_integration(k * dt, thermo, v, mass, kinetic, vmax)
+        oc.vv_kick_drift(x, v, f, mass, dt)
+        f = oc.eam(box, x, oc.neighbors(box, x, rv), phi, ed, em)[0]
+        oc.vv_kick(v, f, mass, dt)
+        kinetic = oc.kinetic(v, mass)
+        kin.append(kinetic)
+        thermo = tt.local_thermo(x, v, mass, phi.max_range())
+        rows.append((k + 1, ttm.te, ttm.int_een, ttm.int_aen, thermo["avg_temp"]))
+    rows = np.array(rows)
+    ref = d["ttm"]
+    np.testing.assert_allclose(rows[:, 1], ref[:, 1], rtol=1e-11)
+    np.testing.assert_allclose(rows[:, 2:], ref[:, 2:], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(kin, d["ledger"][1:1 + len(kin), 1], rtol=1e-10)
+    np.testing.assert_allclose(thermo["temp"], d["local_temp"], rtol=1e-9)
+    np.testing.assert_allclose(thermo["dens"], d["local_dens"], rtol=1e-12)

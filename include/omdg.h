@@ -196,6 +196,33 @@ int omdg_set_profiling(omdg_ctx* ctx, int on);
 /* name_buf receives "name;name;..."; ms[] the summed milliseconds, calls[] the launch counts. */
 int omdg_kernel_times(omdg_ctx* ctx, char* name_buf, int name_cap, double* ms, long* calls, int cap, int* nkern);
 
+/* ------------------------------------- local thermodynamics, two-temperature */
+
+/*
+ * ThermoDetector in intensive mode (include/detect/ThermoDetector.h:176-237):
+ * after every step, each atom's local centre-of-mass velocity, temperature
+ * and density over itself and its neighbours within ercut (<= 0: the largest
+ * cutoff of the force kernels, as the reference's default).
+ */
+int omdg_set_thermo_detector(omdg_ctx* ctx, int on, double ercut);
+/* Local temperature (K), density (1/A^3) and centre-of-mass velocity (n*3) per atom, caller order; may be NULL. */
+int omdg_local_thermo(omdg_ctx* ctx, double* temperature, double* density, double* vcm);
+/*
+ * TTM_Homogen (include/misc/TTM_Homogen_SCNA.h): a homogeneous electron
+ * temperature coupled to the lattice by scaling-corrected velocity rescaling
+ * about each atom's local centre of mass.  table_file holds the
+ * ELECTRON_PHONON_COUPLING and ELECTRON_HEAT_CAPACITY sections (each with a
+ * Constant); atom_volume in A^3; electron_temperature < 0 starts from the
+ * lattice temperature; coupling starts once the elapsed time exceeds
+ * pulse_offset (ps).  Turns the detector on.
+ */
+int omdg_set_ttm(omdg_ctx* ctx, const char* table_file, double atom_volume, double electron_temperature,
+                 double pulse_offset);
+/* Electron temperature, integrated electron energy, integrated energy per atom given to the lattice, and the mean
+   local lattice temperature (the "e_temp:", "int_Een:", "int_Aen:" slots and GetTemperatureAvg). */
+int omdg_ttm_state(omdg_ctx* ctx, double* electron_temperature, double* int_een, double* int_aen,
+                   double* lattice_temperature);
+
 /* ------------------------------------------------------ neural surrogate */
 
 /*

@@ -268,6 +268,7 @@ int omdg_destroy(omdg_ctx* c) {
         }
         nn_release(p);
     }
+    ttm_release(c);
     for (auto e : c->event_pool) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -832,7 +833,8 @@ static int capture_step(Context* c, GraphState& gs) {
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return check_cuda(c, e, "capture begin");
     long l0 = c->launches, l1 = 0, l2 = 0;
-    int rc = integrate_kick_drift(c, 0);
+    int rc = (c->ttm && ttm_active(c)) ? ttm_pre(c) : OMDG_OK;  // PreIntegration (TTM_Homogen_SCNA.h:352)
+    if (!rc) rc = integrate_kick_drift(c, 0);
     cudaGraph_t g = nullptr;
     cudaStreamCaptureStatus cst;
     const cudaGraphNode_t* deps = nullptr;
@@ -875,6 +877,7 @@ static int capture_step(Context* c, GraphState& gs) {
     l2 = c->launches;
     if (!rc) rc = forces_compute(c);
     if (!rc) rc = integrate_kick(c, 0);
+    if (!rc && c->ttm) rc = thermo_detect(c);  // ExecuteDetectors (system.cpp:976)
     long l3 = c->launches;
     // captured launches are counted when the graph replays, not here
     c->graph_step_kernels = (l1 - l0) + (l3 - l2);
@@ -963,6 +966,7 @@ int omdg_compute_forces(omdg_ctx* c) {
     if ((rc = threebody_prepare(c))) return rc;
     if ((rc = forces_compute(c))) return rc;
     if ((rc = measure_energies(c, 0))) return rc;
+    if (c->ttm && (rc = thermo_detect(c))) return rc;
     prof_collect(c);
     if ((rc = check_status(c))) return rc;
     // a non-step evaluation writes the ledger row the next step would use
@@ -1001,6 +1005,8 @@ int omdg_set_compat(omdg_ctx* c, const char* key, int on) {
 
 int omdg_set_thermostat(omdg_ctx* c, double temperature, double tau) {
     if (!c) return OMDG_EINVAL;
+    if (tau > 0.0 && c->ttm && ttm_active(c))
+        return set_error(c, OMDG_EINVAL, "the Berendsen thermostat and the two-temperature model exclude each other");
     c->thermo_T = temperature;
     c->thermo_tau = tau;
     invalidate_graph(c);
@@ -1017,6 +1023,8 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         if ((rc = build_list(c))) return rc;
         if ((rc = threebody_prepare(c))) return rc;
         if ((rc = step_state_init(c))) return rc;
+        // TTM's first PreIntegration only measures (TTM_Homogen_SCNA.h:356-366)
+        if (c->ttm && (rc = thermo_detect(c))) return rc;
         if ((rc = forces_compute(c))) return rc;
         if ((rc = measure_energies(c, 0))) return rc;
         if ((rc = check_status(c))) return rc;
@@ -1037,10 +1045,12 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
     if (c->async_steps == 0) c->launches_at_sync = c->launches;
     if (c->profiling) {
         for (int k = 0; k < nsteps; k++) {
+            if (c->ttm && ttm_active(c) && (rc = ttm_pre(c))) return rc;
             if ((rc = integrate_kick_drift(c, k))) return rc;
             if ((rc = eager_maybe_rebuild(c))) return rc;
             if ((rc = forces_compute(c))) return rc;
             if ((rc = integrate_kick(c, k))) return rc;
+            if (c->ttm && (rc = thermo_detect(c))) return rc;
         }
         prof_collect(c);
     } else {

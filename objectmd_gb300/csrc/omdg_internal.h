@@ -91,6 +91,7 @@ struct __align__(32) PosPack {
 enum PotKind { POT_EAM = 1, POT_PAIR = 2, POT_SW = 3, POT_TERSOFF = 4, POT_ZBL = 5, POT_NN = 6 };
 
 struct NNState;  // neural surrogate (nn_potential.cu)
+struct TTMCtx;   // local thermodynamics and the two-temperature model (ttm.cu)
 
 struct SWParams {
     double eps, A, B, p, q, sigma, a, lambda, gamma, icos0;
@@ -174,6 +175,7 @@ struct Context {
     void* d_rep_geom = nullptr;          // RepGeom[nrep] (nlist.cu)
     void* d_rep_shift = nullptr;         // ShiftF[nrep]: periodic lengths for pair_delta
     double* d_rep_sums = nullptr;        // per-replica ledger sums
+    TTMCtx* ttm = nullptr;               // ThermoDetector / TTM_Homogen state (null: off)
     int* d_rep_start = nullptr;          // nrep + 1
     int ncell_cap = 0;
     int* scan_partials = nullptr;
@@ -293,6 +295,10 @@ int gather_slots(Context* c, bool zero_virial);
 int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask);
 int nn_launch(Context* c, Potential& pot, bool first);
 int replica_prepare(Context* c);  // per-replica cell grids and shifts (host, before a build)
+int thermo_detect(Context* c);    // local temperatures after a step (ttm.cu)
+int ttm_pre(Context* c);          // electron temperature step and rescaling before a step
+void ttm_release(Context* c);
+bool ttm_active(const Context* c);
 int replica_sums(Context* c, double* kinetic, double* potential);  // per-replica ledger (synchronous)
 void update_rc(Context* c);         // largest cutoff; drops the list and the step graph
 void invalidate_graph(Context* c);

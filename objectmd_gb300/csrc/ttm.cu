@@ -1,0 +1,515 @@
+// Local thermodynamics (ThermoDetector, include/detect/ThermoDetector.h) and
+// the homogeneous scaling-corrected two-temperature model (TTM_Homogen,
+// include/misc/TTM_Homogen_SCNA.h) on the device.
+//
+// Detector, after every step (ExtractTemperature, ThermoDetector.h:176-237),
+// over each atom and its list neighbours within ercut:
+//   k_thermo_cm     v_cm_i = sum m_j v_j / sum m_j, n_i = 1 + neighbours
+//   k_thermo_temp   T_i = 2/(3 k_B) 1/2 sum m_j |v_j - v_cm_j|^2 / n_i,
+//                   density n_i / (4/3 pi ercut^3); block partials of the
+//                   averages (atoms with n_i >= 2), kinetic energy, max v^2
+//   k_thermo_final  one block, fixed order
+// TTM, before the kick-drift of every step (PreIntegration, :337-376):
+//   k_ttm_fd        one thread: electron temperature step (fd_main_loop, :232-263)
+//   k_ttm_scale     rescaling about the local centre of mass (velocity_scalling, :272-330)
+//   k_ttm_sum       one block: integrated lattice energy
+// Distances as CalcDistance: an FP32 screen from the position packs, and
+// sqrt((dx dx + dy dy) + dz dz) <= ercut in FP64 near the edge.
+#include <cmath>
+#include <string>
+
+#include "device_common.cuh"
+
+namespace omdg {
+
+constexpr int TH_BLOCK = 128;
+
+struct TTMState {
+    double te, int_een, int_aen, n_zero, coup;
+    double t_avg, d_avg, kin, vmax2, elapsed;
+    int firstfd, active, navg, pad;
+};
+
+struct ThermoParams {
+    int n, hshift, maxnb;
+    ShiftF L;
+    double L64[3];
+    double rc, rc2;
+    float rc2_lo, rc2_hi;
+    double volcut, fac;
+};
+
+struct TTMCtx {
+    bool ttm = false;
+    HostTable g, ce;
+    DevTable dg{}, dce{};
+    double4_32a* coef64[2] = {nullptr, nullptr};
+    double g0 = 0, c0 = 0, vol = 0, te0 = -1, offset = 0;
+    double ercut = -1;                  // <= 0: the largest cutoff of the force kernels
+    double *vcm = nullptr, *temp = nullptr, *dens = nullptr;  // 3n, n, n
+    int* nneig = nullptr;
+    double* partial = nullptr;          // per block: T, dens, count, kinetic, max v^2; + scale partials
+    TTMState* st = nullptr;
+    int cap = 0, nblocks = 0;
+};
+
+// Within ercut: the FP32 screen, and the reference's FP64 distance in the band.
+__device__ __forceinline__ bool th_within(const ThermoParams& p, const PosPack& pi, const PosPack& pj, unsigned e,
+                                          int i, int j, const double* __restrict__ x, const double* __restrict__ y,
+                                          const double* __restrict__ z) {
+    const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, p.L);
+    const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+    if (r2 > p.rc2_hi) return false;
+    if (r2 < p.rc2_lo) return true;
+    const int sx = nbr_sx(e), sy = nbr_sy(e), sz = nbr_sz(e);
+    const double gx = sx == 0 ? 0.0 : (sx > 0 ? p.L64[0] : -p.L64[0]);
+    const double gy = sy == 0 ? 0.0 : (sy > 0 ? p.L64[1] : -p.L64[1]);
+    const double gz = sz == 0 ? 0.0 : (sz > 0 ? p.L64[2] : -p.L64[2]);
+    const double dx = __dsub_rn(x[i], __dadd_rn(x[j], gx));
+    const double dy = __dsub_rn(y[i], __dadd_rn(y[j], gy));
+    const double dz = __dsub_rn(z[i], __dadd_rn(z[j], gz));
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz))) <= p.rc;
+}
+
+__global__ void __launch_bounds__(TH_BLOCK) k_thermo_cm(ThermoParams p, const PosPack* __restrict__ pack,
+                                                        const unsigned* __restrict__ nbr,
+                                                        const int* __restrict__ nnb, const double* __restrict__ x,
+                                                        const double* __restrict__ y, const double* __restrict__ z,
+                                                        const double* __restrict__ vx, const double* __restrict__ vy,
+                                                        const double* __restrict__ vz, const int* __restrict__ type,
+                                                        const double* __restrict__ mass, double* __restrict__ vcm,
+                                                        int* __restrict__ nneig) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const PosPack pi = pack[i];
+    double ms = mass[type[i]];
+    double px = ms * vx[i], py = ms * vy[i], pz = ms * vz[i];
+    int cnt = 1;
+    const int m = nnb[i];
+    for (int s = 0; s < m; s++) {
+        const unsigned e = nbr[nbr_at(i, s, p.hshift, p.maxnb)];
+        const int j = nbr_index(e);
+        if (!th_within(p, pi, pack[j], e, i, j, x, y, z)) continue;
+        const double mj = mass[type[j]];
+        ms += mj;
+        px = fma(mj, vx[j], px);
+        py = fma(mj, vy[j], py);
+        pz = fma(mj, vz[j], pz);
+        cnt++;
+    }
+    vcm[i] = px / ms;
+    vcm[p.n + i] = py / ms;
+    vcm[2 * (size_t)p.n + i] = pz / ms;
+    nneig[i] = cnt;
+}
+
+__device__ __forceinline__ double th_ek(int j, const double* __restrict__ vx, const double* __restrict__ vy,
+                                        const double* __restrict__ vz, const double* __restrict__ vcm, int n,
+                                        double mj) {
+    const double cx = vx[j] - vcm[j], cy = vy[j] - vcm[n + j], cz = vz[j] - vcm[2 * (size_t)n + j];
+    return mj * (cx * cx + cy * cy + cz * cz);
+}
+
+__global__ void __launch_bounds__(TH_BLOCK) k_thermo_temp(
+    ThermoParams p, const PosPack* __restrict__ pack, const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+    const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+    const double* __restrict__ vx, const double* __restrict__ vy, const double* __restrict__ vz,
+    const int* __restrict__ type, const double* __restrict__ mass, const double* __restrict__ vcm,
+    const int* __restrict__ nneig, double* __restrict__ temp, double* __restrict__ dens, double* __restrict__ partial) {
+    __shared__ double st[5][TH_BLOCK];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double a_t = 0.0, a_d = 0.0, a_n = 0.0, kin = 0.0, v2max = 0.0;
+    if (i < p.n) {
+        const PosPack pi = pack[i];
+        const double mi = mass[type[i]];
+        double sum = th_ek(i, vx, vy, vz, vcm, p.n, mi);
+        const int m = nnb[i];
+        for (int s = 0; s < m; s++) {
+            const unsigned e = nbr[nbr_at(i, s, p.hshift, p.maxnb)];
+            const int j = nbr_index(e);
+            if (!th_within(p, pi, pack[j], e, i, j, x, y, z)) continue;
+            sum += th_ek(j, vx, vy, vz, vcm, p.n, mass[type[j]]);
+        }
+        const int nn = nneig[i];
+        const double t = p.fac * (0.5 * sum / (double)nn);
+        const double dn = (double)nn / p.volcut;
+        temp[i] = t;
+        dens[i] = dn;
+        if (nn >= 2) {
+            a_t = t;
+            a_d = dn;
+            a_n = 1.0;
+        }
+        const double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+        kin = mi * v2;
+        v2max = v2;
+    }
+    st[0][threadIdx.x] = a_t;
+    st[1][threadIdx.x] = a_d;
+    st[2][threadIdx.x] = a_n;
+    st[3][threadIdx.x] = kin;
+    st[4][threadIdx.x] = v2max;
+    __syncthreads();
+    for (int off = TH_BLOCK / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            for (int q = 0; q < 4; q++) st[q][threadIdx.x] += st[q][threadIdx.x + off];
+            st[4][threadIdx.x] = fmax(st[4][threadIdx.x], st[4][threadIdx.x + off]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 5; q++) partial[5 * (size_t)blockIdx.x + q] = st[q][0];
+}
+
+__global__ void k_thermo_final(int nblocks, const double* __restrict__ partial, TTMState* st) {
+    __shared__ double red[5][256];
+    double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        for (int q = 0; q < 4; q++) a[q] += partial[5 * (size_t)b + q];
+        a[4] = fmax(a[4], partial[5 * (size_t)b + 4]);
+    }
+    for (int q = 0; q < 5; q++) red[q][threadIdx.x] = a[q];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            for (int q = 0; q < 4; q++) red[q][threadIdx.x] += red[q][threadIdx.x + off];
+            red[4][threadIdx.x] = fmax(red[4][threadIdx.x], red[4][threadIdx.x + off]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double cnt = red[2][0];
+        st->t_avg = cnt > 0.0 ? red[0][0] / cnt : 0.0;
+        st->d_avg = cnt > 0.0 ? red[1][0] / cnt : 0.0;
+        st->navg = (int)cnt;
+        st->kin = 0.5 * red[3][0];
+        st->vmax2 = red[4][0];
+    }
+}
+
+struct TTMParams {
+    DevTable g, ce;
+    double g0, c0, vol, te0, offset, dt;
+    int natoms;
+};
+
+__global__ void k_ttm_fd(TTMParams p, TTMState* st, unsigned* status) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const bool active = st->elapsed > p.offset;
+    st->active = active ? 1 : 0;
+    st->elapsed += p.dt;
+    if (!active) return;
+    const double ta = st->t_avg;
+    double v, dv;
+    if (st->firstfd) {
+        if (st->te < 0.0) st->te = ta;
+        tab_read64(p.ce, st->te, v, dv, status);
+        st->int_een = 0.5 * st->te * p.c0 * v * p.vol;
+        st->int_aen = 2.0 * st->kin / p.natoms;
+        st->n_zero = st->d_avg;
+        st->firstfd = 0;
+    }
+    tab_read64(p.g, st->te, v, dv, status);
+    const double de = -p.g0 * v * (st->te - ta) * p.dt;
+    st->int_een += de * p.vol;
+    tab_read64(p.ce, st->te, v, dv, status);
+    st->te += de / (p.c0 * v);
+    tab_read64(p.g, st->te, v, dv, status);
+    st->coup = p.g0 * v;
+}
+
+__global__ void __launch_bounds__(TH_BLOCK) k_ttm_scale(TTMParams p, int n, double volcut,
+                                                        const TTMState* __restrict__ st, double* __restrict__ vx,
+                                                        double* __restrict__ vy, double* __restrict__ vz,
+                                                        const int* __restrict__ type, const double* __restrict__ mass,
+                                                        const double* __restrict__ vcm,
+                                                        const double* __restrict__ temp,
+                                                        const double* __restrict__ dens, double* __restrict__ partial) {
+    __shared__ double se[TH_BLOCK], sc[TH_BLOCK];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double de = 0.0, cnt = 0.0;
+    if (st->active && i < n && dens[i] * volcut > 3.0) {
+        const double m = mass[type[i]];
+        const double e = st->coup * (st->te - temp[i]) * p.vol * p.dt;
+        const double cmx = vcm[i], cmy = vcm[n + i], cmz = vcm[2 * (size_t)n + i];
+        const double ux = vx[i], uy = vy[i], uz = vz[i];
+        const double cx = ux - cmx, cy = uy - cmy, cz = uz - cmz;
+        const double c2 = cx * cx + cy * cy + cz * cz;
+        const double small = st->vmax2 * 1e-12;
+        if (!(c2 < small)) {
+            const double cmc = cmx * cx + cmy * cy + cmz * cz;
+            const double cm2 = cmx * cmx + cmy * cmy + cmz * cmz;
+            const double v2 = ux * ux + uy * uy + uz * uz;
+            const double rr = cmc * cmc + c2 * (2.0 * e / m + v2 - cm2);
+            if (!(rr < 0.0)) {
+                const double sa = (-cmc + sqrt(rr)) / c2;
+                vx[i] = cmx + sa * cx;
+                vy[i] = cmy + sa * cy;
+                vz[i] = cmz + sa * cz;
+                de = e;
+                cnt = 1.0;
+            }
+        }
+    }
+    se[threadIdx.x] = de;
+    sc[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int off = TH_BLOCK / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            se[threadIdx.x] += se[threadIdx.x + off];
+            sc[threadIdx.x] += sc[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[2 * (size_t)blockIdx.x] = se[0];
+        partial[2 * (size_t)blockIdx.x + 1] = sc[0];
+    }
+}
+
+__global__ void k_ttm_sum(int nblocks, const double* __restrict__ partial, TTMState* st) {
+    __shared__ double se[256], sc[256];
+    double e = 0.0, c = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        e += partial[2 * (size_t)b];
+        c += partial[2 * (size_t)b + 1];
+    }
+    se[threadIdx.x] = e;
+    sc[threadIdx.x] = c;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            se[threadIdx.x] += se[threadIdx.x + off];
+            sc[threadIdx.x] += sc[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && st->active && sc[0] > 0.0) st->int_aen += se[0] / sc[0];
+}
+
+// ------------------------------------------------------------------ host
+static int th_ensure(Context* c, TTMCtx& t) {
+    if (t.cap >= c->n && t.st) return OMDG_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(c->stream, &cs);
+    if (cs != cudaStreamCaptureStatusNone) return set_error(c, OMDG_ESTATE, "detector buffers missing in capture");
+    cudaFree(t.vcm);
+    cudaFree(t.temp);
+    cudaFree(t.dens);
+    cudaFree(t.nneig);
+    cudaFree(t.partial);
+    const size_t n = (size_t)std::max(c->cap, c->n);
+    t.nblocks = grid_for((int)n, TH_BLOCK);
+    cudaError_t e = cudaMalloc(&t.vcm, sizeof(double) * 3 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&t.temp, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&t.dens, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&t.nneig, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&t.partial, sizeof(double) * 5 * t.nblocks);
+    if (e == cudaSuccess && !t.st) {
+        e = cudaMalloc(&t.st, sizeof(TTMState));
+        TTMState h{};
+        h.te = t.te0;
+        h.firstfd = 1;
+        if (e == cudaSuccess) e = cudaMemcpy(t.st, &h, sizeof(h), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) return set_error(c, OMDG_ENOMEM, "detector buffers");
+    t.cap = (int)n;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+static ThermoParams th_params(const Context* c, const TTMCtx& t) {
+    ThermoParams p;
+    p.n = c->n;
+    p.hshift = c->nbr_hshift;
+    p.maxnb = c->maxnb;
+    p.L = make_shift(c->box);
+    for (int d = 0; d < 3; d++) p.L64[d] = c->box.periodic[d] ? c->box.L[d] : 0.0;
+    p.rc = t.ercut > 0 ? t.ercut : c->rc_max;
+    p.rc2 = p.rc * p.rc;
+    p.rc2_lo = (float)(p.rc2 * (1.0 - 2e-5));
+    p.rc2_hi = (float)(p.rc2 * (1.0 + 2e-5));
+    p.volcut = 4.0 * M_PI * p.rc * p.rc * p.rc / 3.0;
+    p.fac = 2.0 / 3.0 / 8.61734279e-05;
+    return p;
+}
+
+int thermo_detect(Context* c) {
+    TTMCtx& t = *c->ttm;
+    int rc = th_ensure(c, t);
+    if (rc) return rc;
+    const ThermoParams p = th_params(c, t);
+    if (p.rc > c->rc_max + c->skin) return set_error(c, OMDG_EINVAL, "detector cutoff beyond the neighbour list");
+    const unsigned* nbr = reinterpret_cast<const unsigned*>(c->nbr);
+    const int g = grid_for(c->n, TH_BLOCK);
+    prof_begin(c, "thermo_detector");
+    k_thermo_cm<<<g, TH_BLOCK, 0, c->stream>>>(p, c->pack, nbr, c->nnb, c->x, c->y, c->z, c->vx, c->vy, c->vz,
+                                                c->type, c->d_mass, t.vcm, t.nneig);
+    k_thermo_temp<<<g, TH_BLOCK, 0, c->stream>>>(p, c->pack, nbr, c->nnb, c->x, c->y, c->z, c->vx, c->vy, c->vz,
+                                                  c->type, c->d_mass, t.vcm, t.nneig, t.temp, t.dens, t.partial);
+    k_thermo_final<<<1, 256, 0, c->stream>>>(g, t.partial, t.st);
+    prof_end(c);
+    c->launches += 3;
+    return check_cuda(c, cudaGetLastError(), "thermo detector");
+}
+
+int ttm_pre(Context* c) {
+    TTMCtx& t = *c->ttm;
+    int rc = th_ensure(c, t);
+    if (rc) return rc;
+    TTMParams p;
+    p.g = t.dg;
+    p.ce = t.dce;
+    p.g0 = t.g0;
+    p.c0 = t.c0;
+    p.vol = t.vol;
+    p.te0 = t.te0;
+    p.offset = t.offset;
+    p.dt = c->dt;
+    p.natoms = c->n;
+    const ThermoParams tp = th_params(c, t);
+    const int g = grid_for(c->n, TH_BLOCK);
+    prof_begin(c, "ttm");
+    k_ttm_fd<<<1, 32, 0, c->stream>>>(p, t.st, c->d_status);
+    k_ttm_scale<<<g, TH_BLOCK, 0, c->stream>>>(p, c->n, tp.volcut, t.st, c->vx, c->vy, c->vz, c->type, c->d_mass,
+                                                t.vcm, t.temp, t.dens, t.partial);
+    k_ttm_sum<<<1, 256, 0, c->stream>>>(g, t.partial, t.st);
+    prof_end(c);
+    c->launches += 3;
+    return check_cuda(c, cudaGetLastError(), "ttm");
+}
+
+bool ttm_active(const Context* c) { return c->ttm && c->ttm->ttm; }
+
+void ttm_release(Context* c) {
+    if (!c->ttm) return;
+    TTMCtx& t = *c->ttm;
+    cudaFree(t.vcm);
+    cudaFree(t.temp);
+    cudaFree(t.dens);
+    cudaFree(t.nneig);
+    cudaFree(t.partial);
+    cudaFree(t.st);
+    cudaFree(t.coef64[0]);
+    cudaFree(t.coef64[1]);
+    delete c->ttm;
+    c->ttm = nullptr;
+}
+
+static int upload64(Context* c, HostTable& h, DevTable& d, double4_32a*& buf) {
+    std::vector<double4_32a> v(h.n);
+    for (int k = 0; k < h.n; k++) v[k] = make_double4_32a(h.a[k], h.b[k], h.c[k], h.d[k]);
+    if (cudaMalloc(&buf, sizeof(double4_32a) * h.n) != cudaSuccess) return set_error(c, OMDG_ENOMEM, "ttm tables");
+    cudaMemcpy(buf, v.data(), sizeof(double4_32a) * h.n, cudaMemcpyHostToDevice);
+    d = DevTable{};
+    d.coef = nullptr;
+    d.coef64 = buf;
+    d.n = h.n;
+    d.dr64 = h.dr;
+    d.off64 = h.off;
+    d.rmult = h.rmult ? 1 : 0;
+    d.allow_hi = h.allow_hi ? 1 : 0;
+    d.allow_lo = h.allow_lo ? 1 : 0;
+    d.out_hi = h.out_hi;
+    d.out_lo = h.out_lo;
+    return OMDG_OK;
+}
+
+}  // namespace omdg
+
+using namespace omdg;
+
+extern "C" {
+
+int omdg_set_thermo_detector(omdg_ctx* c, int on, double ercut) {
+    if (!c) return OMDG_EINVAL;
+    if (c->nrep > 0) return set_error(c, OMDG_EINVAL, "the detector runs on single boxes");
+    if (!on) {
+        if (c->ttm && c->ttm->ttm) return set_error(c, OMDG_ESTATE, "the two-temperature model needs the detector");
+        ttm_release(c);
+        invalidate_graph(c);
+        return OMDG_OK;
+    }
+    if (!c->ttm) c->ttm = new TTMCtx();
+    c->ttm->ercut = ercut;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_set_ttm(omdg_ctx* c, const char* table_file, double atom_volume, double electron_temperature,
+                 double pulse_offset) {
+    if (!c || !table_file || !(atom_volume > 0)) return c ? set_error(c, OMDG_EINVAL, "atom_volume must be > 0")
+                                                          : OMDG_EINVAL;
+    if (c->thermo_tau > 0.0)
+        return set_error(c, OMDG_EINVAL, "the two-temperature model and the Berendsen thermostat exclude each other");
+    cudaSetDevice(c->device);
+    int rc = omdg_set_thermo_detector(c, 1, c->ttm ? c->ttm->ercut : -1.0);
+    if (rc) return rc;
+    TTMCtx& t = *c->ttm;
+    std::string err;
+    if ((rc = table_load(table_file, "ELECTRON_PHONON_COUPLING", t.g, err)) ||
+        (rc = table_load(table_file, "ELECTRON_HEAT_CAPACITY", t.ce, err)))
+        return set_error(c, rc, err);
+    if (!t.g.has_constant || !t.ce.has_constant) return set_error(c, OMDG_EFILE, "TTM tables need a Constant");
+    table_coef(t.g);
+    table_coef(t.ce);
+    cudaFree(t.coef64[0]);
+    cudaFree(t.coef64[1]);
+    t.coef64[0] = t.coef64[1] = nullptr;
+    if ((rc = upload64(c, t.g, t.dg, t.coef64[0])) || (rc = upload64(c, t.ce, t.dce, t.coef64[1]))) return rc;
+    t.g0 = t.g.constant;
+    t.c0 = t.ce.constant;
+    t.vol = atom_volume;
+    t.te0 = electron_temperature;
+    t.offset = pulse_offset;
+    t.ttm = true;
+    if (t.st) {  // restart the model
+        TTMState h{};
+        h.te = t.te0;
+        h.firstfd = 1;
+        cudaMemcpy(t.st, &h, sizeof(h), cudaMemcpyHostToDevice);
+    }
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_ttm_state(omdg_ctx* c, double* electron_temperature, double* int_een, double* int_aen,
+                   double* lattice_temperature) {
+    if (!c) return OMDG_EINVAL;
+    if (!c->ttm || !c->ttm->st) return set_error(c, OMDG_ESTATE, "no detector state yet");
+    cudaSetDevice(c->device);
+    TTMState h;
+    cudaError_t e = cudaMemcpyAsync(&h, c->ttm->st, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "ttm state");
+    if (electron_temperature) *electron_temperature = h.te;
+    if (int_een) *int_een = h.int_een;
+    if (int_aen) *int_aen = h.int_aen;
+    if (lattice_temperature) *lattice_temperature = h.t_avg;
+    return OMDG_OK;
+}
+
+int omdg_local_thermo(omdg_ctx* c, double* temperature, double* density, double* vcm) {
+    if (!c) return OMDG_EINVAL;
+    if (!c->ttm || !c->ttm->temp) return set_error(c, OMDG_ESTATE, "no detector state yet");
+    cudaSetDevice(c->device);
+    const int n = c->n;
+    std::vector<double> t(n), d(n), v(3 * (size_t)n);
+    std::vector<int> id(n);
+    cudaMemcpyAsync(t.data(), c->ttm->temp, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(d.data(), c->ttm->dens, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(v.data(), c->ttm->vcm, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(id.data(), c->id, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "local thermo");
+    for (int i = 0; i < n; i++) {
+        const int k = id[i];  // caller index of sorted atom i
+        if (temperature) temperature[k] = t[i];
+        if (density) density[k] = d[i];
+        if (vcm)
+            for (int q = 0; q < 3; q++) vcm[3 * (size_t)k + q] = v[(size_t)q * n + i];
+    }
+    return OMDG_OK;
+}
+
+}  // extern "C"

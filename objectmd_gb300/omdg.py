@@ -72,6 +72,10 @@ SIGNATURES = {
     "omdg_count_neighbors_static": [_vp, _i, _P(_d), _P(_d), _P(_i), _d, _vp, _vp, _cp, _i],
     "omdg_set_replicas": [_vp, _i, _P(_i), _P(_d), _P(_d), _P(_i)],
     "omdg_replica_ledger": [_vp, _i, _P(_d), _P(_d)],
+    "omdg_set_thermo_detector": [_vp, _i, _d],
+    "omdg_local_thermo": [_vp, _P(_d), _P(_d), _P(_d)],
+    "omdg_set_ttm": [_vp, _cp, _d, _d, _d],
+    "omdg_ttm_state": [_vp, _P(_d), _P(_d), _P(_d), _P(_d)],
     "omdg_add_nn": [_vp, _i, _i, _cp, _cp],
     "omdg_nn_fallback_atoms": [_vp, _P(_l)],
     "omdg_nn_create": [_P(_vp), _i],
@@ -351,6 +355,25 @@ class Context:
         p = np.zeros(self.nrep)
         self._check(self.lib.omdg_replica_ledger(self.h, self.nrep, _dp(k), _dp(p)))
         return k, p
+
+    def set_thermo_detector(self, on=True, ercut=-1.0):
+        self._check(self.lib.omdg_set_thermo_detector(self.h, 1 if on else 0, float(ercut)))
+
+    def local_thermo(self):
+        t, d, v = np.zeros(self.n), np.zeros(self.n), np.zeros((self.n, 3))
+        self._check(self.lib.omdg_local_thermo(self.h, _dp(t), _dp(d), _dp(v)))
+        return {"temperature": t, "density": d, "vcm": v}
+
+    def set_ttm(self, table_file, atom_volume, electron_temperature=-1.0, pulse_offset=0.0):
+        self._check(self.lib.omdg_set_ttm(self.h, table_file.encode(), float(atom_volume),
+                                          float(electron_temperature), float(pulse_offset)))
+
+    def ttm_state(self):
+        te, een, aen, tl = _d(), _d(), _d(), _d()
+        self._check(self.lib.omdg_ttm_state(self.h, ctypes.byref(te), ctypes.byref(een), ctypes.byref(aen),
+                                            ctypes.byref(tl)))
+        return {"electron_temperature": te.value, "int_een": een.value, "int_aen": aen.value,
+                "lattice_temperature": tl.value}
 
     def add_nn(self, model_file, tersoff_fallback=None, ta=0, tb=0):
         fb = tersoff_fallback.encode() if tersoff_fallback else None

@@ -249,6 +249,9 @@ def run_gpu(args):
     desc = w["desc"] if not args.ncell else "%s (ncell %d)" % (w["desc"], args.ncell)
     n = len(x)
     ctx = make_context(w, x, v, lo, hi, device=device, tune=not args.no_tune)
+    for kv in args.launch:
+        k, val = kv.split("=")
+        ctx.set_launch(k, int(val))
     if args.eager:
         ctx.set_profiling(True)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
@@ -570,6 +573,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--launch", action="append", default=[], metavar="KEY=VALUE",
+                    help="set a launch shape after tuning (omdg_set_launch), e.g. build_lanes=1")
     ap.add_argument("--eager", action="store_true",
                     help="launch the step kernels one by one instead of replaying the captured graph "
                          "(profilers cannot see kernels inside a graph with conditional nodes)")

@@ -112,7 +112,7 @@ static bool dalloc(T*& p, size_t count) {
 
 static void free_atoms(Context* c) {
     void* ptrs[] = {c->x,    c->y,     c->z,      c->vx,     c->vy,          c->vz,          c->fx,
-                    c->fy,   c->fz,    c->pe,     c->vir,    c->pack,        c->xref,        c->type,
+                    c->fy,   c->fz,    c->pe,     c->vir,    c->pack,        c->xref,        c->loc,         c->type,
                     c->id,   c->inv,   c->fp,     c->femb,   c->cell,        c->perm,        c->stage_d,
                     c->stage_i, c->cell_sorted, c->f64, c->extra, c->stage_extra, c->nnb, c->d_red};
     for (void* p : ptrs) cudaFree(p);
@@ -120,6 +120,7 @@ static void free_atoms(Context* c) {
     c->fx = c->fy = c->fz = c->pe = c->vir = nullptr;
     c->pack = nullptr;
     c->xref = nullptr;
+    c->loc = nullptr;
     c->type = c->id = c->inv = nullptr;
     c->fp = c->femb = nullptr;
     c->cell = c->perm = nullptr;
@@ -139,7 +140,7 @@ static int alloc_atoms(Context* c, int n) {
     bool ok = dalloc(c->x, cap) && dalloc(c->y, cap) && dalloc(c->z, cap) && dalloc(c->vx, cap) &&
               dalloc(c->vy, cap) && dalloc(c->vz, cap) && dalloc(c->fx, cap) && dalloc(c->fy, cap) &&
               dalloc(c->fz, cap) && dalloc(c->pe, cap) && dalloc(c->vir, cap) && dalloc(c->pack, cap) &&
-              dalloc(c->xref, cap) && dalloc(c->type, cap) && dalloc(c->id, cap) && dalloc(c->inv, cap) &&
+              dalloc(c->xref, cap) && dalloc(c->loc, cap) && dalloc(c->type, cap) && dalloc(c->id, cap) && dalloc(c->inv, cap) &&
               dalloc(c->fp, cap) && dalloc(c->femb, cap) && dalloc(c->cell, cap) && dalloc(c->perm, cap) &&
               dalloc(c->stage_d, (size_t)6 * cap) && dalloc(c->stage_i, (size_t)2 * cap) &&
               dalloc(c->cell_sorted, cap) && dalloc(c->nnb, cap);

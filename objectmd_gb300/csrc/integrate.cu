@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
 }
 
 constexpr int RED_BLOCK = 256;
-constexpr int KICK_ATOMS = 4;
+constexpr int KICK_ATOMS = 1;
 
 __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, double* __restrict__ vx, double* __restrict__ vy,
                                                     double* __restrict__ vz, const float* __restrict__ fx,

@@ -284,22 +284,52 @@ __device__ __forceinline__ void split(double X, float& hi, float& lo) {
     lo = __double2float_rn(__dsub_rn(X, (double)hi));
 }
 
+// The list screen works in a cell-local frame: each cell has an FP32
+// reference point R(c) = fma(c, h, base) per axis (base = the pack-frame
+// corner of cell 0), and an atom's local coordinate u = (X_hi - R) + X_lo is
+// exact up to its final FP32 rounding (X_hi - R is Sterbenz-exact).  The
+// build recomputes R(c) with the same expression.
+struct LocFrame {
+    int nc[3];
+    float base[3], h[3];
+};
+
+__device__ __forceinline__ float cell_ref(int c, float h, float base) { return fmaf((float)c, h, base); }
+
 __global__ void k_pack(int n, const double* __restrict__ x, const double* __restrict__ y,
                        const double* __restrict__ z, const int* __restrict__ type, PackFrame f,
-                       PosPack* __restrict__ pack, float4* __restrict__ xref) {
+                       PosPack* __restrict__ pack, float4* __restrict__ xref, const int* __restrict__ cell,
+                       LocFrame lf, float4* __restrict__ loc, unsigned* umax) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    PosPack p;
-    double X = __dadd_rn(__dsub_rn(x[i], f.org[0]), f.P[0]);
-    double Y = __dadd_rn(__dsub_rn(y[i], f.org[1]), f.P[1]);
-    double Z = __dadd_rn(__dsub_rn(z[i], f.org[2]), f.P[2]);
-    split(X, p.hi.x, p.lo.x);
-    split(Y, p.hi.y, p.lo.y);
-    split(Z, p.hi.z, p.lo.z);
-    p.hi.w = __int_as_float(type[i]);
-    p.lo.w = 0.f;
-    pack[i] = p;
-    if (xref) xref[i] = make_float4(p.hi.x, p.hi.y, p.hi.z, 0.f);
+    float m = 0.f;
+    if (i < n) {
+        PosPack p;
+        double X = __dadd_rn(__dsub_rn(x[i], f.org[0]), f.P[0]);
+        double Y = __dadd_rn(__dsub_rn(y[i], f.org[1]), f.P[1]);
+        double Z = __dadd_rn(__dsub_rn(z[i], f.org[2]), f.P[2]);
+        split(X, p.hi.x, p.lo.x);
+        split(Y, p.hi.y, p.lo.y);
+        split(Z, p.hi.z, p.lo.z);
+        p.hi.w = __int_as_float(type[i]);
+        p.lo.w = 0.f;
+        pack[i] = p;
+        if (xref) xref[i] = make_float4(p.hi.x, p.hi.y, p.hi.z, 0.f);
+        if (loc) {
+            const int c = cell[i];
+            const int cx = c % lf.nc[0], cy = (c / lf.nc[0]) % lf.nc[1], cz = c / (lf.nc[0] * lf.nc[1]);
+            const float ux = __fadd_rn(__fsub_rn(p.hi.x, cell_ref(cx, lf.h[0], lf.base[0])), p.lo.x);
+            const float uy = __fadd_rn(__fsub_rn(p.hi.y, cell_ref(cy, lf.h[1], lf.base[1])), p.lo.y);
+            const float uz = __fadd_rn(__fsub_rn(p.hi.z, cell_ref(cz, lf.h[2], lf.base[2])), p.lo.z);
+            loc[i] = make_float4(ux, uy, uz, 0.f);
+            m = fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
+            if (!(m <= 3.0e38f)) m = 3.0e38f;  // non-finite: flagged by the cell assignment
+        }
+    }
+    if (loc) {
+        // the largest |u| sets the width of the screening band
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(umax, __float_as_uint(m));
+    }
 }
 
 struct BuildParams {
@@ -310,6 +340,8 @@ struct BuildParams {
     double L64[3];
     double rsq;           // Rv*Rv in FP64 (VerletList.cpp:161)
     float rsq_lo, rsq_hi; // FP32 screening band around rsq
+    float rv;             // Rv rounded to FP32
+    float base[3], h[3];  // cell reference points (LocFrame)
 };
 
 // Per axis, the (cell, image) pairs a cell's neighbours live in.
@@ -347,61 +379,120 @@ __device__ __forceinline__ int axis_candidates(int c, int nc, int periodic, int*
     return m;
 }
 
-__global__ void __launch_bounds__(128) k_build(BuildParams p, const PosPack* __restrict__ pack,
+// Per axis, how many (cell, image) candidates a cell has and the idx-th one
+// (the same enumeration as axis_candidates, without a local array).
+__device__ __forceinline__ int axis_count(int nc, int periodic) { return (periodic && nc < 3) ? 3 * nc : 3; }
+
+__device__ __forceinline__ bool axis_cell(int c, int nc, int periodic, int idx, int& cell, int& shift) {
+    if (periodic) {
+        if (nc >= 3) {
+            int k = c + idx - 1;
+            shift = 0;
+            if (k < 0) {
+                k += nc;
+                shift = -1;
+            } else if (k >= nc) {
+                k -= nc;
+                shift = 1;
+            }
+            cell = k;
+        } else {
+            cell = idx / 3;
+            shift = idx % 3 - 1;
+        }
+        return true;
+    }
+    const int k = c + idx - 1;
+    cell = k;
+    shift = 0;
+    return k >= 0 && k < nc;
+}
+
+// The reference's FP64 test (dx = x_i - (x_j + s), r2 = (dx*dx + dy*dy) +
+// dz*dz <= Rv^2) for the rare pairs inside the FP32 screening band.
+__device__ __noinline__ bool exact_within(double Lx, double Ly, double Lz, double rsq, const double* __restrict__ x,
+                                          const double* __restrict__ y, const double* __restrict__ z, int i, int k,
+                                          unsigned code) {
+    const int sx = nbr_sx(code), sy = nbr_sy(code), sz = nbr_sz(code);
+    double gx = sx == 0 ? 0.0 : (sx > 0 ? Lx : -Lx);
+    double gy = sy == 0 ? 0.0 : (sy > 0 ? Ly : -Ly);
+    double gz = sz == 0 ? 0.0 : (sz > 0 ? Lz : -Lz);
+    double dx = __dsub_rn(x[i], __dadd_rn(x[k], gx));
+    double dy = __dsub_rn(y[i], __dadd_rn(y[k], gy));
+    double dz = __dsub_rn(z[i], __dadd_rn(z[k], gz));
+    double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    return rr <= rsq && !(k == i && code == nbr_encode(0, 0, 0, 0));
+}
+
+// One thread per centre atom, screening in the cell-local frame: a
+// candidate costs one 16-byte load of its local coordinate, the difference
+// against the centre shifted by the (cell, image) offset R(c_i) - R(c_k) - sL
+// (computed once per cell), and the squared length.  Every FP32 step is
+// bounded by a few ulps of max(|u|, h); pairs within that band of Rv take
+// the reference's FP64 test, so the list is the reference's exactly.  Rows
+// come out in the traversal order of the other build variants.
+__global__ void __launch_bounds__(128) k_build(BuildParams p, const float4* __restrict__ loc,
                                                const double* __restrict__ x, const double* __restrict__ y,
                                                const double* __restrict__ z, const int* __restrict__ cell,
-                                               const int* __restrict__ start, unsigned* __restrict__ nbr,
-                                               int* __restrict__ nnb, unsigned* status, int* need) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+                                               const int* __restrict__ start, const unsigned* __restrict__ umax,
+                                               unsigned* __restrict__ nbr, int* __restrict__ nnb, unsigned* status,
+                                               int* need) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    PosPack pi = pack[i];
-    int ci = cell[i];
-    int cx = ci % p.nc[0], cy = (ci / p.nc[0]) % p.nc[1], cz = ci / (p.nc[0] * p.nc[1]);
-    int ccx[6], csx[6], ccy[6], csy[6], ccz[6], csz[6];
-    int mx = axis_candidates(cx, p.nc[0], p.periodic[0], ccx, csx);
-    int my = axis_candidates(cy, p.nc[1], p.periodic[1], ccy, csy);
-    int mz = axis_candidates(cz, p.nc[2], p.periodic[2], ccz, csz);
+    // band: per component |error| <= 3 ulp(2 max(|u|, h)) (two operand
+    // roundings, the offset, the difference); 2x margin, then sqrt(3) for
+    // the length and 1e-6 relative for the squares
+    const float U = fmaxf(__uint_as_float(*umax), fmaxf(p.h[0], fmaxf(p.h[1], p.h[2])));
+    const float dlt = 1.7320509f * (12.f * U * 2.3841858e-7f) + 1e-6f * p.rv;
+    const float rl = fmaxf(p.rv - dlt, 0.f), rh = p.rv + dlt;
+    const float rsq_lo = rl * rl * (1.f - 1e-6f), rsq_hi = rh * rh * (1.f + 1e-6f);
+    const float4 ui = loc[i];
+    const int ci = cell[i];
+    const int cx = ci % p.nc[0], cy = (ci / p.nc[0]) % p.nc[1], cz = ci / (p.nc[0] * p.nc[1]);
+    const float rx = cell_ref(cx, p.h[0], p.base[0]), ry = cell_ref(cy, p.h[1], p.base[1]),
+                rz = cell_ref(cz, p.h[2], p.base[2]);
+    const int mx = axis_count(p.nc[0], p.periodic[0]);
+    const int my = axis_count(p.nc[1], p.periodic[1]);
+    const int mz = axis_count(p.nc[2], p.periodic[2]);
+    const unsigned self_code = nbr_encode(0, 0, 0, 0);
     int cnt = 0;
-    double xi = 0, yi = 0, zi = 0;
-    bool have64 = false;
-    for (int a = 0; a < mz; a++)
-        for (int b = 0; b < my; b++)
+#pragma unroll 1
+    for (int a = 0; a < mz; a++) {
+        int kz, sz;
+        if (!axis_cell(cz, p.nc[2], p.periodic[2], a, kz, sz)) continue;
+        const float pz = ui.z + (((rz - cell_ref(kz, p.h[2], p.base[2])) - sel_shift(sz, p.L.hz)) -
+                                 sel_shift(sz, p.L.lz));
+#pragma unroll 1
+        for (int b = 0; b < my; b++) {
+            int ky, sy;
+            if (!axis_cell(cy, p.nc[1], p.periodic[1], b, ky, sy)) continue;
+            const float py = ui.y + (((ry - cell_ref(ky, p.h[1], p.base[1])) - sel_shift(sy, p.L.hy)) -
+                                     sel_shift(sy, p.L.ly));
+#pragma unroll 1
             for (int q = 0; q < mx; q++) {
-                int c = (ccz[a] * p.nc[1] + ccy[b]) * p.nc[0] + ccx[q];
-                unsigned code = nbr_encode(0, csx[q], csy[b], csz[a]);
-                bool self_image = (csx[q] == 0 && csy[b] == 0 && csz[a] == 0);
-                int e = start[c + 1];
+                int kx, sx;
+                if (!axis_cell(cx, p.nc[0], p.periodic[0], q, kx, sx)) continue;
+                const float px = ui.x + (((rx - cell_ref(kx, p.h[0], p.base[0])) - sel_shift(sx, p.L.hx)) -
+                                         sel_shift(sx, p.L.lx));
+                const int c = (kz * p.nc[1] + ky) * p.nc[0] + kx;
+                const unsigned code = nbr_encode(0, sx, sy, sz);
+                const int e = start[c + 1];
                 for (int k = start[c]; k < e; k++) {
-                    if (self_image && k == i) continue;
-                    PosPack pk = pack[k];
-                    float3 d = pair_delta(pi.hi, pi.lo, pk.hi, pk.lo, code, p.L);
-                    float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-                    if (r2 > p.rsq_hi) continue;
-                    bool in = r2 < p.rsq_lo;
-                    if (!in) {
-                        // Borderline: decide with the reference's FP64 arithmetic,
-                        // dx = x_i - (x_j + s), r2 = (dx*dx + dy*dy) + dz*dz.
-                        if (!have64) {
-                            xi = x[i];
-                            yi = y[i];
-                            zi = z[i];
-                            have64 = true;
-                        }
-                        double sx = csx[q] == 0 ? 0.0 : (csx[q] > 0 ? p.L64[0] : -p.L64[0]);
-                        double sy = csy[b] == 0 ? 0.0 : (csy[b] > 0 ? p.L64[1] : -p.L64[1]);
-                        double sz = csz[a] == 0 ? 0.0 : (csz[a] > 0 ? p.L64[2] : -p.L64[2]);
-                        double dx = __dsub_rn(xi, __dadd_rn(x[k], sx));
-                        double dy = __dsub_rn(yi, __dadd_rn(y[k], sy));
-                        double dz = __dsub_rn(zi, __dadd_rn(z[k], sz));
-                        double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-                        in = rr <= p.rsq;
-                    }
-                    if (!in) continue;
+                    const float4 uk = loc[k];
+                    const float dx = px - uk.x, dy = py - uk.y, dz = pz - uk.z;
+                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    if (r2 > rsq_hi) continue;
+                    if (k == i && code == self_code) continue;
+                    // borderline pairs: the reference's FP64 arithmetic, out of line
+                    if (!(r2 < rsq_lo) && !exact_within(p.L64[0], p.L64[1], p.L64[2], p.rsq, x, y, z, i, k, code))
+                        continue;
                     if (r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
                     if (cnt < p.maxnb) nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
                     cnt++;
                 }
             }
+        }
+    }
     if (cnt > p.maxnb) {
         atomicOr(status, ERR_NBR_OVERFLOW);
         atomicMax(need, cnt);
@@ -507,35 +598,6 @@ __global__ void __launch_bounds__(128) k_build_rep(BuildParams p, const RepGeom*
     nnb[i] = cnt;
 }
 
-// Per axis, how many (cell, image) candidates a cell has and the idx-th one
-// (the same enumeration as axis_candidates, without a local array).
-__device__ __forceinline__ int axis_count(int nc, int periodic) { return (periodic && nc < 3) ? 3 * nc : 3; }
-
-__device__ __forceinline__ bool axis_cell(int c, int nc, int periodic, int idx, int& cell, int& shift) {
-    if (periodic) {
-        if (nc >= 3) {
-            int k = c + idx - 1;
-            shift = 0;
-            if (k < 0) {
-                k += nc;
-                shift = -1;
-            } else if (k >= nc) {
-                k -= nc;
-                shift = 1;
-            }
-            cell = k;
-        } else {
-            cell = idx / 3;
-            shift = idx % 3 - 1;
-        }
-        return true;
-    }
-    const int k = c + idx - 1;
-    cell = k;
-    shift = 0;
-    return k >= 0 && k < nc;
-}
-
 // Same list as k_build with LANES threads per atom: the lanes test
 // consecutive atoms of a cell together and append the accepted ones in lane
 // order (ballot + prefix popcount), so each row keeps exactly the
@@ -619,22 +681,6 @@ __global__ void __launch_bounds__(256) k_build_lanes(BuildParams p, const PosPac
 // appending in lane order.  Rows come out identical to k_build's.
 constexpr int BUILD_CELL_THREADS = 128;
 constexpr int BUILD_GROUP = 8;
-
-// The reference's FP64 test (dx = x_i - (x_j + s), r2 = (dx*dx + dy*dy) +
-// dz*dz <= Rv^2) for the rare pairs inside the FP32 screening band.
-__device__ __noinline__ bool exact_within(double Lx, double Ly, double Lz, double rsq, const double* __restrict__ x,
-                                          const double* __restrict__ y, const double* __restrict__ z, int i, int k,
-                                          unsigned code) {
-    const int sx = nbr_sx(code), sy = nbr_sy(code), sz = nbr_sz(code);
-    double gx = sx == 0 ? 0.0 : (sx > 0 ? Lx : -Lx);
-    double gy = sy == 0 ? 0.0 : (sy > 0 ? Ly : -Ly);
-    double gz = sz == 0 ? 0.0 : (sz > 0 ? Lz : -Lz);
-    double dx = __dsub_rn(x[i], __dadd_rn(x[k], gx));
-    double dy = __dsub_rn(y[i], __dadd_rn(y[k], gy));
-    double dz = __dsub_rn(z[i], __dadd_rn(z[k], gz));
-    double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    return rr <= rsq && !(k == i && code == nbr_encode(0, 0, 0, 0));
-}
 
 __global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildParams p, const PosPack* __restrict__ pack,
                                                                     const double* __restrict__ x,
@@ -928,7 +974,7 @@ PackFrame pack_frame(const Context* c) {
 int integrate_pack(Context* c) {
     if (c->n == 0) return OMDG_OK;
     k_pack<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack,
-                                                       c->xref);
+                                                       c->xref, nullptr, LocFrame{}, nullptr, nullptr);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "pack");
 }
@@ -971,8 +1017,17 @@ int nlist_build(Context* c) {
     c->launches += 2;
     prof_end(c);
     prof_begin(c, "pack");
-    k_pack<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack, c->xref);
-    c->launches++;
+    LocFrame lf;
+    for (int d = 0; d < 3; d++) {
+        lf.nc[d] = g.nc[d];
+        lf.h[d] = (float)g.h[d];
+        lf.base[d] = (float)(g.org[d] - c->box.org[d] + c->box.P[d]);
+    }
+    unsigned* umax = reinterpret_cast<unsigned*>(c->d_flags + 3);
+    k_zero_ints<<<1, 32, 0, s>>>(1, c->d_flags + 3, c->d_flags + 3);
+    k_pack<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack, c->xref,
+                                            cell_sorted, lf, reps ? nullptr : c->loc, umax);
+    c->launches += 2;
     prof_end(c);
 
     BuildParams bp;
@@ -989,6 +1044,11 @@ int nlist_build(Context* c) {
     bp.rsq = rv * rv;
     bp.rsq_lo = (float)(bp.rsq * (1.0 - 2e-5));
     bp.rsq_hi = (float)(bp.rsq * (1.0 + 2e-5));
+    bp.rv = (float)rv;
+    for (int d = 0; d < 3; d++) {
+        bp.base[d] = lf.base[d];
+        bp.h[d] = lf.h[d];
+    }
     prof_begin(c, "nlist_build");
     int combos = 1;
     for (int d = 0; d < 3; d++) combos *= (g.periodic[d] && g.nc[d] < 3) ? 3 * g.nc[d] : 3;
@@ -1011,7 +1071,7 @@ int nlist_build(Context* c) {
                                                                c->cell_start, reinterpret_cast<unsigned*>(c->nbr),
                                                                c->nnb, c->d_status, c->d_flags + 1);
     } else {
-        k_build<<<grid_for(n, 128), 128, 0, s>>>(bp, c->pack, c->x, c->y, c->z, cell_sorted, c->cell_start,
+        k_build<<<grid_for(n, 128), 128, 0, s>>>(bp, c->loc, c->x, c->y, c->z, cell_sorted, c->cell_start, umax,
                                                  reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
                                                  c->d_flags + 1);
     }

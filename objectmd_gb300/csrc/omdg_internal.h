@@ -154,6 +154,7 @@ struct Context {
     float *pe = nullptr, *vir = nullptr;
     PosPack* pack = nullptr;
     float4* xref = nullptr;   // pack-frame position at the last build (FP32)
+    float4* loc = nullptr;    // position relative to its cell's corner at the last build (FP32)
     int* type = nullptr;
     int* id = nullptr;        // caller index of sorted atom
     int* inv = nullptr;       // sorted index of caller atom
@@ -241,7 +242,8 @@ struct Context {
 
     // device status and reductions
     unsigned* d_status = nullptr;   // error bits
-    int* d_flags = nullptr;         // [0] rebuild request
+    int* d_flags = nullptr;         // [0] rebuild request, [1] row length needed, [2] ghost count,
+                                    // [3] largest cell-local coordinate of the last build (float bits)
     double* d_red = nullptr;        // block partials
     int red_cap = 0;
     double* d_ledger = nullptr;     // per step: kinetic, potential, virial, lambda

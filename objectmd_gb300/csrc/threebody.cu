@@ -12,6 +12,8 @@
 // FP32 arithmetic on relative vectors from the FP64 positions, Kahan sums in
 // pass B.  Per-atom energies follow the reference: each pair half to each
 // atom, V3/3 to each triplet member (sw.cpp:182-233); Tersoff: 1/2 V_ij to i.
+#include <cmath>
+
 #include "device_common.cuh"
 
 namespace omdg {
@@ -28,7 +30,20 @@ struct SWDev {
     float sx0, sx1, sa0, sa1, sa2, sa3;
     float zc, ze0, ze1, ze2, ze3;
     int first;
+    int ip, iq;  // p and q as integers when they are (then r^-p by multiplication), else -1
 };
+
+// r^-k for a small non-negative integer k
+__device__ __forceinline__ float inv_ipow(float r, int k) {
+    const float ir = 1.0f / r;
+    float res = 1.0f, b = ir;
+    while (k > 0) {
+        if (k & 1) res *= b;
+        b *= b;
+        k >>= 1;
+    }
+    return res;
+}
 
 __device__ __forceinline__ void sw_two_body(const SWDev& p, float r, float& fr, float& half_e) {
     if (p.usezbl && r < p.sx0) {
@@ -48,7 +63,8 @@ __device__ __forceinline__ void sw_two_body(const SWDev& p, float r, float& fr, 
     } else {
         // sw.cpp:166-189
         const float ira = 1.0f / (r - p.rc);
-        const float rp = powf(r, -p.p), rq = powf(r, -p.q);
+        const float rp = p.ip >= 0 ? inv_ipow(r, p.ip) : powf(r, -p.p);
+        const float rq = p.iq >= 0 ? inv_ipow(r, p.iq) : powf(r, -p.q);
         const float fex = expf(p.sigma * ira);
         fr = (p.c1 * rp - p.c2 * rq + (p.c3 * rp - p.c4 * rq) * ira * ira * r) * fex / (r * r);
         half_e = 0.5f * (p.c5 * rp - p.c6 * rq) * fex;
@@ -104,25 +120,36 @@ __global__ void __launch_bounds__(128) k_sw_a(SWDev p, const PosPack* __restrict
         nc++;
     }
     if (nc > TB_MAXN) nc = TB_MAXN;
-    // triplets centred on i (sw.cpp:191-236), each unordered pair (j, k) once
+    // triplets centred on i (sw.cpp:191-236), each unordered pair (j, k) once;
+    // every neighbour's share is summed here and stored in its slot once.  The
+    // per-neighbour factors exp(c7 / (r - rc)), 1 / r and c7 / ((r - rc)^2 r)
+    // are computed once per neighbour instead of once per triplet.
+    float sjx[TB_MAXN], sjy[TB_MAXN], sjz[TB_MAXN], sje[TB_MAXN];
+    float ex[TB_MAXN], ir[TB_MAXN], gr[TB_MAXN];
     for (int a = 0; a < nc; a++) {
-        const float r1 = rr[a], dx1 = vx[a], dy1 = vy[a], dz1 = vz[a];
-        const float ira0 = 1.0f / (r1 - p.rc), fira0 = p.c7 * ira0;
-        const float ex0 = expf(fira0);
+        sjx[a] = sjy[a] = sjz[a] = sje[a] = 0.f;
+        const float ira = 1.0f / (rr[a] - p.rc), fira = p.c7 * ira;
+        ex[a] = expf(fira);
+        ir[a] = 1.0f / rr[a];
+        gr[a] = fira * ira * ir[a];
+    }
+    for (int a = 0; a < nc; a++) {
+        const float dx1 = vx[a], dy1 = vy[a], dz1 = vz[a];
+        const float ex0 = ex[a], ir1 = ir[a], g0 = gr[a];
         float gjx = 0.f, gjy = 0.f, gjz = 0.f, gje = 0.f;
         for (int b = a + 1; b < nc; b++) {
-            const float r2_ = rr[b], dx2 = vx[b], dy2 = vy[b], dz2 = vz[b];
-            const float ira1 = 1.0f / (r2_ - p.rc), fira1 = p.c7 * ira1;
-            const float ir1r2 = 1.0f / (r1 * r2_);
-            const float fex = ex0 * expf(fira1);
+            const float dx2 = vx[b], dy2 = vy[b], dz2 = vz[b];
+            const float ir2 = ir[b];
+            const float ir1r2 = ir1 * ir2;
+            const float fex = ex0 * ex[b];
             const float cs = (dx1 * dx2 + dy1 * dy2 + dz1 * dz2) * ir1r2;
             const float dcos = cs - p.c10;
             const float ftheta = p.c9 * fex * dcos;
             const float ft12 = ir1r2 * ftheta;
             const float fpot = p.c8 * fex * dcos * dcos;
             const float fcos = cs * ftheta;
-            const float fr0 = fpot * fira0 * ira0 / r1, fr1 = fpot * fira1 * ira1 / r2_;
-            const float ft0 = fcos / (r1 * r1), ft1 = fcos / (r2_ * r2_);
+            const float fr0 = fpot * g0, fr1 = fpot * gr[b];
+            const float ft0 = fcos * ir1 * ir1, ft1 = fcos * ir2 * ir2;
             const float fx0 = dx1 * (fr0 + ft0) - dx2 * ft12, fx1 = dx2 * (fr1 + ft1) - dx1 * ft12;
             const float fy0 = dy1 * (fr0 + ft0) - dy2 * ft12, fy1 = dy2 * (fr1 + ft1) - dy1 * ft12;
             const float fz0 = dz1 * (fr0 + ft0) - dz2 * ft12, fz1 = dz2 * (fr1 + ft1) - dz1 * ft12;
@@ -135,23 +162,18 @@ __global__ void __launch_bounds__(128) k_sw_a(SWDev p, const PosPack* __restrict
             gjy += fy0;
             gjz += fz0;
             gje += third;
-            // the k member's share goes straight to its slot (it is a later slot)
-            const size_t atk = nbr_at(i, sl[b], p.hshift, p.maxnb);
-            float4 cur = slot[atk];
-            cur.x += fx1;
-            cur.y += fy1;
-            cur.z += fz1;
-            cur.w += third;
-            slot[atk] = cur;
+            sjx[b] += fx1;
+            sjy[b] += fy1;
+            sjz[b] += fz1;
+            sje[b] += third;
         }
-        const size_t atj = nbr_at(i, sl[a], p.hshift, p.maxnb);
-        float4 cur = slot[atj];
-        cur.x += gjx;
-        cur.y += gjy;
-        cur.z += gjz;
-        cur.w += gje;
-        slot[atj] = cur;
+        sjx[a] += gjx;
+        sjy[a] += gjy;
+        sjz[a] += gjz;
+        sje[a] += gje;
     }
+    for (int a = 0; a < nc; a++)
+        slot[nbr_at(i, sl[a], p.hshift, p.maxnb)] = make_float4(sjx[a], sjy[a], sjz[a], sje[a]);
     if (p.first) {
         fx[i] = ax;
         fy[i] = ay;
@@ -286,6 +308,9 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
     }
     if (nc > TB_MAXN) nc = TB_MAXN;
     float fix = 0.f, fiy = 0.f, fiz = 0.f, ei = 0.f, wi = 0.f;
+    // forces on the neighbours, summed here and stored in their slots once
+    float skx[TB_MAXN], sky[TB_MAXN], skz[TB_MAXN];
+    for (int a = 0; a < nc; a++) skx[a] = sky[a] = skz[a] = 0.f;
     for (int a = 0; a < nc; a++) {
         const float rij = rr[a];
         const float ex_ = ux[a], ey_ = uy[a], ez_ = uz[a];
@@ -348,22 +373,18 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
             fiy += ky;
             fiz += kz;
             // force on k = -gradient
-            const size_t atk = nbr_at(i, sl[b], p.hshift, p.maxnb);
-            float4 cur = slot[atk];
-            cur.x -= kx;
-            cur.y -= ky;
-            cur.z -= kz;
-            slot[atk] = cur;
+            skx[b] -= kx;
+            sky[b] -= ky;
+            skz[b] -= kz;
         }
-        const size_t atj = nbr_at(i, sl[a], p.hshift, p.maxnb);
-        float4 cur = slot[atj];
-        cur.x -= sjx;
-        cur.y -= sjy;
-        cur.z -= sjz;
-        slot[atj] = cur;
+        skx[a] -= sjx;
+        sky[a] -= sjy;
+        skz[a] -= sjz;
         ei += 0.5f * vij;
         wi += 0.5f * dv_dr * rij;
     }
+    for (int a = 0; a < nc; a++)
+        slot[nbr_at(i, sl[a], p.hshift, p.maxnb)] = make_float4(skx[a], sky[a], skz[a], 0.f);
     if (p.first) {
         fx[i] = fix;
         fy[i] = fiy;
@@ -478,6 +499,8 @@ int sw_launch(Context* c, Potential& pot, bool first) {
     p.B = (float)s.B;
     p.p = (float)s.p;
     p.q = (float)s.q;
+    p.ip = (s.p >= 0 && s.p <= 16 && s.p == std::floor(s.p)) ? (int)s.p : -1;
+    p.iq = (s.q >= 0 && s.q <= 16 && s.q == std::floor(s.q)) ? (int)s.q : -1;
     p.sigma = (float)s.sigma;
     p.eps = (float)s.eps;
     p.c1 = (float)s.c1;

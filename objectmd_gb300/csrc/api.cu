@@ -215,14 +215,14 @@ int omdg_create(omdg_ctx** out, int device) {
     if (sms > 0) c->num_sms = sms;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned) * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_flags, sizeof(int) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_flags, sizeof(int) * 8);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_state, step_state_bytes());
     if (e == cudaSuccess) e = cudaMalloc(&c->d_mass, sizeof(double) * MAX_TYPES);
     c->ledger_cap = 1 << 16;
     if (e == cudaSuccess) e = cudaMalloc(&c->d_ledger, sizeof(double) * 4 * c->ledger_cap);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_ledger, sizeof(double) * 4 * c->ledger_cap);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(unsigned) * 4, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_flags, 0, sizeof(int) * 4, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_flags, 0, sizeof(int) * 8, c->stream);
     if (e != cudaSuccess) {
         delete c;
         return OMDG_ECUDA;

@@ -185,4 +185,116 @@ __device__ __forceinline__ bool tab_read64(const DevTable& t, double r, double& 
     return true;
 }
 
+// ------------------------------------------------------------------
+// FP64 work on GB300 runs on a pipe about 1/64 of the FP32 one, so the
+// integration and reduction kernels keep FP64 instructions for the state
+// updates only.  Conversions go through the bit patterns and sums through
+// FP32 pairs (hi + lo, about 44 significant bits).
+
+// Rare cases convert through the FP64 pipe out of line: a call is never
+// if-converted, so its FP64 instructions do not issue for the common case.
+static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
+
+// float -> double exactly, by the bit pattern (zero, infinities and NaN
+// included); subnormal floats convert out of line.
+__device__ __forceinline__ double f2d_exact(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned m = u & 0x7FFFFFu;
+    if (e == 0u && m != 0u) return f2d_slow(f);
+    const unsigned long long de = e == 0u ? 0ull : (e == 0xFFu ? 0x7FFull : (unsigned long long)(e + 896u));
+    const unsigned long long d =
+        ((unsigned long long)(u & 0x80000000u) << 32) | (de << 52) | ((unsigned long long)m << 29);
+    return __longlong_as_double((long long)d);
+}
+
+struct F2 {
+    float hi, lo;
+};
+
+static __device__ __noinline__ F2 split_slow(double X) {
+    F2 r;
+    r.hi = __double2float_rn(X);
+    r.lo = __double2float_rn(__dsub_rn(X, (double)r.hi));
+    return r;
+}
+
+// X = hi + lo with hi = X rounded to 24 significant bits (half away from
+// zero on the bit pattern) and lo = the FP32 rounding of X - hi, from the
+// integer bits; zero gives zeros.  Outside 2^-60 <= |X| < 2^100 (tiny,
+// huge, non-finite) the FP64 conversions decide, out of line.
+__device__ __forceinline__ void split_bits(double X, float& hi, float& lo) {
+    const long long b = __double_as_longlong(X);
+    const long long a = b & 0x7FFFFFFFFFFFFFFFll;
+    const int E = (int)(a >> 52) - 1023;
+    if (a == 0) {
+        hi = 0.f;
+        lo = 0.f;
+        return;
+    }
+    if (E < -60 || E >= 100) {
+        const F2 r = split_slow(X);
+        hi = r.hi;
+        lo = r.lo;
+        return;
+    }
+    const long long hb = (a + (1ll << 28)) & ~((1ll << 29) - 1);
+    const int eh = (int)(hb >> 52) - 1023 + 127;
+    const int sgn = (int)((unsigned long long)b >> 32) & (int)0x80000000;
+    hi = __int_as_float(sgn | (eh << 23) | (int)((hb >> 29) & 0x7FFFFF));
+    const int diff = (int)(a - hb);  // units of the last bit of |X|, |diff| <= 2^28
+    const float l = __int2float_rn(diff) * __int_as_float((E - 52 + 127) << 23);
+    lo = b < 0 ? -l : l;
+}
+
+__device__ __forceinline__ F2 f2_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    const F2 s = f2_two_sum(a.hi, b.hi);
+    const float t = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    const float h = __fadd_rn(s.hi, t);
+    return {h, __fsub_rn(t, __fsub_rn(h, s.hi))};
+}
+
+// a * b for a, b given as pairs (the lo * lo term dropped)
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    const float h = __fadd_rn(p, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, p))};
+}
+
+// The pack coordinate X = x + Q as FP32 hi + lo without FP64 arithmetic:
+// x split by bits, Q given as a pair (qh, ql); TwoSum of the hi parts is
+// exact, the remainder is rounded once and the pair renormalised, so
+// |lo| <= ulp(hi)/2 and hi + lo is X to about 2^-47 relative.  Every pack
+// writer uses this one function.
+__device__ __forceinline__ void pack_coord(double x, float qh, float ql, float& hi, float& lo) {
+    float xh, xl;
+    split_bits(x, xh, xl);
+    const F2 s = f2_two_sum(xh, qh);
+    const float t = __fadd_rn(s.lo, __fadd_rn(xl, ql));
+    hi = __fadd_rn(s.hi, t);
+    lo = __fsub_rn(t, __fsub_rn(hi, s.hi));
+}
+
+__device__ __forceinline__ F2 f2_from(double x) {
+    F2 r;
+    split_bits(x, r.hi, r.lo);
+    return r;
+}
+
+__device__ __forceinline__ double f2_to_double(F2 a) { return __dadd_rn(f2d_exact(a.hi), f2d_exact(a.lo)); }
+
+__device__ __forceinline__ F2 f2_shfl_xor(F2 a, int o) {
+    return {__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+}
+
 }  // namespace omdg

@@ -8,8 +8,13 @@
 //               x += dt v, refresh the FP32 position packs, flag a rebuild
 //               when an atom moved more than skin/2 since the last build
 //   kick        v += dt/2 f/m, block partials of sum m v^2, sum potential,
-//               sum virial (FP64, fixed order)
-//   finalize    one block: ledger row, thermostat factor, step counter
+//               sum virial (FP32 pairs within a block, FP64 across blocks,
+//               fixed order); the last block writes the ledger row, the
+//               thermostat factor and the step counter
+//
+// GB300's FP64 pipe is about 1/64 of its FP32 pipe: the FP64 instructions
+// here are the state updates themselves (fma for v and x); conversions use
+// the bit patterns, the pack refresh and the sums use FP32 pairs.
 #include <vector>
 
 #include "device_common.cuh"
@@ -33,21 +38,9 @@ struct IntParams {
     float half_skin2;       // (skin/2)^2
     int use_f64;
     double Q[3];            // P - org: the pack coordinate is X = x + Q
+    float Qh[3], Ql[3];     // Q as an FP32 pair (pack_coord)
+    float mh[MAX_TYPES], ml[MAX_TYPES];  // mass per type as an FP32 pair
 };
-
-// hi = X rounded to 24 significant bits, lo = X - hi, with integer
-// operations on the FP64 bit pattern instead of FP64 arithmetic (the FP64
-// pipe is the scarce one).  Valid for positive normal X; hi and the
-// remainder are exact, lo is the FP32 rounding of the remainder.
-__device__ __forceinline__ void split_pack(double X, float& hi, float& lo) {
-    const long long b = __double_as_longlong(X);
-    const long long hb = (b + (1ll << 28)) & ~((1ll << 29) - 1);
-    const int eh = (int)((hb >> 52) & 0x7FF) - 1023 + 127;
-    hi = __int_as_float((eh << 23) | (int)((hb >> 29) & 0x7FFFFF));
-    const int diff = (int)(b - hb);  // in units of X's last mantissa bit, |diff| <= 2^28
-    const int ex = (int)((b >> 52) & 0x7FF) - 1023 - 52 + 127;
-    lo = __int2float_rn(diff) * __int_as_float(ex << 23);
-}
 
 __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
                                                     double* __restrict__ z, double* __restrict__ vx,
@@ -61,7 +54,7 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
     if (threadIdx.x == 0) moved = 0;
     __syncthreads();
     if (i < p.n) {
-        double lam = st->lambda;
+        const double lam = st->lambda;
         int t = type[i];
         double h = p.hdtm[t];
         double ax, ay, az;
@@ -70,12 +63,18 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
             ay = f64[3 * (size_t)i + 1];
             az = f64[3 * (size_t)i + 2];
         } else {
-            ax = fx[i];
-            ay = fy[i];
-            az = fz[i];
+            ax = f2d_exact(fx[i]);
+            ay = f2d_exact(fy[i]);
+            az = f2d_exact(fz[i]);
         }
-        // pending thermostat factor (exactly 1.0 when none is pending)
-        double ux = vx[i] * lam, uy = vy[i] * lam, uz = vz[i] * lam;
+        double ux = vx[i], uy = vy[i], uz = vz[i];
+        // a pending thermostat factor (the product by 1.0 is the identity;
+        // compared by bits to keep the test off the FP64 pipe)
+        if (__double_as_longlong(lam) != 0x3FF0000000000000ll) {
+            ux *= lam;
+            uy *= lam;
+            uz *= lam;
+        }
         ux = fma(ax, h, ux);
         uy = fma(ay, h, uy);
         uz = fma(az, h, uz);
@@ -89,9 +88,9 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
         y[i] = Y;
         z[i] = Z;
         PosPack pk;
-        split_pack(__dadd_rn(X, p.Q[0]), pk.hi.x, pk.lo.x);
-        split_pack(__dadd_rn(Y, p.Q[1]), pk.hi.y, pk.lo.y);
-        split_pack(__dadd_rn(Z, p.Q[2]), pk.hi.z, pk.lo.z);
+        pack_coord(X, p.Qh[0], p.Ql[0], pk.hi.x, pk.lo.x);
+        pack_coord(Y, p.Qh[1], p.Ql[1], pk.hi.y, pk.lo.y);
+        pack_coord(Z, p.Qh[2], p.Ql[2], pk.hi.z, pk.lo.z);
         pk.hi.w = __int_as_float(t);
         pk.lo.w = 0.f;
         pack[i] = pk;
@@ -104,92 +103,37 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
 }
 
 constexpr int RED_BLOCK = 256;
-constexpr int KICK_ATOMS = 1;
-
-__global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, double* __restrict__ vx, double* __restrict__ vy,
-                                                    double* __restrict__ vz, const float* __restrict__ fx,
-                                                    const float* __restrict__ fy, const float* __restrict__ fz,
-                                                    const double* __restrict__ f64, const int* __restrict__ type,
-                                                    const double* __restrict__ mass, const float* __restrict__ pe,
-                                                    const float* __restrict__ vir, double* __restrict__ partial,
-                                                    int kick) {
-    // each thread takes KICK_ATOMS atoms, blockDim apart (coalesced)
-    double k = 0, e = 0, w = 0;
-    const int base = blockIdx.x * blockDim.x * KICK_ATOMS + threadIdx.x;
-#pragma unroll
-    for (int a = 0; a < KICK_ATOMS; a++) {
-        const int i = base + a * blockDim.x;
-        if (i >= p.n) break;
-        int t = type[i];
-        double ux = vx[i], uy = vy[i], uz = vz[i];
-        if (kick) {
-            double h = p.hdtm[t];
-            if (p.use_f64) {
-                ux = fma((double)f64[3 * (size_t)i], h, ux);
-                uy = fma((double)f64[3 * (size_t)i + 1], h, uy);
-                uz = fma((double)f64[3 * (size_t)i + 2], h, uz);
-            } else {
-                ux = fma((double)fx[i], h, ux);
-                uy = fma((double)fy[i], h, uy);
-                uz = fma((double)fz[i], h, uz);
-            }
-            vx[i] = ux;
-            vy[i] = uy;
-            vz[i] = uz;
-        }
-        k = fma(mass[t], fma(ux, ux, fma(uy, uy, uz * uz)), k);
-        e += p.use_f64 ? f64[3 * (size_t)p.n + i] : (double)pe[i];
-        w += (double)vir[i];
-    }
-    // fixed-order block reduction
-    __shared__ double sk[RED_BLOCK], se[RED_BLOCK], sw[RED_BLOCK];
-    sk[threadIdx.x] = k;
-    se[threadIdx.x] = e;
-    sw[threadIdx.x] = w;
-    __syncthreads();
-    for (int off = RED_BLOCK / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off) {
-            sk[threadIdx.x] += sk[threadIdx.x + off];
-            se[threadIdx.x] += se[threadIdx.x + off];
-            sw[threadIdx.x] += sw[threadIdx.x + off];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        partial[3 * blockIdx.x + 0] = sk[0];
-        partial[3 * blockIdx.x + 1] = se[0];
-        partial[3 * blockIdx.x + 2] = sw[0];
-    }
-}
 
 struct FinParams {
-    int nblocks;
     int natoms;
     int ledger_cap;
     int count_step;       // 1: this is a RunKernel step (advance Step)
     const int* ghosts;    // reference compatibility: periodic images added to the atom count (or null)
     unsigned* status;     // ERR_NONFINITE when a total is NaN or infinite
+    unsigned* ticket;     // blocks done (the last one resets it)
     double dt, tau, tset; // thermostat (tau <= 0: off)
     double temp_factor;   // 2/3/k_B (unit.h:66-104)
 };
 
-__global__ void k_finalize(FinParams p, const double* __restrict__ partial, double* __restrict__ ledger,
-                           StepState* st) {
-    __shared__ double sk[256], se[256], sw[256];
+// Ledger row, thermostat factor and step counter from the block partials
+// (one block; each thread sums a contiguous run of partials, then a fixed
+// tree).  Partials are read through L2: other blocks wrote them.
+__device__ void finalize_block(const FinParams& p, int nblocks, const double* partial, double* ledger,
+                               StepState* st) {
+    __shared__ double sk[RED_BLOCK], se[RED_BLOCK], sw[RED_BLOCK];
     double k = 0, e = 0, w = 0;
-    // each thread sums a contiguous run of blocks, then a fixed tree
-    int per = (p.nblocks + blockDim.x - 1) / blockDim.x;
-    int b0 = threadIdx.x * per, b1 = min(p.nblocks, b0 + per);
+    const int per = (nblocks + RED_BLOCK - 1) / RED_BLOCK;
+    const int b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
     for (int b = b0; b < b1; b++) {
-        k += partial[3 * b];
-        e += partial[3 * b + 1];
-        w += partial[3 * b + 2];
+        k += __ldcg(partial + 3 * b);
+        e += __ldcg(partial + 3 * b + 1);
+        w += __ldcg(partial + 3 * b + 2);
     }
     sk[threadIdx.x] = k;
     se[threadIdx.x] = e;
     sw[threadIdx.x] = w;
     __syncthreads();
-    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    for (int off = RED_BLOCK / 2; off > 0; off >>= 1) {
         if (threadIdx.x < off) {
             sk[threadIdx.x] += sk[threadIdx.x + off];
             se[threadIdx.x] += se[threadIdx.x + off];
@@ -219,7 +163,83 @@ __global__ void k_finalize(FinParams p, const double* __restrict__ partial, doub
             st->row = row + 1;
             if (st->rebuild_every > 0 && (st->step % st->rebuild_every) == 0) st->rebuild = 1;
         }
+        *p.ticket = 0u;
     }
+}
+
+// Second half kick v += dt/2 f/m (kick = 1) and the energy ledger: per
+// atom m v^2, the potential and the virial as FP32 pairs, a fixed xor tree
+// per warp and over the warps, FP64 block partials; the last block to
+// finish sums the partials in block order (finalize_block).
+__global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, FinParams f, double* __restrict__ vx,
+                                                    double* __restrict__ vy, double* __restrict__ vz,
+                                                    const float* __restrict__ fx, const float* __restrict__ fy,
+                                                    const float* __restrict__ fz, const double* __restrict__ f64,
+                                                    const int* __restrict__ type, const float* __restrict__ pe,
+                                                    const float* __restrict__ vir, double* __restrict__ partial,
+                                                    double* __restrict__ ledger, StepState* st, int kick) {
+    const int i = blockIdx.x * RED_BLOCK + threadIdx.x;
+    F2 k = {0.f, 0.f}, e = {0.f, 0.f}, w = {0.f, 0.f};
+    if (i < p.n) {
+        const int t = type[i];
+        double ux = vx[i], uy = vy[i], uz = vz[i];
+        if (kick) {
+            const double h = p.hdtm[t];
+            if (p.use_f64) {
+                ux = fma(f64[3 * (size_t)i], h, ux);
+                uy = fma(f64[3 * (size_t)i + 1], h, uy);
+                uz = fma(f64[3 * (size_t)i + 2], h, uz);
+            } else {
+                ux = fma(f2d_exact(fx[i]), h, ux);
+                uy = fma(f2d_exact(fy[i]), h, uy);
+                uz = fma(f2d_exact(fz[i]), h, uz);
+            }
+            vx[i] = ux;
+            vy[i] = uy;
+            vz[i] = uz;
+        }
+        const F2 sx = f2_from(ux), sy = f2_from(uy), sz = f2_from(uz);
+        const F2 v2 = f2_add(f2_add(f2_mul(sx, sx), f2_mul(sy, sy)), f2_mul(sz, sz));
+        k = f2_mul(v2, F2{p.mh[t], p.ml[t]});
+        e = p.use_f64 ? f2_from(f64[3 * (size_t)p.n + i]) : F2{pe[i], 0.f};
+        w = F2{vir[i], 0.f};
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        k = f2_add(k, f2_shfl_xor(k, o));
+        e = f2_add(e, f2_shfl_xor(e, o));
+        w = f2_add(w, f2_shfl_xor(w, o));
+    }
+    __shared__ F2 wk[RED_BLOCK / 32], we[RED_BLOCK / 32], ww[RED_BLOCK / 32];
+    __shared__ bool last;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        wk[warp] = k;
+        we[warp] = e;
+        ww[warp] = w;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const F2 z = {0.f, 0.f};
+        k = lane < RED_BLOCK / 32 ? wk[lane] : z;
+        e = lane < RED_BLOCK / 32 ? we[lane] : z;
+        w = lane < RED_BLOCK / 32 ? ww[lane] : z;
+        for (int o = RED_BLOCK / 64; o > 0; o >>= 1) {
+            k = f2_add(k, f2_shfl_xor(k, o));
+            e = f2_add(e, f2_shfl_xor(e, o));
+            w = f2_add(w, f2_shfl_xor(w, o));
+        }
+        if (lane == 0) {
+            partial[3 * blockIdx.x + 0] = f2_to_double(k);
+            partial[3 * blockIdx.x + 1] = f2_to_double(e);
+            partial[3 * blockIdx.x + 2] = f2_to_double(w);
+            __threadfence();
+            last = atomicAdd(f.ticket, 1u) == gridDim.x - 1;
+        }
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    finalize_block(f, gridDim.x, partial, ledger, st);
 }
 
 struct GhostParams {
@@ -305,6 +325,10 @@ static IntParams int_params(Context* c) {
     IntParams p;
     p.n = c->n;
     for (int t = 0; t < MAX_TYPES; t++) p.hdtm[t] = c->mass[t] > 0 ? (0.5 * c->dt) / c->mass[t] : 0.0;
+    for (int t = 0; t < MAX_TYPES; t++) {
+        p.mh[t] = (float)c->mass[t];
+        p.ml[t] = (float)(c->mass[t] - (double)p.mh[t]);
+    }
     p.dt = c->dt;
     for (int d = 0; d < 3; d++) {
         p.org[d] = c->box.org[d];
@@ -313,7 +337,11 @@ static IntParams int_params(Context* c) {
     float hs = (float)(0.5 * c->skin);
     p.half_skin2 = hs * hs;
     p.use_f64 = c->use_f64 ? 1 : 0;
-    for (int d = 0; d < 3; d++) p.Q[d] = c->box.P[d] - c->box.org[d];
+    for (int d = 0; d < 3; d++) {
+        p.Q[d] = c->box.P[d] - c->box.org[d];
+        p.Qh[d] = (float)p.Q[d];
+        p.Ql[d] = (float)(p.Q[d] - (double)p.Qh[d]);
+    }
     return p;
 }
 
@@ -330,13 +358,8 @@ int integrate_kick_drift(Context* c, int) {
 
 static int reduce_and_finalize(Context* c, int kick, int count_step) {
     IntParams p = int_params(c);
-    int nb = grid_for(c->n, RED_BLOCK * KICK_ATOMS);
-    prof_begin(c, "kick");
-    k_kick<<<nb, RED_BLOCK, 0, c->stream>>>(p, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz, c->f64, c->type, c->d_mass,
-                                            c->pe, c->vir, c->d_red, kick);
-    prof_end(c);
+    int nb = grid_for(c->n, RED_BLOCK);
     FinParams f;
-    f.nblocks = nb;
     f.natoms = c->n;
     f.ledger_cap = c->ledger_cap;
     f.count_step = count_step;
@@ -346,6 +369,7 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
     f.temp_factor = 2.0 / 3.0 / 8.61734279e-05;
     f.ghosts = nullptr;
     f.status = c->d_status;
+    f.ticket = reinterpret_cast<unsigned*>(c->d_flags + 4);
     if (c->thermo_count_ghosts && count_step && c->thermo_tau > 0.0) {
         // TempController::GetSystemTemperature divides by GetTotalAtom(), which
         // on MDSystemGrid is GetNAtom(): owners plus their periodic ghost images
@@ -366,11 +390,13 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
         c->launches += 2;
         f.ghosts = c->d_flags + 2;
     }
-    prof_begin(c, "finalize");
-    k_finalize<<<1, 256, 0, c->stream>>>(f, c->d_red, c->d_ledger, reinterpret_cast<StepState*>(c->d_state));
+    prof_begin(c, "kick");
+    k_kick<<<nb, RED_BLOCK, 0, c->stream>>>(p, f, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz, c->f64, c->type, c->pe,
+                                            c->vir, c->d_red, c->d_ledger,
+                                            reinterpret_cast<StepState*>(c->d_state), kick);
     prof_end(c);
-    c->launches += 2;
-    return check_cuda(c, cudaGetLastError(), "kick/finalize");
+    c->launches += 1;
+    return check_cuda(c, cudaGetLastError(), "kick");
 }
 
 int integrate_kick(Context* c, int) { return reduce_and_finalize(c, 1, 1); }

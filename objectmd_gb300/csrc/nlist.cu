@@ -24,7 +24,7 @@ namespace omdg {
 
 struct CellGeom {
     int nc[3];
-    double org[3], h[3];
+    double org[3], h[3], inv_h[3];
     int periodic[3];
     double lo[3], L[3];
 };
@@ -35,6 +35,7 @@ static CellGeom cell_geom(const Context* c) {
         g.nc[d] = c->box.nc[d];
         g.org[d] = c->box.cell_org[d];
         g.h[d] = c->box.cell_h[d];
+        g.inv_h[d] = 1.0 / c->box.cell_h[d];
         g.periodic[d] = c->box.periodic[d];
         g.lo[d] = c->box.lo[d];
         g.L[d] = c->box.L[d];
@@ -42,8 +43,35 @@ static CellGeom cell_geom(const Context* c) {
     return g;
 }
 
-__device__ __forceinline__ int cell_coord(double x, double org, double h, int nc) {
-    int k = (int)floor(__ddiv_rn(__dsub_rn(x, org), h));
+// systemgrid.cpp:132-138: an atom is owned iff floor((x - x0) / lx) == 0,
+// else it becomes the image x -/+ lx (comhandler.cpp:427-432).  Out of line:
+// only atoms that crossed a face get here.
+__device__ __noinline__ double wrap_crossed(double p, double lo, double L) {
+    const int u = (int)floor(__ddiv_rn(__dsub_rn(p, lo), L));
+    if (u < 0) return __dadd_rn(p, L);
+    if (u >= 1) return __dadd_rn(p, -L);
+    return p;
+}
+
+// Cell coordinate along one axis, wrapping p on a periodic axis first.  For
+// a = p - x0 and lx positive, floor(a / lx) == 0 is 0 <= a < lx (a < lx gives
+// fl(a / lx) < 1, a >= lx gives fl(a / lx) >= 1), tested on the bit patterns
+// (non-negative doubles order as integers; NaN fails).  The cell is
+// floor(a / h) by the reciprocal (the FP64 pipe divides slowly); cells are
+// at least Rv (1 + 1e-12) wide, so a few ulps of misplacement at a face
+// never separates a pair within Rv by more than one cell.  Periodic axes
+// have their cell origin at x0.
+__device__ __forceinline__ int axis_cell_of(double& p, int periodic, double lo, double L, double cell_org,
+                                            double inv_h, int nc) {
+    double a = __dsub_rn(p, periodic ? lo : cell_org);
+    if (periodic) {
+        const long long ba = __double_as_longlong(a);
+        if (!(ba >= 0 && ba < __double_as_longlong(L))) {
+            p = wrap_crossed(p, lo, L);
+            a = __dsub_rn(p, lo);
+        }
+    }
+    const int k = (int)floor(__dmul_rn(a, inv_h));
     return k < 0 ? 0 : (k >= nc ? nc - 1 : k);
 }
 
@@ -52,20 +80,12 @@ __global__ void k_cell_assign(int n, double* __restrict__ x, double* __restrict_
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double p[3] = {x[i], y[i], z[i]};
-    for (int d = 0; d < 3; d++) {
-        if (!g.periodic[d]) continue;
-        // systemgrid.cpp:132-138: owned iff floor((x - x0) / lx) == 0; the owner
-        // otherwise becomes the image x + shift (comhandler.cpp:427-432).
-        int u = (int)floor(__ddiv_rn(__dsub_rn(p[d], g.lo[d]), g.L[d]));
-        if (u < 0) p[d] = __dadd_rn(p[d], g.L[d]);
-        else if (u >= 1) p[d] = __dadd_rn(p[d], -g.L[d]);
-    }
+    const int cx = axis_cell_of(p[0], g.periodic[0], g.lo[0], g.L[0], g.org[0], g.inv_h[0], g.nc[0]);
+    const int cy = axis_cell_of(p[1], g.periodic[1], g.lo[1], g.L[1], g.org[1], g.inv_h[1], g.nc[1]);
+    const int cz = axis_cell_of(p[2], g.periodic[2], g.lo[2], g.L[2], g.org[2], g.inv_h[2], g.nc[2]);
     x[i] = p[0];
     y[i] = p[1];
     z[i] = p[2];
-    int cx = cell_coord(p[0], g.org[0], g.h[0], g.nc[0]);
-    int cy = cell_coord(p[1], g.org[1], g.h[1], g.nc[1]);
-    int cz = cell_coord(p[2], g.org[2], g.h[2], g.nc[2]);
     int c = (cz * g.nc[1] + cy) * g.nc[0] + cx;
     if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) {
         // spread non-finite atoms over the cells so that the per-cell work stays
@@ -275,14 +295,11 @@ __global__ void k_sorted_cell(int n, const int* __restrict__ perm, const int* __
     if (k < n) cell_new[k] = cell_old[perm[k]];
 }
 
+// The pack coordinate is X = x + Q with Q = P - org, formed as FP32 hi + lo
+// by pack_coord (the integrator refreshes the pack with the same function).
 struct PackFrame {
-    double org[3], P[3];
+    float Qh[3], Ql[3];
 };
-
-__device__ __forceinline__ void split(double X, float& hi, float& lo) {
-    hi = __double2float_rn(X);
-    lo = __double2float_rn(__dsub_rn(X, (double)hi));
-}
 
 // The list screen works in a cell-local frame: each cell has an FP32
 // reference point R(c) = fma(c, h, base) per axis (base = the pack-frame
@@ -304,12 +321,9 @@ __global__ void k_pack(int n, const double* __restrict__ x, const double* __rest
     float m = 0.f;
     if (i < n) {
         PosPack p;
-        double X = __dadd_rn(__dsub_rn(x[i], f.org[0]), f.P[0]);
-        double Y = __dadd_rn(__dsub_rn(y[i], f.org[1]), f.P[1]);
-        double Z = __dadd_rn(__dsub_rn(z[i], f.org[2]), f.P[2]);
-        split(X, p.hi.x, p.lo.x);
-        split(Y, p.hi.y, p.lo.y);
-        split(Z, p.hi.z, p.lo.z);
+        pack_coord(x[i], f.Qh[0], f.Ql[0], p.hi.x, p.lo.x);
+        pack_coord(y[i], f.Qh[1], f.Ql[1], p.hi.y, p.lo.y);
+        pack_coord(z[i], f.Qh[2], f.Ql[2], p.hi.z, p.lo.z);
         p.hi.w = __int_as_float(type[i]);
         p.lo.w = 0.f;
         pack[i] = p;
@@ -505,7 +519,7 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const float4* __re
 // Replica mode: every replica has its own periodic lengths and cell grid,
 // and its cells occupy the global cell range [cell_base, cell_base + cells).
 struct RepGeom {
-    double lo[3], L[3], cell_org[3], cell_h[3];
+    double lo[3], L[3], cell_org[3], cell_h[3], inv_h[3];
     int nc[3], periodic[3];
     int cell_base;
     ShiftF S;
@@ -518,18 +532,12 @@ __global__ void k_cell_assign_rep(int n, double* __restrict__ x, double* __restr
     if (i >= n) return;
     const RepGeom& g = rg[rep_of[i]];
     double p[3] = {x[i], y[i], z[i]};
-    for (int d = 0; d < 3; d++) {
-        if (!g.periodic[d]) continue;
-        const int u = (int)floor(__ddiv_rn(__dsub_rn(p[d], g.lo[d]), g.L[d]));
-        if (u < 0) p[d] = __dadd_rn(p[d], g.L[d]);
-        else if (u >= 1) p[d] = __dadd_rn(p[d], -g.L[d]);
-    }
+    const int cx = axis_cell_of(p[0], g.periodic[0], g.lo[0], g.L[0], g.cell_org[0], g.inv_h[0], g.nc[0]);
+    const int cy = axis_cell_of(p[1], g.periodic[1], g.lo[1], g.L[1], g.cell_org[1], g.inv_h[1], g.nc[1]);
+    const int cz = axis_cell_of(p[2], g.periodic[2], g.lo[2], g.L[2], g.cell_org[2], g.inv_h[2], g.nc[2]);
     x[i] = p[0];
     y[i] = p[1];
     z[i] = p[2];
-    const int cx = cell_coord(p[0], g.cell_org[0], g.cell_h[0], g.nc[0]);
-    const int cy = cell_coord(p[1], g.cell_org[1], g.cell_h[1], g.nc[1]);
-    const int cz = cell_coord(p[2], g.cell_org[2], g.cell_h[2], g.nc[2]);
     int c = g.cell_base + (cz * g.nc[1] + cy) * g.nc[0] + cx;
     if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) {
         atomicOr(status, ERR_NONFINITE);
@@ -827,14 +835,20 @@ __global__ void k_reverse(int n, int hshift, int maxnb, const unsigned* __restri
 
 // ---------------------------------------------------------------- host side
 
+// Cells along an axis of extent ext: as many as fit with each at least
+// Rv (1 + 1e-12) wide (the margin absorbs cell_coord's rounding).
+static int cells_along(double ext, double rv) {
+    const int nc = (int)(ext / (rv * (1.0 + 1e-12)));
+    return nc < 1 ? 1 : nc;
+}
+
 void nlist_prepare_geometry(Context* c) {
     double rv = c->rc_max + c->skin;
     BoxGeom& b = c->box;
     for (int d = 0; d < 3; d++) {
         if (b.periodic[d]) {
             b.cell_org[d] = b.lo[d];
-            int nc = (int)(b.L[d] / rv);
-            b.nc[d] = nc < 1 ? 1 : nc;
+            b.nc[d] = cells_along(b.L[d], rv);
             b.cell_h[d] = b.L[d] / b.nc[d];
         } else {
             // free axis: a fixed grid over the box with a margin; atoms
@@ -843,8 +857,7 @@ void nlist_prepare_geometry(Context* c) {
             double margin = 2.0 * rv;
             b.cell_org[d] = b.lo[d] - margin;
             double ext = b.L[d] + 2.0 * margin;
-            int nc = (int)(ext / rv);
-            b.nc[d] = nc < 1 ? 1 : nc;
+            b.nc[d] = cells_along(ext, rv);
             b.cell_h[d] = ext / b.nc[d];
         }
     }
@@ -865,17 +878,16 @@ int replica_prepare(Context* c) {
             g.periodic[d] = c->rep_periodic[d];
             if (g.periodic[d]) {
                 g.cell_org[d] = g.lo[d];
-                const int nc = (int)(g.L[d] / rv);
-                g.nc[d] = nc < 1 ? 1 : nc;
+                g.nc[d] = cells_along(g.L[d], rv);
                 g.cell_h[d] = g.L[d] / g.nc[d];
             } else {
                 const double margin = 2.0 * rv;
                 g.cell_org[d] = g.lo[d] - margin;
                 const double ext = g.L[d] + 2.0 * margin;
-                const int nc = (int)(ext / rv);
-                g.nc[d] = nc < 1 ? 1 : nc;
+                g.nc[d] = cells_along(ext, rv);
                 g.cell_h[d] = ext / g.nc[d];
             }
+            g.inv_h[d] = 1.0 / g.cell_h[d];
         }
         const float lh[3] = {(float)g.L[0], (float)g.L[1], (float)g.L[2]};
         g.S.hx = lh[0];
@@ -965,8 +977,9 @@ static int ensure_cells(Context* c, int m) {
 PackFrame pack_frame(const Context* c) {
     PackFrame f;
     for (int d = 0; d < 3; d++) {
-        f.org[d] = c->box.org[d];
-        f.P[d] = c->box.P[d];
+        const double Q = c->box.P[d] - c->box.org[d];
+        f.Qh[d] = (float)Q;
+        f.Ql[d] = (float)(Q - (double)f.Qh[d]);
     }
     return f;
 }

@@ -243,7 +243,8 @@ struct Context {
     // device status and reductions
     unsigned* d_status = nullptr;   // error bits
     int* d_flags = nullptr;         // [0] rebuild request, [1] row length needed, [2] ghost count,
-                                    // [3] largest cell-local coordinate of the last build (float bits)
+                                    // [3] largest cell-local coordinate of the last build (float bits),
+                                    // [4] blocks done in the current kick (reset by the last block)
     double* d_red = nullptr;        // block partials
     int red_cap = 0;
     double* d_ledger = nullptr;     // per step: kinetic, potential, virial, lambda

@@ -295,6 +295,18 @@ __global__ void k_sorted_cell(int n, const int* __restrict__ perm, const int* __
     if (k < n) cell_new[k] = cell_old[perm[k]];
 }
 
+// Replica mode: every replica has its own periodic lengths and cell grid,
+// and its cells occupy the global cell range [cell_base, cell_base + cells).
+// base and hf are the replica's cell reference points in the pack frame
+// (LocFrame below).
+struct RepGeom {
+    double lo[3], L[3], cell_org[3], cell_h[3], inv_h[3];
+    int nc[3], periodic[3];
+    int cell_base;
+    ShiftF S;
+    float base[3], hf[3];
+};
+
 // The pack coordinate is X = x + Q with Q = P - org, formed as FP32 hi + lo
 // by pack_coord (the integrator refreshes the pack with the same function).
 struct PackFrame {
@@ -316,7 +328,8 @@ __device__ __forceinline__ float cell_ref(int c, float h, float base) { return f
 __global__ void k_pack(int n, const double* __restrict__ x, const double* __restrict__ y,
                        const double* __restrict__ z, const int* __restrict__ type, PackFrame f,
                        PosPack* __restrict__ pack, float4* __restrict__ xref, const int* __restrict__ cell,
-                       LocFrame lf, float4* __restrict__ loc, unsigned* umax) {
+                       LocFrame lf, const int* __restrict__ rep_of, const RepGeom* __restrict__ rg,
+                       float4* __restrict__ loc, unsigned* umax) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     float m = 0.f;
     if (i < n) {
@@ -329,7 +342,16 @@ __global__ void k_pack(int n, const double* __restrict__ x, const double* __rest
         pack[i] = p;
         if (xref) xref[i] = make_float4(p.hi.x, p.hi.y, p.hi.z, 0.f);
         if (loc) {
-            const int c = cell[i];
+            int c = cell[i];
+            if (rep_of) {  // the replica's own grid and reference points
+                const RepGeom& g = rg[rep_of[i]];
+                c -= g.cell_base;
+                for (int d = 0; d < 3; d++) {
+                    lf.nc[d] = g.nc[d];
+                    lf.h[d] = g.hf[d];
+                    lf.base[d] = g.base[d];
+                }
+            }
             const int cx = c % lf.nc[0], cy = (c / lf.nc[0]) % lf.nc[1], cz = c / (lf.nc[0] * lf.nc[1]);
             const float ux = __fadd_rn(__fsub_rn(p.hi.x, cell_ref(cx, lf.h[0], lf.base[0])), p.lo.x);
             const float uy = __fadd_rn(__fsub_rn(p.hi.y, cell_ref(cy, lf.h[1], lf.base[1])), p.lo.y);
@@ -356,45 +378,13 @@ struct BuildParams {
     float rsq_lo, rsq_hi; // FP32 screening band around rsq
     float rv;             // Rv rounded to FP32
     float base[3], h[3];  // cell reference points (LocFrame)
+    float hmax;           // largest cell size over all grids (screening band)
 };
 
-// Per axis, the (cell, image) pairs a cell's neighbours live in.
-__device__ __forceinline__ int axis_candidates(int c, int nc, int periodic, int* cc, int* cs) {
-    int m = 0;
-    if (periodic) {
-        if (nc >= 3) {
-            for (int o = -1; o <= 1; o++) {
-                int k = c + o, s = 0;
-                if (k < 0) {
-                    k += nc;
-                    s = -1;
-                } else if (k >= nc) {
-                    k -= nc;
-                    s = 1;
-                }
-                cc[m] = k;
-                cs[m++] = s;
-            }
-        } else {
-            for (int k = 0; k < nc; k++)
-                for (int s = -1; s <= 1; s++) {
-                    cc[m] = k;
-                    cs[m++] = s;
-                }
-        }
-    } else {
-        for (int o = -1; o <= 1; o++) {
-            int k = c + o;
-            if (k < 0 || k >= nc) continue;
-            cc[m] = k;
-            cs[m++] = 0;
-        }
-    }
-    return m;
-}
-
-// Per axis, how many (cell, image) candidates a cell has and the idx-th one
-// (the same enumeration as axis_candidates, without a local array).
+// Per axis, how many (cell, image) candidates a cell has and the idx-th one,
+// in traversal order: cells c-1, c, c+1 (a periodic axis wraps them with
+// image -1 / +1, a free axis drops the ones off the grid); a periodic axis
+// of fewer than 3 cells takes every cell with images -1, 0, +1.
 __device__ __forceinline__ int axis_count(int nc, int periodic) { return (periodic && nc < 3) ? 3 * nc : 3; }
 
 __device__ __forceinline__ bool axis_cell(int c, int nc, int periodic, int idx, int& cell, int& shift) {
@@ -445,50 +435,75 @@ __device__ __noinline__ bool exact_within(double Lx, double Ly, double Lz, doubl
 // bounded by a few ulps of max(|u|, h); pairs within that band of Rv take
 // the reference's FP64 test, so the list is the reference's exactly.  Rows
 // come out in the traversal order of the other build variants.
-__global__ void __launch_bounds__(128) k_build(BuildParams p, const float4* __restrict__ loc,
-                                               const double* __restrict__ x, const double* __restrict__ y,
-                                               const double* __restrict__ z, const int* __restrict__ cell,
-                                               const int* __restrict__ start, const unsigned* __restrict__ umax,
-                                               unsigned* __restrict__ nbr, int* __restrict__ nnb, unsigned* status,
-                                               int* need) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+//
+// Grid accessors: the single box reads the kernel parameters, a replica its
+// RepGeom entry (both inline to plain loads).
+struct BoxGrid {
+    const BuildParams& p;
+    __device__ int nc(int d) const { return p.nc[d]; }
+    __device__ int periodic(int d) const { return p.periodic[d]; }
+    __device__ float base(int d) const { return p.base[d]; }
+    __device__ float h(int d) const { return p.h[d]; }
+    __device__ double L64(int d) const { return p.L64[d]; }
+    __device__ const ShiftF& L() const { return p.L; }
+    __device__ int cell_base() const { return 0; }
+};
+
+struct RepGrid {
+    const RepGeom* r;
+    __device__ int nc(int d) const { return r->nc[d]; }
+    __device__ int periodic(int d) const { return r->periodic[d]; }
+    __device__ float base(int d) const { return r->base[d]; }
+    __device__ float h(int d) const { return r->hf[d]; }
+    __device__ double L64(int d) const { return r->L[d]; }
+    __device__ const ShiftF& L() const { return r->S; }
+    __device__ int cell_base() const { return r->cell_base; }
+};
+
+template <class G>
+__device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int i, const float4* __restrict__ loc,
+                                          const double* __restrict__ x, const double* __restrict__ y,
+                                          const double* __restrict__ z, const int* __restrict__ cell,
+                                          const int* __restrict__ start, const unsigned* __restrict__ umax,
+                                          unsigned* __restrict__ nbr, int* __restrict__ nnb, unsigned* status,
+                                          int* need) {
     // band: per component |error| <= 3 ulp(2 max(|u|, h)) (two operand
     // roundings, the offset, the difference); 2x margin, then sqrt(3) for
     // the length and 1e-6 relative for the squares
-    const float U = fmaxf(__uint_as_float(*umax), fmaxf(p.h[0], fmaxf(p.h[1], p.h[2])));
+    const float U = fmaxf(__uint_as_float(*umax), p.hmax);
     const float dlt = 1.7320509f * (12.f * U * 2.3841858e-7f) + 1e-6f * p.rv;
     const float rl = fmaxf(p.rv - dlt, 0.f), rh = p.rv + dlt;
     const float rsq_lo = rl * rl * (1.f - 1e-6f), rsq_hi = rh * rh * (1.f + 1e-6f);
     const float4 ui = loc[i];
-    const int ci = cell[i];
-    const int cx = ci % p.nc[0], cy = (ci / p.nc[0]) % p.nc[1], cz = ci / (p.nc[0] * p.nc[1]);
-    const float rx = cell_ref(cx, p.h[0], p.base[0]), ry = cell_ref(cy, p.h[1], p.base[1]),
-                rz = cell_ref(cz, p.h[2], p.base[2]);
-    const int mx = axis_count(p.nc[0], p.periodic[0]);
-    const int my = axis_count(p.nc[1], p.periodic[1]);
-    const int mz = axis_count(p.nc[2], p.periodic[2]);
+    const int nx = g.nc(0), ny = g.nc(1), nz = g.nc(2);
+    const int ci = cell[i] - g.cell_base();
+    const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
+    const float rx = cell_ref(cx, g.h(0), g.base(0)), ry = cell_ref(cy, g.h(1), g.base(1)),
+                rz = cell_ref(cz, g.h(2), g.base(2));
+    const int mx = axis_count(nx, g.periodic(0));
+    const int my = axis_count(ny, g.periodic(1));
+    const int mz = axis_count(nz, g.periodic(2));
     const unsigned self_code = nbr_encode(0, 0, 0, 0);
     int cnt = 0;
 #pragma unroll 1
     for (int a = 0; a < mz; a++) {
         int kz, sz;
-        if (!axis_cell(cz, p.nc[2], p.periodic[2], a, kz, sz)) continue;
-        const float pz = ui.z + (((rz - cell_ref(kz, p.h[2], p.base[2])) - sel_shift(sz, p.L.hz)) -
-                                 sel_shift(sz, p.L.lz));
+        if (!axis_cell(cz, nz, g.periodic(2), a, kz, sz)) continue;
+        const float pz = ui.z + (((rz - cell_ref(kz, g.h(2), g.base(2))) - sel_shift(sz, g.L().hz)) -
+                                 sel_shift(sz, g.L().lz));
 #pragma unroll 1
         for (int b = 0; b < my; b++) {
             int ky, sy;
-            if (!axis_cell(cy, p.nc[1], p.periodic[1], b, ky, sy)) continue;
-            const float py = ui.y + (((ry - cell_ref(ky, p.h[1], p.base[1])) - sel_shift(sy, p.L.hy)) -
-                                     sel_shift(sy, p.L.ly));
+            if (!axis_cell(cy, ny, g.periodic(1), b, ky, sy)) continue;
+            const float py = ui.y + (((ry - cell_ref(ky, g.h(1), g.base(1))) - sel_shift(sy, g.L().hy)) -
+                                     sel_shift(sy, g.L().ly));
 #pragma unroll 1
             for (int q = 0; q < mx; q++) {
                 int kx, sx;
-                if (!axis_cell(cx, p.nc[0], p.periodic[0], q, kx, sx)) continue;
-                const float px = ui.x + (((rx - cell_ref(kx, p.h[0], p.base[0])) - sel_shift(sx, p.L.hx)) -
-                                         sel_shift(sx, p.L.lx));
-                const int c = (kz * p.nc[1] + ky) * p.nc[0] + kx;
+                if (!axis_cell(cx, nx, g.periodic(0), q, kx, sx)) continue;
+                const float px = ui.x + (((rx - cell_ref(kx, g.h(0), g.base(0))) - sel_shift(sx, g.L().hx)) -
+                                         sel_shift(sx, g.L().lx));
+                const int c = g.cell_base() + (kz * ny + ky) * nx + kx;
                 const unsigned code = nbr_encode(0, sx, sy, sz);
                 const int e = start[c + 1];
                 for (int k = start[c]; k < e; k++) {
@@ -498,7 +513,8 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const float4* __re
                     if (r2 > rsq_hi) continue;
                     if (k == i && code == self_code) continue;
                     // borderline pairs: the reference's FP64 arithmetic, out of line
-                    if (!(r2 < rsq_lo) && !exact_within(p.L64[0], p.L64[1], p.L64[2], p.rsq, x, y, z, i, k, code))
+                    if (!(r2 < rsq_lo) &&
+                        !exact_within(g.L64(0), g.L64(1), g.L64(2), p.rsq, x, y, z, i, k, code))
                         continue;
                     if (r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
                     if (cnt < p.maxnb) nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
@@ -515,15 +531,24 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const float4* __re
     nnb[i] = cnt;
 }
 
+// REP: the atom's replica supplies the grid, reference points and lengths.
+template <bool REP>
+__global__ void __launch_bounds__(128) k_build(BuildParams p, const RepGeom* __restrict__ rg,
+                                               const int* __restrict__ rep_of, const float4* __restrict__ loc,
+                                               const double* __restrict__ x, const double* __restrict__ y,
+                                               const double* __restrict__ z, const int* __restrict__ cell,
+                                               const int* __restrict__ start, const unsigned* __restrict__ umax,
+                                               unsigned* __restrict__ nbr, int* __restrict__ nnb, unsigned* status,
+                                               int* need) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    if (REP)
+        build_row(p, RepGrid{rg + rep_of[i]}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need);
+    else
+        build_row(p, BoxGrid{p}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need);
+}
+
 // ------------------------------------------------------------------ replicas
-// Replica mode: every replica has its own periodic lengths and cell grid,
-// and its cells occupy the global cell range [cell_base, cell_base + cells).
-struct RepGeom {
-    double lo[3], L[3], cell_org[3], cell_h[3], inv_h[3];
-    int nc[3], periodic[3];
-    int cell_base;
-    ShiftF S;
-};
 
 __global__ void k_cell_assign_rep(int n, double* __restrict__ x, double* __restrict__ y, double* __restrict__ z,
                                   const int* __restrict__ rep_of, const RepGeom* __restrict__ rg,
@@ -545,65 +570,6 @@ __global__ void k_cell_assign_rep(int n, double* __restrict__ x, double* __restr
     }
     cell[i] = c;
     atomicAdd(&count[c], 1);
-}
-
-// Thread per atom over the 27 cells of its replica's grid; the same screen
-// and FP64 tie-break as k_build, with the replica's periodic lengths.
-__global__ void __launch_bounds__(128) k_build_rep(BuildParams p, const RepGeom* __restrict__ rg,
-                                                   const int* __restrict__ rep_of, const PosPack* __restrict__ pack,
-                                                   const double* __restrict__ x, const double* __restrict__ y,
-                                                   const double* __restrict__ z, const int* __restrict__ cell,
-                                                   const int* __restrict__ start, unsigned* __restrict__ nbr,
-                                                   int* __restrict__ nnb, unsigned* status, int* need) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    const RepGeom& g = rg[rep_of[i]];
-    const PosPack pi = pack[i];
-    const int ci = cell[i] - g.cell_base;
-    const int cx = ci % g.nc[0], cy = (ci / g.nc[0]) % g.nc[1], cz = ci / (g.nc[0] * g.nc[1]);
-    int ccx[6], csx[6], ccy[6], csy[6], ccz[6], csz[6];
-    const int mx = axis_candidates(cx, g.nc[0], g.periodic[0], ccx, csx);
-    const int my = axis_candidates(cy, g.nc[1], g.periodic[1], ccy, csy);
-    const int mz = axis_candidates(cz, g.nc[2], g.periodic[2], ccz, csz);
-    const ShiftF S = g.S;
-    int cnt = 0;
-    for (int a = 0; a < mz; a++)
-        for (int b = 0; b < my; b++)
-            for (int q = 0; q < mx; q++) {
-                const int c = g.cell_base + (ccz[a] * g.nc[1] + ccy[b]) * g.nc[0] + ccx[q];
-                const unsigned code = nbr_encode(0, csx[q], csy[b], csz[a]);
-                const bool self_image = (csx[q] == 0 && csy[b] == 0 && csz[a] == 0);
-                const int e = start[c + 1];
-                for (int k = start[c]; k < e; k++) {
-                    if (self_image && k == i) continue;
-                    const PosPack pk = pack[k];
-                    const float3 d = pair_delta(pi.hi, pi.lo, pk.hi, pk.lo, code, S);
-                    const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-                    if (r2 > p.rsq_hi) continue;
-                    bool in = r2 < p.rsq_lo;
-                    if (!in) {
-                        const double sx = csx[q] == 0 ? 0.0 : (csx[q] > 0 ? g.L[0] : -g.L[0]);
-                        const double sy = csy[b] == 0 ? 0.0 : (csy[b] > 0 ? g.L[1] : -g.L[1]);
-                        const double sz = csz[a] == 0 ? 0.0 : (csz[a] > 0 ? g.L[2] : -g.L[2]);
-                        const double dx = __dsub_rn(x[i], __dadd_rn(x[k], sx));
-                        const double dy = __dsub_rn(y[i], __dadd_rn(y[k], sy));
-                        const double dz = __dsub_rn(z[i], __dadd_rn(z[k], sz));
-                        const double rr =
-                            __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-                        in = rr <= p.rsq;
-                    }
-                    if (!in) continue;
-                    if (r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
-                    if (cnt < p.maxnb) nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
-                    cnt++;
-                }
-            }
-    if (cnt > p.maxnb) {
-        atomicOr(status, ERR_NBR_OVERFLOW);
-        atomicMax(need, cnt);
-        cnt = p.maxnb;
-    }
-    nnb[i] = cnt;
 }
 
 // Same list as k_build with LANES threads per atom: the lanes test
@@ -870,6 +836,7 @@ int replica_prepare(Context* c) {
     std::vector<RepGeom> rg(c->nrep);
     std::vector<ShiftF> sh(c->nrep);
     int base = 0;
+    double hmax = 0.0;
     for (int r = 0; r < c->nrep; r++) {
         RepGeom& g = rg[r];
         for (int d = 0; d < 3; d++) {
@@ -888,6 +855,9 @@ int replica_prepare(Context* c) {
                 g.cell_h[d] = ext / g.nc[d];
             }
             g.inv_h[d] = 1.0 / g.cell_h[d];
+            g.base[d] = (float)(g.cell_org[d] - c->box.org[d] + c->box.P[d]);
+            g.hf[d] = (float)g.cell_h[d];
+            hmax = std::max(hmax, g.cell_h[d]);
         }
         const float lh[3] = {(float)g.L[0], (float)g.L[1], (float)g.L[2]};
         g.S.hx = lh[0];
@@ -901,6 +871,7 @@ int replica_prepare(Context* c) {
         base += g.nc[0] * g.nc[1] * g.nc[2];
     }
     c->rep_cells = base;
+    c->rep_hmax = hmax;
     // The step graph holds these pointers: allocate once (omdg_set_replicas
     // frees them) and reallocate only for a larger atom capacity, dropping
     // the graph then.  Contents are rewritten in place.
@@ -987,7 +958,8 @@ PackFrame pack_frame(const Context* c) {
 int integrate_pack(Context* c) {
     if (c->n == 0) return OMDG_OK;
     k_pack<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack,
-                                                       c->xref, nullptr, LocFrame{}, nullptr, nullptr);
+                                                       c->xref, nullptr, LocFrame{}, nullptr, nullptr,
+                                                       nullptr, nullptr);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "pack");
 }
@@ -1038,8 +1010,9 @@ int nlist_build(Context* c) {
     }
     unsigned* umax = reinterpret_cast<unsigned*>(c->d_flags + 3);
     k_zero_ints<<<1, 32, 0, s>>>(1, c->d_flags + 3, c->d_flags + 3);
+    const RepGeom* rg = reps ? static_cast<const RepGeom*>(c->d_rep_geom) : nullptr;
     k_pack<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack, c->xref,
-                                            cell_sorted, lf, reps ? nullptr : c->loc, umax);
+                                            cell_sorted, lf, reps ? c->d_rep_of : nullptr, rg, c->loc, umax);
     c->launches += 2;
     prof_end(c);
 
@@ -1058,18 +1031,20 @@ int nlist_build(Context* c) {
     bp.rsq_lo = (float)(bp.rsq * (1.0 - 2e-5));
     bp.rsq_hi = (float)(bp.rsq * (1.0 + 2e-5));
     bp.rv = (float)rv;
+    bp.hmax = 0.f;
     for (int d = 0; d < 3; d++) {
         bp.base[d] = lf.base[d];
         bp.h[d] = lf.h[d];
+        bp.hmax = fmaxf(bp.hmax, lf.h[d]);
     }
+    if (reps) bp.hmax = (float)c->rep_hmax;
     prof_begin(c, "nlist_build");
     int combos = 1;
     for (int d = 0; d < 3; d++) combos *= (g.periodic[d] && g.nc[d] < 3) ? 3 * g.nc[d] : 3;
     if (reps) {
-        k_build_rep<<<grid_for(n, 128), 128, 0, s>>>(bp, static_cast<const RepGeom*>(c->d_rep_geom), c->d_rep_of,
-                                                     c->pack, c->x, c->y, c->z, cell_sorted, c->cell_start,
-                                                     reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
-                                                     c->d_flags + 1);
+        k_build<true><<<grid_for(n, 128), 128, 0, s>>>(bp, rg, c->d_rep_of, c->loc, c->x, c->y, c->z, cell_sorted,
+                                                       c->cell_start, umax, reinterpret_cast<unsigned*>(c->nbr),
+                                                       c->nnb, c->d_status, c->d_flags + 1);
     } else if (c->build_lanes == 0 && combos <= 64) {
         const int cap = 1024;  // staged candidates per chunk (32 bytes each)
         k_build_cells<<<m, BUILD_CELL_THREADS, cap * 2 * sizeof(float4), s>>>(
@@ -1084,9 +1059,10 @@ int nlist_build(Context* c) {
                                                                c->cell_start, reinterpret_cast<unsigned*>(c->nbr),
                                                                c->nnb, c->d_status, c->d_flags + 1);
     } else {
-        k_build<<<grid_for(n, 128), 128, 0, s>>>(bp, c->loc, c->x, c->y, c->z, cell_sorted, c->cell_start, umax,
-                                                 reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
-                                                 c->d_flags + 1);
+        k_build<false><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
+                                                        cell_sorted, c->cell_start, umax,
+                                                        reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
+                                                        c->d_flags + 1);
     }
     c->launches++;
     prof_end(c);

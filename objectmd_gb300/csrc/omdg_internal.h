@@ -171,6 +171,7 @@ struct Context {
     std::vector<double> rep_lo, rep_hi;  // nrep x 3
     int rep_periodic[3] = {1, 1, 0};
     int rep_cells = 0;                   // cells over all replicas
+    double rep_hmax = 0.0;               // largest replica cell size (list screening band)
     int* d_rep_of = nullptr;             // replica of each atom (index order)
     int rep_of_cap = 0;
     void* d_rep_geom = nullptr;          // RepGeom[nrep] (nlist.cu)

@@ -323,6 +323,84 @@ int omdg_nn_load(omdg_nn* nn, const char* path);
 int omdg_count_neighbors_static(const double* x, int n, const double lo[3], const double hi[3], const int periodic[3],
                                 double rcut, int* count, void* stream, char* err, int err_len);
 
+/* ------------------------------------------------------------ checkpoints */
+
+/*
+ * Binary checkpoint in the reference's own format, so that a run resumes
+ * here or hands off to the CPU code and back (MDSystem::SaveSimulation /
+ * LoadSimulation, system.cpp:726-827; AtomContainer::Save / Load,
+ * container.cpp:554-680).  File order:
+ *   "OMD (c) Y ROSANDI" and a time stamp, 32 bytes each (NUL padded);
+ *   the SaveVariables block (system.cpp:656-668, omdg_sim_vars below);
+ *   int count of restart variables, each a label and a value string;
+ *   int count of containers and their names, 32 bytes each;
+ *   "== END OF CONFIG HEADER ===" (32 bytes);
+ *   per container: "$ATOMCONTAINER:" (32 bytes), the name, material, file
+ *   and parameter strings, id, M, Z, Value, posprec, valprec, write_mode,
+ *   the atom count and the raw Atom records (base.h:114-125).
+ * A string is an int length (with the NUL) and its bytes.  Host byte order
+ * and the LP64 layout, on which x86-64 and aarch64 agree.
+ */
+#define OMDG_AUXVAR 16 /* MAXAUXVAR (config.h:26) */
+#define OMDG_FLAG_ACTIVE 1 /* FLAG_ACTIVE (base.h:230) */
+
+typedef struct omdg_sim_vars { /* MDSystem::SaveVariables, in file order */
+    long long begin_time;      /* SimBeginTime (time_t) */
+    int step;                  /* Step */
+    int pboundary;             /* PBoundary: 1 x | 2 y | 4 z (system.h:44-46) */
+    double energy, kinetic, virial, potential, base_potential, elapsed_time;
+    double box[12]; /* SysBox: x0 x1 y0 y1 z0 z1 lx ly lz hlx hly hlz (base.h:54-60) */
+    int write_mode;
+} omdg_sim_vars;
+
+typedef struct omdg_container_desc { /* a container's saved header (container.cpp:566-581) */
+    char name[256], material[256], filename[256], param[1024];
+    int id;                         /* the tid of its atoms */
+    double mass, z, value;          /* M (simulation units), Z, Value */
+    int posprec, valprec, write_mode;
+    int natoms;                     /* its atoms: the next natoms records */
+} omdg_container_desc;
+
+typedef struct omdg_atom_record { /* Atom (base.h:114-125), 232 bytes */
+    int tid, gid, nid, flag;
+    double x, y, z, vx, vy, vz, fx, fy, fz, potential, virial;
+    double aux[OMDG_AUXVAR];
+} omdg_atom_record;
+
+/* Host only (no device work): write a checkpoint from caller arrays.  stamp
+   NULL takes ctime(now) as the reference does; labels/values are nvar
+   restart-variable strings (DataSlot label and AsString, system.cpp:743-748);
+   atoms holds the containers' records back to back. */
+int omdg_checkpoint_write(const char* path, const char* stamp, const omdg_sim_vars* vars, int nvar,
+                          const char* const* labels, const char* const* values, int ncont,
+                          const omdg_container_desc* cont, const omdg_atom_record* atoms, char* err, int err_len);
+/* Host only: the counts, to size omdg_checkpoint_read's arrays. */
+int omdg_checkpoint_info(const char* path, int* ncont, int* natoms, int* nvar, char* err, int err_len);
+/* Host only: read everything.  stamp gets 32 bytes; the restart variables
+   come back in var_buf as label NUL value NUL pairs. */
+int omdg_checkpoint_read(const char* path, omdg_sim_vars* vars, char* stamp, int ncont_cap, omdg_container_desc* cont,
+                         int natom_cap, omdg_atom_record* atoms, char* var_buf, int var_buf_len, char* err,
+                         int err_len);
+
+/* MDSystem::SaveSimulation (system.cpp:767-771) from the context's state.
+   Atoms go out in caller order, container after container (cont[k].natoms
+   each, summing to the atom count): tid = the atom's type, nid = its caller
+   index, gid and flag from the caller (NULL: 0 and OMDG_FLAG_ACTIVE), aux
+   from the caller (n * OMDG_AUXVAR, NULL: zeros); x, v, f, potential and
+   virial from the device; Step, the last ledger row (E = K + P - P0), P0,
+   the elapsed time (sum of the steps' dt, system.cpp:979) and the box from
+   the context. */
+int omdg_save_simulation(omdg_ctx* ctx, const char* path, int ncont, const omdg_container_desc* cont, const int* gid,
+                         const int* flag, const double* aux, int nvar, const char* const* labels,
+                         const char* const* values);
+/* CONTINUE_MODE (system.cpp:1004-1019, LoadSimulation): box and periodicity
+   from SysBox and PBoundary, atoms in file order with type = tid (each
+   type's mass and Z from the container whose id it is), velocities, and the
+   stored forces for the first half-kick (no FirstRun); Step, P0 and the
+   elapsed time continue from the file.  Potentials may be added before or
+   after.  cont (cap entries, may be NULL) receives the container headers. */
+int omdg_load_simulation(omdg_ctx* ctx, const char* path, int cap, omdg_container_desc* cont, int* ncont);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,7 +22,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC", "-Xptxas",
            "-warn-spills"] + ARCH
 SOURCES = ["api.cu", "nlist.cu", "eam.cu", "eam_fast.cu", "pair.cu", "threebody.cu", "integrate.cu", "io.cu",
-           "static_count.cu", "nn_net.cu", "nn_train.cu", "nn_potential.cu", "ttm.cu", "table.cpp"]
+           "static_count.cu", "nn_net.cu", "nn_train.cu", "nn_potential.cu", "ttm.cu", "table.cpp",
+           "checkpoint.cpp"]
 
 
 def _newer(target, deps):

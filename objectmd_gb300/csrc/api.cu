@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <ctime>
 #include <fstream>
 #include <map>
 #include <sstream>
@@ -17,6 +18,7 @@ size_t step_state_bytes();
 int step_state_init(Context* c);
 int step_state_reset(Context* c, int reset_row, int rebuild_every);
 int step_state_read(Context* c, long long* step, int* row, int* rebuild);
+int step_state_set_step(Context* c, long long step);
 int step_clear_rebuild(Context* c);
 int launch_set_rebuild_cond(Context* c, cudaGraphConditionalHandle h);
 int threebody_prepare(Context* c);
@@ -358,6 +360,10 @@ int omdg_set_atoms(omdg_ctx* c, int n, const double* x, const double* v, const i
     if (rc) return rc;
     c->n = n;
     c->ntypes = ntypes;
+    c->caller_type.assign(type, type + n);
+    c->elapsed = 0.0;
+    c->step = 0;
+    c->resume = false;
     for (int t = 0; t < MAX_TYPES; t++) {
         c->mass[t] = t < ntypes ? mass_by_type[t] : 0.0;
         c->zat[t] = (t < ntypes && z_by_type) ? z_by_type[t] : 0.0;
@@ -1019,8 +1025,32 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
     if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
     cudaSetDevice(c->device);
     int rc;
+    if (!c->first_run_done && c->resume) {
+        // CONTINUE_MODE (system.cpp:1004-1019): no FirstRun; the stored forces
+        // drive the first half-kick and Step, P0 and the ledger continue
+        if ((rc = build_list(c))) return rc;
+        if ((rc = threebody_prepare(c))) return rc;
+        if ((rc = step_state_init(c))) return rc;
+        if ((rc = step_state_set_step(c, c->resume_step))) return rc;
+        // one eager evaluation does the kernels' first-use setup outside the
+        // step graph's capture; the stored forces then replace its result
+        if ((rc = forces_compute(c))) return rc;
+        if ((rc = check_status(c))) return rc;
+        if ((rc = io_set_forces(c, c->resume_f.data()))) return rc;
+        if ((rc = step_state_reset(c, 1, c->rebuild_every))) return rc;
+        c->last_kin = c->resume_vars[0];
+        c->last_pot = c->resume_vars[1];
+        c->last_vir = c->resume_vars[2];
+        c->base_potential = c->resume_vars[3];
+        c->step = c->resume_step;
+        c->resume = false;
+        c->resume_f.clear();
+        c->resume_f.shrink_to_fit();
+        c->first_run_done = true;
+    }
     if (!c->first_run_done) {
         // FirstRun (system.cpp:860-873): one force evaluation, energies, base potential
+        c->begin_time = (long long)std::time(nullptr);
         if ((rc = build_list(c))) return rc;
         if ((rc = threebody_prepare(c))) return rc;
         if ((rc = step_state_init(c))) return rc;
@@ -1066,6 +1096,7 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         c->graph_steps += nsteps;
     }
     c->async_steps += nsteps;
+    for (int k = 0; k < nsteps; k++) c->elapsed += c->dt;  // ElapsedTime += TimeStep (system.cpp:979)
     if (nsteps > 0 && c->thermo_tau > 0.0) c->lambda_pending = true;
     return OMDG_OK;
 }
@@ -1133,6 +1164,144 @@ int omdg_ledger(omdg_ctx* c, double* kinetic, double* potential, double* base_po
     if (potential) *potential = c->last_pot;
     if (base_potential) *base_potential = c->base_potential;
     if (virial) *virial = c->last_vir;
+    return OMDG_OK;
+}
+
+int omdg_save_simulation(omdg_ctx* c, const char* path, int ncont, const omdg_container_desc* cont, const int* gid,
+                         const int* flag, const double* aux, int nvar, const char* const* labels,
+                         const char* const* values) {
+    if (!c || !path || ncont <= 0 || !cont) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    long total = 0;
+    for (int k = 0; k < ncont; k++) total += cont[k].natoms;
+    if (total != c->n) return set_error(c, OMDG_EINVAL, "the containers' atom counts do not sum to the atom count");
+    cudaSetDevice(c->device);
+    int rc = omdg_sync(c);
+    if (rc) return rc;
+    const int n = c->n;
+    std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), f(3 * (size_t)n), pot(n), vir(n);
+    if ((rc = omdg_get_state(c, x.data(), v.data(), f.data(), pot.data(), vir.data()))) return rc;
+    if (c->resume) f = c->resume_f;  // not stepped since the load: the stored forces
+    omdg_sim_vars vars;
+    std::memset(&vars, 0, sizeof(vars));
+    vars.begin_time = c->begin_time;
+    vars.step = (int)c->step;
+    vars.pboundary = (c->box.periodic[0] ? 1 : 0) | (c->box.periodic[1] ? 2 : 0) | (c->box.periodic[2] ? 4 : 0);
+    const double K = c->resume ? c->resume_vars[0] : c->last_kin, P = c->resume ? c->resume_vars[1] : c->last_pot;
+    const double W = c->resume ? c->resume_vars[2] : c->last_vir, P0 = c->resume ? c->resume_vars[3] : c->base_potential;
+    vars.kinetic = K;
+    vars.potential = P;
+    vars.virial = W;
+    vars.base_potential = P0;
+    vars.energy = K + P - P0;  // system.cpp:970
+    vars.elapsed_time = c->elapsed;
+    for (int d = 0; d < 3; d++) {
+        vars.box[2 * d] = c->box.lo[d];
+        vars.box[2 * d + 1] = c->box.hi[d];
+        vars.box[6 + d] = c->box.L[d];
+        vars.box[9 + d] = c->box.L[d] / 2.0;
+    }
+    std::vector<omdg_atom_record> recs(n);
+    for (int i = 0; i < n; i++) {
+        omdg_atom_record& a = recs[i];
+        std::memset(&a, 0, sizeof(a));
+        a.tid = c->caller_type[i];
+        a.gid = gid ? gid[i] : 0;
+        a.nid = i;
+        a.flag = flag ? flag[i] : OMDG_FLAG_ACTIVE;
+        a.x = x[3 * i];
+        a.y = x[3 * i + 1];
+        a.z = x[3 * i + 2];
+        a.vx = v[3 * i];
+        a.vy = v[3 * i + 1];
+        a.vz = v[3 * i + 2];
+        a.fx = f[3 * i];
+        a.fy = f[3 * i + 1];
+        a.fz = f[3 * i + 2];
+        a.potential = pot[i];
+        a.virial = vir[i];
+        if (aux)
+            for (int q = 0; q < OMDG_AUXVAR; q++) a.aux[q] = aux[(size_t)OMDG_AUXVAR * i + q];
+    }
+    char err[256] = {0};
+    rc = omdg_checkpoint_write(path, nullptr, &vars, nvar, labels, values, ncont, cont, recs.data(), err, sizeof(err));
+    if (rc) return set_error(c, rc, err[0] ? err : "checkpoint write");
+    return OMDG_OK;
+}
+
+int omdg_load_simulation(omdg_ctx* c, const char* path, int cap, omdg_container_desc* cont, int* ncont) {
+    if (!c || !path) return OMDG_EINVAL;
+    char err[256] = {0};
+    int nc = 0, na = 0, nv = 0;
+    int rc = omdg_checkpoint_info(path, &nc, &na, &nv, err, sizeof(err));
+    if (rc) return set_error(c, rc, err);
+    if (na <= 0) return set_error(c, OMDG_EFILE, "checkpoint holds no atoms");
+    std::vector<omdg_container_desc> ds(nc);
+    std::vector<omdg_atom_record> recs(na);
+    omdg_sim_vars vars;
+    if ((rc = omdg_checkpoint_read(path, &vars, nullptr, nc, ds.data(), na, recs.data(), nullptr, 0, err,
+                                   sizeof(err))))
+        return set_error(c, rc, err);
+    // types are the atoms' tid; each type's mass and Z from the container
+    // whose id it is, else from the first container holding such atoms
+    int ntypes = 0;
+    for (const omdg_atom_record& a : recs) {
+        if (a.tid < 0 || a.tid >= MAX_TYPES) return set_error(c, OMDG_EFILE, "atom tid outside 0..7");
+        ntypes = std::max(ntypes, a.tid + 1);
+    }
+    std::vector<double> mass(ntypes, -1.0), znum(ntypes, 0.0);
+    for (const omdg_container_desc& d : ds)
+        if (d.id >= 0 && d.id < ntypes && mass[d.id] < 0) {
+            mass[d.id] = d.mass;
+            znum[d.id] = d.z;
+        }
+    {
+        size_t at = 0;
+        for (const omdg_container_desc& d : ds) {
+            for (int k = 0; k < d.natoms; k++, at++) {
+                const int t = recs[at].tid;
+                if (mass[t] < 0) {
+                    mass[t] = d.mass;
+                    znum[t] = d.z;
+                }
+            }
+        }
+    }
+    for (int t = 0; t < ntypes; t++)
+        if (!(mass[t] > 0)) mass[t] = 1.0;  // a type without atoms
+    const double lo[3] = {vars.box[0], vars.box[2], vars.box[4]};
+    const double hi[3] = {vars.box[1], vars.box[3], vars.box[5]};
+    const int per[3] = {vars.pboundary & 1 ? 1 : 0, vars.pboundary & 2 ? 1 : 0, vars.pboundary & 4 ? 1 : 0};
+    if ((rc = omdg_set_box(c, lo, hi, per))) return rc;
+    std::vector<double> x(3 * (size_t)na), v(3 * (size_t)na), f(3 * (size_t)na);
+    std::vector<int> type(na);
+    for (int i = 0; i < na; i++) {
+        const omdg_atom_record& a = recs[i];
+        x[3 * i] = a.x;
+        x[3 * i + 1] = a.y;
+        x[3 * i + 2] = a.z;
+        v[3 * i] = a.vx;
+        v[3 * i + 1] = a.vy;
+        v[3 * i + 2] = a.vz;
+        f[3 * i] = a.fx;
+        f[3 * i + 1] = a.fy;
+        f[3 * i + 2] = a.fz;
+        type[i] = a.tid;
+    }
+    if ((rc = omdg_set_atoms(c, na, x.data(), v.data(), type.data(), ntypes, mass.data(), znum.data()))) return rc;
+    c->resume = true;
+    c->resume_step = vars.step;
+    c->resume_vars[0] = vars.kinetic;
+    c->resume_vars[1] = vars.potential;
+    c->resume_vars[2] = vars.virial;
+    c->resume_vars[3] = vars.base_potential;
+    c->resume_f.swap(f);
+    c->step = vars.step;
+    c->elapsed = vars.elapsed_time;
+    c->begin_time = vars.begin_time;
+    if (ncont) *ncont = nc;
+    if (cont)
+        for (int k = 0; k < nc && k < cap; k++) cont[k] = ds[k];
     return OMDG_OK;
 }
 

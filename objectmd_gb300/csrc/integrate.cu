@@ -417,6 +417,18 @@ int step_state_reset(Context* c, int reset_row, int rebuild_every) {
     return check_cuda(c, e, "step state");
 }
 
+// Step counter of a resumed run (Step from a checkpoint).
+int step_state_set_step(Context* c, long long step) {
+    StepState h;
+    cudaError_t e = cudaMemcpyAsync(&h, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "step state");
+    h.step = step;
+    e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return check_cuda(c, e, "step state");
+}
+
 int step_state_graph_rebuilds(Context* c, int* nrebuild) {
     StepState h;
     cudaError_t e = cudaMemcpyAsync(&h, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);

@@ -61,6 +61,22 @@ __global__ void k_from_caller3(int n, const int* __restrict__ id, const double* 
     c[k] = in[o + 2];
 }
 
+__global__ void k_from_caller3f(int n, const int* __restrict__ id, const double* __restrict__ in,
+                                float* __restrict__ a, float* __restrict__ b, float* __restrict__ c,
+                                double* __restrict__ f64) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    size_t o = 3 * (size_t)id[k];
+    a[k] = (float)in[o];
+    b[k] = (float)in[o + 1];
+    c[k] = (float)in[o + 2];
+    if (f64) {
+        f64[3 * (size_t)k] = in[o];
+        f64[3 * (size_t)k + 1] = in[o + 1];
+        f64[3 * (size_t)k + 2] = in[o + 2];
+    }
+}
+
 // Staging layout (doubles): x [0,3n) v [3n,6n) f [6n,9n) pot [9n,10n) vir [10n,11n).
 static int ensure_io(Context* c) {
     size_t need = (size_t)11 * c->cap;
@@ -121,6 +137,19 @@ int io_set_state(Context* c, const double* x, const double* v) {
         k_from_caller3<<<g, 256, 0, s>>>(n, c->id, c->d_io + n3, c->vx, c->vy, c->vz);
     }
     return check_cuda(c, cudaGetLastError(), "state upload");
+}
+
+// Upload forces given in caller order (n*3 FP64; the FP32 arrays get their
+// rounding, the FP64 block of the FP64 pair mode the values themselves).
+int io_set_forces(Context* c, const double* f) {
+    int rc = ensure_io(c);
+    if (rc) return rc;
+    int n = c->n, g = grid_for(n, 256);
+    cudaStream_t s = c->stream;
+    const size_t n3 = 3 * (size_t)n;
+    cudaMemcpyAsync(c->d_io + 2 * n3, f, sizeof(double) * n3, cudaMemcpyHostToDevice, s);
+    k_from_caller3f<<<g, 256, 0, s>>>(n, c->id, c->d_io + 2 * n3, c->fx, c->fy, c->fz, c->use_f64 ? c->f64 : nullptr);
+    return check_cuda(c, cudaGetLastError(), "force upload");
 }
 
 }  // namespace omdg

@@ -253,6 +253,14 @@ struct Context {
     double* h_ledger = nullptr;     // pinned copy
     double base_potential = 0;
     double last_kin = 0, last_pot = 0, last_vir = 0;
+    double elapsed = 0;                 // ElapsedTime: the steps' dt summed in order (system.cpp:979)
+    long long begin_time = 0;           // SimBeginTime: wall clock (time_t) of the first step or the checkpoint
+    std::vector<int> caller_type;       // atom types in caller order (checkpoint records)
+    // a run resumed from a checkpoint: applied at the first step instead of FirstRun
+    bool resume = false;
+    long long resume_step = 0;
+    double resume_vars[4] = {0, 0, 0, 0};  // kinetic, potential, virial, base potential
+    std::vector<double> resume_f;          // stored forces, caller order
     int last_rows = 0;
     long launches = 0;
 
@@ -313,6 +321,7 @@ int step_state_graph_rebuilds(Context* c, int* nrebuild);
 // caller-order transfers (io.cu); asynchronous on the context stream
 int io_get_state(Context* c, double* x, double* v, double* f, double* pot, double* vir);
 int io_set_state(Context* c, const double* x, const double* v);
+int io_set_forces(Context* c, const double* f);
 
 // grid sizing
 inline int grid_for(int n, int block) { return (n + block - 1) / block; }

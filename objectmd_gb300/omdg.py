@@ -33,6 +33,50 @@ ERRORS = {
 _P = ctypes.POINTER
 _d, _i, _l, _vp, _cp = ctypes.c_double, ctypes.c_int, ctypes.c_long, ctypes.c_void_p, ctypes.c_char_p
 _f = ctypes.c_float
+
+
+# ---- the reference's binary checkpoint (include/omdg.h, checkpoints)
+AUXVAR = 16
+FLAG_ACTIVE = 1
+
+
+class SimVars(ctypes.Structure):
+    """MDSystem::SaveVariables (system.cpp:656-668)."""
+    _fields_ = [("begin_time", ctypes.c_longlong), ("step", _i), ("pboundary", _i), ("energy", _d),
+                ("kinetic", _d), ("virial", _d), ("potential", _d), ("base_potential", _d),
+                ("elapsed_time", _d), ("box", _d * 12), ("write_mode", _i)]
+
+
+class ContainerDesc(ctypes.Structure):
+    """A container's saved header (container.cpp:566-581)."""
+    _fields_ = [("name", ctypes.c_char * 256), ("material", ctypes.c_char * 256),
+                ("filename", ctypes.c_char * 256), ("param", ctypes.c_char * 1024), ("id", _i), ("mass", _d),
+                ("z", _d), ("value", _d), ("posprec", _i), ("valprec", _i), ("write_mode", _i), ("natoms", _i)]
+
+
+# Atom (base.h:114-125): 232 bytes
+ATOM_DTYPE = np.dtype([("tid", "<i4"), ("gid", "<i4"), ("nid", "<i4"), ("flag", "<i4"), ("x", "<f8"),
+                       ("y", "<f8"), ("z", "<f8"), ("vx", "<f8"), ("vy", "<f8"), ("vz", "<f8"), ("fx", "<f8"),
+                       ("fy", "<f8"), ("fz", "<f8"), ("potential", "<f8"), ("virial", "<f8"),
+                       ("aux", "<f8", (AUXVAR,))])
+assert ATOM_DTYPE.itemsize == 232
+
+
+def container(name, natoms, id=0, mass=1.0, z=0.0, material="", filename="", param="", value=0.0, posprec=0,
+              valprec=0, write_mode=0):
+    d = ContainerDesc()
+    d.name = name.encode()
+    d.material = material.encode()
+    d.filename = filename.encode()
+    d.param = param.encode()
+    d.id, d.mass, d.z, d.value = int(id), float(mass), float(z), float(value)
+    d.posprec, d.valprec, d.write_mode, d.natoms = int(posprec), int(valprec), int(write_mode), int(natoms)
+    return d
+
+
+def _strings(items):
+    arr = (_cp * max(1, len(items)))(*[x.encode() for x in items])
+    return arr
 SIGNATURES = {
     "omdg_create": [_P(_vp), _i],
     "omdg_destroy": [_vp],
@@ -96,6 +140,11 @@ SIGNATURES = {
     "omdg_nn_predict": [_vp, _i, _i, _i, _P(_d), _P(_d)],
     "omdg_nn_save": [_vp, _cp],
     "omdg_nn_load": [_vp, _cp],
+    "omdg_checkpoint_write": [_cp, _cp, _P(SimVars), _i, _P(_cp), _P(_cp), _i, _P(ContainerDesc), _vp, _cp, _i],
+    "omdg_checkpoint_info": [_cp, _P(_i), _P(_i), _P(_i), _cp, _i],
+    "omdg_checkpoint_read": [_cp, _P(SimVars), _cp, _i, _P(ContainerDesc), _i, _vp, _cp, _i, _cp, _i],
+    "omdg_save_simulation": [_vp, _cp, _i, _P(ContainerDesc), _P(_i), _P(_i), _P(_d), _i, _P(_cp), _P(_cp)],
+    "omdg_load_simulation": [_vp, _cp, _i, _P(ContainerDesc), _P(_i)],
 }
 STRING_RESULT = ("omdg_last_error", "omdg_nn_last_error")
 
@@ -138,6 +187,47 @@ def count_neighbors_static(x_ptr, n, lo, hi, periodic, rcut, count_ptr, stream=N
     rc = lib.omdg_count_neighbors_static(x_ptr, int(n), lo3, hi3, per3, float(rcut), count_ptr, stream, err, 256)
     if rc != OMDG_OK:
         raise OMDGError(rc, err.value.decode())
+
+
+def checkpoint_write(path, vars, containers, atoms, restart_vars=(), stamp=None):
+    """omdg_checkpoint_write (host only): vars a SimVars, containers a list of
+    ContainerDesc, atoms an ATOM_DTYPE array (the containers' atoms back to
+    back), restart_vars (label, value) string pairs."""
+    lib = load()
+    atoms = np.ascontiguousarray(atoms, dtype=ATOM_DTYPE)
+    conts = (ContainerDesc * len(containers))(*containers)
+    labels = _strings([l for l, _ in restart_vars])
+    values = _strings([v for _, v in restart_vars])
+    err = ctypes.create_string_buffer(256)
+    rc = lib.omdg_checkpoint_write(path.encode(), None if stamp is None else stamp.encode(), ctypes.byref(vars),
+                                   len(restart_vars), labels, values, len(containers), conts,
+                                   atoms.ctypes.data_as(_vp), err, 256)
+    if rc != OMDG_OK:
+        raise OMDGError(rc, err.value.decode())
+
+
+def checkpoint_read(path):
+    """omdg_checkpoint_read (host only) -> (SimVars, stamp bytes, [ContainerDesc],
+    ATOM_DTYPE array, [(label, value)])."""
+    lib = load()
+    err = ctypes.create_string_buffer(256)
+    nc, na, nv = _i(), _i(), _i()
+    rc = lib.omdg_checkpoint_info(path.encode(), ctypes.byref(nc), ctypes.byref(na), ctypes.byref(nv), err, 256)
+    if rc != OMDG_OK:
+        raise OMDGError(rc, err.value.decode())
+    vars = SimVars()
+    stamp = ctypes.create_string_buffer(32)
+    conts = (ContainerDesc * max(1, nc.value))()
+    atoms = np.zeros(na.value, dtype=ATOM_DTYPE)
+    vlen = 1 << 20
+    vbuf = ctypes.create_string_buffer(vlen)
+    rc = lib.omdg_checkpoint_read(path.encode(), ctypes.byref(vars), stamp, nc.value, conts, na.value,
+                                  atoms.ctypes.data_as(_vp), vbuf, vlen, err, 256)
+    if rc != OMDG_OK:
+        raise OMDGError(rc, err.value.decode())
+    parts = vbuf.raw.split(b"\0")
+    rv = [(parts[2 * k].decode(), parts[2 * k + 1].decode()) for k in range(nv.value)]
+    return vars, stamp.raw, list(conts)[:nc.value], atoms, rv
 
 
 NN_PARAMS = 6337  # W1[64x32] b1[64] W2[64x64] b2[64] w3[64] b3
@@ -309,8 +399,15 @@ class Context:
         self._check(self.lib.omdg_set_atoms(self.h, n, _dp(x), _dp(v), _ip(t), len(m), _dp(m), _dp(z)))
         self.n = n
 
+    def num_atoms(self):
+        """omdg_num_atoms: the library's atom count (host buffers are sized from it)."""
+        n = _i()
+        self._check(self.lib.omdg_num_atoms(self.h, ctypes.byref(n)))
+        self.n = n.value
+        return n.value
+
     def get_state(self):
-        n = self.n
+        n = self.num_atoms()
         x = np.zeros((n, 3))
         v = np.zeros((n, 3))
         f = np.zeros((n, 3))
@@ -442,6 +539,26 @@ class Context:
         self._check(self.lib.omdg_ledger(self.h, ctypes.byref(k), ctypes.byref(p), ctypes.byref(b), ctypes.byref(w)))
         return {"kinetic": k.value, "potential": p.value, "base_potential": b.value, "virial": w.value,
                 "energy": k.value + p.value - b.value}
+
+    def save_simulation(self, path, containers, gid=None, flag=None, aux=None, restart_vars=()):
+        """omdg_save_simulation: the reference's checkpoint from this context."""
+        conts = (ContainerDesc * len(containers))(*containers)
+        g = None if gid is None else np.ascontiguousarray(gid, dtype=np.int32)
+        f = None if flag is None else np.ascontiguousarray(flag, dtype=np.int32)
+        a = None if aux is None else np.ascontiguousarray(aux, dtype=np.float64)
+        labels = _strings([l for l, _ in restart_vars])
+        values = _strings([v for _, v in restart_vars])
+        self._check(self.lib.omdg_save_simulation(self.h, path.encode(), len(containers), conts,
+                                                  None if g is None else _ip(g), None if f is None else _ip(f),
+                                                  None if a is None else _dp(a), len(restart_vars), labels, values))
+
+    def load_simulation(self, path, cap=64):
+        """omdg_load_simulation: resume from a checkpoint; returns its containers."""
+        conts = (ContainerDesc * cap)()
+        nc = _i()
+        self._check(self.lib.omdg_load_simulation(self.h, path.encode(), cap, conts, ctypes.byref(nc)))
+        self.num_atoms()
+        return list(conts)[:min(cap, nc.value)]
 
     def ledger_history(self, cap=1 << 16):
         k = np.zeros(cap)

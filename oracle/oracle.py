@@ -289,11 +289,14 @@ def berendsen_factor(dt, tau, tset, tnow):
 # ------------------------------------------------------- reference executable
 
 def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh=0, dump_nbr=False,
-                  pair2=None, tcontrol=None, table_dir=None, swfix=False, time_only=False, timeout=3600, ttm=None):
+                  pair2=None, tcontrol=None, table_dir=None, swfix=False, time_only=False, timeout=3600, ttm=None,
+                  save=None, cont=None):
     """Run the reference's own code (oracle/_ref/ref_driver) on an Import file.
 
     Returns a dict with 'atoms' (nid, tid, x, v, f, potential, virial sorted
     by nid), optional 'nbr' tuples, 'ledger' rows and the summary values.
+    save: write the reference's binary checkpoint there after the run;
+    cont: resume from that checkpoint (steps is then the Step to stop at).
     """
     exe = REF_DRIVER_SWFIX if swfix else REF_DRIVER
     if not os.path.exists(exe):
@@ -306,6 +309,10 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
         args += ["pair2", pair2]
     if tcontrol:
         args += ["tcontrol", repr(tcontrol[0]), repr(tcontrol[1])]
+    if save:
+        args += ["save", os.path.abspath(save)]
+    if cont:
+        args += ["continue", os.path.abspath(cont)]
     if ttm:  # (electron-phonon table file, atom volume, initial electron temperature)
         args += ["ttm", os.path.abspath(ttm[0]), repr(float(ttm[1])), repr(float(ttm[2]))]
     env = dict(os.environ)

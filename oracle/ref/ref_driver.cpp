@@ -26,6 +26,11 @@
  *                        (step Te int_Een int_Aen avg_temp) and thermo.txt (nid T_i n_i)
  *   dump_nbr    0|1      write the neighbour tuples of the final list
  *   time_only   0|1      only print the RunKernel wall time
+ *   save        <file>   after the run, the reference's binary checkpoint
+ *                        (MDSystemGrid::SaveSimulation, systemgrid.cpp:848-852)
+ *   continue    <file>   resume from a binary checkpoint (CONTINUE_MODE,
+ *                        system.cpp:218-222, 1004-1019); `steps` is then the
+ *                        Step to stop at, not a count
  *
  * Outputs in <outdir>: atoms.txt (nid x y z vx vy vz fx fy fz potential virial
  * for local atoms sorted by nid), nbr.txt (nid_i nid_j sx sy sz), ledger.txt
@@ -200,6 +205,7 @@ public:
         }
         fclose(f);
         if (get("dump_nbr", "0") != "0") DumpNeighbours();
+        if (opt.count("save")) SaveSimulation(get("save", ""));
         if (ttmlog) {
             fclose(ttmlog);
             ttmlog = 0;
@@ -309,6 +315,10 @@ int main(int argc, char** argv) {
     args.push_back("time.max");
     args.push_back("1e30");
     args.push_back("--silent");
+    if (opt.count("continue")) {
+        args.push_back("continue");
+        args.push_back(opt["continue"][0]);
+    }
     if (!opt.count("steps") || atoi(opt["steps"][0].c_str()) == 0) args.push_back("mode.static");
     if (opt.count("ttm")) {
         args.push_back("ttmsc.electron-phonon_file");

@@ -117,12 +117,30 @@ def ttm_case(tdir, work):
               atom_volume=np.array(vol), te0=np.array(te0), ttm=res["ttm"], local_temp=th[:, 1], local_dens=th[:, 2])
 
 
+def checkpoint_case(tdir):
+    """The reference's own binary checkpoint: EAM Al 500 saved after 5 steps
+    (MDSystemGrid::SaveSimulation), and its state at Step 10, continued from
+    that file (CONTINUE_MODE).  The file is stored compressed in an npz."""
+    f = os.path.join(GOLD, "eam_al_500.dat")
+    path = os.path.join(tempfile.mkdtemp(prefix="omdck_"), "eam_al_500.bin")
+    oc.run_reference(f, "eam", "aluminum5000", steps=5, dt=0.002, table_dir=tdir, save=path)
+    res = oc.run_reference(f, "eam", "aluminum5000", steps=10, dt=0.002, table_dir=tdir, cont=path)
+    a = res["atoms"]
+    raw = np.frombuffer(open(path, "rb").read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(GOLD, "checkpoint_eam_al_500.npz"), binary=raw, dt=np.array(0.002),
+                        x10=a[:, 2:5], v10=a[:, 5:8], f10=a[:, 8:11], pot10=a[:, 11], ledger=res["ledger"])
+    print("wrote checkpoint_eam_al_500", raw.size, "bytes")
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not oc.build_reference(REF):
         raise SystemExit("reference sources not found at %s" % REF)
     if only == "ttm":
         ttm_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
+        return
+    if only == "checkpoint":
+        checkpoint_case(table_dir())
         return
     write_eam5000(os.path.join(TABLES, "eam.aluminum5000"))
     with open(os.path.join(TABLES, "pair.lj.argon"), "w") as fh:
@@ -200,6 +218,7 @@ def main(only=None):
                             dval=tab[:, 2])
         print("wrote table_%s" % sec.lower(), len(tab))
     ttm_case(tdir, work)
+    checkpoint_case(tdir)
     print("done")
 
 

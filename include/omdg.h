@@ -323,6 +323,38 @@ int omdg_nn_load(omdg_nn* nn, const char* path);
 int omdg_count_neighbors_static(const double* x, int n, const double lo[3], const double hi[3], const int periodic[3],
                                 double rcut, int* count, void* stream, char* err, int err_len);
 
+/* ------------------------------------------------- impact-run modifies */
+
+/*
+ * The modifies of the reference's impact runs (test/si-impact/main.cpp:73-76)
+ * on the device.  Modifies act on atom groups (AtomGroup selections such as
+ * SelectType + SelectInverseBox, main.cpp:55-65): bit g of member[i] puts
+ * caller atom i in group g (0..7); group -1 in the calls below means every
+ * atom.  Membership is fixed, as the reference selects at setup.
+ */
+int omdg_set_groups(omdg_ctx* ctx, const unsigned char* member);
+/* FLAG_ACTIVE per atom (Atom::flag bit 0, base.h:230; SetActive, base.h:285):
+   inactive atoms are not integrated (integrator.cpp:233, :250), not listed
+   (VerletList.cpp:97) and not measured (system.cpp:1067, :1085). */
+int omdg_set_active(omdg_ctx* ctx, const int* active);
+int omdg_get_active(omdg_ctx* ctx, int* active);
+/* ForceDamper (ForceDamper.h:30-36): after the forces, f -= factor * v. */
+int omdg_add_force_damper(omdg_ctx* ctx, int group, double factor);
+/* CoordClamp (CoordClamp.h:23-42): after the forces, f = v = 0 on the axes
+   CoordClamp::Init selects from `axes`; it tests `if(saxis.find('x'))`, so an
+   axis is clamped when its letter is absent or not first ("xyz": y and z). */
+int omdg_add_coord_clamp(omdg_ctx* ctx, int group, const char* axes);
+/* RangeLimiter (RangeLimiter.h:21-54): after each step, group atoms beyond
+   the box -/+ border are deactivated. */
+int omdg_add_range_limiter(omdg_ctx* ctx, int group, double border);
+/* DynamicTimeStep(maxpath, max, update) (DynamicTimeStep.h:44-70): every
+   `update` steps TimeStep = min(maxpath / (1.1 sqrt(SqrMaxVelocity)), max),
+   SqrMaxVelocity over active atoms (system.cpp:1075-1094); evaluated on the
+   device between steps.  TimeStep starts at max (Init with no velocity). */
+int omdg_set_dynamic_timestep(omdg_ctx* ctx, double maxpath, double max_dt, int update);
+/* Integrator->TimeStep and ElapsedTime (system.cpp:979) as the device has them. */
+int omdg_get_timestep(omdg_ctx* ctx, double* dt, double* elapsed);
+
 /* ------------------------------------------------------------ checkpoints */
 
 /*

@@ -18,7 +18,9 @@ size_t step_state_bytes();
 int step_state_init(Context* c);
 int step_state_reset(Context* c, int reset_row, int rebuild_every);
 int step_state_read(Context* c, long long* step, int* row, int* rebuild);
-int step_state_set_step(Context* c, long long step);
+int step_state_resume(Context* c, long long step, double elapsed);
+int step_state_set_dt(Context* c);
+int step_state_times(Context* c, double* dt, double* elapsed);
 int step_clear_rebuild(Context* c);
 int launch_set_rebuild_cond(Context* c, cudaGraphConditionalHandle h);
 int threebody_prepare(Context* c);
@@ -116,7 +118,7 @@ static void free_atoms(Context* c) {
     void* ptrs[] = {c->x,    c->y,     c->z,      c->vx,     c->vy,          c->vz,          c->fx,
                     c->fy,   c->fz,    c->pe,     c->vir,    c->pack,        c->xref,        c->loc,         c->type,
                     c->id,   c->inv,   c->fp,     c->femb,   c->cell,        c->perm,        c->stage_d,
-                    c->stage_i, c->cell_sorted, c->f64, c->extra, c->stage_extra, c->nnb, c->d_red};
+                    c->stage_i, c->cell_sorted, c->f64, c->extra, c->stage_extra, c->nnb, c->d_red, c->aflag};
     for (void* p : ptrs) cudaFree(p);
     c->x = c->y = c->z = c->vx = c->vy = c->vz = nullptr;
     c->fx = c->fy = c->fz = c->pe = c->vir = nullptr;
@@ -133,6 +135,7 @@ static void free_atoms(Context* c) {
     c->extra = c->stage_extra = nullptr;
     c->nnb = nullptr;
     c->d_red = nullptr;
+    c->aflag = nullptr;
     c->cap = 0;
 }
 
@@ -144,10 +147,10 @@ static int alloc_atoms(Context* c, int n) {
               dalloc(c->fz, cap) && dalloc(c->pe, cap) && dalloc(c->vir, cap) && dalloc(c->pack, cap) &&
               dalloc(c->xref, cap) && dalloc(c->loc, cap) && dalloc(c->type, cap) && dalloc(c->id, cap) && dalloc(c->inv, cap) &&
               dalloc(c->fp, cap) && dalloc(c->femb, cap) && dalloc(c->cell, cap) && dalloc(c->perm, cap) &&
-              dalloc(c->stage_d, (size_t)6 * cap) && dalloc(c->stage_i, (size_t)2 * cap) &&
+              dalloc(c->stage_d, (size_t)6 * cap) && dalloc(c->stage_i, (size_t)3 * cap) && dalloc(c->aflag, cap) &&
               dalloc(c->cell_sorted, cap) && dalloc(c->nnb, cap);
     int nb = grid_for(cap, 256) + 1;
-    ok = ok && dalloc(c->d_red, (size_t)3 * nb);
+    ok = ok && dalloc(c->d_red, (size_t)4 * nb);
     if (!ok) return set_error(c, OMDG_ENOMEM, "atom arrays");
     c->cap = cap;
     c->red_cap = nb;
@@ -361,6 +364,7 @@ int omdg_set_atoms(omdg_ctx* c, int n, const double* x, const double* v, const i
     c->n = n;
     c->ntypes = ntypes;
     c->caller_type.assign(type, type + n);
+    c->flags_used = false;
     c->elapsed = 0.0;
     c->step = 0;
     c->resume = false;
@@ -391,6 +395,8 @@ int omdg_set_atoms(omdg_ctx* c, int n, const double* x, const double* v, const i
     cudaMemcpyAsync(c->type, type, sizeof(int) * n, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(c->id, hid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(c->inv, hid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    const std::vector<unsigned> active(n, 1u);  // FLAG_ACTIVE, no groups
+    cudaMemcpyAsync(c->aflag, active.data(), sizeof(unsigned) * n, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(c->d_mass, c->mass, sizeof(double) * MAX_TYPES, cudaMemcpyHostToDevice, s);
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return check_cuda(c, e, "atom upload");
@@ -819,7 +825,7 @@ int forces_compute(Context* c) {
         if (rc) return rc;
         first = false;
     }
-    return OMDG_OK;
+    return post_force_modifies(c);  // MODIFY_POST_FORCE (integrator.cpp:215)
 }
 
 // Eager rebuild of the list when the device asks for it (reads the flag).
@@ -990,8 +996,102 @@ int omdg_compute_forces(omdg_ctx* c) {
 int omdg_set_timestep(omdg_ctx* c, double dt) {
     if (!c || !(dt > 0)) return OMDG_EINVAL;
     c->dt = dt;
+    cudaSetDevice(c->device);
+    invalidate_graph(c);          // captured TTM kernels carry dt
+    return step_state_set_dt(c);  // the step kernels read dt from the step state
+}
+
+int omdg_get_timestep(omdg_ctx* c, double* dt, double* elapsed) {
+    if (!c) return OMDG_EINVAL;
+    cudaSetDevice(c->device);
+    return step_state_times(c, dt, elapsed);
+}
+
+// ------------------------------------------------------ impact-run modifies
+
+static bool valid_group(int g) { return g >= -1 && g < 8; }
+
+int omdg_set_groups(omdg_ctx* c, const unsigned char* member) {
+    if (!c || !member) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    cudaSetDevice(c->device);
+    std::vector<unsigned> f(c->n);
+    for (int i = 0; i < c->n; i++) f[i] = (unsigned)member[i] << 8;
+    c->flags_used = true;
+    invalidate_graph(c);
+    return io_set_flags(c, f.data(), 0xFFu);  // group bits replaced, the active bit kept
+}
+
+int omdg_set_active(omdg_ctx* c, const int* active) {
+    if (!c || !active) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    cudaSetDevice(c->device);
+    std::vector<unsigned> f(c->n);
+    for (int i = 0; i < c->n; i++) f[i] = active[i] ? 1u : 0u;
+    c->flags_used = true;
+    c->list_valid = false;  // the list takes active atoms only
+    invalidate_graph(c);
+    return io_set_flags(c, f.data(), ~1u);
+}
+
+int omdg_get_active(omdg_ctx* c, int* active) {
+    if (!c || !active) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    cudaSetDevice(c->device);
+    std::vector<unsigned> f(c->n);
+    int rc = io_get_flags(c, f.data());
+    if (rc) return rc;
+    for (int i = 0; i < c->n; i++) active[i] = (int)(f[i] & 1u);
+    return OMDG_OK;
+}
+
+int omdg_add_force_damper(omdg_ctx* c, int group, double factor) {
+    if (!c || !valid_group(group) || !std::isfinite(factor)) return OMDG_EINVAL;
+    if (c->post_ops.size() >= 4) return set_error(c, OMDG_EINVAL, "at most 4 force modifies");
+    c->post_ops.push_back({1, group, factor, 0});
+    c->flags_used = true;
     invalidate_graph(c);
     return OMDG_OK;
+}
+
+int omdg_add_coord_clamp(omdg_ctx* c, int group, const char* axes) {
+    if (!c || !valid_group(group)) return OMDG_EINVAL;
+    if (c->post_ops.size() >= 4) return set_error(c, OMDG_EINVAL, "at most 4 force modifies");
+    // CoordClamp::Init (CoordClamp.h:28-33) tests `if(saxis.find('x'))`: an
+    // axis is clamped when its letter is absent or not the first character
+    // ("xyz" clamps y and z)
+    const std::string a = axes ? axes : "xyz";
+    int mask = 0;
+    if (a.find('x') != 0) mask |= 1;
+    if (a.find('y') != 0) mask |= 2;
+    if (a.find('z') != 0) mask |= 4;
+    c->post_ops.push_back({2, group, 0.0, mask});
+    c->flags_used = true;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_add_range_limiter(omdg_ctx* c, int group, double border) {
+    if (!c || !valid_group(group) || !std::isfinite(border)) return OMDG_EINVAL;
+    c->range_on = true;
+    c->range_group = group;
+    c->range_border = border;
+    c->flags_used = true;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_set_dynamic_timestep(omdg_ctx* c, double maxpath, double max_dt, int update) {
+    if (!c || !(maxpath > 0) || !(max_dt > 0) || update < 1) return OMDG_EINVAL;
+    if (c->ttm) return set_error(c, OMDG_EINVAL, "a dynamic time step cannot drive the TTM");
+    c->dyn_update = update;
+    c->dyn_maxpath = maxpath;
+    c->dyn_maxdt = max_dt;
+    // DynamicTimeStep::Init with no measured velocity: TimeStep = max
+    c->dt = max_dt;
+    cudaSetDevice(c->device);
+    invalidate_graph(c);
+    return step_state_set_dt(c);
 }
 
 int omdg_set_first_step_mode(omdg_ctx* c, int reference_first_step) {
@@ -1031,7 +1131,7 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         if ((rc = build_list(c))) return rc;
         if ((rc = threebody_prepare(c))) return rc;
         if ((rc = step_state_init(c))) return rc;
-        if ((rc = step_state_set_step(c, c->resume_step))) return rc;
+        if ((rc = step_state_resume(c, c->resume_step, c->elapsed))) return rc;
         // one eager evaluation does the kernels' first-use setup outside the
         // step graph's capture; the stored forces then replace its result
         if ((rc = forces_compute(c))) return rc;
@@ -1057,7 +1157,10 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         // TTM's first PreIntegration only measures (TTM_Homogen_SCNA.h:356-366)
         if (c->ttm && (rc = thermo_detect(c))) return rc;
         if ((rc = forces_compute(c))) return rc;
-        if ((rc = measure_energies(c, 0))) return rc;
+        c->first_measure = true;  // DynamicTimeStep's Step-0 update follows this measurement
+        rc = measure_energies(c, 0);
+        c->first_measure = false;
+        if (rc) return rc;
         if ((rc = check_status(c))) return rc;
         double row[4];
         cudaMemcpy(row, c->d_ledger, sizeof(row), cudaMemcpyDeviceToHost);
@@ -1096,7 +1199,6 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         c->graph_steps += nsteps;
     }
     c->async_steps += nsteps;
-    for (int k = 0; k < nsteps; k++) c->elapsed += c->dt;  // ElapsedTime += TimeStep (system.cpp:979)
     if (nsteps > 0 && c->thermo_tau > 0.0) c->lambda_pending = true;
     return OMDG_OK;
 }
@@ -1124,6 +1226,7 @@ int omdg_sync(omdg_ctx* c) {
     int rows;
     if ((rc = step_state_read(c, &step, &rows, nullptr))) return rc;
     c->step = step;
+    if ((rc = step_state_times(c, nullptr, &c->elapsed))) return rc;
     int cap = c->ledger_cap;
     int nrow = std::min(rows, cap);
     if (nrow > 0) {
@@ -1182,6 +1285,11 @@ int omdg_save_simulation(omdg_ctx* c, const char* path, int ncont, const omdg_co
     std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), f(3 * (size_t)n), pot(n), vir(n);
     if ((rc = omdg_get_state(c, x.data(), v.data(), f.data(), pot.data(), vir.data()))) return rc;
     if (c->resume) f = c->resume_f;  // not stepped since the load: the stored forces
+    std::vector<unsigned> dflag;
+    if (c->flags_used) {
+        dflag.resize(n);
+        if ((rc = io_get_flags(c, dflag.data()))) return rc;
+    }
     omdg_sim_vars vars;
     std::memset(&vars, 0, sizeof(vars));
     vars.begin_time = c->begin_time;
@@ -1208,7 +1316,7 @@ int omdg_save_simulation(omdg_ctx* c, const char* path, int ncont, const omdg_co
         a.tid = c->caller_type[i];
         a.gid = gid ? gid[i] : 0;
         a.nid = i;
-        a.flag = flag ? flag[i] : OMDG_FLAG_ACTIVE;
+        a.flag = flag ? flag[i] : (dflag.empty() ? OMDG_FLAG_ACTIVE : (int)(dflag[i] & 1u));
         a.x = x[3 * i];
         a.y = x[3 * i + 1];
         a.z = x[3 * i + 2];
@@ -1289,6 +1397,13 @@ int omdg_load_simulation(omdg_ctx* c, const char* path, int cap, omdg_container_
         type[i] = a.tid;
     }
     if ((rc = omdg_set_atoms(c, na, x.data(), v.data(), type.data(), ntypes, mass.data(), znum.data()))) return rc;
+    bool any_inactive = false;
+    for (const omdg_atom_record& r : recs) any_inactive = any_inactive || !(r.flag & OMDG_FLAG_ACTIVE);
+    if (any_inactive) {  // SetActive(false) atoms stay out of the integration and the list
+        std::vector<int> act(na);
+        for (int i = 0; i < na; i++) act[i] = recs[i].flag & OMDG_FLAG_ACTIVE;
+        if ((rc = omdg_set_active(c, act.data()))) return rc;
+    }
     c->resume = true;
     c->resume_step = vars.step;
     c->resume_vars[0] = vars.kinetic;

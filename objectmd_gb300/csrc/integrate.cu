@@ -28,18 +28,24 @@ struct StepState {
     double lambda;       // velocity factor to apply before the next kick
     int rebuild_every;   // >0: rebuild when step % rebuild_every == 0
     int nrebuild;        // list builds taken by the graph's conditional node
+    double dt;               // TimeStep (DynamicTimeStep changes it here, between steps)
+    double hdtm[MAX_TYPES];  // (dt/2) / m per type, refreshed with dt
+    double elapsed;          // ElapsedTime (system.cpp:979)
+    double sqrmaxv;          // SqrMaxVelocity of the last measurement (system.cpp:1075-1094)
 };
 
 struct IntParams {
     int n;
-    double hdtm[MAX_TYPES];  // (dt/2) / m per type
-    double dt;
     double org[3], P[3];
     float half_skin2;       // (skin/2)^2
     int use_f64;
     double Q[3];            // P - org: the pack coordinate is X = x + Q
     float Qh[3], Ql[3];     // Q as an FP32 pair (pack_coord)
     float mh[MAX_TYPES], ml[MAX_TYPES];  // mass per type as an FP32 pair
+    int range_on;                        // RangeLimiter (RangeLimiter.h:33-54)
+    unsigned range_group;                // group bits it acts on
+    double range_lo[3], range_hi[3];     // box -/+ border
+    int need_vmax;                       // measure SqrMaxVelocity (DynamicTimeStep)
 };
 
 __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
@@ -48,15 +54,32 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
                                                     const float* __restrict__ fx, const float* __restrict__ fy,
                                                     const float* __restrict__ fz, const double* __restrict__ f64,
                                                     const int* __restrict__ type, PosPack* __restrict__ pack,
-                                                    const float4* __restrict__ xref, StepState* st) {
+                                                    const float4* __restrict__ xref, unsigned* __restrict__ aflag,
+                                                    StepState* st) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     __shared__ int moved;
     if (threadIdx.x == 0) moved = 0;
     __syncthreads();
-    if (i < p.n) {
+    unsigned fl = 1u;
+    if (i < p.n && aflag) {
+        fl = aflag[i];
+        // RangeLimiter::PostIntegration of the previous step (positions are
+        // unchanged since): a group atom beyond box -/+ border is deactivated,
+        // and the list is rebuilt without it
+        if (p.range_on && (fl & 1u) && (fl & p.range_group)) {
+            const double X0 = x[i], Y0 = y[i], Z0 = z[i];
+            if (X0 < p.range_lo[0] || X0 > p.range_hi[0] || Y0 < p.range_lo[1] || Y0 > p.range_hi[1] ||
+                Z0 < p.range_lo[2] || Z0 > p.range_hi[2]) {
+                fl &= ~1u;
+                aflag[i] = fl;
+                moved = 1;
+            }
+        }
+    }
+    if (i < p.n && (fl & 1u)) {  // inactive atoms: the integrator skips them (integrator.cpp:233, :250)
         const double lam = st->lambda;
         int t = type[i];
-        double h = p.hdtm[t];
+        const double h = st->hdtm[t], dt = st->dt;
         double ax, ay, az;
         if (p.use_f64) {
             ax = f64[3 * (size_t)i];
@@ -78,9 +101,9 @@ __global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restr
         ux = fma(ax, h, ux);
         uy = fma(ay, h, uy);
         uz = fma(az, h, uz);
-        double X = fma(p.dt, ux, x[i]);
-        double Y = fma(p.dt, uy, y[i]);
-        double Z = fma(p.dt, uz, z[i]);
+        double X = fma(dt, ux, x[i]);
+        double Y = fma(dt, uy, y[i]);
+        double Z = fma(dt, uz, z[i]);
         vx[i] = ux;
         vy[i] = uy;
         vz[i] = uz;
@@ -111,8 +134,13 @@ struct FinParams {
     const int* ghosts;    // reference compatibility: periodic images added to the atom count (or null)
     unsigned* status;     // ERR_NONFINITE when a total is NaN or infinite
     unsigned* ticket;     // blocks done (the last one resets it)
-    double dt, tau, tset; // thermostat (tau <= 0: off)
+    double tau, tset;     // thermostat (tau <= 0: off)
     double temp_factor;   // 2/3/k_B (unit.h:66-104)
+    int need_vmax;        // SqrMaxVelocity from the block partials
+    int dyn_update;       // DynamicTimeStep period (0: off; DynamicTimeStep.h:58-70)
+    int dyn_apply;        // this measurement precedes a step's PreIntegration
+    double dyn_maxpath, dyn_maxdt;
+    double mass[MAX_TYPES];
 };
 
 // Ledger row, thermostat factor and step counter from the block partials
@@ -120,24 +148,27 @@ struct FinParams {
 // tree).  Partials are read through L2: other blocks wrote them.
 __device__ void finalize_block(const FinParams& p, int nblocks, const double* partial, double* ledger,
                                StepState* st) {
-    __shared__ double sk[RED_BLOCK], se[RED_BLOCK], sw[RED_BLOCK];
-    double k = 0, e = 0, w = 0;
+    __shared__ double sk[RED_BLOCK], se[RED_BLOCK], sw[RED_BLOCK], sv[RED_BLOCK];
+    double k = 0, e = 0, w = 0, vm = 0;
     const int per = (nblocks + RED_BLOCK - 1) / RED_BLOCK;
     const int b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
     for (int b = b0; b < b1; b++) {
-        k += __ldcg(partial + 3 * b);
-        e += __ldcg(partial + 3 * b + 1);
-        w += __ldcg(partial + 3 * b + 2);
+        k += __ldcg(partial + 4 * b);
+        e += __ldcg(partial + 4 * b + 1);
+        w += __ldcg(partial + 4 * b + 2);
+        if (p.need_vmax) vm = fmax(vm, __ldcg(partial + 4 * b + 3));
     }
     sk[threadIdx.x] = k;
     se[threadIdx.x] = e;
     sw[threadIdx.x] = w;
+    sv[threadIdx.x] = vm;
     __syncthreads();
     for (int off = RED_BLOCK / 2; off > 0; off >>= 1) {
         if (threadIdx.x < off) {
             sk[threadIdx.x] += sk[threadIdx.x + off];
             se[threadIdx.x] += se[threadIdx.x + off];
             sw[threadIdx.x] += sw[threadIdx.x + off];
+            sv[threadIdx.x] = fmax(sv[threadIdx.x], sv[threadIdx.x + off]);
         }
         __syncthreads();
     }
@@ -154,14 +185,28 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const double* pa
             // TempController::PostIntegration: T from the system kinetic energy
             const double count = (double)p.natoms + (p.ghosts ? (double)*p.ghosts : 0.0);
             double T = p.temp_factor * kinetic / count;
-            if (T > 0.0) lam = sqrt(1. + p.dt / p.tau * (p.tset / T - 1.));
+            if (T > 0.0) lam = sqrt(1. + st->dt / p.tau * (p.tset / T - 1.));
         }
         ledger[4 * slot + 3] = lam;
+        if (p.need_vmax) st->sqrmaxv = sv[0];
         if (p.count_step) {
             st->lambda = lam;
+            st->elapsed += st->dt;  // ElapsedTime += TimeStep; Step++ (system.cpp:979-980)
             st->step += 1;
             st->row = row + 1;
             if (st->rebuild_every > 0 && (st->step % st->rebuild_every) == 0) st->rebuild = 1;
+        }
+        if (p.dyn_update > 0 && p.dyn_apply && (st->step % p.dyn_update) == 0) {
+            // DynamicTimeStep::PreIntegration of the next step
+            double ndt;
+            if (st->sqrmaxv > 0.0) {
+                ndt = p.dyn_maxpath / (sqrt(st->sqrmaxv) * 1.10);
+                if (ndt > p.dyn_maxdt) ndt = p.dyn_maxdt;
+            } else {
+                ndt = p.dyn_maxdt;
+            }
+            st->dt = ndt;
+            for (int t = 0; t < MAX_TYPES; t++) st->hdtm[t] = p.mass[t] > 0 ? (0.5 * ndt) / p.mass[t] : 0.0;
         }
         *p.ticket = 0u;
     }
@@ -176,15 +221,18 @@ __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, FinParams f, do
                                                     const float* __restrict__ fx, const float* __restrict__ fy,
                                                     const float* __restrict__ fz, const double* __restrict__ f64,
                                                     const int* __restrict__ type, const float* __restrict__ pe,
-                                                    const float* __restrict__ vir, double* __restrict__ partial,
+                                                    const float* __restrict__ vir,
+                                                    const unsigned* __restrict__ aflag, double* __restrict__ partial,
                                                     double* __restrict__ ledger, StepState* st, int kick) {
     const int i = blockIdx.x * RED_BLOCK + threadIdx.x;
     F2 k = {0.f, 0.f}, e = {0.f, 0.f}, w = {0.f, 0.f};
-    if (i < p.n) {
+    double vmax = 0.0;
+    // inactive atoms: not integrated, not measured (system.cpp:1067, :1085)
+    if (i < p.n && (!aflag || (aflag[i] & 1u))) {
         const int t = type[i];
         double ux = vx[i], uy = vy[i], uz = vz[i];
         if (kick) {
-            const double h = p.hdtm[t];
+            const double h = st->hdtm[t];
             if (p.use_f64) {
                 ux = fma(f64[3 * (size_t)i], h, ux);
                 uy = fma(f64[3 * (size_t)i + 1], h, uy);
@@ -203,19 +251,25 @@ __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, FinParams f, do
         k = f2_mul(v2, F2{p.mh[t], p.ml[t]});
         e = p.use_f64 ? f2_from(f64[3 * (size_t)p.n + i]) : F2{pe[i], 0.f};
         w = F2{vir[i], 0.f};
+        if (p.need_vmax)  // sqrv = vx*vx + vy*vy + vz*vz (system.cpp:1086)
+            vmax = __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz));
     }
+    if (p.need_vmax)
+        for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
     for (int o = 16; o > 0; o >>= 1) {
         k = f2_add(k, f2_shfl_xor(k, o));
         e = f2_add(e, f2_shfl_xor(e, o));
         w = f2_add(w, f2_shfl_xor(w, o));
     }
     __shared__ F2 wk[RED_BLOCK / 32], we[RED_BLOCK / 32], ww[RED_BLOCK / 32];
+    __shared__ double wv[RED_BLOCK / 32];
     __shared__ bool last;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) {
         wk[warp] = k;
         we[warp] = e;
         ww[warp] = w;
+        wv[warp] = vmax;
     }
     __syncthreads();
     if (warp == 0) {
@@ -229,9 +283,13 @@ __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, FinParams f, do
             w = f2_add(w, f2_shfl_xor(w, o));
         }
         if (lane == 0) {
-            partial[3 * blockIdx.x + 0] = f2_to_double(k);
-            partial[3 * blockIdx.x + 1] = f2_to_double(e);
-            partial[3 * blockIdx.x + 2] = f2_to_double(w);
+            double bv = 0.0;
+            if (p.need_vmax)
+                for (int q = 0; q < RED_BLOCK / 32; q++) bv = fmax(bv, wv[q]);
+            partial[4 * blockIdx.x + 0] = f2_to_double(k);
+            partial[4 * blockIdx.x + 1] = f2_to_double(e);
+            partial[4 * blockIdx.x + 2] = f2_to_double(w);
+            partial[4 * blockIdx.x + 3] = bv;
             __threadfence();
             last = atomicAdd(f.ticket, 1u) == gridDim.x - 1;
         }
@@ -319,17 +377,98 @@ int replica_sums(Context* c, double* kinetic, double* potential) {
     return OMDG_OK;
 }
 
+// PostForce modifies of the impact runs, in the order added: ForceDamper
+// (ForceDamper.h:30-36: f -= factor v) and CoordClamp (CoordClamp.h:36-42:
+// f = v = 0 on the clamped axes), each on its group's atoms.
+struct PostOpDev {
+    int kind;  // 1 damper, 2 clamp
+    unsigned group;
+    double factor;
+    int axes;
+};
+constexpr int MAX_POST_OPS = 4;
+struct PostParams {
+    int n, nops;
+    PostOpDev op[MAX_POST_OPS];
+};
+
+__global__ void k_post_force(PostParams p, const unsigned* __restrict__ aflag, float* __restrict__ fx,
+                             float* __restrict__ fy, float* __restrict__ fz, double* __restrict__ f64,
+                             double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const unsigned fl = aflag[i];
+    for (int k = 0; k < p.nops; k++) {
+        const PostOpDev& o = p.op[k];
+        if (o.group != ~0u && !(fl & o.group)) continue;
+        if (o.kind == 1) {
+            const double a = __dsub_rn(f64 ? f64[3 * (size_t)i] : (double)fx[i], __dmul_rn(o.factor, vx[i]));
+            const double b = __dsub_rn(f64 ? f64[3 * (size_t)i + 1] : (double)fy[i], __dmul_rn(o.factor, vy[i]));
+            const double c = __dsub_rn(f64 ? f64[3 * (size_t)i + 2] : (double)fz[i], __dmul_rn(o.factor, vz[i]));
+            fx[i] = (float)a;
+            fy[i] = (float)b;
+            fz[i] = (float)c;
+            if (f64) {
+                f64[3 * (size_t)i] = a;
+                f64[3 * (size_t)i + 1] = b;
+                f64[3 * (size_t)i + 2] = c;
+            }
+        } else {
+            if (o.axes & 1) {
+                fx[i] = 0.f;
+                vx[i] = 0.0;
+                if (f64) f64[3 * (size_t)i] = 0.0;
+            }
+            if (o.axes & 2) {
+                fy[i] = 0.f;
+                vy[i] = 0.0;
+                if (f64) f64[3 * (size_t)i + 1] = 0.0;
+            }
+            if (o.axes & 4) {
+                fz[i] = 0.f;
+                vz[i] = 0.0;
+                if (f64) f64[3 * (size_t)i + 2] = 0.0;
+            }
+        }
+    }
+}
+
+int post_force_modifies(Context* c) {
+    if (c->post_ops.empty() || c->n == 0) return OMDG_OK;
+    PostParams p;
+    p.n = c->n;
+    p.nops = (int)c->post_ops.size();
+    if (p.nops > MAX_POST_OPS) return set_error(c, OMDG_EINVAL, "at most 4 force modifies");
+    for (int k = 0; k < p.nops; k++) {
+        const Context::PostOp& o = c->post_ops[k];
+        p.op[k].kind = o.kind;
+        p.op[k].group = group_bits(o.group);
+        p.op[k].factor = o.factor;
+        p.op[k].axes = o.axes;
+    }
+    k_post_force<<<grid_for(c->n, 256), 256, 0, c->stream>>>(p, c->aflag, c->fx, c->fy, c->fz,
+                                                             c->use_f64 ? c->f64 : nullptr, c->vx, c->vy, c->vz);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "force modifies");
+}
+
 // ------------------------------------------------------------------ host
 
 static IntParams int_params(Context* c) {
     IntParams p;
     p.n = c->n;
-    for (int t = 0; t < MAX_TYPES; t++) p.hdtm[t] = c->mass[t] > 0 ? (0.5 * c->dt) / c->mass[t] : 0.0;
     for (int t = 0; t < MAX_TYPES; t++) {
         p.mh[t] = (float)c->mass[t];
         p.ml[t] = (float)(c->mass[t] - (double)p.mh[t]);
     }
-    p.dt = c->dt;
+    // RangeLimiter::Init (RangeLimiter.h:21-29): the box -/+ the border
+    p.range_on = c->range_on ? 1 : 0;
+    p.range_group = group_bits(c->range_group);
+    for (int d = 0; d < 3; d++) {
+        p.range_lo[d] = c->box.lo[d] - c->range_border;
+        p.range_hi[d] = c->box.hi[d] + c->range_border;
+    }
+    p.need_vmax = c->dyn_update > 0 ? 1 : 0;
     for (int d = 0; d < 3; d++) {
         p.org[d] = c->box.org[d];
         p.P[d] = c->box.P[d];
@@ -350,6 +489,7 @@ int integrate_kick_drift(Context* c, int) {
     prof_begin(c, "kick_drift");
     k_kick_drift<<<grid_for(c->n, 256), 256, 0, c->stream>>>(p, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->fx, c->fy,
                                                              c->fz, c->f64, c->type, c->pack, c->xref,
+                                                             c->flags_used ? c->aflag : nullptr,
                                                              reinterpret_cast<StepState*>(c->d_state));
     prof_end(c);
     c->launches++;
@@ -363,13 +503,18 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
     f.natoms = c->n;
     f.ledger_cap = c->ledger_cap;
     f.count_step = count_step;
-    f.dt = c->dt;
     f.tau = c->thermo_tau;
     f.tset = c->thermo_T;
     f.temp_factor = 2.0 / 3.0 / 8.61734279e-05;
     f.ghosts = nullptr;
     f.status = c->d_status;
     f.ticket = reinterpret_cast<unsigned*>(c->d_flags + 4);
+    f.need_vmax = p.need_vmax;
+    f.dyn_update = c->dyn_update;
+    f.dyn_apply = (count_step || c->first_measure) ? 1 : 0;
+    f.dyn_maxpath = c->dyn_maxpath;
+    f.dyn_maxdt = c->dyn_maxdt;
+    for (int t = 0; t < MAX_TYPES; t++) f.mass[t] = c->mass[t];
     if (c->thermo_count_ghosts && count_step && c->thermo_tau > 0.0) {
         // TempController::GetSystemTemperature divides by GetTotalAtom(), which
         // on MDSystemGrid is GetNAtom(): owners plus their periodic ghost images
@@ -392,7 +537,7 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
     }
     prof_begin(c, "kick");
     k_kick<<<nb, RED_BLOCK, 0, c->stream>>>(p, f, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz, c->f64, c->type, c->pe,
-                                            c->vir, c->d_red, c->d_ledger,
+                                            c->vir, c->flags_used ? c->aflag : nullptr, c->d_red, c->d_ledger,
                                             reinterpret_cast<StepState*>(c->d_state), kick);
     prof_end(c);
     c->launches += 1;
@@ -417,16 +562,45 @@ int step_state_reset(Context* c, int reset_row, int rebuild_every) {
     return check_cuda(c, e, "step state");
 }
 
-// Step counter of a resumed run (Step from a checkpoint).
-int step_state_set_step(Context* c, long long step) {
-    StepState h;
-    cudaError_t e = cudaMemcpyAsync(&h, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return check_cuda(c, e, "step state");
-    h.step = step;
-    e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
+static void set_dt(StepState& h, const Context* c, double dt) {
+    h.dt = dt;
+    for (int t = 0; t < MAX_TYPES; t++) h.hdtm[t] = c->mass[t] > 0 ? (0.5 * dt) / c->mass[t] : 0.0;
+}
+
+static int state_rw(Context* c, StepState& h, bool write) {
+    cudaError_t e = cudaMemcpyAsync(write ? (void*)c->d_state : (void*)&h, write ? (const void*)&h : c->d_state,
+                                    sizeof(StepState), write ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
+                                    c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return check_cuda(c, e, "step state");
+}
+
+// Step counter and elapsed time of a resumed run (from a checkpoint).
+int step_state_resume(Context* c, long long step, double elapsed) {
+    StepState h;
+    int rc = state_rw(c, h, false);
+    if (rc) return rc;
+    h.step = step;
+    h.elapsed = elapsed;
+    return state_rw(c, h, true);
+}
+
+// TimeStep set by the caller (omdg_set_timestep) once the state exists.
+int step_state_set_dt(Context* c) {
+    StepState h;
+    int rc = state_rw(c, h, false);
+    if (rc) return rc;
+    set_dt(h, c, c->dt);
+    return state_rw(c, h, true);
+}
+
+int step_state_times(Context* c, double* dt, double* elapsed) {
+    StepState h;
+    int rc = state_rw(c, h, false);
+    if (rc) return rc;
+    if (dt) *dt = h.dt;
+    if (elapsed) *elapsed = h.elapsed;
+    return OMDG_OK;
 }
 
 int step_state_graph_rebuilds(Context* c, int* nrebuild) {
@@ -457,6 +631,9 @@ int step_state_init(Context* c) {
     h.lambda = 1.0;
     h.rebuild_every = c->rebuild_every;
     h.nrebuild = 0;
+    set_dt(h, c, c->dyn_update > 0 ? c->dyn_maxdt : c->dt);  // DynamicTimeStep::Init with no velocity yet
+    h.elapsed = 0.0;
+    h.sqrmaxv = 0.0;
     cudaError_t e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return check_cuda(c, e, "step state");

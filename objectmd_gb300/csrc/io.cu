@@ -139,6 +139,44 @@ int io_set_state(Context* c, const double* x, const double* v) {
     return check_cuda(c, cudaGetLastError(), "state upload");
 }
 
+__global__ void k_flags_from_caller(int n, const int* __restrict__ id, const unsigned* __restrict__ in,
+                                    unsigned keep, unsigned* __restrict__ flag) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    flag[k] = (flag[k] & keep) | (in[id[k]] & ~keep);
+}
+
+__global__ void k_flags_to_caller(int n, const int* __restrict__ id, const unsigned* __restrict__ flag,
+                                  unsigned* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    out[id[k]] = flag[k];
+}
+
+// Per-atom flag words in caller order; bits in keep_mask keep their device
+// values.  Synchronous (the staging is a temporary device buffer).
+int io_set_flags(Context* c, const unsigned* flags, unsigned keep_mask) {
+    unsigned* d = nullptr;
+    const int n = c->n;
+    if (cudaMalloc(&d, sizeof(unsigned) * n) != cudaSuccess) return set_error(c, OMDG_ENOMEM, "flag staging");
+    cudaMemcpyAsync(d, flags, sizeof(unsigned) * n, cudaMemcpyHostToDevice, c->stream);
+    k_flags_from_caller<<<grid_for(n, 256), 256, 0, c->stream>>>(n, c->id, d, keep_mask, c->aflag);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    return check_cuda(c, e == cudaSuccess ? cudaGetLastError() : e, "flag upload");
+}
+
+int io_get_flags(Context* c, unsigned* flags) {
+    unsigned* d = nullptr;
+    const int n = c->n;
+    if (cudaMalloc(&d, sizeof(unsigned) * n) != cudaSuccess) return set_error(c, OMDG_ENOMEM, "flag staging");
+    k_flags_to_caller<<<grid_for(n, 256), 256, 0, c->stream>>>(n, c->id, c->aflag, d);
+    cudaMemcpyAsync(flags, d, sizeof(unsigned) * n, cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    return check_cuda(c, e == cudaSuccess ? cudaGetLastError() : e, "flag read-back");
+}
+
 // Upload forces given in caller order (n*3 FP64; the FP32 arrays get their
 // rounding, the FP64 block of the FP64 pair mode the values themselves).
 int io_set_forces(Context* c, const double* f) {

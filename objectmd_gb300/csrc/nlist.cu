@@ -242,6 +242,7 @@ __global__ void k_cell_sort(int m, const int* __restrict__ start, int* __restric
 struct AtomArrays {
     double *x, *y, *z, *vx, *vy, *vz;
     int *type, *id;
+    unsigned* flag;
     double* extra;   // optional per-atom FP64 state (extra_n values per atom, slot-major)
     int extra_n;
 };
@@ -258,6 +259,7 @@ __global__ void k_permute_gather(int n, const int* __restrict__ perm, AtomArrays
     st.vz[k] = a.vz[o];
     st.type[k] = a.type[o];
     st.id[k] = a.id[o];
+    st.flag[k] = a.flag[o];
     for (int q = 0; q < a.extra_n; q++) st.extra[(size_t)q * n + k] = a.extra[(size_t)q * n + o];
 }
 
@@ -272,6 +274,7 @@ __global__ void k_permute_copyback(int n, AtomArrays st, AtomArrays a) {
     a.vz[k] = st.vz[k];
     a.type[k] = st.type[k];
     a.id[k] = st.id[k];
+    a.flag[k] = st.flag[k];
     for (int q = 0; q < a.extra_n; q++) a.extra[(size_t)q * n + k] = st.extra[(size_t)q * n + k];
 }
 
@@ -329,7 +332,7 @@ __global__ void k_pack(int n, const double* __restrict__ x, const double* __rest
                        const double* __restrict__ z, const int* __restrict__ type, PackFrame f,
                        PosPack* __restrict__ pack, float4* __restrict__ xref, const int* __restrict__ cell,
                        LocFrame lf, const int* __restrict__ rep_of, const RepGeom* __restrict__ rg,
-                       float4* __restrict__ loc, unsigned* umax) {
+                       const unsigned* __restrict__ aflag, float4* __restrict__ loc, unsigned* umax) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     float m = 0.f;
     if (i < n) {
@@ -356,9 +359,15 @@ __global__ void k_pack(int n, const double* __restrict__ x, const double* __rest
             const float ux = __fadd_rn(__fsub_rn(p.hi.x, cell_ref(cx, lf.h[0], lf.base[0])), p.lo.x);
             const float uy = __fadd_rn(__fsub_rn(p.hi.y, cell_ref(cy, lf.h[1], lf.base[1])), p.lo.y);
             const float uz = __fadd_rn(__fsub_rn(p.hi.z, cell_ref(cz, lf.h[2], lf.base[2])), p.lo.z);
-            loc[i] = make_float4(ux, uy, uz, 0.f);
-            m = fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
-            if (!(m <= 3.0e38f)) m = 3.0e38f;  // non-finite: flagged by the cell assignment
+            if (aflag && !(aflag[i] & 1u)) {
+                // inactive (SetActive false): far from every centre, so no
+                // list takes it, and outside the band's max |u|
+                loc[i] = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
+            } else {
+                loc[i] = make_float4(ux, uy, uz, 0.f);
+                m = fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
+                if (!(m <= 3.0e38f)) m = 3.0e38f;  // non-finite: flagged by the cell assignment
+            }
         }
     }
     if (loc) {
@@ -475,6 +484,10 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
     const float rl = fmaxf(p.rv - dlt, 0.f), rh = p.rv + dlt;
     const float rsq_lo = rl * rl * (1.f - 1e-6f), rsq_hi = rh * rh * (1.f + 1e-6f);
     const float4 ui = loc[i];
+    if (ui.x == 3.0e38f) {  // inactive centre (k_pack): an empty row
+        nnb[i] = 0;
+        return;
+    }
     const int nx = g.nc(0), ny = g.nc(1), nz = g.nc(2);
     const int ci = cell[i] - g.cell_base();
     const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
@@ -959,7 +972,7 @@ int integrate_pack(Context* c) {
     if (c->n == 0) return OMDG_OK;
     k_pack<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack,
                                                        c->xref, nullptr, LocFrame{}, nullptr, nullptr,
-                                                       nullptr, nullptr);
+                                                       nullptr, nullptr, nullptr);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "pack");
 }
@@ -989,10 +1002,11 @@ int nlist_build(Context* c) {
     k_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->cell, c->cell_start, c->cell_fill, c->perm);
     k_cell_sort_warp<<<grid_for(m, 8), 256, 0, s>>>(m, c->cell_start, c->perm);
     c->launches += 7;
-    AtomArrays cur{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->extra, c->extra_n};
+    AtomArrays cur{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->aflag, c->extra, c->extra_n};
     AtomArrays stg{c->stage_d, c->stage_d + c->cap, c->stage_d + 2 * (size_t)c->cap, c->stage_d + 3 * (size_t)c->cap,
                    c->stage_d + 4 * (size_t)c->cap, c->stage_d + 5 * (size_t)c->cap, c->stage_i,
-                   c->stage_i + c->cap, c->stage_extra, c->extra_n};
+                   c->stage_i + c->cap, reinterpret_cast<unsigned*>(c->stage_i + 2 * (size_t)c->cap),
+                   c->stage_extra, c->extra_n};
     k_permute_gather<<<grid_for(n, 256), 256, 0, s>>>(n, c->perm, cur, stg);
     k_permute_copyback<<<grid_for(n, 256), 256, 0, s>>>(n, stg, cur);
     c->launches += 2;
@@ -1012,7 +1026,8 @@ int nlist_build(Context* c) {
     k_zero_ints<<<1, 32, 0, s>>>(1, c->d_flags + 3, c->d_flags + 3);
     const RepGeom* rg = reps ? static_cast<const RepGeom*>(c->d_rep_geom) : nullptr;
     k_pack<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack, c->xref,
-                                            cell_sorted, lf, reps ? c->d_rep_of : nullptr, rg, c->loc, umax);
+                                            cell_sorted, lf, reps ? c->d_rep_of : nullptr, rg,
+                                            c->flags_used ? c->aflag : nullptr, c->loc, umax);
     c->launches += 2;
     prof_end(c);
 
@@ -1045,6 +1060,11 @@ int nlist_build(Context* c) {
         k_build<true><<<grid_for(n, 128), 128, 0, s>>>(bp, rg, c->d_rep_of, c->loc, c->x, c->y, c->z, cell_sorted,
                                                        c->cell_start, umax, reinterpret_cast<unsigned*>(c->nbr),
                                                        c->nnb, c->d_status, c->d_flags + 1);
+    } else if (c->flags_used) {  // only the cell-local build skips inactive atoms
+        k_build<false><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
+                                                        cell_sorted, c->cell_start, umax,
+                                                        reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
+                                                        c->d_flags + 1);
     } else if (c->build_lanes == 0 && combos <= 64) {
         const int cap = 1024;  // staged candidates per chunk (32 bytes each)
         k_build_cells<<<m, BUILD_CELL_THREADS, cap * 2 * sizeof(float4), s>>>(

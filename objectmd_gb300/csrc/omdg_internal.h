@@ -183,6 +183,8 @@ struct Context {
     int* scan_partials = nullptr;
     double* stage_d = nullptr;   // permutation staging: 6 FP64 arrays x cap
     int* stage_i = nullptr;      // permutation staging: 2 int arrays x cap
+    unsigned* aflag = nullptr;   // per atom: bit 0 FLAG_ACTIVE (base.h:230), bits 8..15 group membership
+    bool flags_used = false;     // an atom was deactivated or a modify acts on groups
     double* extra = nullptr;     // optional per-atom FP64 state carried through sorts
     double* stage_extra = nullptr;
     int extra_n = 0;
@@ -238,6 +240,20 @@ struct Context {
     bool reference_first_step = true;
     long step = 0;
     double thermo_T = 0, thermo_tau = 0;
+    // modifies of the impact runs (test/si-impact/main.cpp:73-76)
+    struct PostOp {
+        int kind;       // 1 ForceDamper, 2 CoordClamp
+        int group;      // -1: every atom
+        double factor;  // ForceDamper factor
+        int axes;       // CoordClamp mask: 1 x, 2 y, 4 z
+    };
+    std::vector<PostOp> post_ops;   // PostForce, in the order added
+    bool range_on = false;          // RangeLimiter
+    int range_group = -1;
+    double range_border = 0;
+    int dyn_update = 0;             // DynamicTimeStep (update period; 0: off)
+    double dyn_maxpath = 0, dyn_maxdt = 0;
+    bool first_measure = false;     // FirstRun's measurement (DynamicTimeStep at Step 0)
     bool thermo_count_ghosts = false;  // reference compatibility (omdg_set_compat)
     bool lambda_pending = false;       // a thermostat factor waits in the step state
 
@@ -322,6 +338,12 @@ int step_state_graph_rebuilds(Context* c, int* nrebuild);
 int io_get_state(Context* c, double* x, double* v, double* f, double* pot, double* vir);
 int io_set_state(Context* c, const double* x, const double* v);
 int io_set_forces(Context* c, const double* f);
+int post_force_modifies(Context* c);  // ForceDamper / CoordClamp after the forces (integrate.cu)
+int io_set_flags(Context* c, const unsigned* flags, unsigned keep_mask);  // caller order; bits in keep_mask survive
+int io_get_flags(Context* c, unsigned* flags);
+
+// Atom group g as its flag bit (bits 8..15); -1: every atom.
+inline unsigned group_bits(int g) { return g < 0 ? ~0u : (1u << (8 + g)); }
 
 // grid sizing
 inline int grid_for(int n, int block) { return (n + block - 1) / block; }

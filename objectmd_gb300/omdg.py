@@ -140,6 +140,14 @@ SIGNATURES = {
     "omdg_nn_predict": [_vp, _i, _i, _i, _P(_d), _P(_d)],
     "omdg_nn_save": [_vp, _cp],
     "omdg_nn_load": [_vp, _cp],
+    "omdg_set_groups": [_vp, _P(ctypes.c_ubyte)],
+    "omdg_set_active": [_vp, _P(_i)],
+    "omdg_get_active": [_vp, _P(_i)],
+    "omdg_add_force_damper": [_vp, _i, _d],
+    "omdg_add_coord_clamp": [_vp, _i, _cp],
+    "omdg_add_range_limiter": [_vp, _i, _d],
+    "omdg_set_dynamic_timestep": [_vp, _d, _d, _i],
+    "omdg_get_timestep": [_vp, _P(_d), _P(_d)],
     "omdg_checkpoint_write": [_cp, _cp, _P(SimVars), _i, _P(_cp), _P(_cp), _i, _P(ContainerDesc), _vp, _cp, _i],
     "omdg_checkpoint_info": [_cp, _P(_i), _P(_i), _P(_i), _cp, _i],
     "omdg_checkpoint_read": [_cp, _P(SimVars), _cp, _i, _P(ContainerDesc), _i, _vp, _cp, _i, _cp, _i],
@@ -539,6 +547,38 @@ class Context:
         self._check(self.lib.omdg_ledger(self.h, ctypes.byref(k), ctypes.byref(p), ctypes.byref(b), ctypes.byref(w)))
         return {"kinetic": k.value, "potential": p.value, "base_potential": b.value, "virial": w.value,
                 "energy": k.value + p.value - b.value}
+
+    # ---- modifies of the impact runs
+    def set_groups(self, member):
+        """member: per atom, bit g set = in group g (0..7)."""
+        m = np.ascontiguousarray(member, dtype=np.uint8)
+        self._check(self.lib.omdg_set_groups(self.h, m.ctypes.data_as(_P(ctypes.c_ubyte))))
+
+    def set_active(self, active):
+        a = np.ascontiguousarray(active, dtype=np.int32)
+        self._check(self.lib.omdg_set_active(self.h, _ip(a)))
+
+    def get_active(self):
+        a = np.zeros(self.num_atoms(), dtype=np.int32)
+        self._check(self.lib.omdg_get_active(self.h, _ip(a)))
+        return a.astype(bool)
+
+    def add_force_damper(self, group, factor):
+        self._check(self.lib.omdg_add_force_damper(self.h, int(group), float(factor)))
+
+    def add_coord_clamp(self, group, axes="xyz"):
+        self._check(self.lib.omdg_add_coord_clamp(self.h, int(group), axes.encode()))
+
+    def add_range_limiter(self, group, border):
+        self._check(self.lib.omdg_add_range_limiter(self.h, int(group), float(border)))
+
+    def set_dynamic_timestep(self, maxpath, max_dt=0.001, update=5):
+        self._check(self.lib.omdg_set_dynamic_timestep(self.h, float(maxpath), float(max_dt), int(update)))
+
+    def get_timestep(self):
+        dt, el = _d(), _d()
+        self._check(self.lib.omdg_get_timestep(self.h, ctypes.byref(dt), ctypes.byref(el)))
+        return dt.value, el.value
 
     def save_simulation(self, path, containers, gid=None, flag=None, aux=None, restart_vars=()):
         """omdg_save_simulation: the reference's checkpoint from this context."""

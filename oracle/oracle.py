@@ -290,13 +290,16 @@ def berendsen_factor(dt, tau, tset, tnow):
 
 def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh=0, dump_nbr=False,
                   pair2=None, tcontrol=None, table_dir=None, swfix=False, time_only=False, timeout=3600, ttm=None,
-                  save=None, cont=None):
+                  save=None, cont=None, damp=None, clamp=None, dyndt=None, range_border=None):
     """Run the reference's own code (oracle/_ref/ref_driver) on an Import file.
 
     Returns a dict with 'atoms' (nid, tid, x, v, f, potential, virial sorted
     by nid), optional 'nbr' tuples, 'ledger' rows and the summary values.
     save: write the reference's binary checkpoint there after the run;
     cont: resume from that checkpoint (steps is then the Step to stop at).
+    damp (factor), clamp (axes), dyndt (maxpath, max, update), range_border:
+    the impact-run modifies on every atom; the result then also holds 'times'
+    (Step, TimeStep, ElapsedTime per step) and 'active' (nid, flag bit).
     """
     exe = REF_DRIVER_SWFIX if swfix else REF_DRIVER
     if not os.path.exists(exe):
@@ -309,6 +312,14 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
         args += ["pair2", pair2]
     if tcontrol:
         args += ["tcontrol", repr(tcontrol[0]), repr(tcontrol[1])]
+    if damp is not None:
+        args += ["damp", repr(float(damp))]
+    if clamp is not None:
+        args += ["clamp", clamp]
+    if dyndt is not None:
+        args += ["dyndt", repr(float(dyndt[0])), repr(float(dyndt[1])), str(int(dyndt[2]))]
+    if range_border is not None:
+        args += ["range", repr(float(range_border))]
     if save:
         args += ["save", os.path.abspath(save)]
     if cont:
@@ -339,7 +350,7 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
     lp = os.path.join(out, "ledger.txt")
     if os.path.exists(lp):
         res["ledger"] = np.loadtxt(lp, ndmin=2)
-    for name in ("ttm", "thermo"):
+    for name in ("ttm", "thermo", "times", "active"):
         fp = os.path.join(out, name + ".txt")
         if os.path.exists(fp):
             res[name] = np.loadtxt(fp, ndmin=2)

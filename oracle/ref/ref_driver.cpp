@@ -26,6 +26,12 @@
  *                        (step Te int_Een int_Aen avg_temp) and thermo.txt (nid T_i n_i)
  *   dump_nbr    0|1      write the neighbour tuples of the final list
  *   time_only   0|1      only print the RunKernel wall time
+ *   damp        <factor> ForceDamper on every atom (damp.factor, damp.target -)
+ *   clamp       <axes>   CoordClamp("-", axes)
+ *   dyndt       <maxpath> <max> <update>  DynamicTimeStep(maxpath, max, update)
+ *   range       <border> RangeLimiter("-", border)
+ *                        (with any of these: times.txt = Step TimeStep ElapsedTime
+ *                        per step, active.txt = nid flag&FLAG_ACTIVE at the end)
  *   save        <file>   after the run, the reference's binary checkpoint
  *                        (MDSystemGrid::SaveSimulation, systemgrid.cpp:848-852)
  *   continue    <file>   resume from a binary checkpoint (CONTINUE_MODE,
@@ -46,6 +52,10 @@ using namespace omd;
 #include <modify/VerletList.h>
 #include <modify/VerletListFull.h>
 #include <modify/TempController.h>
+#include <modify/ForceDamper.h>
+#include <modify/CoordClamp.h>
+#include <modify/DynamicTimeStep.h>
+#include <modify/RangeLimiter.h>
 #include <detect/ThermoDetector.h>
 #include <misc/TTM_Homogen_SCNA.h>
 
@@ -94,11 +104,13 @@ public:
     double t_begin, t_end;
     FILE* ledger;
     FILE* ttmlog;
+    FILE* timelog;
     ThermoDetector* thermo;
 
     OracleSim(int& argc, char**& argv, const std::string& od,
               const std::map<std::string, std::vector<std::string> >& o)
         : MDSystemGrid(argc, argv), opt(o), outdir(od), nsteps(0), t_begin(0), t_end(0), ledger(0), ttmlog(0),
+          timelog(0),
           thermo(0) {
         nsteps = atoi(get("steps", "0").c_str());
     }
@@ -145,6 +157,13 @@ public:
         if (opt.count("tcontrol"))
             AddModify(new TempController(atof(get("tcontrol", "300", 0).c_str()),
                                          atof(get("tcontrol", "0.1", 1).c_str())));
+        /* the impact-run modifies, in test/si-impact/main.cpp's order */
+        if (opt.count("damp")) AddModify(new ForceDamper);
+        if (opt.count("clamp")) AddModify(new CoordClamp("-", get("clamp", "xyz")));
+        if (opt.count("dyndt"))
+            AddModify(new DynamicTimeStep(atof(get("dyndt", "0.1", 0).c_str()), atof(get("dyndt", "0.001", 1).c_str()),
+                                          atoi(get("dyndt", "5", 2).c_str())));
+        if (opt.count("range")) AddModify(new RangeLimiter("-", atof(get("range", "1000", 0).c_str())));
     }
 
     void SystemSetting() {}
@@ -153,6 +172,7 @@ public:
         bool base = MDSystemGrid::CheckRun();
         if (ledger && Step > 0)
             fprintf(ledger, "%d %.17g %.17g %.17g\n", Step, Kinetic, Potential, Energy);
+        if (timelog) fprintf(timelog, "%d %.17g %.17g\n", Step, Integrator->TimeStep, ElapsedTime);
         if (ttmlog && Step > 0)
             fprintf(ttmlog, "%d %.17g %.17g %.17g %.17g\n", Step, GetMessageSlot("e_temp:")->AsDouble(),
                     GetMessageSlot("int_Een:")->AsDouble(), GetMessageSlot("int_Aen:")->AsDouble(),
@@ -166,6 +186,8 @@ public:
             if (ledger)
                 fprintf(ledger, "%d %.17g %.17g %.17g\n", 0, Kinetic, BasePotential, 0.0);
             if (opt.count("ttm")) ttmlog = fopen((outdir + "/ttm.txt").c_str(), "w");
+            if (opt.count("damp") || opt.count("clamp") || opt.count("dyndt") || opt.count("range"))
+                timelog = fopen((outdir + "/times.txt").c_str(), "w");
         }
         t_begin = wall_now();
     }
@@ -206,6 +228,13 @@ public:
         fclose(f);
         if (get("dump_nbr", "0") != "0") DumpNeighbours();
         if (opt.count("save")) SaveSimulation(get("save", ""));
+        if (timelog) {
+            fclose(timelog);
+            timelog = 0;
+            FILE* t = fopen((outdir + "/active.txt").c_str(), "w");
+            for (int k = 0; k < nloc; k++) fprintf(t, "%d %d\n", Atoms(order[k]).nid, Atoms(order[k]).flag & FLAG_ACTIVE);
+            fclose(t);
+        }
         if (ttmlog) {
             fclose(ttmlog);
             ttmlog = 0;
@@ -279,7 +308,7 @@ int main(int argc, char** argv) {
     std::map<std::string, std::vector<std::string> > opt;
     for (int i = 2; i < argc;) {
         std::string key = argv[i++];
-        int nval = (key == "tcontrol") ? 2 : (key == "ttm" ? 3 : 1);
+        int nval = (key == "tcontrol") ? 2 : ((key == "ttm" || key == "dyndt") ? 3 : 1);
         for (int k = 0; k < nval && i < argc; k++) opt[key].push_back(argv[i++]);
     }
     /* Table mode: the reference TableReader itself (treader.cpp) evaluated at
@@ -315,6 +344,12 @@ int main(int argc, char** argv) {
     args.push_back("time.max");
     args.push_back("1e30");
     args.push_back("--silent");
+    if (opt.count("damp")) {  // ForceDamper::ReadParameter (ForceDamper.h:24-27)
+        args.push_back("damp.factor");
+        args.push_back(opt["damp"][0]);
+        args.push_back("damp.target");
+        args.push_back("-");
+    }
     if (opt.count("continue")) {
         args.push_back("continue");
         args.push_back(opt["continue"][0]);

@@ -132,6 +132,33 @@ def checkpoint_case(tdir):
     print("wrote checkpoint_eam_al_500", raw.size, "bytes")
 
 
+MODIFY_CASES = {  # the impact-run modifies on every atom of an EAM Al slab
+    "damp_clamp": dict(damp=0.05, clamp="xyz"),
+    "dyndt": dict(dyndt=(0.02, 0.004, 3)),
+    "range": dict(range_border=1.0),
+}
+
+
+def modifies_case(tdir, work):
+    """EAM Al 500-atom slab (free z), its top atom launched upward at 60 A/ps,
+    30 steps of 2 fs with ForceDamper + CoordClamp, DynamicTimeStep or
+    RangeLimiter: the reference's trajectories, time steps and active flags."""
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=5, a=4.05, sigma=0.05, temp=300.0, seed_pos=41, seed_vel=42)
+    top = int(np.argmax(x[:, 2]))
+    v[top] = [5.0, -3.0, 60.0]
+    f = os.path.join(work, "eam_al_slab.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), periodic=(True, True, False), species=("aluminum",))
+    out = dict(box_lo=lo, box_hi=hi, top=np.array(top), steps=np.array(30), dt=np.array(0.002))
+    for name, kw in MODIFY_CASES.items():
+        res = oc.run_reference(f, "eam", "aluminum5000", steps=30, dt=0.002, table_dir=tdir, **kw)
+        a = res["atoms"]
+        out.update({name + "_x": a[:, 2:5], name + "_v": a[:, 5:8], name + "_times": res["times"],
+                    name + "_active": res["active"][:, 1].astype(np.int32), name + "_ledger": res["ledger"]})
+    np.savez_compressed(os.path.join(GOLD, "modifies_eam_al_slab.npz"), **out)
+    shutil.copy(f, os.path.join(GOLD, "eam_al_slab.dat"))
+    print("wrote modifies_eam_al_slab")
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not oc.build_reference(REF):
@@ -141,6 +168,9 @@ def main(only=None):
         return
     if only == "checkpoint":
         checkpoint_case(table_dir())
+        return
+    if only == "modifies":
+        modifies_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
         return
     write_eam5000(os.path.join(TABLES, "eam.aluminum5000"))
     with open(os.path.join(TABLES, "pair.lj.argon"), "w") as fh:
@@ -219,6 +249,7 @@ def main(only=None):
         print("wrote table_%s" % sec.lower(), len(tab))
     ttm_case(tdir, work)
     checkpoint_case(tdir)
+    modifies_case(tdir, work)
     print("done")
 
 

@@ -145,10 +145,11 @@ struct FinParams {
 
 // Ledger row, thermostat factor and step counter from the block partials
 // (one block; each thread sums a contiguous run of partials, then a fixed
-// tree).  Partials are read through L2: other blocks wrote them.
+// xor tree per warp and over the warps).  Partials are read through L2:
+// other blocks wrote them.
 __device__ void finalize_block(const FinParams& p, int nblocks, const double* partial, double* ledger,
                                StepState* st) {
-    __shared__ double sk[RED_BLOCK], se[RED_BLOCK], sw[RED_BLOCK], sv[RED_BLOCK];
+    __shared__ double sk[RED_BLOCK / 32], se[RED_BLOCK / 32], sw[RED_BLOCK / 32], sv[RED_BLOCK / 32];
     double k = 0, e = 0, w = 0, vm = 0;
     const int per = (nblocks + RED_BLOCK - 1) / RED_BLOCK;
     const int b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
@@ -158,28 +159,40 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const double* pa
         w += __ldcg(partial + 4 * b + 2);
         if (p.need_vmax) vm = fmax(vm, __ldcg(partial + 4 * b + 3));
     }
-    sk[threadIdx.x] = k;
-    se[threadIdx.x] = e;
-    sw[threadIdx.x] = w;
-    sv[threadIdx.x] = vm;
+    // fixed xor tree within each warp, then over the warps in warp 0
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) {
+        k += __shfl_xor_sync(0xffffffffu, k, o);
+        e += __shfl_xor_sync(0xffffffffu, e, o);
+        w += __shfl_xor_sync(0xffffffffu, w, o);
+        if (p.need_vmax) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+    }
+    if (lane == 0) {
+        sk[warp] = k;
+        se[warp] = e;
+        sw[warp] = w;
+        sv[warp] = vm;
+    }
     __syncthreads();
-    for (int off = RED_BLOCK / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off) {
-            sk[threadIdx.x] += sk[threadIdx.x + off];
-            se[threadIdx.x] += se[threadIdx.x + off];
-            sw[threadIdx.x] += sw[threadIdx.x + off];
-            sv[threadIdx.x] = fmax(sv[threadIdx.x], sv[threadIdx.x + off]);
-        }
-        __syncthreads();
+    if (warp != 0) return;
+    k = lane < RED_BLOCK / 32 ? sk[lane] : 0.0;
+    e = lane < RED_BLOCK / 32 ? se[lane] : 0.0;
+    w = lane < RED_BLOCK / 32 ? sw[lane] : 0.0;
+    vm = lane < RED_BLOCK / 32 ? sv[lane] : 0.0;
+    for (int o = RED_BLOCK / 64; o > 0; o >>= 1) {
+        k += __shfl_xor_sync(0xffffffffu, k, o);
+        e += __shfl_xor_sync(0xffffffffu, e, o);
+        w += __shfl_xor_sync(0xffffffffu, w, o);
+        if (p.need_vmax) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
     }
     if (threadIdx.x == 0) {
-        double kinetic = 0.5 * sk[0];
-        if (!(isfinite(kinetic) && isfinite(se[0]))) atomicOr(p.status, ERR_NONFINITE);
+        double kinetic = 0.5 * k;
+        if (!(isfinite(kinetic) && isfinite(e))) atomicOr(p.status, ERR_NONFINITE);
         int row = st->row;
         int slot = row % p.ledger_cap;  // ring buffer between host reads
         ledger[4 * slot + 0] = kinetic;
-        ledger[4 * slot + 1] = se[0];
-        ledger[4 * slot + 2] = 0.5 * sw[0];
+        ledger[4 * slot + 1] = e;
+        ledger[4 * slot + 2] = 0.5 * w;
         double lam = 1.0;
         if (p.count_step && p.tau > 0.0 && st->step != 0) {
             // TempController::PostIntegration: T from the system kinetic energy
@@ -188,7 +201,7 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const double* pa
             if (T > 0.0) lam = sqrt(1. + st->dt / p.tau * (p.tset / T - 1.));
         }
         ledger[4 * slot + 3] = lam;
-        if (p.need_vmax) st->sqrmaxv = sv[0];
+        if (p.need_vmax) st->sqrmaxv = vm;
         if (p.count_step) {
             st->lambda = lam;
             st->elapsed += st->dt;  // ElapsedTime += TimeStep; Step++ (system.cpp:979-980)

@@ -62,7 +62,9 @@ int omdg_num_atoms(omdg_ctx* ctx, int* n);
 /* Copies device state to host arrays in caller order; any pointer may be NULL.
    x, v, f are n*3; pot, vir are n (per-atom potential and virial as Atom::potential/virial). */
 int omdg_get_state(omdg_ctx* ctx, double* x, double* v, double* f, double* pot, double* vir);
-/* Overwrites positions / velocities (n*3 FP64, caller order); marks the list dirty. */
+/* Overwrites positions / velocities (n*3 FP64, caller order).  New positions
+   keep the neighbour list unless an atom moved more than skin/2 since it was
+   built; the next step or force evaluation then rebuilds it. */
 int omdg_set_positions(omdg_ctx* ctx, const double* x);
 int omdg_set_velocities(omdg_ctx* ctx, const double* v);
 

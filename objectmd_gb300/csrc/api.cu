@@ -460,9 +460,10 @@ int omdg_set_positions(omdg_ctx* c, const double* x) {
     cudaSetDevice(c->device);
     int rc = io_set_state(c, x, nullptr);
     if (rc) return rc;
-    // positions moved by the caller: refresh the packs and request a rebuild
+    // positions set by the caller: refresh the packs; the list stays valid
+    // unless an atom moved more than skin/2 since it was built (the device
+    // displacement check then requests the rebuild the next step takes)
     if ((rc = integrate_pack(c))) return rc;
-    c->list_valid = false;
     return request_rebuild(c);
 }
 
@@ -975,7 +976,7 @@ int omdg_compute_forces(omdg_ctx* c) {
     cudaSetDevice(c->device);
     int rc;
     if (!c->list_valid && (rc = build_list(c))) return rc;
-    if (c->first_run_done && (rc = eager_maybe_rebuild(c))) return rc;
+    else if ((rc = eager_maybe_rebuild(c))) return rc;  // moved more than skin/2 since the build
     if ((rc = threebody_prepare(c))) return rc;
     if ((rc = forces_compute(c))) return rc;
     if ((rc = measure_energies(c, 0))) return rc;

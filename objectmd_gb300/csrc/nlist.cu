@@ -970,8 +970,9 @@ PackFrame pack_frame(const Context* c) {
 
 int integrate_pack(Context* c) {
     if (c->n == 0) return OMDG_OK;
+    // xref keeps the positions of the last build (the displacement reference)
     k_pack<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack,
-                                                       c->xref, nullptr, LocFrame{}, nullptr, nullptr,
+                                                       nullptr, nullptr, LocFrame{}, nullptr, nullptr,
                                                        nullptr, nullptr, nullptr);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "pack");

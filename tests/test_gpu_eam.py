@@ -165,3 +165,29 @@ def test_eam_nve_drift_over_10k_steps(omdg_lib):
         e1 = ctx.ledger()["energy"]
     assert np.isfinite(e1)
     assert abs(e1 - e0) / len(x) < 5e-4
+
+
+def test_position_upload_keeps_or_rebuilds_the_list(omdg_lib):
+    """Positions set by the caller keep the list while every atom stays within
+    skin/2 of where the list was built, and trigger a rebuild otherwise; the
+    forces equal those of a fresh context on the same positions either way."""
+    d = load_case("eam_al_500")
+    rng = np.random.default_rng(8)
+    with make_eam(omdg_lib, d, rebuild_every=0) as ctx:
+        ctx.compute_forces()
+        r0 = ctx.stats()["rebuilds"]
+        for shift, rebuilt in ((0.05, False), (0.4, True)):  # skin/2 = 0.15 A
+            x = d["x0"].copy()
+            x[7] += rng.normal(size=3) * shift / np.sqrt(3.0) + np.array([shift, 0.0, 0.0])
+            ctx.set_positions(x)
+            ctx.compute_forces()
+            r1 = ctx.stats()["rebuilds"]
+            assert (r1 > r0) == rebuilt
+            r0 = r1
+            f = ctx.get_state()["f"]
+            fresh = dict(d)
+            fresh["x0"] = x
+            with make_eam(omdg_lib, fresh, rebuild_every=0) as ref:
+                ref.compute_forces()
+                fr = ref.get_state()["f"]
+            assert np.abs(f - fr).max() <= 1e-6 * np.abs(fr).max() + 1e-7

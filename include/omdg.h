@@ -357,6 +357,37 @@ int omdg_set_dynamic_timestep(omdg_ctx* ctx, double maxpath, double max_dt, int 
 /* Integrator->TimeStep and ElapsedTime (system.cpp:979) as the device has them. */
 int omdg_get_timestep(omdg_ctx* ctx, double* dt, double* elapsed);
 
+/* ------------------------------------------------------------------ output */
+
+/* DumpAtoms write modes (container.h:34-45). */
+#define OMDG_WM_APPEND 1
+#define OMDG_WM_VELOCITY 2
+#define OMDG_WM_FORCE 4
+#define OMDG_WM_DEADATOM 8
+#define OMDG_WM_BARE 16
+#define OMDG_WM_GHOST 32
+#define OMDG_WM_POTENTIAL 64
+#define OMDG_WM_VIRIAL 128
+#define OMDG_WM_TID 256
+#define OMDG_WM_GID 512
+#define OMDG_WM_NID 1024
+#define OMDG_WM_ZIP 2048
+
+/* AtomContainer::DumpAtoms (container.cpp:417-519), the Object-MD data file
+   of the context's atoms from device state, in caller (nid) order: unless
+   WM_BARE or WM_APPEND the header (Box, the caller's info lines as "#<line>",
+   Material, Fields), then per active atom (all with WM_DEADATOM) x y z fixed
+   with posprec digits and the mode's fields in scientific with valprec
+   (id = type, gid from the caller or 0, nid = caller index).  WM_ZIP (gzip)
+   is refused; there are no ghost atoms to include. */
+int omdg_dump_atoms(omdg_ctx* ctx, const char* path, int mode, int posprec, int valprec, const char* material,
+                    int ninfo, const char* const* info, const int* gid);
+/* SysMonitor (SysMonitor.h): appends the md.out lines of the steps completed
+   by the last omdg_step / omdg_sync with Step % every == 0 and Step != 0:
+   "Step ElapsedTime TimeStep Ek Ep E" with SysMonitor's formats, from the
+   device ledger; header != 0 truncates the file and writes the label line. */
+int omdg_monitor_append(omdg_ctx* ctx, const char* path, int every, int header);
+
 /* ------------------------------------------------------------ checkpoints */
 
 /*

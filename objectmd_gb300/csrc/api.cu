@@ -224,8 +224,8 @@ int omdg_create(omdg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaMalloc(&c->d_state, step_state_bytes());
     if (e == cudaSuccess) e = cudaMalloc(&c->d_mass, sizeof(double) * MAX_TYPES);
     c->ledger_cap = 1 << 16;
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_ledger, sizeof(double) * 4 * c->ledger_cap);
-    if (e == cudaSuccess) e = cudaMallocHost(&c->h_ledger, sizeof(double) * 4 * c->ledger_cap);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_ledger, sizeof(double) * LEDGER_W * c->ledger_cap);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_ledger, sizeof(double) * LEDGER_W * c->ledger_cap);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(unsigned) * 4, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_flags, 0, sizeof(int) * 8, c->stream);
     if (e != cudaSuccess) {
@@ -987,7 +987,7 @@ int omdg_compute_forces(omdg_ctx* c) {
     int cur = 0;
     if ((rc = step_state_read(c, nullptr, &cur, nullptr))) return rc;
     double row[4];
-    cudaMemcpy(row, c->d_ledger + 4 * (size_t)(cur % c->ledger_cap), sizeof(row), cudaMemcpyDeviceToHost);
+    cudaMemcpy(row, c->d_ledger + LEDGER_W * (size_t)(cur % c->ledger_cap), sizeof(row), cudaMemcpyDeviceToHost);
     c->last_kin = row[0];
     c->last_pot = row[1];
     c->last_vir = row[2];
@@ -1233,16 +1233,16 @@ int omdg_sync(omdg_ctx* c) {
     if (nrow > 0) {
         // the device ledger is a ring: rows older than `cap` steps were overwritten
         std::vector<double> ring(4 * (size_t)cap);
-        cudaMemcpy(ring.data(), c->d_ledger, sizeof(double) * 4 * (size_t)std::min(rows, cap),
+        cudaMemcpy(ring.data(), c->d_ledger, sizeof(double) * LEDGER_W * (size_t)std::min(rows, cap),
                    cudaMemcpyDeviceToHost);
         int first = rows > cap ? rows % cap : 0;
         for (int k = 0; k < nrow; k++) {
             int slot = (first + k) % cap;
-            for (int q = 0; q < 4; q++) c->h_ledger[4 * k + q] = ring[4 * slot + q];
+            for (int q = 0; q < LEDGER_W; q++) c->h_ledger[LEDGER_W * k + q] = ring[LEDGER_W * slot + q];
         }
-        c->last_kin = c->h_ledger[4 * (nrow - 1)];
-        c->last_pot = c->h_ledger[4 * (nrow - 1) + 1];
-        c->last_vir = c->h_ledger[4 * (nrow - 1) + 2];
+        c->last_kin = c->h_ledger[LEDGER_W * (nrow - 1)];
+        c->last_pot = c->h_ledger[LEDGER_W * (nrow - 1) + 1];
+        c->last_vir = c->h_ledger[LEDGER_W * (nrow - 1) + 2];
     }
     c->last_rows = nrow;
     c->last_launches = c->launches - c->launches_at_sync;
@@ -1425,8 +1425,8 @@ int omdg_ledger_history(omdg_ctx* c, double* kinetic, double* potential, int cap
     if (!c || !rows) return OMDG_EINVAL;
     int m = std::min(cap, c->last_rows);
     for (int k = 0; k < m; k++) {
-        if (kinetic) kinetic[k] = c->h_ledger[4 * k];
-        if (potential) potential[k] = c->h_ledger[4 * k + 1];
+        if (kinetic) kinetic[k] = c->h_ledger[LEDGER_W * k];
+        if (potential) potential[k] = c->h_ledger[LEDGER_W * k + 1];
     }
     *rows = m;
     return OMDG_OK;

@@ -190,9 +190,14 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const double* pa
         if (!(isfinite(kinetic) && isfinite(e))) atomicOr(p.status, ERR_NONFINITE);
         int row = st->row;
         int slot = row % p.ledger_cap;  // ring buffer between host reads
-        ledger[4 * slot + 0] = kinetic;
-        ledger[4 * slot + 1] = e;
-        ledger[4 * slot + 2] = 0.5 * w;
+        double* row_out = ledger + LEDGER_W * (size_t)slot;
+        row_out[0] = kinetic;
+        row_out[1] = e;
+        row_out[2] = 0.5 * w;
+        row_out[4] = (double)st->step;  // SysMonitor's Step, ElapsedTime and TimeStep of this step
+        row_out[5] = st->elapsed;
+        row_out[6] = st->dt;
+        row_out[7] = 0.0;
         double lam = 1.0;
         if (p.count_step && p.tau > 0.0 && st->step != 0) {
             // TempController::PostIntegration: T from the system kinetic energy
@@ -200,7 +205,7 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const double* pa
             double T = p.temp_factor * kinetic / count;
             if (T > 0.0) lam = sqrt(1. + st->dt / p.tau * (p.tset / T - 1.));
         }
-        ledger[4 * slot + 3] = lam;
+        row_out[3] = lam;
         if (p.need_vmax) st->sqrmaxv = vm;
         if (p.count_step) {
             st->lambda = lam;

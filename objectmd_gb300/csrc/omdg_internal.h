@@ -264,7 +264,8 @@ struct Context {
                                     // [4] blocks done in the current kick (reset by the last block)
     double* d_red = nullptr;        // block partials
     int red_cap = 0;
-    double* d_ledger = nullptr;     // per step: kinetic, potential, virial, lambda
+    double* d_ledger = nullptr;     // per step LEDGER_W doubles: kinetic, potential, virial, lambda,
+                                    // Step, ElapsedTime (both before the step's increment), TimeStep
     int ledger_cap = 0;
     double* h_ledger = nullptr;     // pinned copy
     double base_potential = 0;
@@ -341,6 +342,8 @@ int io_set_forces(Context* c, const double* f);
 int post_force_modifies(Context* c);  // ForceDamper / CoordClamp after the forces (integrate.cu)
 int io_set_flags(Context* c, const unsigned* flags, unsigned keep_mask);  // caller order; bits in keep_mask survive
 int io_get_flags(Context* c, unsigned* flags);
+
+constexpr int LEDGER_W = 8;  // doubles per ledger row
 
 // Atom group g as its flag bit (bits 8..15); -1: every atom.
 inline unsigned group_bits(int g) { return g < 0 ? ~0u : (1u << (8 + g)); }

@@ -148,6 +148,8 @@ SIGNATURES = {
     "omdg_add_range_limiter": [_vp, _i, _d],
     "omdg_set_dynamic_timestep": [_vp, _d, _d, _i],
     "omdg_get_timestep": [_vp, _P(_d), _P(_d)],
+    "omdg_dump_atoms": [_vp, _cp, _i, _i, _i, _cp, _i, _P(_cp), _P(_i)],
+    "omdg_monitor_append": [_vp, _cp, _i, _i],
     "omdg_checkpoint_write": [_cp, _cp, _P(SimVars), _i, _P(_cp), _P(_cp), _i, _P(ContainerDesc), _vp, _cp, _i],
     "omdg_checkpoint_info": [_cp, _P(_i), _P(_i), _P(_i), _cp, _i],
     "omdg_checkpoint_read": [_cp, _P(SimVars), _cp, _i, _P(ContainerDesc), _i, _vp, _cp, _i, _cp, _i],
@@ -547,6 +549,23 @@ class Context:
         self._check(self.lib.omdg_ledger(self.h, ctypes.byref(k), ctypes.byref(p), ctypes.byref(b), ctypes.byref(w)))
         return {"kinetic": k.value, "potential": p.value, "base_potential": b.value, "virial": w.value,
                 "energy": k.value + p.value - b.value}
+
+    # ---- output
+    WM = {"append": 1, "velocity": 2, "force": 4, "deadatom": 8, "bare": 16, "ghost": 32, "potential": 64,
+          "virial": 128, "tid": 256, "gid": 512, "nid": 1024}
+
+    def dump_atoms(self, path, mode, posprec=5, valprec=5, material="", info=(), gid=None):
+        """omdg_dump_atoms: the reference's data file (mode: WM_* bits or names)."""
+        if not isinstance(mode, int):
+            mode = sum(self.WM[m] for m in mode)
+        g = None if gid is None else np.ascontiguousarray(gid, dtype=np.int32)
+        lines = _strings(list(info))
+        self._check(self.lib.omdg_dump_atoms(self.h, path.encode(), int(mode), int(posprec), int(valprec),
+                                             material.encode(), len(info), lines, None if g is None else _ip(g)))
+
+    def monitor_append(self, path, every=1, header=False):
+        """omdg_monitor_append: SysMonitor's md.out lines of the last step call."""
+        self._check(self.lib.omdg_monitor_append(self.h, path.encode(), int(every), 1 if header else 0))
 
     # ---- modifies of the impact runs
     def set_groups(self, member):

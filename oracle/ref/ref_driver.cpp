@@ -32,6 +32,8 @@
  *   range       <border> RangeLimiter("-", border)
  *                        (with any of these: times.txt = Step TimeStep ElapsedTime
  *                        per step, active.txt = nid flag&FLAG_ACTIVE at the end)
+ *   dump        <file> <mode>  after the run, DumpAtoms(file, mode) (container.cpp:417-519)
+ *   monitor     <file> <every> SysMonitor(file) with monitor.every (SysMonitor.h)
  *   save        <file>   after the run, the reference's binary checkpoint
  *                        (MDSystemGrid::SaveSimulation, systemgrid.cpp:848-852)
  *   continue    <file>   resume from a binary checkpoint (CONTINUE_MODE,
@@ -57,6 +59,7 @@ using namespace omd;
 #include <modify/DynamicTimeStep.h>
 #include <modify/RangeLimiter.h>
 #include <detect/ThermoDetector.h>
+#include <detect/SysMonitor.h>
 #include <misc/TTM_Homogen_SCNA.h>
 
 #include <sys/time.h>
@@ -164,6 +167,7 @@ public:
             AddModify(new DynamicTimeStep(atof(get("dyndt", "0.1", 0).c_str()), atof(get("dyndt", "0.001", 1).c_str()),
                                           atoi(get("dyndt", "5", 2).c_str())));
         if (opt.count("range")) AddModify(new RangeLimiter("-", atof(get("range", "1000", 0).c_str())));
+        if (opt.count("monitor")) AddDetector(new SysMonitor(get("monitor", "md.out", 0)));
     }
 
     void SystemSetting() {}
@@ -227,6 +231,7 @@ public:
         }
         fclose(f);
         if (get("dump_nbr", "0") != "0") DumpNeighbours();
+        if (opt.count("dump")) DumpAtoms(get("dump", "dump.dat", 0), atoi(get("dump", "0", 1).c_str()));
         if (opt.count("save")) SaveSimulation(get("save", ""));
         if (timelog) {
             fclose(timelog);
@@ -308,7 +313,8 @@ int main(int argc, char** argv) {
     std::map<std::string, std::vector<std::string> > opt;
     for (int i = 2; i < argc;) {
         std::string key = argv[i++];
-        int nval = (key == "tcontrol") ? 2 : ((key == "ttm" || key == "dyndt") ? 3 : 1);
+        int nval = (key == "tcontrol" || key == "dump" || key == "monitor") ? 2
+                   : ((key == "ttm" || key == "dyndt") ? 3 : 1);
         for (int k = 0; k < nval && i < argc; k++) opt[key].push_back(argv[i++]);
     }
     /* Table mode: the reference TableReader itself (treader.cpp) evaluated at
@@ -344,6 +350,10 @@ int main(int argc, char** argv) {
     args.push_back("time.max");
     args.push_back("1e30");
     args.push_back("--silent");
+    if (opt.count("monitor")) {  // SysMonitor::ReadParameter (SysMonitor.h)
+        args.push_back("monitor.every");
+        args.push_back(opt["monitor"][1]);
+    }
     if (opt.count("damp")) {  // ForceDamper::ReadParameter (ForceDamper.h:24-27)
         args.push_back("damp.factor");
         args.push_back(opt["damp"][0]);

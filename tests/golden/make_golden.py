@@ -132,6 +132,24 @@ def checkpoint_case(tdir):
     print("wrote checkpoint_eam_al_500", raw.size, "bytes")
 
 
+def output_case(tdir):
+    """The reference's output path on EAM Al 500, 6 steps of 2 fs:
+    DumpAtoms (velocity, force, potential, id, nid) and SysMonitor's md.out
+    every 2 steps; a second run writes DumpAtoms (velocity, id, nid) and the
+    binary checkpoint of the same final state."""
+    f = os.path.join(GOLD, "eam_al_500.dat")
+    work = tempfile.mkdtemp(prefix="omdout_")
+    dump1, md, dump2, ck = (os.path.join(work, n) for n in ("dump1.dat", "md.out", "dump2.dat", "final.bin"))
+    oc.run_reference(f, "eam", "aluminum5000", steps=6, dt=0.002, table_dir=tdir, dump=(dump1, 2 | 4 | 64 | 256 | 1024),
+                     monitor=(md, 2))
+    oc.run_reference(f, "eam", "aluminum5000", steps=6, dt=0.002, table_dir=tdir, dump=(dump2, 2 | 256 | 1024),
+                     save=ck)
+    raw = lambda p: np.frombuffer(open(p, "rb").read(), dtype=np.uint8)  # noqa: E731
+    np.savez_compressed(os.path.join(GOLD, "output_eam_al_500.npz"), dump_full=raw(dump1), monitor=raw(md),
+                        dump_state=raw(dump2), checkpoint=raw(ck), dt=np.array(0.002), steps=np.array(6))
+    print("wrote output_eam_al_500")
+
+
 MODIFY_CASES = {  # the impact-run modifies on every atom of an EAM Al slab
     "damp_clamp": dict(damp=0.05, clamp="xyz"),
     "dyndt": dict(dyndt=(0.02, 0.004, 3)),
@@ -168,6 +186,9 @@ def main(only=None):
         return
     if only == "checkpoint":
         checkpoint_case(table_dir())
+        return
+    if only == "output":
+        output_case(table_dir())
         return
     if only == "modifies":
         modifies_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
@@ -250,6 +271,7 @@ def main(only=None):
     ttm_case(tdir, work)
     checkpoint_case(tdir)
     modifies_case(tdir, work)
+    output_case(tdir)
     print("done")
 
 

@@ -1,0 +1,109 @@
+"""The output path against the reference's own files
+(tests/golden/output_eam_al_500.npz, EAM Al 500, 6 steps of 2 fs):
+
+- DumpAtoms of a state loaded from the reference's checkpoint (positions,
+  velocities, id, nid: FP64 values taken over exactly) equals the reference's
+  DumpAtoms of that state line for line; the reference writes its storage
+  order, so lines are compared as a set.
+- DumpAtoms (velocity, force, potential, id, nid) and SysMonitor's md.out
+  after 6 steps run here: the same header and number formats; values within
+  the EAM NVE tolerances (positions 1e-5 A, the 5-decimal print; velocities
+  1e-4 of their scale; forces 1e-4 eV/A; energies 1e-6 relative).
+"""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLD, TABLES, load_case
+
+pytestmark = pytest.mark.gpu
+
+EAM_TABLE = os.path.join(TABLES, "eam.aluminum5000")
+INFO = ["$ PeriodicBoundary 7"]  # the Import header line the reference keeps
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(os.path.join(GOLD, "output_eam_al_500.npz"))
+
+
+def text(a):
+    return a.tobytes().decode()
+
+
+def split(doc):
+    lines = doc.splitlines()
+    head = [l for l in lines if l.startswith("#")]
+    body = [l for l in lines if not l.startswith("#")]
+    return head, body
+
+
+def test_dump_of_a_loaded_state_equals_the_reference(omdg_lib, golden, tmp_path):
+    ck = tmp_path / "final.bin"
+    ck.write_bytes(golden["checkpoint"].tobytes())
+    out = str(tmp_path / "dump.dat")
+    with omdg_lib.Context(0) as ctx:
+        ctx.load_simulation(str(ck))
+        ctx.dump_atoms(out, ("velocity", "tid", "nid"), posprec=5, valprec=5, material="aluminum", info=INFO)
+    mine = open(out).read()
+    ref = text(golden["dump_state"])
+    h1, b1 = split(mine)
+    h2, b2 = split(ref)
+    assert h1 == h2
+    assert sorted(b1) == sorted(b2)
+
+
+def fields(line):
+    return [float(t) for t in line.split()]
+
+
+def test_dump_and_monitor_after_steps(omdg_lib, golden, tmp_path):
+    from objectmd_gb300 import inputs
+
+    d = load_case("eam_al_500")
+    dump, md = str(tmp_path / "dump.dat"), str(tmp_path / "md.out")
+    with omdg_lib.Context(0) as ctx:
+        ctx.set_box(d["box_lo"], d["box_hi"], (True, True, True))
+        ctx.set_atoms(d["x0"], d["v0"], masses=[inputs.md_mass("aluminum")], znum=[13.0])
+        ctx.add_eam(EAM_TABLE)
+        ctx.set_neighbor(0.3, 1)
+        ctx.set_timestep(float(golden["dt"]))
+        ctx.step(int(golden["steps"]))
+        ctx.monitor_append(md, every=2, header=True)
+        ctx.dump_atoms(dump, ("velocity", "force", "potential", "tid", "nid"), material="aluminum", info=INFO)
+    h1, b1 = split(open(dump).read())
+    h2, b2 = split(text(golden["dump_full"]))
+    assert h1 == h2
+    # the reference's number formats: x y z fixed with 5 decimals, then
+    # scientific with 5 (velocity, force, potential), then the integer ids
+    fixed, sci, integer = re.compile(r"^-?\d+\.\d{5}$"), re.compile(r"^-?\d\.\d{5}e[+-]\d{2}$"), re.compile(r"^\d+$")
+    pattern = [fixed] * 3 + [sci] * 7 + [integer] * 2
+    assert len(b1) == len(b2)
+    ref = {int(fields(l)[-1]): l for l in b2}
+    for l in b1:
+        nid = int(fields(l)[-1])
+        r = ref[nid]
+        for tok, rtok, pat in zip(l.split(), r.split(), pattern):
+            assert pat.match(tok) and pat.match(rtok), (tok, rtok)
+        assert len(l.split()) == len(r.split()) == len(pattern)
+        a, b = np.array(fields(l)), np.array(fields(r))
+        assert np.abs(a[0:3] - b[0:3]).max() <= 1.1e-5
+        assert np.abs(a[3:6] - b[3:6]).max() <= 1e-4 * max(1.0, np.abs(b[3:6]).max())
+        assert np.abs(a[6:9] - b[6:9]).max() <= 1e-4
+        assert abs(a[9] - b[9]) <= 1e-5 * abs(b[9]) + 5e-5  # pot printed with 6 significant digits
+        assert a[10:] .tolist() == b[10:].tolist()
+    m1 = open(md).read().splitlines()
+    m2 = text(golden["monitor"]).splitlines()
+    assert m1[0] == m2[0] and len(m1) == len(m2)
+    energy = re.compile(r"^-?\d\.\d{10}E[+-]\d{2}$")
+    for l1, l2 in zip(m1[1:], m2[1:]):
+        t1, t2 = l1.split(), l2.split()
+        assert t1[:3] == t2[:3]  # Step, ElapsedTime, TimeStep: the same strings
+        assert all(energy.match(t) for t in t1[3:] + t2[3:])
+        ek, ep, e = (float(t) for t in t1[3:])
+        rek, rep, re_ = (float(t) for t in t2[3:])
+        assert abs(ek - rek) <= 1e-6 * abs(rek)
+        # Ep = P - P0 and E differ by the potential's 5e-8 relative tolerance (|P| ~ 1670 eV)
+        assert abs(ep - rep) <= 2e-4 and abs(e - re_) <= 2e-4

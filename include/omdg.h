@@ -354,6 +354,14 @@ int omdg_add_range_limiter(omdg_ctx* ctx, int group, double border);
    SqrMaxVelocity over active atoms (system.cpp:1075-1094); evaluated on the
    device between steps.  TimeStep starts at max (Init with no velocity). */
 int omdg_set_dynamic_timestep(omdg_ctx* ctx, double maxpath, double max_dt, int update);
+/* EnergySource, pulse mode (EnergySource.h:78-131): from ElapsedTime >= start
+   (its first call there only arms it) until start + width, each step scales
+   every active atom's velocity by sqrt(1 + 2 delta / (m v^2)), delta =
+   energy * dt / width (width at least dt), skipping v^2 < (1e-6 |v|max)^2.
+   start must be > 0 (start = 0 draws random velocities, SetKineticEnergy);
+   not with DynamicTimeStep (the reference refuses it) nor with the Berendsen
+   thermostat (its factor waits in the step state until the next kick). */
+int omdg_add_energy_source(omdg_ctx* ctx, double energy, double start, double width);
 /* Integrator->TimeStep and ElapsedTime (system.cpp:979) as the device has them. */
 int omdg_get_timestep(omdg_ctx* ctx, double* dt, double* elapsed);
 

@@ -848,6 +848,7 @@ static int capture_step(Context* c, GraphState& gs) {
     if (e != cudaSuccess) return check_cuda(c, e, "capture begin");
     long l0 = c->launches, l1 = 0, l2 = 0;
     int rc = (c->ttm && ttm_active(c)) ? ttm_pre(c) : OMDG_OK;  // PreIntegration (TTM_Homogen_SCNA.h:352)
+    if (!rc) rc = energy_source(c);                                 // PreIntegration (EnergySource.h:113)
     if (!rc) rc = integrate_kick_drift(c, 0);
     cudaGraph_t g = nullptr;
     cudaStreamCaptureStatus cst;
@@ -1082,9 +1083,24 @@ int omdg_add_range_limiter(omdg_ctx* c, int group, double border) {
     return OMDG_OK;
 }
 
+int omdg_add_energy_source(omdg_ctx* c, double energy, double start, double width) {
+    if (!c || !std::isfinite(energy) || !(start > 0) || !std::isfinite(width)) return OMDG_EINVAL;
+    if (c->dyn_update > 0) return set_error(c, OMDG_EINVAL, "EnergySource is incompatible with DynamicTimeStep");
+    if (c->thermo_tau > 0) return set_error(c, OMDG_EINVAL, "EnergySource with the Berendsen thermostat is not supported");
+    // EnergySource::CheckParameter (EnergySource.h:85-95): pulse mode
+    if (width < c->dt) width = c->dt;
+    c->src_on = true;
+    c->src_delta = energy * c->dt / width;
+    c->src_start = start;
+    c->src_width = width;
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
 int omdg_set_dynamic_timestep(omdg_ctx* c, double maxpath, double max_dt, int update) {
     if (!c || !(maxpath > 0) || !(max_dt > 0) || update < 1) return OMDG_EINVAL;
     if (c->ttm) return set_error(c, OMDG_EINVAL, "a dynamic time step cannot drive the TTM");
+    if (c->src_on) return set_error(c, OMDG_EINVAL, "DynamicTimeStep is incompatible with EnergySource");
     c->dyn_update = update;
     c->dyn_maxpath = maxpath;
     c->dyn_maxdt = max_dt;
@@ -1115,6 +1131,8 @@ int omdg_set_thermostat(omdg_ctx* c, double temperature, double tau) {
     if (!c) return OMDG_EINVAL;
     if (tau > 0.0 && c->ttm && ttm_active(c))
         return set_error(c, OMDG_EINVAL, "the Berendsen thermostat and the two-temperature model exclude each other");
+    if (tau > 0.0 && c->src_on)
+        return set_error(c, OMDG_EINVAL, "EnergySource with the Berendsen thermostat is not supported");
     c->thermo_T = temperature;
     c->thermo_tau = tau;
     invalidate_graph(c);
@@ -1181,6 +1199,7 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
     if (c->profiling) {
         for (int k = 0; k < nsteps; k++) {
             if (c->ttm && ttm_active(c) && (rc = ttm_pre(c))) return rc;
+            if ((rc = energy_source(c))) return rc;
             if ((rc = integrate_kick_drift(c, k))) return rc;
             if ((rc = eager_maybe_rebuild(c))) return rc;
             if ((rc = forces_compute(c))) return rc;

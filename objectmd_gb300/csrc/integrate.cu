@@ -32,6 +32,8 @@ struct StepState {
     double hdtm[MAX_TYPES];  // (dt/2) / m per type, refreshed with dt
     double elapsed;          // ElapsedTime (system.cpp:979)
     double sqrmaxv;          // SqrMaxVelocity of the last measurement (system.cpp:1075-1094)
+    int src_first;           // EnergySource: the first call inside the window only arms it
+    int src_scale;           // EnergySource: scale velocities at the next PreIntegration
 };
 
 struct IntParams {
@@ -141,6 +143,8 @@ struct FinParams {
     int dyn_apply;        // this measurement precedes a step's PreIntegration
     double dyn_maxpath, dyn_maxdt;
     double mass[MAX_TYPES];
+    int src_on;                 // EnergySource (EnergySource.h:103-133)
+    double src_start, src_stop;
 };
 
 // Ledger row, thermostat factor and step counter from the block partials
@@ -213,6 +217,14 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const double* pa
             st->step += 1;
             st->row = row + 1;
             if (st->rebuild_every > 0 && (st->step % st->rebuild_every) == 0) st->rebuild = 1;
+            if (p.src_on) {  // EnergySource::PreIntegration of the next step
+                int scale = 0;
+                if (st->elapsed >= p.src_start) {
+                    if (st->src_first) st->src_first = 0;  // firstcall: return
+                    else scale = st->elapsed < p.src_stop ? 1 : 0;
+                }
+                st->src_scale = scale;
+            }
         }
         if (p.dyn_update > 0 && p.dyn_apply && (st->step % p.dyn_update) == 0) {
             // DynamicTimeStep::PreIntegration of the next step
@@ -470,6 +482,35 @@ int post_force_modifies(Context* c) {
     return check_cuda(c, cudaGetLastError(), "force modifies");
 }
 
+// EnergySource pulse (EnergySource.h:113-131): every active atom with
+// v^2 >= (1e-6 |v|max)^2 gets v *= sqrt(1 + 2 delta / (v^2 m)).
+__global__ void k_energy_source(int n, double delta, const int* __restrict__ type, const double* __restrict__ mass,
+                                const unsigned* __restrict__ aflag, double* __restrict__ vx, double* __restrict__ vy,
+                                double* __restrict__ vz, const StepState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !st->src_scale) return;
+    if (aflag && !(aflag[i] & 1u)) return;
+    // the reference's expressions, without contraction into fma
+    const double vmax = __dmul_rn(sqrt(st->sqrmaxv), 1e-6);
+    const double small = __dmul_rn(vmax, vmax);
+    const double ux = vx[i], uy = vy[i], uz = vz[i];
+    const double c2 = __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz));
+    if (c2 < small) return;
+    const double chi = sqrt(__dadd_rn(1.0, __ddiv_rn(__ddiv_rn(__dmul_rn(2.0, delta), c2), mass[type[i]])));
+    vx[i] = __dmul_rn(ux, chi);
+    vy[i] = __dmul_rn(uy, chi);
+    vz[i] = __dmul_rn(uz, chi);
+}
+
+int energy_source(Context* c) {
+    if (!c->src_on || c->n == 0) return OMDG_OK;
+    k_energy_source<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->src_delta, c->type, c->d_mass,
+                                                                c->flags_used ? c->aflag : nullptr, c->vx, c->vy,
+                                                                c->vz, reinterpret_cast<StepState*>(c->d_state));
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "energy source");
+}
+
 // ------------------------------------------------------------------ host
 
 static IntParams int_params(Context* c) {
@@ -486,7 +527,7 @@ static IntParams int_params(Context* c) {
         p.range_lo[d] = c->box.lo[d] - c->range_border;
         p.range_hi[d] = c->box.hi[d] + c->range_border;
     }
-    p.need_vmax = c->dyn_update > 0 ? 1 : 0;
+    p.need_vmax = (c->dyn_update > 0 || c->src_on) ? 1 : 0;
     for (int d = 0; d < 3; d++) {
         p.org[d] = c->box.org[d];
         p.P[d] = c->box.P[d];
@@ -533,6 +574,9 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
     f.dyn_maxpath = c->dyn_maxpath;
     f.dyn_maxdt = c->dyn_maxdt;
     for (int t = 0; t < MAX_TYPES; t++) f.mass[t] = c->mass[t];
+    f.src_on = c->src_on ? 1 : 0;
+    f.src_start = c->src_start;
+    f.src_stop = c->src_start + c->src_width;
     if (c->thermo_count_ghosts && count_step && c->thermo_tau > 0.0) {
         // TempController::GetSystemTemperature divides by GetTotalAtom(), which
         // on MDSystemGrid is GetNAtom(): owners plus their periodic ghost images
@@ -652,6 +696,8 @@ int step_state_init(Context* c) {
     set_dt(h, c, c->dyn_update > 0 ? c->dyn_maxdt : c->dt);  // DynamicTimeStep::Init with no velocity yet
     h.elapsed = 0.0;
     h.sqrmaxv = 0.0;
+    h.src_first = 1;
+    h.src_scale = 0;
     cudaError_t e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return check_cuda(c, e, "step state");

@@ -251,6 +251,8 @@ struct Context {
     bool range_on = false;          // RangeLimiter
     int range_group = -1;
     double range_border = 0;
+    bool src_on = false;            // EnergySource pulse: delta per step, window [start, start + width)
+    double src_delta = 0, src_start = 0, src_width = 0;
     int dyn_update = 0;             // DynamicTimeStep (update period; 0: off)
     double dyn_maxpath = 0, dyn_maxdt = 0;
     bool first_measure = false;     // FirstRun's measurement (DynamicTimeStep at Step 0)
@@ -339,6 +341,7 @@ int step_state_graph_rebuilds(Context* c, int* nrebuild);
 int io_get_state(Context* c, double* x, double* v, double* f, double* pot, double* vir);
 int io_set_state(Context* c, const double* x, const double* v);
 int io_set_forces(Context* c, const double* f);
+int energy_source(Context* c);  // EnergySource's PreIntegration scaling (integrate.cu)
 int post_force_modifies(Context* c);  // ForceDamper / CoordClamp after the forces (integrate.cu)
 int io_set_flags(Context* c, const unsigned* flags, unsigned keep_mask);  // caller order; bits in keep_mask survive
 int io_get_flags(Context* c, unsigned* flags);

@@ -148,6 +148,7 @@ SIGNATURES = {
     "omdg_add_range_limiter": [_vp, _i, _d],
     "omdg_set_dynamic_timestep": [_vp, _d, _d, _i],
     "omdg_get_timestep": [_vp, _P(_d), _P(_d)],
+    "omdg_add_energy_source": [_vp, _d, _d, _d],
     "omdg_dump_atoms": [_vp, _cp, _i, _i, _i, _cp, _i, _P(_cp), _P(_i)],
     "omdg_monitor_append": [_vp, _cp, _i, _i],
     "omdg_checkpoint_write": [_cp, _cp, _P(SimVars), _i, _P(_cp), _P(_cp), _i, _P(ContainerDesc), _vp, _cp, _i],
@@ -593,6 +594,9 @@ class Context:
 
     def set_dynamic_timestep(self, maxpath, max_dt=0.001, update=5):
         self._check(self.lib.omdg_set_dynamic_timestep(self.h, float(maxpath), float(max_dt), int(update)))
+
+    def add_energy_source(self, energy, start, width):
+        self._check(self.lib.omdg_add_energy_source(self.h, float(energy), float(start), float(width)))
 
     def get_timestep(self):
         dt, el = _d(), _d()

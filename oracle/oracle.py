@@ -291,7 +291,7 @@ def berendsen_factor(dt, tau, tset, tnow):
 def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh=0, dump_nbr=False,
                   pair2=None, tcontrol=None, table_dir=None, swfix=False, time_only=False, timeout=3600, ttm=None,
                   save=None, cont=None, damp=None, clamp=None, dyndt=None, range_border=None, dump=None,
-                  monitor=None):
+                  monitor=None, source=None):
     """Run the reference's own code (oracle/_ref/ref_driver) on an Import file.
 
     Returns a dict with 'atoms' (nid, tid, x, v, f, potential, virial sorted
@@ -321,6 +321,8 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
         args += ["dyndt", repr(float(dyndt[0])), repr(float(dyndt[1])), str(int(dyndt[2]))]
     if range_border is not None:
         args += ["range", repr(float(range_border))]
+    if source is not None:  # (energy per atom, start, width): EnergySource pulse
+        args += ["source", repr(float(source[0])), repr(float(source[1])), repr(float(source[2]))]
     if dump:  # (file, write mode): DumpAtoms after the run
         args += ["dump", os.path.abspath(dump[0]), str(int(dump[1]))]
     if monitor:  # (file, every): SysMonitor

@@ -32,6 +32,7 @@
  *   range       <border> RangeLimiter("-", border)
  *                        (with any of these: times.txt = Step TimeStep ElapsedTime
  *                        per step, active.txt = nid flag&FLAG_ACTIVE at the end)
+ *   source      <energy> <start> <width>  EnergySource, pulse mode (source.* parameters)
  *   dump        <file> <mode>  after the run, DumpAtoms(file, mode) (container.cpp:417-519)
  *   monitor     <file> <every> SysMonitor(file) with monitor.every (SysMonitor.h)
  *   save        <file>   after the run, the reference's binary checkpoint
@@ -58,6 +59,7 @@ using namespace omd;
 #include <modify/CoordClamp.h>
 #include <modify/DynamicTimeStep.h>
 #include <modify/RangeLimiter.h>
+#include <modify/EnergySource.h>
 #include <detect/ThermoDetector.h>
 #include <detect/SysMonitor.h>
 #include <misc/TTM_Homogen_SCNA.h>
@@ -168,6 +170,7 @@ public:
                                           atoi(get("dyndt", "5", 2).c_str())));
         if (opt.count("range")) AddModify(new RangeLimiter("-", atof(get("range", "1000", 0).c_str())));
         if (opt.count("monitor")) AddDetector(new SysMonitor(get("monitor", "md.out", 0)));
+        if (opt.count("source")) AddModify(new EnergySource);
     }
 
     void SystemSetting() {}
@@ -190,7 +193,8 @@ public:
             if (ledger)
                 fprintf(ledger, "%d %.17g %.17g %.17g\n", 0, Kinetic, BasePotential, 0.0);
             if (opt.count("ttm")) ttmlog = fopen((outdir + "/ttm.txt").c_str(), "w");
-            if (opt.count("damp") || opt.count("clamp") || opt.count("dyndt") || opt.count("range"))
+            if (opt.count("damp") || opt.count("clamp") || opt.count("dyndt") || opt.count("range") ||
+                opt.count("source"))
                 timelog = fopen((outdir + "/times.txt").c_str(), "w");
         }
         t_begin = wall_now();
@@ -314,7 +318,7 @@ int main(int argc, char** argv) {
     for (int i = 2; i < argc;) {
         std::string key = argv[i++];
         int nval = (key == "tcontrol" || key == "dump" || key == "monitor") ? 2
-                   : ((key == "ttm" || key == "dyndt") ? 3 : 1);
+                   : ((key == "ttm" || key == "dyndt" || key == "source") ? 3 : 1);
         for (int k = 0; k < nval && i < argc; k++) opt[key].push_back(argv[i++]);
     }
     /* Table mode: the reference TableReader itself (treader.cpp) evaluated at
@@ -350,6 +354,16 @@ int main(int argc, char** argv) {
     args.push_back("time.max");
     args.push_back("1e30");
     args.push_back("--silent");
+    if (opt.count("source")) {  // EnergySource::ReadParameter (EnergySource.h:78-83)
+        args.push_back("source.energy");
+        args.push_back(opt["source"][0]);
+        args.push_back("source.start");
+        args.push_back(opt["source"][1]);
+        args.push_back("source.width");
+        args.push_back(opt["source"][2]);
+        args.push_back("source.mode");
+        args.push_back("pulse");
+    }
     if (opt.count("monitor")) {  // SysMonitor::ReadParameter (SysMonitor.h)
         args.push_back("monitor.every");
         args.push_back(opt["monitor"][1]);

@@ -154,6 +154,7 @@ MODIFY_CASES = {  # the impact-run modifies on every atom of an EAM Al slab
     "damp_clamp": dict(damp=0.05, clamp="xyz"),
     "dyndt": dict(dyndt=(0.02, 0.004, 3)),
     "range": dict(range_border=1.0),
+    "source": dict(source=(0.05, 0.01, 0.02)),
 }
 
 

@@ -9,6 +9,8 @@ at 60 A/ps, 30 steps of 2 fs, every atom targeted.
   30 steps within 1e-6 relative (the time step follows the fastest atom).
 - RangeLimiter(1.0): the escaping atom is deactivated at the same step and
   frozen; the same atoms stay active.
+- EnergySource(0.05, start 0.01, width 0.02): the pulse rescales the same
+  steps' velocities.
 
 Positions within 1e-6 A, velocities within 1e-4 of their scale, ledger
 kinetic 1e-6 and potential 5e-8 relative (the EAM NVE tolerances).
@@ -109,3 +111,13 @@ def test_groups_select_the_atoms_a_modify_acts_on(omdg_lib, slab):
     others = np.arange(n) != top
     assert st["v"][top, 1] == 0 and st["v"][top, 2] == 0 and st["v"][top, 0] != 0
     assert (st["v"][others, 1:] != 0).any()
+
+
+def test_energy_source_pulse(omdg_lib, slab):
+    """EnergySource(0.05 eV per atom, start 0.01 ps, width 0.02 ps): its first
+    call at Step 5 only arms it, then Steps 6..14 scale the velocities."""
+    d = slab[-1]
+    st, kin, pot, _, _, _ = run(omdg_lib, slab, lambda c: c.add_energy_source(0.05, 0.01, 0.02))
+    check(st, kin, pot, d, "source")
+    ref = d["source_ledger"][1:, 1]
+    assert ref[6] > ref[5] + 1.0  # the first scaled step

@@ -104,39 +104,53 @@ __global__ void __launch_bounds__(512) k_pair32(PairParams p, const PosPack* __r
 }
 
 // FP64 end to end: dx = x_i - (x_j + s), r = sqrt(r2), TableReader in FP64.
-__global__ void __launch_bounds__(256) k_pair64(PairParams p, const double* __restrict__ x,
+// PAIR64_LANES lanes per atom take every PAIR64_LANES-th row entry, and the
+// lanes' FP64 sums meet in a fixed xor tree, so the FP64 work of a small box
+// spreads over the whole chip (one thread per atom left most SMs idle).
+constexpr int PAIR64_LANES = 32;
+
+__global__ void __launch_bounds__(128) k_pair64(PairParams p, const double* __restrict__ x,
                                                 const double* __restrict__ y, const double* __restrict__ z,
                                                 const int* __restrict__ type, const unsigned* __restrict__ nbr,
                                                 const int* __restrict__ nnb, double* __restrict__ f64,
                                                 float* __restrict__ pe, float* __restrict__ vir, unsigned* status) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    int ti = type[i];
-    double xi = x[i], yi = y[i], zi = z[i];
+    const int lane = threadIdx.x & (PAIR64_LANES - 1);
+    const int i = blockIdx.x * (blockDim.x / PAIR64_LANES) + threadIdx.x / PAIR64_LANES;
+    if (i >= p.n) return;  // whole warps leave together
+    const int ti = type[i];
+    const double xi = x[i], yi = y[i], zi = z[i];
     double ax = 0, ay = 0, az = 0, ae = 0, av = 0;
-    bool any = p.all_types || ti == p.ta || ti == p.tb;
-    int m = any ? nnb[i] : 0;
-    for (int s = 0; s < m; s++) {
-        unsigned e = __ldg(&nbr[nbr_at(i, s, p.hshift, p.maxnb)]);
-        int j = nbr_index(e);
+    const bool any = p.all_types || ti == p.ta || ti == p.tb;
+    const int m = any ? nnb[i] : 0;
+    for (int s = lane; s < m; s += PAIR64_LANES) {
+        const unsigned e = __ldg(&nbr[nbr_at(i, s, p.hshift, p.maxnb)]);
+        const int j = nbr_index(e);
         if (!p.all_types && !types_match(ti, type[j], p.ta, p.tb)) continue;
-        int sx = nbr_sx(e), sy = nbr_sy(e), sz = nbr_sz(e);
-        double gx = __dadd_rn(x[j], sx == 0 ? 0.0 : (sx > 0 ? p.L64[0] : -p.L64[0]));
-        double gy = __dadd_rn(y[j], sy == 0 ? 0.0 : (sy > 0 ? p.L64[1] : -p.L64[1]));
-        double gz = __dadd_rn(z[j], sz == 0 ? 0.0 : (sz > 0 ? p.L64[2] : -p.L64[2]));
-        double dx = __dsub_rn(xi, gx), dy = __dsub_rn(yi, gy), dz = __dsub_rn(zi, gz);
-        double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-        double r = __dsqrt_rn(r2);
+        const int sx = nbr_sx(e), sy = nbr_sy(e), sz = nbr_sz(e);
+        const double gx = __dadd_rn(x[j], sx == 0 ? 0.0 : (sx > 0 ? p.L64[0] : -p.L64[0]));
+        const double gy = __dadd_rn(y[j], sy == 0 ? 0.0 : (sy > 0 ? p.L64[1] : -p.L64[1]));
+        const double gz = __dadd_rn(z[j], sz == 0 ? 0.0 : (sz > 0 ? p.L64[2] : -p.L64[2]));
+        const double dx = __dsub_rn(xi, gx), dy = __dsub_rn(yi, gy), dz = __dsub_rn(zi, gz);
+        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        const double r = __dsqrt_rn(r2);
         if (!(r < p.rc64)) continue;
         double ph, dph;
         tab_read64(p.phi, r, ph, dph, status);
-        double fr = __ddiv_rn(-dph, r);
+        const double fr = __ddiv_rn(-dph, r);
         ax = __dadd_rn(ax, __dmul_rn(dx, fr));
         ay = __dadd_rn(ay, __dmul_rn(dy, fr));
         az = __dadd_rn(az, __dmul_rn(dz, fr));
         ae = __dadd_rn(ae, __dmul_rn(0.5, ph));
         av = __dadd_rn(av, __dmul_rn(fr, r2));
     }
+    for (int o = PAIR64_LANES / 2; o > 0; o >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, o);
+        ay += __shfl_xor_sync(0xffffffffu, ay, o);
+        az += __shfl_xor_sync(0xffffffffu, az, o);
+        ae += __shfl_xor_sync(0xffffffffu, ae, o);
+        av += __shfl_xor_sync(0xffffffffu, av, o);
+    }
+    if (lane != 0) return;
     if (p.first) {
         f64[3 * (size_t)i + 0] = ax;
         f64[3 * (size_t)i + 1] = ay;
@@ -180,7 +194,7 @@ int pair_launch(Context* c, Potential& pot, bool first) {
     int block = c->pair_block;
     if (pot.fp64) {
         prof_begin(c, "pair64");
-        k_pair64<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->x, c->y, c->z, c->type,
+        k_pair64<<<grid_for(c->n, 128 / PAIR64_LANES), 128, 0, c->stream>>>(p, c->x, c->y, c->z, c->type,
                                                               reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
                                                               c->f64, c->pe, c->vir, c->d_status);
     } else {

@@ -21,6 +21,8 @@ int step_state_read(Context* c, long long* step, int* row, int* rebuild);
 int step_state_resume(Context* c, long long step, double elapsed);
 int step_state_set_dt(Context* c);
 int step_state_times(Context* c, double* dt, double* elapsed);
+int step_state_fetch(Context* c, unsigned* status, long long* step, int* row, double* elapsed);
+int step_state_rewind(Context* c);
 int step_clear_rebuild(Context* c);
 int launch_set_rebuild_cond(Context* c, cudaGraphConditionalHandle h);
 int threebody_prepare(Context* c);
@@ -36,11 +38,18 @@ int check_cuda(Context* c, cudaError_t e, const char* what) {
                      std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+static int status_error(Context* c, unsigned st);
+
 int check_status(Context* c) {
     unsigned st = 0;
     cudaError_t e = cudaMemcpyAsync(&st, c->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return check_cuda(c, e, "status read");
+    return status_error(c, st);
+}
+
+// Maps (and clears) a non-zero device status word.
+static int status_error(Context* c, unsigned st) {
     if (!st) return OMDG_OK;
     unsigned zero = 0;
     cudaMemcpyAsync(c->d_status, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, c->stream);
@@ -226,6 +235,7 @@ int omdg_create(omdg_ctx** out, int device) {
     c->ledger_cap = 1 << 16;
     if (e == cudaSuccess) e = cudaMalloc(&c->d_ledger, sizeof(double) * LEDGER_W * c->ledger_cap);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_ledger, sizeof(double) * LEDGER_W * c->ledger_cap);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_sync, 16 + step_state_bytes());
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(unsigned) * 4, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_flags, 0, sizeof(int) * 8, c->stream);
     if (e != cudaSuccess) {
@@ -266,6 +276,7 @@ int omdg_destroy(omdg_ctx* c) {
     cudaFree(c->d_mass);
     cudaFree(c->d_ledger);
     cudaFreeHost(c->h_ledger);
+    cudaFreeHost(c->h_sync);
     for (auto& p : c->pots) {
         for (int k = 0; k < 3; k++) {
             cudaFree(p.d_coef[k]);
@@ -1226,10 +1237,13 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
 int omdg_sync(omdg_ctx* c) {
     if (!c) return OMDG_EINVAL;
     cudaSetDevice(c->device);
-    cudaError_t e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return check_cuda(c, e, "step");
-    int rc;
-    if ((rc = check_status(c))) {
+    unsigned status = 0;
+    long long step = 0;
+    int rows = 0;
+    double elapsed = 0.0;
+    int rc = step_state_fetch(c, &status, &step, &rows, &elapsed);  // waits for the queued steps
+    if (rc) return rc;
+    if ((rc = status_error(c, status))) {
         if (rc == OMDG_ESTATE) {
             // a neighbour row overflowed during the run: grow for the next call
             int m = (int)(1.25 * c->maxnb) + 16;
@@ -1242,23 +1256,27 @@ int omdg_sync(omdg_ctx* c) {
         return rc;
     }
     if (c->async_steps == 0) return OMDG_OK;
-    long long step;
-    int rows;
-    if ((rc = step_state_read(c, &step, &rows, nullptr))) return rc;
     c->step = step;
-    if ((rc = step_state_times(c, nullptr, &c->elapsed))) return rc;
-    int cap = c->ledger_cap;
-    int nrow = std::min(rows, cap);
+    c->elapsed = elapsed;
+    const int cap = c->ledger_cap;
+    const int nrow = std::min(rows, cap);
     if (nrow > 0) {
-        // the device ledger is a ring: rows older than `cap` steps were overwritten
-        std::vector<double> ring(4 * (size_t)cap);
-        cudaMemcpy(ring.data(), c->d_ledger, sizeof(double) * LEDGER_W * (size_t)std::min(rows, cap),
-                   cudaMemcpyDeviceToHost);
-        int first = rows > cap ? rows % cap : 0;
-        for (int k = 0; k < nrow; k++) {
-            int slot = (first + k) % cap;
-            for (int q = 0; q < LEDGER_W; q++) c->h_ledger[LEDGER_W * k + q] = ring[LEDGER_W * slot + q];
+        // the device ledger is a ring: rows older than `cap` steps were
+        // overwritten; the rest come back in order into the pinned copy
+        const size_t w = sizeof(double) * LEDGER_W;
+        cudaError_t e;
+        if (rows <= cap) {
+            e = cudaMemcpyAsync(c->h_ledger, c->d_ledger, w * nrow, cudaMemcpyDeviceToHost, c->stream);
+        } else {
+            const int first = rows % cap;
+            e = cudaMemcpyAsync(c->h_ledger, c->d_ledger + (size_t)LEDGER_W * first, w * (cap - first),
+                                cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(c->h_ledger + (size_t)LEDGER_W * (cap - first), c->d_ledger, w * first,
+                                    cudaMemcpyDeviceToHost, c->stream);
         }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return check_cuda(c, e, "ledger read-back");
         c->last_kin = c->h_ledger[LEDGER_W * (nrow - 1)];
         c->last_pot = c->h_ledger[LEDGER_W * (nrow - 1) + 1];
         c->last_vir = c->h_ledger[LEDGER_W * (nrow - 1) + 2];
@@ -1266,7 +1284,7 @@ int omdg_sync(omdg_ctx* c) {
     c->last_rows = nrow;
     c->last_launches = c->launches - c->launches_at_sync;
     c->async_steps = 0;
-    return step_state_reset(c, 1, c->rebuild_every);
+    return step_state_rewind(c);
 }
 
 int omdg_step(omdg_ctx* c, int nsteps) {

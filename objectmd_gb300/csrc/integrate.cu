@@ -665,6 +665,35 @@ int step_state_times(Context* c, double* dt, double* elapsed) {
     return OMDG_OK;
 }
 
+// One round trip after the queued steps: the status word and the step state
+// into the pinned staging block, then one stream synchronisation.
+int step_state_fetch(Context* c, unsigned* status, long long* step, int* row, double* elapsed) {
+    unsigned char* h = static_cast<unsigned char*>(c->h_sync);
+    cudaError_t e = cudaMemcpyAsync(h, c->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h + 16, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "step");
+    const StepState* st = reinterpret_cast<const StepState*>(h + 16);
+    *status = *reinterpret_cast<const unsigned*>(h);
+    *step = st->step;
+    *row = st->row;
+    *elapsed = st->elapsed;
+    return OMDG_OK;
+}
+
+__global__ void k_rewind(StepState* st, int rebuild_every) {
+    st->row = 0;
+    st->rebuild_every = rebuild_every;
+}
+
+// Ledger rows restart at 0 for the next omdg_step call (stream ordered, no wait).
+int step_state_rewind(Context* c) {
+    k_rewind<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state), c->rebuild_every);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "step state");
+}
+
 int step_state_graph_rebuilds(Context* c, int* nrebuild) {
     StepState h;
     cudaError_t e = cudaMemcpyAsync(&h, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);

@@ -270,6 +270,7 @@ struct Context {
                                     // Step, ElapsedTime (both before the step's increment), TimeStep
     int ledger_cap = 0;
     double* h_ledger = nullptr;     // pinned copy
+    void* h_sync = nullptr;         // pinned staging of the status word and the step state
     double base_potential = 0;
     double last_kin = 0, last_pot = 0, last_vir = 0;
     double elapsed = 0;                 // ElapsedTime: the steps' dt summed in order (system.cpp:979)

@@ -62,8 +62,8 @@ WORKLOADS = {
                        ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
     "impact_256": dict(kind="impact", desc="impact ensemble: 256 Si diamond slabs of 1,000-16,000 atoms (log-uniform, "
                        "1.30M atoms), periodic x/y, free surface, 300 K, one Ar at 10-500 eV each; Tersoff + ZBL Ar-Si "
-                       "(rc 3.0 A), skin 1.0 A, dt 0.5 fs; all replicas in one context", ncell=0, a=5.431, sigma=0.03,
-                       temp=300.0, dt=0.0005, seeds=(6, 6)),
+                       "(rc 3.0 A), skin 0.5 A, dt 0.5 fs; all replicas in one context", ncell=0, a=5.431, sigma=0.03,
+                       temp=300.0, dt=0.0005, seeds=(6, 6), skin=0.5),
     "lj_ar_4000": dict(kind="lj", desc="LJ Ar FCC 10^3 = 4000 atoms, FP64, rc 2.5 sigma, skin 0.3, 100 K, dt 1 fs",
                        ncell=10, a=5.26, sigma=0.0, temp=100.0, dt=0.001, seeds=(1, 1)),
 }
@@ -202,7 +202,7 @@ def make_context(w, x, v, lo, hi, device=0, tune=True):
         ctx.set_atoms(x, v, types=e["types"], masses=e["masses"], znum=e["znum"])
         ctx.add_tersoff(os.path.join(SI_DIR, "tersoff.silicon27"))
         ctx.add_zbl(1, 0, 3.0, 0.5)
-        ctx.set_neighbor(skin=1.0, rebuild_every=0)
+        ctx.set_neighbor(skin=w.get("skin", 1.0), rebuild_every=0)
         ctx.set_timestep(w["dt"])
         ctx.set_first_step_mode(True)
         if tune:
@@ -221,7 +221,7 @@ def make_context(w, x, v, lo, hi, device=0, tune=True):
         ctx.add_nn(NN_MODEL, os.path.join(SI_DIR, "tersoff.silicon27"))
     else:
         ctx.add_sw(os.path.join(SI_DIR, "sw.silicon"))
-    ctx.set_neighbor(skin=0.3, rebuild_every=0)
+    ctx.set_neighbor(skin=w.get("skin", 0.3), rebuild_every=0)
     ctx.set_timestep(w["dt"])
     ctx.set_first_step_mode(True)
     if tune:
@@ -247,6 +247,9 @@ def run_gpu(args):
         dist.init_process_group("nccl", init_method="env://")
     w, x, v, lo, hi = make_workload(args.workload, args.ncell)
     desc = w["desc"] if not args.ncell else "%s (ncell %d)" % (w["desc"], args.ncell)
+    if args.skin is not None:
+        w["skin"] = args.skin
+        desc += " (skin %g A)" % args.skin
     n = len(x)
     ctx = make_context(w, x, v, lo, hi, device=device, tune=not args.no_tune)
     for kv in args.launch:
@@ -573,6 +576,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--skin", type=float, default=None,
+                    help="Verlet skin in A instead of the workload's (omdg_set_neighbor)")
     ap.add_argument("--launch", action="append", default=[], metavar="KEY=VALUE",
                     help="set a launch shape after tuning (omdg_set_launch), e.g. build_lanes=1")
     ap.add_argument("--eager", action="store_true",

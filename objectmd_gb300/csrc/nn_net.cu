@@ -460,7 +460,9 @@ cudaError_t nn_mlp_launch(const NNDevNet& net, const float* gt, int rows, float*
     cudaError_t e = cudaFuncSetAttribute(k_nn_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int tiles = (rows + MLP_ROWS - 1) / MLP_ROWS;
-    const int grid = std::min(tiles, 2 * std::max(1, num_sms));
+    // 4 CTAs per SM: about 51 KB of shared memory and 128 of the SM's 512
+    // TMEM columns each, so the allocations never wait; four MMA chains overlap
+    const int grid = std::min(tiles, 4 * std::max(1, num_sms));
     k_nn_mlp<<<grid, MLP_ROWS, smem, s>>>(net.img, net.vec, gt, rows, E, u, status);
     return cudaGetLastError();
 }

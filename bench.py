@@ -31,6 +31,7 @@ import multiprocessing as mp
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -117,7 +118,9 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        # the samples go to a temporary file (OMDG_CLOCKS_DIR to keep them elsewhere)
+        out = os.environ.get("OMDG_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out, "clocks_bench_%d.csv" % os.getpid())
 
     def start(self):
         try:

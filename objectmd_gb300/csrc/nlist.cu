@@ -247,10 +247,16 @@ struct AtomArrays {
     int extra_n;
 };
 
-__global__ void k_permute_gather(int n, const int* __restrict__ perm, AtomArrays a, AtomArrays st) {
+// Also writes the sorted atoms' cells and the caller-to-sorted map (the new
+// position k of caller atom id[o]).
+__global__ void k_permute_gather(int n, const int* __restrict__ perm, AtomArrays a, AtomArrays st,
+                                 const int* __restrict__ cell_old, int* __restrict__ cell_new,
+                                 int* __restrict__ inv) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int o = perm[k];
+    cell_new[k] = cell_old[o];
+    inv[a.id[o]] = k;
     st.x[k] = a.x[o];
     st.y[k] = a.y[o];
     st.z[k] = a.z[o];
@@ -286,17 +292,8 @@ __global__ void k_zero_ints(int m, int* __restrict__ a, int* __restrict__ b) {
     }
 }
 
-__global__ void k_inverse(int n, const int* __restrict__ id, int* __restrict__ inv) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) inv[id[k]] = k;
-}
 
 // Cell of each sorted atom (cell[] is indexed by the previous order).
-__global__ void k_sorted_cell(int n, const int* __restrict__ perm, const int* __restrict__ cell_old,
-                              int* __restrict__ cell_new) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) cell_new[k] = cell_old[perm[k]];
-}
 
 // Replica mode: every replica has its own periodic lengths and cell grid,
 // and its cells occupy the global cell range [cell_base, cell_base + cells).
@@ -1008,12 +1005,9 @@ int nlist_build(Context* c) {
                    c->stage_d + 4 * (size_t)c->cap, c->stage_d + 5 * (size_t)c->cap, c->stage_i,
                    c->stage_i + c->cap, reinterpret_cast<unsigned*>(c->stage_i + 2 * (size_t)c->cap),
                    c->stage_extra, c->extra_n};
-    k_permute_gather<<<grid_for(n, 256), 256, 0, s>>>(n, c->perm, cur, stg);
-    k_permute_copyback<<<grid_for(n, 256), 256, 0, s>>>(n, stg, cur);
-    c->launches += 2;
     int* cell_sorted = c->cell_sorted;
-    k_sorted_cell<<<grid_for(n, 256), 256, 0, s>>>(n, c->perm, c->cell, cell_sorted);
-    k_inverse<<<grid_for(n, 256), 256, 0, s>>>(n, c->id, c->inv);
+    k_permute_gather<<<grid_for(n, 256), 256, 0, s>>>(n, c->perm, cur, stg, c->cell, cell_sorted, c->inv);
+    k_permute_copyback<<<grid_for(n, 256), 256, 0, s>>>(n, stg, cur);
     c->launches += 2;
     prof_end(c);
     prof_begin(c, "pack");

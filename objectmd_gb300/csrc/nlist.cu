@@ -187,16 +187,45 @@ __global__ void k_scatter(int n, const int* __restrict__ cell, const int* __rest
 // the final order (and every later floating-point sum) deterministic.
 constexpr int CELL_SORT_MAX = 1024;
 
-// One warp per cell: for cells of up to 32 atoms each lane holds one atom
-// index and its rank (how many of the cell's indices are smaller) is counted
-// with shuffles; the lanes then write in place.  Larger cells fall back to
-// lane 0's insertion sort (bounded as in k_cell_sort).
-__global__ void k_cell_sort_warp(int m, const int* __restrict__ start, int* __restrict__ perm) {
+// Cells of up to CELL_SORT_SMALL atoms, one thread each: the indices sort in
+// registers by an odd-even transposition network (fully unrolled).
+constexpr int CELL_SORT_SMALL = 8;
+
+__global__ void k_cell_sort_small(int m, const int* __restrict__ start, int* __restrict__ perm) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m) return;
+    const int b = start[c], k = start[c + 1] - b;
+    if (k <= 1 || k > CELL_SORT_SMALL) return;
+    int v[CELL_SORT_SMALL];
+#pragma unroll
+    for (int q = 0; q < CELL_SORT_SMALL; q++) v[q] = q < k ? perm[b + q] : INT_MAX;
+#pragma unroll
+    for (int r = 0; r < CELL_SORT_SMALL; r++) {
+#pragma unroll
+        for (int q = r & 1; q + 1 < CELL_SORT_SMALL; q += 2) {
+            const int lo = min(v[q], v[q + 1]), hi = max(v[q], v[q + 1]);
+            v[q] = lo;
+            v[q + 1] = hi;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < CELL_SORT_SMALL; q++)
+        if (q < k) perm[b + q] = v[q];
+}
+
+// Larger cells, one warp each (k_cell_sort_small takes the cells of at most
+// `skip` atoms when it runs): for cells of
+// up to 32 atoms each lane holds one atom index and its rank (how many of the
+// cell's indices are smaller) is counted with shuffles; the lanes then write
+// in place.  Cells of more than 32 atoms take lane 0's insertion sort; a
+// pathological cell beyond CELL_SORT_MAX is left unsorted (its order is then
+// not reproducible) rather than sorted in O(k^2).
+__global__ void k_cell_sort_warp(int m, const int* __restrict__ start, int* __restrict__ perm, int skip) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += warps) {
         const int b = start[c], k = start[c + 1] - b;
-        if (k <= 1) continue;
+        if (k <= skip) continue;  // empty, single, or sorted by k_cell_sort_small
         if (k <= 32) {
             const int v = lane < k ? perm[b + lane] : INT_MAX;
             int r = 0;
@@ -218,23 +247,6 @@ __global__ void k_cell_sort_warp(int m, const int* __restrict__ start, int* __re
     }
 }
 
-__global__ void k_cell_sort(int m, const int* __restrict__ start, int* __restrict__ perm) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= m) return;
-    int b = start[c], e = start[c + 1];
-    // insertion sort (cells hold ~10-20 atoms); a pathological cell is left
-    // unsorted (its order is then not reproducible) rather than sorted in O(k^2)
-    if (e - b > CELL_SORT_MAX) return;
-    for (int k = b + 1; k < e; k++) {
-        int v = perm[k];
-        int q = k - 1;
-        while (q >= b && perm[q] > v) {
-            perm[q + 1] = perm[q];
-            q--;
-        }
-        perm[q + 1] = v;
-    }
-}
 
 // Per-atom state that survives a rebuild, gathered into staging and copied
 // back so every array keeps its address (a captured step graph replays the
@@ -998,7 +1010,17 @@ int nlist_build(Context* c) {
     k_scan_totals<<<1, 1024, 0, s>>>(ntiles, m, c->cell_tile_sum, c->cell_start);
     k_scan_add<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->cell_tile_sum);
     k_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->cell, c->cell_start, c->cell_fill, c->perm);
-    k_cell_sort_warp<<<grid_for(m, 8), 256, 0, s>>>(m, c->cell_start, c->perm);
+    // most cells of a sparse grid (replica margins, vacuum) hold 0 or 1 atoms:
+    // a bounded grid of warps strides over the cells instead of one warp each
+    // sparse grids (a few atoms per cell) sort most cells a thread each;
+    // dense ones (EAM: ~20 atoms per cell) leave every cell to the warps
+    const bool sparse = n < 8 * m;
+    if (sparse) {
+        k_cell_sort_small<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->perm);
+        c->launches++;
+    }
+    k_cell_sort_warp<<<std::min(grid_for(m, 8), 16 * c->num_sms), 256, 0, s>>>(m, c->cell_start, c->perm,
+                                                                                sparse ? CELL_SORT_SMALL : 1);
     c->launches += 7;
     AtomArrays cur{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->aflag, c->extra, c->extra_n};
     AtomArrays stg{c->stage_d, c->stage_d + c->cap, c->stage_d + 2 * (size_t)c->cap, c->stage_d + 3 * (size_t)c->cap,

@@ -1082,7 +1082,7 @@ int nlist_build(Context* c) {
                                                         cell_sorted, c->cell_start, umax,
                                                         reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
                                                         c->d_flags + 1);
-    } else if (c->build_lanes == 0 && combos <= 64) {
+    } else if (c->build_lanes == 0 && combos <= 64 && !sparse) {  // a cell CTA wants >= 8 atoms per cell
         const int cap = 1024;  // staged candidates per chunk (32 bytes each)
         k_build_cells<<<m, BUILD_CELL_THREADS, cap * 2 * sizeof(float4), s>>>(
             bp, c->pack, c->x, c->y, c->z, c->cell_start, cap, reinterpret_cast<unsigned*>(c->nbr), c->nnb,

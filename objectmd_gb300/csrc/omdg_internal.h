@@ -218,7 +218,8 @@ struct Context {
 
     // launch shapes (defaults; the tuner may change them)
     int num_sms = 152;
-    int build_lanes = 0;       // list build: 0 cell-centric (shared memory), else threads per atom (1, 4, 8)
+    int build_lanes = 0;       // list build: 1, 4, 8 threads per atom; 0 cell-centric (shared memory)
+                               // on grids of >= 8 atoms per cell, else one thread per atom
     int nbr_hshift = 3;        // sliced-ELL slice height H = 2^hshift
     int eam_block = 256;
     int eam_lanes = 4;         // threads per atom

@@ -256,15 +256,178 @@ __device__ __forceinline__ float ters_fc(const TersDev& p, float r, float& dfc) 
         return 1.f;
     }
     if (r < p.R + p.D) {
-        const float arg = 1.57079632679489662f * (r - p.R) / p.D;  // pi (r-R) / (2D)
         float sn, cs;
-        sincosf(arg, &sn, &cs);
+        sincospif(0.5f * (r - p.R) / p.D, &sn, &cs);  // sin, cos of pi (r-R) / (2D)
         dfc = -0.78539816339744831f / p.D * cs;  // -pi/(4D) cos
         return 0.5f - 0.5f * sn;
     }
     dfc = 0.f;
     return 0.f;
 }
+
+// f(b) for the in-cutoff neighbours b < nc: fully unrolled over K (the
+// arrays f touches stay in registers), or a rolled loop over local arrays
+// (then the kernel's register count stays that of the unrolled path).
+template <int K, bool UNR, class F>
+__device__ __forceinline__ void for_nbrs(int nc, F&& f) {
+    if constexpr (UNR) {
+#pragma unroll
+        for (int b = 0; b < K; b++)
+            if (b < nc) f(b);
+    } else {
+#pragma unroll 1
+        for (int b = 0; b < nc; b++) f(b);
+    }
+}
+
+// The bonds centred on one atom, for its nc <= K in-cutoff neighbours
+// (unit vectors u from the centre, distances r).  Per neighbour the cutoff
+// f_c(r), f_c'(r) and 1/r are evaluated once; per triplet (a, b) the angular
+// and radial factors once, in the zeta sweep, with what the x_k gradient
+// needs kept for its sweep.
+template <int K, bool UNR>
+__device__ __forceinline__ void ters_bonds(const TersDev& p, const int nc, const float (&ux)[K],
+                                           const float (&uy)[K], const float (&uz)[K], const float (&rr)[K],
+                                           float (&skx)[K], float (&sky)[K], float (&skz)[K], float& fix,
+                                           float& fiy, float& fiz, float& ei, float& wi) {
+    float fc[K], dfc[K], ir[K];
+    for_nbrs<K, UNR>(nc, [&](int b) {
+        fc[b] = ters_fc(p, rr[b], dfc[b]);
+        ir[b] = 1.0f / rr[b];
+        skx[b] = sky[b] = skz[b] = 0.f;
+    });
+    const float g0 = 1.f + p.c2 / p.d2;
+    for_nbrs<K, UNR>(nc, [&](int a) {
+        const float rij = rr[a];
+        const float ex_ = ux[a], ey_ = uy[a], ez_ = uz[a];
+        // zeta_ij and its gradient w.r.t. x_j; per k the x_k coefficients
+        float zeta = 0.f, gjx = 0.f, gjy = 0.f, gjz = 0.f;
+        float ck[K], cc[K], cs[K];
+        for_nbrs<K, UNR>(nc, [&](int b) {
+            if (b == a) return;
+            const float c = ex_ * ux[b] + ey_ * uy[b] + ez_ * uz[b];
+            const float hc = p.h - c;
+            const float rden = 1.f / (p.d2 + hc * hc);
+            const float g = g0 - p.c2 * rden;
+            const float dg = -2.f * p.c2 * hc * rden * rden;
+            const float dr = rij - rr[b];
+            const float ex = expf(p.l3c * dr * dr * dr);
+            const float dex = 3.f * p.l3c * dr * dr * ex;
+            zeta += fc[b] * g * ex;
+            const float cj = fc[b] * dg * ex * ir[a], cu = fc[b] * g * dex;
+            gjx += cj * (ux[b] - c * ex_) + cu * ex_;
+            gjy += cj * (uy[b] - c * ey_) + cu * ey_;
+            gjz += cj * (uz[b] - c * ez_) + cu * ez_;
+            ck[b] = dfc[b] * g * ex - fc[b] * g * dex;
+            cc[b] = fc[b] * dg * ex * ir[b];
+            cs[b] = c;
+        });
+        const float fR = p.A * expf(-p.l1 * rij), fA = p.B * expf(-p.l2 * rij);
+        float bij, dbdz;
+        ters_bond_order(p, zeta, bij, dbdz);
+        const float vij = fc[a] * (fR - bij * fA);
+        const float dv_dr = dfc[a] * (fR - bij * fA) + fc[a] * (-p.l1 * fR + bij * p.l2 * fA);
+        const float dv_dz = -fc[a] * fA * dbdz;
+        // gradient of 1/2 V_ij: x_j part
+        const float sjx = 0.5f * (dv_dr * ex_ + dv_dz * gjx);
+        const float sjy = 0.5f * (dv_dr * ey_ + dv_dz * gjy);
+        const float sjz = 0.5f * (dv_dr * ez_ + dv_dz * gjz);
+        fix += sjx;  // the x_i gradient is minus the sum of the others
+        fiy += sjy;
+        fiz += sjz;
+        const float s = 0.5f * dv_dz;
+        // x_k parts
+        for_nbrs<K, UNR>(nc, [&](int b) {
+            if (b == a) return;
+            const float kx = s * (ck[b] * ux[b] + cc[b] * (ex_ - cs[b] * ux[b]));
+            const float ky = s * (ck[b] * uy[b] + cc[b] * (ey_ - cs[b] * uy[b]));
+            const float kz = s * (ck[b] * uz[b] + cc[b] * (ez_ - cs[b] * uz[b]));
+            fix += kx;
+            fiy += ky;
+            fiz += kz;
+            // force on k = -gradient
+            skx[b] -= kx;
+            sky[b] -= ky;
+            skz[b] -= kz;
+        });
+        skx[a] -= sjx;
+        sky[a] -= sjy;
+        skz[a] -= sjz;
+        ei += 0.5f * vij;
+        wi += 0.5f * dv_dr * rij;
+    });
+}
+
+// Relative vector from centre i to its list entry at `at`, when the pair is
+// one this potential evaluates and lies within the cutoff.
+__device__ __forceinline__ bool ters_neighbor(const TersDev& p, const PosPack& pi, const ShiftF& L,
+                                              const PosPack* __restrict__ pack, unsigned e, float3& u, float& r) {
+    const PosPack pj = pack[nbr_index(e)];
+    if (!p.single_type && pack_type(pj.hi) != p.ta) return false;
+    const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, L);
+    const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+    if (!(r2 < p.rc2)) return false;
+    r = sqrtf(r2);
+    if (!(r < p.rc)) return false;
+    const float ri = 1.0f / r;
+    u = make_float3(-d.x * ri, -d.y * ri, -d.z * ri);  // unit vector from i to the neighbour
+    return true;
+}
+
+__device__ __forceinline__ void ters_store(const TersDev& p, int i, float fix, float fiy, float fiz, float ei,
+                                           float wi, float* __restrict__ fx, float* __restrict__ fy,
+                                           float* __restrict__ fz, float* __restrict__ pe, float* __restrict__ vir) {
+    if (p.first) {
+        fx[i] = fix;
+        fy[i] = fiy;
+        fz[i] = fiz;
+        pe[i] = ei;
+        vir[i] = wi;
+    } else {
+        fx[i] += fix;
+        fy[i] += fiy;
+        fz[i] += fiz;
+        pe[i] += ei;
+        vir[i] += wi;
+    }
+}
+
+// A centre with more in-cutoff neighbours than the register path holds (a
+// collision cascade): up to TB_MAXN of them over local arrays.
+__device__ __noinline__ void ters_centre_wide(const TersDev& p, int i, const PosPack pi, const ShiftF L,
+                                              const PosPack* __restrict__ pack, const unsigned* __restrict__ nbr,
+                                              int m, float4* __restrict__ slot, float* __restrict__ fx,
+                                              float* __restrict__ fy, float* __restrict__ fz, float* __restrict__ pe,
+                                              float* __restrict__ vir, unsigned* status) {
+    float ux[TB_MAXN], uy[TB_MAXN], uz[TB_MAXN], rr[TB_MAXN];
+    int sl[TB_MAXN];
+    int nc = 0;
+    for (int s = 0; s < m; s++) {
+        const size_t at = nbr_at(i, s, p.hshift, p.maxnb);
+        float3 u;
+        float r;
+        if (!ters_neighbor(p, pi, L, pack, nbr[at], u, r)) continue;
+        if (nc < TB_MAXN) {
+            ux[nc] = u.x;
+            uy[nc] = u.y;
+            uz[nc] = u.z;
+            rr[nc] = r;
+            sl[nc] = s;
+        } else {
+            atomicOr(status, ERR_NBR_OVERFLOW);
+        }
+        nc++;
+    }
+    if (nc > TB_MAXN) nc = TB_MAXN;
+    float fix = 0.f, fiy = 0.f, fiz = 0.f, ei = 0.f, wi = 0.f;
+    float skx[TB_MAXN], sky[TB_MAXN], skz[TB_MAXN];
+    ters_bonds<TB_MAXN, false>(p, nc, ux, uy, uz, rr, skx, sky, skz, fix, fiy, fiz, ei, wi);
+    for (int a = 0; a < nc; a++)
+        slot[nbr_at(i, sl[a], p.hshift, p.maxnb)] = make_float4(skx[a], sky[a], skz[a], 0.f);
+    ters_store(p, i, fix, fiy, fiz, ei, wi, fx, fy, fz, pe, vir);
+}
+
+constexpr int TERS_REG = 4;  // in-cutoff neighbours the register path holds (diamond: 4)
 
 __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __restrict__ pack,
                                                    const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
@@ -279,125 +442,37 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
     const bool mine = p.single_type || pack_type(pi.hi) == p.ta;
     const ShiftF L = p.rep_L ? p.rep_L[p.rep_of[i]] : p.L;
     const int m = nnb[i];
-    float ux[TB_MAXN], uy[TB_MAXN], uz[TB_MAXN], rr[TB_MAXN];
-    int sl[TB_MAXN];
+    // the in-cutoff neighbours go to registers by select; every other slot
+    // of the row gets its zero here
+    float ux[TERS_REG], uy[TERS_REG], uz[TERS_REG], rr[TERS_REG];
+    int sl[TERS_REG];
+#pragma unroll
+    for (int k = 0; k < TERS_REG; k++) ux[k] = uy[k] = uz[k] = rr[k] = 0.f, sl[k] = 0;
     int nc = 0;
     for (int s = 0; s < m; s++) {
         const size_t at = nbr_at(i, s, p.hshift, p.maxnb);
-        slot[at] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (!mine) continue;
-        const unsigned e = nbr[at];
-        const PosPack pj = pack[nbr_index(e)];
-        if (!p.single_type && pack_type(pj.hi) != p.ta) continue;
-        const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, L);
-        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-        if (!(r2 < p.rc2)) continue;
-        const float r = sqrtf(r2);
-        if (!(r < p.rc)) continue;
-        if (nc < TB_MAXN) {
-            const float ri = 1.0f / r;
-            ux[nc] = -d.x * ri;  // unit vector from i to the neighbour
-            uy[nc] = -d.y * ri;
-            uz[nc] = -d.z * ri;
-            rr[nc] = r;
-            sl[nc] = s;
+        float3 u;
+        float r;
+        if (mine && ters_neighbor(p, pi, L, pack, nbr[at], u, r)) {
+#pragma unroll
+            for (int k = 0; k < TERS_REG; k++)
+                if (k == nc) ux[k] = u.x, uy[k] = u.y, uz[k] = u.z, rr[k] = r, sl[k] = s;
+            nc++;
         } else {
-            atomicOr(status, ERR_NBR_OVERFLOW);
+            slot[at] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        nc++;
     }
-    if (nc > TB_MAXN) nc = TB_MAXN;
+    if (nc > TERS_REG) {
+        ters_centre_wide(p, i, pi, L, pack, nbr, m, slot, fx, fy, fz, pe, vir, status);
+        return;
+    }
     float fix = 0.f, fiy = 0.f, fiz = 0.f, ei = 0.f, wi = 0.f;
-    // forces on the neighbours, summed here and stored in their slots once
-    float skx[TB_MAXN], sky[TB_MAXN], skz[TB_MAXN];
-    for (int a = 0; a < nc; a++) skx[a] = sky[a] = skz[a] = 0.f;
-    for (int a = 0; a < nc; a++) {
-        const float rij = rr[a];
-        const float ex_ = ux[a], ey_ = uy[a], ez_ = uz[a];
-        // zeta_ij and its gradient w.r.t. x_j (the x_k parts are applied below)
-        float zeta = 0.f, gjx = 0.f, gjy = 0.f, gjz = 0.f;
-        for (int b = 0; b < nc; b++) {
-            if (b == a) continue;
-            const float rik = rr[b];
-            const float cs = ex_ * ux[b] + ey_ * uy[b] + ez_ * uz[b];
-            float dfc;
-            const float fc = ters_fc(p, rik, dfc);
-            const float hc = p.h - cs;
-            const float den = p.d2 + hc * hc;
-            const float g = 1.f + p.c2 / p.d2 - p.c2 / den;
-            const float dg = -2.f * p.c2 * hc / (den * den);
-            const float dr = rij - rik;
-            const float ex = expf(p.l3c * dr * dr * dr);
-            const float dex = 3.f * p.l3c * dr * dr * ex;
-            zeta += fc * g * ex;
-            const float cj = fc * dg * ex / rij, cu = fc * g * dex;
-            gjx += cj * (ux[b] - cs * ex_) + cu * ex_;
-            gjy += cj * (uy[b] - cs * ey_) + cu * ey_;
-            gjz += cj * (uz[b] - cs * ez_) + cu * ez_;
-        }
-        float dfc_ij;
-        const float fc_ij = ters_fc(p, rij, dfc_ij);
-        const float fR = p.A * expf(-p.l1 * rij), fA = p.B * expf(-p.l2 * rij);
-        float bij, dbdz;
-        ters_bond_order(p, zeta, bij, dbdz);
-        const float vij = fc_ij * (fR - bij * fA);
-        const float dv_dr = dfc_ij * (fR - bij * fA) + fc_ij * (-p.l1 * fR + bij * p.l2 * fA);
-        const float dv_dz = -fc_ij * fA * dbdz;
-        // gradient of 1/2 V_ij: x_j part
-        float sjx = 0.5f * (dv_dr * ex_ + dv_dz * gjx);
-        float sjy = 0.5f * (dv_dr * ey_ + dv_dz * gjy);
-        float sjz = 0.5f * (dv_dr * ez_ + dv_dz * gjz);
-        fix += sjx;  // the x_i gradient is minus the sum of the others
-        fiy += sjy;
-        fiz += sjz;
-        // x_k parts
-        for (int b = 0; b < nc; b++) {
-            if (b == a) continue;
-            const float rik = rr[b];
-            const float cs = ex_ * ux[b] + ey_ * uy[b] + ez_ * uz[b];
-            float dfc;
-            const float fc = ters_fc(p, rik, dfc);
-            const float hc = p.h - cs;
-            const float den = p.d2 + hc * hc;
-            const float g = 1.f + p.c2 / p.d2 - p.c2 / den;
-            const float dg = -2.f * p.c2 * hc / (den * den);
-            const float dr = rij - rik;
-            const float ex = expf(p.l3c * dr * dr * dr);
-            const float dex = 3.f * p.l3c * dr * dr * ex;
-            const float ck = dfc * g * ex - fc * g * dex, cc = fc * dg * ex / rik;
-            const float s = 0.5f * dv_dz;
-            const float kx = s * (ck * ux[b] + cc * (ex_ - cs * ux[b]));
-            const float ky = s * (ck * uy[b] + cc * (ey_ - cs * uy[b]));
-            const float kz = s * (ck * uz[b] + cc * (ez_ - cs * uz[b]));
-            fix += kx;
-            fiy += ky;
-            fiz += kz;
-            // force on k = -gradient
-            skx[b] -= kx;
-            sky[b] -= ky;
-            skz[b] -= kz;
-        }
-        skx[a] -= sjx;
-        sky[a] -= sjy;
-        skz[a] -= sjz;
-        ei += 0.5f * vij;
-        wi += 0.5f * dv_dr * rij;
-    }
-    for (int a = 0; a < nc; a++)
-        slot[nbr_at(i, sl[a], p.hshift, p.maxnb)] = make_float4(skx[a], sky[a], skz[a], 0.f);
-    if (p.first) {
-        fx[i] = fix;
-        fy[i] = fiy;
-        fz[i] = fiz;
-        pe[i] = ei;
-        vir[i] = wi;
-    } else {
-        fx[i] += fix;
-        fy[i] += fiy;
-        fz[i] += fiz;
-        pe[i] += ei;
-        vir[i] += wi;
-    }
+    float skx[TERS_REG], sky[TERS_REG], skz[TERS_REG];
+    ters_bonds<TERS_REG, true>(p, nc, ux, uy, uz, rr, skx, sky, skz, fix, fiy, fiz, ei, wi);
+#pragma unroll
+    for (int a = 0; a < TERS_REG; a++)
+        if (a < nc) slot[nbr_at(i, sl[a], p.hshift, p.maxnb)] = make_float4(skx[a], sky[a], skz[a], 0.f);
+    ters_store(p, i, fix, fiy, fiz, ei, wi, fx, fy, fz, pe, vir);
 }
 
 // ------------------------------------------------------------------ ZBL pair

@@ -427,8 +427,7 @@ def run_e2e(ctx, n, steps, torch):
     ctx.step(1)
     t0 = time.perf_counter()
     for k in range(steps):
-        ctx.set_positions(x)
-        ctx.set_velocities(v)
+        ctx.set_state(x=x, v=v)
         ctx.step(1)
         ctx.get_state_into(x=x, v=v, f=f)
         ctx.ledger()

@@ -64,9 +64,14 @@ int omdg_num_atoms(omdg_ctx* ctx, int* n);
 int omdg_get_state(omdg_ctx* ctx, double* x, double* v, double* f, double* pot, double* vir);
 /* Overwrites positions / velocities (n*3 FP64, caller order).  New positions
    keep the neighbour list unless an atom moved more than skin/2 since it was
-   built; the next step or force evaluation then rebuilds it. */
+   built; the next step or force evaluation then rebuilds it.  Each call
+   returns once the caller's arrays have been read.  omdg_set_state uploads
+   both in one call (either may be NULL).  Pinned host arrays (cudaHostAlloc,
+   cudaHostRegister) are read and written by the device directly, here and in
+   omdg_get_state; other memory goes through a device staging copy. */
 int omdg_set_positions(omdg_ctx* ctx, const double* x);
 int omdg_set_velocities(omdg_ctx* ctx, const double* v);
+int omdg_set_state(omdg_ctx* ctx, const double* x, const double* v);
 
 /*
  * Replica mode (no single counterpart in the reference: each of its impact

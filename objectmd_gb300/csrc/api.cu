@@ -21,7 +21,7 @@ int step_state_read(Context* c, long long* step, int* row, int* rebuild);
 int step_state_resume(Context* c, long long step, double elapsed);
 int step_state_set_dt(Context* c);
 int step_state_times(Context* c, double* dt, double* elapsed);
-int step_state_fetch(Context* c, unsigned* status, long long* step, int* row, double* elapsed);
+int step_state_fetch(Context* c, unsigned* status, long long* step, int* row, double* elapsed, int rows);
 int step_state_rewind(Context* c);
 int step_clear_rebuild(Context* c);
 int launch_set_rebuild_cond(Context* c, cudaGraphConditionalHandle h);
@@ -192,8 +192,6 @@ static void compute_frame(Context* c) {
 
 using namespace omdg;
 
-
-static Context* C(omdg_ctx* c) { return static_cast<Context*>(c); }
 
 // graph state kept beside the context
 struct GraphState {
@@ -465,29 +463,30 @@ int omdg_get_state(omdg_ctx* c, double* x, double* v, double* f, double* pot, do
     return check_cuda(c, cudaStreamSynchronize(c->stream), "state read-back");
 }
 
+// Positions set by the caller refresh the packs; the list stays valid
+// unless an atom moved more than skin/2 since it was built (the upload's
+// displacement check then requests the rebuild the next step takes).
+// Velocities given by the caller replace any pending thermostat factor.
+// The call returns once the caller's arrays have been read.
+int omdg_set_state(omdg_ctx* c, const double* x, const double* v) {
+    if (!c) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    if (!x && !v) return OMDG_OK;
+    cudaSetDevice(c->device);
+    int rc = v ? drop_thermostat_factor(c) : OMDG_OK;
+    if (rc) return rc;
+    if ((rc = io_set_state(c, x, v))) return rc;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "state upload");
+}
+
 int omdg_set_positions(omdg_ctx* c, const double* x) {
     if (!c || !x) return OMDG_EINVAL;
-    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
-    cudaSetDevice(c->device);
-    int rc = io_set_state(c, x, nullptr);
-    if (rc) return rc;
-    // positions set by the caller: refresh the packs; the list stays valid
-    // unless an atom moved more than skin/2 since it was built (the device
-    // displacement check then requests the rebuild the next step takes)
-    if ((rc = integrate_pack(c))) return rc;
-    return request_rebuild(c);
+    return omdg_set_state(c, x, nullptr);
 }
 
 int omdg_set_velocities(omdg_ctx* c, const double* v) {
     if (!c || !v) return OMDG_EINVAL;
-    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
-    cudaSetDevice(c->device);
-    // velocities given by the caller replace any pending thermostat factor
-    int rc = drop_thermostat_factor(c);
-    if (rc) return rc;
-    rc = io_set_state(c, nullptr, v);
-    if (rc) return rc;
-    return check_cuda(c, cudaStreamSynchronize(c->stream), "velocity upload");
+    return omdg_set_state(c, nullptr, v);
 }
 
 }  // extern "C"
@@ -1241,7 +1240,10 @@ int omdg_sync(omdg_ctx* c) {
     long long step = 0;
     int rows = 0;
     double elapsed = 0.0;
-    int rc = step_state_fetch(c, &status, &step, &rows, &elapsed);  // waits for the queued steps
+    // the queued steps write one ledger row each, from row 0: those rows
+    // come back in the same round trip as the step state
+    const int expect = (c->async_steps > 0 && c->async_steps <= c->ledger_cap) ? (int)c->async_steps : 0;
+    int rc = step_state_fetch(c, &status, &step, &rows, &elapsed, expect);  // waits for the queued steps
     if (rc) return rc;
     if ((rc = status_error(c, status))) {
         if (rc == OMDG_ESTATE) {
@@ -1260,9 +1262,10 @@ int omdg_sync(omdg_ctx* c) {
     c->elapsed = elapsed;
     const int cap = c->ledger_cap;
     const int nrow = std::min(rows, cap);
-    if (nrow > 0) {
-        // the device ledger is a ring: rows older than `cap` steps were
-        // overwritten; the rest come back in order into the pinned copy
+    if (nrow > 0 && rows != expect) {
+        // (rows == expect: fetched with the step state)  The device ledger
+        // is a ring: rows older than `cap` steps were overwritten; the rest
+        // come back in order into the pinned copy
         const size_t w = sizeof(double) * LEDGER_W;
         cudaError_t e;
         if (rows <= cap) {
@@ -1277,6 +1280,8 @@ int omdg_sync(omdg_ctx* c) {
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) return check_cuda(c, e, "ledger read-back");
+    }
+    if (nrow > 0) {
         c->last_kin = c->h_ledger[LEDGER_W * (nrow - 1)];
         c->last_pot = c->h_ledger[LEDGER_W * (nrow - 1) + 1];
         c->last_vir = c->h_ledger[LEDGER_W * (nrow - 1) + 2];

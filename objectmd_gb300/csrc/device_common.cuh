@@ -297,4 +297,25 @@ __device__ __forceinline__ F2 f2_shfl_xor(F2 a, int o) {
     return {__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
 }
 
+// Caller-order transfers move blocks of IO_BLOCK atoms.  A block's rows of C
+// doubles are contiguous in the caller's array, so they pass through shared
+// memory with coalesced accesses on the caller's side (host memory over the
+// chip-to-chip link, or the device staging buffer); the sorted side is
+// gathered or scattered through the caller-to-sorted map.
+constexpr int IO_BLOCK = 256;
+
+// rows [b0, b0 + cnt) of an n x C caller array into s[0, C*cnt)
+template <int C>
+__device__ __forceinline__ void io_stage_in(const double* __restrict__ in, int b0, int cnt, double* s) {
+    const double* src = in + (size_t)C * b0;
+    for (int q = threadIdx.x; q < C * cnt; q += IO_BLOCK) s[q] = src[q];
+}
+
+// s[0, C*cnt) out to rows [b0, b0 + cnt) of an n x C caller array
+template <int C>
+__device__ __forceinline__ void io_stage_out(const double* s, int b0, int cnt, double* __restrict__ out) {
+    double* dst = out + (size_t)C * b0;
+    for (int q = threadIdx.x; q < C * cnt; q += IO_BLOCK) dst[q] = s[q];
+}
+
 }  // namespace omdg

@@ -666,12 +666,17 @@ int step_state_times(Context* c, double* dt, double* elapsed) {
 }
 
 // One round trip after the queued steps: the status word and the step state
-// into the pinned staging block, then one stream synchronisation.
-int step_state_fetch(Context* c, unsigned* status, long long* step, int* row, double* elapsed) {
+// into the pinned staging block and, when rows > 0, the first `rows` ledger
+// rows into the pinned ledger copy (what the queued steps write when none
+// stopped early), then one stream synchronisation.
+int step_state_fetch(Context* c, unsigned* status, long long* step, int* row, double* elapsed, int rows) {
     unsigned char* h = static_cast<unsigned char*>(c->h_sync);
     cudaError_t e = cudaMemcpyAsync(h, c->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h + 16, c->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && rows > 0)
+        e = cudaMemcpyAsync(c->h_ledger, c->d_ledger, sizeof(double) * LEDGER_W * rows, cudaMemcpyDeviceToHost,
+                            c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return check_cuda(c, e, "step");
     const StepState* st = reinterpret_cast<const StepState*>(h + 16);
@@ -769,22 +774,62 @@ int drop_thermostat_factor(Context* c) {
 
 // Flags a rebuild when positions written by the caller moved an atom more
 // than skin/2 from where the list was built.
-__global__ void k_check_disp(IntParams p, const PosPack* __restrict__ pack, const float4* __restrict__ xref,
-                             StepState* st) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    PosPack pk = pack[i];
-    float4 r0 = xref[i];
-    float dx = (pk.hi.x - r0.x) + pk.lo.x, dy = (pk.hi.y - r0.y) + pk.lo.y, dz = (pk.hi.z - r0.z) + pk.lo.z;
-    if (dx * dx + dy * dy + dz * dz > p.half_skin2) st->rebuild = 1;
+// Positions and/or velocities from the caller (rows of three in caller
+// order, at device-addressable addresses) in one pass: the sorted arrays,
+// and for positions the pack in the integrator's frame and the displacement
+// check against the last build (the list is kept unless an atom moved more
+// than skin/2).
+__global__ void __launch_bounds__(IO_BLOCK) k_upload_state(IntParams p, const int* __restrict__ inv,
+                                                           const double* __restrict__ in_x,
+                                                           const double* __restrict__ in_v, double* __restrict__ x,
+                                                           double* __restrict__ y, double* __restrict__ z,
+                                                           double* __restrict__ vx, double* __restrict__ vy,
+                                                           double* __restrict__ vz, const int* __restrict__ type,
+                                                           PosPack* __restrict__ pack,
+                                                           const float4* __restrict__ xref, StepState* st) {
+    __shared__ double s[2][3 * IO_BLOCK];
+    __shared__ int moved;
+    const int b0 = blockIdx.x * IO_BLOCK, cnt = min(IO_BLOCK, p.n - b0), t = threadIdx.x;
+    if (t == 0) moved = 0;
+    if (in_x) io_stage_in<3>(in_x, b0, cnt, s[0]);
+    if (in_v) io_stage_in<3>(in_v, b0, cnt, s[1]);
+    __syncthreads();
+    if (t < cnt) {
+        const int i = inv[b0 + t];
+        if (in_v) {
+            vx[i] = s[1][3 * t];
+            vy[i] = s[1][3 * t + 1];
+            vz[i] = s[1][3 * t + 2];
+        }
+        if (in_x) {
+            const double X = s[0][3 * t], Y = s[0][3 * t + 1], Z = s[0][3 * t + 2];
+            x[i] = X;
+            y[i] = Y;
+            z[i] = Z;
+            PosPack pk;
+            pack_coord(X, p.Qh[0], p.Ql[0], pk.hi.x, pk.lo.x);
+            pack_coord(Y, p.Qh[1], p.Ql[1], pk.hi.y, pk.lo.y);
+            pack_coord(Z, p.Qh[2], p.Ql[2], pk.hi.z, pk.lo.z);
+            pk.hi.w = __int_as_float(type[i]);
+            pk.lo.w = 0.f;
+            pack[i] = pk;
+            const float4 r0 = xref[i];
+            const float dx = (pk.hi.x - r0.x) + pk.lo.x, dy = (pk.hi.y - r0.y) + pk.lo.y,
+                        dz = (pk.hi.z - r0.z) + pk.lo.z;
+            if (dx * dx + dy * dy + dz * dz > p.half_skin2) moved = 1;
+        }
+    }
+    __syncthreads();
+    if (t == 0 && moved) st->rebuild = 1;
 }
 
-int request_rebuild(Context* c) {
+int upload_state(Context* c, const double* in_x, const double* in_v) {
     IntParams p = int_params(c);
-    k_check_disp<<<grid_for(c->n, 256), 256, 0, c->stream>>>(p, c->pack, c->xref,
-                                                             reinterpret_cast<StepState*>(c->d_state));
+    k_upload_state<<<(c->n + IO_BLOCK - 1) / IO_BLOCK, IO_BLOCK, 0, c->stream>>>(
+        p, c->inv, in_x, in_v, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->pack, c->xref,
+        reinterpret_cast<StepState*>(c->d_state));
     c->launches++;
-    return check_cuda(c, cudaGetLastError(), "displacement check");
+    return check_cuda(c, cudaGetLastError(), "state upload");
 }
 
 int step_clear_rebuild(Context* c) {

@@ -1,79 +1,85 @@
 // Host<->device state transfer in the caller's atom order.  The device keeps
-// atoms in cell order; these kernels permute through the id/inv maps on the
-// GPU so a transfer is one contiguous copy of n*3 doubles per array, which
-// is what an Object-MD application's host mirror of Atom x/v/f needs
-// (SyncData points, gadget.h:212-213).
+// atoms in cell order; these kernels permute through the caller-to-sorted
+// map on the GPU, so each array crosses the host link once as n rows of
+// doubles, which is what an Object-MD application's host mirror of Atom
+// x/v/f needs (SyncData points, gadget.h:212-213).  Pinned host arrays are
+// read and written by the kernels themselves (no staging copy).
 #include "device_common.cuh"
 
 namespace omdg {
 
-__global__ void k_to_caller3(int n, const int* __restrict__ id, const double* __restrict__ a,
-                             const double* __restrict__ b, const double* __restrict__ c, double* __restrict__ out) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    size_t o = 3 * (size_t)id[k];
-    out[o] = a[k];
-    out[o + 1] = b[k];
-    out[o + 2] = c[k];
+// Sorted arrays (C components, SoA of type T) to caller-order rows: thread
+// t gathers caller atom b0 + t from its sorted index.
+template <int C, typename T>
+__global__ void __launch_bounds__(IO_BLOCK) k_soa_to_rows(int n, const int* __restrict__ inv, const T* __restrict__ a,
+                                                          const T* __restrict__ b, const T* __restrict__ c,
+                                                          double* __restrict__ out) {
+    __shared__ double s[C * IO_BLOCK];
+    const int b0 = blockIdx.x * IO_BLOCK, cnt = min(IO_BLOCK, n - b0), t = threadIdx.x;
+    if (t < cnt) {
+        const int i = inv[b0 + t];
+        s[C * t] = (double)a[i];
+        if (C == 3) {
+            s[C * t + 1] = (double)b[i];
+            s[C * t + 2] = (double)c[i];
+        }
+    }
+    __syncthreads();
+    io_stage_out<C>(s, b0, cnt, out);
 }
 
-__global__ void k_to_caller3f(int n, const int* __restrict__ id, const float* __restrict__ a,
-                              const float* __restrict__ b, const float* __restrict__ c, double* __restrict__ out) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    size_t o = 3 * (size_t)id[k];
-    out[o] = a[k];
-    out[o + 1] = b[k];
-    out[o + 2] = c[k];
+// Positions, velocities and forces to caller-order rows in one pass (any
+// output may be null): a block gathers its atoms' nine values, then writes
+// the three row segments.  Forces are FP32 arrays, or FP64 interleaved.
+__global__ void __launch_bounds__(IO_BLOCK) k_state_to_rows(int n, const int* __restrict__ inv,
+                                                            const double* __restrict__ x, const double* __restrict__ y,
+                                                            const double* __restrict__ z, const double* __restrict__ vx,
+                                                            const double* __restrict__ vy,
+                                                            const double* __restrict__ vz, const float* __restrict__ fx,
+                                                            const float* __restrict__ fy, const float* __restrict__ fz,
+                                                            const double* __restrict__ f64, double* __restrict__ ox,
+                                                            double* __restrict__ ov, double* __restrict__ of) {
+    __shared__ double s[3][3 * IO_BLOCK];
+    const int b0 = blockIdx.x * IO_BLOCK, cnt = min(IO_BLOCK, n - b0), t = threadIdx.x;
+    if (t < cnt) {
+        const int i = inv[b0 + t];
+        if (ox) s[0][3 * t] = x[i], s[0][3 * t + 1] = y[i], s[0][3 * t + 2] = z[i];
+        if (ov) s[1][3 * t] = vx[i], s[1][3 * t + 1] = vy[i], s[1][3 * t + 2] = vz[i];
+        if (of) {
+            if (f64) {
+                const double* r = f64 + 3 * (size_t)i;
+                s[2][3 * t] = r[0], s[2][3 * t + 1] = r[1], s[2][3 * t + 2] = r[2];
+            } else {
+                s[2][3 * t] = fx[i], s[2][3 * t + 1] = fy[i], s[2][3 * t + 2] = fz[i];
+            }
+        }
+    }
+    __syncthreads();
+    if (ox) io_stage_out<3>(s[0], b0, cnt, ox);
+    if (ov) io_stage_out<3>(s[1], b0, cnt, ov);
+    if (of) io_stage_out<3>(s[2], b0, cnt, of);
 }
 
-__global__ void k_to_caller3d(int n, const int* __restrict__ id, const double* __restrict__ f64,
-                              double* __restrict__ out) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    size_t o = 3 * (size_t)id[k];
-    out[o] = f64[3 * (size_t)k];
-    out[o + 1] = f64[3 * (size_t)k + 1];
-    out[o + 2] = f64[3 * (size_t)k + 2];
-}
-
-__global__ void k_to_caller1f(int n, const int* __restrict__ id, const float* __restrict__ a,
-                              double* __restrict__ out) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    out[id[k]] = a[k];
-}
-
-__global__ void k_to_caller1d(int n, const int* __restrict__ id, const double* __restrict__ a,
-                              double* __restrict__ out) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    out[id[k]] = a[k];
-}
-
-__global__ void k_from_caller3(int n, const int* __restrict__ id, const double* __restrict__ in,
-                               double* __restrict__ a, double* __restrict__ b, double* __restrict__ c) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    size_t o = 3 * (size_t)id[k];
-    a[k] = in[o];
-    b[k] = in[o + 1];
-    c[k] = in[o + 2];
-}
-
-__global__ void k_from_caller3f(int n, const int* __restrict__ id, const double* __restrict__ in,
-                                float* __restrict__ a, float* __restrict__ b, float* __restrict__ c,
-                                double* __restrict__ f64) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    size_t o = 3 * (size_t)id[k];
-    a[k] = (float)in[o];
-    b[k] = (float)in[o + 1];
-    c[k] = (float)in[o + 2];
-    if (f64) {
-        f64[3 * (size_t)k] = in[o];
-        f64[3 * (size_t)k + 1] = in[o + 1];
-        f64[3 * (size_t)k + 2] = in[o + 2];
+// Caller-order force rows to the sorted FP32 arrays (and the FP64 forces,
+// three interleaved per atom, when the context keeps them)
+__global__ void __launch_bounds__(IO_BLOCK) k_rows_to_forces(int n, const int* __restrict__ inv,
+                                                             const double* __restrict__ in, float* __restrict__ fx,
+                                                             float* __restrict__ fy, float* __restrict__ fz,
+                                                             double* __restrict__ f64) {
+    __shared__ double s[3 * IO_BLOCK];
+    const int b0 = blockIdx.x * IO_BLOCK, cnt = min(IO_BLOCK, n - b0), t = threadIdx.x;
+    io_stage_in<3>(in, b0, cnt, s);
+    __syncthreads();
+    if (t < cnt) {
+        const int i = inv[b0 + t];
+        fx[i] = (float)s[3 * t];
+        fy[i] = (float)s[3 * t + 1];
+        fz[i] = (float)s[3 * t + 2];
+        if (f64) {
+            f64[3 * (size_t)i] = s[3 * t];
+            f64[3 * (size_t)i + 1] = s[3 * t + 1];
+            f64[3 * (size_t)i + 2] = s[3 * t + 2];
+        }
     }
 }
 
@@ -88,55 +94,90 @@ static int ensure_io(Context* c) {
     return OMDG_OK;
 }
 
-// One contiguous async copy per requested array; the caller synchronizes.
+// p (count doubles) when kernels can read and write it at its own address:
+// pinned or registered host memory, both ends inside registered ranges, on
+// a device that addresses registered memory by its host pointer.  Else null
+// (pageable memory takes a copy through the staging buffer).
+const double* host_view(Context* c, const double* p, size_t count) {
+    if (!p || count == 0) return nullptr;
+    if (c->host_ptr_ok < 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrCanUseHostPointerForRegisteredMem, c->device) != cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        c->host_ptr_ok = v ? 1 : 0;
+    }
+    if (!c->host_ptr_ok) return nullptr;
+    for (const double* q : {p, p + count - 1}) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer != static_cast<const void*>(q)) return nullptr;
+    }
+    return p;
+}
+
+// Per requested array one kernel, writing the caller's rows in place when
+// its memory is addressable, else into the staging buffer and one copy;
+// the caller synchronizes.
 int io_get_state(Context* c, double* x, double* v, double* f, double* pot, double* vir) {
     int rc = ensure_io(c);
     if (rc) return rc;
-    int n = c->n, g = grid_for(n, 256);
+    const int n = c->n, g = (n + IO_BLOCK - 1) / IO_BLOCK;
     cudaStream_t s = c->stream;
+    const size_t n3 = 3 * (size_t)n;
+    // destination of one array: the caller's memory or its staging slot
+    auto dest = [&](double* h, size_t count, double* stage) { return host_view(c, h, count) ? h : stage; };
+    auto finish = [&](double* h, double* d, size_t count) {
+        if (d != h) cudaMemcpyAsync(h, d, sizeof(double) * count, cudaMemcpyDeviceToHost, s);
+    };
     double* st = c->d_io;
-    size_t n3 = 3 * (size_t)n;
-    if (x) {
-        k_to_caller3<<<g, 256, 0, s>>>(n, c->id, c->x, c->y, c->z, st);
-        cudaMemcpyAsync(x, st, sizeof(double) * n3, cudaMemcpyDeviceToHost, s);
-    }
-    if (v) {
-        k_to_caller3<<<g, 256, 0, s>>>(n, c->id, c->vx, c->vy, c->vz, st + n3);
-        cudaMemcpyAsync(v, st + n3, sizeof(double) * n3, cudaMemcpyDeviceToHost, s);
-    }
-    if (f) {
-        if (c->use_f64) k_to_caller3d<<<g, 256, 0, s>>>(n, c->id, c->f64, st + 2 * n3);
-        else k_to_caller3f<<<g, 256, 0, s>>>(n, c->id, c->fx, c->fy, c->fz, st + 2 * n3);
-        cudaMemcpyAsync(f, st + 2 * n3, sizeof(double) * n3, cudaMemcpyDeviceToHost, s);
+    if (x || v || f) {
+        double* dx = x ? dest(x, n3, st) : nullptr;
+        double* dv = v ? dest(v, n3, st + n3) : nullptr;
+        double* df = f ? dest(f, n3, st + 2 * n3) : nullptr;
+        k_state_to_rows<<<g, IO_BLOCK, 0, s>>>(n, c->inv, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz,
+                                               c->use_f64 ? c->f64 : nullptr, dx, dv, df);
+        if (x) finish(x, dx, n3);
+        if (v) finish(v, dv, n3);
+        if (f) finish(f, df, n3);
     }
     if (pot) {
-        if (c->use_f64) k_to_caller1d<<<g, 256, 0, s>>>(n, c->id, c->f64 + n3, st + 3 * n3);
-        else k_to_caller1f<<<g, 256, 0, s>>>(n, c->id, c->pe, st + 3 * n3);
-        cudaMemcpyAsync(pot, st + 3 * n3, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+        double* d = dest(pot, n, st + 3 * n3);
+        if (c->use_f64)
+            k_soa_to_rows<1, double><<<g, IO_BLOCK, 0, s>>>(n, c->inv, c->f64 + n3, nullptr, nullptr, d);
+        else k_soa_to_rows<1, float><<<g, IO_BLOCK, 0, s>>>(n, c->inv, c->pe, nullptr, nullptr, d);
+        finish(pot, d, n);
     }
     if (vir) {
-        k_to_caller1f<<<g, 256, 0, s>>>(n, c->id, c->vir, st + 3 * n3 + n);
-        cudaMemcpyAsync(vir, st + 3 * n3 + n, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+        double* d = dest(vir, n, st + 3 * n3 + n);
+        k_soa_to_rows<1, float><<<g, IO_BLOCK, 0, s>>>(n, c->inv, c->vir, nullptr, nullptr, d);
+        finish(vir, d, n);
     }
     return check_cuda(c, cudaGetLastError(), "state read-back");
 }
 
-// Upload positions and/or velocities given in caller order.
+// Upload positions and/or velocities given in caller order (positions also
+// refresh the pack and the displacement check).
 int io_set_state(Context* c, const double* x, const double* v) {
     int rc = ensure_io(c);
     if (rc) return rc;
-    int n = c->n, g = grid_for(n, 256);
     cudaStream_t s = c->stream;
-    size_t n3 = 3 * (size_t)n;
-    if (x) {
-        cudaMemcpyAsync(c->d_io, x, sizeof(double) * n3, cudaMemcpyHostToDevice, s);
-        k_from_caller3<<<g, 256, 0, s>>>(n, c->id, c->d_io, c->x, c->y, c->z);
-    }
-    if (v) {
-        cudaMemcpyAsync(c->d_io + n3, v, sizeof(double) * n3, cudaMemcpyHostToDevice, s);
-        k_from_caller3<<<g, 256, 0, s>>>(n, c->id, c->d_io + n3, c->vx, c->vy, c->vz);
-    }
-    return check_cuda(c, cudaGetLastError(), "state upload");
+    const size_t n3 = 3 * (size_t)c->n;
+    // source of one array: the caller's memory or its staging slot
+    auto source = [&](const double* h, double* stage) -> const double* {
+        if (!h) return nullptr;
+        if (host_view(c, h, n3)) return h;
+        cudaMemcpyAsync(stage, h, sizeof(double) * n3, cudaMemcpyHostToDevice, s);
+        return stage;
+    };
+    const double* sx = source(x, c->d_io);
+    const double* sv = source(v, c->d_io + n3);
+    if (!sx && !sv) return OMDG_OK;
+    return upload_state(c, sx, sv);
 }
 
 __global__ void k_flags_from_caller(int n, const int* __restrict__ id, const unsigned* __restrict__ in,
@@ -182,11 +223,12 @@ int io_get_flags(Context* c, unsigned* flags) {
 int io_set_forces(Context* c, const double* f) {
     int rc = ensure_io(c);
     if (rc) return rc;
-    int n = c->n, g = grid_for(n, 256);
+    const int n = c->n;
     cudaStream_t s = c->stream;
     const size_t n3 = 3 * (size_t)n;
     cudaMemcpyAsync(c->d_io + 2 * n3, f, sizeof(double) * n3, cudaMemcpyHostToDevice, s);
-    k_from_caller3f<<<g, 256, 0, s>>>(n, c->id, c->d_io + 2 * n3, c->fx, c->fy, c->fz, c->use_f64 ? c->f64 : nullptr);
+    k_rows_to_forces<<<(n + IO_BLOCK - 1) / IO_BLOCK, IO_BLOCK, 0, s>>>(n, c->inv, c->d_io + 2 * n3, c->fx, c->fy,
+                                                                       c->fz, c->use_f64 ? c->f64 : nullptr);
     return check_cuda(c, cudaGetLastError(), "force upload");
 }
 

@@ -193,6 +193,7 @@ struct Context {
     bool use_f64 = false;
     double* d_mass = nullptr;    // mass per type (device)
     double* d_io = nullptr;      // caller-order transfer staging
+    int host_ptr_ok = -1;        // registered host memory is addressable by kernels at its own address (-1: not asked)
     size_t io_cap = 0;
     long async_steps = 0;        // steps enqueued since the last omdg_sync
     long launches_at_sync = 0, last_launches = 0;
@@ -322,7 +323,8 @@ int integrate_kick(Context* c, int step_index);
 int integrate_pack(Context* c);
 int measure_energies(Context* c, int row);
 int zero_forces(Context* c);
-int request_rebuild(Context* c);
+// caller-order x and/or v rows (device-addressable): sorted arrays; for x also the pack and displacement check
+int upload_state(Context* c, const double* in_x, const double* in_v);
 int resolve_thermostat(Context* c);
 int gather_slots(Context* c, bool zero_virial);
 int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask);
@@ -339,7 +341,10 @@ void nn_release(Potential& pot);
 int drop_thermostat_factor(Context* c);
 int step_state_graph_rebuilds(Context* c, int* nrebuild);
 
-// caller-order transfers (io.cu); asynchronous on the context stream
+// caller-order transfers (io.cu); asynchronous on the context stream.  Pinned
+// or registered host arrays are read and written by the kernels directly;
+// other host memory goes through the device staging buffer and one copy.
+const double* host_view(Context* c, const double* p, size_t count);
 int io_get_state(Context* c, double* x, double* v, double* f, double* pot, double* vir);
 int io_set_state(Context* c, const double* x, const double* v);
 int io_set_forces(Context* c, const double* f);

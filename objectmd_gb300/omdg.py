@@ -88,6 +88,7 @@ SIGNATURES = {
     "omdg_get_state": [_vp, _P(_d), _P(_d), _P(_d), _P(_d), _P(_d)],
     "omdg_set_positions": [_vp, _P(_d)],
     "omdg_set_velocities": [_vp, _P(_d)],
+    "omdg_set_state": [_vp, _P(_d), _P(_d)],
     "omdg_add_eam": [_vp, _i, _i, _cp],
     "omdg_add_pair_table": [_vp, _i, _i, _cp, _i],
     "omdg_add_sw": [_vp, _i, _i, _cp],
@@ -434,6 +435,12 @@ class Context:
     def set_velocities(self, v):
         v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
         self._check(self.lib.omdg_set_velocities(self.h, _dp(v)))
+
+    def set_state(self, x=None, v=None):
+        """Positions and/or velocities in one call (pinned arrays are read in place)."""
+        x = None if x is None else np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        self._check(self.lib.omdg_set_state(self.h, _dp(x), _dp(v)))
 
     def add_eam(self, table_file, ta=0, tb=0):
         self._check(self.lib.omdg_add_eam(self.h, ta, tb, table_file.encode()))

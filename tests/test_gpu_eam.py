@@ -191,3 +191,38 @@ def test_position_upload_keeps_or_rebuilds_the_list(omdg_lib):
                 ref.compute_forces()
                 fr = ref.get_state()["f"]
             assert np.abs(f - fr).max() <= 1e-6 * np.abs(fr).max() + 1e-7
+
+
+def test_pinned_transfers_equal_staged_transfers(omdg_lib):
+    """Pinned host arrays are read and written by the device in place,
+    pageable ones through a staging copy: the same state comes back bit for
+    bit either way, uploads from pinned arrays land exactly, and a pinned
+    upload that moves an atom beyond skin/2 triggers the rebuild."""
+    torch = pytest.importorskip("torch")
+    d = load_case("eam_al_500")
+    n = len(d["x0"])
+    pin = lambda *shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+    with make_eam(omdg_lib, d, rebuild_every=0) as ctx:
+        ctx.step(3)
+        x, v, f, pot, vir = pin(n, 3), pin(n, 3), pin(n, 3), pin(n), pin(n)
+        ctx.get_state_into(x=x, v=v, f=f, pot=pot, vir=vir)
+        st = ctx.get_state()  # pageable arrays
+        for a, k in ((x, "x"), (v, "v"), (f, "f"), (pot, "pot"), (vir, "vir")):
+            np.testing.assert_array_equal(a, st[k])
+        rng = np.random.default_rng(5)
+        x += rng.normal(size=x.shape) * 0.01
+        v *= 1.5
+        ctx.set_state(x=x, v=v)
+        st = ctx.get_state()
+        np.testing.assert_array_equal(st["x"], x)
+        np.testing.assert_array_equal(st["v"], v)
+        ctx.compute_forces()
+        r0 = ctx.stats()["rebuilds"]
+        x[11, 0] += 0.4  # skin/2 = 0.15 A
+        ctx.set_state(x=x)
+        ctx.compute_forces()
+        assert ctx.stats()["rebuilds"] > r0
+        f_pinned = ctx.get_state()["f"]
+        ctx.set_positions(np.array(x))  # the same positions from pageable memory
+        ctx.compute_forces()
+        np.testing.assert_array_equal(ctx.get_state()["f"], f_pinned)

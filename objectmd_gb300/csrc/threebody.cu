@@ -246,7 +246,7 @@ __device__ __forceinline__ void ters_bond_order(const TersDev& p, float zeta, fl
         return;
     }
     const float bn = expf(nlx);
-    b = powf(1.f + bn, -0.5f / p.nn);
+    b = exp2f((-0.5f / p.nn) * log2f(1.f + bn));  // (1 + bn)^(-1/2n), |exponent| < 2: ~3e-7 relative
     db = -0.5f * b * bn / ((1.f + bn) * zeta);
 }
 

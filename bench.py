@@ -12,9 +12,9 @@ force, kick, energy ledger.
 Timing: W untimed warm-up steps, then K steps each bracketed by CUDA events
 on the library's stream, with an L2 flush (a 512 MB write) enqueued before
 every step outside the events.  `value` = atoms * K / sum(step times).  `e2e`
-repeats the K steps through the public C ABI with pinned host buffers: every
-step uploads positions and velocities, steps, and reads positions,
-velocities, forces and the energy ledger back.
+repeats the K steps through the public C ABI (omdg_step_io) with pinned host
+buffers: every step uploads positions and velocities, steps, and reads
+positions, velocities, forces and the energy ledger back.
 
 --impl reference times the oracle's CPU restatement of the same path
 (oracle/omd_oracle.c, compiled on this host) on every host core: one process
@@ -420,16 +420,16 @@ def surrogate_report(ctx, w, x0, v0, lo, hi, device, args, torch):
 
 
 def run_e2e(ctx, n, steps, torch):
-    """Per step: pinned H2D of x and v, one step, D2H of x, v, f and the ledger."""
+    """Per step one omdg_step_io call from pinned host arrays: H2D of x and v,
+    one step, D2H of x, v and f (x and f while the step's last kernels run),
+    then the ledger."""
     pin = lambda: torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
     x, v, f = pin(), pin(), pin()
     ctx.get_state_into(x=x, v=v)
-    ctx.step(1)
+    ctx.step_io(1, x_in=x, v_in=v, x_out=x, v_out=v, f_out=f)  # captures the step with its downloads
     t0 = time.perf_counter()
     for k in range(steps):
-        ctx.set_state(x=x, v=v)
-        ctx.step(1)
-        ctx.get_state_into(x=x, v=v, f=f)
+        ctx.step_io(1, x_in=x, v_in=v, x_out=x, v_out=v, f_out=f)
         ctx.ledger()
     t1 = time.perf_counter()
     return {"value": n * steps / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": 2 * 24 * n,

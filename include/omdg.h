@@ -152,6 +152,14 @@ int omdg_step(omdg_ctx* ctx, int nsteps);
    omdg_sync waits for them, checks the device status and updates the ledger. */
 int omdg_step_async(omdg_ctx* ctx, int nsteps);
 int omdg_sync(omdg_ctx* ctx);
+/* One MD call driven from host arrays (caller order, n*3 FP64; any pointer
+   may be NULL): uploads x_in / v_in as omdg_set_state does, runs nsteps as
+   omdg_step does, and writes the last step's positions, velocities and
+   forces as omdg_get_state does; returns once they are in place.  With
+   pinned output arrays and no thermostat, the last step writes x and f to
+   the host while its force and kick kernels run. */
+int omdg_step_io(omdg_ctx* ctx, const double* x_in, const double* v_in, int nsteps, double* x_out, double* v_out,
+                 double* f_out);
 int omdg_set_first_step_mode(omdg_ctx* ctx, int reference_first_step);
 
 /*
@@ -187,7 +195,9 @@ int omdg_stats(omdg_ctx* ctx, long* rebuilds, long* launches);
  * Launch shapes (no reference counterpart: the reference is scalar C++).
  * Keys: "eam_block", "eam_lanes" (threads per atom), "eam_stage" (spline
  * knots in shared memory), "eam_ctas_per_sm", "pair_block", "pair_lanes",
- * "tb_block", "tb_lanes", "nbr_hshift" (log2 of the neighbour slice height).
+ * "tb_block", "tb_lanes", "nbr_hshift" (log2 of the neighbour slice height),
+ * "build_lanes" (list build: 0 cell CTAs, else threads per atom), "io_blocks"
+ * (blocks of omdg_step_io's downloads beside the step's kernels).
  */
 int omdg_set_launch(omdg_ctx* ctx, const char* key, int value);
 int omdg_get_launch(omdg_ctx* ctx, const char* key, int* value);

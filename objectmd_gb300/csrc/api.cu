@@ -199,6 +199,15 @@ struct GraphState {
     cudaGraph_t graph = nullptr;
     cudaStream_t side = nullptr;
     bool valid = false;
+    // the same step with download branches into pinned host arrays
+    // (omdg_step_io), keyed by the x, v, f output pointers
+    cudaGraphExec_t io_exec = nullptr;
+    cudaGraph_t io_graph = nullptr;
+    cudaStream_t io_side = nullptr;
+    cudaEvent_t io_ev[4] = {};
+    double* io_key[3] = {};
+    long io_kernels = 0;
+    bool io_valid = false;
 };
 static std::map<Context*, GraphState> g_graphs;
 
@@ -206,11 +215,14 @@ namespace omdg {
 void invalidate_graph(Context* c) {
     auto it = g_graphs.find(c);
     if (it == g_graphs.end()) return;
-    if (it->second.exec) cudaGraphExecDestroy(it->second.exec);
-    if (it->second.graph) cudaGraphDestroy(it->second.graph);
-    it->second.exec = nullptr;
-    it->second.graph = nullptr;
-    it->second.valid = false;
+    GraphState& gs = it->second;
+    if (gs.exec) cudaGraphExecDestroy(gs.exec);
+    if (gs.graph) cudaGraphDestroy(gs.graph);
+    if (gs.io_exec) cudaGraphExecDestroy(gs.io_exec);
+    if (gs.io_graph) cudaGraphDestroy(gs.io_graph);
+    gs.exec = gs.io_exec = nullptr;
+    gs.graph = gs.io_graph = nullptr;
+    gs.valid = gs.io_valid = false;
 }
 }  // namespace omdg
 
@@ -252,7 +264,11 @@ int omdg_destroy(omdg_ctx* c) {
     invalidate_graph(c);
     auto it = g_graphs.find(c);
     if (it != g_graphs.end()) {
-        if (it->second.side) cudaStreamDestroy(it->second.side);
+        GraphState& gs = it->second;
+        if (gs.side) cudaStreamDestroy(gs.side);
+        if (gs.io_side) cudaStreamDestroy(gs.io_side);
+        for (cudaEvent_t ev : gs.io_ev)
+            if (ev) cudaEventDestroy(ev);
         g_graphs.erase(it);
     }
     free_atoms(c);
@@ -851,9 +867,28 @@ static int eager_maybe_rebuild(Context* c) {
     return OMDG_OK;
 }
 
-static int capture_step(Context* c, GraphState& gs) {
+// io (omdg_step_io): x, v, f pinned host outputs (each may be null).  The
+// captured step then forks a branch that writes x once the positions (and
+// any rebuild's order) are final, f once the forces are, and v after the
+// kick, while the force and kick kernels run; the branch joins before the
+// step ends.
+static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr) {
     cudaStream_t s = c->stream;
     if (!gs.side) cudaStreamCreateWithFlags(&gs.side, cudaStreamNonBlocking);
+    if (io && !gs.io_side) {
+        cudaStreamCreateWithFlags(&gs.io_side, cudaStreamNonBlocking);
+        for (cudaEvent_t& ev : gs.io_ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    }
+    long io_launches = 0;
+    // one download on the branch once the main stream's work so far is done
+    auto branch = [&](int k, double* x, double* v, double* f) -> int {
+        if (!x && !v && !f) return OMDG_OK;
+        cudaError_t e2 = cudaEventRecord(gs.io_ev[k], s);
+        if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(gs.io_side, gs.io_ev[k], 0);
+        if (e2 != cudaSuccess) return check_cuda(c, e2, "download branch");
+        io_launches++;
+        return io_rows_to_host(c, gs.io_side, x, v, f);
+    };
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return check_cuda(c, e, "capture begin");
     long l0 = c->launches, l1 = 0, l2 = 0;
@@ -900,9 +935,17 @@ static int capture_step(Context* c, GraphState& gs) {
         }
     }
     l2 = c->launches;
+    if (!rc && io) rc = branch(0, io[0], nullptr, nullptr);
     if (!rc) rc = forces_compute(c);
+    if (!rc && io) rc = branch(1, nullptr, nullptr, io[2]);
     if (!rc) rc = integrate_kick(c, 0);
     if (!rc && c->ttm) rc = thermo_detect(c);  // ExecuteDetectors (system.cpp:976)
+    if (!rc && io) rc = branch(2, nullptr, io[1], nullptr);
+    if (!rc && io_launches > 0) {  // join the branch
+        e = cudaEventRecord(gs.io_ev[3], gs.io_side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, gs.io_ev[3], 0);
+        if (e != cudaSuccess) rc = check_cuda(c, e, "download join");
+    }
     long l3 = c->launches;
     // captured launches are counted when the graph replays, not here
     c->graph_step_kernels = (l1 - l0) + (l3 - l2);
@@ -922,9 +965,17 @@ static int capture_step(Context* c, GraphState& gs) {
         cudaGraphDestroy(graph);
         return check_cuda(c, e, "graph instantiate");
     }
-    gs.graph = graph;
-    gs.exec = exec;
-    gs.valid = true;
+    if (io) {
+        gs.io_graph = graph;
+        gs.io_exec = exec;
+        gs.io_valid = true;
+        for (int k = 0; k < 3; k++) gs.io_key[k] = io[k];
+        gs.io_kernels = io_launches;
+    } else {
+        gs.graph = graph;
+        gs.exec = exec;
+        gs.valid = true;
+    }
     // the rebuild count is advanced on the host only for eager builds
     return OMDG_OK;
 }
@@ -1298,6 +1349,52 @@ int omdg_step(omdg_ctx* c, int nsteps) {
     return omdg_sync(c);
 }
 
+int omdg_step_io(omdg_ctx* c, const double* x_in, const double* v_in, int nsteps, double* x_out, double* v_out,
+                 double* f_out) {
+    if (!c || nsteps < 1) return OMDG_EINVAL;
+    if (c->n == 0) return set_error(c, OMDG_ESTATE, "no atoms");
+    cudaSetDevice(c->device);
+    int rc;
+    if (x_in || v_in) {
+        // read by the upload kernel, which completes before this call returns
+        if (v_in && (rc = drop_thermostat_factor(c))) return rc;
+        if ((rc = io_set_state(c, x_in, v_in))) return rc;
+    }
+    const size_t n3 = 3 * (size_t)c->n;
+    // overlapped downloads: graph replay, pinned outputs, and no thermostat
+    // factor pending on the velocities at the end of the step
+    bool overlap = !c->profiling && c->thermo_tau <= 0.0 && (x_out || v_out || f_out);
+    for (double* p : {x_out, v_out, f_out})
+        if (overlap && p && !host_view(c, p, n3)) overlap = false;
+    if (!overlap) {
+        if ((rc = omdg_step(c, nsteps))) return rc;
+        if (!x_out && !v_out && !f_out) return OMDG_OK;
+        return omdg_get_state(c, x_out, v_out, f_out, nullptr, nullptr);
+    }
+    if ((rc = omdg_step_async(c, nsteps - 1))) return rc;  // also FirstRun and list upkeep
+    if (!c->list_valid) {
+        if ((rc = build_list(c))) return rc;
+        if ((rc = threebody_prepare(c))) return rc;
+    }
+    GraphState& gs = g_graphs[c];
+    double* key[3] = {x_out, v_out, f_out};
+    if (!gs.io_valid || gs.io_key[0] != x_out || gs.io_key[1] != v_out || gs.io_key[2] != f_out) {
+        if (gs.io_exec) cudaGraphExecDestroy(gs.io_exec);
+        if (gs.io_graph) cudaGraphDestroy(gs.io_graph);
+        gs.io_exec = nullptr;
+        gs.io_graph = nullptr;
+        gs.io_valid = false;
+        if ((rc = capture_step(c, gs, key))) return rc;
+    }
+    if (c->async_steps == 0) c->launches_at_sync = c->launches;
+    cudaError_t e = cudaGraphLaunch(gs.io_exec, c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "graph launch");
+    c->graph_steps += 1;
+    c->launches += gs.io_kernels;
+    c->async_steps += 1;
+    return omdg_sync(c);
+}
+
 int omdg_replica_ledger(omdg_ctx* c, int nrep, double* kinetic, double* potential) {
     if (!c || nrep != c->nrep) return c ? set_error(c, OMDG_EINVAL, "nrep differs from the context's") : OMDG_EINVAL;
     cudaSetDevice(c->device);
@@ -1533,6 +1630,7 @@ static int* launch_knob(Context* c, const std::string& k) {
     if (k == "tb_lanes") return &c->tb_lanes;
     if (k == "nbr_hshift") return &c->nbr_hshift;
     if (k == "build_lanes") return &c->build_lanes;
+    if (k == "io_blocks") return &c->io_blocks;
     return nullptr;
 }
 
@@ -1544,6 +1642,7 @@ static bool valid_knob(const std::string& k, int v) {
     if (k == "eam_ctas_per_sm") return v >= 1 && v <= 32;
     if (k == "eam_stage") return v == 0 || v == 1;
     if (k == "build_lanes") return v == 0 || v == 1 || v == 4 || v == 8;
+    if (k == "io_blocks") return v >= 1 && v <= 65535;
     return false;
 }
 

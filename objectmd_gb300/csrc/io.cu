@@ -4,6 +4,8 @@
 // doubles, which is what an Object-MD application's host mirror of Atom
 // x/v/f needs (SyncData points, gadget.h:212-213).  Pinned host arrays are
 // read and written by the kernels themselves (no staging copy).
+#include <algorithm>
+
 #include "device_common.cuh"
 
 namespace omdg {
@@ -29,8 +31,10 @@ __global__ void __launch_bounds__(IO_BLOCK) k_soa_to_rows(int n, const int* __re
 }
 
 // Positions, velocities and forces to caller-order rows in one pass (any
-// output may be null): a block gathers its atoms' nine values, then writes
-// the three row segments.  Forces are FP32 arrays, or FP64 interleaved.
+// output may be null): a block gathers the nine values of IO_BLOCK atoms,
+// then writes the three row segments; blocks stride over the chunks, so a
+// small grid can run beside other kernels.  Forces are FP32 arrays, or
+// FP64 interleaved.
 __global__ void __launch_bounds__(IO_BLOCK) k_state_to_rows(int n, const int* __restrict__ inv,
                                                             const double* __restrict__ x, const double* __restrict__ y,
                                                             const double* __restrict__ z, const double* __restrict__ vx,
@@ -40,24 +44,28 @@ __global__ void __launch_bounds__(IO_BLOCK) k_state_to_rows(int n, const int* __
                                                             const double* __restrict__ f64, double* __restrict__ ox,
                                                             double* __restrict__ ov, double* __restrict__ of) {
     __shared__ double s[3][3 * IO_BLOCK];
-    const int b0 = blockIdx.x * IO_BLOCK, cnt = min(IO_BLOCK, n - b0), t = threadIdx.x;
-    if (t < cnt) {
-        const int i = inv[b0 + t];
-        if (ox) s[0][3 * t] = x[i], s[0][3 * t + 1] = y[i], s[0][3 * t + 2] = z[i];
-        if (ov) s[1][3 * t] = vx[i], s[1][3 * t + 1] = vy[i], s[1][3 * t + 2] = vz[i];
-        if (of) {
-            if (f64) {
-                const double* r = f64 + 3 * (size_t)i;
-                s[2][3 * t] = r[0], s[2][3 * t + 1] = r[1], s[2][3 * t + 2] = r[2];
-            } else {
-                s[2][3 * t] = fx[i], s[2][3 * t + 1] = fy[i], s[2][3 * t + 2] = fz[i];
+    const int t = threadIdx.x;
+    for (int b0 = blockIdx.x * IO_BLOCK; b0 < n; b0 += gridDim.x * IO_BLOCK) {
+        const int cnt = min(IO_BLOCK, n - b0);
+        if (t < cnt) {
+            const int i = inv[b0 + t];
+            if (ox) s[0][3 * t] = x[i], s[0][3 * t + 1] = y[i], s[0][3 * t + 2] = z[i];
+            if (ov) s[1][3 * t] = vx[i], s[1][3 * t + 1] = vy[i], s[1][3 * t + 2] = vz[i];
+            if (of) {
+                if (f64) {
+                    const double* r = f64 + 3 * (size_t)i;
+                    s[2][3 * t] = r[0], s[2][3 * t + 1] = r[1], s[2][3 * t + 2] = r[2];
+                } else {
+                    s[2][3 * t] = fx[i], s[2][3 * t + 1] = fy[i], s[2][3 * t + 2] = fz[i];
+                }
             }
         }
+        __syncthreads();
+        if (ox) io_stage_out<3>(s[0], b0, cnt, ox);
+        if (ov) io_stage_out<3>(s[1], b0, cnt, ov);
+        if (of) io_stage_out<3>(s[2], b0, cnt, of);
+        __syncthreads();  // the next chunk reuses the staging
     }
-    __syncthreads();
-    if (ox) io_stage_out<3>(s[0], b0, cnt, ox);
-    if (ov) io_stage_out<3>(s[1], b0, cnt, ov);
-    if (of) io_stage_out<3>(s[2], b0, cnt, of);
 }
 
 // Caller-order force rows to the sorted FP32 arrays (and the FP64 forces,
@@ -158,6 +166,19 @@ int io_get_state(Context* c, double* x, double* v, double* f, double* pot, doubl
         finish(vir, d, n);
     }
     return check_cuda(c, cudaGetLastError(), "state read-back");
+}
+
+// Positions, velocities and/or forces written by one kernel on stream s
+// straight into the caller's pinned host arrays (every non-null pointer
+// must pass host_view); the step graph's download branches use it.
+int io_rows_to_host(Context* c, cudaStream_t s, double* x, double* v, double* f) {
+    const int n = c->n;
+    // a bounded grid: the link, not the SMs, sets the pace, and the force
+    // and kick kernels running beside it keep the rest of the GPU
+    const int g = std::min((n + IO_BLOCK - 1) / IO_BLOCK, c->io_blocks);
+    k_state_to_rows<<<g, IO_BLOCK, 0, s>>>(n, c->inv, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz,
+                                           c->use_f64 ? c->f64 : nullptr, x, v, f);
+    return check_cuda(c, cudaGetLastError(), "state download");
 }
 
 // Upload positions and/or velocities given in caller order (positions also

@@ -219,6 +219,7 @@ struct Context {
 
     // launch shapes (defaults; the tuner may change them)
     int num_sms = 152;
+    int io_blocks = 152;       // blocks of the download kernels beside a step (omdg_step_io)
     int build_lanes = 0;       // list build: 1, 4, 8 threads per atom; 0 cell-centric (shared memory)
                                // on grids of >= 8 atoms per cell, else one thread per atom
     int nbr_hshift = 3;        // sliced-ELL slice height H = 2^hshift
@@ -345,6 +346,7 @@ int step_state_graph_rebuilds(Context* c, int* nrebuild);
 // or registered host arrays are read and written by the kernels directly;
 // other host memory goes through the device staging buffer and one copy.
 const double* host_view(Context* c, const double* p, size_t count);
+int io_rows_to_host(Context* c, cudaStream_t s, double* x, double* v, double* f);  // pinned outputs, one kernel
 int io_get_state(Context* c, double* x, double* v, double* f, double* pot, double* vir);
 int io_set_state(Context* c, const double* x, const double* v);
 int io_set_forces(Context* c, const double* f);

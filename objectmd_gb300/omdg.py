@@ -89,6 +89,7 @@ SIGNATURES = {
     "omdg_set_positions": [_vp, _P(_d)],
     "omdg_set_velocities": [_vp, _P(_d)],
     "omdg_set_state": [_vp, _P(_d), _P(_d)],
+    "omdg_step_io": [_vp, _P(_d), _P(_d), _i, _P(_d), _P(_d), _P(_d)],
     "omdg_add_eam": [_vp, _i, _i, _cp],
     "omdg_add_pair_table": [_vp, _i, _i, _cp, _i],
     "omdg_add_sw": [_vp, _i, _i, _cp],
@@ -542,6 +543,17 @@ class Context:
     def step(self, nsteps=1):
         self._check(self.lib.omdg_step(self.h, int(nsteps)))
 
+    def step_io(self, nsteps=1, x_in=None, v_in=None, x_out=None, v_out=None, f_out=None):
+        """Upload, nsteps steps and read-back in one call (omdg_step_io); outputs are
+        caller-provided float64 (n, 3) arrays, written in place (pinned ones while
+        the last step runs)."""
+        arr = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1, 3)  # noqa: E731
+        for a in (x_out, v_out, f_out):
+            if a is not None and not (a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]):
+                raise ValueError("outputs must be C-contiguous float64 arrays")
+        self._check(self.lib.omdg_step_io(self.h, _dp(arr(x_in)), _dp(arr(v_in)), int(nsteps), _dp(x_out),
+                                          _dp(v_out), _dp(f_out)))
+
     def step_async(self, nsteps=1):
         self._check(self.lib.omdg_step_async(self.h, int(nsteps)))
 
@@ -657,7 +669,7 @@ class Context:
 
     def launch_shapes(self):
         keys = ("eam_block", "eam_lanes", "eam_stage", "eam_ctas_per_sm", "pair_block", "pair_lanes", "tb_block",
-                "tb_lanes", "nbr_hshift", "build_lanes")
+                "tb_lanes", "nbr_hshift", "build_lanes", "io_blocks")
         return {k: self.get_launch(k) for k in keys}
 
     def autotune(self, reps=3):

@@ -226,3 +226,38 @@ def test_pinned_transfers_equal_staged_transfers(omdg_lib):
         ctx.set_positions(np.array(x))  # the same positions from pageable memory
         ctx.compute_forces()
         np.testing.assert_array_equal(ctx.get_state()["f"], f_pinned)
+
+
+@pytest.mark.parametrize("rebuild_every", [0, 1])
+def test_step_io_equals_upload_step_readback(omdg_lib, rebuild_every):
+    """omdg_step_io (upload, steps, read-back in one call) gives bit for bit
+    what set_state + step + get_state give: with pinned outputs (written by
+    the step graph's download branch while the last step runs; with a list
+    rebuild in every step the positions are read after its permutation), with
+    pageable outputs, and again after the output arrays change."""
+    torch = pytest.importorskip("torch")
+    d = load_case("eam_al_500")
+    n = len(d["x0"])
+    pin = lambda: torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+    rng = np.random.default_rng(3)
+    x_in = d["x0"] + rng.normal(size=(n, 3)) * 0.02
+    v_in = d["v0"] * 1.2
+    with make_eam(omdg_lib, d, rebuild_every=rebuild_every) as a, \
+            make_eam(omdg_lib, d, rebuild_every=rebuild_every) as b:
+        a.step(2)
+        b.step(2)
+        for outs in ((pin(), pin(), pin()), (pin(), pin(), pin()), (np.zeros((n, 3)), np.zeros((n, 3)),
+                                                                      np.zeros((n, 3)))):
+            x, v, f = outs
+            a.step_io(3, x_in=x_in, v_in=v_in, x_out=x, v_out=v, f_out=f)
+            b.set_state(x=x_in, v=v_in)
+            b.step(3)
+            st = b.get_state()
+            np.testing.assert_array_equal(x, st["x"])
+            np.testing.assert_array_equal(v, st["v"])
+            np.testing.assert_array_equal(f, st["f"])
+            ka, pa = a.ledger_history()
+            kb, pb = b.ledger_history()
+            np.testing.assert_array_equal(ka, kb)
+            np.testing.assert_array_equal(pa, pb)
+            x_in, v_in = st["x"], st["v"]

@@ -8,8 +8,8 @@
 //               x += dt v, refresh the FP32 position packs, flag a rebuild
 //               when an atom moved more than skin/2 since the last build
 //   kick        v += dt/2 f/m, block partials of sum m v^2, sum potential,
-//               sum virial (FP32 pairs within a block, FP64 across blocks,
-//               fixed order); the last block writes the ledger row, the
+//               sum virial (FP32 pairs, fixed order; FP64 for the totals
+//               only); the last block writes the ledger row, the
 //               thermostat factor and the step counter
 //
 // GB300's FP64 pipe is about 1/64 of its FP32 pipe: the FP64 instructions
@@ -50,7 +50,7 @@ struct IntParams {
     int need_vmax;                       // measure SqrMaxVelocity (DynamicTimeStep)
 };
 
-__global__ void __launch_bounds__(256) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
+__global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
                                                     double* __restrict__ z, double* __restrict__ vx,
                                                     double* __restrict__ vy, double* __restrict__ vz,
                                                     const float* __restrict__ fx, const float* __restrict__ fy,
@@ -147,48 +147,66 @@ struct FinParams {
     double src_start, src_stop;
 };
 
+// Block partials: sum m v^2, sum potential, sum virial as FP32 pairs, and
+// the block's largest squared speed as the bit pattern of a non-negative
+// double (integer order is value order): two float4 per block.
+struct BlockPartial {
+    float4 ke, wv;  // (k.hi, k.lo, e.hi, e.lo), (w.hi, w.lo, vmax bits low, high)
+};
+
+__device__ __forceinline__ unsigned long long vmax_bits(const float4& wv) {
+    return ((unsigned long long)__float_as_uint(wv.w) << 32) | __float_as_uint(wv.z);
+}
+
 // Ledger row, thermostat factor and step counter from the block partials
 // (one block; each thread sums a contiguous run of partials, then a fixed
-// xor tree per warp and over the warps).  Partials are read through L2:
-// other blocks wrote them.
-__device__ void finalize_block(const FinParams& p, int nblocks, const double* partial, double* ledger,
+// xor tree per warp and over the warps, all on FP32 pairs; FP64 only for
+// the totals).  Partials are read through L2: other blocks wrote them.
+__device__ void finalize_block(const FinParams& p, int nblocks, const BlockPartial* partial, double* ledger,
                                StepState* st) {
-    __shared__ double sk[RED_BLOCK / 32], se[RED_BLOCK / 32], sw[RED_BLOCK / 32], sv[RED_BLOCK / 32];
-    double k = 0, e = 0, w = 0, vm = 0;
+    __shared__ F2 sk[RED_BLOCK / 32], se[RED_BLOCK / 32], sw[RED_BLOCK / 32];
+    __shared__ unsigned long long sv[RED_BLOCK / 32];
+    F2 kf = {0.f, 0.f}, ef = {0.f, 0.f}, wf = {0.f, 0.f};
+    unsigned long long vb = 0ull;
     const int per = (nblocks + RED_BLOCK - 1) / RED_BLOCK;
     const int b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
+#pragma unroll 4
     for (int b = b0; b < b1; b++) {
-        k += __ldcg(partial + 4 * b);
-        e += __ldcg(partial + 4 * b + 1);
-        w += __ldcg(partial + 4 * b + 2);
-        if (p.need_vmax) vm = fmax(vm, __ldcg(partial + 4 * b + 3));
+        const float4 ke = __ldcg(&partial[b].ke), wv = __ldcg(&partial[b].wv);
+        kf = f2_add(kf, F2{ke.x, ke.y});
+        ef = f2_add(ef, F2{ke.z, ke.w});
+        wf = f2_add(wf, F2{wv.x, wv.y});
+        if (p.need_vmax) vb = max(vb, vmax_bits(wv));
     }
     // fixed xor tree within each warp, then over the warps in warp 0
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int o = 16; o > 0; o >>= 1) {
-        k += __shfl_xor_sync(0xffffffffu, k, o);
-        e += __shfl_xor_sync(0xffffffffu, e, o);
-        w += __shfl_xor_sync(0xffffffffu, w, o);
-        if (p.need_vmax) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+        kf = f2_add(kf, f2_shfl_xor(kf, o));
+        ef = f2_add(ef, f2_shfl_xor(ef, o));
+        wf = f2_add(wf, f2_shfl_xor(wf, o));
+        if (p.need_vmax) vb = max(vb, __shfl_xor_sync(0xffffffffu, vb, o));
     }
     if (lane == 0) {
-        sk[warp] = k;
-        se[warp] = e;
-        sw[warp] = w;
-        sv[warp] = vm;
+        sk[warp] = kf;
+        se[warp] = ef;
+        sw[warp] = wf;
+        sv[warp] = vb;
     }
     __syncthreads();
     if (warp != 0) return;
-    k = lane < RED_BLOCK / 32 ? sk[lane] : 0.0;
-    e = lane < RED_BLOCK / 32 ? se[lane] : 0.0;
-    w = lane < RED_BLOCK / 32 ? sw[lane] : 0.0;
-    vm = lane < RED_BLOCK / 32 ? sv[lane] : 0.0;
+    const F2 z = {0.f, 0.f};
+    kf = lane < RED_BLOCK / 32 ? sk[lane] : z;
+    ef = lane < RED_BLOCK / 32 ? se[lane] : z;
+    wf = lane < RED_BLOCK / 32 ? sw[lane] : z;
+    vb = lane < RED_BLOCK / 32 ? sv[lane] : 0ull;
     for (int o = RED_BLOCK / 64; o > 0; o >>= 1) {
-        k += __shfl_xor_sync(0xffffffffu, k, o);
-        e += __shfl_xor_sync(0xffffffffu, e, o);
-        w += __shfl_xor_sync(0xffffffffu, w, o);
-        if (p.need_vmax) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+        kf = f2_add(kf, f2_shfl_xor(kf, o));
+        ef = f2_add(ef, f2_shfl_xor(ef, o));
+        wf = f2_add(wf, f2_shfl_xor(wf, o));
+        if (p.need_vmax) vb = max(vb, __shfl_xor_sync(0xffffffffu, vb, o));
     }
+    const double k = f2_to_double(kf), e = f2_to_double(ef), w = f2_to_double(wf);
+    const double vm = __longlong_as_double((long long)vb);
     if (threadIdx.x == 0) {
         double kinetic = 0.5 * k;
         if (!(isfinite(kinetic) && isfinite(e))) atomicOr(p.status, ERR_NONFINITE);
@@ -244,19 +262,19 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const double* pa
 
 // Second half kick v += dt/2 f/m (kick = 1) and the energy ledger: per
 // atom m v^2, the potential and the virial as FP32 pairs, a fixed xor tree
-// per warp and over the warps, FP64 block partials; the last block to
+// per warp and over the warps, FP32-pair block partials; the last block to
 // finish sums the partials in block order (finalize_block).
-__global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, FinParams f, double* __restrict__ vx,
+__global__ void __launch_bounds__(RED_BLOCK, 8) k_kick(IntParams p, FinParams f, double* __restrict__ vx,
                                                     double* __restrict__ vy, double* __restrict__ vz,
                                                     const float* __restrict__ fx, const float* __restrict__ fy,
                                                     const float* __restrict__ fz, const double* __restrict__ f64,
                                                     const int* __restrict__ type, const float* __restrict__ pe,
                                                     const float* __restrict__ vir,
-                                                    const unsigned* __restrict__ aflag, double* __restrict__ partial,
+                                                    const unsigned* __restrict__ aflag, BlockPartial* __restrict__ partial,
                                                     double* __restrict__ ledger, StepState* st, int kick) {
     const int i = blockIdx.x * RED_BLOCK + threadIdx.x;
     F2 k = {0.f, 0.f}, e = {0.f, 0.f}, w = {0.f, 0.f};
-    double vmax = 0.0;
+    unsigned long long vmax = 0ull;  // bits of the largest squared speed
     // inactive atoms: not integrated, not measured (system.cpp:1067, :1085)
     if (i < p.n && (!aflag || (aflag[i] & 1u))) {
         const int t = type[i];
@@ -282,17 +300,18 @@ __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, FinParams f, do
         e = p.use_f64 ? f2_from(f64[3 * (size_t)p.n + i]) : F2{pe[i], 0.f};
         w = F2{vir[i], 0.f};
         if (p.need_vmax)  // sqrv = vx*vx + vy*vy + vz*vz (system.cpp:1086)
-            vmax = __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz));
+            vmax = (unsigned long long)__double_as_longlong(
+                __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz)));
     }
     if (p.need_vmax)
-        for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        for (int o = 16; o > 0; o >>= 1) vmax = max(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
     for (int o = 16; o > 0; o >>= 1) {
         k = f2_add(k, f2_shfl_xor(k, o));
         e = f2_add(e, f2_shfl_xor(e, o));
         w = f2_add(w, f2_shfl_xor(w, o));
     }
     __shared__ F2 wk[RED_BLOCK / 32], we[RED_BLOCK / 32], ww[RED_BLOCK / 32];
-    __shared__ double wv[RED_BLOCK / 32];
+    __shared__ unsigned long long wv[RED_BLOCK / 32];
     __shared__ bool last;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) {
@@ -313,13 +332,12 @@ __global__ void __launch_bounds__(RED_BLOCK) k_kick(IntParams p, FinParams f, do
             w = f2_add(w, f2_shfl_xor(w, o));
         }
         if (lane == 0) {
-            double bv = 0.0;
+            unsigned long long bv = 0ull;
             if (p.need_vmax)
-                for (int q = 0; q < RED_BLOCK / 32; q++) bv = fmax(bv, wv[q]);
-            partial[4 * blockIdx.x + 0] = f2_to_double(k);
-            partial[4 * blockIdx.x + 1] = f2_to_double(e);
-            partial[4 * blockIdx.x + 2] = f2_to_double(w);
-            partial[4 * blockIdx.x + 3] = bv;
+                for (int q = 0; q < RED_BLOCK / 32; q++) bv = max(bv, wv[q]);
+            partial[blockIdx.x].ke = make_float4(k.hi, k.lo, e.hi, e.lo);
+            partial[blockIdx.x].wv = make_float4(w.hi, w.lo, __uint_as_float((unsigned)bv),
+                                                 __uint_as_float((unsigned)(bv >> 32)));
             __threadfence();
             last = atomicAdd(f.ticket, 1u) == gridDim.x - 1;
         }
@@ -599,7 +617,8 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
     }
     prof_begin(c, "kick");
     k_kick<<<nb, RED_BLOCK, 0, c->stream>>>(p, f, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz, c->f64, c->type, c->pe,
-                                            c->vir, c->flags_used ? c->aflag : nullptr, c->d_red, c->d_ledger,
+                                            c->vir, c->flags_used ? c->aflag : nullptr,
+                                            reinterpret_cast<BlockPartial*>(c->d_red), c->d_ledger,
                                             reinterpret_cast<StepState*>(c->d_state), kick);
     prof_end(c);
     c->launches += 1;

@@ -405,6 +405,20 @@ int omdg_get_timestep(omdg_ctx* ctx, double* dt, double* elapsed);
    is refused; there are no ghost atoms to include. */
 int omdg_dump_atoms(omdg_ctx* ctx, const char* path, int mode, int posprec, int valprec, const char* material,
                     int ninfo, const char* const* info, const int* gid);
+/* ThermoDetector's data file (ThermoDetector.h:100-115, 232-420, through
+   DataDumper::Measure, DataDumper.h): the detector (omdg_set_thermo_detector)
+   must have run on the current state (a step or omdg_compute_forces).  Info
+   lines: "$ DetectorVolume" (4/3 pi ercut^3), the caller's lines, then
+   "$ Temperature <T> K (kinetic)", "$ Pressure <P> GPa" (the system's, about
+   the centre-of-mass velocity, over the active atoms' bounding box) and
+   "$ Time <elapsed>"; per atom the columns temp press dens after x y z, in
+   aux_format (NULL: "%0.5e"), then the mode's fields as omdg_dump_atoms.
+   summary (may be NULL) receives 5 values: system temperature (K), system
+   pressure (GPa), and the averages of the local temperature, density and
+   pressure (ThermoDetector's GetTemperatureAvg, GetDensityAvg,
+   GetPressureAvg). */
+int omdg_dump_thermo(omdg_ctx* ctx, const char* path, int mode, int posprec, int valprec, const char* material,
+                     int ninfo, const char* const* info, const char* aux_format, double* summary);
 /* SysMonitor (SysMonitor.h): appends the md.out lines of the steps completed
    by the last omdg_step / omdg_sync with Step % every == 0 and Step != 0:
    "Step ElapsedTime TimeStep Ek Ep E" with SysMonitor's formats, from the

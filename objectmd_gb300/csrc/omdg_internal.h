@@ -332,6 +332,7 @@ int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask);
 int nn_launch(Context* c, Potential& pot, bool first);
 int replica_prepare(Context* c);  // per-replica cell grids and shifts (host, before a build)
 int thermo_detect(Context* c);    // local temperatures after a step (ttm.cu)
+double thermo_ercut(const Context* c);  // the detector's cutoff (its own, else the largest force cutoff); -1: off
 int ttm_pre(Context* c);          // electron temperature step and rescaling before a step
 void ttm_release(Context* c);
 bool ttm_active(const Context* c);

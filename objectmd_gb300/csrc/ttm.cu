@@ -334,6 +334,11 @@ static ThermoParams th_params(const Context* c, const TTMCtx& t) {
     return p;
 }
 
+double thermo_ercut(const Context* c) {
+    if (!c->ttm) return -1.0;
+    return c->ttm->ercut > 0 ? c->ttm->ercut : c->rc_max;
+}
+
 int thermo_detect(Context* c) {
     TTMCtx& t = *c->ttm;
     int rc = th_ensure(c, t);

@@ -152,6 +152,7 @@ SIGNATURES = {
     "omdg_get_timestep": [_vp, _P(_d), _P(_d)],
     "omdg_add_energy_source": [_vp, _d, _d, _d],
     "omdg_dump_atoms": [_vp, _cp, _i, _i, _i, _cp, _i, _P(_cp), _P(_i)],
+    "omdg_dump_thermo": [_vp, _cp, _i, _i, _i, _cp, _i, _P(_cp), _cp, _P(_d)],
     "omdg_monitor_append": [_vp, _cp, _i, _i],
     "omdg_checkpoint_write": [_cp, _cp, _P(SimVars), _i, _P(_cp), _P(_cp), _i, _P(ContainerDesc), _vp, _cp, _i],
     "omdg_checkpoint_info": [_cp, _P(_i), _P(_i), _P(_i), _cp, _i],
@@ -582,6 +583,18 @@ class Context:
         lines = _strings(list(info))
         self._check(self.lib.omdg_dump_atoms(self.h, path.encode(), int(mode), int(posprec), int(valprec),
                                              material.encode(), len(info), lines, None if g is None else _ip(g)))
+
+    def dump_thermo(self, path, mode=0, posprec=5, valprec=5, material="", info=(), aux_format=None):
+        """omdg_dump_thermo: ThermoDetector's data file of the current state; returns the
+        system temperature and pressure and the local averages."""
+        if not isinstance(mode, int):
+            mode = sum(self.WM[m] for m in mode)
+        lines = _strings(list(info))
+        out = (_d * 5)()
+        self._check(self.lib.omdg_dump_thermo(self.h, path.encode(), int(mode), int(posprec), int(valprec),
+                                              material.encode(), len(info), lines,
+                                              aux_format.encode() if aux_format else None, out))
+        return dict(zip(("temperature", "pressure", "avg_temperature", "avg_density", "avg_pressure"), out))
 
     def monitor_append(self, path, every=1, header=False):
         """omdg_monitor_append: SysMonitor's md.out lines of the last step call."""

@@ -291,7 +291,7 @@ def berendsen_factor(dt, tau, tset, tnow):
 def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh=0, dump_nbr=False,
                   pair2=None, tcontrol=None, table_dir=None, swfix=False, time_only=False, timeout=3600, ttm=None,
                   save=None, cont=None, damp=None, clamp=None, dyndt=None, range_border=None, dump=None,
-                  monitor=None, source=None):
+                  monitor=None, source=None, thermodump=False):
     """Run the reference's own code (oracle/_ref/ref_driver) on an Import file.
 
     Returns a dict with 'atoms' (nid, tid, x, v, f, potential, virial sorted
@@ -301,6 +301,8 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
     damp (factor), clamp (axes), dyndt (maxpath, max, update), range_border:
     the impact-run modifies on every atom; the result then also holds 'times'
     (Step, TimeStep, ElapsedTime per step) and 'active' (nid, flag bit).
+    thermodump: an intensive ThermoDetector whose data file of the final
+    state is returned as 'thermo_dump' (bytes) with 'thermo' (nid T_i n_i).
     """
     exe = REF_DRIVER_SWFIX if swfix else REF_DRIVER
     if not os.path.exists(exe):
@@ -327,6 +329,8 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
         args += ["dump", os.path.abspath(dump[0]), str(int(dump[1]))]
     if monitor:  # (file, every): SysMonitor
         args += ["monitor", os.path.abspath(monitor[0]), str(int(monitor[1]))]
+    if thermodump:  # ThermoDetector's data file after the run: <out>/thermo.001
+        args += ["thermodump", "thermo"]
     if save:
         args += ["save", os.path.abspath(save)]
     if cont:
@@ -361,4 +365,7 @@ def run_reference(import_file, kind, table, steps=0, dt=0.001, skin=0.3, refresh
         fp = os.path.join(out, name + ".txt")
         if os.path.exists(fp):
             res[name] = np.loadtxt(fp, ndmin=2)
+    tp = os.path.join(out, "thermo.001")
+    if os.path.exists(tp):
+        res["thermo_dump"] = open(tp, "rb").read()
     return res

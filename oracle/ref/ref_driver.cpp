@@ -35,6 +35,9 @@
  *   source      <energy> <start> <width>  EnergySource, pulse mode (source.* parameters)
  *   dump        <file> <mode>  after the run, DumpAtoms(file, mode) (container.cpp:417-519)
  *   monitor     <file> <every> SysMonitor(file) with monitor.every (SysMonitor.h)
+ *   thermodump  <name>   an intensive ThermoDetector (ThermoDetector.h) whose data
+ *                        file (DataDumper::Measure) is written once after the run:
+ *                        <outdir>/<name>.001
  *   save        <file>   after the run, the reference's binary checkpoint
  *                        (MDSystemGrid::SaveSimulation, systemgrid.cpp:848-852)
  *   continue    <file>   resume from a binary checkpoint (CONTINUE_MODE,
@@ -154,11 +157,13 @@ public:
             AddForce(k, "target", "target");
             AddForce(new TForcePair(pair2), "projectile", "target");
         }
-        if (opt.count("ttm")) {
-            thermo = new ThermoDetector(1e30);  // sample time beyond the run: no dump files
+        if (opt.count("ttm") || opt.count("thermodump")) {
+            // sample time beyond the run: no dump files during it
+            thermo = new ThermoDetector(1e30, -1.0, outdir + "/" + get("thermodump", "thermo"));
+            thermo->SetIntensive(true);
             AddDetector(thermo);
-            AddModify(new TTM_Homogen());
         }
+        if (opt.count("ttm")) AddModify(new TTM_Homogen());
         if (opt.count("tcontrol"))
             AddModify(new TempController(atof(get("tcontrol", "300", 0).c_str()),
                                          atof(get("tcontrol", "0.1", 1).c_str())));
@@ -237,6 +242,7 @@ public:
         if (get("dump_nbr", "0") != "0") DumpNeighbours();
         if (opt.count("dump")) DumpAtoms(get("dump", "dump.dat", 0), atoi(get("dump", "0", 1).c_str()));
         if (opt.count("save")) SaveSimulation(get("save", ""));
+        if (opt.count("thermodump")) thermo->Measure();  // the detector's data file of the final state
         if (timelog) {
             fclose(timelog);
             timelog = 0;

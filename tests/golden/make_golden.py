@@ -150,6 +150,24 @@ def output_case(tdir):
     print("wrote output_eam_al_500")
 
 
+def thermo_case(tdir):
+    """ThermoDetector's data file (intensive, ercut = the EAM cutoff) of EAM
+    Al FCC 8^3 = 2048 atoms (periodic, 300 K) after 6 steps of 2 fs, with the
+    binary checkpoint of the same state.  The box is large enough for atoms
+    farther than two cutoffs from every face, where the reference's ghost
+    copies do not enter the local temperatures."""
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=8, a=4.05, sigma=0.05, temp=300.0, seed_pos=12, seed_vel=13)
+    work = tempfile.mkdtemp(prefix="omdthermo_")
+    f = os.path.join(work, "eam_al_2048.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), periodic=(True, True, True), species=("aluminum",))
+    ck = os.path.join(work, "final.bin")
+    res = oc.run_reference(f, "eam", "aluminum5000", steps=6, dt=0.002, table_dir=tdir, thermodump=True, save=ck)
+    raw = lambda b: np.frombuffer(b, dtype=np.uint8)  # noqa: E731
+    np.savez_compressed(os.path.join(GOLD, "thermo_eam_al_2048.npz"), thermo_dump=raw(res["thermo_dump"]),
+                        checkpoint=raw(open(ck, "rb").read()), thermo=res["thermo"])
+    print("wrote thermo_eam_al_2048")
+
+
 MODIFY_CASES = {  # the impact-run modifies on every atom of an EAM Al slab
     "damp_clamp": dict(damp=0.05, clamp="xyz"),
     "dyndt": dict(dyndt=(0.02, 0.004, 3)),
@@ -190,6 +208,9 @@ def main(only=None):
         return
     if only == "output":
         output_case(table_dir())
+        return
+    if only == "thermo":
+        thermo_case(table_dir())
         return
     if only == "modifies":
         modifies_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
@@ -273,6 +294,7 @@ def main(only=None):
     checkpoint_case(tdir)
     modifies_case(tdir, work)
     output_case(tdir)
+    thermo_case(tdir)
     print("done")
 
 

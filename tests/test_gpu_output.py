@@ -107,3 +107,61 @@ def test_dump_and_monitor_after_steps(omdg_lib, golden, tmp_path):
         assert abs(ek - rek) <= 1e-6 * abs(rek)
         # Ep = P - P0 and E differ by the potential's 5e-8 relative tolerance (|P| ~ 1670 eV)
         assert abs(ep - rep) <= 2e-4 and abs(e - re_) <= 2e-4
+
+
+def test_thermo_dump_of_a_loaded_state(omdg_lib, tmp_path):
+    """ThermoDetector's data file (tests/golden/thermo_eam_al_2048.npz: the
+    reference's intensive detector on periodic EAM Al 2048 after 6 steps,
+    with the checkpoint of that state): loaded here, forces evaluated, the
+    same file.  Headers equal line for line except the pressure value (it
+    carries the FP32 per-atom virials: 1e-5 relative).  Per atom, keyed by
+    the printed position: the density as printed for every atom; the
+    temperature as printed and the local pressure within 1e-5 relative +
+    1e-4 GPa for the atoms farther than two detector cutoffs from every
+    periodic face.  (Nearer a face the reference sums neighbours' kinetic
+    energies about the centre-of-mass velocities of their ghost copies,
+    taken over the ghosts' neighbours inside the ghost shell only; here an
+    image neighbour uses its owner's full neighbourhood.  An FP64
+    restatement of this detector agrees with the reference to 5e-16 there.)"""
+    g = np.load(os.path.join(GOLD, "thermo_eam_al_2048.npz"))
+    ck = tmp_path / "final.bin"
+    ck.write_bytes(g["checkpoint"].tobytes())
+    out = str(tmp_path / "thermo.001")
+    ercut = 5.558  # the EAM cutoff: the detector's default
+    with omdg_lib.Context(0) as ctx:
+        ctx.load_simulation(str(ck))
+        ctx.add_eam(EAM_TABLE)
+        ctx.set_neighbor(0.3, 1)
+        ctx.set_thermo_detector(True)
+        ctx.compute_forces()
+        summ = ctx.dump_thermo(out, mode=0, material="aluminum", info=INFO)
+    h1, b1 = split(open(out).read())
+    h2, b2 = split(text(g["thermo_dump"]))
+    assert len(h1) == len(h2) and len(b1) == len(b2)
+    for l1, l2 in zip(h1, h2):
+        if l1.startswith("#$ Pressure"):
+            p1, p2 = float(l1.split()[2]), float(l2.split()[2])
+            assert abs(p1 - p2) <= 1e-5 * abs(p2) + 1e-5, (l1, l2)
+            assert abs(summ["pressure"] - p2) <= 1e-5 * abs(p2) + 1e-5
+        else:
+            assert l1 == l2
+    t_sys = float([l for l in h2 if l.startswith("#$ Temperature")][0].split()[2])
+    assert abs(summ["temperature"] - t_sys) <= 1e-5 * t_sys
+    box = [float(t) for t in [l for l in h2 if l.startswith("#$ Box")][0].split()[2:]]
+    lo, hi = np.array(box[:3]), np.array(box[3:])
+    ref = {tuple(l.split()[:3]): fields(l) for l in b2}
+    deep = 0
+    for l in b1:
+        key = tuple(l.split()[:3])
+        assert key in ref, key
+        x, (t, p, n) = np.array(fields(l)[:3]), fields(l)[3:]
+        rt, rp, rn = ref[key][3:]
+        # printed with 6 significant digits: equal, or one unit of the last
+        # digit apart where an FP64 value sits on a rounding boundary
+        assert abs(n - rn) <= 1.01e-5 * abs(rn)
+        if ((x - lo) > 2 * ercut).all() and ((hi - x) > 2 * ercut).all():
+            deep += 1
+            assert abs(t - rt) <= 1.01e-5 * abs(rt), (key, t, rt)
+            assert abs(p - rp) <= 1e-5 * abs(rp) + 1e-4, (key, p, rp)
+    assert deep >= 50
+    assert summ["avg_temperature"] > 0 and summ["avg_density"] > 0

@@ -422,7 +422,11 @@ int omdg_dump_thermo(omdg_ctx* ctx, const char* path, int mode, int posprec, int
 /* SysMonitor (SysMonitor.h): appends the md.out lines of the steps completed
    by the last omdg_step / omdg_sync with Step % every == 0 and Step != 0:
    "Step ElapsedTime TimeStep Ek Ep E" with SysMonitor's formats, from the
-   device ledger; header != 0 truncates the file and writes the label line. */
+   device ledger; with the thermo detector on, also ThermoDetector's slots
+   temp: avtemp: pres: avpres: (system temperature, average local
+   temperature, system pressure, average local pressure; %0.3E), measured
+   on the device after every step.  header != 0 truncates the file and
+   writes the label line. */
 int omdg_monitor_append(omdg_ctx* ctx, const char* path, int every, int header);
 
 /* ------------------------------------------------------------ checkpoints */

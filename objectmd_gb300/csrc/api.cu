@@ -939,7 +939,7 @@ static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr)
     if (!rc) rc = forces_compute(c);
     if (!rc && io) rc = branch(1, nullptr, nullptr, io[2]);
     if (!rc) rc = integrate_kick(c, 0);
-    if (!rc && c->ttm) rc = thermo_detect(c);  // ExecuteDetectors (system.cpp:976)
+    if (!rc && c->ttm) rc = thermo_detect(c, true);  // ExecuteDetectors (system.cpp:976)
     if (!rc && io) rc = branch(2, nullptr, io[1], nullptr);
     if (!rc && io_launches > 0) {  // join the branch
         e = cudaEventRecord(gs.io_ev[3], gs.io_side);
@@ -1042,7 +1042,7 @@ int omdg_compute_forces(omdg_ctx* c) {
     if ((rc = threebody_prepare(c))) return rc;
     if ((rc = forces_compute(c))) return rc;
     if ((rc = measure_energies(c, 0))) return rc;
-    if (c->ttm && (rc = thermo_detect(c))) return rc;
+    if (c->ttm && (rc = thermo_detect(c, false))) return rc;
     prof_collect(c);
     if ((rc = check_status(c))) return rc;
     // a non-step evaluation writes the ledger row the next step would use
@@ -1235,7 +1235,7 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         if ((rc = threebody_prepare(c))) return rc;
         if ((rc = step_state_init(c))) return rc;
         // TTM's first PreIntegration only measures (TTM_Homogen_SCNA.h:356-366)
-        if (c->ttm && (rc = thermo_detect(c))) return rc;
+        if (c->ttm && (rc = thermo_detect(c, false))) return rc;
         if ((rc = forces_compute(c))) return rc;
         c->first_measure = true;  // DynamicTimeStep's Step-0 update follows this measurement
         rc = measure_energies(c, 0);
@@ -1265,7 +1265,7 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
             if ((rc = eager_maybe_rebuild(c))) return rc;
             if ((rc = forces_compute(c))) return rc;
             if ((rc = integrate_kick(c, k))) return rc;
-            if (c->ttm && (rc = thermo_detect(c))) return rc;
+            if (c->ttm && (rc = thermo_detect(c, true))) return rc;
         }
         prof_collect(c);
     } else {

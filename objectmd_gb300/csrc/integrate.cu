@@ -712,6 +712,10 @@ __global__ void k_rewind(StepState* st, int rebuild_every) {
 }
 
 // Ledger rows restart at 0 for the next omdg_step call (stream ordered, no wait).
+// Device address of the step state's ledger row counter (read by kernels
+// that fill columns of the current row).
+const int* step_state_row(Context* c) { return &reinterpret_cast<StepState*>(c->d_state)->row; }
+
 int step_state_rewind(Context* c) {
     k_rewind<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state), c->rebuild_every);
     c->launches++;

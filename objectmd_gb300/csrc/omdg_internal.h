@@ -270,7 +270,9 @@ struct Context {
     double* d_red = nullptr;        // block partials
     int red_cap = 0;
     double* d_ledger = nullptr;     // per step LEDGER_W doubles: kinetic, potential, virial, lambda,
-                                    // Step, ElapsedTime (both before the step's increment), TimeStep
+                                    // Step, ElapsedTime (both before the step's increment), TimeStep, 0,
+                                    // and with the thermo detector its system temperature, average
+                                    // local temperature, system pressure, average local pressure
     int ledger_cap = 0;
     double* h_ledger = nullptr;     // pinned copy
     void* h_sync = nullptr;         // pinned staging of the status word and the step state
@@ -331,7 +333,8 @@ int gather_slots(Context* c, bool zero_virial);
 int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask);
 int nn_launch(Context* c, Potential& pot, bool first);
 int replica_prepare(Context* c);  // per-replica cell grids and shifts (host, before a build)
-int thermo_detect(Context* c);    // local temperatures after a step (ttm.cu)
+int thermo_detect(Context* c, bool after_step);  // local thermodynamics (ttm.cu); after_step: the step advanced the ledger row
+const int* step_state_row(Context* c);           // device address of the ledger row counter (integrate.cu)
 double thermo_ercut(const Context* c);  // the detector's cutoff (its own, else the largest force cutoff); -1: off
 int ttm_pre(Context* c);          // electron temperature step and rescaling before a step
 void ttm_release(Context* c);
@@ -356,7 +359,7 @@ int post_force_modifies(Context* c);  // ForceDamper / CoordClamp after the forc
 int io_set_flags(Context* c, const unsigned* flags, unsigned keep_mask);  // caller order; bits in keep_mask survive
 int io_get_flags(Context* c, unsigned* flags);
 
-constexpr int LEDGER_W = 8;  // doubles per ledger row
+constexpr int LEDGER_W = 12;  // doubles per ledger row
 
 // Atom group g as its flag bit (bits 8..15); -1: every atom.
 inline unsigned group_bits(int g) { return g < 0 ? ~0u : (1u << (8 + g)); }

@@ -213,14 +213,19 @@ int omdg_monitor_append(omdg_ctx* ctx, const char* path, int every, int header) 
     if (!c || !path || every < 1) return OMDG_EINVAL;
     FILE* fo = std::fopen(path, header ? "w" : "a");
     if (!fo) return set_error(c, OMDG_EFILE, std::string("unable to create file ") + path);
-    if (header) std::fputs("#@ t: dt: Ek: Ep: E: \n", fo);  // SysMonitor::Measure's label line
+    // a thermo detector registers four more slots (ThermoDetector.h:118-127)
+    const bool thermo = thermo_ercut(c) > 0;
+    if (header)  // SysMonitor::Measure's label line
+        std::fputs(thermo ? "#@ t: dt: Ek: Ep: E: temp: avtemp: pres: avpres: \n" : "#@ t: dt: Ek: Ep: E: \n", fo);
     for (int k = 0; k < c->last_rows; k++) {
         const double* r = c->h_ledger + (size_t)LEDGER_W * k;
         const int step = (int)r[4];
         if (step == 0 || step % every) continue;  // Detect: Step % every; Measure skips Step 0
         const double ep = r[1] - c->base_potential;             // RelPotential
         const double e = r[0] + r[1] - c->base_potential;       // MechanicEnergy
-        std::fprintf(fo, "%d %0.6E %0.3E %0.10E %0.10E %0.10E \n", step, r[5], r[6], r[0], ep, e);
+        std::fprintf(fo, "%d %0.6E %0.3E %0.10E %0.10E %0.10E ", step, r[5], r[6], r[0], ep, e);
+        if (thermo) std::fprintf(fo, "%0.3E %0.3E %0.3E %0.3E ", r[8], r[9], r[10], r[11]);
+        std::fputs("\n", fo);
     }
     const bool ok = !std::ferror(fo);
     std::fclose(fo);

@@ -15,6 +15,7 @@
 //   k_ttm_sum       one block: integrated lattice energy
 // Distances as CalcDistance: an FP32 screen from the position packs, and
 // sqrt((dx dx + dy dy) + dz dz) <= ercut in FP64 near the edge.
+#include <cfloat>
 #include <cmath>
 #include <string>
 
@@ -110,15 +111,32 @@ __device__ __forceinline__ double th_ek(int j, const double* __restrict__ vx, co
     return mj * (cx * cx + cy * cy + cz * cz);
 }
 
+// Block partials of the detector, per block TH_Q doubles: 0 sum T_i, 1 sum
+// n_i, 2 count (atoms with n_i >= 2), 3 sum m v^2 (every atom), 4 max v^2
+// (the two-temperature model's); over active atoms (MeasureSystemTempPres,
+// ExtractPressure): 5-7 sum m v, 8 sum m, 9 sum m v^2, 10 sum virial, 11 sum
+// local pressure, 12 count, 13-15 min x y z, 16-18 max x y z.
+constexpr int TH_Q = 19;
+constexpr double TH_GPA = 160.22;  // MD_GIGAPASCAL (conversion.h:39)
+
+__device__ __forceinline__ bool th_is_max(int q) { return q == 4 || q >= 16; }
+__device__ __forceinline__ bool th_is_min(int q) { return q >= 13 && q < 16; }
+
+__device__ __forceinline__ double th_combine(int q, double a, double b) {
+    return th_is_max(q) ? fmax(a, b) : (th_is_min(q) ? fmin(a, b) : a + b);
+}
+
 __global__ void __launch_bounds__(TH_BLOCK) k_thermo_temp(
     ThermoParams p, const PosPack* __restrict__ pack, const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
     const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
     const double* __restrict__ vx, const double* __restrict__ vy, const double* __restrict__ vz,
     const int* __restrict__ type, const double* __restrict__ mass, const double* __restrict__ vcm,
-    const int* __restrict__ nneig, double* __restrict__ temp, double* __restrict__ dens, double* __restrict__ partial) {
-    __shared__ double st[5][TH_BLOCK];
+    const int* __restrict__ nneig, const float* __restrict__ vir, const unsigned* __restrict__ aflag,
+    double* __restrict__ temp, double* __restrict__ dens, double* __restrict__ partial) {
+    __shared__ double st[TH_Q][TH_BLOCK];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double a_t = 0.0, a_d = 0.0, a_n = 0.0, kin = 0.0, v2max = 0.0;
+    double q[TH_Q];
+    for (int k = 0; k < TH_Q; k++) q[k] = th_is_max(k) && k != 4 ? -DBL_MAX : (th_is_min(k) ? DBL_MAX : 0.0);
     if (i < p.n) {
         const PosPack pi = pack[i];
         const double mi = mass[type[i]];
@@ -135,46 +153,60 @@ __global__ void __launch_bounds__(TH_BLOCK) k_thermo_temp(
         const double dn = (double)nn / p.volcut;
         temp[i] = t;
         dens[i] = dn;
-        if (nn >= 2) {
-            a_t = t;
-            a_d = dn;
-            a_n = 1.0;
+        const bool active = !aflag || (aflag[i] & 1u);
+        if (nn >= 2 && active) {
+            q[0] = t;
+            q[1] = dn;
+            q[2] = 1.0;
         }
         const double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
-        kin = mi * v2;
-        v2max = v2;
+        q[3] = mi * v2;
+        q[4] = v2;
+        if (active) {
+            q[5] = mi * vx[i];
+            q[6] = mi * vy[i];
+            q[7] = mi * vz[i];
+            q[8] = mi;
+            q[9] = mi * v2;
+            q[10] = (double)vir[i];
+            // a_i = Unit->Pressure(n_i virial_i / 6 + sumek_i / (3 V)), sumek_i = 2 T_i n_i / fac
+            q[11] = TH_GPA * dn * ((double)vir[i] / 6.0 + 2.0 * t / (3.0 * p.fac));
+            q[12] = 1.0;
+            q[13] = q[16] = x[i];
+            q[14] = q[17] = y[i];
+            q[15] = q[18] = z[i];
+        }
     }
-    st[0][threadIdx.x] = a_t;
-    st[1][threadIdx.x] = a_d;
-    st[2][threadIdx.x] = a_n;
-    st[3][threadIdx.x] = kin;
-    st[4][threadIdx.x] = v2max;
+    for (int k = 0; k < TH_Q; k++) st[k][threadIdx.x] = q[k];
     __syncthreads();
     for (int off = TH_BLOCK / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off) {
-            for (int q = 0; q < 4; q++) st[q][threadIdx.x] += st[q][threadIdx.x + off];
-            st[4][threadIdx.x] = fmax(st[4][threadIdx.x], st[4][threadIdx.x + off]);
-        }
+        if (threadIdx.x < off)
+            for (int k = 0; k < TH_Q; k++)
+                st[k][threadIdx.x] = th_combine(k, st[k][threadIdx.x], st[k][threadIdx.x + off]);
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        for (int q = 0; q < 5; q++) partial[5 * (size_t)blockIdx.x + q] = st[q][0];
+        for (int k = 0; k < TH_Q; k++) partial[TH_Q * (size_t)blockIdx.x + k] = st[k][0];
 }
 
-__global__ void k_thermo_final(int nblocks, const double* __restrict__ partial, TTMState* st) {
-    __shared__ double red[5][256];
-    double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
-        for (int q = 0; q < 4; q++) a[q] += partial[5 * (size_t)b + q];
-        a[4] = fmax(a[4], partial[5 * (size_t)b + 4]);
-    }
-    for (int q = 0; q < 5; q++) red[q][threadIdx.x] = a[q];
+// The detector's totals (one block, fixed order).  With a ledger row, its
+// columns 8-11 take SysMonitor's temp:, avtemp:, pres:, avpres: slots
+// (ThermoDetector.h:118-127): the system temperature about the
+// centre-of-mass velocity and pressure over the active atoms' bounding box
+// (MeasureSystemTempPres, :329-420), the average local temperature and
+// pressure.
+__global__ void k_thermo_final(int nblocks, const double* __restrict__ partial, TTMState* st, double fac,
+                               double* ledger, int ledger_cap, const int* row, int shift) {
+    __shared__ double red[TH_Q][256];
+    double a[TH_Q];
+    for (int k = 0; k < TH_Q; k++) a[k] = th_is_max(k) && k != 4 ? -DBL_MAX : (th_is_min(k) ? DBL_MAX : 0.0);
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+        for (int k = 0; k < TH_Q; k++) a[k] = th_combine(k, a[k], partial[TH_Q * (size_t)b + k]);
+    for (int k = 0; k < TH_Q; k++) red[k][threadIdx.x] = a[k];
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off) {
-            for (int q = 0; q < 4; q++) red[q][threadIdx.x] += red[q][threadIdx.x + off];
-            red[4][threadIdx.x] = fmax(red[4][threadIdx.x], red[4][threadIdx.x + off]);
-        }
+        if (threadIdx.x < off)
+            for (int k = 0; k < TH_Q; k++) red[k][threadIdx.x] = th_combine(k, red[k][threadIdx.x], red[k][threadIdx.x + off]);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -184,6 +216,24 @@ __global__ void k_thermo_final(int nblocks, const double* __restrict__ partial, 
         st->navg = (int)cnt;
         st->kin = 0.5 * red[3][0];
         st->vmax2 = red[4][0];
+        if (ledger) {
+            // the row of the step just completed (shift 1), or of the
+            // measurement that does not advance the step (shift 0)
+            double* ledger_row = ledger + LEDGER_W * (size_t)(((*row - shift) % ledger_cap + ledger_cap) % ledger_cap);
+            const double msum = red[8][0], nact = red[12][0];
+            double twoek = red[9][0];  // sum m |v - v_cm|^2 = sum m v^2 - |sum m v|^2 / M
+            if (msum > 0.0)
+                twoek -= (red[5][0] * red[5][0] + red[6][0] * red[6][0] + red[7][0] * red[7][0]) / msum;
+            double vol = 1.0;
+            for (int d = 0; d < 3; d++) {
+                const double ext = red[16 + d][0] - red[13 + d][0];
+                vol *= ext > 0.0 ? ext : 1.0;
+            }
+            ledger_row[8] = nact > 0.0 ? fac * 0.5 * twoek / nact : 0.0;
+            ledger_row[9] = st->t_avg;
+            ledger_row[10] = TH_GPA * (0.5 * red[10][0] + twoek) / (3.0 * vol);
+            ledger_row[11] = nact > 0.0 ? red[11][0] / nact : 0.0;
+        }
     }
 }
 
@@ -304,7 +354,7 @@ static int th_ensure(Context* c, TTMCtx& t) {
     if (e == cudaSuccess) e = cudaMalloc(&t.temp, sizeof(double) * n);
     if (e == cudaSuccess) e = cudaMalloc(&t.dens, sizeof(double) * n);
     if (e == cudaSuccess) e = cudaMalloc(&t.nneig, sizeof(int) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&t.partial, sizeof(double) * 5 * t.nblocks);
+    if (e == cudaSuccess) e = cudaMalloc(&t.partial, sizeof(double) * TH_Q * t.nblocks);
     if (e == cudaSuccess && !t.st) {
         e = cudaMalloc(&t.st, sizeof(TTMState));
         TTMState h{};
@@ -339,7 +389,7 @@ double thermo_ercut(const Context* c) {
     return c->ttm->ercut > 0 ? c->ttm->ercut : c->rc_max;
 }
 
-int thermo_detect(Context* c) {
+int thermo_detect(Context* c, bool after_step) {
     TTMCtx& t = *c->ttm;
     int rc = th_ensure(c, t);
     if (rc) return rc;
@@ -351,8 +401,10 @@ int thermo_detect(Context* c) {
     k_thermo_cm<<<g, TH_BLOCK, 0, c->stream>>>(p, c->pack, nbr, c->nnb, c->x, c->y, c->z, c->vx, c->vy, c->vz,
                                                 c->type, c->d_mass, t.vcm, t.nneig);
     k_thermo_temp<<<g, TH_BLOCK, 0, c->stream>>>(p, c->pack, nbr, c->nnb, c->x, c->y, c->z, c->vx, c->vy, c->vz,
-                                                  c->type, c->d_mass, t.vcm, t.nneig, t.temp, t.dens, t.partial);
-    k_thermo_final<<<1, 256, 0, c->stream>>>(g, t.partial, t.st);
+                                                  c->type, c->d_mass, t.vcm, t.nneig, c->vir,
+                                                  c->flags_used ? c->aflag : nullptr, t.temp, t.dens, t.partial);
+    k_thermo_final<<<1, 256, 0, c->stream>>>(g, t.partial, t.st, p.fac, c->d_ledger, c->ledger_cap,
+                                             step_state_row(c), after_step ? 1 : 0);
     prof_end(c);
     c->launches += 3;
     return check_cuda(c, cudaGetLastError(), "thermo detector");

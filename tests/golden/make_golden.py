@@ -163,8 +163,16 @@ def thermo_case(tdir):
     ck = os.path.join(work, "final.bin")
     res = oc.run_reference(f, "eam", "aluminum5000", steps=6, dt=0.002, table_dir=tdir, thermodump=True, save=ck)
     raw = lambda b: np.frombuffer(b, dtype=np.uint8)  # noqa: E731
+    # SysMonitor with the detector's slots, every 2 of 6 steps, on a free EAM
+    # Al cluster (no ghost copies: the local averages are the reference's too)
+    cx, cv, (clo, chi) = inputs.aluminium_cluster(ncell=6, temp=300.0)
+    cf = os.path.join(work, "al_cluster.dat")
+    inputs.write_import(cf, cx, cv, box=(clo, chi), periodic=(False, False, False), species=("aluminum",))
+    md = os.path.join(work, "md.out")
+    oc.run_reference(cf, "eam", "aluminum5000", steps=6, dt=0.002, table_dir=tdir, thermodump=True, monitor=(md, 2))
     np.savez_compressed(os.path.join(GOLD, "thermo_eam_al_2048.npz"), thermo_dump=raw(res["thermo_dump"]),
-                        checkpoint=raw(open(ck, "rb").read()), thermo=res["thermo"])
+                        checkpoint=raw(open(ck, "rb").read()), thermo=res["thermo"], monitor=raw(open(md, "rb").read()),
+                        cluster_x=cx, cluster_v=cv, cluster_lo=clo, cluster_hi=chi)
     print("wrote thermo_eam_al_2048")
 
 

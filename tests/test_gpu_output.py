@@ -165,3 +165,37 @@ def test_thermo_dump_of_a_loaded_state(omdg_lib, tmp_path):
             assert abs(p - rp) <= 1e-5 * abs(rp) + 1e-4, (key, p, rp)
     assert deep >= 50
     assert summ["avg_temperature"] > 0 and summ["avg_density"] > 0
+
+
+def test_monitor_with_thermo_detector_slots(omdg_lib, tmp_path):
+    """SysMonitor with a ThermoDetector registered (tests/golden/
+    thermo_eam_al_2048.npz: the reference's md.out on a free EAM Al cluster
+    of 864 atoms, 6 steps of 2 fs, every 2): the same label line with
+    temp: avtemp: pres: avpres:, those four printed as %0.3E and within 2e-3
+    relative + 2e-3 (GPa) of the reference's: system temperature about the
+    centre-of-mass velocity, average local temperature, system pressure over
+    the atoms' bounding box and average local pressure (FP32 virials)."""
+    from objectmd_gb300 import inputs
+
+    g = np.load(os.path.join(GOLD, "thermo_eam_al_2048.npz"))
+    md = str(tmp_path / "md.out")
+    with omdg_lib.Context(0) as ctx:
+        ctx.set_box(g["cluster_lo"], g["cluster_hi"], (False, False, False))
+        ctx.set_atoms(g["cluster_x"], g["cluster_v"], masses=[inputs.md_mass("aluminum")], znum=[13.0])
+        ctx.add_eam(EAM_TABLE)
+        ctx.set_neighbor(0.3, 1)
+        ctx.set_timestep(0.002)
+        ctx.set_thermo_detector(True)
+        ctx.step(6)
+        ctx.monitor_append(md, every=2, header=True)
+    m1 = open(md).read().splitlines()
+    m2 = text(g["monitor"]).splitlines()
+    assert m1[0] == m2[0] and len(m1) == len(m2)
+    slot = re.compile(r"^-?\d\.\d{3}E[+-]\d{2}$")
+    for l1, l2 in zip(m1[1:], m2[1:]):
+        t1, t2 = l1.split(), l2.split()
+        assert len(t1) == len(t2) == 10
+        assert t1[:3] == t2[:3]
+        assert all(slot.match(t) for t in t1[6:])
+        for a, b in zip(t1[6:], t2[6:]):
+            assert abs(float(a) - float(b)) <= 2e-3 * abs(float(b)) + 2e-3, (l1, l2)

@@ -109,6 +109,17 @@ def dist_env():
     return rank, world, local
 
 
+def slowest_rank_ms(total_ms, world, torch, device):
+    """The timed region of the slowest rank (each rank's sum of its step
+    times; replicas only, so this max is the one collective)."""
+    if world <= 1:
+        return total_ms
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -296,12 +307,7 @@ def run_gpu(args):
     clk = clocks.stop()
     st1 = ctx.stats()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-        torch.distributed.barrier()
+    total_ms = slowest_rank_ms(sum(step_ms), world, torch, "cuda")
     value = world * n * args.steps / (total_ms * 1e-3)
     launches = st1["launches"] - st0["launches"]
     rebuilds = st1["rebuilds"] - st0["rebuilds"]

@@ -127,14 +127,15 @@ static void free_atoms(Context* c) {
     void* ptrs[] = {c->x,    c->y,     c->z,      c->vx,     c->vy,          c->vz,          c->fx,
                     c->fy,   c->fz,    c->pe,     c->vir,    c->pack,        c->xref,        c->loc,         c->type,
                     c->id,   c->inv,   c->fp,     c->femb,   c->cell,        c->perm,        c->stage_d,
-                    c->stage_i, c->cell_sorted, c->f64, c->extra, c->stage_extra, c->nnb, c->d_red, c->aflag};
+                    c->stage_i, c->cell_sorted, c->f64, c->extra, c->stage_extra, c->nnb, c->d_red, c->aflag,
+                    c->ters_wide};
     for (void* p : ptrs) cudaFree(p);
     c->x = c->y = c->z = c->vx = c->vy = c->vz = nullptr;
     c->fx = c->fy = c->fz = c->pe = c->vir = nullptr;
     c->pack = nullptr;
     c->xref = nullptr;
     c->loc = nullptr;
-    c->type = c->id = c->inv = nullptr;
+    c->type = c->id = c->inv = c->ters_wide = nullptr;
     c->fp = c->femb = nullptr;
     c->cell = c->perm = nullptr;
     c->stage_d = nullptr;
@@ -157,7 +158,7 @@ static int alloc_atoms(Context* c, int n) {
               dalloc(c->xref, cap) && dalloc(c->loc, cap) && dalloc(c->type, cap) && dalloc(c->id, cap) && dalloc(c->inv, cap) &&
               dalloc(c->fp, cap) && dalloc(c->femb, cap) && dalloc(c->cell, cap) && dalloc(c->perm, cap) &&
               dalloc(c->stage_d, (size_t)6 * cap) && dalloc(c->stage_i, (size_t)3 * cap) && dalloc(c->aflag, cap) &&
-              dalloc(c->cell_sorted, cap) && dalloc(c->nnb, cap);
+              dalloc(c->cell_sorted, cap) && dalloc(c->nnb, cap) && dalloc(c->ters_wide, (size_t)cap + 1);
     int nb = grid_for(cap, 256) + 1;
     ok = ok && dalloc(c->d_red, (size_t)4 * nb);
     if (!ok) return set_error(c, OMDG_ENOMEM, "atom arrays");

@@ -208,6 +208,7 @@ struct Context {
     int* nnb = nullptr;
     int* rev = nullptr;       // slot of i in row j (three-body kernels)
     float4* slot_buf = nullptr;  // per-slot force contributions (three-body kernels)
+    int* ters_wide = nullptr;    // Tersoff centres past the register path: [0] count, then their indices
     int maxnb = 0;
     long nbr_bytes = 0;
     double skin = 0.3;

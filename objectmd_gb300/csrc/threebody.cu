@@ -429,12 +429,12 @@ __device__ __noinline__ void ters_centre_wide(const TersDev& p, int i, const Pos
 
 constexpr int TERS_REG = 4;  // in-cutoff neighbours the register path holds (diamond: 4)
 
-__global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __restrict__ pack,
+__global__ void __launch_bounds__(128, 6) k_tersoff_a(TersDev p, const PosPack* __restrict__ pack,
                                                    const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                    float4* __restrict__ slot, float* __restrict__ fx,
                                                    float* __restrict__ fy, float* __restrict__ fz,
                                                    float* __restrict__ pe, float* __restrict__ vir, unsigned* status,
-                                                   const int* __restrict__ mask) {
+                                                   const int* __restrict__ mask, int* __restrict__ wide) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     if (mask && !mask[i]) return;  // centres another potential evaluates
@@ -462,8 +462,8 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
             slot[at] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
-    if (nc > TERS_REG) {
-        ters_centre_wide(p, i, pi, L, pack, nbr, m, slot, fx, fy, fz, pe, vir, status);
+    if (nc > TERS_REG) {  // queued for k_tersoff_wide, so its warp does not wait on it
+        wide[1 + atomicAdd(wide, 1)] = i;
         return;
     }
     float fix = 0.f, fiy = 0.f, fiz = 0.f, ei = 0.f, wi = 0.f;
@@ -473,6 +473,23 @@ __global__ void __launch_bounds__(128) k_tersoff_a(TersDev p, const PosPack* __r
     for (int a = 0; a < TERS_REG; a++)
         if (a < nc) slot[nbr_at(i, sl[a], p.hshift, p.maxnb)] = make_float4(skx[a], sky[a], skz[a], 0.f);
     ters_store(p, i, fix, fiy, fiz, ei, wi, fx, fy, fz, pe, vir);
+}
+
+// The queued centres (wide[0] of them, indices from wide[1]): a grid-stride
+// loop, so the few centres of a collision cascade run in dense warps.
+__global__ void __launch_bounds__(128) k_tersoff_wide(TersDev p, const PosPack* __restrict__ pack,
+                                                      const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                                      const int* __restrict__ wide, float4* __restrict__ slot,
+                                                      float* __restrict__ fx, float* __restrict__ fy,
+                                                      float* __restrict__ fz, float* __restrict__ pe,
+                                                      float* __restrict__ vir, unsigned* status) {
+    const int cnt = wide[0];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+        const int i = wide[1 + k];
+        const PosPack pi = pack[i];
+        const ShiftF L = p.rep_L ? p.rep_L[p.rep_of[i]] : p.L;
+        ters_centre_wide(p, i, pi, L, pack, nbr, nnb[i], slot, fx, fy, fz, pe, vir, status);
+    }
 }
 
 // ------------------------------------------------------------------ ZBL pair
@@ -647,11 +664,15 @@ int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask) {
     p.rc2 = p.rc * p.rc * 1.0001f;
     p.first = first ? 1 : 0;
     prof_begin(c, mask ? "tersoff_fallback" : "tersoff_centre");
+    cudaMemsetAsync(c->ters_wide, 0, sizeof(int), c->stream);
     k_tersoff_a<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr),
                                                              c->nnb, c->slot_buf, c->fx, c->fy, c->fz, c->pe, c->vir,
-                                                             c->d_status, mask);
+                                                             c->d_status, mask, c->ters_wide);
+    k_tersoff_wide<<<2 * c->num_sms, 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr),
+                                                          c->nnb, c->ters_wide, c->slot_buf, c->fx, c->fy, c->fz,
+                                                          c->pe, c->vir, c->d_status);
     prof_end(c);
-    c->launches++;
+    c->launches += 2;
     return check_cuda(c, cudaGetLastError(), "tersoff");
 }
 

@@ -20,6 +20,22 @@ namespace omdg {
 
 constexpr int TB_MAXN = 24;  // neighbours within the cutoff one atom can hold
 
+// f(b) for the in-cutoff neighbours b < nc: fully unrolled over K (the
+// arrays f touches stay in registers), or a rolled loop over local arrays
+// (then the kernel's register count stays that of the unrolled path).
+template <int K, bool UNR, class F>
+__device__ __forceinline__ void for_nbrs(int nc, F&& f) {
+    if constexpr (UNR) {
+#pragma unroll
+        for (int b = 0; b < K; b++)
+            if (b < nc) f(b);
+    } else {
+#pragma unroll 1
+        for (int b = 0; b < nc; b++) f(b);
+    }
+}
+
+
 struct SWDev {
     int n, hshift, maxnb, single_type, ta;
     ShiftF L;
@@ -71,13 +87,12 @@ __device__ __forceinline__ void sw_two_body(const SWDev& p, float r, float& fr, 
     }
 }
 
-__global__ void __launch_bounds__(128) k_sw_a(SWDev p, const PosPack* __restrict__ pack,
-                                              const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
-                                              float4* __restrict__ slot, float* __restrict__ fx,
-                                              float* __restrict__ fy, float* __restrict__ fz, float* __restrict__ pe,
-                                              unsigned* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+// A centre with more in-cutoff neighbours than the register path holds:
+// up to TB_MAXN of them over local arrays (the two-body terms as well).
+__device__ __noinline__ void sw_centre_wide(const SWDev& p, int i, const PosPack* __restrict__ pack,
+                                            const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                            float4* __restrict__ slot, float* __restrict__ fx, float* __restrict__ fy,
+                                            float* __restrict__ fz, float* __restrict__ pe, unsigned* status) {
     const PosPack pi = pack[i];
     const int ti = pack_type(pi.hi);
     const bool mine = p.single_type || ti == p.ta;
@@ -187,6 +202,139 @@ __global__ void __launch_bounds__(128) k_sw_a(SWDev p, const PosPack* __restrict
     }
 }
 
+constexpr int SW_REG = 8;  // in-cutoff neighbours the register path holds (diamond: 4 + thermal second shell)
+
+__device__ __forceinline__ void sw_store(const SWDev& p, int i, float ax, float ay, float az, float ae,
+                                         float* __restrict__ fx, float* __restrict__ fy, float* __restrict__ fz,
+                                         float* __restrict__ pe) {
+    if (p.first) {
+        fx[i] = ax;
+        fy[i] = ay;
+        fz[i] = az;
+        pe[i] = ae;
+    } else {
+        fx[i] += ax;
+        fy[i] += ay;
+        fz[i] += az;
+        pe[i] += ae;
+    }
+}
+
+// Pass A of SW for centre i with up to SW_REG in-cutoff neighbours in
+// registers (fully unrolled loops, insertion by select); centres with more
+// are queued for k_sw_wide.  Same terms and summation order as the wide
+// path.
+__global__ void __launch_bounds__(128) k_sw_a(SWDev p, const PosPack* __restrict__ pack,
+                                              const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                              float4* __restrict__ slot, float* __restrict__ fx,
+                                              float* __restrict__ fy, float* __restrict__ fz, float* __restrict__ pe,
+                                              unsigned* status, int* __restrict__ wide) {
+    constexpr int K = SW_REG;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const PosPack pi = pack[i];
+    const int ti = pack_type(pi.hi);
+    const bool mine = p.single_type || ti == p.ta;
+    const int m = nnb[i];
+    float vx[K], vy[K], vz[K], rr[K];
+    int sl[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) vx[k] = vy[k] = vz[k] = 0.f, rr[k] = 1.f, sl[k] = 0;
+    int nc = 0;
+    float ax = 0.f, ay = 0.f, az = 0.f, ae = 0.f;
+    for (int s = 0; s < m; s++) {
+        const size_t at = nbr_at(i, s, p.hshift, p.maxnb);
+        slot[at] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!mine) continue;
+        const unsigned e = nbr[at];
+        const PosPack pj = pack[nbr_index(e)];
+        if (!p.single_type && pack_type(pj.hi) != p.ta) continue;
+        const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, p.L);  // x_i - x_j
+        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        if (!(r2 < p.rc2)) continue;
+        const float r = sqrtf(r2);
+        if (!(r < p.rc)) continue;  // r == rc: every SW term is zero (and 1/(r - rc) infinite)
+        float fr, he;
+        sw_two_body(p, r, fr, he);
+        ax += d.x * fr;
+        ay += d.y * fr;
+        az += d.z * fr;
+        ae += he;
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (k == nc) vx[k] = -d.x, vy[k] = -d.y, vz[k] = -d.z, rr[k] = r, sl[k] = s;
+        nc++;
+    }
+    if (nc > K) {  // queued: k_sw_wide evaluates the whole centre
+        wide[1 + atomicAdd(wide, 1)] = i;
+        return;
+    }
+    // triplets centred on i (sw.cpp:191-236), each unordered pair (j, k) once
+    float sjx[K], sjy[K], sjz[K], sje[K], ex[K], ir[K], gr[K];
+    for_nbrs<K, true>(nc, [&](int a) {
+        sjx[a] = sjy[a] = sjz[a] = sje[a] = 0.f;
+        const float ira = 1.0f / (rr[a] - p.rc), fira = p.c7 * ira;
+        ex[a] = expf(fira);
+        ir[a] = 1.0f / rr[a];
+        gr[a] = fira * ira * ir[a];
+    });
+    for_nbrs<K, true>(nc, [&](int a) {
+        const float dx1 = vx[a], dy1 = vy[a], dz1 = vz[a];
+        const float ex0 = ex[a], ir1 = ir[a], g0 = gr[a];
+        float gjx = 0.f, gjy = 0.f, gjz = 0.f, gje = 0.f;
+        for_nbrs<K, true>(nc, [&](int b) {
+            if (b <= a) return;
+            const float dx2 = vx[b], dy2 = vy[b], dz2 = vz[b];
+            const float ir2 = ir[b];
+            const float ir1r2 = ir1 * ir2;
+            const float fex = ex0 * ex[b];
+            const float cs = (dx1 * dx2 + dy1 * dy2 + dz1 * dz2) * ir1r2;
+            const float dcos = cs - p.c10;
+            const float ftheta = p.c9 * fex * dcos;
+            const float ft12 = ir1r2 * ftheta;
+            const float fpot = p.c8 * fex * dcos * dcos;
+            const float fcos = cs * ftheta;
+            const float fr0 = fpot * g0, fr1 = fpot * gr[b];
+            const float ft0 = fcos * ir1 * ir1, ft1 = fcos * ir2 * ir2;
+            const float fx0 = dx1 * (fr0 + ft0) - dx2 * ft12, fx1 = dx2 * (fr1 + ft1) - dx1 * ft12;
+            const float fy0 = dy1 * (fr0 + ft0) - dy2 * ft12, fy1 = dy2 * (fr1 + ft1) - dy1 * ft12;
+            const float fz0 = dz1 * (fr0 + ft0) - dz2 * ft12, fz1 = dz2 * (fr1 + ft1) - dz1 * ft12;
+            ax -= fx0 + fx1;
+            ay -= fy0 + fy1;
+            az -= fz0 + fz1;
+            const float third = fpot * (1.0f / 3.0f);
+            ae += third;
+            gjx += fx0;
+            gjy += fy0;
+            gjz += fz0;
+            gje += third;
+            sjx[b] += fx1;
+            sjy[b] += fy1;
+            sjz[b] += fz1;
+            sje[b] += third;
+        });
+        sjx[a] += gjx;
+        sjy[a] += gjy;
+        sjz[a] += gjz;
+        sje[a] += gje;
+    });
+    for_nbrs<K, true>(nc, [&](int a) {
+        slot[nbr_at(i, sl[a], p.hshift, p.maxnb)] = make_float4(sjx[a], sjy[a], sjz[a], sje[a]);
+    });
+    sw_store(p, i, ax, ay, az, ae, fx, fy, fz, pe);
+}
+
+// The queued centres (wide[0] of them, indices from wide[1]).
+__global__ void __launch_bounds__(128) k_sw_wide(SWDev p, const PosPack* __restrict__ pack,
+                                                 const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                                 const int* __restrict__ wide, float4* __restrict__ slot,
+                                                 float* __restrict__ fx, float* __restrict__ fy,
+                                                 float* __restrict__ fz, float* __restrict__ pe, unsigned* status) {
+    const int cnt = wide[0];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x)
+        sw_centre_wide(p, wide[1 + k], pack, nbr, nnb, slot, fx, fy, fz, pe, status);
+}
+
 // Gathers what every neighbour's pass A left for i; clears no state.
 __global__ void __launch_bounds__(128) k_slot_gather(int n, int hshift, int maxnb, const unsigned* __restrict__ nbr,
                                                      const int* __restrict__ nnb, const int* __restrict__ rev,
@@ -263,21 +411,6 @@ __device__ __forceinline__ float ters_fc(const TersDev& p, float r, float& dfc) 
     }
     dfc = 0.f;
     return 0.f;
-}
-
-// f(b) for the in-cutoff neighbours b < nc: fully unrolled over K (the
-// arrays f touches stay in registers), or a rolled loop over local arrays
-// (then the kernel's register count stays that of the unrolled path).
-template <int K, bool UNR, class F>
-__device__ __forceinline__ void for_nbrs(int nc, F&& f) {
-    if constexpr (UNR) {
-#pragma unroll
-        for (int b = 0; b < K; b++)
-            if (b < nc) f(b);
-    } else {
-#pragma unroll 1
-        for (int b = 0; b < nc; b++) f(b);
-    }
 }
 
 // The bonds centred on one atom, for its nc <= K in-cutoff neighbours
@@ -619,10 +752,15 @@ int sw_launch(Context* c, Potential& pot, bool first) {
     p.ze3 = (float)s.ze3;
     p.first = first ? 1 : 0;
     prof_begin(c, "sw_centre");
+    cudaMemsetAsync(c->ters_wide, 0, sizeof(int), c->stream);
     k_sw_a<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
-                                                        c->slot_buf, c->fx, c->fy, c->fz, c->pe, c->d_status);
+                                                        c->slot_buf, c->fx, c->fy, c->fz, c->pe, c->d_status,
+                                                        c->ters_wide);
+    k_sw_wide<<<2 * c->num_sms, 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb,
+                                                     c->ters_wide, c->slot_buf, c->fx, c->fy, c->fz, c->pe,
+                                                     c->d_status);
     prof_end(c);
-    c->launches++;
+    c->launches += 2;
     int rc = check_cuda(c, cudaGetLastError(), "sw");
     if (rc) return rc;
     return gather_slots(c, first);

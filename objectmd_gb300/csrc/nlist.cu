@@ -801,19 +801,26 @@ __global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildParams 
 }
 
 // rev at (i, s): the slot of (i, -image) in the row of j = nbr at (i, s).
+// For every list entry (i, s) -> j, the slot of i in row j: REV_LANES
+// threads per centre, each searching for every REV_LANES-th entry (the
+// searches are independent chains of loads; lanes keep more of them in
+// flight).
+constexpr int REV_LANES = 4;
+
 __global__ void k_reverse(int n, int hshift, int maxnb, const unsigned* __restrict__ nbr,
                           const int* __restrict__ nnb, int* __restrict__ rev, unsigned* status) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int i = (int)(t / REV_LANES), lane = (int)(t % REV_LANES);
     if (i >= n) return;
     int m = nnb[i];
-    for (int s = 0; s < m; s++) {
+    for (int s = lane; s < m; s += REV_LANES) {
         unsigned e = nbr[nbr_at(i, s, hshift, maxnb)];
         int j = nbr_index(e);
         unsigned want = nbr_encode(i, -nbr_sx(e), -nbr_sy(e), -nbr_sz(e));
         int mj = nnb[j], found = -1;
-        for (int t = 0; t < mj; t++)
-            if (nbr[nbr_at(j, t, hshift, maxnb)] == want) {
-                found = t;
+        for (int u = 0; u < mj; u++)
+            if (nbr[nbr_at(j, u, hshift, maxnb)] == want) {
+                found = u;
                 break;
             }
         if (found < 0) atomicOr(status, ERR_NBR_OVERFLOW);
@@ -1105,7 +1112,7 @@ int nlist_build(Context* c) {
     prof_end(c);
     if (c->need_rev) {
         prof_begin(c, "nlist_reverse");
-        k_reverse<<<grid_for(n, 128), 128, 0, s>>>(n, c->nbr_hshift, c->maxnb,
+        k_reverse<<<grid_for(n, 128 / REV_LANES), 128, 0, s>>>(n, c->nbr_hshift, c->maxnb,
                                                    reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->rev,
                                                    c->d_status);
         c->launches++;

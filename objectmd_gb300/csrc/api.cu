@@ -159,7 +159,7 @@ static int alloc_atoms(Context* c, int n) {
               dalloc(c->fp, cap) && dalloc(c->femb, cap) && dalloc(c->cell, cap) && dalloc(c->perm, cap) &&
               dalloc(c->stage_d, (size_t)6 * cap) && dalloc(c->stage_i, (size_t)3 * cap) && dalloc(c->aflag, cap) &&
               dalloc(c->cell_sorted, cap) && dalloc(c->nnb, cap) && dalloc(c->ters_wide, (size_t)cap + 1);
-    int nb = grid_for(cap, 256) + 1;
+    int nb = grid_for(cap, RED_BLOCK) + 1;
     ok = ok && dalloc(c->d_red, (size_t)4 * nb);
     if (!ok) return set_error(c, OMDG_ENOMEM, "atom arrays");
     c->cap = cap;

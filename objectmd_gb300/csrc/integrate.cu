@@ -127,7 +127,6 @@ __global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __re
     if (threadIdx.x == 0 && moved) st->rebuild = 1;
 }
 
-constexpr int RED_BLOCK = 256;
 
 struct FinParams {
     int natoms;
@@ -264,7 +263,7 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const BlockParti
 // atom m v^2, the potential and the virial as FP32 pairs, a fixed xor tree
 // per warp and over the warps, FP32-pair block partials; the last block to
 // finish sums the partials in block order (finalize_block).
-__global__ void __launch_bounds__(RED_BLOCK, 8) k_kick(IntParams p, FinParams f, double* __restrict__ vx,
+__global__ void __launch_bounds__(RED_BLOCK, 2048 / RED_BLOCK) k_kick(IntParams p, FinParams f, double* __restrict__ vx,
                                                     double* __restrict__ vy, double* __restrict__ vz,
                                                     const float* __restrict__ fx, const float* __restrict__ fy,
                                                     const float* __restrict__ fz, const double* __restrict__ f64,

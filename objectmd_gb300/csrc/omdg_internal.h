@@ -361,6 +361,7 @@ int io_set_flags(Context* c, const unsigned* flags, unsigned keep_mask);  // cal
 int io_get_flags(Context* c, unsigned* flags);
 
 constexpr int LEDGER_W = 12;  // doubles per ledger row
+constexpr int RED_BLOCK = 256;  // threads of the kick kernel's blocks (one 32-byte partial each)
 
 // Atom group g as its flag bit (bits 8..15); -1: every atom.
 inline unsigned group_bits(int g) { return g < 0 ? ~0u : (1u << (8 + g)); }

@@ -190,6 +190,13 @@ int omdg_set_compat(omdg_ctx* ctx, const char* key, int on);
 
 /* Number of neighbour-list builds so far and of kernel launches issued by the last omdg_step. */
 int omdg_stats(omdg_ctx* ctx, long* rebuilds, long* launches);
+/*
+ * No reference counterpart (the reference has one scalar loop per potential).
+ * Centres the last Stillinger-Weber or Tersoff force pass queued for the
+ * dense second pass (k_sw_wide / k_tersoff_wide: more in-cutoff neighbours
+ * than the register path holds, 8 for SW and 4 for Tersoff).  Synchronous.
+ */
+int omdg_wide_centres(omdg_ctx* ctx, int* count);
 
 /*
  * Launch shapes (no reference counterpart: the reference is scalar C++).
@@ -321,8 +328,9 @@ int omdg_nn_load(omdg_nn* nn, const char* path);
  * Work is queued on `stream` (a cudaStream_t; NULL = the legacy default
  * stream) of the current device and the call returns without waiting.
  *
- * Limits: n <= OMDG_STATIC_MAX_ATOMS; every periodic axis at least 3 rcut
- * long; the cell grid is coarsened to OMDG_STATIC_MAX_CELLS cells when the box
+ * Limits: n <= OMDG_STATIC_MAX_ATOMS; every periodic axis longer than 3 rcut
+ * (cells are at least rcut (1 + 1e-12) wide, so an axis of exactly 3 rcut is
+ * rejected); the cell grid is coarsened to OMDG_STATIC_MAX_CELLS cells when the box
  * holds more.  Scratch is one fixed __device__ array of about 1.4 MB per
  * device, shared by every call: calls that overlap in time (on different
  * streams, or from several host threads at once) race on it and give wrong
@@ -330,7 +338,10 @@ int omdg_nn_load(omdg_nn* nn, const char* path);
  * start at zero are cleared by each call itself.  The first call on a device
  * looks the scratch address up (cudaGetSymbolAddress, which also loads the
  * module's kernels), so make it once at setup, with that device current and
- * before any stream capture.
+ * before any stream capture.  That address is kept for the life of the
+ * process and never looked up again: after cudaDeviceReset (or anything else
+ * that destroys the device's primary context) it is stale, so do not call
+ * this entry point on that device again in the same process.
  *
  * Returns OMDG_OK, OMDG_EINVAL (bad argument, box too small), OMDG_ERANGE
  * (n above the limit) or OMDG_ECUDA; err (may be NULL) receives the message.

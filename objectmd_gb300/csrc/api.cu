@@ -1590,6 +1590,18 @@ int omdg_stats(omdg_ctx* c, long* rebuilds, long* launches) {
     return OMDG_OK;
 }
 
+int omdg_wide_centres(omdg_ctx* c, int* count) {
+    if (!c || !count) return OMDG_EINVAL;
+    *count = 0;
+    if (!c->ters_wide) return OMDG_OK;
+    int v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, c->ters_wide, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "omdg_wide_centres");
+    *count = v;
+    return OMDG_OK;
+}
+
 int omdg_set_profiling(omdg_ctx* c, int on) {
     if (!c) return OMDG_EINVAL;
     c->profiling = on != 0;

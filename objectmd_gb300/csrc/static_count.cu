@@ -226,8 +226,8 @@ extern "C" int omdg_count_neighbors_static(const double* x, int n, const double 
         g.nc[d] = (int)std::min(fit, 1024.0);
         if (g.periodic[d] && g.nc[d] < 3)
             return sc_fail(err, err_len, OMDG_EINVAL,
-                           "periodic axis %d is shorter than 3 rcut (%.6g < %.6g): too small for the static path", d,
-                           g.L[d], 3.0 * rcut);
+                           "periodic axis %d is not longer than 3 rcut (%.17g vs %.17g): too small for the static path",
+                           d, g.L[d], 3.0 * rcut);
         if (g.nc[d] < 1) g.nc[d] = 1;
     }
     // coarsen the widest axis until the grid fits the scratch (wider cells stay correct)

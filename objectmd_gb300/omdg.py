@@ -110,6 +110,7 @@ SIGNATURES = {
     "omdg_set_thermostat": [_vp, _d, _d],
     "omdg_set_compat": [_vp, _cp, _i],
     "omdg_stats": [_vp, _P(_l), _P(_l)],
+    "omdg_wide_centres": [_vp, _P(_i)],
     "omdg_set_launch": [_vp, _cp, _i],
     "omdg_get_launch": [_vp, _cp, _P(_i)],
     "omdg_autotune": [_vp, _i, _P(_d)],
@@ -666,6 +667,12 @@ class Context:
         r, l = _l(), _l()
         self._check(self.lib.omdg_stats(self.h, ctypes.byref(r), ctypes.byref(l)))
         return {"rebuilds": r.value, "launches": l.value}
+
+    def wide_centres(self):
+        """Centres the last SW/Tersoff force pass sent to the dense second pass."""
+        k = _i()
+        self._check(self.lib.omdg_wide_centres(self.h, ctypes.byref(k)))
+        return k.value
 
     def stream(self):
         s = _vp()

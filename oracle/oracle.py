@@ -36,9 +36,10 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_reference(ref_root: str = "/root/reference") -> bool:
-    """Compile the reference sources into oracle/_ref (only where they exist)."""
-    if not os.path.isdir(ref_root):
+def build_reference(ref_root: str) -> bool:
+    """Compile the reference sources found under ``ref_root`` (the Object-MD
+    source tree) into oracle/_ref; False where that tree is absent."""
+    if not ref_root or not os.path.isdir(ref_root):
         return False
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + ref_root, "-j8"])
     return os.path.exists(REF_DRIVER)

@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 from objectmd_gb300 import inputs  # noqa: E402
 from oracle import oracle as oc  # noqa: E402
 
-REF = os.environ.get("OMD_REFERENCE", "/root/reference")
+REF = os.environ.get("OMD_REFERENCE", "")  # the Object-MD source tree (required to generate)
 GOLD = os.path.join(ROOT, "tests", "golden")
 TABLES = os.path.join(GOLD, "tables")
 
@@ -73,8 +73,9 @@ def write_eam5000(path):
 def table_dir():
     """OMD_TABLE for reference runs: the reference tables plus the generated ones."""
     d = tempfile.mkdtemp(prefix="omdtab_")
-    for f in os.listdir(os.path.join(REF, "tables")):
-        os.symlink(os.path.join(REF, "tables", f), os.path.join(d, f))
+    if REF:
+        for f in os.listdir(os.path.join(REF, "tables")):
+            os.symlink(os.path.join(REF, "tables", f), os.path.join(d, f))
     for f in os.listdir(TABLES):
         dst = os.path.join(d, f)
         if os.path.lexists(dst):
@@ -206,6 +207,8 @@ def modifies_case(tdir, work):
 
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
+    if not REF:
+        raise SystemExit("make_golden.py: set OMD_REFERENCE to the Object-MD source tree")
     if not oc.build_reference(REF):
         raise SystemExit("reference sources not found at %s" % REF)
     if only == "ttm":

@@ -87,6 +87,50 @@ def test_tersoff_vs_oracle(omdg_lib, oracle_lib, ncell, sigma, temp):
     check(st["f"], fref, st["pot"], eref, etol=5e-6)
 
 
+def interstitial_silicon(ncell, seed):
+    """Diamond Si with three atoms planted on tetrahedral interstitial sites
+    ((1/2, 1/2, 1/2) of a cubic cell, relative to its first site): each has 4 neighbours at sqrt(3)/4 a
+    and 6 at a/2, inside both cutoffs, and its 4 nearest hosts gain a fifth."""
+    from objectmd_gb300 import inputs
+
+    a = 5.431
+    x, v, (lo, hi) = inputs.diamond_silicon(ncell=ncell, a=a, sigma=0.03, temp=1000.0, seed_pos=seed,
+                                            seed_vel=seed + 1)
+    cells = np.array([[1, 1, 1], [ncell // 2, 2, ncell - 2], [ncell - 2, ncell // 2, 3]], dtype=np.float64)
+    extra = np.array(lo)[None, :] + (cells + 0.5) * a + a / 8  # lattice sites are offset by a/8
+    rng = np.random.default_rng(seed + 2)
+    x = np.vstack([x, extra + rng.normal(0.0, 0.03, extra.shape)])
+    v = np.vstack([v, np.zeros_like(extra)])
+    return x, v, lo, hi
+
+
+@pytest.mark.parametrize("kind", ["sw", "tersoff"])
+def test_dense_centres_take_the_wide_kernel(omdg_lib, oracle_lib, kind):
+    """Centres with more in-cutoff neighbours than the register path holds go
+    to k_sw_wide / k_tersoff_wide; their forces must still match the oracle,
+    and the queue count shows that the dense pass ran."""
+    oc = oracle_lib
+    x, v, lo, hi = interstitial_silicon(6, 61)
+    box = oc.make_box(lo, hi, (1, 1, 1))
+    if kind == "sw":
+        p = oc.SWParam(eps=2.1683, A=7.049556277, B=0.6022245584, p=4, q=0, sigma=2.0951, a=1.80, lam=21.0,
+                       gamma=1.2, icos0=-3.0, usezbl=1, sx0=1.2107, sx1=1.8456, sa0=335.0594, sa1=-492.3905,
+                       sa2=244.5280, sa3=-41.2347, z1=14, z2=14)
+        fref, eref, _ = oc.sw(box, x, oc.neighbors(box, x, 2.0951 * 1.8 + 0.3), p)
+        etol = 2e-6
+    else:
+        p = oc.TersoffParam(A=3264.7, B=95.373, lambda1=3.2394, lambda2=1.3258, lambda3=1.3258, beta=0.33675,
+                            n=22.956, c=4.8381, d=2.0417, h=0.0, R=2.7, D=0.15)
+        fref, eref, _ = oc.tersoff(box, x, oc.neighbors(box, x, 2.85 + 0.3), p)
+        etol = 5e-6
+    with si_context(omdg_lib, x, v, lo, hi, kind) as ctx:
+        ctx.compute_forces()
+        st = ctx.get_state()
+        wide = ctx.wide_centres()
+    assert wide >= 3, wide
+    check(st["f"], fref, st["pot"], eref, etol=etol)
+
+
 def test_tersoff_nve_conserves_energy(omdg_lib):
     from objectmd_gb300 import inputs
 

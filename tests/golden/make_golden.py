@@ -205,6 +205,18 @@ def modifies_case(tdir, work):
     print("wrote modifies_eam_al_slab")
 
 
+def lj4000_case(tdir, work):
+    """Lennard-Jones argon as configured for the plain FP64 method: FCC 10^3
+    cells = 4000 atoms, a = 5.26 A, Maxwell-Boltzmann 100 K (seed 1, zero net
+    momentum), the 2.5 sigma LJ table, skin 0.3 A, 1000 NVE steps of 1 fs on
+    the reference's TForcePair; its final atoms and ledger."""
+    x, v, (lo, hi) = inputs.lj_argon(ncell=10, a=5.26, temp=100.0, seed_vel=1)
+    f = os.path.join(work, "lj_ar_4000.dat")
+    inputs.write_import(f, x, v, box=(lo, hi), species=("argon",))
+    res = oc.run_reference(f, "pair", "lj.argon", steps=1000, dt=0.001, table_dir=tdir)
+    save_case("lj_ar_4000", f, res, box_lo=lo, box_hi=hi, steps=np.array(1000), dt=np.array(0.001))
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not REF:
@@ -225,6 +237,9 @@ def main(only=None):
         return
     if only == "modifies":
         modifies_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
+        return
+    if only == "lj4000":
+        lj4000_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
         return
     write_eam5000(os.path.join(TABLES, "eam.aluminum5000"))
     with open(os.path.join(TABLES, "pair.lj.argon"), "w") as fh:
@@ -304,6 +319,7 @@ def main(only=None):
     ttm_case(tdir, work)
     checkpoint_case(tdir)
     modifies_case(tdir, work)
+    lj4000_case(tdir, work)
     output_case(tdir)
     thermo_case(tdir)
     print("done")

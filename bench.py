@@ -62,8 +62,8 @@ WORKLOADS = {
                        "network, Tersoff fallback) on Si diamond 40^3 = 512,000 atoms, 1000 K, skin 0.3, dt 1 fs",
                        ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
     "impact_256": dict(kind="impact", desc="impact ensemble: 256 Si diamond slabs of 1,000-16,000 atoms (log-uniform, "
-                       "1.30M atoms), periodic x/y, free surface, 300 K, one Ar at 10-500 eV each; Tersoff + ZBL Ar-Si "
-                       "(rc 3.0 A), skin 0.5 A, dt 0.5 fs; all replicas in one context", ncell=0, a=5.431, sigma=0.03,
+                       "1.30M atoms), periodic x/y, free surface, 300 K, one Ar at 10-500 eV each; Tersoff + the reference's "
+                       "Ar-Si ZBL table (zero past 3.2 A), skin 0.5 A, dt 0.5 fs; all replicas in one context", ncell=0, a=5.431, sigma=0.03,
                        temp=300.0, dt=0.0005, seeds=(6, 6), skin=0.5),
     "lj_ar_4000": dict(kind="lj", desc="LJ Ar FCC 10^3 = 4000 atoms, FP64, rc 2.5 sigma, skin 0.3, 100 K, dt 1 fs",
                        ncell=10, a=5.26, sigma=0.0, temp=100.0, dt=0.001, seeds=(1, 1)),
@@ -215,7 +215,8 @@ def make_context(w, x, v, lo, hi, device=0, tune=True):
         ctx.set_replicas(e["natoms"], e["lo"], e["hi"], (1, 1, 0))
         ctx.set_atoms(x, v, types=e["types"], masses=e["masses"], znum=e["znum"])
         ctx.add_tersoff(os.path.join(SI_DIR, "tersoff.silicon27"))
-        ctx.add_zbl(1, 0, 3.0, 0.5)
+        # Ar-Si: the reference's own table (TForcePair, test/si-impact/main.cpp:71)
+        ctx.add_pair_table(os.path.join(SI_DIR, "pair.ar-si.zbl"), 1, 0)
         ctx.set_neighbor(skin=w.get("skin", 1.0), rebuild_every=0)
         ctx.set_timestep(w["dt"])
         ctx.set_first_step_mode(True)

@@ -544,10 +544,28 @@ static int upload_table(Context* c, Potential& p, int k, HostTable& t, bool fp64
     return OMDG_OK;
 }
 
+// A pair table contributes nothing beyond the start of its negligible tail
+// (|value| and |slope| below 1e-9 eV and eV/A per pair there): such tails
+// come from tables splined to zero well before their last knot, like the
+// reference's Ar-Si ZBL table (zero past 3.2 A, knots to 5.1 A).  The list
+// radius follows that shorter range; the reference's CutRadius (the whole
+// table, tpair.h:59) stays what omdg_max_cut_radius reports.
+constexpr double TABLE_TAIL_TOL = 1e-9;
+
 void update_rc(Context* c) {
     // integrator.cpp:108-113: the largest CutRadius over all force kernels
-    double m = -1.0;
-    for (auto& p : c->pots) m = std::max(m, p.rc);
+    double m = -1.0, ref = -1.0;
+    for (auto& p : c->pots) {
+        if (p.kind == POT_PAIR)
+            p.rc_list = c->table_full_range ? p.rc : std::min(p.rc, table_negligible_from(p.t0, TABLE_TAIL_TOL));
+        else
+            p.rc_list = p.rc;
+        m = std::max(m, p.rc_list);
+        ref = std::max(ref, p.rc);
+    }
+    c->rc_ref = ref;
+    // the detector's cutoff (its own, else the reference's CutRadius) must be in the list too
+    if (c->ttm) m = std::max(m, thermo_ercut(c));
     c->rc_max = m;
     c->list_valid = false;
     c->maxnb = 0;
@@ -763,7 +781,7 @@ int omdg_add_zbl(omdg_ctx* c, int ta, int tb, double rcut, double width) {
 
 int omdg_max_cut_radius(omdg_ctx* c, double* rc) {
     if (!c || !rc) return OMDG_EINVAL;
-    *rc = c->rc_max;
+    *rc = c->rc_ref;
     return OMDG_OK;
 }
 
@@ -839,8 +857,8 @@ int forces_compute(Context* c) {
     bool first = true;
     for (auto& p : c->pots) {
         if (p.fallback_only) continue;  // run by the potential that owns it
-        if (c->nrep > 0 && p.kind != POT_TERSOFF && p.kind != POT_ZBL)
-            return set_error(c, OMDG_EINVAL, "replica mode evaluates Tersoff and ZBL kernels only");
+        if (c->nrep > 0 && p.kind != POT_TERSOFF && p.kind != POT_ZBL && !(p.kind == POT_PAIR && !p.fp64))
+            return set_error(c, OMDG_EINVAL, "replica mode evaluates Tersoff, ZBL and FP32 pair-table kernels only");
         int rc = OMDG_OK;
         switch (p.kind) {
             case POT_EAM: rc = eam_launch(c, p, first); break;
@@ -1184,7 +1202,10 @@ int omdg_set_compat(omdg_ctx* c, const char* key, int on) {
     std::string k(key);
     if (k == "first_step_zero_force") c->reference_first_step = on != 0;
     else if (k == "thermostat_counts_ghosts") c->thermo_count_ghosts = on != 0;
-    else return set_error(c, OMDG_EINVAL, "unknown compatibility key " + k);
+    else if (k == "pair_table_full_range") {
+        c->table_full_range = on != 0;
+        update_rc(c);
+    } else return set_error(c, OMDG_EINVAL, "unknown compatibility key " + k);
     invalidate_graph(c);
     return OMDG_OK;
 }

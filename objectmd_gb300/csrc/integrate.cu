@@ -601,7 +601,7 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
         // periodic axis an atom within Rv of a face has one more image.
         GhostParams g;
         g.n = c->n;
-        double rv = c->rc_max + c->skin;
+        double rv = c->rc_ref + c->skin;  // the reference's ghost shell
         for (int d = 0; d < 3; d++) {
             g.lo[d] = c->box.lo[d];
             g.hi[d] = c->box.hi[d];

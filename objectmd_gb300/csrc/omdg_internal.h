@@ -50,6 +50,10 @@ int table_load(const std::string& file, const std::string& name, HostTable& t, s
 void table_coef(HostTable& t);
 // Reference evaluation (FP64) used by host-side checks.
 bool table_read(const HostTable& t, double r, double& val, double& dval);
+// Start of the table's negligible tail: the first knot from which every
+// segment stays within tol in value and in slope (per r for RMULT tables);
+// max_range() when there is none.
+double table_negligible_from(const HostTable& t, double tol);
 
 struct DevTable {
     const float4* coef;    // (a, b, c, d) per knot
@@ -119,6 +123,7 @@ struct Potential {
     TersoffParams ters{};
     ZBLParams zbl{};
     double rc = 0;         // CutRadius as the reference sets it
+    double rc_list = 0;    // the radius this kernel needs in the neighbour list (<= rc)
     NNState* nn = nullptr; // POT_NN: model, device network and per-atom buffers
     bool fallback_only = false;  // evaluated only for the atoms a POT_NN hands over
     // device copies
@@ -236,7 +241,9 @@ struct Context {
 
     // potentials
     std::vector<Potential> pots;
-    double rc_max = 0;
+    double rc_max = 0;          // the list radius: largest kernel radius (and the detector's cutoff)
+    double rc_ref = 0;          // the reference's CutRadius: largest over the kernels (integrator.cpp:108-113)
+    bool table_full_range = false;  // pair tables' negligible tails stay in the list radius (compat)
 
     // integrator
     double dt = 0.001;

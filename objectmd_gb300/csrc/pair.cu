@@ -18,6 +18,8 @@ struct PairParams {
     double rc64;
     int ta, tb, all_types;
     int first;
+    const ShiftF* rep_L;  // replica mode: periodic lengths of each replica (else null)
+    const int* rep_of;
 };
 
 __device__ __forceinline__ bool types_match(int a, int b, int ta, int tb) {
@@ -52,6 +54,7 @@ __global__ void __launch_bounds__(512) k_pair32(PairParams p, const PosPack* __r
         int ii = valid ? i : p.n - 1;
         PosPack pi = pack[ii];
         int ti = pack_type(pi.hi);
+        const ShiftF L = p.rep_L ? p.rep_L[p.rep_of[ii]] : p.L;
         bool any = valid && (p.all_types || ti == p.ta || ti == p.tb);
         int m = any ? nnb[ii] : 0;
         Kahan ax, ay, az, ae;
@@ -60,9 +63,10 @@ __global__ void __launch_bounds__(512) k_pair32(PairParams p, const PosPack* __r
             unsigned e = __ldg(&nbr[nbr_at(ii, s, p.hshift, p.maxnb)]);
             int j = nbr_index(e);
             const float4* pj = reinterpret_cast<const float4*>(pack + j);
-            float4 hj = __ldg(pj), lj = __ldg(pj + 1);
+            const float4 hj = __ldg(pj);  // the type word first: most rows of a mixed system skip here
             if (!p.all_types && !types_match(ti, pack_type(hj), p.ta, p.tb)) continue;
-            float3 d = pair_delta(pi.hi, pi.lo, hj, lj, e, p.L);
+            const float4 lj = __ldg(pj + 1);
+            float3 d = pair_delta(pi.hi, pi.lo, hj, lj, e, L);
             float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
             if (r2 >= p.rc2) continue;
             float rinv = rsqrtf(r2);
@@ -191,6 +195,9 @@ int pair_launch(Context* c, Potential& pot, bool first) {
     p.tb = pot.tb;
     p.all_types = c->ntypes == 1 ? 1 : 0;
     p.first = first ? 1 : 0;
+    p.rep_L = c->nrep > 0 ? static_cast<const ShiftF*>(c->d_rep_shift) : nullptr;
+    p.rep_of = c->nrep > 0 ? c->d_rep_of : nullptr;
+    if (pot.fp64 && c->nrep > 0) return set_error(c, OMDG_EINVAL, "replica mode has no FP64 pair kernel");
     int block = c->pair_block;
     if (pot.fp64) {
         prof_begin(c, "pair64");

@@ -121,6 +121,24 @@ void table_coef(HostTable& t) {
     }
 }
 
+double table_negligible_from(const HostTable& t, double tol) {
+    const double dr = t.dr;
+    int k0 = t.n - 1;  // segments [k0, n-1) are all negligible
+    for (int k = t.n - 2; k >= 0; k--) {
+        const double a = std::fabs(t.a[k]), b = std::fabs(t.b[k]), c = std::fabs(t.c[k]), d = std::fabs(t.d[k]);
+        double vmax = d + dr * (c + dr * (b + dr * a));
+        double dmax = c + dr * (2.0 * b + 3.0 * dr * a);
+        if (t.rmult) {  // value / r and (slope - value / r) / r
+            const double r = std::max(t.off + k * dr, 1e-12);
+            dmax = (dmax + vmax / r) / r;
+            vmax /= r;
+        }
+        if (!(vmax <= tol && dmax <= tol)) break;
+        k0 = k;
+    }
+    return k0 >= t.n - 1 ? t.max_range() : t.off + k0 * dr;
+}
+
 bool table_read(const HostTable& t, double r, double& val, double& dval) {
     double rval = r - t.off;
     int x = (int)(rval / t.dr);

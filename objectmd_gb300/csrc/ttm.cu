@@ -375,7 +375,7 @@ static ThermoParams th_params(const Context* c, const TTMCtx& t) {
     p.maxnb = c->maxnb;
     p.L = make_shift(c->box);
     for (int d = 0; d < 3; d++) p.L64[d] = c->box.periodic[d] ? c->box.L[d] : 0.0;
-    p.rc = t.ercut > 0 ? t.ercut : c->rc_max;
+    p.rc = t.ercut > 0 ? t.ercut : c->rc_ref;
     p.rc2 = p.rc * p.rc;
     p.rc2_lo = (float)(p.rc2 * (1.0 - 2e-5));
     p.rc2_hi = (float)(p.rc2 * (1.0 + 2e-5));
@@ -386,7 +386,7 @@ static ThermoParams th_params(const Context* c, const TTMCtx& t) {
 
 double thermo_ercut(const Context* c) {
     if (!c->ttm) return -1.0;
-    return c->ttm->ercut > 0 ? c->ttm->ercut : c->rc_max;
+    return c->ttm->ercut > 0 ? c->ttm->ercut : c->rc_ref;
 }
 
 int thermo_detect(Context* c, bool after_step) {
@@ -484,12 +484,12 @@ int omdg_set_thermo_detector(omdg_ctx* c, int on, double ercut) {
     if (!on) {
         if (c->ttm && c->ttm->ttm) return set_error(c, OMDG_ESTATE, "the two-temperature model needs the detector");
         ttm_release(c);
-        invalidate_graph(c);
+        update_rc(c);
         return OMDG_OK;
     }
     if (!c->ttm) c->ttm = new TTMCtx();
     c->ttm->ercut = ercut;
-    invalidate_graph(c);
+    update_rc(c);  // the list must reach the detector's cutoff
     return OMDG_OK;
 }
 

@@ -348,6 +348,51 @@ int oc_pair_table_typed(const oc_box* box, int n, const double* x, const int* ty
     return 0;
 }
 
+int oc_zbl(const oc_box* box, int n, const double* x, const int* type, int ta, int tb, double z1, double z2,
+           double rc, double width, const int* offsets, const int* nbr_j, const int* nbr_code, double* f, double* e,
+           double* vir) {
+    /* sw.cpp:84-91 */
+    const double znor = 0.468521928 / (pow(z1, 0.23) + pow(z2, 0.23));
+    const double zc = 14.39964415 * z1 * z2;
+    const double ze[4] = {3.2000 / znor, 0.9423 / znor, 0.4029 / znor, 0.2016 / znor};
+    const double cf[4] = {0.1818, 0.5099, 0.2802, 0.02817};
+    const double rsw = rc - width;
+    for (int i = 0; i < n; i++) {
+        for (int k = offsets[i]; k < offsets[i + 1]; k++) {
+            int j = nbr_j[k];
+            int a = type[i], b = type[j];
+            if (!((a == ta && b == tb) || (a == tb && b == ta))) continue;
+            double s[3], d[3];
+            shift_vec(box, nbr_code[k], s);
+            double r = sqrt(pair_dist2(x + 3 * i, x + 3 * j, s, d));
+            if (!(r < rc)) continue;
+            /* sw.cpp:121-134: fpot and fr = -dfpot/dr / r */
+            double fex[4], sum = 0.0, dsum = 0.0;
+            for (int q = 0; q < 4; q++) {
+                fex[q] = cf[q] * exp(-ze[q] * r);
+                sum += fex[q];
+                dsum += (1.0 / r + ze[q]) * fex[q];
+            }
+            double phi = sum * zc / r;
+            double dphi = -dsum * zc / r; /* d phi / dr */
+            double S = 1.0, dS = 0.0;
+            if (r > rsw) {
+                double t = (r - rsw) / width;
+                S = 1.0 - t * t * t * (10.0 - 15.0 * t + 6.0 * t * t);
+                dS = -30.0 * t * t * (1.0 - t) * (1.0 - t) / width;
+            }
+            double v = phi * S, dv = dphi * S + phi * dS;
+            double fr = -dv / r;
+            f[3 * i + 0] += d[0] * fr;
+            f[3 * i + 1] += d[1] * fr;
+            f[3 * i + 2] += d[2] * fr;
+            e[i] += 0.5 * v;
+            vir[i] += fr * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        }
+    }
+    return 0;
+}
+
 int oc_pair_table(const oc_box* box, int n, const double* x, const int* offsets, const int* nbr_j,
                   const int* nbr_code, const oc_table* phi, double* f, double* e, double* vir) {
     zero3(n, f, e, vir);

@@ -90,6 +90,15 @@ int oc_pair_table_typed(const oc_box* box, int n, const double* x, const int* ty
                         const int* offsets, const int* nbr_j, const int* nbr_code, const oc_table* phi, double* f,
                         double* e, double* vir);
 
+/* Universal ZBL screened Coulomb between types (ta,tb) in either order, as
+   StillingerWeber::ZBL (sw.cpp:118-146, constants sw.cpp:84-91), for r < rc,
+   times the switch S(r) = 1 - t^3 (10 - 15 t + 6 t^2), t = (r - rc + width) /
+   width, on [rc - width, rc] (the cut of omdg_add_zbl; the reference's ZBL
+   core has none).  Adds to f, e, vir. */
+int oc_zbl(const oc_box* box, int n, const double* x, const int* type, int ta, int tb, double z1, double z2,
+           double rc, double width, const int* offsets, const int* nbr_j, const int* nbr_code, double* f, double* e,
+           double* vir);
+
 /* integrator.cpp:225-259 first half: v += dt/2 f/m ; x += dt v (active atoms). */
 void oc_vv_kick_drift(int n, double* x, double* v, const double* f, const double* mass, double dt);
 /* integrator.cpp:249-257 second half: v += dt/2 f/m. */

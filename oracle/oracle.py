@@ -100,7 +100,8 @@ def lib():
                                              P(d)]
         _lib.oc_sw.argtypes = nb + [P(SWParam), P(d), P(d), P(d)]
         _lib.oc_tersoff.argtypes = nb + [P(TersoffParam), P(d), P(d), P(d)]
-        for fn in ("oc_eam", "oc_pair_table", "oc_pair_table_typed", "oc_sw", "oc_tersoff"):
+        _lib.oc_zbl.argtypes = [P(_Box), i, P(d), P(i), i, i, d, d, d, d, P(i), P(i), P(i), P(d), P(d), P(d)]
+        for fn in ("oc_eam", "oc_pair_table", "oc_pair_table_typed", "oc_sw", "oc_tersoff", "oc_zbl"):
             getattr(_lib, fn).restype = i
         _lib.oc_vv_kick_drift.argtypes = [i, P(d), P(d), P(d), P(d), d]
         _lib.oc_vv_kick.argtypes = [i, P(d), P(d), P(d), d]
@@ -259,6 +260,21 @@ def pair_table_typed(box, x, types, ta, tb, nb, phi: Table, f, e, vir):
                                    ctypes.byref(phi.t), _dp(f), _dp(e), _dp(vir))
     if rc:
         raise RuntimeError("oc_pair_table_typed failed")
+
+
+def zbl(box, x, types, ta, tb, z1, z2, rc, width, nb, f=None, e=None, vir=None):
+    """Universal ZBL (sw.cpp:118-146) on (ta, tb) pairs with omdg_add_zbl's
+    switch over [rc - width, rc]; adds to f, e, vir (new arrays if None)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    types = np.ascontiguousarray(types, dtype=np.int32)
+    n = len(x)
+    f = np.zeros((n, 3)) if f is None else f
+    e = np.zeros(n) if e is None else e
+    vir = np.zeros(n) if vir is None else vir
+    off, j, c = nb
+    lib().oc_zbl(ctypes.byref(box), n, _dp(x), _ip(types), ta, tb, z1, z2, rc, width, _ip(off), _ip(j), _ip(c),
+                 _dp(f), _dp(e), _dp(vir))
+    return f, e, vir
 
 
 def sw(box, x, nb, p: SWParam):

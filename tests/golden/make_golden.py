@@ -217,6 +217,65 @@ def lj4000_case(tdir, work):
     save_case("lj_ar_4000", f, res, box_lo=lo, box_hi=hi, steps=np.array(1000), dt=np.array(0.001))
 
 
+def impact_slab(site, height, speed, seed):
+    """Si diamond slab 6 x 6 x 3 cells (864 atoms, periodic x/y, free z, 300 K)
+    and one Ar atom `height` A above surface atom number `site` (of 9 on a
+    3 x 3 grid), moving down at `speed` A/ps.  Si is type 0 ("target"), Ar
+    type 1 ("projectile"), the convention of the reference's test/si-impact
+    (which has one projectile: the reference needs a projectile-projectile
+    force as soon as there are two, integrator.cpp:133-143)."""
+    a = 5.431
+    x, lo, hi = inputs.lattice(inputs.DIAMOND_BASIS, (6, 6, 3), a, 0.125)
+    x = inputs.perturb(x, 0.03, seed, lo, hi, (True, True, False))
+    v = inputs.maxwell_boltzmann(len(x), 300.0, inputs.md_mass("silicon"), seed + 1)
+    top = np.where(x[:, 2] > x[:, 2].max() - 0.5)[0]
+    gx, gy = site // 3, site % 3
+    want = np.array([(gx + 0.3) * 2 * a, (gy + 0.3) * 2 * a])
+    s = top[np.argmin(np.sum((x[top, :2] - want) ** 2, axis=1))]
+    ar = x[s] + np.array([0.25, -0.15, height])
+    lo = np.array([lo[0], lo[1], lo[2]])
+    hi = np.array([hi[0], hi[1], x[:, 2].max() + 12.0])
+    types = np.concatenate([np.zeros(len(x), dtype=np.int32), [1]]).astype(np.int32)
+    return (np.vstack([x, ar]), np.vstack([v, [0.0, 0.0, -speed]]), types, lo, hi)
+
+
+def impact_case(tdir, work):
+    """Stillinger-Weber Si (every triplet) plus the reference's own Ar-Si table
+    (tables/pair.ar-si.zbl: universal ZBL splined to zero over 3.0-3.2 A, knots
+    to 5.1 A) through TForcePair between projectile and target, as in
+    test/si-impact/main.cpp:70-71.  The table is written to tests/golden/tables
+    for the GPU runs.  Static: 9 runs, the Ar atom 0.6-3.1 A above a surface
+    atom.  Trajectory: the Ar atom 3.5 A above, moving down at 200 A/ps
+    (83 eV), 80 steps of 0.5 fs."""
+    shutil.copy(os.path.join(REF, "tables", "pair.ar-si.zbl"), os.path.join(TABLES, "pair.ar-si.zbl"))
+    out = {}
+    hs = [0.6, 0.9, 1.2, 1.6, 2.0, 2.4, 2.7, 2.9, 3.1]
+    xs, fs, ps, vs = [], [], [], []
+    for k, h in enumerate(hs):
+        x, v, t, lo, hi = impact_slab(k, h, 0.0, 71)
+        f = os.path.join(work, "impact_static%d.dat" % k)
+        inputs.write_import(f, x, v, types=t, box=(lo, hi), periodic=(True, True, False),
+                            species=("silicon", "argon"), names=("target", "projectile"))
+        res = oc.run_reference(f, "sw", "silicon", steps=0, table_dir=tdir, swfix=True, pair2="ar-si.zbl")
+        a = res["atoms"]
+        xs.append(x)
+        fs.append(a[:, 8:11])
+        ps.append(a[:, 11])
+        vs.append(a[:, 12])
+    out.update(static_x0=np.array(xs), static_v0=v, types=t, box_lo=lo, box_hi=hi, static_f=np.array(fs),
+               static_pot=np.array(ps), static_vir=np.array(vs), heights=np.array(hs))
+    x, v, t, lo, hi = impact_slab(4, 3.5, 200.0, 73)
+    f = os.path.join(work, "impact_nve.dat")
+    inputs.write_import(f, x, v, types=t, box=(lo, hi), periodic=(True, True, False), species=("silicon", "argon"),
+                        names=("target", "projectile"))
+    res = oc.run_reference(f, "sw", "silicon", steps=80, dt=0.0005, table_dir=tdir, swfix=True, pair2="ar-si.zbl")
+    a = res["atoms"]
+    out.update(nve_x0=x, nve_v0=v, nve_lo=lo, nve_hi=hi, nve_x=a[:, 2:5], nve_v=a[:, 5:8], nve_f=a[:, 8:11],
+               nve_ledger=res["ledger"], steps=np.array(80), dt=np.array(0.0005))
+    np.savez_compressed(os.path.join(GOLD, "impact_ar_si_slab.npz"), **out)
+    print("wrote impact_ar_si_slab")
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not REF:
@@ -237,6 +296,9 @@ def main(only=None):
         return
     if only == "modifies":
         modifies_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
+        return
+    if only == "impact":
+        impact_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
         return
     if only == "lj4000":
         lj4000_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
@@ -320,6 +382,7 @@ def main(only=None):
     checkpoint_case(tdir)
     modifies_case(tdir, work)
     lj4000_case(tdir, work)
+    impact_case(tdir, work)
     output_case(tdir)
     thermo_case(tdir)
     print("done")

@@ -243,3 +243,29 @@ def test_ttm_oracle_matches_reference(oracle_lib):
     np.testing.assert_allclose(kin, d["ledger"][1:1 + len(kin), 1], rtol=1e-10)
     np.testing.assert_allclose(thermo["temp"], d["local_temp"], rtol=1e-9)
     np.testing.assert_allclose(thermo["dens"], d["local_dens"], rtol=1e-12)
+
+
+def test_oracle_sw_and_ar_si_table_match_the_reference_impact_slab(oracle_lib):
+    """SW on the Si atoms plus the reference's Ar-Si table between Ar and Si
+    (test/si-impact/main.cpp:70-71) equals the reference's own static forces
+    and energies for an Ar atom 0.6-3.1 A above a Si slab (periodic x/y, free
+    z); the reference build takes SW third atoms of the kernel's types only."""
+    oc = oracle_lib
+    d = dict(np.load(os.path.join(GOLD, "impact_ar_si_slab.npz")))
+    sw = oc.SWParam(eps=2.1683, A=7.049556277, B=0.6022245584, p=4, q=0, sigma=2.0951, a=1.80, lam=21.0, gamma=1.2,
+                    icos0=-3.0, usezbl=1, sx0=1.2107, sx1=1.8456, sa0=335.0594, sa1=-492.3905, sa2=244.5280,
+                    sa3=-41.2347, z1=14, z2=14)
+    phi = oc.Table.from_file(os.path.join(GOLD, "tables", "pair.ar-si.zbl"))
+    types = d["types"]
+    si = types == 0
+    box = oc.make_box(d["box_lo"], d["box_hi"], (1, 1, 0))
+    for k in range(len(d["heights"])):
+        x = d["static_x0"][k]
+        fs, es, _ = oc.sw(box, x[si], oc.neighbors(box, x[si], 2.0951 * 1.8 + 0.3), sw)
+        f = np.zeros_like(x)
+        e = np.zeros(len(x))
+        f[si], e[si] = fs, es
+        oc.pair_table_typed(box, x, types, 1, 0, oc.neighbors(box, x, phi.max_range() + 0.3), phi, f, e,
+                            np.zeros(len(x)))
+        assert np.abs(f - d["static_f"][k]).max() <= 1e-11 * np.abs(d["static_f"][k]).max()
+        assert np.abs(e - d["static_pot"][k]).max() <= 1e-12

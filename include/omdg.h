@@ -311,6 +311,28 @@ int omdg_nn_predict(omdg_nn* nn, int conf0, int nconf, int fp32, double* energy_
 int omdg_nn_save(omdg_nn* nn, const char* path);
 int omdg_nn_load(omdg_nn* nn, const char* path);
 
+/* ------------------------------------------------------- bounded waits */
+
+/*
+ * No reference counterpart (the reference has no device code).  Every wait
+ * of the tensor-core kernels (an mbarrier for a bulk copy or an MMA) polls at
+ * most `polls` times (0 restores the default, 4,194,304); when it gives up,
+ * the CTA waits for its own copy or MMA to finish, records ERR_TIMEOUT, which
+ * the calling entry point returns as OMDG_ECUDA "a bounded device wait
+ * expired", and returns.  Process-wide; takes effect at the next launch.
+ */
+int omdg_set_wait_polls(int polls);
+
+/*
+ * No reference counterpart.  Makes one kind of bounded wait run out on the
+ * current device and returns its status word in *status (ERR_TIMEOUT = 32
+ * when it gave up): which 0 = an mbarrier that nothing arrives at, in a CTA
+ * holding TMEM as the tensor-core kernels do; which 1 = a grid barrier whose
+ * arrival count the grid can never reach.  Neither hangs nor faults: the
+ * kernel returns after `polls` polls and the device stays usable.
+ */
+int omdg_selftest_wait(int which, int polls, unsigned* status);
+
 /* ------------------------------------------------- allocation-free counting */
 
 /*

@@ -48,15 +48,69 @@ int check_status(Context* c) {
     return status_error(c, st);
 }
 
-// Maps (and clears) a non-zero device status word.
+static std::string fmt(const char* f, double v) {
+    char b[64];
+    std::snprintf(b, sizeof(b), f, v);
+    return b;
+}
+
+// The reference's text for an overlap (CalcSqrDistance, gadget.cpp:149-159):
+// the pair's distance, enumeration numbers (caller order) and positions.
+static std::string overlap_text(Context* c, unsigned si, unsigned sj) {
+    if (si == ~0u || (int)si >= c->n || (int)sj >= c->n) return "CalcSqrDistance: overlapping atoms";
+    double p[2][3];
+    int nid[2];
+    const unsigned ij[2] = {si, sj};
+    for (int a = 0; a < 2; a++) {
+        cudaMemcpy(&p[a][0], c->x + ij[a], sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&p[a][1], c->y + ij[a], sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&p[a][2], c->z + ij[a], sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&nid[a], c->id + ij[a], sizeof(int), cudaMemcpyDeviceToHost);
+    }
+    double r2 = 0.0;
+    for (int d = 0; d < 3; d++) {
+        double dd = p[0][d] - p[1][d];
+        if (c->box.periodic[d]) dd -= c->box.L[d] * std::nearbyint(dd / c->box.L[d]);
+        r2 += dd * dd;
+    }
+    return "CalcSqrDistance: overlapping atoms: r=" + fmt("%1.1E", std::sqrt(r2)) + " between atom nid=" +
+           std::to_string(nid[0]) + " and nid=" + std::to_string(nid[1]) + " (" + fmt("%0.5E", p[0][0]) + "," +
+           fmt("%0.5E", p[0][1]) + "," + fmt("%0.5E", p[0][2]) + ") -- (" + fmt("%0.5E", p[1][0]) + "," +
+           fmt("%0.5E", p[1][1]) + "," + fmt("%0.5E", p[1][2]) + ")";
+}
+
+// The reference's text for a table read outside its range (TableReader::read,
+// treader.cpp:199-218), from the recorded value and table.
+static std::string range_text(Context* c, unsigned vbits, unsigned src) {
+    const int pi = (int)(src >> 2), sec = (int)(src & 3u);
+    if (src == ~0u || pi >= (int)c->pots.size() || sec > 2) return "table read outside its range";
+    const Potential& p = c->pots[pi];
+    const HostTable& t = sec == 0 ? p.t0 : (sec == 1 ? p.t1 : p.t2);
+    float vf;
+    std::memcpy(&vf, &vbits, sizeof(vf));
+    const double r = vf, rval = r - t.off;
+    const int x = (int)(rval / t.dr);
+    const double dx = rval - (double)x * t.dr;
+    return std::string(x > t.n - 1 ? "high" : "low") + " limit exeeded in " + t.name + "@" + t.file +
+           " (read) index=" + std::to_string(x) + " r=" + fmt("%0.5E", r) + " delta=" + fmt("%0.5E", dx) +
+           " low_limit=" + fmt("%0.5E", t.off) + " hi_limit=" + fmt("%0.5E", t.max_range());
+}
+
+// Maps (and clears) a non-zero device status word; the status block's
+// details name the first overlapping pair or out-of-range value.
 static int status_error(Context* c, unsigned st) {
     if (!st) return OMDG_OK;
-    unsigned zero = 0;
-    cudaMemcpyAsync(c->d_status, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, c->stream);
+    unsigned det[ST_WORDS];
+    cudaMemcpyAsync(det, c->d_status, sizeof(det), cudaMemcpyDeviceToHost, c->stream);
     cudaStreamSynchronize(c->stream);
-    if (st & ERR_TABLE_RANGE)
-        return set_error(c, OMDG_ERANGE, "table read outside its range (the reference dies here: treader.cpp:199-218)");
-    if (st & ERR_OVERLAP) return set_error(c, OMDG_EOVERLAP, "overlapping atoms: r^2 < 1e-6 (gadget.cpp:149)");
+    static const unsigned blank[ST_RANGE_SRC + 1] = {0u, ~0u, ~0u, ~0u, ~0u};
+    cudaMemcpyAsync(c->d_status, blank, sizeof(blank), cudaMemcpyHostToDevice, c->stream);
+    cudaStreamSynchronize(c->stream);
+    // the list may hold what the bad input made of it: the next use rebuilds it
+    if (st & (ERR_OVERLAP | ERR_NONFINITE | ERR_CELL | ERR_TABLE_RANGE)) c->list_valid = false;
+    // the reference meets an overlap (gadget.cpp:149) before the table read it would fail
+    if (st & ERR_OVERLAP) return set_error(c, OMDG_EOVERLAP, overlap_text(c, det[ST_OV_I], det[ST_OV_J]));
+    if (st & ERR_TABLE_RANGE) return set_error(c, OMDG_ERANGE, range_text(c, det[ST_RANGE_V], det[ST_RANGE_SRC]));
     if (st & ERR_NONFINITE) return set_error(c, OMDG_ENONFINITE, "non-finite position or force");
     if (st & ERR_NBR_OVERFLOW) return set_error(c, OMDG_ESTATE, "neighbour capacity exceeded");
     if (st & ERR_TIMEOUT) return set_error(c, OMDG_ECUDA, "a bounded device wait expired (tensor-core kernel)");
@@ -239,7 +293,7 @@ int omdg_create(omdg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (sms > 0) c->num_sms = sms;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned) * ST_WORDS);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_flags, sizeof(int) * 8);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_state, step_state_bytes());
     if (e == cudaSuccess) e = cudaMalloc(&c->d_mass, sizeof(double) * MAX_TYPES);
@@ -247,7 +301,8 @@ int omdg_create(omdg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaMalloc(&c->d_ledger, sizeof(double) * LEDGER_W * c->ledger_cap);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_ledger, sizeof(double) * LEDGER_W * c->ledger_cap);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_sync, 16 + step_state_bytes());
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(unsigned) * 4, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0xff, sizeof(unsigned) * ST_WORDS, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(unsigned), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_flags, 0, sizeof(int) * 8, c->stream);
     if (e != cudaSuccess) {
         delete c;
@@ -518,6 +573,7 @@ static int upload_table(Context* c, Potential& p, int k, HostTable& t, bool fp64
         return set_error(c, OMDG_ENOMEM, "table upload");
     cudaMemcpy(p.d_coef[k], h.data(), sizeof(float4) * t.n, cudaMemcpyHostToDevice);
     DevTable& d = p.dt[k];
+    d.src = (int)c->pots.size() * 4 + k;  // the potential is appended after its tables
     d.coef = p.d_coef[k];
     d.coef64 = nullptr;
     if (fp64) {

@@ -98,6 +98,41 @@ struct Kahan {
     __device__ __forceinline__ float value() const { return s; }
 };
 
+// Error reports with their details (the status block in omdg_internal.h):
+// the first report of each kind keeps its pair or value.
+__device__ __forceinline__ void report_overlap(unsigned* status, int i, int j) {
+    atomicOr(status, ERR_OVERLAP);
+    if (atomicCAS(status + ST_OV_I, 0xffffffffu, (unsigned)i) == 0xffffffffu) status[ST_OV_J] = (unsigned)j;
+}
+__device__ __forceinline__ void report_range(unsigned* status, float v, int src) {
+    atomicOr(status, ERR_TABLE_RANGE);
+    if (atomicCAS(status + ST_RANGE_SRC, 0xffffffffu, (unsigned)src) == 0xffffffffu)
+        status[ST_RANGE_V] = __float_as_uint(v);
+}
+
+// Grid barrier for kernels whose CTAs are all resident (one CTA per SM or
+// fewer): each CTA's thread 0 adds one arrival, then polls until the count
+// reaches `target` or `polls` polls have passed.  Returns false (and sets
+// ERR_TIMEOUT) when it gave up; the caller then leaves its loop.
+__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int polls, unsigned* status) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(counter, 1u);
+        int k = 0;
+        for (; k < polls; k++) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(counter) : "memory");
+            if (v >= target) break;
+        }
+        ok = k < polls;
+        if (!ok) atomicOr(status, ERR_TIMEOUT);
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
 // ------------------------------------------------------------ spline reads
 // TableReader::read (treader.cpp:193-229): index by truncation, the two
 // edge rules, cubic value and derivative, RMULT division.  Returns false
@@ -112,7 +147,7 @@ __device__ __forceinline__ bool tab_read(const DevTable& t, const float4* __rest
             v = dv = t.out_hi;
             return true;
         }
-        atomicOr(status, ERR_TABLE_RANGE);
+        report_range(status, r, t.src);
         v = dv = 0.f;
         return false;
     }
@@ -121,7 +156,7 @@ __device__ __forceinline__ bool tab_read(const DevTable& t, const float4* __rest
             v = dv = t.out_lo;
             return true;
         }
-        atomicOr(status, ERR_TABLE_RANGE);
+        report_range(status, r, t.src);
         v = dv = 0.f;
         return false;
     }
@@ -157,7 +192,7 @@ __device__ __forceinline__ bool tab_read64(const DevTable& t, double r, double& 
             v = dv = t.out_hi;
             return true;
         }
-        atomicOr(status, ERR_TABLE_RANGE);
+        report_range(status, (float)r, t.src);
         v = dv = 0.0;
         return false;
     }
@@ -166,7 +201,7 @@ __device__ __forceinline__ bool tab_read64(const DevTable& t, double r, double& 
             v = dv = t.out_lo;
             return true;
         }
-        atomicOr(status, ERR_TABLE_RANGE);
+        report_range(status, (float)r, t.src);
         v = dv = 0.0;
         return false;
     }

@@ -113,8 +113,12 @@ __global__ void __launch_bounds__(512) k_eam_density(EAMParams p, const PosPack*
             int st;
             int x = knot(p.rho, r, dx, st);
             if (st) {
-                if (st == 3) bad = 1;
-                else acc.add(st == 1 ? p.rho.out_lo : p.rho.out_hi);
+                if (st == 3) {
+                    if (!bad) report_range(status, r, p.rho.src);
+                    bad = 1;
+                } else {
+                    acc.add(st == 1 ? p.rho.out_lo : p.rho.out_hi);
+                }
                 continue;
             }
             int xs = x - p.stage_k0;
@@ -124,7 +128,6 @@ __global__ void __launch_bounds__(512) k_eam_density(EAMParams p, const PosPack*
             if (p.rho.rmult) v = v / r;
             acc.add(v);
         }
-        if (bad) atomicOr(status, ERR_TABLE_RANGE);
         float s = acc.s, c = acc.c;
         lane_reduce<LANES>(s, c);
         if (lane == 0 && valid) {
@@ -186,7 +189,10 @@ __global__ void __launch_bounds__(512) k_eam_force(EAMParams p, const PosPack* _
                 int x = knot(p.phi, r, dx, st);
                 if (st) {
                     // out-of-range reads keep the reference's OutOfRange values
-                    if (st == 3) bad = 1;
+                    if (st == 3) {
+                        if (!bad) report_range(status, r, p.phi.src);
+                        bad = 1;
+                    }
                     ph = dph = st == 1 ? p.phi.out_lo : p.phi.out_hi;
                     if (!(r > p.rc_rho)) drho = st == 1 ? p.rho.out_lo : p.rho.out_hi;
                 } else {
@@ -224,7 +230,7 @@ __global__ void __launch_bounds__(512) k_eam_force(EAMParams p, const PosPack* _
             ae.add(0.5f * ph);
             av = fmaf(fr, r2, av);
         }
-        if (bad) atomicOr(status, ERR_TABLE_RANGE);
+
         lane_reduce<LANES>(ax.s, ax.c);
         lane_reduce<LANES>(ay.s, ay.c);
         lane_reduce<LANES>(az.s, az.c);

@@ -29,6 +29,7 @@ struct EAMFast {
     int e_n, e_rmult;
     int stage_k0, stage_n;
     int first;
+    int src_phi, src_rho, src_emb;  // table ids for error reports (DevTable::src)
 };
 
 __device__ __forceinline__ void build_shift_table(const EAMFast& p, float4* s_hi, float4* s_lo) {
@@ -124,7 +125,9 @@ __global__ void __launch_bounds__(256, 4) k_eamf_density(EAMFast p, PosPack* pac
                 if (!(r <= p.rc_rho)) continue;
                 int x = __float2int_rz(fmaf(r, p.inv_dr, -offdr));
                 if (x < 0) {
-                    bad = true;  // closer than the first knot: outside every tabulated range here
+                    // closer than the first knot: outside every tabulated range here
+                    if (!bad) report_range(status, r, p.src_rho);
+                    bad = true;
                     continue;
                 }
                 x = min(x, p.nknot - 2);
@@ -137,7 +140,6 @@ __global__ void __launch_bounds__(256, 4) k_eamf_density(EAMFast p, PosPack* pac
                 acc.add(v);
             }
         }
-        if (bad) atomicOr(status, ERR_TABLE_RANGE);
         float sum = acc.s, comp = acc.c;
         twosum_reduce<LANES>(sum, comp);
         if (lane == 0 && valid) {
@@ -147,7 +149,7 @@ __global__ void __launch_bounds__(256, 4) k_eamf_density(EAMFast p, PosPack* pac
             int x = __float2int_rz(rval * p.e_inv_dr);
             float F = 0.f, dF = 0.f;
             if (x < -1 || x > p.e_n - 1) {
-                atomicOr(status, ERR_TABLE_RANGE);
+                report_range(status, rho, p.src_emb);
             } else {
                 float dx = fmaf(-(float)x, p.e_dr, rval);
                 if (x == p.e_n - 1) {
@@ -223,6 +225,7 @@ __global__ void __launch_bounds__(256, 4) k_eamf_force(EAMFast p, const PosPack*
                 if (!(r <= p.rc_phi)) continue;
                 int x = __float2int_rz(fmaf(r, p.inv_dr, -offdr));
                 if (x < 0) {
+                    if (!bad) report_range(status, r, p.src_phi);
                     bad = true;
                     continue;
                 }
@@ -255,7 +258,6 @@ __global__ void __launch_bounds__(256, 4) k_eamf_force(EAMFast p, const PosPack*
                 av = fmaf(fr, r2, av);
             }
         }
-        if (bad) atomicOr(status, ERR_TABLE_RANGE);
         twosum_reduce<LANES>(ax.s, ax.c);
         twosum_reduce<LANES>(ay.s, ay.c);
         twosum_reduce<LANES>(az.s, az.c);
@@ -333,6 +335,9 @@ int eam_fast_launch(Context* c, Potential& pot, bool first) {
     p.e_n = pot.t2.n;
     p.e_rmult = pot.t2.rmult ? 1 : 0;
     p.first = first ? 1 : 0;
+    p.src_phi = pot.dt[0].src;
+    p.src_rho = pot.dt[1].src;
+    p.src_emb = pot.dt[2].src;
     int k0 = 0, ns = 0;
     if (c->eam_stage) {
         k0 = (int)((c->eam_stage_frac * pot.t1.max_range() - pot.t1.off) / pot.t1.dr);

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __re
         pack[i] = pk;
         float4 r0 = xref[i];
         float dx = (pk.hi.x - r0.x) + pk.lo.x, dy = (pk.hi.y - r0.y) + pk.lo.y, dz = (pk.hi.z - r0.z) + pk.lo.z;
-        if (dx * dx + dy * dy + dz * dz > p.half_skin2) moved = 1;
+        if (!(dx * dx + dy * dy + dz * dz <= p.half_skin2)) moved = 1;  // NaN counts as moved
     }
     __syncthreads();
     if (threadIdx.x == 0 && moved) st->rebuild = 1;
@@ -838,7 +838,7 @@ __global__ void __launch_bounds__(IO_BLOCK) k_upload_state(IntParams p, const in
             const float4 r0 = xref[i];
             const float dx = (pk.hi.x - r0.x) + pk.lo.x, dy = (pk.hi.y - r0.y) + pk.lo.y,
                         dz = (pk.hi.z - r0.z) + pk.lo.z;
-            if (dx * dx + dy * dy + dz * dz > p.half_skin2) moved = 1;
+            if (!(dx * dx + dy * dy + dz * dz <= p.half_skin2)) moved = 1;  // NaN counts as moved
         }
     }
     __syncthreads();

@@ -538,7 +538,7 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
                     if (!(r2 < rsq_lo) &&
                         !exact_within(g.L64(0), g.L64(1), g.L64(2), p.rsq, x, y, z, i, k, code))
                         continue;
-                    if (r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
+                    if (r2 < 1e-6f) report_overlap(status, i, k);
                     if (cnt < p.maxnb) nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
                     cnt++;
                 }
@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(256) k_build_lanes(BuildParams p, const PosPac
                                                       __dmul_rn(dz, dz));
                                 in = rr <= p.rsq;
                             }
-                            if (in && r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
+                            if (in && r2 < 1e-6f) report_overlap(status, i, k);
                         }
                     }
                     const unsigned bal = __ballot_sync(gmask, in) >> gbase;
@@ -778,7 +778,7 @@ __global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildParams 
                         if (r2 >= p.rsq_lo && r2 <= p.rsq_hi)
                             in = exact_within(p.L64[0], p.L64[1], p.L64[2], p.rsq, x, y, z, i,
                                               (int)(entry & (unsigned)INDEX_MASK), code);
-                        if (in && r2 < 1e-6f) atomicOr(status, ERR_OVERLAP);
+                        if (in && r2 < 1e-6f) report_overlap(status, i, (int)(entry & (unsigned)INDEX_MASK));
                     }
                     const unsigned bal = __ballot_sync(gmask, in) >> gbase;
                     if (in) {

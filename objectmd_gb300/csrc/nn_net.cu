@@ -300,7 +300,7 @@ __device__ __forceinline__ void tc_handoff() {
 __global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __restrict__ img,
                                                        const float* __restrict__ vec, const float* __restrict__ gt,
                                                        int rows, float* __restrict__ E, float* __restrict__ U,
-                                                       unsigned* status) {
+                                                       unsigned* status, int polls) {
     extern __shared__ uint8_t smem_raw[];
     MLPSmem& S = *reinterpret_cast<MLPSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int t = threadIdx.x, warp = t >> 5;
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __r
         bulk_g2s(S.w1t, img, (uint32_t)(sizeof(__nv_bfloat16) * NN_IMG_ELEMS), &S.bar_load);
         bulk_g2s(S.vec, vec, (uint32_t)(sizeof(float) * NN_VEC_FLOATS), &S.bar_load);
     }
-    if (!mbar_wait(&S.bar_load, 0)) S.abort = 1;
+    mbar_wait_or_drain(&S.bar_load, 0, polls, S.abort);
     __syncthreads();
 
     const uint32_t sx = smem_u32(S.x), sh = smem_u32(S.h);
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __r
             tc_gemm(tmem, sx, sw1, NN_DESC, ID64);
             tc_commit(&S.bar_mma);
         }
-        if (!mbar_wait(&S.bar_mma, phase)) S.abort = 1;
+        mbar_wait_or_drain(&S.bar_mma, phase, polls, S.abort);
         phase ^= 1u;
         tc_fence_after();
         float a1[NN_H];
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __r
             tc_gemm(tmem + 64, sh, sw2, NN_H, ID64);
             tc_commit(&S.bar_mma);
         }
-        if (!mbar_wait(&S.bar_mma, phase)) S.abort = 1;
+        mbar_wait_or_drain(&S.bar_mma, phase, polls, S.abort);
         phase ^= 1u;
         tc_fence_after();
         float e = S.vec[NN_VEC_B3];
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __r
             tc_gemm(tmem, sh, sw2t, NN_H, ID64);
             tc_commit(&S.bar_mma);
         }
-        if (!mbar_wait(&S.bar_mma, phase)) S.abort = 1;
+        mbar_wait_or_drain(&S.bar_mma, phase, polls, S.abort);
         phase ^= 1u;
         tc_fence_after();
         {
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __r
             tc_gemm(tmem + 64, sh, sw1t, NN_H, ID32);
             tc_commit(&S.bar_mma);
         }
-        if (!mbar_wait(&S.bar_mma, phase)) S.abort = 1;
+        mbar_wait_or_drain(&S.bar_mma, phase, polls, S.abort);
         phase ^= 1u;
         tc_fence_after();
         {
@@ -463,7 +463,7 @@ cudaError_t nn_mlp_launch(const NNDevNet& net, const float* gt, int rows, float*
     // 4 CTAs per SM: about 51 KB of shared memory and 128 of the SM's 512
     // TMEM columns each, so the allocations never wait; four MMA chains overlap
     const int grid = std::min(tiles, 4 * std::max(1, num_sms));
-    k_nn_mlp<<<grid, MLP_ROWS, smem, s>>>(net.img, net.vec, gt, rows, E, u, status);
+    k_nn_mlp<<<grid, MLP_ROWS, smem, s>>>(net.img, net.vec, gt, rows, E, u, status, tc_wait_polls());
     return cudaGetLastError();
 }
 

@@ -25,6 +25,11 @@ enum : unsigned {
     ERR_TIMEOUT = 32u,     // a bounded device wait (mbarrier) expired
 };
 
+// The status block: word 0 the bits above; then the first overlapping pair
+// (sorted indices) and the first value read outside a table with its table
+// (DevTable::src); ~0 where nothing was recorded.
+enum : int { ST_WORDS = 8, ST_OV_I = 1, ST_OV_J = 2, ST_RANGE_V = 3, ST_RANGE_SRC = 4 };
+
 constexpr int CODE_SHIFT = 26;                // nbr entry = j | code << 26
 constexpr int INDEX_MASK = (1 << CODE_SHIFT) - 1;
 constexpr int MAX_ATOMS = INDEX_MASK;         // 67,108,863
@@ -66,6 +71,7 @@ struct DevTable {
     float out_lo, out_hi;
     float rc;      // max_range as float
     double rc64;   // max_range
+    int src;       // potential index * 4 + section (0 PAIR/phi, 1 EDENS, 2 EMBED): names the table in errors
 };
 
 // ------------------------------------------------------------ box geometry
@@ -372,6 +378,9 @@ constexpr int RED_BLOCK = 256;  // threads of the kick kernel's blocks (one 32-b
 
 // Atom group g as its flag bit (bits 8..15); -1: every atom.
 inline unsigned group_bits(int g) { return g < 0 ? ~0u : (1u << (8 + g)); }
+
+// run-time poll limit of the tensor-core kernels' mbarrier waits (waits.cu)
+int tc_wait_polls();
 
 // grid sizing
 inline int grid_for(int n, int block) { return (n + block - 1) / block; }

@@ -54,10 +54,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (int k = 0; k < TC_WAIT_LIMIT; k++)
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, int polls) {
+    for (int k = 0; k < polls; k++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    return mbar_wait_n(bar, parity, TC_WAIT_LIMIT);
+}
+
+// A wait of `polls` (the run-time limit, omdg_set_wait_polls) that, when it
+// gives up, marks the CTA aborted and then waits up to TC_WAIT_LIMIT polls
+// more on the same phase: the copy or MMA this CTA itself issued on the
+// barrier finishes before the CTA frees its TMEM and shared memory.
+__device__ __forceinline__ void mbar_wait_or_drain(uint64_t* bar, uint32_t parity, int polls, volatile int& abort) {
+    if (mbar_wait_n(bar, parity, polls)) return;
+    abort = 1;
+    mbar_wait_n(bar, parity, TC_WAIT_LIMIT);
 }
 
 // ------------------------------------------------------------------ bulk copy

@@ -29,6 +29,9 @@ ERRORS = {
     -8: "OMDG_ENONFINITE",
 }
 
+OMDG_EINVAL, OMDG_ECUDA, OMDG_ERANGE, OMDG_EOVERLAP = -1, -2, -3, -4
+OMDG_ENOMEM, OMDG_ESTATE, OMDG_EFILE, OMDG_ENONFINITE = -5, -6, -7, -8
+
 # every symbol include/omdg.h declares, with its ctypes signature
 _P = ctypes.POINTER
 _d, _i, _l, _vp, _cp = ctypes.c_double, ctypes.c_int, ctypes.c_long, ctypes.c_void_p, ctypes.c_char_p
@@ -111,6 +114,8 @@ SIGNATURES = {
     "omdg_set_compat": [_vp, _cp, _i],
     "omdg_stats": [_vp, _P(_l), _P(_l)],
     "omdg_wide_centres": [_vp, _P(_i)],
+    "omdg_set_wait_polls": [_i],
+    "omdg_selftest_wait": [_i, _i, _P(ctypes.c_uint)],
     "omdg_set_launch": [_vp, _cp, _i],
     "omdg_get_launch": [_vp, _cp, _P(_i)],
     "omdg_autotune": [_vp, _i, _P(_d)],
@@ -187,6 +192,23 @@ def load(path: str = LIB_PATH):
         fn.restype = _cp if name in STRING_RESULT else _i
     _lib = lib
     return lib
+
+
+def set_wait_polls(polls):
+    """omdg_set_wait_polls: poll limit of the tensor-core kernels' waits (0: default)."""
+    rc = load().omdg_set_wait_polls(int(polls))
+    if rc != OMDG_OK:
+        raise OMDGError(rc, "omdg_set_wait_polls(%d)" % polls)
+
+
+def selftest_wait(which, polls):
+    """omdg_selftest_wait: the status word after making a bounded wait run
+    out (which 0: mbarrier in a TMEM-holding CTA, 1: grid barrier)."""
+    st = ctypes.c_uint(0)
+    rc = load().omdg_selftest_wait(int(which), int(polls), ctypes.byref(st))
+    if rc != OMDG_OK:
+        raise OMDGError(rc, "omdg_selftest_wait")
+    return st.value
 
 
 def count_neighbors_static(x_ptr, n, lo, hi, periodic, rcut, count_ptr, stream=None):

@@ -149,7 +149,14 @@ int omdg_set_timestep(omdg_ctx* ctx, double dt);
  */
 int omdg_step(omdg_ctx* ctx, int nsteps);
 /* omdg_step without the final wait: enqueues nsteps on the context stream.
-   omdg_sync waits for them, checks the device status and updates the ledger. */
+   omdg_sync waits for them, checks the device status and updates the ledger.
+   When a list rebuild inside the queued steps needs longer rows than were
+   allocated (the reference grows its rows instead, VerletListFull.cpp:127-136),
+   the steps after it are discarded: omdg_sync restores the state that rebuild
+   started from, grows the rows, redoes that step and replays the rest, so the
+   result equals a run with ample rows bit for bit (not with the two-temperature
+   model, whose electron state is outside the restored copy: there the overflow
+   is reported as OMDG_ESTATE). */
 int omdg_step_async(omdg_ctx* ctx, int nsteps);
 int omdg_sync(omdg_ctx* ctx);
 /* One MD call driven from host arrays (caller order, n*3 FP64; any pointer
@@ -204,7 +211,9 @@ int omdg_wide_centres(omdg_ctx* ctx, int* count);
  * knots in shared memory), "eam_ctas_per_sm", "pair_block", "pair_lanes",
  * "tb_block", "tb_lanes", "nbr_hshift" (log2 of the neighbour slice height),
  * "build_lanes" (list build: 0 cell CTAs, else threads per atom), "io_blocks"
- * (blocks of omdg_step_io's downloads beside the step's kernels).
+ * (blocks of omdg_step_io's downloads beside the step's kernels), "nbr_capacity"
+ * (row capacity of the next first list build; 0 sizes it from the density;
+ * rows grow by themselves when a build needs more).
  */
 int omdg_set_launch(omdg_ctx* ctx, const char* key, int value);
 int omdg_get_launch(omdg_ctx* ctx, const char* key, int* value);

@@ -182,6 +182,7 @@ static void free_atoms(Context* c) {
                     c->fy,   c->fz,    c->pe,     c->vir,    c->pack,        c->xref,        c->loc,         c->type,
                     c->id,   c->inv,   c->fp,     c->femb,   c->cell,        c->perm,        c->stage_d,
                     c->stage_i, c->cell_sorted, c->f64, c->extra, c->stage_extra, c->nnb, c->d_red, c->aflag,
+                    c->snap_d, c->snap_i,
                     c->ters_wide};
     for (void* p : ptrs) cudaFree(p);
     c->x = c->y = c->z = c->vx = c->vy = c->vz = nullptr;
@@ -196,6 +197,8 @@ static void free_atoms(Context* c) {
     c->stage_i = nullptr;
     c->cell_sorted = nullptr;
     c->f64 = nullptr;
+    c->snap_d = nullptr;
+    c->snap_i = nullptr;
     c->extra = c->stage_extra = nullptr;
     c->nnb = nullptr;
     c->d_red = nullptr;
@@ -215,6 +218,8 @@ static int alloc_atoms(Context* c, int n) {
               dalloc(c->cell_sorted, cap) && dalloc(c->nnb, cap) && dalloc(c->ters_wide, (size_t)cap + 1);
     int nb = grid_for(cap, RED_BLOCK) + 1;
     ok = ok && dalloc(c->d_red, (size_t)4 * nb);
+    ok = ok && dalloc(c->snap_d, (size_t)6 * cap) && dalloc(c->snap_i, (size_t)3 * cap);
+    if (ok && !c->snap_state) ok = cudaMalloc(&c->snap_state, step_state_bytes()) == cudaSuccess;
     if (!ok) return set_error(c, OMDG_ENOMEM, "atom arrays");
     c->cap = cap;
     c->red_cap = nb;
@@ -328,6 +333,7 @@ int omdg_destroy(omdg_ctx* c) {
         g_graphs.erase(it);
     }
     free_atoms(c);
+    cudaFree(c->snap_state);
     cudaFree(c->nbr);
     cudaFree(c->rev);
     cudaFree(c->slot_buf);
@@ -878,7 +884,7 @@ static int build_list(Context* c) {
         }
         double rv = c->rc_max + c->skin;
         double est = c->n / vol * 4.18879 * rv * rv * rv;
-        int m = (int)(2.0 * est) + 32;
+        int m = c->nbr_capacity > 0 ? c->nbr_capacity : (int)(2.0 * est) + 32;
         int rc = nlist_reserve(c, m);
         if (rc) return rc;
     }
@@ -1001,7 +1007,9 @@ static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr)
             if (e != cudaSuccess) rc = check_cuda(c, e, "body capture");
             if (!rc) {
                 c->stream = gs.side;
+                c->build_in_step = true;
                 rc = nlist_build(c);
+                c->build_in_step = false;
                 c->stream = s;
                 cudaGraph_t body_out = nullptr;
                 e = cudaStreamEndCapture(gs.side, &body_out);
@@ -1340,7 +1348,10 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
             if (c->ttm && ttm_active(c) && (rc = ttm_pre(c))) return rc;
             if ((rc = energy_source(c))) return rc;
             if ((rc = integrate_kick_drift(c, k))) return rc;
-            if ((rc = eager_maybe_rebuild(c))) return rc;
+            c->build_in_step = true;
+            rc = eager_maybe_rebuild(c);
+            c->build_in_step = false;
+            if (rc) return rc;
             if ((rc = forces_compute(c))) return rc;
             if ((rc = integrate_kick(c, k))) return rc;
             if (c->ttm && (rc = thermo_detect(c, true))) return rc;
@@ -1362,6 +1373,67 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
     return OMDG_OK;
 }
 
+}  // extern "C"
+
+namespace omdg {
+
+// A neighbour row overflowed in a rebuild of the queued steps.  Every later
+// rebuild was skipped, so the snapshot holds the input of that rebuild (the
+// state after the step's first half-kick and drift).  Restore it, grow the
+// rows, redo the rebuild and the rest of that step, then replay the steps
+// still owed.  The counting sort and the list are deterministic functions of
+// that state, so the trajectory is the one an ample capacity gives, bit for
+// bit.  (The two-temperature model keeps electron state outside the
+// snapshot; a run with it reports the overflow instead.)
+static int recover_overflow(omdg_ctx* c) {
+    const long owed_total = c->async_steps;
+    int need = 0;
+    cudaError_t e = cudaMemcpy(&need, c->d_flags + 1, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return check_cuda(c, e, "overflow recovery");
+    // restore the rebuild's input and the step state as it was then
+    {
+        const size_t n = (size_t)c->n, cap = (size_t)c->cap;
+        double* dst_d[6] = {c->x, c->y, c->z, c->vx, c->vy, c->vz};
+        for (int k = 0; k < 6 && e == cudaSuccess; k++)
+            e = cudaMemcpyAsync(dst_d[k], c->snap_d + k * cap, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream);
+        int* dst_i[3] = {c->type, c->id, reinterpret_cast<int*>(c->aflag)};
+        for (int k = 0; k < 3 && e == cudaSuccess; k++)
+            e = cudaMemcpyAsync(dst_i[k], c->snap_i + k * cap, sizeof(int) * n, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->d_state, c->snap_state, step_state_bytes(), cudaMemcpyDeviceToDevice, c->stream);
+        const int zero = 0;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(step_state_halted(c), &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return check_cuda(c, e, "overflow recovery");
+    }
+    int rowk = 0;  // ledger rows restart with the queued steps: the failed step's row is its index
+    int rc = step_state_read(c, nullptr, &rowk, nullptr);
+    if (rc) return rc;
+    // grow the rows (status cleared), then the failed step's rebuild and the rest of that step
+    static const unsigned blank[ST_RANGE_SRC + 1] = {0u, ~0u, ~0u, ~0u, ~0u};
+    cudaMemcpy(c->d_status, blank, sizeof(blank), cudaMemcpyHostToDevice);
+    const int m = (int)(1.25 * std::max(need, c->maxnb)) + 16;
+    c->maxnb = 0;
+    if ((rc = nlist_reserve(c, m))) return rc;
+    invalidate_graph(c);
+    if ((rc = build_list(c))) return rc;
+    if ((rc = threebody_prepare(c))) return rc;
+    if ((rc = forces_compute(c))) return rc;
+    if ((rc = integrate_kick(c, 0))) return rc;
+    if ((rc = check_status(c))) return rc;
+    c->overflow_recoveries++;
+    const long done = (long)rowk + 1;  // steps finished, the recovered one included
+    const long owed = owed_total - done;
+    if (owed > 0 && (rc = omdg_step_async(c, (int)owed))) return rc;
+    c->async_steps = owed_total;
+    return omdg_sync(c);
+}
+
+}  // namespace omdg
+
+extern "C" {
+
 int omdg_sync(omdg_ctx* c) {
     if (!c) return OMDG_EINVAL;
     cudaSetDevice(c->device);
@@ -1374,6 +1446,9 @@ int omdg_sync(omdg_ctx* c) {
     const int expect = (c->async_steps > 0 && c->async_steps <= c->ledger_cap) ? (int)c->async_steps : 0;
     int rc = step_state_fetch(c, &status, &step, &rows, &elapsed, expect);  // waits for the queued steps
     if (rc) return rc;
+    if ((status & ERR_NBR_OVERFLOW) && !(status & ~ERR_NBR_OVERFLOW) && c->async_steps > 0 && c->snap_d &&
+        !(c->ttm && ttm_active(c)))
+        return recover_overflow(c);
     if ((rc = status_error(c, status))) {
         if (rc == OMDG_ESTATE) {
             // a neighbour row overflowed during the run: grow for the next call
@@ -1470,7 +1545,12 @@ int omdg_step_io(omdg_ctx* c, const double* x_in, const double* v_in, int nsteps
     c->graph_steps += 1;
     c->launches += gs.io_kernels;
     c->async_steps += 1;
-    return omdg_sync(c);
+    const long rec0 = c->overflow_recoveries;
+    if ((rc = omdg_sync(c))) return rc;
+    // a replay after a row overflow redid the steps whose outputs the graph wrote
+    if (c->overflow_recoveries != rec0 && (x_out || v_out || f_out))
+        return omdg_get_state(c, x_out, v_out, f_out, nullptr, nullptr);
+    return OMDG_OK;
 }
 
 int omdg_replica_ledger(omdg_ctx* c, int nrep, double* kinetic, double* potential) {
@@ -1721,6 +1801,7 @@ static int* launch_knob(Context* c, const std::string& k) {
     if (k == "nbr_hshift") return &c->nbr_hshift;
     if (k == "build_lanes") return &c->build_lanes;
     if (k == "io_blocks") return &c->io_blocks;
+    if (k == "nbr_capacity") return &c->nbr_capacity;
     return nullptr;
 }
 
@@ -1733,6 +1814,7 @@ static bool valid_knob(const std::string& k, int v) {
     if (k == "eam_stage") return v == 0 || v == 1;
     if (k == "build_lanes") return v == 0 || v == 1 || v == 4 || v == 8;
     if (k == "io_blocks") return v >= 1 && v <= 65535;
+    if (k == "nbr_capacity") return v >= 0 && v <= 4096;
     return false;
 }
 
@@ -1791,6 +1873,10 @@ int omdg_set_launch(omdg_ctx* c, const char* key, int value) {
     if (*p == value) return OMDG_OK;
     *p = value;
     if (k == "build_lanes") c->list_valid = false;
+    if (k == "nbr_capacity") {  // applies at the next first build
+        c->list_valid = false;
+        c->maxnb = 0;
+    }
     if (k == "nbr_hshift") {
         // the list layout changes: reallocate and rebuild before the next use
         int m = c->maxnb;

@@ -34,6 +34,7 @@ struct StepState {
     double sqrmaxv;          // SqrMaxVelocity of the last measurement (system.cpp:1075-1094)
     int src_first;           // EnergySource: the first call inside the window only arms it
     int src_scale;           // EnergySource: scale velocities at the next PreIntegration
+    int halted;              // a rebuild overflowed its rows: later rebuilds are skipped until omdg_sync recovers
 };
 
 struct IntParams {
@@ -714,6 +715,7 @@ __global__ void k_rewind(StepState* st, int rebuild_every) {
 // Device address of the step state's ledger row counter (read by kernels
 // that fill columns of the current row).
 const int* step_state_row(Context* c) { return &reinterpret_cast<StepState*>(c->d_state)->row; }
+int* step_state_halted(Context* c) { return &reinterpret_cast<StepState*>(c->d_state)->halted; }
 
 int step_state_rewind(Context* c) {
     k_rewind<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state), c->rebuild_every);
@@ -754,6 +756,7 @@ int step_state_init(Context* c) {
     h.sqrmaxv = 0.0;
     h.src_first = 1;
     h.src_scale = 0;
+    h.halted = 0;
     cudaError_t e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return check_cuda(c, e, "step state");
@@ -863,8 +866,9 @@ int step_clear_rebuild(Context* c) {
 // Graph-side rebuild predicate: copies the request into the conditional
 // handle and clears it.
 __global__ void k_set_rebuild_cond(StepState* st, cudaGraphConditionalHandle h) {
-    cudaGraphSetConditional(h, st->rebuild ? 1u : 0u);
-    if (st->rebuild) st->nrebuild += 1;
+    const bool go = st->rebuild && !st->halted;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+    if (go) st->nrebuild += 1;
     st->rebuild = 0;
 }
 

@@ -281,6 +281,31 @@ __global__ void k_permute_gather(int n, const int* __restrict__ perm, AtomArrays
     for (int q = 0; q < a.extra_n; q++) st.extra[(size_t)q * n + k] = a.extra[(size_t)q * n + o];
 }
 
+// The state a rebuild reorders, copied before the rebuild of a step (unless
+// an earlier rebuild of the queued steps overflowed: then the copy of that
+// rebuild's input is kept), with the step state.
+__global__ void k_snapshot(int n, const int* __restrict__ halted, AtomArrays a, AtomArrays snap,
+                           const unsigned char* __restrict__ st, unsigned char* __restrict__ st_snap, int st_bytes) {
+    if (*halted) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < st_bytes) st_snap[k] = st[k];
+    if (k >= n) return;
+    snap.x[k] = a.x[k];
+    snap.y[k] = a.y[k];
+    snap.z[k] = a.z[k];
+    snap.vx[k] = a.vx[k];
+    snap.vy[k] = a.vy[k];
+    snap.vz[k] = a.vz[k];
+    snap.type[k] = a.type[k];
+    snap.id[k] = a.id[k];
+    snap.flag[k] = a.flag[k];
+}
+
+// An overflowed build halts the queued steps' later rebuilds.
+__global__ void k_halt_on_overflow(const unsigned* __restrict__ status, int* halted) {
+    if (*status & ERR_NBR_OVERFLOW) *halted = 1;
+}
+
 __global__ void k_permute_copyback(int n, AtomArrays st, AtomArrays a) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -1004,6 +1029,17 @@ int nlist_build(Context* c) {
     if (rc) return rc;
     cudaStream_t s = c->stream;
     prof_begin(c, "cell_sort");
+    if (c->build_in_step && c->snap_d) {
+        AtomArrays cur0{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->aflag, nullptr, 0};
+        AtomArrays snap{c->snap_d, c->snap_d + c->cap, c->snap_d + 2 * (size_t)c->cap, c->snap_d + 3 * (size_t)c->cap,
+                        c->snap_d + 4 * (size_t)c->cap, c->snap_d + 5 * (size_t)c->cap, c->snap_i,
+                        c->snap_i + c->cap, reinterpret_cast<unsigned*>(c->snap_i + 2 * (size_t)c->cap), nullptr, 0};
+        const int sb = (int)step_state_bytes();
+        k_snapshot<<<grid_for(std::max(n, sb), 256), 256, 0, s>>>(
+            n, step_state_halted(c), cur0, snap, static_cast<const unsigned char*>(c->d_state),
+            static_cast<unsigned char*>(c->snap_state), sb);
+        c->launches++;
+    }
     k_zero_ints<<<grid_for(m + 1, 256), 256, 0, s>>>(m + 1, c->cell_count, c->cell_fill);
     if (reps)
         k_cell_assign_rep<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->d_rep_of,
@@ -1109,6 +1145,10 @@ int nlist_build(Context* c) {
                                                         c->d_flags + 1);
     }
     c->launches++;
+    if (c->build_in_step) {
+        k_halt_on_overflow<<<1, 1, 0, s>>>(c->d_status, step_state_halted(c));
+        c->launches++;
+    }
     prof_end(c);
     if (c->need_rev) {
         prof_begin(c, "nlist_reverse");

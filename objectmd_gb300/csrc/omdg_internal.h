@@ -217,6 +217,16 @@ struct Context {
     // neighbour list: nbr[s*n + i] = j | code << 26, count in nnb[i]
     int* nbr = nullptr;
     int* nnb = nullptr;
+    // list overflow inside queued steps: every in-step rebuild first copies the
+    // state it reorders (positions, velocities, types, ids, flags) and the step
+    // state here; a rebuild that overflows halts later rebuilds, and omdg_sync
+    // restores this copy, grows the list and replays from that rebuild
+    double* snap_d = nullptr;   // 6 x cap: x, y, z, vx, vy, vz
+    int* snap_i = nullptr;      // 3 x cap: type, id, flags
+    void* snap_state = nullptr; // StepState
+    bool build_in_step = false; // the build being issued belongs to a step (snapshot and halt)
+    int nbr_capacity = 0;       // launch key: the first build's row capacity (0: from the density)
+    long overflow_recoveries = 0;  // queued steps replayed after a row overflow
     int* rev = nullptr;       // slot of i in row j (three-body kernels)
     float4* slot_buf = nullptr;  // per-slot force contributions (three-body kernels)
     int* ters_wide = nullptr;    // Tersoff centres past the register path: [0] count, then their indices
@@ -349,6 +359,8 @@ int nn_launch(Context* c, Potential& pot, bool first);
 int replica_prepare(Context* c);  // per-replica cell grids and shifts (host, before a build)
 int thermo_detect(Context* c, bool after_step);  // local thermodynamics (ttm.cu); after_step: the step advanced the ledger row
 const int* step_state_row(Context* c);           // device address of the ledger row counter (integrate.cu)
+int* step_state_halted(Context* c);              // device address of the step state's halt flag
+size_t step_state_bytes();
 double thermo_ercut(const Context* c);  // the detector's cutoff (its own, else the largest force cutoff); -1: off
 int ttm_pre(Context* c);          // electron temperature step and rescaling before a step
 void ttm_release(Context* c);

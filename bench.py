@@ -16,11 +16,17 @@ repeats the K steps through the public C ABI (omdg_step_io) with pinned host
 buffers: every step uploads positions and velocities, steps, and reads
 positions, velocities, forces and the energy ledger back.
 
+The default run also times, as sub-objects of its one JSON line, Tersoff Si
+diamond 40^3 = 512,000 atoms at 1000 K and the neural surrogate on the same
+cell (with its force RMSE against Tersoff), each with its HBM and
+instruction-issue roofs (the MLP: its tensor-pipe fraction) and a one-core
+CPU baseline (--no-sub leaves them out).
+
 --impl reference times the oracle's CPU restatement of the same path
-(oracle/omd_oracle.c, compiled on this host) on every host core: one process
-per core, each an independent EAM box of the same shape and density (the
-reference's MPI domain decomposition at ideal scaling), rebuilding its
-neighbour list every step as the reference does by default.
+(oracle/omd_oracle.c, compiled on this host, pinned to the reference's own
+outputs) on the same box as the GPU arm, in as many OpenMP threads as the
+host has, with both of the reference's rebuild policies: the list rebuilt
+every step (its default) and every 10 steps (comm.refresh 10).
 """
 from __future__ import annotations
 
@@ -249,6 +255,115 @@ def mean_neighbours(ctx):
     return float(len(j)) / max(1, len(off) - 1)
 
 
+# MLP of the surrogate, per atom: z1 = G W1 (32x64), z2 = a1 W2 (64x64) and the
+# two products of the force backward pass (64x64, 64x32), 2 flops per MAC
+MLP_FLOP_PER_ATOM = 2 * (32 * 64 + 64 * 64 + 64 * 64 + 64 * 32)
+
+
+def load_inst(kernel):
+    """Warp instructions per atom of one launch (committed ncu figures)."""
+    p = os.path.join(ROOT, "profiles", "instructions_per_atom.txt")
+    try:
+        for line in open(p):
+            f = line.split()
+            if len(f) == 2 and f[0] == kernel:
+                return float(f[1])
+    except OSError:
+        pass
+    return None
+
+
+def issue_roof(kernel, n, t_ms, torch, device):
+    """Instruction-issue roof: every SM sub-partition issues one warp
+    instruction a cycle at the maximum SM clock (MEASURED_PEAKS.json)."""
+    ipa = load_inst(kernel)
+    if ipa is None or not t_ms:
+        return None
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    try:
+        mhz = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["sm_max_mhz"])
+    except Exception:
+        mhz = 2070.0
+    peak = 4 * sms * mhz * 1e6 / 1e12
+    achieved = ipa * n / (t_ms * 1e-3) / 1e12
+    return {"bound": "issue", "kernel": kernel, "warp_instructions_per_atom": ipa, "achieved": round(achieved, 4),
+            "peak": round(peak, 4), "unit": "T warp-instructions/s", "frac": round(achieved / peak, 4),
+            "source": "ncu smsp__inst_executed per atom (profiles/instructions_per_atom.txt) / CUDA-event time"}
+
+
+def timed_steps(ctx, n, steps, stream, flush_l2, torch):
+    """Device time of `steps` graph-replayed steps, each bracketed by events
+    on the context stream with an L2 flush before it; then the per-kernel
+    times of the same number of eagerly launched steps."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    st0 = ctx.stats()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush_l2()
+            starts[k].record(stream)
+            ctx.step_async(1)
+            ends[k].record(stream)
+    ctx.sync()
+    torch.cuda.synchronize()
+    st1 = ctx.stats()
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ctx.set_profiling(True)
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush_l2()
+            ctx.step_async(1)
+    ctx.sync()
+    kt = ctx.kernel_times()
+    ctx.set_profiling(False)
+    kernels = {k: {"ms_per_launch": ms / max(1, c), "launches": c} for k, (ms, c) in kt.items()}
+    return total_ms, kernels, st1["rebuilds"] - st0["rebuilds"], st1["launches"] - st0["launches"]
+
+
+def sub_workload(name, args, device, torch, flush_l2):
+    """Another configured workload, measured as the main one (device-timed
+    atom-steps/s, per-kernel times, HBM and issue roofs, one-core CPU
+    baseline); for the surrogate also its force RMSE against Tersoff, plain
+    Tersoff on the same cell and the MLP's tensor-pipe fraction."""
+    w, x, v, lo, hi = make_workload(name)
+    n = len(x)
+    ctx = make_context(w, x, v, lo, hi, device=device, tune=not args.no_tune)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+    ctx.step(max(3, args.warmup))
+    nf = mean_neighbours(ctx)
+    total_ms, kernels, rebuilds, launches = timed_steps(ctx, n, args.steps, stream, flush_l2, torch)
+    value = n * args.steps / (total_ms * 1e-3)
+    peaks = load_peaks()
+    out = {"workload": w["desc"], "value": value, "unit": UNIT, "ms_per_step": total_ms / args.steps,
+           "atoms": n, "mean_neighbours": round(nf, 2), "neighbour_rebuilds_in_timed_steps": rebuilds,
+           "gpu_launches": launches, "kernels": {k: round(v_["ms_per_launch"] * 1e3, 2) for k, v_ in kernels.items()},
+           "kernels_unit": "us per launch"}
+    cand = [(k, v_) for k, v_ in kernels.items() if k in ALG_BYTES]
+    if cand:
+        dom_name, dom = max(cand, key=lambda kv: kv[1]["ms_per_launch"] * kv[1]["launches"])
+        alg = ALG_BYTES[dom_name](nf) * n
+        ach = alg / (dom["ms_per_launch"] * 1e-3) / 1e9
+        out["roofline"] = {"bound": "hbm", "kernel": dom_name, "achieved": round(ach, 1), "peak": peaks["hbm"],
+                           "unit": "GB/s", "frac": round(ach / peaks["hbm"], 4), "traffic": load_traffic(dom_name, n),
+                           "peak_source": peaks["src"], "alg_bytes_per_launch": int(alg)}
+        out["issue_roofline"] = issue_roof(dom_name, n, dom["ms_per_launch"], torch, device)
+    if "nn_mlp" in kernels:
+        t = kernels["nn_mlp"]["ms_per_launch"]
+        tf = MLP_FLOP_PER_ATOM * n / (t * 1e-3) / 1e12
+        sus = load_peaks().get("bf16_sustained")
+        out["mlp_roofline"] = {"bound": "tensor", "kernel": "nn_mlp", "flop_per_atom": MLP_FLOP_PER_ATOM,
+                               "achieved": round(tf, 2), "peak": sus, "unit": "TFLOP/s",
+                               "frac": round(tf / sus, 4) if sus else None,
+                               "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops_sustained)"}
+    if w["kind"] == "nn":
+        out["surrogate"] = surrogate_report(ctx, w, x, v, lo, hi, device, args, torch)
+    ctx.close()
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(argparse.Namespace(**dict(vars(args), workload=name)))
+    return out
+
+
 # ------------------------------------------------------------------ GB300 arm
 def run_gpu(args):
     import torch
@@ -350,6 +465,7 @@ def run_gpu(args):
     surrogate = None
     if w["kind"] == "nn":
         surrogate = surrogate_report(ctx, w, x, v, lo, hi, device, args, torch)
+    issue = issue_roof(dom_name, n, dom_t, torch, device)
 
     out = {
         "metric": METRIC,
@@ -382,11 +498,27 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "energy": {"kinetic": led["kinetic"], "potential": led["potential"], "energy": led["energy"]},
         "surrogate": surrogate,
+        "issue_roofline": issue,
         "wall_s_timed_loop": t_wall1 - t_wall0,
     }
+    # the other headline workloads, as sub-objects of the same line
+    if args.workload == "eam_al_256k" and not args.ncell and not args.no_sub and world == 1:
+        ctx.close()
+        ctx = None
+        subs = {}
+        for name in ("tersoff_si_512k", "nn_si_512k"):
+            subs[name] = sub_workload(name, args, device, torch, flush_l2)
+        out["workloads"] = subs
+        nn, ts = subs["nn_si_512k"], subs["tersoff_si_512k"]
+        out["surrogate"] = {"nn_atom_steps_per_s": nn["value"], "tersoff_atom_steps_per_s": ts["value"],
+                            "nn_over_tersoff": nn["value"] / ts["value"],
+                            "force_rmse_eV_per_A": nn.get("surrogate", {}).get("after_md", {}).get(
+                                "force_rmse_eV_per_A"),
+                            "goal_eV_per_A": 0.030}
     if rank == 0:
         print(json.dumps(out), flush=True)
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -456,9 +588,10 @@ def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         d = json.load(open(p))
-        return {"hbm": float(d["hbm_gbs"]), "src": "measured (MEASURED_PEAKS.json hbm_gbs)"}
+        return {"hbm": float(d["hbm_gbs"]), "src": "measured (MEASURED_PEAKS.json hbm_gbs)",
+                "bf16_sustained": float(d.get("bf16_tflops_sustained", 0.0)) or None}
     except Exception:
-        return {"hbm": 6800.0, "src": "fallback 6.8 TB/s"}
+        return {"hbm": 6800.0, "src": "fallback 6.8 TB/s", "bf16_sustained": 1700.0}
 
 
 def load_traffic(kernel, n_atoms):
@@ -486,9 +619,11 @@ NN_MODEL = os.path.join(ROOT, "objectmd_gb300", "models", "nn_tersoff_si.nn")
 
 
 def _cpu_worker(args_tuple):
-    """One process: the oracle's step (kick-drift, wrap, neighbour list rebuilt
-    every step as the reference's default comm.refresh, forces, kick)."""
-    name, ncell, steps, warm = args_tuple
+    """The oracle's step (kick-drift, wrap, neighbour list rebuilt every
+    `refresh` steps -- 1 is the reference's default comm.refresh, 10 its
+    comm.refresh 10 -- forces, kick) on `threads` OpenMP threads."""
+    name, ncell, steps, warm, refresh, threads = args_tuple
+    os.environ["OMP_NUM_THREADS"] = str(threads)  # before the oracle library loads
     sys.path.insert(0, ROOT)
     from objectmd_gb300 import inputs
     from oracle import oracle as oc
@@ -519,11 +654,16 @@ def _cpu_worker(args_tuple):
     v = np.ascontiguousarray(v)
     f = np.zeros((n, 3))
     dt = w["dt"]
+    bufs = (np.zeros(n + 1, dtype=np.int32), np.zeros(n * 160, dtype=np.int32), np.zeros(n * 160, dtype=np.int32))
+    state = {"nb": None, "k": 0}
 
     def one_step():
         oc.vv_kick_drift(x, v, f, mass, dt)
-        x[:] = oc.wrap(box, x)
-        f[:] = force(oc.neighbors(box, x, rv))
+        if state["nb"] is None or state["k"] % refresh == 0:
+            x[:] = oc.wrap(box, x)
+            state["nb"] = oc.neighbors(box, x, rv, buffers=bufs)
+        state["k"] += 1
+        f[:] = force(state["nb"])
         oc.vv_kick(v, f, mass, dt)
 
     for _ in range(warm):
@@ -541,41 +681,50 @@ def cpu_baseline(args):
     nc = CPU_SAMPLE_NCELL[kind]
     ctx = mp.get_context("spawn")
     with ctx.Pool(1) as pool:
-        n, steps, sec = pool.map(_cpu_worker, [(args.workload, nc, args.cpu_steps, 1)])[0]
+        n, steps, sec = pool.map(_cpu_worker, [(args.workload, nc, args.cpu_steps, 1, 1, 1)])[0]
     return {"value": n * steps / sec, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": "%s, lattice %d^3 = %d atoms, %d steps (neighbour list rebuilt every step, as the reference's "
                       "default comm.refresh), oracle/omd_oracle.c on one host core" % (kind, nc, n, steps)}
 
 
 def run_reference(args):
+    """The reference's algorithm (the oracle port: oracle/omd_oracle.c, pinned
+    to the reference's own outputs to 1e-12) on the same box as the GPU arm,
+    all host threads, under both of the reference's rebuild policies: the list
+    rebuilt every step (comm.refresh unset, its default) and every 10 steps
+    (comm.refresh 10).  The line's value is the faster of the two."""
     rank, world, local = dist_env()
     if rank != 0:
         return
     cores = os.cpu_count() or 1
     w = WORKLOADS[args.workload]
-    desc, nc, basis = w["desc"], args.ncell or w["ncell"], BASIS[w["kind"]]
-    n_total = basis * nc ** 3
-    # split the box into `cores` equal sub-boxes of the same density
-    per = max(1, n_total // cores)
-    sub = max(3, int(round((per / basis) ** (1.0 / 3.0))))
-    steps = max(1, min(args.steps, 5))
+    desc = w["desc"] if not args.ncell else "%s (ncell %d)" % (w["desc"], args.ncell)
+    steps = max(10, args.steps)
+    warm = max(1, min(args.warmup, 3))
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(args.workload, sub, steps, max(0, min(args.warmup, 1)))] * cores)
+    policies = {}
+    with ctx.Pool(1) as pool:
+        for refresh in (1, 10):
+            n, k, sec = pool.map(_cpu_worker, [(args.workload, args.ncell or None, steps, warm, refresh, cores)])[0]
+            policies[refresh] = (n, k, sec)
     t1 = time.perf_counter()
-    atoms = sum(r[0] for r in res)
-    slowest = max(r[2] for r in res)
-    value = atoms * steps / slowest
-    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
-           "warmup": args.warmup, "ms_per_step": slowest / steps * 1e3, "higher_is_better": True,
+    rates = {r: n * k / sec for r, (n, k, sec) in policies.items()}
+    best = max(rates, key=rates.get)
+    n, k, sec = policies[best]
+    value = rates[best]
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": k,
+           "warmup": args.warmup, "ms_per_step": sec / k * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": desc, "atoms_total": atoms, "host_processes": cores,
-                      "per_process": "%s lattice %d^3 = %d atoms" % (w["kind"], sub, basis * sub ** 3)},
+           "config": {"workload": desc, "atoms_total": n, "host_threads": cores,
+                      "rebuild_policy": "every %d steps (comm.refresh %d)" % (best, best) if best > 1 else
+                      "every step (comm.refresh unset)"},
+           "rebuild_policies": {"every_step": {"value": rates[1], "ms_per_step": policies[1][2] / k * 1e3},
+                                "refresh_10": {"value": rates[10], "ms_per_step": policies[10][2] / k * 1e3}},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": "%d independent %s boxes of %d atoms, %d steps each, neighbour list rebuilt "
-                                      "every step (oracle/omd_oracle.c, the reference's algorithm restated)" %
-                                      (cores, w["kind"], basis * sub ** 3, steps)},
+                            "sample": "the GPU arm's box (%d atoms), %d steps per policy after %d warm-up, "
+                                      "oracle/omd_oracle.c (the reference's algorithm restated and pinned to its "
+                                      "outputs to 1e-12) in %d OpenMP threads" % (n, k, warm, cores)},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "wall_s": t1 - t0}
     print(json.dumps(out), flush=True)
@@ -594,6 +743,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="time only --workload (the default run adds Tersoff Si 512k and the NN surrogate)")
     ap.add_argument("--skin", type=float, default=None,
                     help="Verlet skin in A instead of the workload's (omdg_set_neighbor)")
     ap.add_argument("--launch", action="append", default=[], metavar="KEY=VALUE",

@@ -9,6 +9,9 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
@@ -113,6 +116,72 @@ static int cmp_tuple(const void* a, const void* b) {
     return x->code < y->code ? -1 : (x->code > y->code);
 }
 
+/* The sorted row of atom i: every (j, image) with r^2 <= rsq over the
+   linked cells (VerletList.cpp:76-199 with the ghost images of
+   comhandler.cpp:288-377).  Returns its length; *row grows as needed. */
+static int atom_row(const oc_box* box, const double* x, double rsq, const int* nc, const int* cell, const int* head,
+                    const int* next, int i, oc_tuple** row, int* rowcap) {
+    int ci[3] = {cell[i] % nc[0], (cell[i] / nc[0]) % nc[1], cell[i] / (nc[0] * nc[1])};
+    int cand_c[3][64], cand_s[3][64], ncand[3];
+    for (int d = 0; d < 3; d++) {
+        ncand[d] = 0;
+        if (box->periodic[d]) {
+            if (nc[d] >= 3) {
+                for (int o = -1; o <= 1; o++) {
+                    int c = ci[d] + o, s = 0;
+                    if (c < 0) {
+                        c += nc[d];
+                        s = -1;
+                    } else if (c >= nc[d]) {
+                        c -= nc[d];
+                        s = 1;
+                    }
+                    cand_c[d][ncand[d]] = c;
+                    cand_s[d][ncand[d]++] = s;
+                }
+            } else {
+                for (int c = 0; c < nc[d]; c++)
+                    for (int s = -1; s <= 1; s++) {
+                        cand_c[d][ncand[d]] = c;
+                        cand_s[d][ncand[d]++] = s;
+                    }
+            }
+        } else {
+            for (int o = -1; o <= 1; o++) {
+                int c = ci[d] + o;
+                if (c < 0 || c >= nc[d]) continue;
+                cand_c[d][ncand[d]] = c;
+                cand_s[d][ncand[d]++] = 0;
+            }
+        }
+    }
+    int nrow = 0;
+    for (int a = 0; a < ncand[2]; a++)
+        for (int b = 0; b < ncand[1]; b++)
+            for (int c = 0; c < ncand[0]; c++) {
+                int code = (cand_s[0][c] + 1) + 3 * (cand_s[1][b] + 1) + 9 * (cand_s[2][a] + 1);
+                double s[3];
+                shift_vec(box, code, s);
+                long cc = ((long)cand_c[2][a] * nc[1] + cand_c[1][b]) * nc[0] + cand_c[0][c];
+                for (int j = head[cc]; j >= 0; j = next[j]) {
+                    if (j == i && code == 13) continue;
+                    double dd[3];
+                    double r2 = pair_dist2(x + 3 * i, x + 3 * j, s, dd);
+                    if (r2 <= rsq) {
+                        if (nrow == *rowcap) {
+                            *rowcap *= 2;
+                            *row = (oc_tuple*)realloc(*row, sizeof(oc_tuple) * (*rowcap));
+                        }
+                        (*row)[nrow].j = j;
+                        (*row)[nrow].code = code;
+                        nrow++;
+                    }
+                }
+            }
+    qsort(*row, nrow, sizeof(oc_tuple), cmp_tuple);
+    return nrow;
+}
+
 long oc_neighbors(const oc_box* box, int n, const double* x, double rv, int* offsets, int* nbr_j, int* nbr_code,
                   long cap) {
     double rsq = rv * rv;
@@ -161,85 +230,70 @@ long oc_neighbors(const oc_box* box, int n, const double* x, double rv, int* off
         next[i] = head[cell[i]];
         head[cell[i]] = i;
     }
-    /* per axis: the list of (cell offset target, image) pairs to visit */
     long count = 0;
-    oc_tuple* row = (oc_tuple*)malloc(sizeof(oc_tuple) * 4096);
-    int rowcap = 4096;
-    for (int i = 0; i < n; i++) {
-        int ci[3] = {cell[i] % nc[0], (cell[i] / nc[0]) % nc[1], cell[i] / (nc[0] * nc[1])};
-        int cand_c[3][64], cand_s[3][64], ncand[3];
-        for (int d = 0; d < 3; d++) {
-            ncand[d] = 0;
-            if (box->periodic[d]) {
-                if (nc[d] >= 3) {
-                    for (int o = -1; o <= 1; o++) {
-                        int c = ci[d] + o, s = 0;
-                        if (c < 0) {
-                            c += nc[d];
-                            s = -1;
-                        } else if (c >= nc[d]) {
-                            c -= nc[d];
-                            s = 1;
-                        }
-                        cand_c[d][ncand[d]] = c;
-                        cand_s[d][ncand[d]++] = s;
-                    }
-                } else {
-                    for (int c = 0; c < nc[d]; c++)
-                        for (int s = -1; s <= 1; s++) {
-                            cand_c[d][ncand[d]] = c;
-                            cand_s[d][ncand[d]++] = s;
-                        }
+    int nth = 1;
+#ifdef _OPENMP
+    nth = omp_get_max_threads();
+#endif
+    if (nth <= 1) {
+        oc_tuple* row = (oc_tuple*)malloc(sizeof(oc_tuple) * 4096);
+        int rowcap = 4096;
+        for (int i = 0; i < n; i++) {
+            int nrow = atom_row(box, x, rsq, nc, cell, head, next, i, &row, &rowcap);
+            offsets[i] = (int)count;
+            for (int k = 0; k < nrow; k++) {
+                if (count >= cap) {
+                    free(row);
+                    free(cell);
+                    free(head);
+                    free(next);
+                    return -1;
                 }
-            } else {
-                for (int o = -1; o <= 1; o++) {
-                    int c = ci[d] + o;
-                    if (c < 0 || c >= nc[d]) continue;
-                    cand_c[d][ncand[d]] = c;
-                    cand_s[d][ncand[d]++] = 0;
-                }
+                nbr_j[count] = row[k].j;
+                nbr_code[count] = row[k].code;
+                count++;
             }
         }
-        int nrow = 0;
-        for (int a = 0; a < ncand[2]; a++)
-            for (int b = 0; b < ncand[1]; b++)
-                for (int c = 0; c < ncand[0]; c++) {
-                    int code = (cand_s[0][c] + 1) + 3 * (cand_s[1][b] + 1) + 9 * (cand_s[2][a] + 1);
-                    double s[3];
-                    shift_vec(box, code, s);
-                    long cc = ((long)cand_c[2][a] * nc[1] + cand_c[1][b]) * nc[0] + cand_c[0][c];
-                    for (int j = head[cc]; j >= 0; j = next[j]) {
-                        if (j == i && code == 13) continue;
-                        double dd[3];
-                        double r2 = pair_dist2(x + 3 * i, x + 3 * j, s, dd);
-                        if (r2 <= rsq) {
-                            if (nrow == rowcap) {
-                                rowcap *= 2;
-                                row = (oc_tuple*)realloc(row, sizeof(oc_tuple) * rowcap);
-                            }
-                            row[nrow].j = j;
-                            row[nrow].code = code;
-                            nrow++;
-                        }
-                    }
+        offsets[n] = (int)count;
+        free(row);
+    } else {
+        /* threads (timing runs): row lengths, their prefix, then the rows */
+        int* len = (int*)malloc(sizeof(int) * (n > 0 ? n : 1));
+#pragma omp parallel
+        {
+            int rowcap = 4096;
+            oc_tuple* row = (oc_tuple*)malloc(sizeof(oc_tuple) * rowcap);
+#pragma omp for schedule(static)
+            for (int i = 0; i < n; i++) len[i] = atom_row(box, x, rsq, nc, cell, head, next, i, &row, &rowcap);
+            free(row);
+        }
+        for (int i = 0; i < n; i++) {
+            offsets[i] = (int)count;
+            count += len[i];
+        }
+        offsets[n] = (int)count;
+        free(len);
+        if (count > cap) {
+            free(cell);
+            free(head);
+            free(next);
+            return -1;
+        }
+#pragma omp parallel
+        {
+            int rowcap = 4096;
+            oc_tuple* row = (oc_tuple*)malloc(sizeof(oc_tuple) * rowcap);
+#pragma omp for schedule(static)
+            for (int i = 0; i < n; i++) {
+                int nrow = atom_row(box, x, rsq, nc, cell, head, next, i, &row, &rowcap);
+                for (int k = 0; k < nrow; k++) {
+                    nbr_j[offsets[i] + k] = row[k].j;
+                    nbr_code[offsets[i] + k] = row[k].code;
                 }
-        qsort(row, nrow, sizeof(oc_tuple), cmp_tuple);
-        offsets[i] = (int)count;
-        for (int k = 0; k < nrow; k++) {
-            if (count >= cap) {
-                free(row);
-                free(cell);
-                free(head);
-                free(next);
-                return -1;
             }
-            nbr_j[count] = row[k].j;
-            nbr_code[count] = row[k].code;
-            count++;
+            free(row);
         }
     }
-    offsets[n] = (int)count;
-    free(row);
     free(cell);
     free(head);
     free(next);
@@ -259,8 +313,11 @@ int oc_eam(const oc_box* box, int n, const double* x, const int* offsets, const 
            double* rho) {
     double rc_phi = oc_table_max_range(phi), rc_rho = oc_table_max_range(edens);
     double* fp = (double*)malloc(sizeof(double) * (n > 0 ? n : 1));
+    int bad = 0;
     zero3(n, f, e, vir);
-    /* density pass: team.cpp:81-92, R <= CutRadius of the density table */
+    /* density pass: team.cpp:81-92, R <= CutRadius of the density table
+       (every atom's sum is its own: threads change nothing but the time) */
+#pragma omp parallel for schedule(static) reduction(| : bad)
     for (int i = 0; i < n; i++) {
         double acc = 0.0;
         for (int k = offsets[i]; k < offsets[i + 1]; k++) {
@@ -270,22 +327,24 @@ int oc_eam(const oc_box* box, int n, const double* x, const int* offsets, const 
             if (R <= rc_rho) {
                 double v, dv;
                 if (oc_table_read(edens, R, &v, &dv)) {
-                    free(fp);
-                    return -1;
+                    bad = 1;
+                    break;
                 }
                 acc += v;
             }
         }
         rho[i] = acc;
-        double Fv, Fd;
-        if (oc_table_read(embed, acc, &Fv, &Fd)) {
-            free(fp);
-            return -1;
-        }
+        double Fv = 0.0, Fd = 0.0;
+        if (oc_table_read(embed, acc, &Fv, &Fd)) bad = 1;
         fp[i] = Fd;
         e[i] = Fv; /* team.cpp:135-145 */
     }
+    if (bad) {
+        free(fp);
+        return -1;
+    }
     /* force pass: team.cpp:224-237 and forcekernel.h:92-110 */
+#pragma omp parallel for schedule(static) reduction(| : bad)
     for (int i = 0; i < n; i++) {
         for (int k = offsets[i]; k < offsets[i + 1]; k++) {
             int j = nbr_j[k];
@@ -296,14 +355,14 @@ int oc_eam(const oc_box* box, int n, const double* x, const int* offsets, const 
             if (R <= rc_phi) {
                 double p, dp, rv_, drho;
                 if (oc_table_read(phi, R, &p, &dp)) {
-                    free(fp);
-                    return -1;
+                    bad = 1;
+                    break;
                 }
                 drho = 0.0;
                 if (!(R > rc_rho)) {
                     if (oc_table_read(edens, R, &rv_, &drho)) {
-                        free(fp);
-                        return -1;
+                        bad = 1;
+                        break;
                     }
                 }
                 double fr = -(fp[i] * drho + fp[j] * drho + dp) / R;
@@ -316,13 +375,15 @@ int oc_eam(const oc_box* box, int n, const double* x, const int* offsets, const 
         }
     }
     free(fp);
-    return 0;
+    return bad ? -1 : 0;
 }
 
 int oc_pair_table_typed(const oc_box* box, int n, const double* x, const int* type, int ta, int tb,
                         const int* offsets, const int* nbr_j, const int* nbr_code, const oc_table* phi, double* f,
                         double* e, double* vir) {
     double rc = oc_table_max_range(phi);
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
     for (int i = 0; i < n; i++) {
         for (int k = offsets[i]; k < offsets[i + 1]; k++) {
             int j = nbr_j[k];
@@ -335,7 +396,10 @@ int oc_pair_table_typed(const oc_box* box, int n, const double* x, const int* ty
             double r = sqrt(pair_dist2(x + 3 * i, x + 3 * j, s, d));
             if (r < rc) {
                 double p, dp;
-                if (oc_table_read(phi, r, &p, &dp)) return -1;
+                if (oc_table_read(phi, r, &p, &dp)) {
+                    bad = 1;
+                    break;
+                }
                 double fr = -dp / r;
                 f[3 * i + 0] += d[0] * fr;
                 f[3 * i + 1] += d[1] * fr;
@@ -345,7 +409,7 @@ int oc_pair_table_typed(const oc_box* box, int n, const double* x, const int* ty
             }
         }
     }
-    return 0;
+    return bad ? -1 : 0;
 }
 
 int oc_zbl(const oc_box* box, int n, const double* x, const int* type, int ta, int tb, double z1, double z2,

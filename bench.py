@@ -523,10 +523,14 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+SURROGATE_MD_STEPS = 500  # 0.5 ps of the surrogate's own MD before the "after_md" comparison
+
+
 def surrogate_report(ctx, w, x0, v0, lo, hi, device, args, torch):
     """Force RMSE of the surrogate against plain Tersoff on the starting
-    configuration and on the configuration the surrogate's MD reached, the
-    fallback count, and plain Tersoff's atom-steps/s on the same cell."""
+    configuration and after SURROGATE_MD_STEPS more steps of the surrogate's
+    own MD (the 1000 K start has equilibrated by then), the fallback count,
+    and plain Tersoff's atom-steps/s on the same cell."""
     from objectmd_gb300 import inputs, omdg
 
     tersoff = os.path.join(SI_DIR, "tersoff.silicon27")
@@ -544,7 +548,8 @@ def surrogate_report(ctx, w, x0, v0, lo, hi, device, args, torch):
             return c.get_state()["f"], (c.nn_fallback_atoms() if use_nn else 0)
 
     rm = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
-    out = {}
+    out = {"md_steps_before_after_md": SURROGATE_MD_STEPS}
+    ctx.step(SURROGATE_MD_STEPS)
     for tag, xx in (("start", x0), ("after_md", ctx.get_state()["x"])):
         fn, nfb = forces(xx, True)
         ft, _ = forces(xx, False)

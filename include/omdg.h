@@ -288,6 +288,10 @@ const char* omdg_nn_last_error(omdg_nn* nn);
    rs on [1.6, 3.2] A with eta_r = 1/(2 h^2), and (eta_a in {0, 0.3}) x (zeta in {1, 2, 4, 8}) x (lambda in {1, -1}). */
 int omdg_nn_set_descriptors(omdg_nn* nn, const float* rs, const float* eta_r, const int* zeta, const float* lambda,
                             const float* eta_a);
+/* Descriptor cutoff rc and the inner radius rin where its switch starts (before the dataset): f_c = 1 up to rin and
+   (cos(pi (r - rin) / (rc - rin)) + 1) / 2 on (rin, rc).  The default is rc = 3.2 A, rin = 0; rin = R - D and
+   rc = R + D give Tersoff's own switch (tersoff.h:183).  OMDG_EINVAL unless 0 <= rin < rc. */
+int omdg_nn_set_cutoff(omdg_nn* nn, float rc, float rin);
 int omdg_nn_set_dataset(omdg_nn* nn, int nconf, const int* natoms, const double* x, const double* box_len,
                         const double* energy, const double* forces);
 /* relative != 0 weights each configuration's force residual by (mean square force of the dataset) / (its own), so

@@ -9,8 +9,12 @@
 namespace omdg {
 
 __device__ __forceinline__ float nn_fc(const NNDescParams& p, float r, float& dfc) {
+    if (r <= p.rin) {
+        dfc = 0.f;
+        return 1.f;
+    }
     float s, c;
-    sincosf(r * p.pi_rc, &s, &c);
+    sincosf((r - p.rin) * p.pi_rc, &s, &c);
     dfc = -0.5f * p.pi_rc * s;
     return 0.5f * (c + 1.f);
 }

@@ -30,14 +30,16 @@ constexpr int NN_PARAMS = NN_OFF_B3 + 1;  // 6337
 // Descriptor set and normalisation, passed to kernels by value.
 //   radial  G_k = sum_j exp(-eta_r[k] (r - rs[k])^2) fc(r)
 //   angular G_m = pref[m] sum_{j<k} (1 + lam[m] cos)^zeta[m] exp(-eta_a[m] (r_ij^2 + r_ik^2)) fc(r_ij) fc(r_ik)
-//   fc(r) = (cos(pi r / rc) + 1) / 2
+//   fc(r) = 1 for r <= rin, (cos(pi (r - rin) / (rc - rin)) + 1) / 2 on (rin, rc)
+// (rin = R - D, rc = R + D is Tersoff's own cutoff switch, tersoff.h:183)
 struct NNDescParams {
     float rs[NN_RAD], eta_r[NN_RAD];
     float lam[NN_ANG], eta_a[NN_ANG], pref[NN_ANG];
     int zeta[NN_ANG];
-    float rc, pi_rc;
+    float rc, pi_rc;                       // pi_rc = pi / (rc - rin)
     float mu[NN_DESC], isig[NN_DESC];      // normalised input (G - mu) * isig
     float gmin[NN_DESC], gmax[NN_DESC];    // training range (fallback outside it)
+    float rin;                             // inner radius of the cutoff switch (0: cosine over [0, rc])
 };
 
 struct NNModel {
@@ -48,8 +50,11 @@ struct NNModel {
 
 // The default descriptor set: 16 radial centres on [1.6, 3.2] A with
 // eta = 1 / (2 h^2) (h the spacing) and 16 angular terms
-// (eta_a in {0, 0.3}) x (zeta in {1, 2, 4, 8}) x (lambda in {+1, -1}).
+// (eta_a in {0, 0.3}) x (zeta in {1, 2, 4, 8}) x (lambda in {+1, -1}),
+// cutoff rc = 3.2 A switched over [0, rc].
 void nn_default_descriptors(NNDescParams& dp);
+// Sets rc, rin and pi_rc; false unless 0 <= rin < rc.
+bool nn_set_cutoff(NNDescParams& dp, float rc, float rin);
 int nn_model_load(const std::string& path, NNModel& m, std::string& err);
 int nn_model_save(const std::string& path, const NNModel& m, std::string& err);
 

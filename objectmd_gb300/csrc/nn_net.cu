@@ -23,6 +23,14 @@
 namespace omdg {
 
 // ------------------------------------------------------------------ model
+bool nn_set_cutoff(NNDescParams& dp, float rc, float rin) {
+    if (!(rin >= 0.f && rin < rc && std::isfinite(rc))) return false;
+    dp.rc = rc;
+    dp.rin = rin;
+    dp.pi_rc = (float)(M_PI / ((double)rc - (double)rin));
+    return true;
+}
+
 void nn_default_descriptors(NNDescParams& dp) {
     const double rc = 3.2, r0 = 1.6;
     const double h = (rc - r0) / (NN_RAD - 1);
@@ -42,8 +50,7 @@ void nn_default_descriptors(NNDescParams& dp) {
                 dp.lam[m] = (float)lam[l];
                 dp.pref[m] = (float)std::pow(2.0, 1.0 - zeta[z]);
             }
-    dp.rc = (float)rc;
-    dp.pi_rc = (float)(M_PI / rc);
+    nn_set_cutoff(dp, (float)rc, 0.f);
     for (int d = 0; d < NN_DESC; d++) {
         dp.mu[d] = 0.f;
         dp.isig[d] = 1.f;
@@ -71,6 +78,7 @@ int nn_model_save(const std::string& path, const NNModel& m, std::string& err) {
     const NNDescParams& p = m.dp;
     o << "omdg-nn 1\n";
     put(o, "rc", &p.rc, 1);
+    put(o, "rin", &p.rin, 1);
     put(o, "rs", p.rs, NN_RAD);
     put(o, "eta_r", p.eta_r, NN_RAD);
     float z[NN_ANG];
@@ -113,6 +121,7 @@ int nn_model_load(const std::string& path, NNModel& m, std::string& err) {
         bool ok = true;
         NNDescParams& p = m.dp;
         if (key == "rc") ok = read(&p.rc, 1);
+        else if (key == "rin") ok = read(&p.rin, 1);
         else if (key == "rs") ok = read(p.rs, NN_RAD);
         else if (key == "eta_r") ok = read(p.eta_r, NN_RAD);
         else if (key == "zeta") {
@@ -148,7 +157,10 @@ int nn_model_load(const std::string& path, NNModel& m, std::string& err) {
         err = path + ": no parameters";
         return OMDG_EFILE;
     }
-    m.dp.pi_rc = (float)(M_PI / m.dp.rc);
+    if (!nn_set_cutoff(m.dp, m.dp.rc, m.dp.rin)) {
+        err = path + ": the cutoff needs 0 <= rin < rc";
+        return OMDG_EFILE;
+    }
     for (int d = 0; d < NN_DESC; d++) {
         if (!(m.sigma[d] > 0.f)) {
             err = path + ": sigma must be positive";

@@ -690,6 +690,13 @@ int omdg_nn_set_descriptors(omdg_nn* t, const float* rs, const float* eta_r, con
     return OMDG_OK;
 }
 
+int omdg_nn_set_cutoff(omdg_nn* t, float rc, float rin) {
+    if (!t) return OMDG_EINVAL;
+    if (t->natoms > 0) return nn_fail(t, OMDG_ESTATE, "set the cutoff before the dataset");
+    if (!nn_set_cutoff(t->model.dp, rc, rin)) return nn_fail(t, OMDG_EINVAL, "the cutoff needs 0 <= rin < rc");
+    return OMDG_OK;
+}
+
 int omdg_nn_set_dataset(omdg_nn* t, int nconf, const int* natoms, const double* x, const double* box_len,
                         const double* energy, const double* forces) {
     if (!t || nconf <= 0 || !natoms || !x || !box_len || !energy || !forces) return OMDG_EINVAL;

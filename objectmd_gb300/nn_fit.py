@@ -78,10 +78,12 @@ def init_params(seed, e_mean):
 
 
 def fit(data, epochs=200, batch=16, lr=1e-3, wE=1.0, wF=1.0, seed=7, device=0, out=MODEL, log=None, lr_final=1e-5,
-        descriptors=None, relative_forces=False, atom_energies=True):
+        descriptors=None, relative_forces=False, atom_energies=True, cutoff=None):
     from objectmd_gb300 import omdg
 
     with omdg.Network(device) as net:
+        if cutoff is not None:
+            net.set_cutoff(*cutoff)
         if descriptors is not None:
             net.set_descriptors(*descriptors)
         net.set_dataset(data["natoms"], data["x"], data["box"], data["energy"], data["forces"])

@@ -134,6 +134,7 @@ SIGNATURES = {
     "omdg_nn_destroy": [_vp],
     "omdg_nn_last_error": [_vp],
     "omdg_nn_set_descriptors": [_vp, _P(_f), _P(_f), _P(_i), _P(_f), _P(_f)],
+    "omdg_nn_set_cutoff": [_vp, _f, _f],
     "omdg_nn_set_dataset": [_vp, _i, _P(_i), _P(_d), _P(_d), _P(_d), _P(_d)],
     "omdg_nn_set_force_weighting": [_vp, _i],
     "omdg_nn_set_atom_energies": [_vp, _P(_d)],
@@ -306,6 +307,10 @@ class Network:
         rs, eta_r, lam, eta_a = f32(rs), f32(eta_r), f32(lam), f32(eta_a)
         zeta = np.ascontiguousarray(zeta, dtype=np.int32)
         self._check(self.lib.omdg_nn_set_descriptors(self.h, _fp(rs), _fp(eta_r), _ip(zeta), _fp(lam), _fp(eta_a)))
+
+    def set_cutoff(self, rc, rin=0.0):
+        """omdg_nn_set_cutoff: descriptor cutoff rc, switch starting at rin."""
+        self._check(self.lib.omdg_nn_set_cutoff(self.h, rc, rin))
 
     def set_dataset(self, natoms, x, box_len, energy, forces):
         natoms = np.ascontiguousarray(natoms, dtype=np.int32)

@@ -7,7 +7,10 @@ The reference has no neural potential; the method restated here is the
 Behler-Parrinello atom-centred network (J. Behler, M. Parrinello, PRL 98,
 146401 (2007); J. Behler, J. Chem. Phys. 134, 074106 (2011)):
 
-  f_c(r)   = 0.5 (cos(pi r / rc) + 1)                       r < rc
+  f_c(r)   = 1                                              r <= rin
+           = 0.5 (cos(pi (r - rin) / (rc - rin)) + 1)        rin < r < rc
+             (rin = 0 by default; rin = R - D, rc = R + D is Tersoff's own
+             switch, tersoff.h:183)
   G2_k(i)  = sum_j exp(-eta_k (r_ij - Rs_k)^2) f_c(r_ij)     (16 radial)
   G5_m(i)  = 2^(1-zeta_m) sum_{j<k} (1 + lambda_m cos theta_jik)^zeta_m
              exp(-eta_m (r_ij^2 + r_ik^2)) f_c(r_ij) f_c(r_ik)  (16 angular)
@@ -41,12 +44,14 @@ def descriptor_params():
     return {"rs": rs, "eta_r": eta_r, "zeta": ang[:, 0], "lam": ang[:, 1], "eta_a": ang[:, 2], "rc": RC}
 
 
-def fc(r, rc):
-    return 0.5 * (np.cos(np.pi * r / rc) + 1.0)
+def fc(r, rc, rin=0.0):
+    t = np.pi * (np.maximum(r, rin) - rin) / (rc - rin)
+    return 0.5 * (np.cos(t) + 1.0)
 
 
-def dfc(r, rc):
-    return -0.5 * np.pi / rc * np.sin(np.pi * r / rc)
+def dfc(r, rc, rin=0.0):
+    t = np.pi * (np.maximum(r, rin) - rin) / (rc - rin)
+    return -0.5 * np.pi / (rc - rin) * np.sin(t)
 
 
 def neighbours(x, lo, hi, rc=RC):
@@ -66,7 +71,7 @@ def neighbours(x, lo, hi, rc=RC):
 def descriptors(x, lo, hi, p):
     """G (n x 32) and the Jacobian: jac[i] = list of (j, dG_i/dx_j (32 x 3));
     dG_i/dx_i = -sum of the neighbour blocks (translation invariance)."""
-    rc = p["rc"]
+    rc, rin = p["rc"], p.get("rin", 0.0)
     nb = neighbours(x, lo, hi, rc)
     n = len(x)
     G = np.zeros((n, N_DESC))
@@ -79,8 +84,8 @@ def descriptors(x, lo, hi, p):
             r = np.linalg.norm(d)
             e = d / r
             g = np.exp(-p["eta_r"] * (r - p["rs"]) ** 2)
-            G[i, :N_RAD] += g * fc(r, rc)
-            dg = g * (dfc(r, rc) - 2.0 * p["eta_r"] * (r - p["rs"]) * fc(r, rc))  # dG/dr
+            G[i, :N_RAD] += g * fc(r, rc, rin)
+            dg = g * (dfc(r, rc, rin) - 2.0 * p["eta_r"] * (r - p["rs"]) * fc(r, rc, rin))  # dG/dr
             blocks[j][:N_RAD] += np.outer(dg, e)
         m = len(nb[i])
         for a in range(m):
@@ -95,12 +100,12 @@ def descriptors(x, lo, hi, p):
                 pw = np.where(base > 0, base, 0.0) ** z
                 dpw = np.where(base > 0, z * np.where(base > 0, base, 1.0) ** (z - 1.0), 0.0) * lam
                 ex = np.exp(-eta * (ra * ra + rb * rb))
-                fa, fb = fc(ra, rc), fc(rb, rc)
+                fa, fb = fc(ra, rc, rin), fc(rb, rc, rin)
                 pref = 2.0 ** (1.0 - z)
                 G[i, N_RAD:] += pref * pw * ex * fa * fb
                 # derivatives w.r.t. ra, rb, cos
-                d_ra = pref * pw * ex * fb * (dfc(ra, rc) - 2.0 * eta * ra * fa)
-                d_rb = pref * pw * ex * fa * (dfc(rb, rc) - 2.0 * eta * rb * fb)
+                d_ra = pref * pw * ex * fb * (dfc(ra, rc, rin) - 2.0 * eta * ra * fa)
+                d_rb = pref * pw * ex * fa * (dfc(rb, rc, rin) - 2.0 * eta * rb * fb)
                 d_cos = pref * dpw * ex * fa * fb
                 ea, eb = da / ra, db / rb
                 dcos_da = (eb - cos * ea) / ra  # d cos / d x_ja

@@ -157,3 +157,42 @@ def test_fallback_is_plain_tersoff(omdg_lib, dataset, tmp_path):
     # zero-valued slots to the Kahan gather, which can move the last bit
     np.testing.assert_allclose(st["f"], ref["f"], rtol=1e-6, atol=1e-6)
     np.testing.assert_allclose(st["pot"], ref["pot"], rtol=1e-6, atol=1e-6)
+
+
+def test_tersoff_switch_descriptors_and_md_path(omdg_lib, tmp_path):
+    """Descriptor cutoff switched over Tersoff's [R - D, R + D] (rin = 2.55,
+    rc = 2.85): the trainer's descriptors match the oracle with bonds on both
+    sides of rin, the switch round-trips through the model file, and the MD
+    force path equals the trainer's prediction."""
+    from objectmd_gb300 import inputs
+    from oracle import nn_oracle as nn
+
+    p = dict(nn.descriptor_params(), rc=2.85, rin=2.55)
+    x, v, (lo, hi) = inputs.diamond_silicon(ncell=2, a=5.431, sigma=0.15, temp=300.0, seed_pos=13, seed_vel=14)
+    Gref, _ = nn.descriptors(x, lo, hi, p)
+    net = omdg_lib.Network(0)
+    net.set_cutoff(2.85, 2.55)
+    box = np.asarray(hi) - np.asarray(lo)
+    net.set_dataset([len(x)], x, [box], [-4.6 * len(x)], np.zeros_like(x))
+    G = net.descriptors()
+    scale = np.abs(Gref).max(0) + 1e-12
+    assert (np.abs(G - Gref) / scale).max() < 2e-5
+    net.normalize_from_dataset()
+    norm = net.normalization()
+    w, _ = nn.init_model(5, norm["mu"], norm["sigma"], -4.6)
+    net.set_weights(nn.flatten(w))
+    model = str(tmp_path / "switch.nn")
+    net.save(model)
+    E, F = net.predict(0, 1)
+    net.close()
+    rin = [ln.split()[1] for ln in open(model) if ln.startswith("rin ")]
+    assert len(rin) == 1 and np.float32(rin[0]) == np.float32(2.55)
+    c = dict(x=x, lo=lo, hi=hi)
+    with surrogate_context(omdg_lib, c, model, True) as ctx:
+        st = ctx.get_state()
+        assert ctx.nn_fallback_atoms() == 0
+    assert np.abs(st["pot"] - E).max() < 2e-3
+    assert np.linalg.norm(st["f"] - F) / np.linalg.norm(F) < 2e-3
+    with pytest.raises(omdg_lib.OMDGError):
+        with omdg_lib.Network(0) as bad:
+            bad.set_cutoff(2.5, 2.6)

@@ -179,6 +179,10 @@ def test_tersoff_switch_descriptors_and_md_path(omdg_lib, tmp_path):
     assert (np.abs(G - Gref) / scale).max() < 2e-5
     net.normalize_from_dataset()
     norm = net.normalization()
+    # the dataset is this one cell: widen its range so that the MD kernels'
+    # FP32 rounding cannot put an extreme atom outside it
+    pad = 0.01 * (norm["gmax"] - norm["gmin"]) + 1e-6
+    net.set_normalization(norm["mu"], norm["sigma"], norm["gmin"] - pad, norm["gmax"] + pad)
     w, _ = nn.init_model(5, norm["mu"], norm["sigma"], -4.6)
     net.set_weights(nn.flatten(w))
     model = str(tmp_path / "switch.nn")

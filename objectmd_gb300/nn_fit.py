@@ -8,8 +8,10 @@ labels are the Tersoff kernel's per-atom energies (E_i = 1/2 sum_j V_ij) and
 forces.  Fitting runs on the
 GPU through omdg_nn_train: descriptors, forward and backward passes, the
 force-loss double backward and Adam are the library's own kernels.  Defaults:
-200 epochs, batches of 16 configurations, Adam with the learning rate decaying
-from 1e-3 to 1e-5 (cosine), loss = per-atom energy MSE + force MSE.
+the descriptors of switch_descriptors() (cutoff switched over Tersoff's own
+[R - D, R + D]), 1000 epochs, batches of 16 configurations, Adam with the
+learning rate decaying from 1e-3 to 1e-5 (cosine), loss = per-atom energy MSE
++ force MSE.
 
     python -m objectmd_gb300.nn_fit --out objectmd_gb300/models/nn_tersoff_si.nn
 """
@@ -65,6 +67,21 @@ def generate(nconf=2000, per_traj=50, ncell=4, tmin=300.0, tmax=2500.0, every=50
     return {"natoms": np.array(natoms), "x": np.concatenate(xs), "box": np.array(boxes),
             "energy": np.array(energies), "forces": np.concatenate(forces), "temperature": np.array(tlist),
             "atom_energy": np.concatenate(eatoms)}
+
+
+def switch_descriptors(r0=1.9, R=2.7, D=0.15):
+    """Descriptor set fitted to Tersoff: the cutoff switched over Tersoff's own
+    [R - D, R + D] (tersoff.h:183), 16 radial centres on [r0, R + D] with
+    eta = 1 / (2 h^2) (h the spacing), the default angular terms.  Returns
+    (cutoff, descriptors) as fit() takes them."""
+    rs = np.linspace(r0, R + D, 16)
+    h = rs[1] - rs[0]
+    eta_r = np.full(16, 1.0 / (2.0 * h * h))
+    ang = [(z, l, e) for e in (0.0, 0.3) for z in (1, 2, 4, 8) for l in (1.0, -1.0)]
+    zeta = np.array([a[0] for a in ang], dtype=np.int32)
+    lam = np.array([a[1] for a in ang])
+    eta_a = np.array([a[2] for a in ang])
+    return (R + D, R - D), (rs, eta_r, zeta, lam, eta_a)
 
 
 def init_params(seed, e_mean):
@@ -147,7 +164,7 @@ def tersoff_snapshot(ncell=8, temp=1000.0, steps=1000, seed=41, device=0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nconf", type=int, default=2000)
-    ap.add_argument("--epochs", type=int, default=200)
+    ap.add_argument("--epochs", type=int, default=1000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--lr-final", type=float, default=1e-5)
@@ -161,8 +178,9 @@ def main():
     data = generate(nconf=args.nconf, seed=args.seed, log=log)
     log("dataset: %d configurations, %d atoms, %.1f s" % (len(data["natoms"]), data["natoms"].sum(),
                                                          time.time() - t0))
+    cutoff, descriptors = switch_descriptors()
     hist, secs = fit(data, args.epochs, args.batch, args.lr, args.wE, args.wF, args.seed, out=args.out, log=log,
-                     lr_final=args.lr_final)
+                     lr_final=args.lr_final, cutoff=cutoff, descriptors=descriptors)
     x, v, lo, hi = tersoff_snapshot(8, 1000.0)
     rmse, frms, nfb = force_rmse(args.out, x, lo, hi)
     log("force RMSE vs Tersoff at 1000 K (4096 atoms): %.4f eV/A (force RMS %.3f, %d fallback atoms)" %

@@ -553,6 +553,36 @@ int omdg_save_simulation(omdg_ctx* ctx, const char* path, int ncont, const omdg_
    after.  cont (cap entries, may be NULL) receives the container headers. */
 int omdg_load_simulation(omdg_ctx* ctx, const char* path, int cap, omdg_container_desc* cont, int* ncont);
 
+/* ------------------------------------------------------------------ finite-difference heat solver
+   FDTDSolver (include/misc/fdtd.hpp, src/omd/fdtd.cpp), single rank, the cells on the device.  The grid is
+   nx x ny x nz cells (nz <= 2 makes it 2D, fdtd.cpp:58-59), cell (i, j, k) at index k nx ny + i + j nx.
+   symbol: the symbol map of SetSymbolMap (fdtd.cpp:450-477): "<chars> <flags>" pairs, flags one character per
+   face (left right top bottom [near far]): '+' occupied, 'p' periodic, anything else empty.  map: one character
+   per cell (SetMap, fdtd.cpp:479-488); a character outside the symbol map marks a cell the face loop skips.
+   Conductivity and capacity start at 1, the cell vector and the source at 0 (fdtd.cpp:186-204).
+   On failure *fd may still be set: read omdg_fdtd_last_error, then omdg_fdtd_destroy it. */
+typedef struct omdg_fdtd omdg_fdtd;
+int omdg_fdtd_create(omdg_fdtd** fd, int device, int nx, int ny, int nz, const char* symbol, const char* map);
+int omdg_fdtd_destroy(omdg_fdtd* fd);
+const char* omdg_fdtd_last_error(omdg_fdtd* fd);
+int omdg_fdtd_set_timestep(omdg_fdtd* fd, double dt);   /* SetTimestep (fdtd.cpp:422-425) */
+int omdg_fdtd_set_spacestep(omdg_fdtd* fd, double h);   /* SetSpacestep (fdtd.cpp:427-433): 1/h^2 */
+/* which 0: SetCell (the cell vector, now); 1: SetSource; 2: SetConductivity; 3: SetCapacity (fdtd.hpp:123-133):
+   the string is kept and re-applied before every step (sync_data, fdtd.cpp:599-603).  Tokens: "<chars> <value>"
+   (every cell with one of the map characters, '*' all) or "@ i,j,k=<value>" / "@ i,j,k,i2,j2,k2=<value>" (one
+   cell or a block), a value optionally followed by ":t0" or ":t0:t1" (the steps it applies in; a token is dropped
+   for good once a step falls outside its range, AssignArray, fdtd.cpp:528-592).  A '{...}' value is a muParser
+   expression, which is not built: OMDG_EINVAL. */
+int omdg_fdtd_assign(omdg_fdtd* fd, int which, const char* str);
+/* Step(n) (fdtd.cpp:671-689): per step the kept strings, one Solve (fdtd.cpp:605-668) on the device, step + 1. */
+int omdg_fdtd_step(omdg_fdtd* fd, int n);
+/* which 0: the cell vector, 1: the source the next step starts from, 2: conductivity, 3: capacity, 4: the
+   external vector; n must be nx ny nz. */
+int omdg_fdtd_get(omdg_fdtd* fd, int which, double* out, long n);
+/* GetExtVector() written by the caller: E for the next solve, which clears it. */
+int omdg_fdtd_set_ext(omdg_fdtd* fd, const double* e, long n);
+int omdg_fdtd_info(omdg_fdtd* fd, int* nx, int* ny, int* nz, int* step);
+
 #ifdef __cplusplus
 }
 #endif

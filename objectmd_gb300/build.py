@@ -23,7 +23,7 @@ CUFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcomp
            "-warn-spills"] + ARCH
 SOURCES = ["api.cu", "nlist.cu", "eam.cu", "eam_fast.cu", "pair.cu", "threebody.cu", "integrate.cu", "io.cu",
            "static_count.cu", "nn_net.cu", "nn_train.cu", "nn_potential.cu", "ttm.cu", "table.cpp",
-           "checkpoint.cpp", "output.cu", "waits.cu"]
+           "checkpoint.cpp", "output.cu", "waits.cu", "fdtd.cu"]
 
 
 def _newer(target, deps):

@@ -130,6 +130,16 @@ SIGNATURES = {
     "omdg_ttm_state": [_vp, _P(_d), _P(_d), _P(_d), _P(_d)],
     "omdg_add_nn": [_vp, _i, _i, _cp, _cp],
     "omdg_nn_fallback_atoms": [_vp, _P(_l)],
+    "omdg_fdtd_create": [_P(_vp), _i, _i, _i, _i, _cp, _cp],
+    "omdg_fdtd_destroy": [_vp],
+    "omdg_fdtd_last_error": [_vp],
+    "omdg_fdtd_set_timestep": [_vp, _d],
+    "omdg_fdtd_set_spacestep": [_vp, _d],
+    "omdg_fdtd_assign": [_vp, _i, _cp],
+    "omdg_fdtd_step": [_vp, _i],
+    "omdg_fdtd_get": [_vp, _i, _P(_d), _l],
+    "omdg_fdtd_set_ext": [_vp, _P(_d), _l],
+    "omdg_fdtd_info": [_vp, _P(_i), _P(_i), _P(_i), _P(_i)],
     "omdg_nn_create": [_P(_vp), _i],
     "omdg_nn_destroy": [_vp],
     "omdg_nn_last_error": [_vp],
@@ -167,7 +177,7 @@ SIGNATURES = {
     "omdg_save_simulation": [_vp, _cp, _i, _P(ContainerDesc), _P(_i), _P(_i), _P(_d), _i, _P(_cp), _P(_cp)],
     "omdg_load_simulation": [_vp, _cp, _i, _P(ContainerDesc), _P(_i)],
 }
-STRING_RESULT = ("omdg_last_error", "omdg_nn_last_error")
+STRING_RESULT = ("omdg_last_error", "omdg_nn_last_error", "omdg_fdtd_last_error")
 
 
 class OMDGError(RuntimeError):
@@ -274,6 +284,82 @@ NN_DESC = 32
 
 def _fp(a):
     return None if a is None else a.ctypes.data_as(_P(_f))
+
+
+class FDTD:
+    """The finite-difference heat solver on one GPU (omdg_fdtd), with the
+    reference's FDTDSolver interface: SetTimestep, SetSpacestep, SetCell,
+    SetSource, SetConductivity, SetCapacity, Step, GetVector, GetExtVector."""
+
+    CELL, SOURCE, CONDUCTIVITY, CAPACITY, EXT = range(5)
+
+    def __init__(self, nx, ny, nz, symbol, map, device=0):
+        self.lib = load()
+        self.h = _vp()
+        rc = self.lib.omdg_fdtd_create(ctypes.byref(self.h), int(device), int(nx), int(ny), int(nz),
+                                       symbol.encode(), map.encode())
+        if rc != OMDG_OK:
+            msg = (self.lib.omdg_fdtd_last_error(self.h) or b"").decode() if self.h else "omdg_fdtd_create failed"
+            self.close()
+            raise OMDGError(rc, msg)
+        a, b, c = _i(), _i(), _i()
+        self._check(self.lib.omdg_fdtd_info(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), None))
+        self.shape = (a.value, b.value, c.value)
+        self.dim = a.value * b.value * c.value
+
+    def _check(self, rc):
+        if rc != OMDG_OK:
+            raise OMDGError(rc, (self.lib.omdg_fdtd_last_error(self.h) or b"").decode())
+
+    def close(self):
+        if self.h:
+            self.lib.omdg_fdtd_destroy(self.h)
+            self.h = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_timestep(self, dt):
+        self._check(self.lib.omdg_fdtd_set_timestep(self.h, float(dt)))
+
+    def set_spacestep(self, h):
+        self._check(self.lib.omdg_fdtd_set_spacestep(self.h, float(h)))
+
+    def set_cell(self, s):
+        self._check(self.lib.omdg_fdtd_assign(self.h, self.CELL, s.encode()))
+
+    def set_source(self, s):
+        self._check(self.lib.omdg_fdtd_assign(self.h, self.SOURCE, s.encode()))
+
+    def set_conductivity(self, s):
+        self._check(self.lib.omdg_fdtd_assign(self.h, self.CONDUCTIVITY, s.encode()))
+
+    def set_capacity(self, s):
+        self._check(self.lib.omdg_fdtd_assign(self.h, self.CAPACITY, s.encode()))
+
+    def step(self, n=1):
+        self._check(self.lib.omdg_fdtd_step(self.h, int(n)))
+
+    def get(self, which=0):
+        out = np.zeros(self.dim)
+        self._check(self.lib.omdg_fdtd_get(self.h, int(which), _dp(out), self.dim))
+        return out
+
+    def vector(self):
+        return self.get(self.CELL)
+
+    def set_ext(self, e):
+        e = np.ascontiguousarray(e, dtype=np.float64).ravel()
+        self._check(self.lib.omdg_fdtd_set_ext(self.h, _dp(e), e.size))
+
+    @property
+    def steps_done(self):
+        st = _i()
+        self._check(self.lib.omdg_fdtd_info(self.h, None, None, None, ctypes.byref(st)))
+        return st.value
 
 
 class Network:

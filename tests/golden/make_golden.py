@@ -276,6 +276,87 @@ def impact_case(tdir, work):
     print("wrote impact_ar_si_slab")
 
 
+def fdtd_map(nx, ny, nz, cell):
+    """The map string of an nx x ny x nz grid (index k nx ny + i + j nx), one
+    character per cell from cell(i, j, k)."""
+    return "".join(cell(i, j, k) for k in range(nz) for j in range(ny) for i in range(nx))
+
+
+def fdtd_specs():
+    """Specs for oracle/_ref/fdtd_driver (oracle/ref/fdtd_driver.cpp)."""
+    def slab(i, j, k):  # x, y periodic; z: '.' above, a free top, the bulk, a held bottom, one dead column
+        if k == 0:
+            return "." if (i, j) == (2, 2) else "v"
+        if k == 1:
+            return "t"
+        if k == 6:
+            return "b"
+        return "d" if (i, j) == (5, 0) else "a"
+
+    specs = {
+        # a TTM-like slab: symbols per layer, block and per-symbol values,
+        # ranged and future sources (the future one never applies), an
+        # external vector entry, a cell outside the symbol map
+        "slab3d": "\n".join([
+            "dim 6 5 7",
+            "symbol a pppp++ t pppp-+ b pppp+- v ------ d pp--++",
+            "map " + fdtd_map(6, 5, 7, slab),
+            "spacestep 2.0",
+            "timestep 0.05",
+            "cell * 300 @ 2,2,1,3,3,1=1000 @ 0,4,5=450.5",
+            "conductivity a 2.0 t 1.5 b 3.0 @ 0,0,3,5,4,4=0.5 d 0",
+            "capacity * 1.0 a 2.5 @ 1,1,2=4.0",
+            "source t 50.0:0:4 @ 0,0,6=20:2:3 a 1.0:7:9",
+            "ext 17 5.0",
+            "ext 100 -2.5",
+            "steps 12",
+        ]),
+        # one symbol with every face occupied: the first cell at each edge
+        # clears that face for the cells after it and for every later step
+        "flat2d_cleared": "\n".join([
+            "dim 7 5 1",
+            "symbol a ++++",
+            "map " + fdtd_map(7, 5, 1, lambda i, j, k: "." if (i, j) == (6, 4) else "a"),
+            "spacestep 1.0",
+            "timestep 0.1",
+            "cell @ 3,2,0=100 @ 6,4,0=1",
+            "steps 5",
+        ]),
+        # nz = 2 is 2D; periodic x, free y edges, cells of zero conductivity
+        # (K = 0 between two of them, K = 0 * c / c beside one)
+        "edges2d": "\n".join([
+            "dim 8 6 2",
+            "symbol a pp++ u pp-+ w pp+- z pp++",
+            "map " + fdtd_map(8, 6, 1, lambda i, j, k: "u" if j == 0 else ("w" if j == 5 else
+                                                                              ("z" if (i in (3, 4) and j == 2) else "a"))),
+            "spacestep 0.5",
+            "timestep 0.01",
+            "cell * 10 @ 0,0,0,1,5,0=40 z 80",
+            "conductivity * 1 z 0 @ 7,3,0=3.5",
+            "capacity w 2 u 0.5",
+            "source @ 6,1,0=100:0:7",
+            "ext 9 1.25",
+            "steps 10",
+        ]),
+    }
+    return specs
+
+
+def fdtd_case():
+    """Cell vectors of the reference's FDTDSolver on each spec."""
+    import subprocess
+
+    drv = os.path.join(ROOT, "oracle", "_ref", "fdtd_driver")
+    out = {}
+    for name, spec in fdtd_specs().items():
+        txt = subprocess.run([drv], input=spec, capture_output=True, text=True, check=True).stdout
+        rows = [[float(v) for v in ln.split()[2:]] for ln in txt.splitlines() if ln.startswith("step ")]
+        out[name + "_spec"] = np.array(spec)
+        out[name + "_rows"] = np.array(rows)
+    np.savez_compressed(os.path.join(GOLD, "fdtd_cases.npz"), **out)
+    print("wrote fdtd_cases")
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not REF:
@@ -299,6 +380,9 @@ def main(only=None):
         return
     if only == "impact":
         impact_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
+        return
+    if only == "fdtd":
+        fdtd_case()
         return
     if only == "lj4000":
         lj4000_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
@@ -385,6 +469,7 @@ def main(only=None):
     impact_case(tdir, work)
     output_case(tdir)
     thermo_case(tdir)
+    fdtd_case()
     print("done")
 
 

@@ -582,6 +582,19 @@ int omdg_fdtd_get(omdg_fdtd* fd, int which, double* out, long n);
 /* GetExtVector() written by the caller: E for the next solve, which clears it. */
 int omdg_fdtd_set_ext(omdg_fdtd* fd, const double* e, long n);
 int omdg_fdtd_info(omdg_fdtd* fd, int* nx, int* ny, int* nz, int* step);
+/* The two-temperature model with the electron temperature on a grid's cells (the coupling include/misc/
+   TTM_Diffusion.h:41,134 sets out to make with FDTDSolver; that header does not compile).  After omdg_set_ttm
+   (tables, atom volume, pulse offset; its electron_temperature is not used: the grid's cell vector is Te, a
+   negative cell taking its cell's lattice temperature at the first active step), every step first sums the
+   detector temperatures of the atoms in each cell (cell (i, j, k) covers origin + h [i, i+1) x [j, j+1) x
+   [k, k+1), periodic axes wrapped into the box; a 2D grid spans every z) into the lattice temperature Ta, sets
+   E = -G0 G(Te) (Te - Ta) for the cells holding atoms and cap = C0 Ce(Te), runs one solve with the MD time step,
+   and rescales each atom's velocity about its local centre of mass with its cell's new Te, as the scalar model
+   does (TTM_Homogen_SCNA.h:272-330).  The grid's kept strings must be unranged (no ":t0:t1"): the coupled step
+   replays on the device.  While coupled the grid takes no omdg_fdtd_step, assign, set_ext or destroy; read its
+   cell vector after omdg_sync.  grid = NULL detaches.  omdg_ttm_state's electron temperature and integrated
+   electron energy are not kept in this mode. */
+int omdg_set_ttm_grid(omdg_ctx* ctx, omdg_fdtd* grid, const double* origin);
 
 #ifdef __cplusplus
 }

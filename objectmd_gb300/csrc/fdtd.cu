@@ -53,6 +53,8 @@ FDDev fd_dev(const FDGrid* g) {
     p.cap = g->dcap;
     p.S = g->dS;
     p.E = g->dE;
+    p.mask_first = p.mask_later = nullptr;
+    p.solves = p.active = nullptr;
     return p;
 }
 
@@ -71,12 +73,13 @@ __device__ __forceinline__ double fd_face(const FDDev& p, const double* __restri
 __global__ void __launch_bounds__(FD_BLOCK) k_fd_solve(FDDev p, const double* __restrict__ T, double* __restrict__ A) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= p.dim) return;
+    if (p.active && !*p.active) return;  // coupled, model not active yet: the cell vector stays
     const double ti = T[idx];
     double acc = ti;  // a cell outside the symbol map keeps A_i = T_i
     if (p.map[idx] >= 0) {
         const int xy = p.nx * p.ny;
         const int k = idx / xy, a = idx % xy, j = a / p.nx, i = a % p.nx;
-        const unsigned m = p.mask[idx];
+        const unsigned m = p.solves ? (*p.solves == 0 ? p.mask_first : p.mask_later)[idx] : p.mask[idx];
         const double ci = p.con[idx];
         acc = 0.0;
         // a face that is set and beyond the grid is periodic: it wraps (fdtd.cpp:277-285)
@@ -103,6 +106,11 @@ int fd_solve(FDGrid* g, cudaStream_t s) {
     g->cur ^= 1;
     g->solves += 1;
     return OMDG_OK;
+}
+
+cudaError_t fd_solve_coupled(const FDDev& p, const double* T, double* A, cudaStream_t s) {
+    k_fd_solve<<<grid_for(p.dim, FD_BLOCK), FD_BLOCK, 0, s>>>(p, T, A);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ host: maps and strings
@@ -369,6 +377,7 @@ int omdg_fdtd_create(omdg_fdtd** out, int device, int nx, int ny, int nz, const 
 
 int omdg_fdtd_destroy(omdg_fdtd* g) {
     if (!g) return OMDG_OK;
+    if (g->coupled) return fd_fail(g, OMDG_ESTATE, "detach the grid from the two-temperature model first");
     cudaSetDevice(g->device);
     if (g->stream) cudaStreamSynchronize(g->stream);
     for (int k = 0; k < 2; k++) {
@@ -403,6 +412,7 @@ int omdg_fdtd_set_spacestep(omdg_fdtd* g, double h) {
 // which: 0 cell vector (SetCell), 1 source (SetSource), 2 conductivity, 3 capacity
 int omdg_fdtd_assign(omdg_fdtd* g, int which, const char* str) {
     if (!g || !str || which < 0 || which > 3) return OMDG_EINVAL;
+    if (g->coupled) return fd_fail(g, OMDG_ESTATE, "detach the grid from the two-temperature model first");
     cudaSetDevice(g->device);
     std::string s(str);
     int rc = OMDG_OK;
@@ -425,6 +435,7 @@ int omdg_fdtd_assign(omdg_fdtd* g, int which, const char* str) {
 // Step(n) (fdtd.cpp:671-689), single rank: per step sync_data, Solve, step++.
 int omdg_fdtd_step(omdg_fdtd* g, int n) {
     if (!g || n < 0) return OMDG_EINVAL;
+    if (g->coupled) return fd_fail(g, OMDG_ESTATE, "the grid is stepped by a context's two-temperature model");
     cudaSetDevice(g->device);
     for (int k = 0; k < n; k++) {
         int rc = fd_sync_data(g);
@@ -456,6 +467,7 @@ int omdg_fdtd_get(omdg_fdtd* g, int which, double* out, long n) {
 // GetExtVector() written by the caller: E for the next solve, which clears it.
 int omdg_fdtd_set_ext(omdg_fdtd* g, const double* e_in, long n) {
     if (!g || !e_in || n != g->dim) return OMDG_EINVAL;
+    if (g->coupled) return fd_fail(g, OMDG_ESTATE, "the coupling writes the external vector");
     cudaSetDevice(g->device);
     cudaError_t e = cudaMemcpyAsync(g->dE, e_in, sizeof(double) * n, cudaMemcpyHostToDevice, g->stream);
     if (e != cudaSuccess) return fd_fail(g, OMDG_ECUDA, std::string("fdtd: ") + cudaGetErrorString(e));

@@ -35,6 +35,13 @@ struct FDDev {
     const double* cap;
     const double* S;
     double* E;
+    // coupled to the atoms (a replayed step graph): the mask chosen on the
+    // device from the solve count, and the step skipped while the model is
+    // not active; null for host-driven steps
+    const uint8_t* mask_first;
+    const uint8_t* mask_later;
+    const int* solves;
+    const int* active;
 };
 
 struct FDGrid {
@@ -58,6 +65,7 @@ struct FDGrid {
     double *dS = nullptr, *dE = nullptr, *dcon = nullptr, *dcap = nullptr;
     int* dmap = nullptr;
     uint8_t* dmask[2] = {nullptr, nullptr};  // first, later
+    bool coupled = false;                // stepped by a context's two-temperature model
 };
 
 int fd_fail(FDGrid* g, int code, const std::string& msg);
@@ -65,6 +73,9 @@ int fd_fail(FDGrid* g, int code, const std::string& msg);
 int fd_upload(FDGrid* g, cudaStream_t s);
 // One Solve on the device (fdtd.cpp:605-668), on stream s.
 int fd_solve(FDGrid* g, cudaStream_t s);
+// The solve of the coupled step: reads dA[1] (the cell vector as the
+// coupling left it), writes dA[0].
+cudaError_t fd_solve_coupled(const FDDev& p, const double* T, double* A, cudaStream_t s);
 // sync_data (fdtd.cpp:599-603): the kept source, conductivity and capacity
 // strings re-applied at the current step.
 int fd_sync_data(FDGrid* g);

@@ -20,6 +20,7 @@
 #include <string>
 
 #include "device_common.cuh"
+#include "fdtd_internal.h"
 
 namespace omdg {
 
@@ -52,6 +53,12 @@ struct TTMCtx {
     double* partial = nullptr;          // per block: T, dens, count, kinetic, max v^2; + scale partials
     TTMState* st = nullptr;
     int cap = 0, nblocks = 0;
+    // diffusing electron temperature: the cells of a finite-difference grid
+    omdg_fdtd* grid = nullptr;
+    double org[3] = {0, 0, 0};
+    unsigned long long* cell_sum = nullptr;  // per cell: lattice temperatures x 2^20
+    int* cell_cnt = nullptr;                 // per cell: atoms counted
+    int* dev_ctr = nullptr;                  // [0] solves done, [1] the model active in this step
 };
 
 // Within ercut: the FP32 screen, and the reference's FP64 distance in the band.
@@ -268,39 +275,31 @@ __global__ void k_ttm_fd(TTMParams p, TTMState* st, unsigned* status) {
     st->coup = p.g0 * v;
 }
 
-__global__ void __launch_bounds__(TH_BLOCK) k_ttm_scale(TTMParams p, int n, double volcut,
-                                                        const TTMState* __restrict__ st, double* __restrict__ vx,
-                                                        double* __restrict__ vy, double* __restrict__ vz,
-                                                        const int* __restrict__ type, const double* __restrict__ mass,
-                                                        const double* __restrict__ vcm,
-                                                        const double* __restrict__ temp,
-                                                        const double* __restrict__ dens, double* __restrict__ partial) {
+// The rescaling of one atom about its local centre-of-mass velocity, given
+// the energy e it receives (velocity_scalling, TTM_Homogen_SCNA.h:294-320).
+// Returns true when the velocity changed.
+__device__ __forceinline__ bool ttm_rescale(int i, int n, double e, double m, double small,
+                                            double* __restrict__ vx, double* __restrict__ vy,
+                                            double* __restrict__ vz, const double* __restrict__ vcm) {
+    const double cmx = vcm[i], cmy = vcm[n + i], cmz = vcm[2 * (size_t)n + i];
+    const double ux = vx[i], uy = vy[i], uz = vz[i];
+    const double cx = ux - cmx, cy = uy - cmy, cz = uz - cmz;
+    const double c2 = cx * cx + cy * cy + cz * cz;
+    if (c2 < small) return false;
+    const double cmc = cmx * cx + cmy * cy + cmz * cz;
+    const double cm2 = cmx * cmx + cmy * cmy + cmz * cmz;
+    const double v2 = ux * ux + uy * uy + uz * uz;
+    const double rr = cmc * cmc + c2 * (2.0 * e / m + v2 - cm2);
+    if (rr < 0.0) return false;
+    const double sa = (-cmc + sqrt(rr)) / c2;
+    vx[i] = cmx + sa * cx;
+    vy[i] = cmy + sa * cy;
+    vz[i] = cmz + sa * cz;
+    return true;
+}
+
+__device__ __forceinline__ void ttm_block_partial(double de, double cnt, double* __restrict__ partial) {
     __shared__ double se[TH_BLOCK], sc[TH_BLOCK];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double de = 0.0, cnt = 0.0;
-    if (st->active && i < n && dens[i] * volcut > 3.0) {
-        const double m = mass[type[i]];
-        const double e = st->coup * (st->te - temp[i]) * p.vol * p.dt;
-        const double cmx = vcm[i], cmy = vcm[n + i], cmz = vcm[2 * (size_t)n + i];
-        const double ux = vx[i], uy = vy[i], uz = vz[i];
-        const double cx = ux - cmx, cy = uy - cmy, cz = uz - cmz;
-        const double c2 = cx * cx + cy * cy + cz * cz;
-        const double small = st->vmax2 * 1e-12;
-        if (!(c2 < small)) {
-            const double cmc = cmx * cx + cmy * cy + cmz * cz;
-            const double cm2 = cmx * cmx + cmy * cmy + cmz * cmz;
-            const double v2 = ux * ux + uy * uy + uz * uz;
-            const double rr = cmc * cmc + c2 * (2.0 * e / m + v2 - cm2);
-            if (!(rr < 0.0)) {
-                const double sa = (-cmc + sqrt(rr)) / c2;
-                vx[i] = cmx + sa * cx;
-                vy[i] = cmy + sa * cy;
-                vz[i] = cmz + sa * cz;
-                de = e;
-                cnt = 1.0;
-            }
-        }
-    }
     se[threadIdx.x] = de;
     sc[threadIdx.x] = cnt;
     __syncthreads();
@@ -314,6 +313,160 @@ __global__ void __launch_bounds__(TH_BLOCK) k_ttm_scale(TTMParams p, int n, doub
     if (threadIdx.x == 0) {
         partial[2 * (size_t)blockIdx.x] = se[0];
         partial[2 * (size_t)blockIdx.x + 1] = sc[0];
+    }
+}
+
+__global__ void __launch_bounds__(TH_BLOCK) k_ttm_scale(TTMParams p, int n, double volcut,
+                                                        const TTMState* __restrict__ st, double* __restrict__ vx,
+                                                        double* __restrict__ vy, double* __restrict__ vz,
+                                                        const int* __restrict__ type, const double* __restrict__ mass,
+                                                        const double* __restrict__ vcm,
+                                                        const double* __restrict__ temp,
+                                                        const double* __restrict__ dens,
+                                                        const unsigned* __restrict__ aflag,
+                                                        double* __restrict__ partial) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double de = 0.0, cnt = 0.0;
+    // inactive atoms are skipped (TTM_Homogen_SCNA.h:288)
+    if (st->active && i < n && (!aflag || (aflag[i] & 1u)) && dens[i] * volcut > 3.0) {
+        const double m = mass[type[i]];
+        const double e = st->coup * (st->te - temp[i]) * p.vol * p.dt;
+        if (ttm_rescale(i, n, e, m, st->vmax2 * 1e-12, vx, vy, vz, vcm)) {
+            de = e;
+            cnt = 1.0;
+        }
+    }
+    ttm_block_partial(de, cnt, partial);
+}
+
+// ------------------------------------------------------------------ diffusing electron temperature
+// The electron temperature lives on the cells of a finite-difference grid
+// (FDTDSolver): per step, before the kick-drift,
+//   k_ttm_grid_lattice  per atom: its detector temperature into its cell's
+//                       sum (atoms counted as in the detector's average:
+//                       active, at least two within ercut), as fixed-point
+//                       integers so that the sums do not depend on order
+//   k_ttm_grid_fd       per cell: Te (a negative Te at the first active step
+//                       takes the cell's lattice temperature, as
+//                       fd_main_loop does for the scalar, :238-241), the
+//                       external vector E = -G0 G(Te) (Te - Ta) where the cell
+//                       holds atoms, the capacity C0 Ce(Te), and the copy the
+//                       solve reads
+//   k_fd_solve          the grid's explicit step (csrc/fdtd.cu)
+//   k_ttm_grid_scale    per atom: the rescaling with its cell's new Te and
+//                       G0 G(Te), as velocity_scalling does with the scalar
+//   k_ttm_sum           the integrated lattice energy
+// With one periodic cell and no source this is the scalar model: the face
+// terms are K (T - T) = 0, so A = Te + (E dt) / cap is fd_main_loop's
+// Te + de / (C0 Ce(Te)), term for term.
+constexpr double TTM_CELL_SCALE = 1048576.0;  // 2^20: lattice temperature fixed point
+
+struct GridTTM {
+    FDDev fd;
+    double* A;   // cell vector (the solve writes it)
+    double* T;   // the copy the solve reads
+    double* cap;
+    double org[3], h;
+    int nx, ny, nz;
+    int periodic[3];
+    double lo[3], L[3];
+    unsigned long long* sum;
+    int* cnt;
+    int* ctr;    // [0] solves done, [1] active in this step
+};
+
+// The grid cell of a position (periodic axes wrapped into the box first);
+// -1 outside the grid.  A 2D grid (nz = 1) spans every z.
+__device__ __forceinline__ int ttm_cell(const GridTTM& q, double x, double y, double z) {
+    const double r[3] = {x, y, z};
+    int c[3];
+    for (int d = 0; d < 3; d++) {
+        double w = r[d];
+        if (q.periodic[d]) w -= floor((w - q.lo[d]) / q.L[d]) * q.L[d];
+        c[d] = (int)floor((w - q.org[d]) / q.h);
+    }
+    if (q.nz == 1) c[2] = 0;
+    if (c[0] < 0 || c[0] >= q.nx || c[1] < 0 || c[1] >= q.ny || c[2] < 0 || c[2] >= q.nz) return -1;
+    return c[2] * q.nx * q.ny + c[0] + c[1] * q.nx;
+}
+
+__global__ void __launch_bounds__(TH_BLOCK) k_ttm_grid_lattice(GridTTM q, int n, const double* __restrict__ x,
+                                                               const double* __restrict__ y,
+                                                               const double* __restrict__ z,
+                                                               const double* __restrict__ temp,
+                                                               const int* __restrict__ nneig,
+                                                               const unsigned* __restrict__ aflag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || nneig[i] < 2 || (aflag && !(aflag[i] & 1u))) return;
+    const int c = ttm_cell(q, x[i], y[i], z[i]);
+    if (c < 0) return;
+    const double t = temp[i] > 0.0 ? temp[i] : 0.0;
+    atomicAdd(&q.sum[c], (unsigned long long)llrint(t * TTM_CELL_SCALE));
+    atomicAdd(&q.cnt[c], 1);
+}
+
+__global__ void __launch_bounds__(TH_BLOCK) k_ttm_grid_fd(TTMParams p, GridTTM q, TTMState* st, unsigned* status) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = st->elapsed > p.offset;
+    if (c == 0) {
+        q.ctr[1] = active ? 1 : 0;
+        st->active = active ? 1 : 0;
+        if (active && st->firstfd) {
+            st->int_aen = 2.0 * st->kin / p.natoms;
+            st->n_zero = st->d_avg;
+        }
+    }
+    if (c >= q.fd.dim) return;
+    const int cnt = q.cnt[c];
+    const double ta = cnt > 0 ? ((double)q.sum[c] / TTM_CELL_SCALE) / (double)cnt : 0.0;
+    q.sum[c] = 0ull;  // ready for the next step's sums
+    q.cnt[c] = 0;
+    if (!active) return;
+    double te = q.A[c];
+    if (st->firstfd && te < 0.0) te = ta;
+    double v, dv;
+    tab_read64(p.g, te, v, dv, status);
+    q.fd.E[c] = cnt > 0 ? -p.g0 * v * (te - ta) : 0.0;
+    tab_read64(p.ce, te, v, dv, status);
+    q.cap[c] = p.c0 * v;
+    q.T[c] = te;
+}
+
+__global__ void __launch_bounds__(TH_BLOCK) k_ttm_grid_scale(TTMParams p, GridTTM q, int n, double volcut,
+                                                             TTMState* st, const double* __restrict__ x,
+                                                             const double* __restrict__ y,
+                                                             const double* __restrict__ z, double* __restrict__ vx,
+                                                             double* __restrict__ vy, double* __restrict__ vz,
+                                                             const int* __restrict__ type,
+                                                             const double* __restrict__ mass,
+                                                             const double* __restrict__ vcm,
+                                                             const double* __restrict__ temp,
+                                                             const double* __restrict__ dens,
+                                                             const unsigned* __restrict__ aflag,
+                                                             double* __restrict__ partial, unsigned* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = q.ctr[1] != 0;
+    double de = 0.0, cnt = 0.0;
+    if (active && i < n && (!aflag || (aflag[i] & 1u)) && dens[i] * volcut > 3.0) {
+        const int c = ttm_cell(q, x[i], y[i], z[i]);
+        if (c >= 0) {
+            const double te = q.A[c];
+            double v, dv;
+            tab_read64(p.g, te, v, dv, status);
+            const double e = p.g0 * v * (te - temp[i]) * p.vol * p.dt;
+            if (ttm_rescale(i, n, e, mass[type[i]], st->vmax2 * 1e-12, vx, vy, vz, vcm)) {
+                de = e;
+                cnt = 1.0;
+            }
+        }
+    }
+    ttm_block_partial(de, cnt, partial);
+    if (i == 0) {  // the step's bookkeeping, after every reader of it
+        st->elapsed += p.dt;
+        if (active) {
+            st->firstfd = 0;
+            q.ctr[0] += 1;
+        }
     }
 }
 
@@ -426,10 +579,49 @@ int ttm_pre(Context* c) {
     p.natoms = c->n;
     const ThermoParams tp = th_params(c, t);
     const int g = grid_for(c->n, TH_BLOCK);
+    const unsigned* aflag = c->flags_used ? c->aflag : nullptr;
     prof_begin(c, "ttm");
+    if (t.grid) {
+        FDGrid* fg = t.grid;
+        GridTTM q;
+        q.fd = fd_dev(fg);
+        q.fd.dt = c->dt;  // the grid steps with the MD time step (fd_time_step, TTM_Homogen_SCNA.h:175)
+        q.fd.mask_first = fg->dmask[0];
+        q.fd.mask_later = fg->dmask[1];
+        q.fd.solves = t.dev_ctr;
+        q.fd.active = t.dev_ctr + 1;
+        q.A = fg->dA[0];
+        q.T = fg->dA[1];
+        q.cap = fg->dcap;
+        q.h = fg->spacestep;
+        q.nx = fg->nx;
+        q.ny = fg->ny;
+        q.nz = fg->nz;
+        for (int d = 0; d < 3; d++) {
+            q.org[d] = t.org[d];
+            q.periodic[d] = c->box.periodic[d];
+            q.lo[d] = c->box.lo[d];
+            q.L[d] = c->box.L[d];
+        }
+        q.sum = t.cell_sum;
+        q.cnt = t.cell_cnt;
+        q.ctr = t.dev_ctr;
+        const int gc = grid_for(fg->dim, TH_BLOCK);
+        k_ttm_grid_lattice<<<g, TH_BLOCK, 0, c->stream>>>(q, c->n, c->x, c->y, c->z, t.temp, t.nneig, aflag);
+        k_ttm_grid_fd<<<gc, TH_BLOCK, 0, c->stream>>>(p, q, t.st, c->d_status);
+        cudaError_t e = fd_solve_coupled(q.fd, q.T, q.A, c->stream);
+        if (e != cudaSuccess) return check_cuda(c, e, "ttm grid solve");
+        k_ttm_grid_scale<<<g, TH_BLOCK, 0, c->stream>>>(p, q, c->n, tp.volcut, t.st, c->x, c->y, c->z, c->vx, c->vy,
+                                                        c->vz, c->type, c->d_mass, t.vcm, t.temp, t.dens, aflag,
+                                                        t.partial, c->d_status);
+        k_ttm_sum<<<1, 256, 0, c->stream>>>(g, t.partial, t.st);
+        prof_end(c);
+        c->launches += 5;
+        return check_cuda(c, cudaGetLastError(), "ttm grid");
+    }
     k_ttm_fd<<<1, 32, 0, c->stream>>>(p, t.st, c->d_status);
     k_ttm_scale<<<g, TH_BLOCK, 0, c->stream>>>(p, c->n, tp.volcut, t.st, c->vx, c->vy, c->vz, c->type, c->d_mass,
-                                                t.vcm, t.temp, t.dens, t.partial);
+                                                t.vcm, t.temp, t.dens, aflag, t.partial);
     k_ttm_sum<<<1, 256, 0, c->stream>>>(g, t.partial, t.st);
     prof_end(c);
     c->launches += 3;
@@ -438,9 +630,29 @@ int ttm_pre(Context* c) {
 
 bool ttm_active(const Context* c) { return c->ttm && c->ttm->ttm; }
 
+// Ends the grid coupling: the grid's solve count and cell vector (dA[0])
+// come back to its host-driven state.
+static void ttm_grid_detach(Context* c, TTMCtx& t) {
+    if (!t.grid) return;
+    int ctr[2] = {0, 0};
+    if (t.dev_ctr && cudaMemcpyAsync(ctr, t.dev_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, c->stream) == cudaSuccess &&
+        cudaStreamSynchronize(c->stream) == cudaSuccess)
+        t.grid->solves = ctr[0];
+    t.grid->cur = 0;
+    t.grid->coupled = false;
+    t.grid = nullptr;
+    cudaFree(t.cell_sum);
+    cudaFree(t.cell_cnt);
+    cudaFree(t.dev_ctr);
+    t.cell_sum = nullptr;
+    t.cell_cnt = nullptr;
+    t.dev_ctr = nullptr;
+}
+
 void ttm_release(Context* c) {
     if (!c->ttm) return;
     TTMCtx& t = *c->ttm;
+    ttm_grid_detach(c, t);
     cudaFree(t.vcm);
     cudaFree(t.temp);
     cudaFree(t.dens);
@@ -526,6 +738,58 @@ int omdg_set_ttm(omdg_ctx* c, const char* table_file, double atom_volume, double
         h.firstfd = 1;
         cudaMemcpy(t.st, &h, sizeof(h), cudaMemcpyHostToDevice);
     }
+    invalidate_graph(c);
+    return OMDG_OK;
+}
+
+int omdg_set_ttm_grid(omdg_ctx* c, omdg_fdtd* grid, const double* origin) {
+    if (!c) return OMDG_EINVAL;
+    cudaSetDevice(c->device);
+    if (!grid) {
+        if (c->ttm) ttm_grid_detach(c, *c->ttm);
+        invalidate_graph(c);
+        return OMDG_OK;
+    }
+    if (!origin) return set_error(c, OMDG_EINVAL, "the grid needs an origin");
+    if (!c->ttm || !c->ttm->ttm) return set_error(c, OMDG_ESTATE, "set the two-temperature model first");
+    if (grid->device != c->device) return set_error(c, OMDG_EINVAL, "the grid lives on another device");
+    if (grid->coupled && c->ttm->grid != grid) return set_error(c, OMDG_ESTATE, "the grid is coupled to another context");
+    for (const std::string* k : {&grid->str_src, &grid->str_con, &grid->str_cap})
+        if (k->find(':') != std::string::npos || k->find('{') != std::string::npos)
+            return set_error(c, OMDG_EINVAL, "time-ranged assignments need host steps of the grid");
+    TTMCtx& t = *c->ttm;
+    ttm_grid_detach(c, t);
+    // the kept strings once more (they are unranged: every later step would
+    // apply the same values), then their images on the device
+    int rc = fd_sync_data(grid);
+    if (!rc) rc = fd_upload(grid, grid->stream);
+    if (rc) return set_error(c, rc, grid->err);
+    cudaError_t e = cudaSuccess;
+    if (grid->cur == 1) {
+        e = cudaMemcpyAsync(grid->dA[0], grid->dA[1], sizeof(double) * grid->dim, cudaMemcpyDeviceToDevice,
+                            grid->stream);
+        grid->cur = 0;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(grid->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&t.cell_sum, sizeof(unsigned long long) * grid->dim);
+    if (e == cudaSuccess) e = cudaMalloc(&t.cell_cnt, sizeof(int) * grid->dim);
+    if (e == cudaSuccess) e = cudaMalloc(&t.dev_ctr, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(t.cell_sum, 0, sizeof(unsigned long long) * grid->dim);
+    if (e == cudaSuccess) e = cudaMemset(t.cell_cnt, 0, sizeof(int) * grid->dim);
+    const int ctr[2] = {grid->solves, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(t.dev_ctr, ctr, sizeof(ctr), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(t.cell_sum);
+        cudaFree(t.cell_cnt);
+        cudaFree(t.dev_ctr);
+        t.cell_sum = nullptr;
+        t.cell_cnt = nullptr;
+        t.dev_ctr = nullptr;
+        return check_cuda(c, e, "ttm grid");
+    }
+    for (int d = 0; d < 3; d++) t.org[d] = origin[d];
+    t.grid = grid;
+    grid->coupled = true;
     invalidate_graph(c);
     return OMDG_OK;
 }

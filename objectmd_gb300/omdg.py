@@ -127,6 +127,7 @@ SIGNATURES = {
     "omdg_set_thermo_detector": [_vp, _i, _d],
     "omdg_local_thermo": [_vp, _P(_d), _P(_d), _P(_d)],
     "omdg_set_ttm": [_vp, _cp, _d, _d, _d],
+    "omdg_set_ttm_grid": [_vp, _vp, _P(_d)],
     "omdg_ttm_state": [_vp, _P(_d), _P(_d), _P(_d), _P(_d)],
     "omdg_add_nn": [_vp, _i, _i, _cp, _cp],
     "omdg_nn_fallback_atoms": [_vp, _P(_l)],
@@ -598,6 +599,13 @@ class Context:
     def set_ttm(self, table_file, atom_volume, electron_temperature=-1.0, pulse_offset=0.0):
         self._check(self.lib.omdg_set_ttm(self.h, table_file.encode(), float(atom_volume),
                                           float(electron_temperature), float(pulse_offset)))
+
+    def set_ttm_grid(self, grid, origin=(0.0, 0.0, 0.0)):
+        """omdg_set_ttm_grid: the electron temperature on an FDTD grid's cells
+        (None detaches)."""
+        o = np.ascontiguousarray(origin, dtype=np.float64)
+        self._check(self.lib.omdg_set_ttm_grid(self.h, grid.h if grid is not None else None, _dp(o)))
+        self._ttm_grid = grid  # keep it alive while coupled
 
     def ttm_state(self):
         te, een, aen, tl = _d(), _d(), _d(), _d()

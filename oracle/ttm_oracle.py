@@ -109,3 +109,53 @@ class TTM:
             k += 1
         self.int_aen += s / k if k else 0.0
         return v
+
+
+CELL_SCALE = 1048576.0  # 2^20: the device sums cell temperatures as integers
+
+
+def grid_cells(x, origin, h, shape, lo=None, L=None, periodic=(False, False, False)):
+    """The grid cell index of each position (-1 outside), as the coupled
+    step assigns atoms: periodic axes wrapped into the box, a 2D grid
+    (nz = 1) spanning every z."""
+    nx, ny, nz = shape
+    out = np.full(len(x), -1)
+    for a, r in enumerate(x):
+        c = []
+        for d in range(3):
+            w = r[d]
+            if periodic[d]:
+                w -= np.floor((w - lo[d]) / L[d]) * L[d]
+            c.append(int(np.floor((w - origin[d]) / h)))
+        if nz == 1:
+            c[2] = 0
+        if 0 <= c[0] < nx and 0 <= c[1] < ny and 0 <= c[2] < nz:
+            out[a] = c[2] * nx * ny + c[0] + c[1] * nx
+    return out
+
+
+def grid_pre_integration(grid, cells, temp, nneig, G, Ce, g0, c0, first):
+    """The coupled step's electron part on an oracle/fdtd_oracle.Grid:
+    lattice temperature per cell (atoms with n_i >= 2, temperatures summed as
+    the device does, in units of 2^-20 K), the negative cells set at the
+    first active step, E = -g0 G(Te) (Te - Ta) where the cell holds atoms,
+    cap = c0 Ce(Te), then one solve.  Returns the per-cell lattice
+    temperatures."""
+    sums = [0] * grid.dim
+    cnt = [0] * grid.dim
+    for a in range(len(temp)):
+        if nneig[a] < 2 or cells[a] < 0:
+            continue
+        t = temp[a] if temp[a] > 0.0 else 0.0
+        sums[cells[a]] += int(np.rint(t * CELL_SCALE))
+        cnt[cells[a]] += 1
+    ta = np.array([(float(sums[c]) / CELL_SCALE) / cnt[c] if cnt[c] else 0.0 for c in range(grid.dim)])
+    for c in range(grid.dim):
+        te = grid.A[c]
+        if first and te < 0.0:
+            te = ta[c]
+        grid.A[c] = te
+        grid.E[c] = -g0 * G.read(te)[0] * (te - ta[c]) if cnt[c] else 0.0
+        grid.cap[c] = c0 * Ce.read(te)[0]
+    grid.solve()
+    return ta

@@ -75,7 +75,8 @@ def test_coupled_grid_step_matches_the_oracle(omdg_lib, oracle_lib):
     org = x0.min(0) - 0.5
     h = float((x0.max(0) - x0.min(0))[:2].max() + 1.0) / 4.0
     sym, cmap = "a pppp", "a" * 16
-    cond = "a 0.8 @ 1,1,0,2,2,0=0.3"
+    # explicit-step stability: 2 (con/2) dt / (h^2 cap) per face well below 1/4 (cap = C0 Ce(Te) ~ 2e-6 to 7e-6)
+    cond = "a 4e-4 @ 1,1,0,2,2,0=1.5e-4"
     dt = float(d["dt"])
     with omdg_lib.FDTD(4, 4, 1, sym, cmap) as g, cluster_ctx(omdg_lib, d) as ctx:
         g.set_spacestep(h)

@@ -197,6 +197,10 @@ int omdg_set_compat(omdg_ctx* ctx, const char* key, int on);
 
 /* Number of neighbour-list builds so far and of kernel launches issued by the last omdg_step. */
 int omdg_stats(omdg_ctx* ctx, long* rebuilds, long* launches);
+/* Replica mode: the list builds of each replica so far.  Inside steps a replica is re-sorted and its rows rebuilt
+   only when one of its own atoms moved more than skin/2 since its last build, as when it runs alone; a periodic
+   rebuild (rebuild_every), a state upload or an eager build takes all of them. */
+int omdg_replica_builds(omdg_ctx* ctx, int* builds, int nrep);
 /*
  * No reference counterpart (the reference has one scalar loop per potential).
  * Centres the last Stillinger-Weber or Tersoff force pass queued for the

@@ -24,6 +24,7 @@ int step_state_times(Context* c, double* dt, double* elapsed);
 int step_state_fetch(Context* c, unsigned* status, long long* step, int* row, double* elapsed, int rows);
 int step_state_rewind(Context* c);
 int step_clear_rebuild(Context* c);
+int step_flag_requested_replicas(Context* c);
 int launch_set_rebuild_cond(Context* c, cudaGraphConditionalHandle h);
 int threebody_prepare(Context* c);
 
@@ -346,6 +347,9 @@ int omdg_destroy(omdg_ctx* c) {
     cudaFree(c->d_rep_geom);
     cudaFree(c->d_rep_shift);
     cudaFree(c->d_rep_sums);
+    cudaFree(c->d_rep_flag);
+    cudaFree(c->d_rep_builds);
+    cudaFree(c->d_cell_rep);
     cudaFree(c->d_status);
     cudaFree(c->d_flags);
     cudaFree(c->d_state);
@@ -407,11 +411,15 @@ int omdg_set_replicas(omdg_ctx* c, int nrep, const int* natoms, const double* lo
     cudaFree(c->d_rep_of);
     cudaFree(c->d_rep_sums);
     cudaFree(c->d_rep_start);
+    cudaFree(c->d_rep_flag);
+    cudaFree(c->d_rep_builds);
+    cudaFree(c->d_cell_rep);
     c->d_rep_start = nullptr;
     c->d_rep_geom = c->d_rep_shift = nullptr;
     c->d_rep_of = nullptr;
     c->rep_of_cap = 0;
     c->d_rep_sums = nullptr;
+    c->d_rep_flag = c->d_rep_builds = c->d_cell_rep = nullptr;
     c->have_box = true;
     compute_frame(c);
     c->list_valid = false;
@@ -942,8 +950,12 @@ static int eager_maybe_rebuild(Context* c) {
     int rc = step_state_read(c, nullptr, nullptr, &rebuild);
     if (rc) return rc;
     if (rebuild) {
+        if ((rc = step_flag_requested_replicas(c))) return rc;
         if ((rc = step_clear_rebuild(c))) return rc;
-        if ((rc = nlist_build(c))) return rc;
+        c->build_partial = c->nrep > 0;
+        rc = nlist_build(c);
+        c->build_partial = false;
+        if (rc) return rc;
     }
     return OMDG_OK;
 }
@@ -1008,7 +1020,9 @@ static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr)
             if (!rc) {
                 c->stream = gs.side;
                 c->build_in_step = true;
+                c->build_partial = c->nrep > 0;  // the flagged replicas only
                 rc = nlist_build(c);
+                c->build_partial = false;
                 c->build_in_step = false;
                 c->stream = s;
                 cudaGraph_t body_out = nullptr;
@@ -1747,6 +1761,16 @@ int omdg_stats(omdg_ctx* c, long* rebuilds, long* launches) {
     return OMDG_OK;
 }
 
+int omdg_replica_builds(omdg_ctx* c, int* builds, int nrep) {
+    if (!c || !builds) return OMDG_EINVAL;
+    if (c->nrep == 0 || !c->d_rep_builds) return set_error(c, OMDG_ESTATE, "no replicas built");
+    if (nrep != c->nrep) return set_error(c, OMDG_EINVAL, "nrep must be the replica count");
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaMemcpyAsync(builds, c->d_rep_builds, sizeof(int) * nrep, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return check_cuda(c, e, "omdg_replica_builds");
+}
+
 int omdg_wide_centres(omdg_ctx* c, int* count) {
     if (!c || !count) return OMDG_EINVAL;
     *count = 0;
@@ -1798,6 +1822,7 @@ static int* launch_knob(Context* c, const std::string& k) {
     if (k == "pair_lanes") return &c->pair_lanes;
     if (k == "tb_block") return &c->tb_block;
     if (k == "tb_lanes") return &c->tb_lanes;
+    if (k == "tb_persistent") return &c->tb_persistent;
     if (k == "nbr_hshift") return &c->nbr_hshift;
     if (k == "build_lanes") return &c->build_lanes;
     if (k == "io_blocks") return &c->io_blocks;
@@ -1811,7 +1836,7 @@ static bool valid_knob(const std::string& k, int v) {
     if (k == "eam_block" || k == "pair_block" || k == "tb_block") return v >= 32 && v <= 1024 && v % 32 == 0;
     if (k == "nbr_hshift") return v >= 0 && v <= 5;
     if (k == "eam_ctas_per_sm") return v >= 1 && v <= 32;
-    if (k == "eam_stage") return v == 0 || v == 1;
+    if (k == "eam_stage" || k == "tb_persistent") return v == 0 || v == 1;
     if (k == "build_lanes") return v == 0 || v == 1 || v == 4 || v == 8;
     if (k == "io_blocks") return v >= 1 && v <= 65535;
     if (k == "nbr_capacity") return v >= 0 && v <= 4096;
@@ -1927,8 +1952,10 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
         for (int lanes : {2, 4, 8, 16})
             for (int block : {128, 256}) cands.push_back(Cand{lanes, block, 0});
     } else if (tb) {
+        // stage: the Tersoff register pass as one resident grid (persistent)
         for (int lanes : {1, 2, 4})
-            for (int block : {64, 128, 256}) cands.push_back(Cand{lanes, block, 0});
+            for (int block : {64, 128, 256})
+                for (int stage : {0, 1}) cands.push_back(Cand{lanes, block, stage});
     }
     int rc = OMDG_OK;
     // list build: cell-CTA, 8 or 4 lanes per atom, or one thread per atom
@@ -1971,6 +1998,7 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
         } else {
             c->tb_lanes = cd.lanes;
             c->tb_block = cd.block;
+            c->tb_persistent = cd.stage;
         }
         if ((rc = omdg_set_launch(c, "nbr_hshift", hs))) return rc;
         if (!c->list_valid && (rc = build_list(c))) return rc;
@@ -1995,6 +2023,7 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
     } else {
         c->tb_lanes = win.lanes;
         c->tb_block = win.block;
+        c->tb_persistent = win.stage;
     }
     if ((rc = omdg_set_launch(c, "nbr_hshift", hs))) return rc;
     if (!c->list_valid && (rc = build_list(c))) return rc;

@@ -35,6 +35,7 @@ struct StepState {
     int src_first;           // EnergySource: the first call inside the window only arms it
     int src_scale;           // EnergySource: scale velocities at the next PreIntegration
     int halted;              // a rebuild overflowed its rows: later rebuilds are skipped until omdg_sync recovers
+    int rebuild_all;         // replica mode: the request covers every replica (periodic rebuild, state upload)
 };
 
 struct IntParams {
@@ -58,11 +59,13 @@ __global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __re
                                                     const float* __restrict__ fz, const double* __restrict__ f64,
                                                     const int* __restrict__ type, PosPack* __restrict__ pack,
                                                     const float4* __restrict__ xref, unsigned* __restrict__ aflag,
-                                                    StepState* st) {
+                                                    StepState* st, const int* __restrict__ rep_of,
+                                                    int* __restrict__ rflag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     __shared__ int moved;
     if (threadIdx.x == 0) moved = 0;
     __syncthreads();
+    bool self_moved = false;  // replica mode: flag this atom's replica
     unsigned fl = 1u;
     if (i < p.n && aflag) {
         fl = aflag[i];
@@ -76,6 +79,7 @@ __global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __re
                 fl &= ~1u;
                 aflag[i] = fl;
                 moved = 1;
+                self_moved = true;
             }
         }
     }
@@ -122,8 +126,12 @@ __global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __re
         pack[i] = pk;
         float4 r0 = xref[i];
         float dx = (pk.hi.x - r0.x) + pk.lo.x, dy = (pk.hi.y - r0.y) + pk.lo.y, dz = (pk.hi.z - r0.z) + pk.lo.z;
-        if (!(dx * dx + dy * dy + dz * dz <= p.half_skin2)) moved = 1;  // NaN counts as moved
+        if (!(dx * dx + dy * dy + dz * dz <= p.half_skin2)) {  // NaN counts as moved
+            moved = 1;
+            self_moved = true;
+        }
     }
+    if (self_moved && rflag) rflag[rep_of[i]] = 1;
     __syncthreads();
     if (threadIdx.x == 0 && moved) st->rebuild = 1;
 }
@@ -234,7 +242,10 @@ __device__ void finalize_block(const FinParams& p, int nblocks, const BlockParti
             st->elapsed += st->dt;  // ElapsedTime += TimeStep; Step++ (system.cpp:979-980)
             st->step += 1;
             st->row = row + 1;
-            if (st->rebuild_every > 0 && (st->step % st->rebuild_every) == 0) st->rebuild = 1;
+            if (st->rebuild_every > 0 && (st->step % st->rebuild_every) == 0) {
+                st->rebuild = 1;
+                st->rebuild_all = 1;
+            }
             if (p.src_on) {  // EnergySource::PreIntegration of the next step
                 int scale = 0;
                 if (st->elapsed >= p.src_start) {
@@ -567,7 +578,9 @@ int integrate_kick_drift(Context* c, int) {
     k_kick_drift<<<grid_for(c->n, 256), 256, 0, c->stream>>>(p, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->fx, c->fy,
                                                              c->fz, c->f64, c->type, c->pack, c->xref,
                                                              c->flags_used ? c->aflag : nullptr,
-                                                             reinterpret_cast<StepState*>(c->d_state));
+                                                             reinterpret_cast<StepState*>(c->d_state),
+                                                             c->nrep > 0 ? c->d_rep_of : nullptr,
+                                                             c->nrep > 0 ? c->d_rep_flag : nullptr);
     prof_end(c);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "kick_drift");
@@ -757,12 +770,16 @@ int step_state_init(Context* c) {
     h.src_first = 1;
     h.src_scale = 0;
     h.halted = 0;
+    h.rebuild_all = 0;
     cudaError_t e = cudaMemcpyAsync(c->d_state, &h, sizeof(StepState), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return check_cuda(c, e, "step state");
 }
 
-__global__ void k_clear_rebuild(StepState* st) { st->rebuild = 0; }
+__global__ void k_clear_rebuild(StepState* st) {
+    st->rebuild = 0;
+    st->rebuild_all = 0;  // the eager build that follows is a full one
+}
 
 // The reference scales velocities at the end of the step
 // (TempController::PostIntegration); here the factor waits in the step state
@@ -845,7 +862,10 @@ __global__ void __launch_bounds__(IO_BLOCK) k_upload_state(IntParams p, const in
         }
     }
     __syncthreads();
-    if (t == 0 && moved) st->rebuild = 1;
+    if (t == 0 && moved) {
+        st->rebuild = 1;
+        st->rebuild_all = 1;
+    }
 }
 
 int upload_state(Context* c, const double* in_x, const double* in_v) {
@@ -857,6 +877,21 @@ int upload_state(Context* c, const double* in_x, const double* in_v) {
     return check_cuda(c, cudaGetLastError(), "state upload");
 }
 
+__global__ void k_flag_all_if_requested(const StepState* st, int nrep, int* rflag) {
+    if (!st->rebuild_all) return;
+    for (int r = threadIdx.x; r < nrep; r += blockDim.x) rflag[r] = 1;
+}
+
+// Replica mode, eager steps: a request for every replica flags them all
+// before the partial build (as the graph's predicate does).
+int step_flag_requested_replicas(Context* c) {
+    if (c->nrep == 0) return OMDG_OK;
+    k_flag_all_if_requested<<<1, 256, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state), c->nrep,
+                                                      c->d_rep_flag);
+    c->launches++;
+    return check_cuda(c, cudaGetLastError(), "replica flags");
+}
+
 int step_clear_rebuild(Context* c) {
     k_clear_rebuild<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state));
     c->launches++;
@@ -865,15 +900,25 @@ int step_clear_rebuild(Context* c) {
 
 // Graph-side rebuild predicate: copies the request into the conditional
 // handle and clears it.
-__global__ void k_set_rebuild_cond(StepState* st, cudaGraphConditionalHandle h) {
+// In replica mode a request for every replica sets every replica's flag
+// (the build then rebuilds the flagged replicas only).
+__global__ void k_set_rebuild_cond(StepState* st, cudaGraphConditionalHandle h, int nrep, int* rflag) {
     const bool go = st->rebuild && !st->halted;
-    cudaGraphSetConditional(h, go ? 1u : 0u);
-    if (go) st->nrebuild += 1;
-    st->rebuild = 0;
+    const bool all = st->rebuild_all != 0;
+    __syncthreads();
+    if (go && all && rflag)
+        for (int r = threadIdx.x; r < nrep; r += blockDim.x) rflag[r] = 1;
+    if (threadIdx.x == 0) {
+        cudaGraphSetConditional(h, go ? 1u : 0u);
+        if (go) st->nrebuild += 1;
+        st->rebuild = 0;
+        if (go) st->rebuild_all = 0;
+    }
 }
 
 int launch_set_rebuild_cond(Context* c, cudaGraphConditionalHandle h) {
-    k_set_rebuild_cond<<<1, 1, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state), h);
+    k_set_rebuild_cond<<<1, 256, 0, c->stream>>>(reinterpret_cast<StepState*>(c->d_state), h, c->nrep,
+                                                 c->nrep > 0 ? c->d_rep_flag : nullptr);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "rebuild predicate");
 }

@@ -174,10 +174,16 @@ __global__ void k_scan_add(int m, int* __restrict__ start, const int* __restrict
     if (k < m) start[k] += tile_off[k / SCAN_TILE];
 }
 
+// Replica filters of a partial rebuild: only atoms (by index) and cells of
+// replicas whose flag is set take part; a null flag array takes everything.
+__device__ __forceinline__ bool rep_on(const int* __restrict__ flag, const int* __restrict__ rep, int k) {
+    return !flag || flag[rep[k]] != 0;
+}
+
 __global__ void k_scatter(int n, const int* __restrict__ cell, const int* __restrict__ start, int* __restrict__ fill,
-                          int* __restrict__ perm) {
+                          int* __restrict__ perm, const int* __restrict__ rep_of, const int* __restrict__ rflag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || !rep_on(rflag, rep_of, i)) return;
     int c = cell[i];
     int s = start[c] + atomicAdd(&fill[c], 1);
     perm[s] = i;
@@ -191,9 +197,10 @@ constexpr int CELL_SORT_MAX = 1024;
 // registers by an odd-even transposition network (fully unrolled).
 constexpr int CELL_SORT_SMALL = 8;
 
-__global__ void k_cell_sort_small(int m, const int* __restrict__ start, int* __restrict__ perm) {
+__global__ void k_cell_sort_small(int m, const int* __restrict__ start, int* __restrict__ perm,
+                                  const int* __restrict__ cell_rep, const int* __restrict__ rflag) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= m) return;
+    if (c >= m || !rep_on(rflag, cell_rep, c)) return;
     const int b = start[c], k = start[c + 1] - b;
     if (k <= 1 || k > CELL_SORT_SMALL) return;
     int v[CELL_SORT_SMALL];
@@ -220,10 +227,12 @@ __global__ void k_cell_sort_small(int m, const int* __restrict__ start, int* __r
 // in place.  Cells of more than 32 atoms take lane 0's insertion sort; a
 // pathological cell beyond CELL_SORT_MAX is left unsorted (its order is then
 // not reproducible) rather than sorted in O(k^2).
-__global__ void k_cell_sort_warp(int m, const int* __restrict__ start, int* __restrict__ perm, int skip) {
+__global__ void k_cell_sort_warp(int m, const int* __restrict__ start, int* __restrict__ perm, int skip,
+                                 const int* __restrict__ cell_rep, const int* __restrict__ rflag) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += warps) {
+        if (!rep_on(rflag, cell_rep, c)) continue;  // uniform over the warp
         const int b = start[c], k = start[c + 1] - b;
         if (k <= skip) continue;  // empty, single, or sorted by k_cell_sort_small
         if (k <= 32) {
@@ -263,9 +272,10 @@ struct AtomArrays {
 // position k of caller atom id[o]).
 __global__ void k_permute_gather(int n, const int* __restrict__ perm, AtomArrays a, AtomArrays st,
                                  const int* __restrict__ cell_old, int* __restrict__ cell_new,
-                                 int* __restrict__ inv) {
+                                 int* __restrict__ inv, const int* __restrict__ rep_of,
+                                 const int* __restrict__ rflag) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    if (k >= n || !rep_on(rflag, rep_of, k)) return;  // a replica's atoms stay in its index range
     int o = perm[k];
     cell_new[k] = cell_old[o];
     inv[a.id[o]] = k;
@@ -306,9 +316,10 @@ __global__ void k_halt_on_overflow(const unsigned* __restrict__ status, int* hal
     if (*status & ERR_NBR_OVERFLOW) *halted = 1;
 }
 
-__global__ void k_permute_copyback(int n, AtomArrays st, AtomArrays a) {
+__global__ void k_permute_copyback(int n, AtomArrays st, AtomArrays a, const int* __restrict__ rep_of,
+                                   const int* __restrict__ rflag) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    if (k >= n || !rep_on(rflag, rep_of, k)) return;
     a.x[k] = st.x[k];
     a.y[k] = st.y[k];
     a.z[k] = st.z[k];
@@ -326,6 +337,24 @@ __global__ void k_zero_ints(int m, int* __restrict__ a, int* __restrict__ b) {
     if (k < m) {
         a[k] = 0;
         b[k] = 0;
+    }
+}
+
+// The cell counters of the flagged replicas (and the sentinel past the last cell).
+__global__ void k_zero_cells_rep(int m, int* __restrict__ count, int* __restrict__ fill,
+                                 const int* __restrict__ cell_rep, const int* __restrict__ rflag) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > m || (k < m && !rep_on(rflag, cell_rep, k))) return;
+    count[k] = 0;
+    fill[k] = 0;
+}
+
+// After a build: count it for each replica rebuilt and clear the flags
+// (all replicas after a full build).
+__global__ void k_rep_build_done(int nrep, int full, int* __restrict__ rflag, int* __restrict__ builds) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrep; r += gridDim.x * blockDim.x) {
+        if (full || rflag[r]) builds[r] += 1;
+        rflag[r] = 0;
     }
 }
 
@@ -366,10 +395,11 @@ __global__ void k_pack(int n, const double* __restrict__ x, const double* __rest
                        const double* __restrict__ z, const int* __restrict__ type, PackFrame f,
                        PosPack* __restrict__ pack, float4* __restrict__ xref, const int* __restrict__ cell,
                        LocFrame lf, const int* __restrict__ rep_of, const RepGeom* __restrict__ rg,
-                       const unsigned* __restrict__ aflag, float4* __restrict__ loc, unsigned* umax) {
+                       const unsigned* __restrict__ aflag, float4* __restrict__ loc, unsigned* umax,
+                       const int* __restrict__ rflag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     float m = 0.f;
-    if (i < n) {
+    if (i < n && (!rflag || rflag[rep_of[i]])) {
         PosPack p;
         pack_coord(x[i], f.Qh[0], f.Ql[0], p.hi.x, p.lo.x);
         pack_coord(y[i], f.Qh[1], f.Ql[1], p.hi.y, p.lo.y);
@@ -586,9 +616,10 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const RepGeom* __r
                                                const double* __restrict__ z, const int* __restrict__ cell,
                                                const int* __restrict__ start, const unsigned* __restrict__ umax,
                                                unsigned* __restrict__ nbr, int* __restrict__ nnb, unsigned* status,
-                                               int* need) {
+                                               int* need, const int* __restrict__ rflag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    if (REP && rflag && !rflag[rep_of[i]]) return;  // the replica keeps its list
     if (REP)
         build_row(p, RepGrid{rg + rep_of[i]}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need);
     else
@@ -599,9 +630,10 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const RepGeom* __r
 
 __global__ void k_cell_assign_rep(int n, double* __restrict__ x, double* __restrict__ y, double* __restrict__ z,
                                   const int* __restrict__ rep_of, const RepGeom* __restrict__ rg,
-                                  int* __restrict__ cell, int* __restrict__ count, unsigned* status) {
+                                  int* __restrict__ cell, int* __restrict__ count, unsigned* status,
+                                  const int* __restrict__ rflag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || !rep_on(rflag, rep_of, i)) return;
     const RepGeom& g = rg[rep_of[i]];
     double p[3] = {x[i], y[i], z[i]};
     const int cx = axis_cell_of(p[0], g.periodic[0], g.lo[0], g.L[0], g.cell_org[0], g.inv_h[0], g.nc[0]);
@@ -934,6 +966,15 @@ int replica_prepare(Context* c) {
     if (e == cudaSuccess && !c->d_rep_shift) e = cudaMalloc(&c->d_rep_shift, sizeof(ShiftF) * c->nrep);
     if (e == cudaSuccess && !c->d_rep_start) e = cudaMalloc(&c->d_rep_start, sizeof(int) * (c->nrep + 1));
     if (e == cudaSuccess && !c->d_rep_sums) e = cudaMalloc(&c->d_rep_sums, sizeof(double) * 2 * c->nrep);
+    if (e == cudaSuccess && !c->d_rep_flag) {
+        e = cudaMalloc(&c->d_rep_flag, sizeof(int) * c->nrep);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->d_rep_flag, 0, sizeof(int) * c->nrep, c->stream);
+    }
+    if (e == cudaSuccess && !c->d_rep_builds) {
+        e = cudaMalloc(&c->d_rep_builds, sizeof(int) * c->nrep);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->d_rep_builds, 0, sizeof(int) * c->nrep, c->stream);
+    }
+    if (e == cudaSuccess && !c->d_cell_rep) e = cudaMalloc(&c->d_cell_rep, sizeof(int) * std::max(1, base));
     if (e == cudaSuccess && (!c->d_rep_of || c->rep_of_cap < c->cap)) {
         cudaFree(c->d_rep_of);
         c->d_rep_of = nullptr;
@@ -942,9 +983,12 @@ int replica_prepare(Context* c) {
         invalidate_graph(c);
     }
     if (e != cudaSuccess) return set_error(c, OMDG_ENOMEM, "replica tables");
-    std::vector<int> of(c->n);
+    std::vector<int> of(c->n), cell_rep(std::max(1, base));
     for (int r = 0; r < c->nrep; r++)
         for (int i = c->rep_start[r]; i < c->rep_start[r + 1]; i++) of[i] = r;
+    for (int r = 0; r < c->nrep; r++)
+        for (int k = rg[r].cell_base; k < (r + 1 < c->nrep ? rg[r + 1].cell_base : base); k++) cell_rep[k] = r;
+    cudaMemcpyAsync(c->d_cell_rep, cell_rep.data(), sizeof(int) * cell_rep.size(), cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(c->d_rep_geom, rg.data(), sizeof(RepGeom) * c->nrep, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(c->d_rep_shift, sh.data(), sizeof(ShiftF) * c->nrep, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(c->d_rep_of, of.data(), sizeof(int) * c->n, cudaMemcpyHostToDevice, c->stream);
@@ -1014,7 +1058,7 @@ int integrate_pack(Context* c) {
     // xref keeps the positions of the last build (the displacement reference)
     k_pack<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack,
                                                        nullptr, nullptr, LocFrame{}, nullptr, nullptr,
-                                                       nullptr, nullptr, nullptr);
+                                                       nullptr, nullptr, nullptr, nullptr);
     c->launches++;
     return check_cuda(c, cudaGetLastError(), "pack");
 }
@@ -1040,11 +1084,18 @@ int nlist_build(Context* c) {
             static_cast<unsigned char*>(c->snap_state), sb);
         c->launches++;
     }
-    k_zero_ints<<<grid_for(m + 1, 256), 256, 0, s>>>(m + 1, c->cell_count, c->cell_fill);
+    // a partial build (replica mode, inside a step): only the replicas whose
+    // atoms moved past skin/2 are re-sorted and re-listed; every replica keeps
+    // its index range and cell range, so the others' arrays stay valid
+    const int* rflag = (reps && c->build_partial) ? c->d_rep_flag : nullptr;
+    if (rflag)
+        k_zero_cells_rep<<<grid_for(m + 1, 256), 256, 0, s>>>(m, c->cell_count, c->cell_fill, c->d_cell_rep, rflag);
+    else
+        k_zero_ints<<<grid_for(m + 1, 256), 256, 0, s>>>(m + 1, c->cell_count, c->cell_fill);
     if (reps)
         k_cell_assign_rep<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->d_rep_of,
                                                              static_cast<const RepGeom*>(c->d_rep_geom), c->cell,
-                                                             c->cell_count, c->d_status);
+                                                             c->cell_count, c->d_status, rflag);
     else
         k_cell_assign<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, g, c->cell, c->cell_count,
                                                          c->d_status);
@@ -1052,18 +1103,18 @@ int nlist_build(Context* c) {
     k_scan_tiles<<<ntiles, SCAN_THREADS, 0, s>>>(m, c->cell_count, c->cell_start, c->cell_tile_sum);
     k_scan_totals<<<1, 1024, 0, s>>>(ntiles, m, c->cell_tile_sum, c->cell_start);
     k_scan_add<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->cell_tile_sum);
-    k_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->cell, c->cell_start, c->cell_fill, c->perm);
+    k_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->cell, c->cell_start, c->cell_fill, c->perm, c->d_rep_of, rflag);
     // most cells of a sparse grid (replica margins, vacuum) hold 0 or 1 atoms:
     // a bounded grid of warps strides over the cells instead of one warp each
     // sparse grids (a few atoms per cell) sort most cells a thread each;
     // dense ones (EAM: ~20 atoms per cell) leave every cell to the warps
     const bool sparse = n < 8 * m;
     if (sparse) {
-        k_cell_sort_small<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->perm);
+        k_cell_sort_small<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->perm, c->d_cell_rep, rflag);
         c->launches++;
     }
-    k_cell_sort_warp<<<std::min(grid_for(m, 8), 16 * c->num_sms), 256, 0, s>>>(m, c->cell_start, c->perm,
-                                                                                sparse ? CELL_SORT_SMALL : 1);
+    k_cell_sort_warp<<<std::min(grid_for(m, 8), 16 * c->num_sms), 256, 0, s>>>(
+        m, c->cell_start, c->perm, sparse ? CELL_SORT_SMALL : 1, c->d_cell_rep, rflag);
     c->launches += 7;
     AtomArrays cur{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->aflag, c->extra, c->extra_n};
     AtomArrays stg{c->stage_d, c->stage_d + c->cap, c->stage_d + 2 * (size_t)c->cap, c->stage_d + 3 * (size_t)c->cap,
@@ -1071,8 +1122,9 @@ int nlist_build(Context* c) {
                    c->stage_i + c->cap, reinterpret_cast<unsigned*>(c->stage_i + 2 * (size_t)c->cap),
                    c->stage_extra, c->extra_n};
     int* cell_sorted = c->cell_sorted;
-    k_permute_gather<<<grid_for(n, 256), 256, 0, s>>>(n, c->perm, cur, stg, c->cell, cell_sorted, c->inv);
-    k_permute_copyback<<<grid_for(n, 256), 256, 0, s>>>(n, stg, cur);
+    k_permute_gather<<<grid_for(n, 256), 256, 0, s>>>(n, c->perm, cur, stg, c->cell, cell_sorted, c->inv,
+                                                      c->d_rep_of, rflag);
+    k_permute_copyback<<<grid_for(n, 256), 256, 0, s>>>(n, stg, cur, c->d_rep_of, rflag);
     c->launches += 2;
     prof_end(c);
     prof_begin(c, "pack");
@@ -1087,7 +1139,7 @@ int nlist_build(Context* c) {
     const RepGeom* rg = reps ? static_cast<const RepGeom*>(c->d_rep_geom) : nullptr;
     k_pack<<<grid_for(n, 256), 256, 0, s>>>(n, c->x, c->y, c->z, c->type, pack_frame(c), c->pack, c->xref,
                                             cell_sorted, lf, reps ? c->d_rep_of : nullptr, rg,
-                                            c->flags_used ? c->aflag : nullptr, c->loc, umax);
+                                            c->flags_used ? c->aflag : nullptr, c->loc, umax, rflag);
     c->launches += 2;
     prof_end(c);
 
@@ -1119,12 +1171,12 @@ int nlist_build(Context* c) {
     if (reps) {
         k_build<true><<<grid_for(n, 128), 128, 0, s>>>(bp, rg, c->d_rep_of, c->loc, c->x, c->y, c->z, cell_sorted,
                                                        c->cell_start, umax, reinterpret_cast<unsigned*>(c->nbr),
-                                                       c->nnb, c->d_status, c->d_flags + 1);
+                                                       c->nnb, c->d_status, c->d_flags + 1, rflag);
     } else if (c->flags_used) {  // only the cell-local build skips inactive atoms
         k_build<false><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
                                                         cell_sorted, c->cell_start, umax,
                                                         reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
-                                                        c->d_flags + 1);
+                                                        c->d_flags + 1, nullptr);
     } else if (c->build_lanes == 0 && combos <= 64 && !sparse) {  // a cell CTA wants >= 8 atoms per cell
         const int cap = 1024;  // staged candidates per chunk (32 bytes each)
         k_build_cells<<<m, BUILD_CELL_THREADS, cap * 2 * sizeof(float4), s>>>(
@@ -1142,11 +1194,16 @@ int nlist_build(Context* c) {
         k_build<false><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
                                                         cell_sorted, c->cell_start, umax,
                                                         reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
-                                                        c->d_flags + 1);
+                                                        c->d_flags + 1, nullptr);
     }
     c->launches++;
     if (c->build_in_step) {
         k_halt_on_overflow<<<1, 1, 0, s>>>(c->d_status, step_state_halted(c));
+        c->launches++;
+    }
+    if (reps) {
+        k_rep_build_done<<<grid_for(c->nrep, 256), 256, 0, s>>>(c->nrep, rflag ? 0 : 1, c->d_rep_flag,
+                                                                 c->d_rep_builds);
         c->launches++;
     }
     prof_end(c);

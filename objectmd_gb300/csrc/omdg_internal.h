@@ -190,6 +190,10 @@ struct Context {
     double* d_rep_sums = nullptr;        // per-replica ledger sums
     TTMCtx* ttm = nullptr;               // ThermoDetector / TTM_Homogen state (null: off)
     int* d_rep_start = nullptr;          // nrep + 1
+    int* d_rep_flag = nullptr;           // per replica: an atom moved past skin/2 (rebuild it)
+    int* d_rep_builds = nullptr;         // per replica: list builds so far
+    int* d_cell_rep = nullptr;           // replica of each cell (rep_cells)
+    bool build_partial = false;          // the build being issued rebuilds only the flagged replicas
     int ncell_cap = 0;
     int* scan_partials = nullptr;
     double* stage_d = nullptr;   // permutation staging: 6 FP64 arrays x cap
@@ -254,6 +258,7 @@ struct Context {
     int pair_lanes = 8;
     int tb_block = 128;        // three-body kernels
     int tb_lanes = 1;
+    int tb_persistent = 0;     // Tersoff register pass: one resident grid striding over the flattened atoms
 
     // potentials
     std::vector<Potential> pots;

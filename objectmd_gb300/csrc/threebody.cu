@@ -562,14 +562,40 @@ __device__ __noinline__ void ters_centre_wide(const TersDev& p, int i, const Pos
 
 constexpr int TERS_REG = 4;  // in-cutoff neighbours the register path holds (diamond: 4)
 
-__global__ void __launch_bounds__(128, 6) k_tersoff_a(TersDev p, const PosPack* __restrict__ pack,
+__device__ __forceinline__ void ters_reg_centre(const TersDev& p, int i, const PosPack* __restrict__ pack,
+                                                const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                                float4* __restrict__ slot, float* __restrict__ fx,
+                                                float* __restrict__ fy, float* __restrict__ fz,
+                                                float* __restrict__ pe, float* __restrict__ vir,
+                                                const int* __restrict__ mask, int* __restrict__ wide);
+
+// One thread per centre.  Launched with fewer threads than centres (the
+// persistent form: one resident grid over the flattened atoms of every
+// replica), each thread strides over the centres.
+constexpr int TERS_CTAS_PER_SM = 6;
+
+template <bool PERSISTENT>
+__global__ void __launch_bounds__(128, TERS_CTAS_PER_SM) k_tersoff_a(TersDev p, const PosPack* __restrict__ pack,
                                                    const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                    float4* __restrict__ slot, float* __restrict__ fx,
                                                    float* __restrict__ fy, float* __restrict__ fz,
                                                    float* __restrict__ pe, float* __restrict__ vir, unsigned* status,
                                                    const int* __restrict__ mask, int* __restrict__ wide) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+    if (PERSISTENT) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x)
+            ters_reg_centre(p, i, pack, nbr, nnb, slot, fx, fy, fz, pe, vir, mask, wide);
+    } else {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < p.n) ters_reg_centre(p, i, pack, nbr, nnb, slot, fx, fy, fz, pe, vir, mask, wide);
+    }
+}
+
+__device__ __forceinline__ void ters_reg_centre(const TersDev& p, int i, const PosPack* __restrict__ pack,
+                                                const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
+                                                float4* __restrict__ slot, float* __restrict__ fx,
+                                                float* __restrict__ fy, float* __restrict__ fz,
+                                                float* __restrict__ pe, float* __restrict__ vir,
+                                                const int* __restrict__ mask, int* __restrict__ wide) {
     if (mask && !mask[i]) return;  // centres another potential evaluates
     const PosPack pi = pack[i];
     const bool mine = p.single_type || pack_type(pi.hi) == p.ta;
@@ -803,9 +829,14 @@ int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask) {
     p.first = first ? 1 : 0;
     prof_begin(c, mask ? "tersoff_fallback" : "tersoff_centre");
     cudaMemsetAsync(c->ters_wide, 0, sizeof(int), c->stream);
-    k_tersoff_a<<<grid_for(c->n, 128), 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr),
-                                                             c->nnb, c->slot_buf, c->fx, c->fy, c->fz, c->pe, c->vir,
-                                                             c->d_status, mask, c->ters_wide);
+    if (c->tb_persistent)
+        k_tersoff_a<true><<<std::min(grid_for(c->n, 128), TERS_CTAS_PER_SM * c->num_sms), 128, 0, c->stream>>>(
+            p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->slot_buf, c->fx, c->fy, c->fz, c->pe,
+            c->vir, c->d_status, mask, c->ters_wide);
+    else
+        k_tersoff_a<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(
+            p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->slot_buf, c->fx, c->fy, c->fz, c->pe,
+            c->vir, c->d_status, mask, c->ters_wide);
     k_tersoff_wide<<<2 * c->num_sms, 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr),
                                                           c->nnb, c->ters_wide, c->slot_buf, c->fx, c->fy, c->fz,
                                                           c->pe, c->vir, c->d_status);

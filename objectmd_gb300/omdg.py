@@ -128,6 +128,7 @@ SIGNATURES = {
     "omdg_local_thermo": [_vp, _P(_d), _P(_d), _P(_d)],
     "omdg_set_ttm": [_vp, _cp, _d, _d, _d],
     "omdg_set_ttm_grid": [_vp, _vp, _P(_d)],
+    "omdg_replica_builds": [_vp, _P(_i), _i],
     "omdg_ttm_state": [_vp, _P(_d), _P(_d), _P(_d), _P(_d)],
     "omdg_add_nn": [_vp, _i, _i, _cp, _cp],
     "omdg_nn_fallback_atoms": [_vp, _P(_l)],
@@ -788,6 +789,12 @@ class Context:
         r, l = _l(), _l()
         self._check(self.lib.omdg_stats(self.h, ctypes.byref(r), ctypes.byref(l)))
         return {"rebuilds": r.value, "launches": l.value}
+
+    def replica_builds(self, nrep):
+        """omdg_replica_builds: list builds per replica."""
+        out = np.zeros(int(nrep), dtype=np.int32)
+        self._check(self.lib.omdg_replica_builds(self.h, _ip(out), int(nrep)))
+        return out
 
     def wide_centres(self):
         """Centres the last SW/Tersoff force pass sent to the dense second pass."""

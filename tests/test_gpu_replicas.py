@@ -86,18 +86,27 @@ def test_replicas_match_single_boxes(omdg_lib, ensemble):
 
 
 def test_replica_trajectories_match_single_boxes(omdg_lib, ensemble):
+    """Also the per-replica rebuilds: a replica is re-listed exactly when it
+    would be running alone (one of its own atoms moved past skin/2), so its
+    build count equals its single box's."""
     e = ensemble
+    nrep = len(e["natoms"])
     with batch_context(omdg_lib, e) as b:
         b.step(50)
         xb = b.get_state()["x"]
+        builds = b.replica_builds(nrep)
+    alone = []
     for r, (sl, ctx) in enumerate(single_contexts(omdg_lib, e)):
         with ctx:
             ctx.step(50)
             x1 = ctx.get_state()["x"]
+            alone.append(ctx.stats()["rebuilds"])
         L = np.asarray(e["hi"][r]) - np.asarray(e["lo"][r])
         dx = xb[sl] - x1
         dx[:, :2] -= np.round(dx[:, :2] / L[:2]) * L[:2]
         assert np.abs(dx).max() < 1e-5, r
+    assert list(builds) == alone
+    assert len(set(alone)) > 1  # the replicas rebuild at their own rates
 
 
 def test_state_upload_between_steps(omdg_lib, ensemble):
@@ -124,3 +133,18 @@ def test_state_upload_between_steps(omdg_lib, ensemble):
         dx = xa[sl] - xb[sl]
         dx[:, :2] -= np.round(dx[:, :2] / L[:2]) * L[:2]
         assert np.abs(dx).max() < 1e-5
+
+
+def test_persistent_tersoff_pass_is_the_same(omdg_lib, ensemble):
+    """The Tersoff register pass as one resident grid striding over the
+    flattened atoms of every replica gives the same forces bit for bit."""
+    e = ensemble
+    out = []
+    for persistent in (0, 1):
+        with batch_context(omdg_lib, e) as b:
+            b.set_launch("tb_persistent", persistent)
+            b.step(10)
+            st = b.get_state()
+            out.append((st["x"], st["f"], st["pot"]))
+    for a, b_ in zip(*out):
+        assert np.array_equal(a, b_)

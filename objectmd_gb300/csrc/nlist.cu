@@ -197,11 +197,16 @@ constexpr int CELL_SORT_MAX = 1024;
 // registers by an odd-even transposition network (fully unrolled).
 constexpr int CELL_SORT_SMALL = 8;
 
+// Cells too large for it go to a queue (big[0] of them, cells from big[1])
+// that k_cell_sort_warp then drains, so that the warps do not walk every
+// cell of a sparse grid.
 __global__ void k_cell_sort_small(int m, const int* __restrict__ start, int* __restrict__ perm,
-                                  const int* __restrict__ cell_rep, const int* __restrict__ rflag) {
+                                  const int* __restrict__ cell_rep, const int* __restrict__ rflag,
+                                  int* __restrict__ big) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m || !rep_on(rflag, cell_rep, c)) return;
     const int b = start[c], k = start[c + 1] - b;
+    if (k > CELL_SORT_SMALL) big[1 + atomicAdd(big, 1)] = c;
     if (k <= 1 || k > CELL_SORT_SMALL) return;
     int v[CELL_SORT_SMALL];
 #pragma unroll
@@ -228,10 +233,13 @@ __global__ void k_cell_sort_small(int m, const int* __restrict__ start, int* __r
 // pathological cell beyond CELL_SORT_MAX is left unsorted (its order is then
 // not reproducible) rather than sorted in O(k^2).
 __global__ void k_cell_sort_warp(int m, const int* __restrict__ start, int* __restrict__ perm, int skip,
-                                 const int* __restrict__ cell_rep, const int* __restrict__ rflag) {
+                                 const int* __restrict__ cell_rep, const int* __restrict__ rflag,
+                                 const int* __restrict__ big) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += warps) {
+    const int total = big ? big[0] : m;  // queued cells, or every cell
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += warps) {
+        const int c = big ? big[1 + w] : w;
         if (!rep_on(rflag, cell_rep, c)) continue;  // uniform over the warp
         const int b = start[c], k = start[c + 1] - b;
         if (k <= skip) continue;  // empty, single, or sorted by k_cell_sort_small
@@ -865,10 +873,12 @@ __global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildParams 
 constexpr int REV_LANES = 4;
 
 __global__ void k_reverse(int n, int hshift, int maxnb, const unsigned* __restrict__ nbr,
-                          const int* __restrict__ nnb, int* __restrict__ rev, unsigned* status) {
+                          const int* __restrict__ nnb, int* __restrict__ rev, unsigned* status,
+                          const int* __restrict__ rep_of, const int* __restrict__ rflag) {
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const int i = (int)(t / REV_LANES), lane = (int)(t % REV_LANES);
     if (i >= n) return;
+    if (rflag && !rflag[rep_of[i]]) return;  // the replica kept its rows, and so their reverse slots
     int m = nnb[i];
     for (int s = lane; s < m; s += REV_LANES) {
         unsigned e = nbr[nbr_at(i, s, hshift, maxnb)];
@@ -1109,12 +1119,15 @@ int nlist_build(Context* c) {
     // sparse grids (a few atoms per cell) sort most cells a thread each;
     // dense ones (EAM: ~20 atoms per cell) leave every cell to the warps
     const bool sparse = n < 8 * m;
+    int* big = nullptr;  // the queue of cells for the warps: the cell_fill array, free again after the scatter
     if (sparse) {
-        k_cell_sort_small<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->perm, c->d_cell_rep, rflag);
-        c->launches++;
+        big = c->cell_fill;
+        k_zero_ints<<<1, 32, 0, s>>>(1, big, big);
+        k_cell_sort_small<<<grid_for(m, 256), 256, 0, s>>>(m, c->cell_start, c->perm, c->d_cell_rep, rflag, big);
+        c->launches += 2;
     }
     k_cell_sort_warp<<<std::min(grid_for(m, 8), 16 * c->num_sms), 256, 0, s>>>(
-        m, c->cell_start, c->perm, sparse ? CELL_SORT_SMALL : 1, c->d_cell_rep, rflag);
+        m, c->cell_start, c->perm, sparse ? CELL_SORT_SMALL : 1, c->d_cell_rep, rflag, big);
     c->launches += 7;
     AtomArrays cur{c->x, c->y, c->z, c->vx, c->vy, c->vz, c->type, c->id, c->aflag, c->extra, c->extra_n};
     AtomArrays stg{c->stage_d, c->stage_d + c->cap, c->stage_d + 2 * (size_t)c->cap, c->stage_d + 3 * (size_t)c->cap,
@@ -1201,19 +1214,20 @@ int nlist_build(Context* c) {
         k_halt_on_overflow<<<1, 1, 0, s>>>(c->d_status, step_state_halted(c));
         c->launches++;
     }
-    if (reps) {
-        k_rep_build_done<<<grid_for(c->nrep, 256), 256, 0, s>>>(c->nrep, rflag ? 0 : 1, c->d_rep_flag,
-                                                                 c->d_rep_builds);
-        c->launches++;
-    }
+
     prof_end(c);
     if (c->need_rev) {
         prof_begin(c, "nlist_reverse");
         k_reverse<<<grid_for(n, 128 / REV_LANES), 128, 0, s>>>(n, c->nbr_hshift, c->maxnb,
                                                    reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->rev,
-                                                   c->d_status);
+                                                   c->d_status, c->d_rep_of, rflag);
         c->launches++;
         prof_end(c);
+    }
+    if (reps) {
+        k_rep_build_done<<<grid_for(c->nrep, 256), 256, 0, s>>>(c->nrep, rflag ? 0 : 1, c->d_rep_flag,
+                                                                 c->d_rep_builds);
+        c->launches++;
     }
     c->rebuilds++;
     c->list_valid = true;

@@ -405,6 +405,8 @@ def run_gpu(args):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     st0 = ctx.stats()
+    nrep = len(w["ensemble"]["natoms"]) if w["kind"] == "impact" and "ensemble" in w else 0
+    rb0 = ctx.replica_builds(nrep) if nrep else None
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -422,6 +424,13 @@ def run_gpu(args):
     t_wall1 = time.perf_counter()
     clk = clocks.stop()
     st1 = ctx.stats()
+    replica_rebuilds = None
+    if nrep:
+        rb = ctx.replica_builds(nrep) - rb0
+        replica_rebuilds = {"replicas": nrep, "replica_builds_in_timed_steps": int(rb.sum()),
+                            "mean_replicas_rebuilt_per_step": round(float(rb.sum()) / args.steps, 2),
+                            "atoms_rebuilt_per_step": round(float((rb * np.asarray(w["ensemble"]["natoms"])).sum())
+                                                            / args.steps, 1)}
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = slowest_rank_ms(sum(step_ms), world, torch, "cuda")
     value = world * n * args.steps / (total_ms * 1e-3)
@@ -483,6 +492,7 @@ def run_gpu(args):
                 ("diamond" if BASIS[w["kind"]] == 8 else "FCC"),
         "config": {"workload": desc, "atoms_per_gpu": n, "mean_neighbours": round(nf, 2),
                    "neighbour_rebuilds_in_timed_steps": rebuilds,
+                   "replica_rebuilds": replica_rebuilds,
                    "l2": "flushed before every step (%d MB write, then read back so the write-back of its dirty "
                          "lines falls outside the step)" % args.flush_mb, "parallelism": "replicas only" if world > 1 else "single GPU",
                    "launch_shapes": ctx.launch_shapes()},

@@ -1356,7 +1356,10 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         if ((rc = build_list(c))) return rc;
         if ((rc = threebody_prepare(c))) return rc;
     }
-    if (c->async_steps == 0) c->launches_at_sync = c->launches;
+    if (c->async_steps == 0) {
+        c->launches_at_sync = c->launches;
+        cudaMemsetAsync(c->d_flags + 6, 0, sizeof(int), c->stream);  // the batch's first rebuild snapshots
+    }
     if (c->profiling) {
         for (int k = 0; k < nsteps; k++) {
             if (c->ttm && ttm_active(c) && (rc = ttm_pre(c))) return rc;
@@ -1392,10 +1395,10 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
 namespace omdg {
 
 // A neighbour row overflowed in a rebuild of the queued steps.  Every later
-// rebuild was skipped, so the snapshot holds the input of that rebuild (the
-// state after the step's first half-kick and drift).  Restore it, grow the
-// rows, redo the rebuild and the rest of that step, then replay the steps
-// still owed.  The counting sort and the list are deterministic functions of
+// rebuild was skipped; the snapshot holds the input of the queued steps'
+// first rebuild (the state after that step's first half-kick and drift), at
+// or before the one that overflowed.  Restore it, grow the rows, redo that
+// rebuild and the rest of its step, then replay the steps still owed.  The counting sort and the list are deterministic functions of
 // that state, so the trajectory is the one an ample capacity gives, bit for
 // bit.  (The two-temperature model keeps electron state outside the
 // snapshot; a run with it reports the overflow instead.)
@@ -1553,7 +1556,10 @@ int omdg_step_io(omdg_ctx* c, const double* x_in, const double* v_in, int nsteps
         gs.io_valid = false;
         if ((rc = capture_step(c, gs, key))) return rc;
     }
-    if (c->async_steps == 0) c->launches_at_sync = c->launches;
+    if (c->async_steps == 0) {
+        c->launches_at_sync = c->launches;
+        cudaMemsetAsync(c->d_flags + 6, 0, sizeof(int), c->stream);
+    }
     cudaError_t e = cudaGraphLaunch(gs.io_exec, c->stream);
     if (e != cudaSuccess) return check_cuda(c, e, "graph launch");
     c->graph_steps += 1;

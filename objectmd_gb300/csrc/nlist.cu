@@ -302,9 +302,13 @@ __global__ void k_permute_gather(int n, const int* __restrict__ perm, AtomArrays
 // The state a rebuild reorders, copied before the rebuild of a step (unless
 // an earlier rebuild of the queued steps overflowed: then the copy of that
 // rebuild's input is kept), with the step state.
-__global__ void k_snapshot(int n, const int* __restrict__ halted, AtomArrays a, AtomArrays snap,
-                           const unsigned char* __restrict__ st, unsigned char* __restrict__ st_snap, int st_bytes) {
-    if (*halted) return;
+// Only the first rebuild of the queued steps takes it (taken is cleared when
+// a new batch of steps starts and set after the copy): a recovery restores
+// that earlier state and replays from there, which reaches the same state.
+__global__ void k_snapshot(int n, const int* __restrict__ halted, const int* __restrict__ taken, AtomArrays a,
+                           AtomArrays snap, const unsigned char* __restrict__ st, unsigned char* __restrict__ st_snap,
+                           int st_bytes) {
+    if (*halted || *taken) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < st_bytes) st_snap[k] = st[k];
     if (k >= n) return;
@@ -318,6 +322,8 @@ __global__ void k_snapshot(int n, const int* __restrict__ halted, AtomArrays a, 
     snap.id[k] = a.id[k];
     snap.flag[k] = a.flag[k];
 }
+
+__global__ void k_set_one(int* p) { *p = 1; }
 
 // An overflowed build halts the queued steps' later rebuilds.
 __global__ void k_halt_on_overflow(const unsigned* __restrict__ status, int* halted) {
@@ -1089,10 +1095,12 @@ int nlist_build(Context* c) {
                         c->snap_d + 4 * (size_t)c->cap, c->snap_d + 5 * (size_t)c->cap, c->snap_i,
                         c->snap_i + c->cap, reinterpret_cast<unsigned*>(c->snap_i + 2 * (size_t)c->cap), nullptr, 0};
         const int sb = (int)step_state_bytes();
+        int* taken = c->d_flags + 6;
         k_snapshot<<<grid_for(std::max(n, sb), 256), 256, 0, s>>>(
-            n, step_state_halted(c), cur0, snap, static_cast<const unsigned char*>(c->d_state),
+            n, step_state_halted(c), taken, cur0, snap, static_cast<const unsigned char*>(c->d_state),
             static_cast<unsigned char*>(c->snap_state), sb);
-        c->launches++;
+        k_set_one<<<1, 1, 0, s>>>(taken);
+        c->launches += 2;
     }
     // a partial build (replica mode, inside a step): only the replicas whose
     // atoms moved past skin/2 are re-sorted and re-listed; every replica keeps

@@ -357,6 +357,31 @@ def fdtd_case():
     print("wrote fdtd_cases")
 
 
+def example_case():
+    """The reference's example system (test/example/example.cpp) run by the
+    reference (oracle/ref/example_fixture.cpp): the state after FirstRun,
+    atoms 0 and 10 and the energies after every step, the final state."""
+    import subprocess
+
+    for name in ("eam.platinum", "def.platinum"):
+        dst = os.path.join(TABLES, name)
+        shutil.copyfile(os.path.join(REF, "tables", name), dst)
+        os.chmod(dst, 0o644)
+    work = tempfile.mkdtemp(prefix="omdex_")
+    env = dict(os.environ, OMD_TABLE=TABLES)
+    subprocess.run([os.path.join(ROOT, "oracle", "_ref", "example_fixture")], cwd=work, env=env, check=True,
+                   capture_output=True)
+    start = np.loadtxt(os.path.join(work, "start.txt"))
+    end = np.loadtxt(os.path.join(work, "end.txt"))
+    box = np.loadtxt(os.path.join(work, "box.txt"))
+    steps = np.loadtxt(os.path.join(work, "steps.txt"))
+    np.savez_compressed(os.path.join(GOLD, "example_pt_fcc111.npz"), x0=start[:, :3], v0=start[:, 3:],
+                        box_lo=box[:3], box_hi=box[3:6], dt=box[6], base_potential=box[7],
+                        traj0=steps[:, 0:3], traj10=steps[:, 3:6], kinetic=steps[:, 6], potential=steps[:, 7],
+                        x_end=end[:, :3], v_end=end[:, 3:])
+    print("wrote example_pt_fcc111", len(start), "atoms", len(steps), "steps")
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not REF:
@@ -383,6 +408,9 @@ def main(only=None):
         return
     if only == "fdtd":
         fdtd_case()
+        return
+    if only == "example":
+        example_case()
         return
     if only == "lj4000":
         lj4000_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
@@ -470,6 +498,7 @@ def main(only=None):
     output_case(tdir)
     thermo_case(tdir)
     fdtd_case()
+    example_case()
     print("done")
 
 

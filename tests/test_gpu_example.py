@@ -1,0 +1,50 @@
+"""The reference's example application (test/example/example.cpp: FCC "111"
+platinum, 30 x 20 x 10, 100 K, EAM platinum, free boundaries, 0.2 ps of 1 fs
+steps) through the C ABI the GPU integrator calls, against the reference's
+own run of that system (tests/golden/example_pt_fcc111.npz, made by
+oracle/ref/example_fixture.cpp with MDIntegrator): the same state after
+FirstRun, then 200 steps.  Atoms 0 and 10 (the example's traj.dat) after
+every step within 1e-5 A, kinetic energy within 1e-6 and potential energy
+within 1e-7 relative every step, and every atom's final position within
+1e-5 A (FP32 forces with compensated sums against the reference's FP64).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import TABLES
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "example_pt_fcc111.npz")
+
+
+def test_example_system_matches_the_reference_run(omdg_lib):
+    from objectmd_gb300 import inputs
+
+    d = np.load(GOLD)
+    steps = len(d["kinetic"])
+    with omdg_lib.Context(0) as ctx:
+        ctx.set_box(d["box_lo"], d["box_hi"], (False, False, False))
+        ctx.set_atoms(d["x0"], d["v0"], masses=[inputs.md_mass("platinum")], znum=[78.0])
+        ctx.add_eam(os.path.join(TABLES, "eam.platinum"))
+        ctx.set_neighbor(0.3, 0)
+        ctx.set_timestep(float(d["dt"]))
+        ctx.set_first_step_mode(True)  # FirstRun's forces are zeroed (system.cpp:860-873)
+        t0, t10, kin, pot = [], [], [], []
+        for _ in range(steps):
+            ctx.step(1)
+            st = ctx.get_state()
+            t0.append(st["x"][0])
+            t10.append(st["x"][10])
+            led = ctx.ledger()
+            kin.append(led["kinetic"])
+            pot.append(led["potential"])
+        assert abs(ctx.ledger()["base_potential"] - float(d["base_potential"])) < 1e-7 * abs(float(d["base_potential"]))
+        xe = ctx.get_state()["x"]
+    assert np.abs(np.array(t0) - d["traj0"]).max() < 1e-5
+    assert np.abs(np.array(t10) - d["traj10"]).max() < 1e-5
+    np.testing.assert_allclose(kin, d["kinetic"], rtol=1e-6)
+    np.testing.assert_allclose(pot, d["potential"], rtol=1e-7)
+    assert np.abs(xe - d["x_end"]).max() < 1e-5

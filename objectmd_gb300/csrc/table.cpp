@@ -11,9 +11,11 @@
 
 namespace omdg {
 
-// treader.cpp:83-136 and param.cpp:106-136 (read_pseudo): collect the
-// '#$NAME key value' tokens up to the '#$NAME --' line, then read
-// NumberOfData values after it.
+// treader.cpp:83-136 and param.cpp:106-136 (read_pseudo): every token after
+// '#$NAME' on its lines goes into one flat list, up to the '#$NAME --' line;
+// a key's value is the token after its first occurrence (param.cpp:165-171,
+// 218-223), so a line such as '#$EDENS eldens Spacing 1e-3' still gives
+// Spacing.  Then NumberOfData values follow the '--' line.
 int table_load(const std::string& file, const std::string& name, HostTable& t, std::string& err) {
     std::ifstream fl(file.c_str());
     if (!fl.good()) {
@@ -21,35 +23,51 @@ int table_load(const std::string& file, const std::string& name, HostTable& t, s
         return OMDG_EFILE;
     }
     std::string tag = "#$" + name;
-    std::map<std::string, std::vector<std::string>> meta;
+    std::vector<std::string> spar;
     std::string line;
     bool found = false;
     while (std::getline(fl, line)) {
         std::istringstream ss(line);
-        std::string s, key;
-        ss >> s >> key;
+        std::string s, tok;
+        ss >> s >> tok;
         if (s != tag) continue;
-        if (key == "--") {
+        if (tok == "--") {
             found = true;
             break;
         }
-        std::vector<std::string> vals;
-        std::string v;
-        while (ss >> v) vals.push_back(v);
-        meta[key] = vals;
+        if (!tok.empty()) spar.push_back(tok);
+        while (ss >> tok) spar.push_back(tok);
     }
     if (!found) {
         err = "can not find table " + name + "@" + file;
         return OMDG_EFILE;
     }
+    auto exists = [&](const char* k) {
+        for (const std::string& v : spar)
+            if (v == k) return true;
+        return false;
+    };
+    // the token after the key's first occurrence (ParamHandler::double_value)
+    auto value_of = [&](const char* k, std::string& out) -> bool {
+        for (size_t i = 0; i < spar.size(); i++)
+            if (spar[i] == k) {
+                if (i + 1 >= spar.size()) return false;
+                out = spar[i + 1];
+                return true;
+            }
+        return false;
+    };
     auto num = [&](const char* k, double def, bool required, double& out) -> bool {
-        auto it = meta.find(k);
-        if (it == meta.end() || it->second.empty()) {
+        std::string v;
+        if (!value_of(k, v)) {
             if (required) return false;
             out = def;
             return true;
         }
-        out = std::strtod(it->second[0].c_str(), nullptr);
+        std::istringstream vs(v);  // as_double (omdtool.cpp:98-104)
+        if (v == "inf") out = 1.79769313486231570815e+308;
+        else if (v == "-inf") out = -1.79769313486231570815e+308;
+        else if (!(vs >> out)) return false;
         return true;
     };
     double nd = 0, dr = 0, off = 0;
@@ -64,17 +82,17 @@ int table_load(const std::string& file, const std::string& name, HostTable& t, s
     t.dr = dr;
     t.off = off;
     t.rmult = false;
-    auto fit = meta.find("Format");
-    if (fit != meta.end() && !fit->second.empty()) {
-        if (fit->second[0] == "RMULT") t.rmult = true;
-        else if (fit->second[0] != "PLAIN") {
-            err = "unsupported format " + fit->second[0];
+    std::string fmt;
+    if (value_of("Format", fmt)) {
+        if (fmt == "RMULT") t.rmult = true;
+        else if (fmt != "PLAIN") {
+            err = "unsupported format " + fmt;
             return OMDG_EFILE;
         }
     }
-    t.allow_lo = meta.count("OutOfRangeLower") > 0;
-    t.allow_hi = meta.count("OutOfRangeUpper") > 0;
-    t.has_constant = meta.count("Constant") > 0;
+    t.allow_lo = exists("OutOfRangeLower");
+    t.allow_hi = exists("OutOfRangeUpper");
+    t.has_constant = exists("Constant");
     num("Constant", 0.0, false, t.constant);
     num("OutOfRangeLower", 0.0, false, t.out_lo);
     num("OutOfRangeUpper", 0.0, false, t.out_hi);

@@ -129,13 +129,15 @@ def _ip(a):
 def parse_table(path: str, name: str = "") -> dict:
     """Read one ``#$NAME``-tagged section of an Object-MD table file.
 
-    Follows TableReader::open_omd (treader.cpp:83-136): the pseudo tags
-    ``#$<name> key value`` give NumberOfData, Spacing, Offset (default 0),
-    Format (PLAIN|RMULT), OutOfRangeLower/Upper; the values follow the line
-    ``#$<name> --``.
+    Follows TableReader::open_omd (treader.cpp:83-136) and read_pseudo
+    (param.cpp:106-136): every token after ``#$<name>`` on its lines goes into
+    one flat list up to the line ``#$<name> --``; a key's value is the token
+    after its first occurrence (param.cpp:165-171, 218-223).  Keys:
+    NumberOfData, Spacing, Offset (default 0), Format (PLAIN|RMULT),
+    OutOfRangeLower/Upper; the values follow the ``--`` line.
     """
     tag = "#$" + name
-    meta = {}
+    spar = []
     values = []
     with open(path) as fh:
         lines = fh.read().split("\n")
@@ -146,24 +148,31 @@ def parse_table(path: str, name: str = "") -> dict:
             if tok[1] == "--":
                 start = k + 1
                 break
-            meta[tok[1]] = tok[2:]
+            spar.extend(tok[1:])
+
+    def value(key, default=None):
+        for i, t in enumerate(spar):
+            if t == key:
+                return spar[i + 1] if i + 1 < len(spar) else default
+        return default
+
     if start is None:
         raise ValueError("can not find table %s@%s" % (name, path))
-    n = int(meta["NumberOfData"][0])
+    n = int(value("NumberOfData"))
     toks = " ".join(lines[start:]).split()
     values = np.array([float(t) for t in toks[:n]], dtype=np.float64)
     if len(values) != n:
         raise ValueError("short table %s@%s" % (name, path))
-    fmt = meta.get("Format", ["PLAIN"])[0]
+    fmt = value("Format", "PLAIN")
     return {
         "n": n,
-        "dr": float(meta["Spacing"][0]),
-        "off": float(meta.get("Offset", ["0"])[0]),
+        "dr": float(value("Spacing")),
+        "off": float(value("Offset", "0")),
         "rmult": 1 if fmt == "RMULT" else 0,
-        "allow_lo": "OutOfRangeLower" in meta,
-        "allow_hi": "OutOfRangeUpper" in meta,
-        "out_lo": float(meta.get("OutOfRangeLower", ["0"])[0]),
-        "out_hi": float(meta.get("OutOfRangeUpper", ["0"])[0]),
+        "allow_lo": "OutOfRangeLower" in spar,
+        "allow_hi": "OutOfRangeUpper" in spar,
+        "out_lo": float(value("OutOfRangeLower", "0")),
+        "out_hi": float(value("OutOfRangeUpper", "0")),
         "values": values,
     }
 

@@ -442,7 +442,7 @@ __global__ void k_pack(int n, const double* __restrict__ x, const double* __rest
                 // list takes it, and outside the band's max |u|
                 loc[i] = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
             } else {
-                loc[i] = make_float4(ux, uy, uz, 0.f);
+                loc[i] = make_float4(ux, uy, uz, __int_as_float(type[i]));  // w: the type, for the row's type mask
                 m = fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
                 if (!(m <= 3.0e38f)) m = 3.0e38f;  // non-finite: flagged by the cell assignment
             }
@@ -553,7 +553,7 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
                                           const double* __restrict__ z, const int* __restrict__ cell,
                                           const int* __restrict__ start, const unsigned* __restrict__ umax,
                                           unsigned* __restrict__ nbr, int* __restrict__ nnb, unsigned* status,
-                                          int* need) {
+                                          int* need, unsigned* __restrict__ nbmask) {
     // band: per component |error| <= 3 ulp(2 max(|u|, h)) (two operand
     // roundings, the offset, the difference); 2x margin, then sqrt(3) for
     // the length and 1e-6 relative for the squares
@@ -564,8 +564,10 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
     const float4 ui = loc[i];
     if (ui.x == 3.0e38f) {  // inactive centre (k_pack): an empty row
         nnb[i] = 0;
+        nbmask[i] = 0u;
         return;
     }
+    unsigned tmask = 0u;  // types the row holds
     const int nx = g.nc(0), ny = g.nc(1), nz = g.nc(2);
     const int ci = cell[i] - g.cell_base();
     const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
@@ -608,6 +610,7 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
                         !exact_within(g.L64(0), g.L64(1), g.L64(2), p.rsq, x, y, z, i, k, code))
                         continue;
                     if (r2 < 1e-6f) report_overlap(status, i, k);
+                    tmask |= 1u << (__float_as_int(uk.w) & 31);
                     if (cnt < p.maxnb) nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
                     cnt++;
                 }
@@ -620,6 +623,7 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
         cnt = p.maxnb;
     }
     nnb[i] = cnt;
+    nbmask[i] = tmask;
 }
 
 // REP: the atom's replica supplies the grid, reference points and lengths.
@@ -630,14 +634,15 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const RepGeom* __r
                                                const double* __restrict__ z, const int* __restrict__ cell,
                                                const int* __restrict__ start, const unsigned* __restrict__ umax,
                                                unsigned* __restrict__ nbr, int* __restrict__ nnb, unsigned* status,
-                                               int* need, const int* __restrict__ rflag) {
+                                               int* need, const int* __restrict__ rflag,
+                                               unsigned* __restrict__ nbmask) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     if (REP && rflag && !rflag[rep_of[i]]) return;  // the replica keeps its list
     if (REP)
-        build_row(p, RepGrid{rg + rep_of[i]}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need);
+        build_row(p, RepGrid{rg + rep_of[i]}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need, nbmask);
     else
-        build_row(p, BoxGrid{p}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need);
+        build_row(p, BoxGrid{p}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need, nbmask);
 }
 
 // ------------------------------------------------------------------ replicas
@@ -1189,15 +1194,18 @@ int nlist_build(Context* c) {
     prof_begin(c, "nlist_build");
     int combos = 1;
     for (int d = 0; d < 3; d++) combos *= (g.periodic[d] && g.nc[d] < 3) ? 3 * g.nc[d] : 3;
+    // the cell-local builds also write each row's type mask
+    c->nbmask_valid = reps || c->flags_used || !(c->build_lanes == 0 && combos <= 64 && !sparse) &&
+                                                   c->build_lanes != 8 && c->build_lanes != 4;
     if (reps) {
         k_build<true><<<grid_for(n, 128), 128, 0, s>>>(bp, rg, c->d_rep_of, c->loc, c->x, c->y, c->z, cell_sorted,
                                                        c->cell_start, umax, reinterpret_cast<unsigned*>(c->nbr),
-                                                       c->nnb, c->d_status, c->d_flags + 1, rflag);
+                                                       c->nnb, c->d_status, c->d_flags + 1, rflag, c->nbmask);
     } else if (c->flags_used) {  // only the cell-local build skips inactive atoms
         k_build<false><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
                                                         cell_sorted, c->cell_start, umax,
                                                         reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
-                                                        c->d_flags + 1, nullptr);
+                                                        c->d_flags + 1, nullptr, c->nbmask);
     } else if (c->build_lanes == 0 && combos <= 64 && !sparse) {  // a cell CTA wants >= 8 atoms per cell
         const int cap = 1024;  // staged candidates per chunk (32 bytes each)
         k_build_cells<<<m, BUILD_CELL_THREADS, cap * 2 * sizeof(float4), s>>>(
@@ -1215,7 +1223,7 @@ int nlist_build(Context* c) {
         k_build<false><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
                                                         cell_sorted, c->cell_start, umax,
                                                         reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,
-                                                        c->d_flags + 1, nullptr);
+                                                        c->d_flags + 1, nullptr, c->nbmask);
     }
     c->launches++;
     if (c->build_in_step) {

@@ -165,7 +165,9 @@ struct Context {
     float *pe = nullptr, *vir = nullptr;
     PosPack* pack = nullptr;
     float4* xref = nullptr;   // pack-frame position at the last build (FP32)
-    float4* loc = nullptr;    // position relative to its cell's corner at the last build (FP32)
+    float4* loc = nullptr;    // position relative to its cell's corner at the last build (FP32); w = the type
+    unsigned* nbmask = nullptr;  // per atom: bit t set when its row holds an atom of type t (cell-local build)
+    bool nbmask_valid = false;   // the last build wrote nbmask
     int* type = nullptr;
     int* id = nullptr;        // caller index of sorted atom
     int* inv = nullptr;       // sorted index of caller atom

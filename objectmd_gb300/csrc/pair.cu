@@ -45,9 +45,12 @@ __global__ void __launch_bounds__(512) k_pair32(PairParams p, const PosPack* __r
                                                 const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                 float* __restrict__ fx, float* __restrict__ fy,
                                                 float* __restrict__ fz, float* __restrict__ pe,
-                                                float* __restrict__ vir, unsigned* status) {
+                                                float* __restrict__ vir, unsigned* status,
+                                                const unsigned* __restrict__ nbmask) {
     const int lane = threadIdx.x & (LANES - 1);
     const int per_block = blockDim.x / LANES;
+    // a typed pair: the partner type(s) a centre of each type looks for
+    const unsigned want_a = 1u << (p.tb & 31), want_b = 1u << (p.ta & 31);
     for (int base = blockIdx.x * per_block; base < p.n; base += gridDim.x * per_block) {
         int i = base + threadIdx.x / LANES;
         bool valid = i < p.n;
@@ -56,6 +59,10 @@ __global__ void __launch_bounds__(512) k_pair32(PairParams p, const PosPack* __r
         int ti = pack_type(pi.hi);
         const ShiftF L = p.rep_L ? p.rep_L[p.rep_of[ii]] : p.L;
         bool any = valid && (p.all_types || ti == p.ta || ti == p.tb);
+        // with the rows' type masks, a row without the partner type is skipped
+        // whole (most rows of a mixed system: a Si atom with no Ar near)
+        if (any && !p.all_types && nbmask)
+            any = (nbmask[ii] & ((ti == p.ta ? want_a : 0u) | (ti == p.tb ? want_b : 0u))) != 0u;
         int m = any ? nnb[ii] : 0;
         Kahan ax, ay, az, ae;
         float av = 0.f;
@@ -177,7 +184,7 @@ static void launch32(Context* c, const PairParams& p, int block) {
     int per_block = block / LANES;
     k_pair32<LANES><<<grid_for(c->n, per_block), block, 0, c->stream>>>(
         p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->fx, c->fy, c->fz, c->pe, c->vir,
-        c->d_status);
+        c->d_status, c->nbmask_valid ? c->nbmask : nullptr);
 }
 
 int pair_launch(Context* c, Potential& pot, bool first) {

@@ -69,8 +69,8 @@ WORKLOADS = {
                        ncell=40, a=5.431, sigma=0.03, temp=1000.0, dt=0.001, seeds=(4, 5)),
     "impact_256": dict(kind="impact", desc="impact ensemble: 256 Si diamond slabs of 1,000-16,000 atoms (log-uniform, "
                        "1.30M atoms), periodic x/y, free surface, 300 K, one Ar at 10-500 eV each; Tersoff + the reference's "
-                       "Ar-Si ZBL table (zero past 3.2 A), skin 0.5 A, dt 0.5 fs; all replicas in one context", ncell=0, a=5.431, sigma=0.03,
-                       temp=300.0, dt=0.0005, seeds=(6, 6), skin=0.5),
+                       "Ar-Si ZBL table (zero past 3.2 A), skin 0.3 A (per-replica rebuilds), dt 0.5 fs; all replicas "
+                       "in one context", ncell=0, a=5.431, sigma=0.03, temp=300.0, dt=0.0005, seeds=(6, 6), skin=0.3),
     "lj_ar_4000": dict(kind="lj", desc="LJ Ar FCC 10^3 = 4000 atoms, FP64, rc 2.5 sigma, skin 0.3, 100 K, dt 1 fs",
                        ncell=10, a=5.26, sigma=0.0, temp=100.0, dt=0.001, seeds=(1, 1)),
 }

@@ -9,7 +9,7 @@ forces.  Fitting runs on the
 GPU through omdg_nn_train: descriptors, forward and backward passes, the
 force-loss double backward and Adam are the library's own kernels.  Defaults:
 the descriptors of switch_descriptors() (cutoff switched over Tersoff's own
-[R - D, R + D]), 1000 epochs, batches of 16 configurations, Adam with the
+[R - D, R + D]), 200 epochs, batches of 16 configurations, Adam with the
 learning rate decaying from 1e-3 to 1e-5 (cosine), loss = per-atom energy MSE
 + force MSE.
 
@@ -164,7 +164,7 @@ def tersoff_snapshot(ncell=8, temp=1000.0, steps=1000, seed=41, device=0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nconf", type=int, default=2000)
-    ap.add_argument("--epochs", type=int, default=1000)
+    ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--lr-final", type=float, default=1e-5)

@@ -4,9 +4,9 @@ training gains over the same network untrained.
 
 Force RMSE against Tersoff on a 1000 K cell equilibrated by Tersoff MD: below
 the 0.030 eV/A goal (the committed model, whose descriptor cutoff switches
-over Tersoff's own [R - D, R + D], measures 0.023 eV/A at 1000 K, 0.0046 at
-300 K and 0.049 at 1700 K on 4096-atom cells on a GB300), at least ten times
-below the untrained network's.
+over Tersoff's own [R - D, R + D], measures 0.025 eV/A at 1000 K, 0.006 at
+300 K and 0.056 at 1700 K on 4096-atom cells on a GB300; 200 epochs), at
+least ten times below the untrained network's.
 """
 import numpy as np
 import pytest

@@ -321,6 +321,39 @@ def timed_steps(ctx, n, steps, stream, flush_l2, torch):
     return total_ms, kernels, st1["rebuilds"] - st0["rebuilds"], st1["launches"] - st0["launches"]
 
 
+FDTD_CELL_BYTES = 53  # k_fd_solve: T, con, cap, S, E (8 B each), map 4, mask 1 read; A 8 written
+
+
+def fdtd_report(device, torch, n=256, steps=100):
+    """The finite-difference heat solver (omdg_fdtd) on an n^3 periodic grid
+    with a hot block: cells/s over `steps` host-driven steps (wall clock,
+    synchronised), and the stencil's HBM roof (53 algorithmic bytes per
+    cell; the grid, 1.3 GB of arrays at n = 256, is ten times the L2)."""
+    from objectmd_gb300 import omdg
+
+    dim = n ** 3
+    with omdg.FDTD(n, n, n, "a pppppp", "a" * dim, device=device) as g:
+        g.set_spacestep(1.0)
+        g.set_timestep(0.05)
+        g.set_cell("* 300 @ %d,%d,%d,%d,%d,%d=2000" % (n // 3, n // 3, n // 3, n // 2, n // 2, n // 2))
+        g.step(3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.step(steps)
+        t1 = time.perf_counter()
+        a = g.vector()
+    sec = (t1 - t0) / steps
+    peaks = load_peaks()
+    gbs = FDTD_CELL_BYTES * dim / sec / 1e9
+    return {"workload": "finite-difference heat solver %d^3 = %d cells, periodic, FP64" % (n, dim),
+            "cells_per_s": dim / sec, "ms_per_step": sec * 1e3, "steps": steps,
+            "timing": "wall clock over host-driven omdg_fdtd_step calls (one kernel each)",
+            "roofline": {"bound": "hbm", "kernel": "fd_solve", "achieved": round(gbs, 1), "peak": peaks["hbm"],
+                         "unit": "GB/s", "frac": round(gbs / peaks["hbm"], 4),
+                         "alg_bytes_per_cell": FDTD_CELL_BYTES},
+            "field_range": [float(a.min()), float(a.max())]}
+
+
 def sub_workload(name, args, device, torch, flush_l2):
     """Another configured workload, measured as the main one (device-timed
     atom-steps/s, per-kernel times, HBM and issue roofs, one-core CPU
@@ -519,6 +552,7 @@ def run_gpu(args):
         for name in ("tersoff_si_512k", "nn_si_512k"):
             subs[name] = sub_workload(name, args, device, torch, flush_l2)
         out["workloads"] = subs
+        out["fdtd"] = fdtd_report(device, torch)
         nn, ts = subs["nn_si_512k"], subs["tersoff_si_512k"]
         out["surrogate"] = {"nn_atom_steps_per_s": nn["value"], "tersoff_atom_steps_per_s": ts["value"],
                             "nn_over_tersoff": nn["value"] / ts["value"],

@@ -14,8 +14,9 @@
 // The FP64 operations are the reference's, in its order, without
 // contraction (explicit _rn intrinsics): results are bit-identical to the
 // reference built with -ffp-contract=off.  HBM-bound: 8 B of the old vector,
-// 8 B con, 8 B cap, 8 B S, 8 B E, 4 B map and 1 B mask read, 8 B written
-// and 8 B of E cleared per cell; the six neighbours' T and con come from L1/L2.
+// 8 B con, 8 B cap, 8 B S, 8 B E, 4 B map and 1 B mask read and 8 B written
+// per cell (53 B; E and S are cleared only where not zero); the six
+// neighbours' T and con come from L1/L2.
 //
 // Host side (the string path of FDTDSolver, fdtd.cpp:100-118, 506-597): the
 // symbol map, the map, and the assignment strings "<symbols> <value>[:t0[:t1]]"
@@ -55,6 +56,7 @@ FDDev fd_dev(const FDGrid* g) {
     p.E = g->dE;
     p.mask_first = p.mask_later = nullptr;
     p.solves = p.active = nullptr;
+    p.keep_S = 0;
     return p;
 }
 
@@ -93,9 +95,12 @@ __global__ void __launch_bounds__(FD_BLOCK) k_fd_solve(FDDev p, const double* __
         }
     }
     // A = T + (2 A h2inv + S + E) dt / cap (fdtd.cpp:664)
-    const double q = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(2.0, acc), p.h2inv), p.S[idx]), p.E[idx]);
+    const double si = p.S[idx], ei = p.E[idx];
+    const double q = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(2.0, acc), p.h2inv), si), ei);
     A[idx] = __dadd_rn(ti, __ddiv_rn(__dmul_rn(q, p.dt), p.cap[idx]));
-    p.E[idx] = 0.0;
+    // E[i] = S[i] = 0 (fdtd.cpp:665), written only where not zero already
+    if (ei != 0.0) p.E[idx] = 0.0;
+    if (!p.keep_S && si != 0.0) p.S[idx] = 0.0;
 }
 
 int fd_solve(FDGrid* g, cudaStream_t s) {
@@ -217,7 +222,7 @@ static void check_expression(std::string& str, int& t0, int& t1, bool& isequ) {
 // AssignArray(ptr, str) (fdtd.cpp:528-592): tokens outside their time range
 // are dropped from str, ranged ones in range are kept (an unranged token is
 // kept for good).
-static int assign_array(FDGrid* g, std::vector<double>& a, std::string& str) {
+static int assign_array(FDGrid* g, std::vector<double>& a, std::string& str, bool& changed) {
     if (str.empty()) return OMDG_OK;
     std::istringstream ss(str);
     str.clear();
@@ -249,6 +254,7 @@ static int assign_array(FDGrid* g, std::vector<double>& a, std::string& str) {
                                        "," + std::to_string(j) + "," + std::to_string(k) + ")");
                 double dv;
                 if (!to_double(v, dv)) return fd_fail(g, OMDG_EINVAL, "conversion error: " + v);
+                if (!(a[idx] == dv) || std::signbit(a[idx]) != std::signbit(dv)) changed = true;
                 a[idx] = dv;
                 return OMDG_OK;
             };
@@ -273,6 +279,7 @@ static int assign_array(FDGrid* g, std::vector<double>& a, std::string& str) {
                             const char sym = (m < 0 || m >= (int)g->bound.size()) ? '.' : g->bound[m].sym;
                             if (c == '*' || sym == c) {
                                 if (!ok) return fd_fail(g, OMDG_EINVAL, "conversion error: " + val);
+                                if (!(a[idx] == dv) || std::signbit(a[idx]) != std::signbit(dv)) changed = true;
                                 a[idx] = dv;
                             }
                         }
@@ -281,25 +288,35 @@ static int assign_array(FDGrid* g, std::vector<double>& a, std::string& str) {
     return OMDG_OK;
 }
 
-int fd_sync_data(FDGrid* g) {
-    int rc = assign_array(g, g->hS, g->str_src);
-    if (!rc) rc = assign_array(g, g->hcon, g->str_con);
-    if (!rc) rc = assign_array(g, g->hcap, g->str_cap);
+// assignments to S: the device S is zero after every solve, so any value
+// written since makes the host image the one to upload
+static int assign_source(FDGrid* g, std::string& str) {
+    bool changed = false;
+    const int rc = assign_array(g, g->hS, str, changed);
+    if (changed) g->dirty_S = g->s_any = true;
     return rc;
 }
 
-static cudaError_t upload_if(double* d, const std::vector<double>& h, std::vector<double>& img, cudaStream_t s) {
-    if (h == img) return cudaSuccess;
-    img = h;
-    // the image is the copy's source: it stays unchanged until the next upload
-    return cudaMemcpyAsync(d, img.data(), sizeof(double) * img.size(), cudaMemcpyHostToDevice, s);
+int fd_sync_data(FDGrid* g) {
+    bool ccon = false, ccap = false;
+    int rc = assign_source(g, g->str_src);
+    if (!rc) rc = assign_array(g, g->hcon, g->str_con, ccon);
+    if (!rc) rc = assign_array(g, g->hcap, g->str_cap, ccap);
+    g->dirty_con |= ccon;
+    g->dirty_cap |= ccap;
+    return rc;
 }
 
+// Host images that changed since the last upload go to the device
+// (stream-ordered; the copy is staged before the call returns).
 int fd_upload(FDGrid* g, cudaStream_t s) {
-    cudaError_t e = upload_if(g->dS, g->hS, g->imgS, s);
-    if (e == cudaSuccess) e = upload_if(g->dcon, g->hcon, g->imgcon, s);
-    if (e == cudaSuccess) e = upload_if(g->dcap, g->hcap, g->imgcap, s);
+    const size_t b = sizeof(double) * g->dim;
+    cudaError_t e = cudaSuccess;
+    if (g->dirty_S) e = cudaMemcpyAsync(g->dS, g->hS.data(), b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && g->dirty_con) e = cudaMemcpyAsync(g->dcon, g->hcon.data(), b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && g->dirty_cap) e = cudaMemcpyAsync(g->dcap, g->hcap.data(), b, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return fd_fail(g, OMDG_ECUDA, std::string("fdtd upload: ") + cudaGetErrorString(e));
+    g->dirty_S = g->dirty_con = g->dirty_cap = false;
     return OMDG_OK;
 }
 
@@ -418,7 +435,8 @@ int omdg_fdtd_assign(omdg_fdtd* g, int which, const char* str) {
     int rc = OMDG_OK;
     if (which == 0) {
         if ((rc = fd_download_A(g))) return rc;
-        if ((rc = assign_array(g, g->hA, s))) return rc;
+        bool changed = false;
+        if ((rc = assign_array(g, g->hA, s, changed))) return rc;
         cudaError_t e = cudaMemcpyAsync(g->dA[g->cur], g->hA.data(), sizeof(double) * g->dim,
                                         cudaMemcpyHostToDevice, g->stream);
         if (e != cudaSuccess) return fd_fail(g, OMDG_ECUDA, std::string("fdtd: ") + cudaGetErrorString(e));
@@ -427,9 +445,13 @@ int omdg_fdtd_assign(omdg_fdtd* g, int which, const char* str) {
     // SetSource / SetConductivity / SetCapacity keep the whole string and
     // apply a copy of it now (fdtd.hpp:126-133)
     std::string& kept = which == 1 ? g->str_src : (which == 2 ? g->str_con : g->str_cap);
-    std::vector<double>& a = which == 1 ? g->hS : (which == 2 ? g->hcon : g->hcap);
     kept = str;
-    return assign_array(g, a, s);
+    if (which == 1) return assign_source(g, s);
+    bool changed = false;
+    rc = assign_array(g, which == 2 ? g->hcon : g->hcap, s, changed);
+    if (which == 2) g->dirty_con |= changed;
+    else g->dirty_cap |= changed;
+    return rc;
 }
 
 // Step(n) (fdtd.cpp:671-689), single rank: per step sync_data, Solve, step++.
@@ -442,7 +464,10 @@ int omdg_fdtd_step(omdg_fdtd* g, int n) {
         if (!rc) rc = fd_upload(g, g->stream);
         if (!rc) rc = fd_solve(g, g->stream);
         if (rc) return rc;
-        std::fill(g->hS.begin(), g->hS.end(), 0.0);  // Solve clears S (fdtd.cpp:666)
+        if (g->s_any) {  // Solve clears S (fdtd.cpp:665), on the device too
+            std::fill(g->hS.begin(), g->hS.end(), 0.0);
+            g->s_any = false;
+        }
         g->step += 1;
     }
     return fd_sync(g);

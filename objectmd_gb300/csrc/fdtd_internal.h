@@ -33,8 +33,9 @@ struct FDDev {
     const uint8_t* mask;
     const double* con;
     const double* cap;
-    const double* S;
+    double* S;
     double* E;
+    int keep_S;  // coupled: S is the kept strings' fixed pattern, not cleared by the solve
     // coupled to the atoms (a replayed step graph): the mask chosen on the
     // device from the solve count, and the step skipped while the model is
     // not active; null for host-driven steps
@@ -59,7 +60,8 @@ struct FDGrid {
     int solves = 0;
     std::string str_src, str_con, str_cap;  // assignment strings kept for sync_data
     std::vector<double> hA, hS, hcon, hcap; // host images of the assigned arrays
-    std::vector<double> imgS, imgcon, imgcap;  // S, con and cap as last uploaded
+    bool dirty_S = true, dirty_con = true, dirty_cap = true;  // the host image changed since the last upload
+    bool s_any = false;                  // hS holds a non-zero value (cleared after each solve)
     double* dA[2] = {nullptr, nullptr};
     int cur = 0;                         // dA[cur] holds the cell vector
     double *dS = nullptr, *dE = nullptr, *dcon = nullptr, *dcap = nullptr;

@@ -590,6 +590,7 @@ int ttm_pre(Context* c) {
         q.fd.mask_later = fg->dmask[1];
         q.fd.solves = t.dev_ctr;
         q.fd.active = t.dev_ctr + 1;
+        q.fd.keep_S = 1;  // the unranged source tokens would assign the same pattern every step
         q.A = fg->dA[0];
         q.T = fg->dA[1];
         q.cap = fg->dcap;

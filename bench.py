@@ -78,12 +78,14 @@ WORKLOADS = {
 # Algorithmic bytes per atom for one launch of each kernel (neighbour list of
 # N_f int32 entries, FP32 packs/forces, FP64 x and v):
 #   eam_density  24 (own position) + 4 N_f (list) + 4 (F' write)
-#   eam_force    24 + 4 N_f + 4 (F'_i) + 12 (f) + 4 (energy)
+#   eam_force    24 + 4 N_f + 4 (F'_i) + 12 (f) + 4 (energy); with the step's
+#                second half-kick in its epilogue (eam_force_kick) + 48 (v)
 #   kick_drift   read x v f, write x v + 32 B position pack
 #   kick         read v f, write v
 ALG_BYTES = {
     "eam_density": lambda nf: 24 + 4 * nf + 4,
     "eam_force": lambda nf: 24 + 4 * nf + 4 + 12 + 4,
+    "eam_force_kick": lambda nf: 24 + 4 * nf + 4 + 12 + 4 + 48,  # + v read and written by the fused half-kick
     "tersoff_centre": lambda nf: 24 + 4 * nf + 4,
     "nn_descriptors": lambda nf: 24 + 4 * nf + 128,
     "nn_force": lambda nf: 24 + 4 * nf + 128 + 4 + 16,

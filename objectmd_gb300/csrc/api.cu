@@ -219,7 +219,8 @@ static int alloc_atoms(Context* c, int n) {
               dalloc(c->fp, cap) && dalloc(c->femb, cap) && dalloc(c->cell, cap) && dalloc(c->perm, cap) &&
               dalloc(c->stage_d, (size_t)6 * cap) && dalloc(c->stage_i, (size_t)3 * cap) && dalloc(c->aflag, cap) &&
               dalloc(c->cell_sorted, cap) && dalloc(c->nnb, cap) && dalloc(c->ters_wide, (size_t)cap + 1);
-    int nb = grid_for(cap, RED_BLOCK) + 1;
+    // block partials: the kick's blocks, or a force kernel's with the kick in its epilogue (>= 8 atoms a block)
+    int nb = grid_for(cap, 8) + 1;
     ok = ok && dalloc(c->d_red, (size_t)4 * nb);
     ok = ok && dalloc(c->snap_d, (size_t)6 * cap) && dalloc(c->snap_i, (size_t)3 * cap);
     if (ok && !c->snap_state) ok = cudaMalloc(&c->snap_state, step_state_bytes()) == cudaSuccess;
@@ -926,6 +927,7 @@ static int build_list(Context* c) {
 
 int forces_compute(Context* c) {
     if (c->pots.empty()) return set_error(c, OMDG_ESTATE, "no force kernel");
+    c->kick_fused = false;
     bool first = true;
     for (auto& p : c->pots) {
         if (p.fallback_only) continue;  // run by the potential that owns it
@@ -1035,7 +1037,9 @@ static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr)
     }
     l2 = c->launches;
     if (!rc && io) rc = branch(0, io[0], nullptr, nullptr);
+    c->fuse_kick = true;
     if (!rc) rc = forces_compute(c);
+    c->fuse_kick = false;
     if (!rc && io) rc = branch(1, nullptr, nullptr, io[2]);
     if (!rc) rc = integrate_kick(c, 0);
     if (!rc && c->ttm) rc = thermo_detect(c, true);  // ExecuteDetectors (system.cpp:976)
@@ -1371,7 +1375,10 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
             rc = eager_maybe_rebuild(c);
             c->build_in_step = false;
             if (rc) return rc;
-            if ((rc = forces_compute(c))) return rc;
+            c->fuse_kick = true;
+            rc = forces_compute(c);
+            c->fuse_kick = false;
+            if (rc) return rc;
             if ((rc = integrate_kick(c, k))) return rc;
             if (c->ttm && (rc = thermo_detect(c, true))) return rc;
         }
@@ -1438,7 +1445,10 @@ static int recover_overflow(omdg_ctx* c) {
     invalidate_graph(c);
     if ((rc = build_list(c))) return rc;
     if ((rc = threebody_prepare(c))) return rc;
-    if ((rc = forces_compute(c))) return rc;
+    c->fuse_kick = true;
+    rc = forces_compute(c);
+    c->fuse_kick = false;
+    if (rc) return rc;
     if ((rc = integrate_kick(c, 0))) return rc;
     if ((rc = check_status(c))) return rc;
     c->overflow_recoveries++;
@@ -1831,6 +1841,7 @@ static int* launch_knob(Context* c, const std::string& k) {
     if (k == "tb_block") return &c->tb_block;
     if (k == "tb_lanes") return &c->tb_lanes;
     if (k == "tb_persistent") return &c->tb_persistent;
+    if (k == "fuse_kick") return &c->fuse_kick_on;
     if (k == "nbr_hshift") return &c->nbr_hshift;
     if (k == "build_lanes") return &c->build_lanes;
     if (k == "io_blocks") return &c->io_blocks;
@@ -1844,7 +1855,7 @@ static bool valid_knob(const std::string& k, int v) {
     if (k == "eam_block" || k == "pair_block" || k == "tb_block") return v >= 32 && v <= 1024 && v % 32 == 0;
     if (k == "nbr_hshift") return v >= 0 && v <= 5;
     if (k == "eam_ctas_per_sm") return v >= 1 && v <= 32;
-    if (k == "eam_stage" || k == "tb_persistent") return v == 0 || v == 1;
+    if (k == "eam_stage" || k == "tb_persistent" || k == "fuse_kick") return v == 0 || v == 1;
     if (k == "build_lanes") return v == 0 || v == 1 || v == 4 || v == 8;
     if (k == "io_blocks") return v >= 1 && v <= 65535;
     if (k == "nbr_capacity") return v >= 0 && v <= 4096;

@@ -12,7 +12,7 @@
 //   - the knot index is clamped instead of branched (r <= rc keeps it below
 //     n-1; the reference's x == n-1 rule selects the same segment),
 //   - forces use Kahan sums, the per-pair energy and virial plain FP32 sums.
-#include "device_common.cuh"
+#include "integrate_dev.cuh"
 
 namespace omdg {
 
@@ -172,13 +172,28 @@ __global__ void __launch_bounds__(256, 4) k_eamf_density(EAMFast p, PosPack* pac
     }
 }
 
-template <int LANES, bool STAGED>
+// KICK: the step's second half-kick and its ledger in the epilogue (the
+// force is final here: one potential, no force modifies), as k_kick does it.
+template <int LANES, bool STAGED, bool KICK>
 __global__ void __launch_bounds__(256, 4) k_eamf_force(EAMFast p, const PosPack* __restrict__ pack,
                                                        const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                        const float* __restrict__ femb, float* __restrict__ fx,
                                                        float* __restrict__ fy, float* __restrict__ fz,
                                                        float* __restrict__ pe, float* __restrict__ vir,
-                                                       unsigned* status) {
+                                                       unsigned* status, KickArgs ka, double* __restrict__ vx,
+                                                       double* __restrict__ vy, double* __restrict__ vz,
+                                                       const unsigned* __restrict__ aflag, double* __restrict__ ledger) {
+    // the kick's ledger terms of each thread wait in shared memory, not in
+    // registers held across the neighbour loop
+    // (one slot per atom of the block: lane 0 of each atom's lanes)
+    constexpr int KS = KICK ? 256 / LANES : 1;
+    __shared__ F2 s_kk[KS], s_ke[KS], s_kw[KS];
+    __shared__ unsigned long long s_kv[KS];
+    const int kslot = threadIdx.x / LANES;
+    if (KICK && (threadIdx.x & (LANES - 1)) == 0) {
+        s_kk[kslot] = s_ke[kslot] = s_kw[kslot] = F2{0.f, 0.f};
+        s_kv[kslot] = 0ull;
+    }
     constexpr int PF = Prefetch<LANES>::N;
     __shared__ float4 s_hi[64], s_lo[64];
     extern __shared__ float4 s_tab[];  // (phi, rho) knot pairs [k0, k0+ns)
@@ -279,26 +294,55 @@ __global__ void __launch_bounds__(256, 4) k_eamf_force(EAMFast p, const PosPack*
                 pe[i] += ve;
                 vir[i] += av;
             }
+            // inactive atoms: not integrated, not measured (system.cpp:1067, :1085)
+            if (KICK && (!aflag || (aflag[i] & 1u))) {
+                F2 kk = s_kk[kslot], ke = s_ke[kslot], kw = s_kw[kslot];
+                unsigned long long kv = s_kv[kslot];
+                // one type on this path; the finalising block changes hdtm only after every block read it
+                kick_atom_terms(ka.p, i, 0, vfx, vfy, vfz, ve, av, ka.st->hdtm[0], vx, vy, vz, kk, ke, kw, kv);
+                s_kk[kslot] = kk;
+                s_ke[kslot] = ke;
+                s_kw[kslot] = kw;
+                s_kv[kslot] = kv;
+            }
         }
+    }
+    if (KICK) {
+        const bool own = (threadIdx.x & (LANES - 1)) == 0;
+        const F2 z = {0.f, 0.f};
+        ledger_block(ka.p, ka.f, own ? s_kk[kslot] : z, own ? s_ke[kslot] : z, own ? s_kw[kslot] : z,
+                     own ? s_kv[kslot] : 0ull, ka.partial, ledger, ka.st);
     }
 }
 
 template <int LANES, bool STAGED>
-static void launch_fast(Context* c, const EAMFast& p, int grid, int block, size_t smem1, size_t smem2) {
+static void launch_fast(Context* c, const EAMFast& p, int grid, int block, size_t smem1, size_t smem2,
+                        const KickArgs* ka) {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_eamf_density<LANES, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_eamf_force<LANES, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_eamf_force<LANES, STAGED, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
+        cudaFuncSetAttribute(k_eamf_force<LANES, STAGED, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
         attr = true;
     }
     prof_begin(c, "eam_density");
     k_eamf_density<LANES, STAGED><<<grid, block, smem1, c->stream>>>(
         p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->fp, c->femb, c->d_status);
     prof_end(c);
-    prof_begin(c, "eam_force");
-    k_eamf_force<LANES, STAGED><<<grid, block, smem2, c->stream>>>(
-        p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->femb, c->fx, c->fy, c->fz, c->pe, c->vir,
-        c->d_status);
+    const unsigned* aflag = c->flags_used ? c->aflag : nullptr;
+    if (ka) {
+        prof_begin(c, "eam_force_kick");
+        k_eamf_force<LANES, STAGED, true><<<grid, block, smem2, c->stream>>>(
+            p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->femb, c->fx, c->fy, c->fz, c->pe,
+            c->vir, c->d_status, *ka, c->vx, c->vy, c->vz, aflag, c->d_ledger);
+    } else {
+        prof_begin(c, "eam_force");
+        k_eamf_force<LANES, STAGED, false><<<grid, block, smem2, c->stream>>>(
+            p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->femb, c->fx, c->fy, c->fz, c->pe,
+            c->vir, c->d_status, KickArgs{}, nullptr, nullptr, nullptr, nullptr, nullptr);
+    }
     prof_end(c);
 }
 
@@ -360,9 +404,21 @@ int eam_fast_launch(Context* c, Potential& pot, bool first) {
     }
     size_t smem1 = (size_t)ns * sizeof(float4), smem2 = 2 * smem1;
     bool st = ns > 0;
+    // the step's second half-kick in the force epilogue: one potential, the
+    // first, and a block of whole warps (the ledger's block tree)
+    KickArgs ka;
+    const KickArgs* kap = nullptr;
+    if (c->fuse_kick && c->fuse_kick_on && first && c->pots.size() == 1 && kick_fusable(c) && block % 32 == 0 &&
+        (block & (block - 1)) == 0) {
+        kick_args(c, ka);
+        if (grid <= ka.partial_cap) {
+            kap = &ka;
+            c->kick_fused = true;
+        }
+    }
 #define OMDG_EAMF(L)                                                 \
-    (st ? launch_fast<L, true>(c, p, grid, block, smem1, smem2)      \
-        : launch_fast<L, false>(c, p, grid, block, smem1, smem2))
+    (st ? launch_fast<L, true>(c, p, grid, block, smem1, smem2, kap) \
+        : launch_fast<L, false>(c, p, grid, block, smem1, smem2, kap))
     switch (lanes) {
         case 1: OMDG_EAMF(1); break;
         case 2: OMDG_EAMF(2); break;

@@ -17,40 +17,9 @@
 // the bit patterns, the pack refresh and the sums use FP32 pairs.
 #include <vector>
 
-#include "device_common.cuh"
+#include "integrate_dev.cuh"
 
 namespace omdg {
-
-struct StepState {
-    long long step;      // RunKernel Step (system.cpp:979)
-    int row;             // ledger row within the current omdg_step call
-    int rebuild;         // rebuild request for the next list build
-    double lambda;       // velocity factor to apply before the next kick
-    int rebuild_every;   // >0: rebuild when step % rebuild_every == 0
-    int nrebuild;        // list builds taken by the graph's conditional node
-    double dt;               // TimeStep (DynamicTimeStep changes it here, between steps)
-    double hdtm[MAX_TYPES];  // (dt/2) / m per type, refreshed with dt
-    double elapsed;          // ElapsedTime (system.cpp:979)
-    double sqrmaxv;          // SqrMaxVelocity of the last measurement (system.cpp:1075-1094)
-    int src_first;           // EnergySource: the first call inside the window only arms it
-    int src_scale;           // EnergySource: scale velocities at the next PreIntegration
-    int halted;              // a rebuild overflowed its rows: later rebuilds are skipped until omdg_sync recovers
-    int rebuild_all;         // replica mode: the request covers every replica (periodic rebuild, state upload)
-};
-
-struct IntParams {
-    int n;
-    double org[3], P[3];
-    float half_skin2;       // (skin/2)^2
-    int use_f64;
-    double Q[3];            // P - org: the pack coordinate is X = x + Q
-    float Qh[3], Ql[3];     // Q as an FP32 pair (pack_coord)
-    float mh[MAX_TYPES], ml[MAX_TYPES];  // mass per type as an FP32 pair
-    int range_on;                        // RangeLimiter (RangeLimiter.h:33-54)
-    unsigned range_group;                // group bits it acts on
-    double range_lo[3], range_hi[3];     // box -/+ border
-    int need_vmax;                       // measure SqrMaxVelocity (DynamicTimeStep)
-};
 
 __global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
                                                     double* __restrict__ z, double* __restrict__ vx,
@@ -137,140 +106,6 @@ __global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __re
 }
 
 
-struct FinParams {
-    int natoms;
-    int ledger_cap;
-    int count_step;       // 1: this is a RunKernel step (advance Step)
-    const int* ghosts;    // reference compatibility: periodic images added to the atom count (or null)
-    unsigned* status;     // ERR_NONFINITE when a total is NaN or infinite
-    unsigned* ticket;     // blocks done (the last one resets it)
-    double tau, tset;     // thermostat (tau <= 0: off)
-    double temp_factor;   // 2/3/k_B (unit.h:66-104)
-    int need_vmax;        // SqrMaxVelocity from the block partials
-    int dyn_update;       // DynamicTimeStep period (0: off; DynamicTimeStep.h:58-70)
-    int dyn_apply;        // this measurement precedes a step's PreIntegration
-    double dyn_maxpath, dyn_maxdt;
-    double mass[MAX_TYPES];
-    int src_on;                 // EnergySource (EnergySource.h:103-133)
-    double src_start, src_stop;
-};
-
-// Block partials: sum m v^2, sum potential, sum virial as FP32 pairs, and
-// the block's largest squared speed as the bit pattern of a non-negative
-// double (integer order is value order): two float4 per block.
-struct BlockPartial {
-    float4 ke, wv;  // (k.hi, k.lo, e.hi, e.lo), (w.hi, w.lo, vmax bits low, high)
-};
-
-__device__ __forceinline__ unsigned long long vmax_bits(const float4& wv) {
-    return ((unsigned long long)__float_as_uint(wv.w) << 32) | __float_as_uint(wv.z);
-}
-
-// Ledger row, thermostat factor and step counter from the block partials
-// (one block; each thread sums a contiguous run of partials, then a fixed
-// xor tree per warp and over the warps, all on FP32 pairs; FP64 only for
-// the totals).  Partials are read through L2: other blocks wrote them.
-__device__ void finalize_block(const FinParams& p, int nblocks, const BlockPartial* partial, double* ledger,
-                               StepState* st) {
-    __shared__ F2 sk[RED_BLOCK / 32], se[RED_BLOCK / 32], sw[RED_BLOCK / 32];
-    __shared__ unsigned long long sv[RED_BLOCK / 32];
-    F2 kf = {0.f, 0.f}, ef = {0.f, 0.f}, wf = {0.f, 0.f};
-    unsigned long long vb = 0ull;
-    const int per = (nblocks + RED_BLOCK - 1) / RED_BLOCK;
-    const int b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
-#pragma unroll 4
-    for (int b = b0; b < b1; b++) {
-        const float4 ke = __ldcg(&partial[b].ke), wv = __ldcg(&partial[b].wv);
-        kf = f2_add(kf, F2{ke.x, ke.y});
-        ef = f2_add(ef, F2{ke.z, ke.w});
-        wf = f2_add(wf, F2{wv.x, wv.y});
-        if (p.need_vmax) vb = max(vb, vmax_bits(wv));
-    }
-    // fixed xor tree within each warp, then over the warps in warp 0
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int o = 16; o > 0; o >>= 1) {
-        kf = f2_add(kf, f2_shfl_xor(kf, o));
-        ef = f2_add(ef, f2_shfl_xor(ef, o));
-        wf = f2_add(wf, f2_shfl_xor(wf, o));
-        if (p.need_vmax) vb = max(vb, __shfl_xor_sync(0xffffffffu, vb, o));
-    }
-    if (lane == 0) {
-        sk[warp] = kf;
-        se[warp] = ef;
-        sw[warp] = wf;
-        sv[warp] = vb;
-    }
-    __syncthreads();
-    if (warp != 0) return;
-    const F2 z = {0.f, 0.f};
-    kf = lane < RED_BLOCK / 32 ? sk[lane] : z;
-    ef = lane < RED_BLOCK / 32 ? se[lane] : z;
-    wf = lane < RED_BLOCK / 32 ? sw[lane] : z;
-    vb = lane < RED_BLOCK / 32 ? sv[lane] : 0ull;
-    for (int o = RED_BLOCK / 64; o > 0; o >>= 1) {
-        kf = f2_add(kf, f2_shfl_xor(kf, o));
-        ef = f2_add(ef, f2_shfl_xor(ef, o));
-        wf = f2_add(wf, f2_shfl_xor(wf, o));
-        if (p.need_vmax) vb = max(vb, __shfl_xor_sync(0xffffffffu, vb, o));
-    }
-    const double k = f2_to_double(kf), e = f2_to_double(ef), w = f2_to_double(wf);
-    const double vm = __longlong_as_double((long long)vb);
-    if (threadIdx.x == 0) {
-        double kinetic = 0.5 * k;
-        if (!(isfinite(kinetic) && isfinite(e))) atomicOr(p.status, ERR_NONFINITE);
-        int row = st->row;
-        int slot = row % p.ledger_cap;  // ring buffer between host reads
-        double* row_out = ledger + LEDGER_W * (size_t)slot;
-        row_out[0] = kinetic;
-        row_out[1] = e;
-        row_out[2] = 0.5 * w;
-        row_out[4] = (double)st->step;  // SysMonitor's Step, ElapsedTime and TimeStep of this step
-        row_out[5] = st->elapsed;
-        row_out[6] = st->dt;
-        row_out[7] = 0.0;
-        double lam = 1.0;
-        if (p.count_step && p.tau > 0.0 && st->step != 0) {
-            // TempController::PostIntegration: T from the system kinetic energy
-            const double count = (double)p.natoms + (p.ghosts ? (double)*p.ghosts : 0.0);
-            double T = p.temp_factor * kinetic / count;
-            if (T > 0.0) lam = sqrt(1. + st->dt / p.tau * (p.tset / T - 1.));
-        }
-        row_out[3] = lam;
-        if (p.need_vmax) st->sqrmaxv = vm;
-        if (p.count_step) {
-            st->lambda = lam;
-            st->elapsed += st->dt;  // ElapsedTime += TimeStep; Step++ (system.cpp:979-980)
-            st->step += 1;
-            st->row = row + 1;
-            if (st->rebuild_every > 0 && (st->step % st->rebuild_every) == 0) {
-                st->rebuild = 1;
-                st->rebuild_all = 1;
-            }
-            if (p.src_on) {  // EnergySource::PreIntegration of the next step
-                int scale = 0;
-                if (st->elapsed >= p.src_start) {
-                    if (st->src_first) st->src_first = 0;  // firstcall: return
-                    else scale = st->elapsed < p.src_stop ? 1 : 0;
-                }
-                st->src_scale = scale;
-            }
-        }
-        if (p.dyn_update > 0 && p.dyn_apply && (st->step % p.dyn_update) == 0) {
-            // DynamicTimeStep::PreIntegration of the next step
-            double ndt;
-            if (st->sqrmaxv > 0.0) {
-                ndt = p.dyn_maxpath / (sqrt(st->sqrmaxv) * 1.10);
-                if (ndt > p.dyn_maxdt) ndt = p.dyn_maxdt;
-            } else {
-                ndt = p.dyn_maxdt;
-            }
-            st->dt = ndt;
-            for (int t = 0; t < MAX_TYPES; t++) st->hdtm[t] = p.mass[t] > 0 ? (0.5 * ndt) / p.mass[t] : 0.0;
-        }
-        *p.ticket = 0u;
-    }
-}
-
 // Second half kick v += dt/2 f/m (kick = 1) and the energy ledger: per
 // atom m v^2, the potential and the virial as FP32 pairs, a fixed xor tree
 // per warp and over the warps, FP32-pair block partials; the last block to
@@ -289,74 +124,30 @@ __global__ void __launch_bounds__(RED_BLOCK, 2048 / RED_BLOCK) k_kick(IntParams 
     // inactive atoms: not integrated, not measured (system.cpp:1067, :1085)
     if (i < p.n && (!aflag || (aflag[i] & 1u))) {
         const int t = type[i];
-        double ux = vx[i], uy = vy[i], uz = vz[i];
-        if (kick) {
-            const double h = st->hdtm[t];
-            if (p.use_f64) {
+        if (kick && !p.use_f64) {
+            kick_atom_terms(p, i, t, fx[i], fy[i], fz[i], pe[i], vir[i], st->hdtm[t], vx, vy, vz, k, e, w, vmax);
+        } else {
+            double ux = vx[i], uy = vy[i], uz = vz[i];
+            if (kick) {
+                const double h = st->hdtm[t];
                 ux = fma(f64[3 * (size_t)i], h, ux);
                 uy = fma(f64[3 * (size_t)i + 1], h, uy);
                 uz = fma(f64[3 * (size_t)i + 2], h, uz);
-            } else {
-                ux = fma(f2d_exact(fx[i]), h, ux);
-                uy = fma(f2d_exact(fy[i]), h, uy);
-                uz = fma(f2d_exact(fz[i]), h, uz);
+                vx[i] = ux;
+                vy[i] = uy;
+                vz[i] = uz;
             }
-            vx[i] = ux;
-            vy[i] = uy;
-            vz[i] = uz;
-        }
-        const F2 sx = f2_from(ux), sy = f2_from(uy), sz = f2_from(uz);
-        const F2 v2 = f2_add(f2_add(f2_mul(sx, sx), f2_mul(sy, sy)), f2_mul(sz, sz));
-        k = f2_mul(v2, F2{p.mh[t], p.ml[t]});
-        e = p.use_f64 ? f2_from(f64[3 * (size_t)p.n + i]) : F2{pe[i], 0.f};
-        w = F2{vir[i], 0.f};
-        if (p.need_vmax)  // sqrv = vx*vx + vy*vy + vz*vz (system.cpp:1086)
-            vmax = (unsigned long long)__double_as_longlong(
-                __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz)));
-    }
-    if (p.need_vmax)
-        for (int o = 16; o > 0; o >>= 1) vmax = max(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-    for (int o = 16; o > 0; o >>= 1) {
-        k = f2_add(k, f2_shfl_xor(k, o));
-        e = f2_add(e, f2_shfl_xor(e, o));
-        w = f2_add(w, f2_shfl_xor(w, o));
-    }
-    __shared__ F2 wk[RED_BLOCK / 32], we[RED_BLOCK / 32], ww[RED_BLOCK / 32];
-    __shared__ unsigned long long wv[RED_BLOCK / 32];
-    __shared__ bool last;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) {
-        wk[warp] = k;
-        we[warp] = e;
-        ww[warp] = w;
-        wv[warp] = vmax;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        const F2 z = {0.f, 0.f};
-        k = lane < RED_BLOCK / 32 ? wk[lane] : z;
-        e = lane < RED_BLOCK / 32 ? we[lane] : z;
-        w = lane < RED_BLOCK / 32 ? ww[lane] : z;
-        for (int o = RED_BLOCK / 64; o > 0; o >>= 1) {
-            k = f2_add(k, f2_shfl_xor(k, o));
-            e = f2_add(e, f2_shfl_xor(e, o));
-            w = f2_add(w, f2_shfl_xor(w, o));
-        }
-        if (lane == 0) {
-            unsigned long long bv = 0ull;
-            if (p.need_vmax)
-                for (int q = 0; q < RED_BLOCK / 32; q++) bv = max(bv, wv[q]);
-            partial[blockIdx.x].ke = make_float4(k.hi, k.lo, e.hi, e.lo);
-            partial[blockIdx.x].wv = make_float4(w.hi, w.lo, __uint_as_float((unsigned)bv),
-                                                 __uint_as_float((unsigned)(bv >> 32)));
-            __threadfence();
-            last = atomicAdd(f.ticket, 1u) == gridDim.x - 1;
+            const F2 sx = f2_from(ux), sy = f2_from(uy), sz = f2_from(uz);
+            const F2 v2 = f2_add(f2_add(f2_mul(sx, sx), f2_mul(sy, sy)), f2_mul(sz, sz));
+            k = f2_mul(v2, F2{p.mh[t], p.ml[t]});
+            e = p.use_f64 ? f2_from(f64[3 * (size_t)p.n + i]) : F2{pe[i], 0.f};
+            w = F2{vir[i], 0.f};
+            if (p.need_vmax)  // sqrv = vx*vx + vy*vy + vz*vz (system.cpp:1086)
+                vmax = (unsigned long long)__double_as_longlong(
+                    __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz)));
         }
     }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    finalize_block(f, gridDim.x, partial, ledger, st);
+    ledger_block(p, f, k, e, w, vmax, partial, ledger, st);
 }
 
 struct GhostParams {
@@ -586,9 +377,7 @@ int integrate_kick_drift(Context* c, int) {
     return check_cuda(c, cudaGetLastError(), "kick_drift");
 }
 
-static int reduce_and_finalize(Context* c, int kick, int count_step) {
-    IntParams p = int_params(c);
-    int nb = grid_for(c->n, RED_BLOCK);
+static FinParams fin_params(Context* c, const IntParams& p, int count_step) {
     FinParams f;
     f.natoms = c->n;
     f.ledger_cap = c->ledger_cap;
@@ -608,6 +397,33 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
     f.src_on = c->src_on ? 1 : 0;
     f.src_start = c->src_start;
     f.src_stop = c->src_start + c->src_width;
+    return f;
+}
+
+// A step's second half-kick can ride in the force kernel's epilogue: FP32
+// forces, and no ghost count for the thermostat (its extra launch precedes
+// the kick).
+bool kick_fusable(const Context* c) {
+    return !c->use_f64 && !(c->thermo_count_ghosts && c->thermo_tau > 0.0) && c->post_ops.empty() && !c->ttm &&
+           c->nrep == 0;
+}
+
+void kick_args(Context* c, KickArgs& ka) {
+    ka.p = int_params(c);
+    ka.f = fin_params(c, ka.p, 1);
+    ka.partial = reinterpret_cast<BlockPartial*>(c->d_red);
+    ka.partial_cap = grid_for(std::max(c->cap, c->n), 8) + 1;
+    ka.st = reinterpret_cast<StepState*>(c->d_state);
+}
+
+static int reduce_and_finalize(Context* c, int kick, int count_step) {
+    if (kick && count_step && c->kick_fused) {  // the force kernel's epilogue took it
+        c->kick_fused = false;
+        return OMDG_OK;
+    }
+    IntParams p = int_params(c);
+    int nb = grid_for(c->n, RED_BLOCK);
+    FinParams f = fin_params(c, p, count_step);
     if (c->thermo_count_ghosts && count_step && c->thermo_tau > 0.0) {
         // TempController::GetSystemTemperature divides by GetTotalAtom(), which
         // on MDSystemGrid is GetNAtom(): owners plus their periodic ghost images

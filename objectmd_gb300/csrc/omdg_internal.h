@@ -196,6 +196,8 @@ struct Context {
     int* d_rep_builds = nullptr;         // per replica: list builds so far
     int* d_cell_rep = nullptr;           // replica of each cell (rep_cells)
     bool build_partial = false;          // the build being issued rebuilds only the flagged replicas
+    bool fuse_kick = false;              // the forces being issued are a step's: the kick may join them
+    bool kick_fused = false;             // the last force launch did the step's second half-kick
     int ncell_cap = 0;
     int* scan_partials = nullptr;
     double* stage_d = nullptr;   // permutation staging: 6 FP64 arrays x cap
@@ -261,6 +263,7 @@ struct Context {
     int tb_block = 128;        // three-body kernels
     int tb_lanes = 1;
     int tb_persistent = 0;     // Tersoff register pass: one resident grid striding over the flattened atoms
+    int fuse_kick_on = 1;      // a step's second half-kick in the force kernel's epilogue where it can go
 
     // potentials
     std::vector<Potential> pots;

@@ -817,7 +817,7 @@ class Context:
 
     def launch_shapes(self):
         keys = ("eam_block", "eam_lanes", "eam_stage", "eam_ctas_per_sm", "pair_block", "pair_lanes", "tb_block",
-                "tb_lanes", "tb_persistent", "nbr_hshift", "build_lanes", "io_blocks")
+                "tb_lanes", "tb_persistent", "fuse_kick", "nbr_hshift", "build_lanes", "io_blocks")
         return {k: self.get_launch(k) for k in keys}
 
     def autotune(self, reps=3):

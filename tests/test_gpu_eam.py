@@ -261,3 +261,31 @@ def test_step_io_equals_upload_step_readback(omdg_lib, rebuild_every):
             np.testing.assert_array_equal(ka, kb)
             np.testing.assert_array_equal(pa, pb)
             x_in, v_in = st["x"], st["v"]
+
+
+def test_kick_in_the_force_epilogue_is_the_same_step(omdg_lib):
+    """The step's second half-kick done by the EAM force kernel's epilogue
+    (the default for one EAM potential) against the separate kick kernel:
+    positions, velocities and forces bit for bit after 30 steps with two
+    rebuilds, the ledger to FP32-pair summation order."""
+    from objectmd_gb300 import inputs
+
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=12, a=4.05, sigma=0.05, temp=600.0, seed_pos=71, seed_vel=72)
+    out = []
+    for fuse in (1, 0):
+        with omdg_lib.Context(0) as ctx:
+            ctx.set_box(lo, hi)
+            ctx.set_atoms(x, v, masses=[inputs.md_mass("aluminum")], znum=[13.0])
+            ctx.add_eam(os.path.join(TABLES, "eam.aluminum5000"))
+            ctx.set_neighbor(0.1, 0)
+            ctx.set_timestep(0.002)
+            ctx.set_launch("fuse_kick", fuse)
+            ctx.step(30)
+            kin, pot = ctx.ledger_history()
+            out.append((ctx.get_state(), kin, pot, ctx.stats()["rebuilds"]))
+    (a, ka, pa, ra), (b, kb, pb, rb) = out
+    assert ra == rb and ra >= 2
+    for k in ("x", "v", "f", "pot"):
+        assert np.array_equal(a[k], b[k]), k
+    np.testing.assert_allclose(ka, kb, rtol=1e-6)
+    np.testing.assert_allclose(pa, pb, rtol=1e-7)

@@ -172,8 +172,9 @@ __global__ void __launch_bounds__(256, 4) k_eamf_density(EAMFast p, PosPack* pac
     }
 }
 
-// KICK: the step's second half-kick and its ledger in the epilogue (the
-// force is final here: one potential, no force modifies), as k_kick does it.
+// KICK: the step's second half-kick and its ledger terms in the epilogue (the
+// force is final here: one potential, no force modifies), as k_kick does
+// them, one ledger partial per warp.
 template <int LANES, bool STAGED, bool KICK>
 __global__ void __launch_bounds__(256, 4) k_eamf_force(EAMFast p, const PosPack* __restrict__ pack,
                                                        const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
@@ -308,10 +309,13 @@ __global__ void __launch_bounds__(256, 4) k_eamf_force(EAMFast p, const PosPack*
         }
     }
     if (KICK) {
+        // one partial per warp, no block barrier (a barrier here would hold
+        // every warp's slot until the block's slowest warp is done); a
+        // one-block kernel sums them and writes the ledger row
         const bool own = (threadIdx.x & (LANES - 1)) == 0;
         const F2 z = {0.f, 0.f};
-        ledger_block(ka.p, ka.f, own ? s_kk[kslot] : z, own ? s_ke[kslot] : z, own ? s_kw[kslot] : z,
-                     own ? s_kv[kslot] : 0ull, ka.partial, ledger, ka.st);
+        warp_partial(ka.p, own ? s_kk[kslot] : z, own ? s_ke[kslot] : z, own ? s_kw[kslot] : z,
+                     own ? s_kv[kslot] : 0ull, ka.partial + (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
     }
 }
 
@@ -337,6 +341,7 @@ static void launch_fast(Context* c, const EAMFast& p, int grid, int block, size_
         k_eamf_force<LANES, STAGED, true><<<grid, block, smem2, c->stream>>>(
             p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->femb, c->fx, c->fy, c->fz, c->pe,
             c->vir, c->d_status, *ka, c->vx, c->vy, c->vz, aflag, c->d_ledger);
+        launch_ledger_finalize(c, *ka, grid * (block >> 5));
     } else {
         prof_begin(c, "eam_force");
         k_eamf_force<LANES, STAGED, false><<<grid, block, smem2, c->stream>>>(
@@ -411,7 +416,7 @@ int eam_fast_launch(Context* c, Potential& pot, bool first) {
     if (c->fuse_kick && c->fuse_kick_on && first && c->pots.size() == 1 && kick_fusable(c) && block % 32 == 0 &&
         (block & (block - 1)) == 0) {
         kick_args(c, ka);
-        if (grid <= ka.partial_cap) {
+        if (grid * (block >> 5) <= ka.partial_cap) {  // one partial per warp
             kap = &ka;
             c->kick_fused = true;
         }

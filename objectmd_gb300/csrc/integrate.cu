@@ -416,6 +416,16 @@ void kick_args(Context* c, KickArgs& ka) {
     ka.st = reinterpret_cast<StepState*>(c->d_state);
 }
 
+__global__ void __launch_bounds__(1024) k_ledger_finalize(FinParams f, int nparts, const BlockPartial* partial,
+                                                          double* ledger, StepState* st) {
+    finalize_block(f, nparts, partial, ledger, st);
+}
+
+void launch_ledger_finalize(Context* c, const KickArgs& ka, int nparts) {
+    k_ledger_finalize<<<1, 1024, 0, c->stream>>>(ka.f, nparts, ka.partial, c->d_ledger, ka.st);
+    c->launches++;
+}
+
 static int reduce_and_finalize(Context* c, int kick, int count_step) {
     if (kick && count_step && c->kick_fused) {  // the force kernel's epilogue took it
         c->kick_fused = false;

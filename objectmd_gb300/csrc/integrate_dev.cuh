@@ -250,6 +250,23 @@ __device__ __forceinline__ void ledger_block(const IntParams& p, const FinParams
     finalize_block(f, gridDim.x, partial, ledger, st);
 }
 
+// One warp's ledger partial (the per-warp half of ledger_block): lane 0
+// writes it.
+__device__ __forceinline__ void warp_partial(const IntParams& p, F2 k, F2 e, F2 w, unsigned long long vmax,
+                                             BlockPartial* __restrict__ out) {
+    if (p.need_vmax)
+        for (int o = 16; o > 0; o >>= 1) vmax = max(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    for (int o = 16; o > 0; o >>= 1) {
+        k = f2_add(k, f2_shfl_xor(k, o));
+        e = f2_add(e, f2_shfl_xor(e, o));
+        w = f2_add(w, f2_shfl_xor(w, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        out->ke = make_float4(k.hi, k.lo, e.hi, e.lo);
+        out->wv = make_float4(w.hi, w.lo, __uint_as_float((unsigned)vmax), __uint_as_float((unsigned)(vmax >> 32)));
+    }
+}
+
 // Host: the kick's parameters for a context (integrate.cu).
 struct KickArgs {
     IntParams p;
@@ -261,5 +278,7 @@ struct KickArgs {
 
 bool kick_fusable(const Context* c);
 void kick_args(Context* c, KickArgs& ka);
+// One block sums nparts warp partials in order and writes the step's ledger row.
+void launch_ledger_finalize(Context* c, const KickArgs& ka, int nparts);
 
 }  // namespace omdg

@@ -210,6 +210,16 @@ int omdg_replica_builds(omdg_ctx* ctx, int* builds, int nrep);
 int omdg_wide_centres(omdg_ctx* ctx, int* count);
 
 /*
+ * No reference counterpart (the reference's EAM loops over its half list,
+ * team.cpp:224-237).  The tiles of the last list build for the tiled EAM
+ * passes (blocks of cells whose halo is staged in shared memory), and how
+ * many of them fit the staging capacity (launch key tile_cap; the others
+ * take the gather path).  Both 0 when the last build wrote no tile slots.
+ * Synchronous.
+ */
+int omdg_tile_counts(omdg_ctx* ctx, int* tiles, int* staged);
+
+/*
  * Launch shapes (no reference counterpart: the reference is scalar C++).
  * Keys: "eam_block", "eam_lanes" (threads per atom), "eam_stage" (spline
  * knots in shared memory), "eam_ctas_per_sm", "pair_block", "pair_lanes",

@@ -341,6 +341,7 @@ int omdg_destroy(omdg_ctx* c) {
     cudaFree(c->nbr);
     cudaFree(c->rev);
     cudaFree(c->slot_buf);
+    tile_release(c);
     cudaFree(c->cell_count);
     cudaFree(c->cell_start);
     cudaFree(c->cell_fill);
@@ -876,6 +877,7 @@ namespace omdg {
 static int build_list(Context* c) {
     if (c->pots.empty()) return set_error(c, OMDG_ESTATE, "no force kernel (integrator.cpp:79)");
     nlist_prepare_geometry(c);
+    if (int rt = tile_prepare(c)) return rt;
     if (c->nrep > 0) {
         if (c->rep_start.back() != c->n) return set_error(c, OMDG_ESTATE, "replica atom counts do not sum to n");
         int rc = replica_prepare(c);
@@ -1801,6 +1803,21 @@ int omdg_wide_centres(omdg_ctx* c, int* count) {
     return OMDG_OK;
 }
 
+int omdg_tile_counts(omdg_ctx* c, int* tiles, int* staged) {
+    if (!c || !tiles || !staged) return OMDG_EINVAL;
+    *tiles = 0;
+    *staged = 0;
+    if (!c->tile_valid || !c->tile_nst || c->tile_count == 0) return OMDG_OK;
+    std::vector<int> nst(c->tile_count);
+    cudaError_t e = cudaMemcpyAsync(nst.data(), c->tile_nst, sizeof(int) * nst.size(), cudaMemcpyDeviceToHost,
+                                    c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return check_cuda(c, e, "omdg_tile_counts");
+    *tiles = c->tile_count;
+    for (int v : nst) *staged += v <= c->tile_cap ? 1 : 0;
+    return OMDG_OK;
+}
+
 int omdg_set_profiling(omdg_ctx* c, int on) {
     if (!c) return OMDG_EINVAL;
     c->profiling = on != 0;
@@ -1846,6 +1863,11 @@ static int* launch_knob(Context* c, const std::string& k) {
     if (k == "build_lanes") return &c->build_lanes;
     if (k == "io_blocks") return &c->io_blocks;
     if (k == "nbr_capacity") return &c->nbr_capacity;
+    if (k == "eam_tile") return &c->eam_tile;
+    if (k == "tile_x") return &c->tile_dim[0];
+    if (k == "tile_y") return &c->tile_dim[1];
+    if (k == "tile_z") return &c->tile_dim[2];
+    if (k == "tile_cap") return &c->tile_cap;
     return nullptr;
 }
 
@@ -1859,6 +1881,9 @@ static bool valid_knob(const std::string& k, int v) {
     if (k == "build_lanes") return v == 0 || v == 1 || v == 4 || v == 8;
     if (k == "io_blocks") return v >= 1 && v <= 65535;
     if (k == "nbr_capacity") return v >= 0 && v <= 4096;
+    if (k == "eam_tile") return v == 0 || v == 1;
+    if (k == "tile_x" || k == "tile_y" || k == "tile_z") return v >= 1 && v <= 4;
+    if (k == "tile_cap") return v >= 64 && v <= 5000;
     return false;
 }
 
@@ -1916,7 +1941,10 @@ int omdg_set_launch(omdg_ctx* c, const char* key, int value) {
     if (!valid_knob(k, value)) return set_error(c, OMDG_EINVAL, "invalid value for " + k);
     if (*p == value) return OMDG_OK;
     *p = value;
-    if (k == "build_lanes") c->list_valid = false;
+    // the build writes tile slots for the tile shape and capacity it sees
+    if (k == "build_lanes" || k == "eam_tile" || k == "tile_x" || k == "tile_y" || k == "tile_z" ||
+        k == "tile_cap")
+        c->list_valid = false;
     if (k == "nbr_capacity") {  // applies at the next first build
         c->list_valid = false;
         c->maxnb = 0;
@@ -1960,21 +1988,25 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
         tb |= p.kind == POT_SW || p.kind == POT_TERSOFF;
     }
     struct Cand {
-        int lanes, block, stage;
+        int lanes, block, stage, tile;
     };
     std::vector<Cand> cands;
+    const int tile_on = c->eam_tile;
     if (eam) {
+        // the tiled passes (where they apply), then the gather passes
+        if (tile_on && tiles_apply(c))
+            for (int lanes : {4, 8, 16}) cands.push_back(Cand{lanes, 256, 0, 1});
         for (int lanes : {4, 8, 16})
             for (int block : {128, 256})
-                for (int stage : {0, 1}) cands.push_back(Cand{lanes, block, stage});
+                for (int stage : {0, 1}) cands.push_back(Cand{lanes, block, stage, 0});
     } else if (pair) {
         for (int lanes : {2, 4, 8, 16})
-            for (int block : {128, 256}) cands.push_back(Cand{lanes, block, 0});
+            for (int block : {128, 256}) cands.push_back(Cand{lanes, block, 0, tile_on});
     } else if (tb) {
         // stage: the Tersoff register pass as one resident grid (persistent)
         for (int lanes : {1, 2, 4})
             for (int block : {64, 128, 256})
-                for (int stage : {0, 1}) cands.push_back(Cand{lanes, block, stage});
+                for (int stage : {0, 1}) cands.push_back(Cand{lanes, block, stage, tile_on});
     }
     int rc = OMDG_OK;
     // list build: cell-CTA, 8 or 4 lanes per atom, or one thread per atom
@@ -2011,6 +2043,10 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
             c->eam_block = cd.block;
             c->eam_stage = cd.stage;
             c->eam_ctas_per_sm = cd.block >= 512 ? 2 : 4;
+            if (c->eam_tile != cd.tile) {
+                c->eam_tile = cd.tile;
+                c->list_valid = false;
+            }
         } else if (pair) {
             c->pair_lanes = cd.lanes;
             c->pair_block = cd.block;
@@ -2036,6 +2072,10 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
         c->eam_block = win.block;
         c->eam_stage = win.stage;
         c->eam_ctas_per_sm = win.block >= 512 ? 2 : 4;
+        if (c->eam_tile != win.tile) {
+            c->eam_tile = win.tile;
+            c->list_valid = false;
+        }
     } else if (pair) {
         c->pair_lanes = win.lanes;
         c->pair_block = win.block;

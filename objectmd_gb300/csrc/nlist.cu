@@ -455,7 +455,22 @@ __global__ void k_pack(int n, const double* __restrict__ x, const double* __rest
     }
 }
 
+// EAM cell tiles: besides the list entry, the build writes each entry's
+// slot in the staged halo of its centre's tile (tile t, halo cell h:
+// sb[t HC + h] + the candidate's offset in its cell).  Halo cells run z, y, x
+// from the cell below the tile's first to the one above its last, the order
+// the build visits a row's cells, so slots increase along a row.
+struct TileOut {
+    unsigned short* slot;  // null: no tile output
+    const unsigned short* sb;
+    const int* nst;
+    int T[3], nt[3];
+    int hx, hy;            // halo cells along x, y (T + 2)
+    int HC, stride, cap;
+};
+
 struct BuildParams {
+    TileOut to;
     int n, maxnb, hshift;
     int nc[3];
     int periodic[3];
@@ -571,6 +586,21 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
     const int nx = g.nc(0), ny = g.nc(1), nz = g.nc(2);
     const int ci = cell[i] - g.cell_base();
     const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
+    // tile slots (single box only): the centre's tile, where it is staged
+    const unsigned short* tsb = nullptr;
+    unsigned short* trow = nullptr;
+    int tox = 0, toy = 0, toz = 0;
+    if (p.to.slot) {
+        const int tx = cx / p.to.T[0], ty = cy / p.to.T[1], tz = cz / p.to.T[2];
+        const int t = (tz * p.to.nt[1] + ty) * p.to.nt[0] + tx;
+        if (p.to.nst[t] <= p.to.cap) {
+            tsb = p.to.sb + (size_t)t * p.to.HC;
+            trow = p.to.slot + (size_t)i * p.to.stride;
+            tox = cx - tx * p.to.T[0];
+            toy = cy - ty * p.to.T[1];
+            toz = cz - tz * p.to.T[2];
+        }
+    }
     const float rx = cell_ref(cx, g.h(0), g.base(0)), ry = cell_ref(cy, g.h(1), g.base(1)),
                 rz = cell_ref(cz, g.h(2), g.base(2));
     const int mx = axis_count(nx, g.periodic(0));
@@ -599,6 +629,8 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
                 const int c = g.cell_base() + (kz * ny + ky) * nx + kx;
                 const unsigned code = nbr_encode(0, sx, sy, sz);
                 const int e = start[c + 1];
+                // slot of candidate k in the tile's staged halo: tb + k
+                const int tb = trow ? (int)tsb[((toz + a) * p.to.hy + (toy + b)) * p.to.hx + (tox + q)] - start[c] : 0;
                 for (int k = start[c]; k < e; k++) {
                     const float4 uk = loc[k];
                     const float dx = px - uk.x, dy = py - uk.y, dz = pz - uk.z;
@@ -611,7 +643,10 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
                         continue;
                     if (r2 < 1e-6f) report_overlap(status, i, k);
                     tmask |= 1u << (__float_as_int(uk.w) & 31);
-                    if (cnt < p.maxnb) nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
+                    if (cnt < p.maxnb) {
+                        nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
+                        if (trow) trow[cnt] = (unsigned short)(tb + k);
+                    }
                     cnt++;
                 }
             }
@@ -643,6 +678,81 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const RepGeom* __r
         build_row(p, RepGrid{rg + rep_of[i]}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need, nbmask);
     else
         build_row(p, BoxGrid{p}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need, nbmask);
+}
+
+// ------------------------------------------------------------------ EAM cell tiles
+
+struct TilePrep {
+    int T[3], nt[3], nc[3], periodic[3];
+    int hx, hy, HC;
+    double corg[3], h[3];   // cell grid origin and widths
+    double borg[3], P[3];   // pack frame: X = x - borg + P
+};
+
+// One CTA per tile: the atom count of each halo cell (z, y, x from the cell
+// below the tile's first to the one above its last; a periodic axis wraps,
+// a free axis has no cells beyond the grid), their exclusive scan as each
+// cell's first staged slot (saturating at 65535; such a tile exceeds every
+// capacity), the total, and the tile's lower corner in the pack frame.
+constexpr int TILE_PREP_THREADS = 256;  // >= the 216 halo cells of a 4x4x4 tile
+
+__global__ void __launch_bounds__(TILE_PREP_THREADS) k_tile_prep(TilePrep tp, const int* __restrict__ start,
+                                                                 unsigned short* __restrict__ sb,
+                                                                 int* __restrict__ nst, float4* __restrict__ org) {
+    __shared__ int s_warp[TILE_PREP_THREADS / 32];
+    const int t = blockIdx.x;
+    const int tx = t % tp.nt[0], ty = (t / tp.nt[0]) % tp.nt[1], tz = t / (tp.nt[0] * tp.nt[1]);
+    const int h = threadIdx.x;
+    int cnt = 0;
+    if (h < tp.HC) {
+        const int l[3] = {h % tp.hx, (h / tp.hx) % tp.hy, h / (tp.hx * tp.hy)};
+        const int t3[3] = {tx, ty, tz};
+        int k[3];
+        bool ok = true;
+        for (int d = 0; d < 3; d++) {
+            int gk = t3[d] * tp.T[d] - 1 + l[d];
+            if (tp.periodic[d]) {
+                if (gk < 0) gk += tp.nc[d];
+                else if (gk >= tp.nc[d]) gk -= tp.nc[d];
+            } else if (gk < 0 || gk >= tp.nc[d]) {
+                ok = false;
+            }
+            k[d] = gk;
+        }
+        if (ok) {
+            const int c = (k[2] * tp.nc[1] + k[1]) * tp.nc[0] + k[0];
+            cnt = start[c + 1] - start[c];
+        }
+    }
+    // block exclusive scan
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_warp[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int v = lane < TILE_PREP_THREADS / 32 ? s_warp[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
+        }
+        if (lane < TILE_PREP_THREADS / 32) s_warp[lane] = v;
+    }
+    __syncthreads();
+    const int excl = incl - cnt + (w > 0 ? s_warp[w - 1] : 0);
+    if (h < tp.HC) sb[(size_t)t * tp.HC + h] = (unsigned short)min(excl, 65535);
+    if (h == tp.HC - 1) nst[t] = excl + cnt;
+    if (h == 0) {
+        const int t3[3] = {tx, ty, tz};
+        float o[3];
+        for (int d = 0; d < 3; d++)
+            o[d] = (float)(__dadd_rn(__dsub_rn(fma((double)(t3[d] * tp.T[d]), tp.h[d], tp.corg[d]), tp.borg[d]),
+                                     tp.P[d]));
+        org[t] = make_float4(o[0], o[1], o[2], 0.f);
+    }
 }
 
 // ------------------------------------------------------------------ replicas
@@ -1018,6 +1128,86 @@ int replica_prepare(Context* c) {
     return check_cuda(c, cudaStreamSynchronize(c->stream), "replica tables");
 }
 
+// The tiled EAM passes apply to one box (no replicas) whose periodic axes
+// have at least three cells (the build's 27-cell stencil), with tiles of at
+// most 4 cells a side.
+int tile_prepare(Context* c) {
+    c->tile_want = false;
+    c->tile_valid = false;
+    if (!tiles_apply(c)) return OMDG_OK;
+    const BoxGeom& b = c->box;
+    for (int d = 0; d < 3; d++) {
+        if (b.periodic[d] && b.nc[d] < 3) return OMDG_OK;
+        if (c->tile_dim[d] < 1 || c->tile_dim[d] > 4) return OMDG_OK;
+    }
+    int nt[3], hc = 1;
+    for (int d = 0; d < 3; d++) {
+        nt[d] = (b.nc[d] + c->tile_dim[d] - 1) / c->tile_dim[d];
+        hc *= c->tile_dim[d] + 2;
+    }
+    const int ntiles = nt[0] * nt[1] * nt[2];
+    if ((long long)ntiles * hc > c->tile_alloc || !c->tile_sb) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(c->stream, &cs);
+        if (cs != cudaStreamCaptureStatusNone) return set_error(c, OMDG_ESTATE, "tile grid grew inside a capture");
+        invalidate_graph(c);
+        cudaFree(c->tile_sb);
+        cudaFree(c->tile_nst);
+        cudaFree(c->tile_org);
+        c->tile_sb = nullptr;
+        c->tile_nst = nullptr;
+        c->tile_org = nullptr;
+        c->tile_alloc = 0;
+        if (cudaMalloc(&c->tile_sb, sizeof(unsigned short) * (size_t)ntiles * hc) != cudaSuccess ||
+            cudaMalloc(&c->tile_nst, sizeof(int) * ntiles) != cudaSuccess ||
+            cudaMalloc(&c->tile_org, sizeof(float4) * ntiles) != cudaSuccess)
+            return set_error(c, OMDG_ENOMEM, "tile tables");
+        c->tile_alloc = ntiles * hc;
+    }
+    for (int d = 0; d < 3; d++) c->tile_nt[d] = nt[d];
+    c->tile_count = ntiles;
+    c->tile_hc = hc;
+    c->tile_want = true;
+    return tile_reserve_slots(c);
+}
+
+// The slot rows: one per atom of the capacity, maxnb rounded up to 8 slots.
+int tile_reserve_slots(Context* c) {
+    if (!c->tile_want || c->maxnb <= 0) return OMDG_OK;
+    const int stride = (c->maxnb + 7) & ~7;
+    const size_t need = (size_t)c->cap * stride;
+    if (need > c->tslot_alloc || !c->tslot) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(c->stream, &cs);
+        if (cs != cudaStreamCaptureStatusNone) return set_error(c, OMDG_ESTATE, "tile slots grew inside a capture");
+        invalidate_graph(c);
+        cudaFree(c->tslot);
+        c->tslot = nullptr;
+        c->tslot_alloc = 0;
+        if (cudaMalloc(&c->tslot, need * sizeof(unsigned short)) != cudaSuccess)
+            return set_error(c, OMDG_ENOMEM, "tile slot rows");
+        c->tslot_alloc = need;
+    }
+    if (stride != c->tile_stride) invalidate_graph(c);
+    c->tile_stride = stride;
+    return OMDG_OK;
+}
+
+void tile_release(Context* c) {
+    cudaFree(c->tile_sb);
+    cudaFree(c->tile_nst);
+    cudaFree(c->tile_org);
+    cudaFree(c->tslot);
+    c->tile_sb = nullptr;
+    c->tile_nst = nullptr;
+    c->tile_org = nullptr;
+    c->tslot = nullptr;
+    c->tile_alloc = 0;
+    c->tslot_alloc = 0;
+    c->tile_want = false;
+    c->tile_valid = false;
+}
+
 size_t nlist_slots(const Context* c, int maxnb) {
     size_t H = (size_t)1 << c->nbr_hshift;
     size_t slices = ((size_t)c->cap + H - 1) / H;
@@ -1041,7 +1231,7 @@ int nlist_reserve(Context* c, int maxnb) {
     }
     c->maxnb = maxnb;
     c->nbr_bytes = (long)need;
-    return OMDG_OK;
+    return tile_reserve_slots(c);
 }
 
 static int ensure_cells(Context* c, int m) {
@@ -1170,6 +1360,41 @@ int nlist_build(Context* c) {
     prof_end(c);
 
     BuildParams bp;
+    bp.to = TileOut{};
+    // tile slots: prepared per tile after the scan, written by the cell-local build
+    const bool tiles = c->tile_want && !reps && c->tslot && c->tile_stride >= c->maxnb;
+    if (tiles) {
+        TilePrep tp;
+        for (int d = 0; d < 3; d++) {
+            tp.T[d] = c->tile_dim[d];
+            tp.nt[d] = c->tile_nt[d];
+            tp.nc[d] = g.nc[d];
+            tp.periodic[d] = g.periodic[d];
+            tp.corg[d] = g.org[d];
+            tp.h[d] = g.h[d];
+            tp.borg[d] = c->box.org[d];
+            tp.P[d] = c->box.P[d];
+        }
+        tp.hx = tp.T[0] + 2;
+        tp.hy = tp.T[1] + 2;
+        tp.HC = c->tile_hc;
+        k_tile_prep<<<c->tile_count, TILE_PREP_THREADS, 0, s>>>(tp, c->cell_start, c->tile_sb, c->tile_nst,
+                                                                c->tile_org);
+        c->launches++;
+        bp.to.slot = c->tslot;
+        bp.to.sb = c->tile_sb;
+        bp.to.nst = c->tile_nst;
+        for (int d = 0; d < 3; d++) {
+            bp.to.T[d] = tp.T[d];
+            bp.to.nt[d] = tp.nt[d];
+        }
+        bp.to.hx = tp.hx;
+        bp.to.hy = tp.hy;
+        bp.to.HC = tp.HC;
+        bp.to.stride = c->tile_stride;
+        bp.to.cap = c->tile_cap;
+    }
+    c->tile_valid = tiles;
     bp.n = n;
     bp.maxnb = c->maxnb;
     bp.hshift = c->nbr_hshift;
@@ -1195,13 +1420,13 @@ int nlist_build(Context* c) {
     int combos = 1;
     for (int d = 0; d < 3; d++) combos *= (g.periodic[d] && g.nc[d] < 3) ? 3 * g.nc[d] : 3;
     // the cell-local builds also write each row's type mask
-    c->nbmask_valid = reps || c->flags_used || !(c->build_lanes == 0 && combos <= 64 && !sparse) &&
+    c->nbmask_valid = reps || c->flags_used || tiles || !(c->build_lanes == 0 && combos <= 64 && !sparse) &&
                                                    c->build_lanes != 8 && c->build_lanes != 4;
     if (reps) {
         k_build<true><<<grid_for(n, 128), 128, 0, s>>>(bp, rg, c->d_rep_of, c->loc, c->x, c->y, c->z, cell_sorted,
                                                        c->cell_start, umax, reinterpret_cast<unsigned*>(c->nbr),
                                                        c->nnb, c->d_status, c->d_flags + 1, rflag, c->nbmask);
-    } else if (c->flags_used) {  // only the cell-local build skips inactive atoms
+    } else if (c->flags_used || tiles) {  // only the cell-local build skips inactive atoms and writes tile slots
         k_build<false><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
                                                         cell_sorted, c->cell_start, umax,
                                                         reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,

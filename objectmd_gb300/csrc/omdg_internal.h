@@ -263,7 +263,28 @@ struct Context {
     int tb_block = 128;        // three-body kernels
     int tb_lanes = 1;
     int tb_persistent = 0;     // Tersoff register pass: one resident grid striding over the flattened atoms
-    int fuse_kick_on = 1;      // a step's second half-kick in the force kernel's epilogue where it can go
+    int fuse_kick_on = 0;      // a step's second half-kick in the force kernel's epilogue where it can go (opt-in:
+                               // with 4 lanes per atom its FP64 work issues at a quarter of the lanes)
+
+    // EAM cell tiles (eam_fast.cu): a tile is a block of tile_dim cells; one
+    // CTA stages the packs of the tile's cells and their one-cell halo in
+    // shared memory, and the list build also writes every row as 16-bit
+    // slots into that staged halo.  A tile whose halo holds more than
+    // tile_cap atoms takes the gather path.
+    int eam_tile = 0;                 // launch key: the tiled EAM passes where they apply
+    int tile_dim[3] = {2, 2, 2};      // launch keys tile_x, tile_y, tile_z: cells per tile
+    int tile_cap = 1536;              // launch key: staged atoms per tile (32 bytes of shared memory each)
+    bool tile_want = false;           // this context's builds write tile slots (tile_prepare)
+    bool tile_valid = false;          // the last build wrote them
+    int tile_nt[3] = {0, 0, 0};       // tiles per axis
+    int tile_count = 0, tile_hc = 0;  // tiles; halo cells per tile
+    int tile_alloc = 0;               // tiles x halo cells allocated
+    int tile_stride = 0;              // u16 slots per row of tslot (maxnb rounded up to 8)
+    size_t tslot_alloc = 0;           // u16 slots allocated
+    unsigned short* tile_sb = nullptr;  // per tile and halo cell: its first staged slot
+    int* tile_nst = nullptr;            // per tile: staged atoms
+    float4* tile_org = nullptr;         // per tile: its lower corner in the pack frame (FP32)
+    unsigned short* tslot = nullptr;    // per atom row: each entry's slot in its tile's staged halo
 
     // potentials
     std::vector<Potential> pots;
@@ -345,6 +366,12 @@ int nlist_build(Context* c);
 void nlist_prepare_geometry(Context* c);
 int nlist_reserve(Context* c, int maxnb);
 size_t nlist_slots(const Context* c, int maxnb);
+// EAM cell tiles: decide whether the builds write tile slots and size the
+// tile tables (host, outside any capture); the slot rows follow maxnb
+bool tiles_apply(const Context* c);
+int tile_prepare(Context* c);
+int tile_reserve_slots(Context* c);
+void tile_release(Context* c);
 
 // forces (eam.cu, pair.cu, threebody.cu)
 int forces_compute(Context* c);

@@ -114,6 +114,7 @@ SIGNATURES = {
     "omdg_set_compat": [_vp, _cp, _i],
     "omdg_stats": [_vp, _P(_l), _P(_l)],
     "omdg_wide_centres": [_vp, _P(_i)],
+    "omdg_tile_counts": [_vp, _P(_i), _P(_i)],
     "omdg_set_wait_polls": [_i],
     "omdg_selftest_wait": [_i, _i, _P(ctypes.c_uint)],
     "omdg_set_launch": [_vp, _cp, _i],
@@ -802,6 +803,12 @@ class Context:
         self._check(self.lib.omdg_wide_centres(self.h, ctypes.byref(k)))
         return k.value
 
+    def tile_counts(self):
+        """omdg_tile_counts: (tiles of the last build, tiles staged in shared memory)."""
+        t, st = _i(), _i()
+        self._check(self.lib.omdg_tile_counts(self.h, ctypes.byref(t), ctypes.byref(st)))
+        return t.value, st.value
+
     def stream(self):
         s = _vp()
         self._check(self.lib.omdg_get_stream(self.h, ctypes.byref(s)))
@@ -817,7 +824,8 @@ class Context:
 
     def launch_shapes(self):
         keys = ("eam_block", "eam_lanes", "eam_stage", "eam_ctas_per_sm", "pair_block", "pair_lanes", "tb_block",
-                "tb_lanes", "tb_persistent", "fuse_kick", "nbr_hshift", "build_lanes", "io_blocks")
+                "tb_lanes", "tb_persistent", "fuse_kick", "nbr_hshift", "build_lanes", "io_blocks", "eam_tile",
+                "tile_x", "tile_y", "tile_z", "tile_cap")
         return {k: self.get_launch(k) for k in keys}
 
     def autotune(self, reps=3):

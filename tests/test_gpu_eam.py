@@ -72,15 +72,104 @@ def test_build_modes_give_the_reference_set(omdg_lib, mode):
     assert mine == set(map(tuple, d["nbr"].tolist()))
 
 
-@pytest.mark.parametrize("lanes,hshift", [(1, 5), (4, 3), (8, 2), (16, 1)])
-def test_eam_lane_shapes_agree(omdg_lib, lanes, hshift):
+@pytest.mark.parametrize("lanes,hshift,stage", [(1, 5, 0), (4, 3, 0), (8, 2, 0), (16, 1, 0), (4, 3, 1), (8, 2, 1)])
+def test_eam_lane_shapes_agree(omdg_lib, lanes, hshift, stage):
+    """Every lane shape of the gather passes, with the spline knots read
+    from global memory or staged in shared memory, against the reference."""
     d = load_case("eam_al_4000")
     with make_eam(omdg_lib, d) as ctx:
+        ctx.set_launch("eam_tile", 0)
         ctx.set_launch("eam_lanes", lanes)
         ctx.set_launch("nbr_hshift", hshift)
+        ctx.set_launch("eam_stage", stage)
         ctx.compute_forces()
         st = ctx.get_state()
     check_forces(st["f"], d["f"], st["pot"], d["pot"])
+
+
+@pytest.mark.parametrize("lanes", [4, 8, 16])
+@pytest.mark.parametrize("shape", [(2, 2, 2), (3, 1, 2), (4, 4, 4)])
+def test_eam_tiles_match_reference(omdg_lib, lanes, shape):
+    """The tiled passes (every tile's halo staged in shared memory, rows of
+    16-bit slots from the list build) against the reference, and against
+    the gather passes on the same list: forces to 1e-6 relative (only pairs
+    across a periodic face round their lo parts in another order)."""
+    d = load_case("eam_al_4000")
+    out = {}
+    for tile in (1, 0):
+        with make_eam(omdg_lib, d) as ctx:
+            ctx.set_launch("eam_tile", tile)
+            ctx.set_launch("tile_cap", 5000)  # a 4x4x4 tile's halo is this whole box
+            for key, v in zip(("tile_x", "tile_y", "tile_z"), shape):
+                ctx.set_launch(key, v)
+            ctx.set_launch("eam_lanes", lanes)
+            ctx.compute_forces()
+            st = ctx.get_state()
+            tiles, staged = ctx.tile_counts()
+            if tile:
+                assert tiles > 1 and staged == tiles
+            else:
+                assert tiles == 0
+            check_forces(st["f"], d["f"], st["pot"], d["pot"])
+            out[tile] = st
+    a, b = out[1], out[0]
+    assert np.linalg.norm(a["f"] - b["f"]) <= 1e-6 * np.linalg.norm(b["f"])
+    assert np.abs(a["pot"] - b["pot"]).max() <= 1e-6
+
+
+def test_eam_tiles_past_capacity_take_the_gather_path(omdg_lib):
+    """Tiles whose halo holds more atoms than tile_cap are evaluated by the
+    gather passes inside the tiled launch: with a cap below every halo none
+    is staged, with one inside the spread of the halo counts some are."""
+    d = load_case("eam_al_4000")
+    with make_eam(omdg_lib, d) as ctx:
+        ctx.set_launch("eam_tile", 1)
+        ctx.set_launch("tile_cap", 64)
+        ctx.compute_forces()
+        st = ctx.get_state()
+        tiles, staged = ctx.tile_counts()
+        assert tiles > 1 and staged == 0
+        check_forces(st["f"], d["f"], st["pot"], d["pot"])
+        mixed = None
+        for cap in range(900, 1500, 5):
+            ctx.set_launch("tile_cap", cap)
+            ctx.build_neighbors()
+            tiles, staged = ctx.tile_counts()
+            if 0 < staged < tiles:
+                mixed = cap
+                break
+        assert mixed is not None
+        ctx.compute_forces()
+        st = ctx.get_state()
+    check_forces(st["f"], d["f"], st["pot"], d["pot"])
+
+
+def test_eam_tiles_free_surface_slab(omdg_lib, oracle_lib):
+    """A slab free in z (no image across it; halo cells past the grid are
+    empty) with the tiled passes, against the FP64 oracle."""
+    from objectmd_gb300 import inputs
+
+    oc = oracle_lib
+    x, v, (lo, hi) = inputs.eam_aluminium(ncell=10, a=4.05, sigma=0.05, temp=300.0, seed_pos=41, seed_vel=42)
+    hi = np.array(hi, dtype=np.float64)
+    hi[2] += 6.0  # vacuum above the slab
+    phi = oc.Table.from_file(EAM_TABLE, "PAIR")
+    ed = oc.Table.from_file(EAM_TABLE, "EDENS")
+    em = oc.Table.from_file(EAM_TABLE, "EMBED")
+    box = oc.make_box(lo, hi, (1, 1, 0))
+    nb = oc.neighbors(box, x, phi.max_range() + 0.3)
+    fref, eref, _, _ = oc.eam(box, x, nb, phi, ed, em)
+    with omdg_lib.Context(0) as ctx:
+        ctx.set_box(lo, hi, (True, True, False))
+        ctx.set_atoms(x, v, masses=[inputs.md_mass("aluminum")], znum=[13.0])
+        ctx.add_eam(EAM_TABLE)
+        ctx.set_neighbor(0.3, 1)
+        ctx.set_launch("eam_tile", 1)
+        ctx.compute_forces()
+        st = ctx.get_state()
+        tiles, staged = ctx.tile_counts()
+    assert tiles > 1 and staged == tiles
+    check_forces(st["f"], fref, st["pot"], eref)
 
 
 def test_eam_large_vs_oracle(omdg_lib, oracle_lib):
@@ -265,7 +354,7 @@ def test_step_io_equals_upload_step_readback(omdg_lib, rebuild_every):
 
 def test_kick_in_the_force_epilogue_is_the_same_step(omdg_lib):
     """The step's second half-kick done by the EAM force kernel's epilogue
-    (the default for one EAM potential) against the separate kick kernel:
+    (launch key fuse_kick, for one EAM potential) against the separate kick kernel:
     positions, velocities and forces bit for bit after 30 steps with two
     rebuilds, the ledger to FP32-pair summation order."""
     from objectmd_gb300 import inputs
@@ -279,6 +368,7 @@ def test_kick_in_the_force_epilogue_is_the_same_step(omdg_lib):
             ctx.add_eam(os.path.join(TABLES, "eam.aluminum5000"))
             ctx.set_neighbor(0.1, 0)
             ctx.set_timestep(0.002)
+            ctx.set_launch("eam_tile", 0)  # the fused kick rides on the gather passes
             ctx.set_launch("fuse_kick", fuse)
             ctx.step(30)
             kin, pot = ctx.ledger_history()

@@ -323,7 +323,9 @@ def timed_steps(ctx, n, steps, stream, flush_l2, torch):
     return total_ms, kernels, st1["rebuilds"] - st0["rebuilds"], st1["launches"] - st0["launches"]
 
 
-FDTD_CELL_BYTES = 53  # k_fd_solve: T, con, cap, S, E (8 B each), map 4, mask 1 read; A 8 written
+# the solve's algorithmic bytes: T, con, cap, S, E (8 B each), map 4, mask 1 read; A 8 written (the kernel
+# reads each cell's three face conductances instead of con: 69 B)
+FDTD_CELL_BYTES = 53
 
 
 def fdtd_report(device, torch, n=256, steps=100):

@@ -13,10 +13,16 @@
 //
 // The FP64 operations are the reference's, in its order, without
 // contraction (explicit _rn intrinsics): results are bit-identical to the
-// reference built with -ffp-contract=off.  HBM-bound: 8 B of the old vector,
-// 8 B con, 8 B cap, 8 B S, 8 B E, 4 B map and 1 B mask read and 8 B written
-// per cell (53 B; E and S are cleared only where not zero); the six
-// neighbours' T and con come from L1/L2.
+// reference built with -ffp-contract=off.  A face's conductance
+// K = con_a con_b / (con_a + con_b) is the same number seen from either cell
+// (both operations commute), so k_fd_faces computes it once per face when
+// the conductivity is uploaded and the step reads it: the step's FP64
+// divisions drop from seven per cell to the one by cap.  The step then moves
+// 8 B of the old vector, 24 B of its own three face conductances, 8 B cap,
+// 8 B S, 8 B E, 4 B map and 1 B mask read and 8 B written per cell (69 B; E
+// and S are cleared only where not zero); the neighbours' T and conductances
+// come from L1/L2.  A face whose conductance is zero adds nothing, as in the
+// reference for finite cell values.
 //
 // Host side (the string path of FDTDSolver, fdtd.cpp:100-118, 506-597): the
 // symbol map, the map, and the assignment strings "<symbols> <value>[:t0[:t1]]"
@@ -50,7 +56,7 @@ FDDev fd_dev(const FDGrid* g) {
     p.h2inv = g->h2inv;
     p.map = g->dmap;
     p.mask = g->dmask[g->solves > 0 ? 1 : 0];
-    p.con = g->dcon;
+    p.K = g->dK;
     p.cap = g->dcap;
     p.S = g->dS;
     p.E = g->dE;
@@ -60,15 +66,28 @@ FDDev fd_dev(const FDGrid* g) {
     return p;
 }
 
-// K (T_nb - T_i) added to acc when con_nb + con_i is not zero (fdtd.cpp:616-622)
-__device__ __forceinline__ double fd_face(const FDDev& p, const double* __restrict__ T, int i, int nb, double ci,
-                                          double ti, double acc) {
-    const double cn = p.con[nb];
-    double K = __dadd_rn(cn, ci);
-    if (K != 0.0) {
-        K = __ddiv_rn(__dmul_rn(cn, ci), K);
-        acc = __dadd_rn(acc, __dmul_rn(K, __dsub_rn(T[nb], ti)));
+// The conductance of each cell's +x, +y and +z face (the neighbour wraps):
+// K = con_nb con_i / (con_nb + con_i), 0 where con_nb + con_i is zero
+// (fdtd.cpp:616-622).
+__global__ void __launch_bounds__(FD_BLOCK) k_fd_faces(int nx, int ny, int nz, const double* __restrict__ con,
+                                                       double* __restrict__ K) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int xy = nx * ny, dim = xy * nz;
+    if (idx >= dim) return;
+    const int k = idx / xy, a = idx % xy, j = a / nx, i = a % nx;
+    const int nb[3] = {k * xy + (i + 1 == nx ? 0 : i + 1) + j * nx, k * xy + i + (j + 1 == ny ? 0 : j + 1) * nx,
+                       (k + 1 == nz ? 0 : k + 1) * xy + i + j * nx};
+    const double ci = con[idx];
+    for (int d = 0; d < 3; d++) {
+        const double cn = con[nb[d]];
+        const double s = __dadd_rn(cn, ci);
+        K[(size_t)d * dim + idx] = s != 0.0 ? __ddiv_rn(__dmul_rn(cn, ci), s) : 0.0;
     }
+}
+
+// K (T_nb - T_i) added to acc (fdtd.cpp:616-622)
+__device__ __forceinline__ double fd_face(const double* __restrict__ T, double K, int nb, double ti, double acc) {
+    if (K != 0.0) acc = __dadd_rn(acc, __dmul_rn(K, __dsub_rn(T[nb], ti)));
     return acc;
 }
 
@@ -82,16 +101,27 @@ __global__ void __launch_bounds__(FD_BLOCK) k_fd_solve(FDDev p, const double* __
         const int xy = p.nx * p.ny;
         const int k = idx / xy, a = idx % xy, j = a / p.nx, i = a % p.nx;
         const unsigned m = p.solves ? (*p.solves == 0 ? p.mask_first : p.mask_later)[idx] : p.mask[idx];
-        const double ci = p.con[idx];
+        const double* Kx = p.K;
+        const double* Ky = p.K + p.dim;
+        const double* Kz = p.K + 2 * (size_t)p.dim;
         acc = 0.0;
         // a face that is set and beyond the grid is periodic: it wraps (fdtd.cpp:277-285)
-        if (m & FD_R) acc = fd_face(p, T, idx, k * xy + (i + 1 == p.nx ? 0 : i + 1) + j * p.nx, ci, ti, acc);
-        if (m & FD_L) acc = fd_face(p, T, idx, k * xy + (i == 0 ? p.nx - 1 : i - 1) + j * p.nx, ci, ti, acc);
-        if (m & FD_B) acc = fd_face(p, T, idx, k * xy + i + (j + 1 == p.ny ? 0 : j + 1) * p.nx, ci, ti, acc);
-        if (m & FD_T) acc = fd_face(p, T, idx, k * xy + i + (j == 0 ? p.ny - 1 : j - 1) * p.nx, ci, ti, acc);
+        if (m & FD_R) acc = fd_face(T, Kx[idx], k * xy + (i + 1 == p.nx ? 0 : i + 1) + j * p.nx, ti, acc);
+        if (m & FD_L) {
+            const int nb = k * xy + (i == 0 ? p.nx - 1 : i - 1) + j * p.nx;
+            acc = fd_face(T, Kx[nb], nb, ti, acc);
+        }
+        if (m & FD_B) acc = fd_face(T, Ky[idx], k * xy + i + (j + 1 == p.ny ? 0 : j + 1) * p.nx, ti, acc);
+        if (m & FD_T) {
+            const int nb = k * xy + i + (j == 0 ? p.ny - 1 : j - 1) * p.nx;
+            acc = fd_face(T, Ky[nb], nb, ti, acc);
+        }
         if (p.nz != 1) {
-            if (m & FD_N) acc = fd_face(p, T, idx, (k == 0 ? p.nz - 1 : k - 1) * xy + i + j * p.nx, ci, ti, acc);
-            if (m & FD_F) acc = fd_face(p, T, idx, (k + 1 == p.nz ? 0 : k + 1) * xy + i + j * p.nx, ci, ti, acc);
+            if (m & FD_N) {
+                const int nb = (k == 0 ? p.nz - 1 : k - 1) * xy + i + j * p.nx;
+                acc = fd_face(T, Kz[nb], nb, ti, acc);
+            }
+            if (m & FD_F) acc = fd_face(T, Kz[idx], (k + 1 == p.nz ? 0 : k + 1) * xy + i + j * p.nx, ti, acc);
         }
     }
     // A = T + (2 A h2inv + S + E) dt / cap (fdtd.cpp:664)
@@ -313,7 +343,13 @@ int fd_upload(FDGrid* g, cudaStream_t s) {
     const size_t b = sizeof(double) * g->dim;
     cudaError_t e = cudaSuccess;
     if (g->dirty_S) e = cudaMemcpyAsync(g->dS, g->hS.data(), b, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && g->dirty_con) e = cudaMemcpyAsync(g->dcon, g->hcon.data(), b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && g->dirty_con) {
+        e = cudaMemcpyAsync(g->dcon, g->hcon.data(), b, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) {
+            k_fd_faces<<<grid_for(g->dim, FD_BLOCK), FD_BLOCK, 0, s>>>(g->nx, g->ny, g->nz, g->dcon, g->dK);
+            e = cudaGetLastError();
+        }
+    }
     if (e == cudaSuccess && g->dirty_cap) e = cudaMemcpyAsync(g->dcap, g->hcap.data(), b, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return fd_fail(g, OMDG_ECUDA, std::string("fdtd upload: ") + cudaGetErrorString(e));
     g->dirty_S = g->dirty_con = g->dirty_cap = false;
@@ -375,6 +411,7 @@ int omdg_fdtd_create(omdg_fdtd** out, int device, int nx, int ny, int nz, const 
     if (e == cudaSuccess) e = cudaMalloc(&g->dS, b8);
     if (e == cudaSuccess) e = cudaMalloc(&g->dE, b8);
     if (e == cudaSuccess) e = cudaMalloc(&g->dcon, b8);
+    if (e == cudaSuccess) e = cudaMalloc(&g->dK, 3 * b8);
     if (e == cudaSuccess) e = cudaMalloc(&g->dcap, b8);
     if (e == cudaSuccess) e = cudaMalloc(&g->dmap, sizeof(int) * g->dim);
     for (int k = 0; k < 2 && e == cudaSuccess; k++) e = cudaMalloc(&g->dmask[k], g->dim);
@@ -404,6 +441,7 @@ int omdg_fdtd_destroy(omdg_fdtd* g) {
     cudaFree(g->dS);
     cudaFree(g->dE);
     cudaFree(g->dcon);
+    cudaFree(g->dK);
     cudaFree(g->dcap);
     cudaFree(g->dmap);
     if (g->own_stream) cudaStreamDestroy(g->stream);

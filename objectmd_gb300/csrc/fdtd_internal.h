@@ -31,7 +31,7 @@ struct FDDev {
     double dt, h2inv;
     const int* map;
     const uint8_t* mask;
-    const double* con;
+    const double* K;  // face conductances: x faces [0, dim), y faces [dim, 2 dim), z faces [2 dim, 3 dim)
     const double* cap;
     double* S;
     double* E;
@@ -65,6 +65,7 @@ struct FDGrid {
     double* dA[2] = {nullptr, nullptr};
     int cur = 0;                         // dA[cur] holds the cell vector
     double *dS = nullptr, *dE = nullptr, *dcon = nullptr, *dcap = nullptr;
+    double* dK = nullptr;                // face conductances from dcon (3 x dim), refreshed with it
     int* dmap = nullptr;
     uint8_t* dmask[2] = {nullptr, nullptr};  // first, later
     bool coupled = false;                // stepped by a context's two-temperature model

@@ -1,7 +1,10 @@
 // Descriptor terms of the neural surrogate (FP32), shared by the training
 // kernels (which store the Jacobian) and the MD kernels (which contract it
 // with dE/dG on the fly).  Behler-Parrinello radial G2 and angular G5 terms
-// (J. Behler, J. Chem. Phys. 134, 074106 (2011)).
+// (J. Behler, J. Chem. Phys. 134, 074106 (2011)).  The exponentials and the
+// cutoff's sine and cosine use the hardware approximations (__expf,
+// __sincosf: a few 1e-7 relative for the arguments met here), far below the
+// BF16 rounding of the network's input.
 #pragma once
 
 #include "nn_internal.h"
@@ -14,7 +17,7 @@ __device__ __forceinline__ float nn_fc(const NNDescParams& p, float r, float& df
         return 1.f;
     }
     float s, c;
-    sincosf((r - p.rin) * p.pi_rc, &s, &c);
+    __sincosf((r - p.rin) * p.pi_rc, &s, &c);
     dfc = -0.5f * p.pi_rc * s;
     return 0.5f * (c + 1.f);
 }
@@ -34,22 +37,35 @@ __device__ __forceinline__ float nn_ipow(float b, int z) {
 __device__ __forceinline__ void nn_radial(const NNDescParams& p, float r, float fc, float dfc, int k, float& val,
                                           float& ddr) {
     const float x = r - p.rs[k];
-    const float g = expf(-p.eta_r[k] * x * x);
+    const float g = __expf(-p.eta_r[k] * x * x);
     val = g * fc;
     ddr = g * (dfc - 2.f * p.eta_r[k] * x * fc);
 }
 
+// exp(-eta (r_a^2 + r_b^2)) of the angular terms, recomputed only when eta
+// changes from one term to the next (the descriptor set groups its terms by
+// eta, so a pair takes one exponential per distinct eta, not one per term).
+struct NNAngExp {
+    float eta = -1.f, ex = 1.f;
+    __device__ __forceinline__ float get(float e, float s2) {
+        if (e != eta) {
+            eta = e;
+            ex = e == 0.f ? 1.f : __expf(-e * s2);
+        }
+        return ex;
+    }
+};
+
 // Angular term m of the neighbour pair (a, b): the value and its derivatives
-// with respect to r_a, r_b and cos(theta).
+// with respect to r_a, r_b and cos(theta); ex = exp(-eta_a[m] (r_a^2 + r_b^2)).
 __device__ __forceinline__ void nn_angular(const NNDescParams& p, int m, float ra, float rb, float cs, float fa,
-                                           float dfa, float fb, float dfb, float& val, float& d_ra, float& d_rb,
-                                           float& d_cs) {
+                                           float dfa, float fb, float dfb, float ex, float& val, float& d_ra,
+                                           float& d_rb, float& d_cs) {
     float base = 1.f + p.lam[m] * cs;
     base = base > 0.f ? base : 0.f;
     const int z = p.zeta[m];
     const float pm1 = nn_ipow(base, z - 1);
     const float pw = pm1 * base;
-    const float ex = p.eta_a[m] == 0.f ? 1.f : expf(-p.eta_a[m] * (ra * ra + rb * rb));
     const float k = p.pref[m] * ex;
     val = k * pw * fa * fb;
     d_ra = k * pw * fb * (dfa - 2.f * p.eta_a[m] * ra * fa);

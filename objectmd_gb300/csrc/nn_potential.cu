@@ -92,10 +92,12 @@ __global__ void __launch_bounds__(128) k_nn_md_desc(NNMD q, NNDescParams p, cons
             float dfb;
             const float fb = nn_fc(p, rr[b], dfb);
             const float cs = (vx[a] * vx[b] + vy[a] * vy[b] + vz[a] * vz[b]) * ia / rr[b];
+            const float s2 = rr[a] * rr[a] + rr[b] * rr[b];
+            NNAngExp ex;
 #pragma unroll
             for (int m = 0; m < NN_ANG; m++) {
                 float v, d1, d2, d3;
-                nn_angular(p, m, rr[a], rr[b], cs, fa, dfa, fb, dfb, v, d1, d2, d3);
+                nn_angular(p, m, rr[a], rr[b], cs, fa, dfa, fb, dfb, ex.get(p.eta_a[m], s2), v, d1, d2, d3);
                 g[NN_RAD + m] += v;
             }
         }
@@ -172,10 +174,13 @@ __global__ void __launch_bounds__(128) k_nn_md_force(NNMD q, NNDescParams p, con
                 const float eb[3] = {vx[b] * ib, vy[b] * ib, vz[b] * ib};
                 const float cs = ea[0] * eb[0] + ea[1] * eb[1] + ea[2] * eb[2];
                 float cra = 0.f, crb = 0.f, ccs = 0.f;
+                const float s2 = rr[a] * rr[a] + rr[b] * rr[b];
+                NNAngExp ex;
 #pragma unroll
                 for (int mm = 0; mm < NN_ANG; mm++) {
                     float v, d_ra, d_rb, d_cs;
-                    nn_angular(p, mm, rr[a], rr[b], cs, fa, dfa, fb, dfb, v, d_ra, d_rb, d_cs);
+                    nn_angular(p, mm, rr[a], rr[b], cs, fa, dfa, fb, dfb, ex.get(p.eta_a[mm], s2), v, d_ra, d_rb,
+                               d_cs);
                     const float w = u[NN_RAD + mm];
                     cra = fmaf(w, d_ra, cra);
                     crb = fmaf(w, d_rb, crb);

@@ -186,9 +186,11 @@ __global__ void k_nn_train_desc(NNDescParams p, long n, const int* __restrict__ 
                 dcb[c] = (ea[c] - cs * eb[c]) * ib;
             }
             float* Jb = J + (size_t)b * 3 * NN_DESC + NN_RAD;
+            const float s2 = ra * ra + rb * rb;
+            NNAngExp ex;
             for (int m = 0; m < NN_ANG; m++) {
                 float v, d_ra, d_rb, d_cs;
-                nn_angular(p, m, ra, rb, cs, fa, dfa, fb, dfb, v, d_ra, d_rb, d_cs);
+                nn_angular(p, m, ra, rb, cs, fa, dfa, fb, dfb, ex.get(p.eta_a[m], s2), v, d_ra, d_rb, d_cs);
                 g[NN_RAD + m] += v;
                 for (int c = 0; c < 3; c++) {
                     Ja[c * NN_DESC + m] += d_ra * ea[c] + d_cs * dca[c];

@@ -1864,6 +1864,7 @@ static int* launch_knob(Context* c, const std::string& k) {
     if (k == "io_blocks") return &c->io_blocks;
     if (k == "nbr_capacity") return &c->nbr_capacity;
     if (k == "eam_tile") return &c->eam_tile;
+    if (k == "nn_fused") return &c->nn_fused;
     if (k == "tile_x") return &c->tile_dim[0];
     if (k == "tile_y") return &c->tile_dim[1];
     if (k == "tile_z") return &c->tile_dim[2];
@@ -1881,7 +1882,7 @@ static bool valid_knob(const std::string& k, int v) {
     if (k == "build_lanes") return v == 0 || v == 1 || v == 4 || v == 8;
     if (k == "io_blocks") return v >= 1 && v <= 65535;
     if (k == "nbr_capacity") return v >= 0 && v <= 4096;
-    if (k == "eam_tile") return v == 0 || v == 1;
+    if (k == "eam_tile" || k == "nn_fused") return v == 0 || v == 1;
     if (k == "tile_x" || k == "tile_y" || k == "tile_z") return v >= 1 && v <= 4;
     if (k == "tile_cap") return v >= 64 && v <= 5000;
     return false;

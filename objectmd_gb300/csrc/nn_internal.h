@@ -80,5 +80,11 @@ void nn_net_free(NNDevNet& net);
 // u = dE/dG in raw descriptor units (rows x 32).  Returns a cudaError.
 cudaError_t nn_mlp_launch(const NNDevNet& net, const float* gt, int rows, float* E, float* u, unsigned* status,
                           int num_sms, cudaStream_t s);
+// The same network with each row's descriptors computed in the kernel from
+// the Verlet list (MD): flags atoms outside the training range and counts them.
+struct NNMD;
+cudaError_t nn_mlp_md_launch(const NNDevNet& net, const NNMD& q, const NNDescParams& dp, const PosPack* pack,
+                             const unsigned* nbr, const int* nnb, int* flag, int* count, float* E, float* u,
+                             unsigned* status, int num_sms, cudaStream_t s);
 
 }  // namespace omdg

@@ -18,6 +18,7 @@
 #include <sstream>
 
 #include "nn_internal.h"
+#include "nn_md.cuh"
 #include "tc_common.cuh"
 
 namespace omdg {
@@ -309,8 +310,24 @@ __device__ __forceinline__ void tc_handoff() {
     tc_fence_after();
 }
 
-__global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __restrict__ img,
-                                                       const float* __restrict__ vec, const float* __restrict__ gt,
+// Where a tile's input rows come from: normalised descriptor rows in global
+// memory (training, prediction), or (MD) computed by each thread from the
+// Verlet list, so the descriptors never leave the chip and their FP32 work
+// overlaps the other resident CTAs' MMA round trips.
+struct MLPInput {
+    const float* gt;        // rows x 32 normalised descriptors (null: MD)
+    NNMD q;
+    NNDescParams dp;
+    const PosPack* pack;
+    const unsigned* nbr;
+    const int* nnb;
+    int* flag;              // 1: outside the training range (Tersoff fallback)
+    int* count;
+};
+
+template <bool MD>
+__global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __restrict__ img,
+                                                       const float* __restrict__ vec, const MLPInput in,
                                                        int rows, float* __restrict__ E, float* __restrict__ U,
                                                        unsigned* status, int polls) {
     extern __shared__ uint8_t smem_raw[];
@@ -354,8 +371,15 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __r
         const bool valid = row < rows;
         {
             float g[NN_DESC];
-            if (valid) {
-                const float4* src = reinterpret_cast<const float4*>(gt + (size_t)row * NN_DESC);
+            if (MD && valid) {
+                nn_md_descriptors(in.q, in.dp, row, in.pack, in.nbr, in.nnb[row], g, status);
+                const bool out = nn_out_of_range(in.dp, g);
+                in.flag[row] = out ? 1 : 0;
+                if (out) atomicAdd(in.count, 1);
+#pragma unroll
+                for (int k = 0; k < NN_DESC; k++) g[k] = (g[k] - in.dp.mu[k]) * in.dp.isig[k];
+            } else if (valid) {
+                const float4* src = reinterpret_cast<const float4*>(in.gt + (size_t)row * NN_DESC);
 #pragma unroll
                 for (int q = 0; q < NN_DESC / 4; q++) {
                     const float4 v = __ldg(src + q);
@@ -465,18 +489,40 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_nn_mlp(const __nv_bfloat16* __r
     if (warp == 0) tmem_dealloc(tmem, MLP_TMEM_COLS);
 }
 
-cudaError_t nn_mlp_launch(const NNDevNet& net, const float* gt, int rows, float* E, float* u, unsigned* status,
-                          int num_sms, cudaStream_t s) {
+template <bool MD>
+static cudaError_t mlp_launch(const NNDevNet& net, const MLPInput& in, int rows, float* E, float* u,
+                              unsigned* status, int num_sms, cudaStream_t s) {
     if (rows <= 0) return cudaSuccess;
     const size_t smem = sizeof(MLPSmem) + 1024;  // + alignment slack
-    cudaError_t e = cudaFuncSetAttribute(k_nn_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_nn_mlp<MD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int tiles = (rows + MLP_ROWS - 1) / MLP_ROWS;
     // 4 CTAs per SM: about 51 KB of shared memory and 128 of the SM's 512
     // TMEM columns each, so the allocations never wait; four MMA chains overlap
     const int grid = std::min(tiles, 4 * std::max(1, num_sms));
-    k_nn_mlp<<<grid, MLP_ROWS, smem, s>>>(net.img, net.vec, gt, rows, E, u, status, tc_wait_polls());
+    k_nn_mlp<MD><<<grid, MLP_ROWS, smem, s>>>(net.img, net.vec, in, rows, E, u, status, tc_wait_polls());
     return cudaGetLastError();
+}
+
+cudaError_t nn_mlp_launch(const NNDevNet& net, const float* gt, int rows, float* E, float* u, unsigned* status,
+                          int num_sms, cudaStream_t s) {
+    MLPInput in{};
+    in.gt = gt;
+    return mlp_launch<false>(net, in, rows, E, u, status, num_sms, s);
+}
+
+cudaError_t nn_mlp_md_launch(const NNDevNet& net, const NNMD& q, const NNDescParams& dp, const PosPack* pack,
+                             const unsigned* nbr, const int* nnb, int* flag, int* count, float* E, float* u,
+                             unsigned* status, int num_sms, cudaStream_t s) {
+    MLPInput in{};
+    in.q = q;
+    in.dp = dp;
+    in.pack = pack;
+    in.nbr = nbr;
+    in.nnb = nnb;
+    in.flag = flag;
+    in.count = count;
+    return mlp_launch<true>(net, in, q.n, E, u, status, num_sms, s);
 }
 
 }  // namespace omdg

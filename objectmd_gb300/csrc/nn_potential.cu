@@ -11,8 +11,7 @@
 // network, so the total is the energy of that mixed per-atom decomposition.
 #include <string>
 
-#include "device_common.cuh"
-#include "nn_desc.cuh"
+#include "nn_md.cuh"
 
 namespace omdg {
 
@@ -28,81 +27,14 @@ struct NNState {
     int fallback = -1;     // index of the Tersoff potential in ctx->pots
 };
 
-struct NNMD {
-    int n, hshift, maxnb, first;
-    ShiftF L;
-    float rc2;
-};
-
-// Neighbours of i inside the descriptor cutoff: vectors x_j - x_i, distances
-// and list slots.  Returns the count (capped at NN_MAXN, overflow flagged).
-__device__ __forceinline__ int nn_gather(const NNMD& q, const NNDescParams& p, int i, const PosPack& pi,
-                                         const PosPack* __restrict__ pack, const unsigned* __restrict__ nbr, int m,
-                                         float* vx, float* vy, float* vz, float* rr, int* sl, unsigned* status) {
-    int nc = 0;
-    for (int s = 0; s < m; s++) {
-        const unsigned e = nbr[nbr_at(i, s, q.hshift, q.maxnb)];
-        const PosPack pj = pack[nbr_index(e)];
-        const float3 d = pair_delta(pi.hi, pi.lo, pj.hi, pj.lo, e, q.L);  // x_i - x_j
-        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-        if (!(r2 < q.rc2)) continue;
-        const float r = sqrtf(r2);
-        if (!(r < p.rc)) continue;
-        if (nc < NN_MAXN) {
-            vx[nc] = -d.x;
-            vy[nc] = -d.y;
-            vz[nc] = -d.z;
-            rr[nc] = r;
-            sl[nc] = s;
-            nc++;
-        } else {
-            atomicOr(status, ERR_NBR_OVERFLOW);
-        }
-    }
-    return nc;
-}
-
 __global__ void __launch_bounds__(128) k_nn_md_desc(NNMD q, NNDescParams p, const PosPack* __restrict__ pack,
                                                     const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                     float* __restrict__ Gt, int* __restrict__ flag, int* count,
                                                     unsigned* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= q.n) return;
-    float vx[NN_MAXN], vy[NN_MAXN], vz[NN_MAXN], rr[NN_MAXN];
-    int sl[NN_MAXN];
-    const int nc = nn_gather(q, p, i, pack[i], pack, nbr, nnb[i], vx, vy, vz, rr, sl, status);
     float g[NN_DESC];
-#pragma unroll
-    for (int k = 0; k < NN_DESC; k++) g[k] = 0.f;
-    for (int a = 0; a < nc; a++) {
-        float dfc;
-        const float fc = nn_fc(p, rr[a], dfc);
-#pragma unroll
-        for (int k = 0; k < NN_RAD; k++) {
-            float v, ddr;
-            nn_radial(p, rr[a], fc, dfc, k, v, ddr);
-            g[k] += v;
-        }
-    }
-    for (int a = 0; a < nc; a++) {
-        float dfa;
-        const float fa = nn_fc(p, rr[a], dfa);
-        const float ia = 1.f / rr[a];
-        for (int b = a + 1; b < nc; b++) {
-            float dfb;
-            const float fb = nn_fc(p, rr[b], dfb);
-            const float cs = (vx[a] * vx[b] + vy[a] * vy[b] + vz[a] * vz[b]) * ia / rr[b];
-            const float s2 = rr[a] * rr[a] + rr[b] * rr[b];
-            NNAngExp ex;
-#pragma unroll
-            for (int m = 0; m < NN_ANG; m++) {
-                float v, d1, d2, d3;
-                nn_angular(p, m, rr[a], rr[b], cs, fa, dfa, fb, dfb, ex.get(p.eta_a[m], s2), v, d1, d2, d3);
-                g[NN_RAD + m] += v;
-            }
-        }
-    }
-    bool out = false;
+    nn_md_descriptors(q, p, i, pack, nbr, nnb[i], g, status);
     float4* dst = reinterpret_cast<float4*>(Gt + (size_t)i * NN_DESC);
 #pragma unroll
     for (int k = 0; k < NN_DESC; k += 4) {
@@ -112,9 +44,8 @@ __global__ void __launch_bounds__(128) k_nn_md_desc(NNMD q, NNDescParams p, cons
         w.z = (g[k + 2] - p.mu[k + 2]) * p.isig[k + 2];
         w.w = (g[k + 3] - p.mu[k + 3]) * p.isig[k + 3];
         dst[k / 4] = w;
-#pragma unroll
-        for (int c = 0; c < 4; c++) out |= !(g[k + c] >= p.gmin[k + c] && g[k + c] <= p.gmax[k + c]);
     }
+    const bool out = nn_out_of_range(p, g);
     flag[i] = out ? 1 : 0;
     if (out) atomicAdd(count, 1);
 }
@@ -254,13 +185,23 @@ int nn_launch(Context* c, Potential& pot, bool first) {
     const unsigned grid = (unsigned)grid_for(c->n, 128);
     const unsigned* nbr = reinterpret_cast<const unsigned*>(c->nbr);
     cudaMemsetAsync(s.count, 0, sizeof(int), c->stream);
-    prof_begin(c, "nn_descriptors");
-    k_nn_md_desc<<<grid, 128, 0, c->stream>>>(q, s.model.dp, c->pack, nbr, c->nnb, s.Gt, s.flag, s.count,
-                                              c->d_status);
-    prof_end(c);
-    prof_begin(c, "nn_mlp");
-    cudaError_t e = nn_mlp_launch(s.net, s.Gt, c->n, s.E, s.U, c->d_status, c->num_sms, c->stream);
-    prof_end(c);
+    cudaError_t e;
+    if (c->nn_fused) {
+        // descriptors computed by the network kernel's own threads
+        prof_begin(c, "nn_desc_mlp");
+        e = nn_mlp_md_launch(s.net, q, s.model.dp, c->pack, nbr, c->nnb, s.flag, s.count, s.E, s.U, c->d_status,
+                             c->num_sms, c->stream);
+        prof_end(c);
+        c->launches -= 1;
+    } else {
+        prof_begin(c, "nn_descriptors");
+        k_nn_md_desc<<<grid, 128, 0, c->stream>>>(q, s.model.dp, c->pack, nbr, c->nnb, s.Gt, s.flag, s.count,
+                                                  c->d_status);
+        prof_end(c);
+        prof_begin(c, "nn_mlp");
+        e = nn_mlp_launch(s.net, s.Gt, c->n, s.E, s.U, c->d_status, c->num_sms, c->stream);
+        prof_end(c);
+    }
     if (e != cudaSuccess) return check_cuda(c, e, "surrogate network");
     prof_begin(c, "nn_force");
     k_nn_md_force<<<grid, 128, 0, c->stream>>>(q, s.model.dp, c->pack, nbr, c->nnb, s.E, s.U, s.flag, c->slot_buf,

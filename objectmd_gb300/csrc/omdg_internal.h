@@ -263,6 +263,8 @@ struct Context {
     int tb_block = 128;        // three-body kernels
     int tb_lanes = 1;
     int tb_persistent = 0;     // Tersoff register pass: one resident grid striding over the flattened atoms
+    int nn_fused = 0;          // the surrogate's descriptors computed inside its tensor-core network kernel (opt-in:
+                               // with four 128-thread CTAs per SM the descriptor work runs slower there)
     int fuse_kick_on = 0;      // a step's second half-kick in the force kernel's epilogue where it can go (opt-in:
                                // with 4 lanes per atom its FP64 work issues at a quarter of the lanes)
 

@@ -140,6 +140,33 @@ def test_md_path_matches_prediction(omdg_lib, dataset, tmp_path):
     assert np.linalg.norm(st["f"] - F) / np.linalg.norm(F) < 2e-3
 
 
+def test_fused_descriptor_network_kernel_is_the_same(omdg_lib, dataset, tmp_path):
+    """Descriptors computed inside the tensor-core network kernel (launch key
+    nn_fused) against the separate descriptor kernel: the same functions on
+    the same rows, so forces, energies and fallback flags agree bit for bit."""
+    from objectmd_gb300 import inputs
+
+    net, _, norm = make_network(omdg_lib, dataset)
+    model = str(tmp_path / "model.nn")
+    net.save(model)
+    net.close()
+    c = dataset[3]
+    out = []
+    for fused in (0, 1):
+        with omdg_lib.Context(0) as ctx:
+            ctx.set_box(c["lo"], c["hi"])
+            ctx.set_atoms(c["x"], np.zeros_like(c["x"]), masses=[inputs.md_mass("silicon")], znum=[14.0])
+            ctx.add_nn(model, TERSOFF)
+            ctx.set_neighbor(0.3, 1)
+            ctx.set_launch("nn_fused", fused)
+            ctx.compute_forces()
+            out.append((ctx.get_state(), ctx.nn_fallback_atoms()))
+    (a, na), (b, nb) = out
+    assert na == nb
+    for k in ("f", "pot", "vir"):
+        assert np.array_equal(a[k], b[k]), k
+
+
 def test_fallback_is_plain_tersoff(omdg_lib, dataset, tmp_path):
     net, w, norm = make_network(omdg_lib, dataset)
     # a training range no atom lies in: every atom falls back

@@ -500,9 +500,10 @@ def run_gpu(args):
     mean_step = total_ms / args.steps
 
     # end to end through the C ABI with host buffers
-    e2e = None
+    e2e = e2e_resident = None
     if not args.no_e2e:
         e2e = run_e2e(ctx, n, args.steps, torch)
+        e2e_resident = run_e2e(ctx, n, args.steps, torch, full=False)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -542,6 +543,7 @@ def run_gpu(args):
         "kernels": {k: round(v_["ms_per_launch"] * 1e3, 2) for k, v_ in kernels.items()},
         "kernels_unit": "us per launch",
         "e2e": e2e,
+        "e2e_state_resident": e2e_resident,
         "cpu_baseline": cpu,
         "energy": {"kinetic": led["kinetic"], "potential": led["potential"], "energy": led["energy"]},
         "surrogate": surrogate,
@@ -553,7 +555,7 @@ def run_gpu(args):
         ctx.close()
         ctx = None
         subs = {}
-        for name in ("tersoff_si_512k", "nn_si_512k"):
+        for name in ("tersoff_si_512k", "nn_si_512k", "sw_si_512k", "impact_256", "lj_ar_4000"):
             subs[name] = sub_workload(name, args, device, torch, flush_l2)
         out["workloads"] = subs
         out["fdtd"] = fdtd_report(device, torch)
@@ -620,21 +622,26 @@ def surrogate_report(ctx, w, x0, v0, lo, hi, device, args, torch):
     return out
 
 
-def run_e2e(ctx, n, steps, torch):
-    """Per step one omdg_step_io call from pinned host arrays: H2D of x and v,
-    one step, D2H of x, v and f (x and f while the step's last kernels run),
-    then the ledger."""
+def run_e2e(ctx, n, steps, torch, full=True):
+    """Per step one omdg_step_io call from pinned host arrays, then the
+    ledger.  full: H2D of x and v, one step, D2H of x, v and f (x and f while
+    the step's last kernels run) -- a caller that hands its whole state over
+    every step.  Otherwise the state stays on the device and only positions
+    come back each step (a trajectory writer)."""
     pin = lambda: torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
     x, v, f = pin(), pin(), pin()
     ctx.get_state_into(x=x, v=v)
-    ctx.step_io(1, x_in=x, v_in=v, x_out=x, v_out=v, f_out=f)  # captures the step with its downloads
+    io = dict(x_in=x, v_in=v, x_out=x, v_out=v, f_out=f) if full else dict(x_out=x)
+    ctx.step_io(1, **io)  # captures the step with its downloads
     t0 = time.perf_counter()
     for k in range(steps):
-        ctx.step_io(1, x_in=x, v_in=v, x_out=x, v_out=v, f_out=f)
+        ctx.step_io(1, **io)
         ctx.ledger()
     t1 = time.perf_counter()
-    return {"value": n * steps / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": 2 * 24 * n,
-            "d2h_bytes_per_step": 3 * 24 * n + 32}
+    return {"value": n * steps / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": (2 * 24 * n) if full else 0,
+            "d2h_bytes_per_step": (3 * 24 * n if full else 24 * n) + 32,
+            "transfers": ("x, v host to device and x, v, f back, every step" if full else
+                          "state resident on the device; x back every step")}
 
 
 def load_peaks():

@@ -227,7 +227,13 @@ int omdg_tile_counts(omdg_ctx* ctx, int* tiles, int* staged);
  * "build_lanes" (list build: 0 cell CTAs, else threads per atom), "io_blocks"
  * (blocks of omdg_step_io's downloads beside the step's kernels), "nbr_capacity"
  * (row capacity of the next first list build; 0 sizes it from the density;
- * rows grow by themselves when a build needs more).
+ * rows grow by themselves when a build needs more), "tb_persistent" (the
+ * Tersoff register pass as one resident grid), "fuse_kick" (the step's second
+ * half-kick in the EAM force kernel's epilogue), "eam_tile" (the tiled EAM
+ * passes: one CTA per block of "tile_x" x "tile_y" x "tile_z" cells, at most
+ * "tile_cap" staged atoms; changing any of them rebuilds the list), "nn_fused"
+ * (the surrogate's descriptors computed inside its network kernel).  All are
+ * 0/1 switches or sizes; results agree across them within FP32 summation order.
  */
 int omdg_set_launch(omdg_ctx* ctx, const char* key, int value);
 int omdg_get_launch(omdg_ctx* ctx, const char* key, int* value);

@@ -386,16 +386,18 @@ __device__ __forceinline__ void ters_bond_order(const TersDev& p, float zeta, fl
         db = 0.f;
         return;
     }
+    // hardware logarithm and exponential: n ln(beta zeta) is off by ~1e-5
+    // absolute, which moves b by ~2e-7 relative (the 1/2n power damps it)
     const float x = p.beta * zeta;
-    const float nlx = p.nn * logf(x);
+    const float nlx = p.nn * __logf(x);
     if (nlx > 60.f) {
         b = rsqrtf(x);
         db = -0.5f * b / zeta;
         return;
     }
-    const float bn = expf(nlx);
-    b = exp2f((-0.5f / p.nn) * log2f(1.f + bn));  // (1 + bn)^(-1/2n), |exponent| < 2: ~3e-7 relative
-    db = -0.5f * b * bn / ((1.f + bn) * zeta);
+    const float bn = __expf(nlx);
+    b = exp2f((-0.5f / p.nn) * __log2f(1.f + bn));  // (1 + bn)^(-1/2n), |exponent| < 2: ~3e-7 relative
+    db = __fdividef(-0.5f * b * bn, (1.f + bn) * zeta);
 }
 
 __device__ __forceinline__ float ters_fc(const TersDev& p, float r, float& dfc) {
@@ -440,11 +442,11 @@ __device__ __forceinline__ void ters_bonds(const TersDev& p, const int nc, const
             if (b == a) return;
             const float c = ex_ * ux[b] + ey_ * uy[b] + ez_ * uz[b];
             const float hc = p.h - c;
-            const float rden = 1.f / (p.d2 + hc * hc);
+            const float rden = __fdividef(1.f, p.d2 + hc * hc);
             const float g = g0 - p.c2 * rden;
             const float dg = -2.f * p.c2 * hc * rden * rden;
             const float dr = rij - rr[b];
-            const float ex = expf(p.l3c * dr * dr * dr);
+            const float ex = __expf(p.l3c * dr * dr * dr);
             const float dex = 3.f * p.l3c * dr * dr * ex;
             zeta += fc[b] * g * ex;
             const float cj = fc[b] * dg * ex * ir[a], cu = fc[b] * g * dex;
@@ -455,7 +457,7 @@ __device__ __forceinline__ void ters_bonds(const TersDev& p, const int nc, const
             cc[b] = fc[b] * dg * ex * ir[b];
             cs[b] = c;
         });
-        const float fR = p.A * expf(-p.l1 * rij), fA = p.B * expf(-p.l2 * rij);
+        const float fR = p.A * __expf(-p.l1 * rij), fA = p.B * __expf(-p.l2 * rij);
         float bij, dbdz;
         ters_bond_order(p, zeta, bij, dbdz);
         const float vij = fc[a] * (fR - bij * fA);

@@ -272,11 +272,6 @@ struct GraphState {
     double* io_key[3] = {};
     long io_kernels = 0;
     bool io_valid = false;
-    // queued steps with the step boundary in one pass (k_kick_next): the
-    // first step of a batch (kick-drift, no closing kick), the middle ones
-    // (k_kick_next, no closing kick) and the last (k_kick_next, closing kick)
-    cudaGraphExec_t vexec[4] = {};
-    cudaGraph_t vgraph[4] = {};
 };
 static std::map<Context*, GraphState> g_graphs;
 
@@ -292,12 +287,6 @@ void invalidate_graph(Context* c) {
     gs.exec = gs.io_exec = nullptr;
     gs.graph = gs.io_graph = nullptr;
     gs.valid = gs.io_valid = false;
-    for (int v = 0; v < 4; v++) {
-        if (gs.vexec[v]) cudaGraphExecDestroy(gs.vexec[v]);
-        if (gs.vgraph[v]) cudaGraphDestroy(gs.vgraph[v]);
-        gs.vexec[v] = nullptr;
-        gs.vgraph[v] = nullptr;
-    }
 }
 }  // namespace omdg
 
@@ -982,14 +971,7 @@ static int eager_maybe_rebuild(Context* c) {
 // any rebuild's order) are final, f once the forces are, and v after the
 // kick, while the force and kick kernels run; the branch joins before the
 // step ends.
-// variant (with io null): 0 the whole step; 1 a batch's first step without
-// its closing kick; 2 k_kick_next (the previous step's kick and this step's
-// kick-drift), no closing kick; 3 k_kick_next and the closing kick.
-enum { STEP_WHOLE = 0, STEP_OPEN = 1, STEP_MID = 2, STEP_CLOSE = 3 };
-
-static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr, int variant = STEP_WHOLE) {
-    const bool head_next = variant == STEP_MID || variant == STEP_CLOSE;
-    const bool tail_kick = variant == STEP_WHOLE || variant == STEP_CLOSE;
+static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr) {
     cudaStream_t s = c->stream;
     if (!gs.side) cudaStreamCreateWithFlags(&gs.side, cudaStreamNonBlocking);
     if (io && !gs.io_side) {
@@ -1011,7 +993,7 @@ static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr,
     long l0 = c->launches, l1 = 0, l2 = 0;
     int rc = (c->ttm && ttm_active(c)) ? ttm_pre(c) : OMDG_OK;  // PreIntegration (TTM_Homogen_SCNA.h:352)
     if (!rc) rc = energy_source(c);                                 // PreIntegration (EnergySource.h:113)
-    if (!rc) rc = head_next ? integrate_kick_next(c) : integrate_kick_drift(c, 0);
+    if (!rc) rc = integrate_kick_drift(c, 0);
     cudaGraph_t g = nullptr;
     cudaStreamCaptureStatus cst;
     const cudaGraphNode_t* deps = nullptr;
@@ -1057,11 +1039,11 @@ static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr,
     }
     l2 = c->launches;
     if (!rc && io) rc = branch(0, io[0], nullptr, nullptr);
-    c->fuse_kick = tail_kick;  // the closing kick may ride in the force kernel
+    c->fuse_kick = true;
     if (!rc) rc = forces_compute(c);
     c->fuse_kick = false;
     if (!rc && io) rc = branch(1, nullptr, nullptr, io[2]);
-    if (!rc && tail_kick) rc = integrate_kick(c, 0);
+    if (!rc) rc = integrate_kick(c, 0);
     if (!rc && c->ttm) rc = thermo_detect(c, true);  // ExecuteDetectors (system.cpp:976)
     if (!rc && io) rc = branch(2, nullptr, io[1], nullptr);
     if (!rc && io_launches > 0) {  // join the branch
@@ -1070,12 +1052,9 @@ static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr,
         if (e != cudaSuccess) rc = check_cuda(c, e, "download join");
     }
     long l3 = c->launches;
-    // captured launches are counted when the graph replays, not here (a
-    // step without its closing kick counts as the whole step less one)
-    if (variant == STEP_WHOLE) {
-        c->graph_step_kernels = (l1 - l0) + (l3 - l2);
-        c->graph_body_kernels = l2 - l1;
-    }
+    // captured launches are counted when the graph replays, not here
+    c->graph_step_kernels = (l1 - l0) + (l3 - l2);
+    c->graph_body_kernels = l2 - l1;
     c->launches = l0;
     c->captured_builds += 1;
     cudaGraph_t graph = nullptr;
@@ -1097,9 +1076,6 @@ static int capture_step(Context* c, GraphState& gs, double* const* io = nullptr,
         gs.io_valid = true;
         for (int k = 0; k < 3; k++) gs.io_key[k] = io[k];
         gs.io_kernels = io_launches;
-    } else if (variant != STEP_WHOLE) {
-        gs.vgraph[variant] = graph;
-        gs.vexec[variant] = exec;
     } else {
         gs.graph = graph;
         gs.exec = exec;
@@ -1414,22 +1390,9 @@ int omdg_step_async(omdg_ctx* c, int nsteps) {
         if (!gs.valid) {
             if ((rc = capture_step(c, gs))) return rc;
         }
-        if (nsteps >= 2 && kick_next_ok(c)) {
-            // every step boundary of the batch in one pass; the batch's last
-            // step closes with its kick, so no half-kick outlives the call
-            for (int v = STEP_OPEN; v <= STEP_CLOSE; v++)
-                if (!gs.vexec[v] && (rc = capture_step(c, gs, nullptr, v))) return rc;
-            for (int k = 0; k < nsteps; k++) {
-                const int v = k == 0 ? STEP_OPEN : (k == nsteps - 1 ? STEP_CLOSE : STEP_MID);
-                cudaError_t e = cudaGraphLaunch(gs.vexec[v], c->stream);
-                if (e != cudaSuccess) return check_cuda(c, e, "graph launch");
-            }
-            c->merged_kicks += nsteps - 1;
-        } else {
-            for (int k = 0; k < nsteps; k++) {
-                cudaError_t e = cudaGraphLaunch(gs.exec, c->stream);
-                if (e != cudaSuccess) return check_cuda(c, e, "graph launch");
-            }
+        for (int k = 0; k < nsteps; k++) {
+            cudaError_t e = cudaGraphLaunch(gs.exec, c->stream);
+            if (e != cudaSuccess) return check_cuda(c, e, "graph launch");
         }
         c->graph_steps += nsteps;
     }
@@ -1813,9 +1776,7 @@ int omdg_stats(omdg_ctx* c, long* rebuilds, long* launches) {
     long eager = c->rebuilds - c->captured_builds;
     if (rebuilds) *rebuilds = eager + graph_builds;
     // kernels issued so far: eager launches plus graph replays
-    if (launches)
-        *launches = c->launches + c->graph_steps * c->graph_step_kernels + graph_builds * c->graph_body_kernels -
-                    c->merged_kicks;
+    if (launches) *launches = c->launches + c->graph_steps * c->graph_step_kernels + graph_builds * c->graph_body_kernels;
     (void)gs;
     return OMDG_OK;
 }
@@ -1904,7 +1865,6 @@ static int* launch_knob(Context* c, const std::string& k) {
     if (k == "nbr_capacity") return &c->nbr_capacity;
     if (k == "eam_tile") return &c->eam_tile;
     if (k == "nn_fused") return &c->nn_fused;
-    if (k == "vv_merge") return &c->vv_merge;
     if (k == "tile_x") return &c->tile_dim[0];
     if (k == "tile_y") return &c->tile_dim[1];
     if (k == "tile_z") return &c->tile_dim[2];
@@ -1922,7 +1882,7 @@ static bool valid_knob(const std::string& k, int v) {
     if (k == "build_lanes") return v == 0 || v == 1 || v == 4 || v == 8;
     if (k == "io_blocks") return v >= 1 && v <= 65535;
     if (k == "nbr_capacity") return v >= 0 && v <= 4096;
-    if (k == "eam_tile" || k == "nn_fused" || k == "vv_merge") return v == 0 || v == 1;
+    if (k == "eam_tile" || k == "nn_fused") return v == 0 || v == 1;
     if (k == "tile_x" || k == "tile_y" || k == "tile_z") return v >= 1 && v <= 4;
     if (k == "tile_cap") return v >= 64 && v <= 5000;
     return false;

@@ -21,18 +21,16 @@
 
 namespace omdg {
 
-// The first half-kick and the drift of atom i, with the position pack, the
-// displacement check and RangeLimiter; every thread of the block calls it
-// (a block flag collects the moves).
-__device__ __forceinline__ void kick_drift_atom(const IntParams& p, int i, double* __restrict__ x,
-                                                double* __restrict__ y, double* __restrict__ z,
-                                                double* __restrict__ vx, double* __restrict__ vy,
-                                                double* __restrict__ vz, const float* __restrict__ fx,
-                                                const float* __restrict__ fy, const float* __restrict__ fz,
-                                                const double* __restrict__ f64, const int* __restrict__ type,
-                                                PosPack* __restrict__ pack, const float4* __restrict__ xref,
-                                                unsigned* __restrict__ aflag, StepState* st,
-                                                const int* __restrict__ rep_of, int* __restrict__ rflag) {
+__global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
+                                                    double* __restrict__ z, double* __restrict__ vx,
+                                                    double* __restrict__ vy, double* __restrict__ vz,
+                                                    const float* __restrict__ fx, const float* __restrict__ fy,
+                                                    const float* __restrict__ fz, const double* __restrict__ f64,
+                                                    const int* __restrict__ type, PosPack* __restrict__ pack,
+                                                    const float4* __restrict__ xref, unsigned* __restrict__ aflag,
+                                                    StepState* st, const int* __restrict__ rep_of,
+                                                    int* __restrict__ rflag) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
     __shared__ int moved;
     if (threadIdx.x == 0) moved = 0;
     __syncthreads();
@@ -105,52 +103,6 @@ __device__ __forceinline__ void kick_drift_atom(const IntParams& p, int i, doubl
     if (self_moved && rflag) rflag[rep_of[i]] = 1;
     __syncthreads();
     if (threadIdx.x == 0 && moved) st->rebuild = 1;
-}
-
-__global__ void __launch_bounds__(256, 8) k_kick_drift(IntParams p, double* __restrict__ x, double* __restrict__ y,
-                                                    double* __restrict__ z, double* __restrict__ vx,
-                                                    double* __restrict__ vy, double* __restrict__ vz,
-                                                    const float* __restrict__ fx, const float* __restrict__ fy,
-                                                    const float* __restrict__ fz, const double* __restrict__ f64,
-                                                    const int* __restrict__ type, PosPack* __restrict__ pack,
-                                                    const float4* __restrict__ xref, unsigned* __restrict__ aflag,
-                                                    StepState* st, const int* __restrict__ rep_of,
-                                                    int* __restrict__ rflag) {
-    kick_drift_atom(p, blockIdx.x * blockDim.x + threadIdx.x, x, y, z, vx, vy, vz, fx, fy, fz, f64, type, pack, xref,
-                    aflag, st, rep_of, rflag);
-}
-
-// One step's second half-kick with its ledger and the next step's first
-// half-kick and drift, in one pass over the atoms: k_kick's and
-// k_kick_drift's operations on each atom in their order, so the trajectory
-// and the ledger equal those of the two kernels bit for bit.  For runs in
-// which nothing acts between the two (no thermostat, no time-step change, no
-// detectors, no energy source, FP32 forces); the kick's terms wait in shared
-// memory while the thread drifts.
-__global__ void __launch_bounds__(RED_BLOCK, 6) k_kick_next(
-    IntParams p, FinParams f, double* __restrict__ x, double* __restrict__ y, double* __restrict__ z,
-    double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz, const float* __restrict__ fx,
-    const float* __restrict__ fy, const float* __restrict__ fz, const int* __restrict__ type,
-    const float* __restrict__ pe, const float* __restrict__ vir, PosPack* __restrict__ pack,
-    const float4* __restrict__ xref, unsigned* __restrict__ aflag, StepState* st, const int* __restrict__ rep_of,
-    int* __restrict__ rflag, BlockPartial* __restrict__ partial, double* __restrict__ ledger) {
-    const int i = blockIdx.x * RED_BLOCK + threadIdx.x;
-    __shared__ F2 s_k[RED_BLOCK], s_e[RED_BLOCK], s_w[RED_BLOCK];
-    __shared__ unsigned long long s_v[RED_BLOCK];
-    {
-        F2 k = {0.f, 0.f}, e = {0.f, 0.f}, w = {0.f, 0.f};
-        unsigned long long vmax = 0ull;
-        if (i < p.n && (!aflag || (aflag[i] & 1u))) {
-            const int t = type[i];
-            kick_atom_terms(p, i, t, fx[i], fy[i], fz[i], pe[i], vir[i], st->hdtm[t], vx, vy, vz, k, e, w, vmax);
-        }
-        s_k[threadIdx.x] = k;
-        s_e[threadIdx.x] = e;
-        s_w[threadIdx.x] = w;
-        s_v[threadIdx.x] = vmax;
-    }
-    kick_drift_atom(p, i, x, y, z, vx, vy, vz, fx, fy, fz, nullptr, type, pack, xref, aflag, st, rep_of, rflag);
-    ledger_block(p, f, s_k[threadIdx.x], s_e[threadIdx.x], s_w[threadIdx.x], s_v[threadIdx.x], partial, ledger, st);
 }
 
 
@@ -513,27 +465,6 @@ static int reduce_and_finalize(Context* c, int kick, int count_step) {
 }
 
 int integrate_kick(Context* c, int) { return reduce_and_finalize(c, 1, 1); }
-
-// The step boundary in one pass (k_kick_next): the step's second half-kick
-// and ledger row, then the next step's first half-kick and drift.
-bool kick_next_ok(const Context* c) {
-    return c->vv_merge && !c->profiling && !(c->thermo_tau > 0.0) && c->dyn_update == 0 && !c->src_on && !c->ttm &&
-           !c->use_f64;
-}
-
-int integrate_kick_next(Context* c) {
-    IntParams p = int_params(c);
-    FinParams f = fin_params(c, p, 1);
-    prof_begin(c, "kick_next");
-    k_kick_next<<<grid_for(c->n, RED_BLOCK), RED_BLOCK, 0, c->stream>>>(
-        p, f, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->fx, c->fy, c->fz, c->type, c->pe, c->vir, c->pack, c->xref,
-        c->flags_used ? c->aflag : nullptr, reinterpret_cast<StepState*>(c->d_state),
-        c->nrep > 0 ? c->d_rep_of : nullptr, c->nrep > 0 ? c->d_rep_flag : nullptr,
-        reinterpret_cast<BlockPartial*>(c->d_red), c->d_ledger);
-    prof_end(c);
-    c->launches++;
-    return check_cuda(c, cudaGetLastError(), "kick_next");
-}
 
 int measure_energies(Context* c, int) { return reduce_and_finalize(c, 0, 0); }
 

@@ -263,8 +263,6 @@ struct Context {
     int tb_block = 128;        // three-body kernels
     int tb_lanes = 1;
     int tb_persistent = 0;     // Tersoff register pass: one resident grid striding over the flattened atoms
-    int vv_merge = 1;          // queued steps join one step's second half-kick to the next one's first (k_kick_next)
-    long merged_kicks = 0;     // step boundaries taken by k_kick_next (one kernel fewer each)
     int nn_fused = 0;          // the surrogate's descriptors computed inside its tensor-core network kernel (opt-in:
                                // with four 128-thread CTAs per SM the descriptor work runs slower there)
     int fuse_kick_on = 0;      // a step's second half-kick in the force kernel's epilogue where it can go (opt-in:
@@ -388,11 +386,6 @@ int zbl_launch(Context* c, Potential& p, bool first);
 // integrator (integrate.cu)
 int integrate_kick_drift(Context* c, int step_index);
 int integrate_kick(Context* c, int step_index);
-// the step boundary in one pass: a step's second half-kick and ledger row,
-// then the next step's first half-kick and drift (kick_next_ok: nothing acts
-// between them in this context)
-bool kick_next_ok(const Context* c);
-int integrate_kick_next(Context* c);
 int integrate_pack(Context* c);
 int measure_energies(Context* c, int row);
 int zero_forces(Context* c);

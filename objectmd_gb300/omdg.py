@@ -824,7 +824,7 @@ class Context:
 
     def launch_shapes(self):
         keys = ("eam_block", "eam_lanes", "eam_stage", "eam_ctas_per_sm", "pair_block", "pair_lanes", "tb_block",
-                "tb_lanes", "tb_persistent", "fuse_kick", "nbr_hshift", "build_lanes", "io_blocks", "vv_merge", "nn_fused", "eam_tile",
+                "tb_lanes", "tb_persistent", "fuse_kick", "nbr_hshift", "build_lanes", "io_blocks", "nn_fused", "eam_tile",
                 "tile_x", "tile_y", "tile_z", "tile_cap")
         return {k: self.get_launch(k) for k in keys}
 

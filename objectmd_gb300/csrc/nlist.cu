@@ -562,7 +562,8 @@ struct RepGrid {
     __device__ int cell_base() const { return r->cell_base; }
 };
 
-template <class G>
+
+template <bool TILES, class G>
 __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int i, const float4* __restrict__ loc,
                                           const double* __restrict__ x, const double* __restrict__ y,
                                           const double* __restrict__ z, const int* __restrict__ cell,
@@ -590,7 +591,7 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
     const unsigned short* tsb = nullptr;
     unsigned short* trow = nullptr;
     int tox = 0, toy = 0, toz = 0;
-    if (p.to.slot) {
+    if (TILES) {
         const int tx = cx / p.to.T[0], ty = cy / p.to.T[1], tz = cz / p.to.T[2];
         const int t = (tz * p.to.nt[1] + ty) * p.to.nt[0] + tx;
         if (p.to.nst[t] <= p.to.cap) {
@@ -630,7 +631,8 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
                 const unsigned code = nbr_encode(0, sx, sy, sz);
                 const int e = start[c + 1];
                 // slot of candidate k in the tile's staged halo: tb + k
-                const int tb = trow ? (int)tsb[((toz + a) * p.to.hy + (toy + b)) * p.to.hx + (tox + q)] - start[c] : 0;
+                const int tb =
+                    TILES && trow ? (int)tsb[((toz + a) * p.to.hy + (toy + b)) * p.to.hx + (tox + q)] - start[c] : 0;
                 for (int k = start[c]; k < e; k++) {
                     const float4 uk = loc[k];
                     const float dx = px - uk.x, dy = py - uk.y, dz = pz - uk.z;
@@ -645,7 +647,7 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
                     tmask |= 1u << (__float_as_int(uk.w) & 31);
                     if (cnt < p.maxnb) {
                         nbr[nbr_at(i, cnt, p.hshift, p.maxnb)] = code | (unsigned)k;
-                        if (trow) trow[cnt] = (unsigned short)(tb + k);
+                        if (TILES && trow) trow[cnt] = (unsigned short)(tb + k);
                     }
                     cnt++;
                 }
@@ -662,7 +664,8 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
 }
 
 // REP: the atom's replica supplies the grid, reference points and lengths.
-template <bool REP>
+// TILES: the rows also go out as EAM tile slots.
+template <bool REP, bool TILES = false>
 __global__ void __launch_bounds__(128) k_build(BuildParams p, const RepGeom* __restrict__ rg,
                                                const int* __restrict__ rep_of, const float4* __restrict__ loc,
                                                const double* __restrict__ x, const double* __restrict__ y,
@@ -675,9 +678,10 @@ __global__ void __launch_bounds__(128) k_build(BuildParams p, const RepGeom* __r
     if (i >= p.n) return;
     if (REP && rflag && !rflag[rep_of[i]]) return;  // the replica keeps its list
     if (REP)
-        build_row(p, RepGrid{rg + rep_of[i]}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need, nbmask);
+        build_row<false>(p, RepGrid{rg + rep_of[i]}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need,
+                         nbmask);
     else
-        build_row(p, BoxGrid{p}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need, nbmask);
+        build_row<TILES>(p, BoxGrid{p}, i, loc, x, y, z, cell, start, umax, nbr, nnb, status, need, nbmask);
 }
 
 // ------------------------------------------------------------------ EAM cell tiles
@@ -1426,7 +1430,12 @@ int nlist_build(Context* c) {
         k_build<true><<<grid_for(n, 128), 128, 0, s>>>(bp, rg, c->d_rep_of, c->loc, c->x, c->y, c->z, cell_sorted,
                                                        c->cell_start, umax, reinterpret_cast<unsigned*>(c->nbr),
                                                        c->nnb, c->d_status, c->d_flags + 1, rflag, c->nbmask);
-    } else if (c->flags_used || tiles) {  // only the cell-local build skips inactive atoms and writes tile slots
+    } else if (tiles) {  // only the cell-local build writes tile slots
+        k_build<false, true><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
+                                                              cell_sorted, c->cell_start, umax,
+                                                              reinterpret_cast<unsigned*>(c->nbr), c->nnb,
+                                                              c->d_status, c->d_flags + 1, nullptr, c->nbmask);
+    } else if (c->flags_used) {  // only the cell-local build skips inactive atoms
         k_build<false><<<grid_for(n, 128), 128, 0, s>>>(bp, nullptr, nullptr, c->loc, c->x, c->y, c->z,
                                                         cell_sorted, c->cell_start, umax,
                                                         reinterpret_cast<unsigned*>(c->nbr), c->nnb, c->d_status,

@@ -666,7 +666,7 @@ __device__ __forceinline__ void build_row(const BuildParams& p, const G& g, int 
 // REP: the atom's replica supplies the grid, reference points and lengths.
 // TILES: the rows also go out as EAM tile slots.
 template <bool REP, bool TILES = false>
-__global__ void __launch_bounds__(128) k_build(BuildParams p, const RepGeom* __restrict__ rg,
+__global__ void __launch_bounds__(128, REP ? 7 : 8) k_build(BuildParams p, const RepGeom* __restrict__ rg,
                                                const int* __restrict__ rep_of, const float4* __restrict__ loc,
                                                const double* __restrict__ x, const double* __restrict__ y,
                                                const double* __restrict__ z, const int* __restrict__ cell,

@@ -203,6 +203,8 @@ __device__ __noinline__ void sw_centre_wide(const SWDev& p, int i, const PosPack
 }
 
 constexpr int SW_REG = 8;  // in-cutoff neighbours the register path holds (diamond: 4 + thermal second shell)
+// k_sw_a at six 128-thread blocks a SM (85 registers, a few spilled) ran the
+// Si 512k step faster than at its natural 121 registers (427 vs 458 us)
 
 __device__ __forceinline__ void sw_store(const SWDev& p, int i, float ax, float ay, float az, float ae,
                                          float* __restrict__ fx, float* __restrict__ fy, float* __restrict__ fz,
@@ -224,7 +226,7 @@ __device__ __forceinline__ void sw_store(const SWDev& p, int i, float ax, float 
 // registers (fully unrolled loops, insertion by select); centres with more
 // are queued for k_sw_wide.  Same terms and summation order as the wide
 // path.
-__global__ void __launch_bounds__(128) k_sw_a(SWDev p, const PosPack* __restrict__ pack,
+__global__ void __launch_bounds__(128, 6) k_sw_a(SWDev p, const PosPack* __restrict__ pack,
                                               const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                               float4* __restrict__ slot, float* __restrict__ fx,
                                               float* __restrict__ fy, float* __restrict__ fz, float* __restrict__ pe,

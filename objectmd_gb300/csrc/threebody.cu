@@ -203,8 +203,8 @@ __device__ __noinline__ void sw_centre_wide(const SWDev& p, int i, const PosPack
 }
 
 constexpr int SW_REG = 8;  // in-cutoff neighbours the register path holds (diamond: 4 + thermal second shell)
-// k_sw_a at six 128-thread blocks a SM (85 registers, a few spilled) ran the
-// Si 512k step faster than at its natural 121 registers (427 vs 458 us)
+// k_sw_a at six 128-thread blocks a SM (80 registers, 252 bytes spilled) ran
+// the Si 512k step faster than at its natural 121 registers (427 vs 458 us)
 
 __device__ __forceinline__ void sw_store(const SWDev& p, int i, float ax, float ay, float az, float ae,
                                          float* __restrict__ fx, float* __restrict__ fy, float* __restrict__ fz,

@@ -262,6 +262,16 @@ def mean_neighbours(ctx):
 MLP_FLOP_PER_ATOM = 2 * (32 * 64 + 64 * 64 + 64 * 64 + 64 * 32)
 
 
+def mlp_roof(kernels, n):
+    """The surrogate network kernel against the measured sustained BF16 rate."""
+    t = kernels["nn_mlp"]["ms_per_launch"]
+    tf = MLP_FLOP_PER_ATOM * n / (t * 1e-3) / 1e12
+    sus = load_peaks().get("bf16_sustained")
+    return {"bound": "tensor", "kernel": "nn_mlp", "flop_per_atom": MLP_FLOP_PER_ATOM, "achieved": round(tf, 2),
+            "peak": sus, "unit": "TFLOP/s", "frac": round(tf / sus, 4) if sus else None,
+            "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops_sustained)"}
+
+
 def load_inst(kernel):
     """Warp instructions per atom of one launch (committed ncu figures)."""
     p = os.path.join(ROOT, "profiles", "instructions_per_atom.txt")
@@ -386,13 +396,7 @@ def sub_workload(name, args, device, torch, flush_l2):
                            "peak_source": peaks["src"], "alg_bytes_per_launch": int(alg)}
         out["issue_roofline"] = issue_roof(dom_name, n, dom["ms_per_launch"], torch, device)
     if "nn_mlp" in kernels:
-        t = kernels["nn_mlp"]["ms_per_launch"]
-        tf = MLP_FLOP_PER_ATOM * n / (t * 1e-3) / 1e12
-        sus = load_peaks().get("bf16_sustained")
-        out["mlp_roofline"] = {"bound": "tensor", "kernel": "nn_mlp", "flop_per_atom": MLP_FLOP_PER_ATOM,
-                               "achieved": round(tf, 2), "peak": sus, "unit": "TFLOP/s",
-                               "frac": round(tf / sus, 4) if sus else None,
-                               "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops_sustained)"}
+        out["mlp_roofline"] = mlp_roof(kernels, n)
     if w["kind"] == "nn":
         out["surrogate"] = surrogate_report(ctx, w, x, v, lo, hi, device, args, torch)
     ctx.close()
@@ -550,6 +554,8 @@ def run_gpu(args):
         "issue_roofline": issue,
         "wall_s_timed_loop": t_wall1 - t_wall0,
     }
+    if "nn_mlp" in kernels:
+        out["mlp_roofline"] = mlp_roof(kernels, n)
     # the other headline workloads, as sub-objects of the same line
     if args.workload == "eam_al_256k" and not args.ncell and not args.no_sub and world == 1:
         ctx.close()

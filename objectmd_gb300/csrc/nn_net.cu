@@ -247,6 +247,7 @@ struct MLPSmem {
 };
 static_assert(sizeof(__nv_bfloat16) * NN_IMG_ELEMS == offsetof(MLPSmem, vec), "image order");
 static_assert(offsetof(MLPSmem, x) % 16 == 0 && offsetof(MLPSmem, h) % 16 == 0, "operand alignment");
+static_assert(sizeof(MLPSmem::h) >= sizeof(float) * MLP_ROWS * NN_DESC, "dE/dG rows staged in h");
 
 // tanh x = 1 - 2 / (e^{2x} + 1), branch-free with the hardware exponential
 // and reciprocal: an absolute error of a few 1e-7 (the activations then round
@@ -264,6 +265,16 @@ __device__ __forceinline__ uint4 pack8(const float* v) {
     r.y = *reinterpret_cast<uint32_t*>(&p1);
     r.z = *reinterpret_cast<uint32_t*>(&p2);
     r.w = *reinterpret_cast<uint32_t*>(&p3);
+    return r;
+}
+
+// four values -> 8 bytes (the pairs pack8 makes)
+__device__ __forceinline__ uint2 pack4(const float4& v) {
+    uint2 r;
+    __nv_bfloat162 p0 = __floats2bfloat162_rn(v.x, v.y);
+    __nv_bfloat162 p1 = __floats2bfloat162_rn(v.z, v.w);
+    r.x = *reinterpret_cast<uint32_t*>(&p0);
+    r.y = *reinterpret_cast<uint32_t*>(&p1);
     return r;
 }
 
@@ -374,25 +385,20 @@ __global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __r
     for (int tile = blockIdx.x; tile < ntiles && !S.abort; tile += gridDim.x) {
         const int row = tile * MLP_ROWS + t;
         const bool valid = row < rows;
-        {
+        // the warp's rows [r0, r0 + 32): one contiguous run of 256 float4 in
+        // the row-major descriptor and dE/dG arrays; lane l moves float4
+        // j*32 + l (row (j*32 + l) / 8, quarter (j*32 + l) % 8), so every
+        // global access of the warp is 512 contiguous bytes
+        const int lane = t & 31, r0 = tile * MLP_ROWS + warp * 32;
+        if (MD) {
             float g[NN_DESC];
-            if (MD && valid) {
+            if (valid) {
                 nn_md_descriptors(in.q, in.dp, row, in.pack, in.nbr, in.nnb[row], g, status);
                 const bool out = nn_out_of_range(in.dp, g);
                 in.flag[row] = out ? 1 : 0;
                 if (out) atomicAdd(in.count, 1);
 #pragma unroll
                 for (int k = 0; k < NN_DESC; k++) g[k] = (g[k] - in.dp.mu[k]) * in.dp.isig[k];
-            } else if (valid) {
-                const float4* src = reinterpret_cast<const float4*>(in.gt + (size_t)row * NN_DESC);
-#pragma unroll
-                for (int q = 0; q < NN_DESC / 4; q++) {
-                    const float4 v = __ldg(src + q);
-                    g[4 * q] = v.x;
-                    g[4 * q + 1] = v.y;
-                    g[4 * q + 2] = v.z;
-                    g[4 * q + 3] = v.w;
-                }
             } else {
 #pragma unroll
                 for (int k = 0; k < NN_DESC; k++) g[k] = 0.f;
@@ -400,8 +406,26 @@ __global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __r
 #pragma unroll
             for (int k8 = 0; k8 < NN_DESC / 8; k8++)
                 *reinterpret_cast<uint4*>(&S.x[tc_tile_off(t, k8 * 8, NN_DESC)]) = pack8(g + 8 * k8);
+        } else {
+            const float4* src = reinterpret_cast<const float4*>(in.gt) + (size_t)r0 * (NN_DESC / 4);
+            float4 v[NN_DESC / 4];
+#pragma unroll
+            for (int j = 0; j < NN_DESC / 4; j++) {
+                const int idx = j * 32 + lane;
+                v[j] = r0 + (idx >> 3) < rows ? __ldg(src + idx) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int j = 0; j < NN_DESC / 4; j++) {
+                const int idx = j * 32 + lane;
+                *reinterpret_cast<uint2*>(&S.x[tc_tile_off(warp * 32 + (idx >> 3), 4 * (idx & 7), NN_DESC)]) =
+                    pack4(v[j]);
+            }
         }
         tc_handoff();
+        // Epilogues work on 32 TMEM columns at a time, and a1 is not kept
+        // across the MMAs: z1 stays in columns [0, 64) until delta1, which
+        // recomputes a1 from it (the same values), so no row of 64 floats
+        // lives through a round trip.
         // z1 -> TMEM columns [0, 64)
         if (t == 0) {
             tc_gemm(tmem, sx, sw1, NN_DESC, ID64);
@@ -410,13 +434,16 @@ __global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __r
         mbar_wait_or_drain(&S.bar_mma, phase, polls, S.abort);
         phase ^= 1u;
         tc_fence_after();
-        float a1[NN_H];
-        tc_ld64(lane_base, a1);
+#pragma unroll 1
+        for (int c = 0; c < NN_H; c += 32) {
+            float a1[32];
+            tc_ld32(lane_base + c, a1);
 #pragma unroll
-        for (int k = 0; k < NN_H; k++) a1[k] = nn_tanh(a1[k] + b1[k]);
+            for (int k = 0; k < 32; k++) a1[k] = nn_tanh(a1[k] + b1[c + k]);
 #pragma unroll
-        for (int k8 = 0; k8 < NN_H / 8; k8++)
-            *reinterpret_cast<uint4*>(&S.h[tc_tile_off(t, k8 * 8, NN_H)]) = pack8(a1 + 8 * k8);
+            for (int k8 = 0; k8 < 4; k8++)
+                *reinterpret_cast<uint4*>(&S.h[tc_tile_off(t, c + k8 * 8, NN_H)]) = pack8(a1 + 8 * k8);
+        }
         tc_handoff();
         if (S.abort) break;
         // z2 -> columns [64, 128)
@@ -428,37 +455,57 @@ __global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __r
         phase ^= 1u;
         tc_fence_after();
         float e = S.vec[NN_VEC_B3];
-        {
-            float z[NN_H];
-            tc_ld64(lane_base + 64, z);
+#pragma unroll 1
+        for (int c = 0; c < NN_H; c += 32) {
+            float z[32];
+            tc_ld32(lane_base + 64 + c, z);
 #pragma unroll
-            for (int k = 0; k < NN_H; k++) {
-                const float a2 = nn_tanh(z[k] + b2[k]);
-                e = fmaf(w3[k], a2, e);
-                z[k] = w3[k] * (1.f - a2 * a2);  // delta2
+            for (int k = 0; k < 32; k++) {
+                const float a2 = nn_tanh(z[k] + b2[c + k]);
+                e = fmaf(w3[c + k], a2, e);
+                z[k] = w3[c + k] * (1.f - a2 * a2);  // delta2
             }
 #pragma unroll
-            for (int k8 = 0; k8 < NN_H / 8; k8++)
-                *reinterpret_cast<uint4*>(&S.h[tc_tile_off(t, k8 * 8, NN_H)]) = pack8(z + 8 * k8);
+            for (int k8 = 0; k8 < 4; k8++)
+                *reinterpret_cast<uint4*>(&S.h[tc_tile_off(t, c + k8 * 8, NN_H)]) = pack8(z + 8 * k8);
         }
         tc_handoff();
         if (S.abort) break;
-        // g1 = delta2 W2 -> columns [0, 64)
+        // g1 = delta2 W2 -> columns [64, 128) (z2 is spent; z1 stays)
         if (t == 0) {
-            tc_gemm(tmem, sh, sw2t, NN_H, ID64);
+            tc_gemm(tmem + 64, sh, sw2t, NN_H, ID64);
             tc_commit(&S.bar_mma);
         }
         mbar_wait_or_drain(&S.bar_mma, phase, polls, S.abort);
         phase ^= 1u;
         tc_fence_after();
-        {
-            float g1[NN_H];
-            tc_ld64(lane_base, g1);
+#pragma unroll 1
+        for (int c = 0; c < NN_H; c += 32) {
+            float g1[32], z1[32];
+            uint32_t r0[16], r1[16], r2[16], r3[16];
+            tc_ld16(lane_base + 64 + c, r0);
+            tc_ld16(lane_base + 64 + c + 16, r1);
+            tc_ld16(lane_base + c, r2);
+            tc_ld16(lane_base + c + 16, r3);
+            tc_wait_ld(r0);
+            tc_wait_ld(r1);
+            tc_wait_ld(r2);
+            tc_wait_ld(r3);
 #pragma unroll
-            for (int k = 0; k < NN_H; k++) g1[k] *= 1.f - a1[k] * a1[k];  // delta1
+            for (int k = 0; k < 16; k++) {
+                g1[k] = __uint_as_float(r0[k]);
+                g1[16 + k] = __uint_as_float(r1[k]);
+                z1[k] = __uint_as_float(r2[k]);
+                z1[16 + k] = __uint_as_float(r3[k]);
+            }
 #pragma unroll
-            for (int k8 = 0; k8 < NN_H / 8; k8++)
-                *reinterpret_cast<uint4*>(&S.h[tc_tile_off(t, k8 * 8, NN_H)]) = pack8(g1 + 8 * k8);
+            for (int k = 0; k < 32; k++) {
+                const float a1 = nn_tanh(z1[k] + b1[c + k]);
+                g1[k] *= 1.f - a1 * a1;  // delta1
+            }
+#pragma unroll
+            for (int k8 = 0; k8 < 4; k8++)
+                *reinterpret_cast<uint4*>(&S.h[tc_tile_off(t, c + k8 * 8, NN_H)]) = pack8(g1 + 8 * k8);
         }
         tc_handoff();
         if (S.abort) break;
@@ -473,13 +520,23 @@ __global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __r
         {
             float u[NN_DESC];
             tc_ld32(lane_base + 64, u);
-            if (valid) {
-                E[row] = e;
-                float4* dst = reinterpret_cast<float4*>(U + (size_t)row * NN_DESC);
+            if (valid) E[row] = e;
+            // dE/dG rows leave through the warp's quarter of S.h (free: the
+            // last MMA has read it), a row's float4 q at slot q ^ (row & 7) so
+            // that neither the row-wise writes nor the run-wise reads meet a
+            // bank conflict; then the same contiguous runs as the loads
+            float4* st = reinterpret_cast<float4*>(S.h) + warp * 32 * (NN_DESC / 4);
 #pragma unroll
-                for (int q = 0; q < NN_DESC / 4; q++)
-                    dst[q] = make_float4(u[4 * q] * isig[4 * q], u[4 * q + 1] * isig[4 * q + 1],
-                                         u[4 * q + 2] * isig[4 * q + 2], u[4 * q + 3] * isig[4 * q + 3]);
+            for (int q = 0; q < NN_DESC / 4; q++)
+                st[lane * (NN_DESC / 4) + (q ^ (lane & 7))] =
+                    make_float4(u[4 * q] * isig[4 * q], u[4 * q + 1] * isig[4 * q + 1],
+                                u[4 * q + 2] * isig[4 * q + 2], u[4 * q + 3] * isig[4 * q + 3]);
+            __syncwarp();
+            float4* dst = reinterpret_cast<float4*>(U) + (size_t)r0 * (NN_DESC / 4);
+#pragma unroll
+            for (int j = 0; j < NN_DESC / 4; j++) {
+                const int idx = j * 32 + lane, r = idx >> 3;
+                if (r0 + r < rows) dst[idx] = st[r * (NN_DESC / 4) + ((idx & 7) ^ (r & 7))];
             }
         }
         // TMEM reads done before the next tile's MMAs overwrite the columns

@@ -56,21 +56,37 @@ struct NNAngExp {
     }
 };
 
+// The default angular set's layout: term m has zeta 2^((m >> 1) & 3) and
+// lambda +1 for even m, -1 for odd m (two eta groups of eight).  Kernels
+// built for it (STD) take zeta and lambda as constants of the unrolled term
+// loop, so the powers of the two bases 1 +- cos are formed once per pair and
+// shared by the terms (the same products in the same order as nn_ipow).
+__host__ __device__ constexpr int nn_std_zeta(int m) { return 1 << ((m >> 1) & 3); }
+__host__ __device__ constexpr float nn_std_lam(int m) { return (m & 1) ? -1.f : 1.f; }
+
+inline bool nn_std_angular(const NNDescParams& p) {
+    for (int m = 0; m < NN_ANG; m++)
+        if (p.zeta[m] != nn_std_zeta(m) || p.lam[m] != nn_std_lam(m)) return false;
+    return true;
+}
+
 // Angular term m of the neighbour pair (a, b): the value and its derivatives
 // with respect to r_a, r_b and cos(theta); ex = exp(-eta_a[m] (r_a^2 + r_b^2)).
+template <bool STD = false>
 __device__ __forceinline__ void nn_angular(const NNDescParams& p, int m, float ra, float rb, float cs, float fa,
                                            float dfa, float fb, float dfb, float ex, float& val, float& d_ra,
                                            float& d_rb, float& d_cs) {
-    float base = 1.f + p.lam[m] * cs;
+    const float lam = STD ? nn_std_lam(m) : p.lam[m];
+    float base = 1.f + lam * cs;
     base = base > 0.f ? base : 0.f;
-    const int z = p.zeta[m];
+    const int z = STD ? nn_std_zeta(m) : p.zeta[m];
     const float pm1 = nn_ipow(base, z - 1);
     const float pw = pm1 * base;
     const float k = p.pref[m] * ex;
     val = k * pw * fa * fb;
     d_ra = k * pw * fb * (dfa - 2.f * p.eta_a[m] * ra * fa);
     d_rb = k * pw * fa * (dfb - 2.f * p.eta_a[m] * rb * fb);
-    d_cs = base > 0.f ? k * (float)z * pm1 * p.lam[m] * fa * fb : 0.f;
+    d_cs = base > 0.f ? k * (float)z * pm1 * lam * fa * fb : 0.f;
 }
 
 }  // namespace omdg

@@ -82,9 +82,10 @@ cudaError_t nn_mlp_launch(const NNDevNet& net, const float* gt, int rows, float*
                           int num_sms, cudaStream_t s);
 // The same network with each row's descriptors computed in the kernel from
 // the Verlet list (MD): flags atoms outside the training range and counts them.
+// std_ang: the descriptor set has the default angular layout.
 struct NNMD;
-cudaError_t nn_mlp_md_launch(const NNDevNet& net, const NNMD& q, const NNDescParams& dp, const PosPack* pack,
-                             const unsigned* nbr, const int* nnb, int* flag, int* count, float* E, float* u,
-                             unsigned* status, int num_sms, cudaStream_t s);
+cudaError_t nn_mlp_md_launch(const NNDevNet& net, const NNMD& q, const NNDescParams& dp, bool std_ang,
+                             const PosPack* pack, const unsigned* nbr, const int* nnb, int* flag, int* count,
+                             float* E, float* u, unsigned* status, int num_sms, cudaStream_t s);
 
 }  // namespace omdg

@@ -43,7 +43,8 @@ __device__ __forceinline__ int nn_gather(const NNMD& q, const NNDescParams& p, i
 }
 
 // Raw descriptors g[32] of atom i (radial, then angular over its neighbour
-// pairs inside the cutoff).
+// pairs inside the cutoff); STD: the default angular layout.
+template <bool STD>
 __device__ __forceinline__ void nn_md_descriptors(const NNMD& q, const NNDescParams& p, int i,
                                                   const PosPack* __restrict__ pack, const unsigned* __restrict__ nbr,
                                                   int m, float* g, unsigned* status) {
@@ -75,7 +76,7 @@ __device__ __forceinline__ void nn_md_descriptors(const NNMD& q, const NNDescPar
 #pragma unroll
             for (int m2 = 0; m2 < NN_ANG; m2++) {
                 float v, d1, d2, d3;
-                nn_angular(p, m2, rr[a], rr[b], cs, fa, dfa, fb, dfb, ex.get(p.eta_a[m2], s2), v, d1, d2, d3);
+                nn_angular<STD>(p, m2, rr[a], rr[b], cs, fa, dfa, fb, dfb, ex.get(p.eta_a[m2], s2), v, d1, d2, d3);
                 g[NN_RAD + m2] += v;
             }
         }

@@ -341,7 +341,8 @@ struct MLPInput {
     int* count;
 };
 
-template <bool MD>
+// MD: descriptors from the Verlet list (STD: the default angular layout).
+template <bool MD, bool STD = false>
 __global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __restrict__ img,
                                                        const float* __restrict__ vec, const MLPInput in,
                                                        int rows, float* __restrict__ E, float* __restrict__ U,
@@ -393,7 +394,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __r
         if (MD) {
             float g[NN_DESC];
             if (valid) {
-                nn_md_descriptors(in.q, in.dp, row, in.pack, in.nbr, in.nnb[row], g, status);
+                nn_md_descriptors<STD>(in.q, in.dp, row, in.pack, in.nbr, in.nnb[row], g, status);
                 const bool out = nn_out_of_range(in.dp, g);
                 in.flag[row] = out ? 1 : 0;
                 if (out) atomicAdd(in.count, 1);
@@ -551,18 +552,19 @@ __global__ void __launch_bounds__(MLP_ROWS, 4) k_nn_mlp(const __nv_bfloat16* __r
     if (warp == 0) tmem_dealloc(tmem, MLP_TMEM_COLS);
 }
 
-template <bool MD>
+template <bool MD, bool STD = false>
 static cudaError_t mlp_launch(const NNDevNet& net, const MLPInput& in, int rows, float* E, float* u,
                               unsigned* status, int num_sms, cudaStream_t s) {
     if (rows <= 0) return cudaSuccess;
     const size_t smem = sizeof(MLPSmem) + 1024;  // + alignment slack
-    cudaError_t e = cudaFuncSetAttribute(k_nn_mlp<MD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_nn_mlp<MD, STD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int tiles = (rows + MLP_ROWS - 1) / MLP_ROWS;
     // 4 CTAs per SM: about 51 KB of shared memory and 128 of the SM's 512
     // TMEM columns each, so the allocations never wait; four MMA chains overlap
     const int grid = std::min(tiles, 4 * std::max(1, num_sms));
-    k_nn_mlp<MD><<<grid, MLP_ROWS, smem, s>>>(net.img, net.vec, in, rows, E, u, status, tc_wait_polls());
+    k_nn_mlp<MD, STD><<<grid, MLP_ROWS, smem, s>>>(net.img, net.vec, in, rows, E, u, status, tc_wait_polls());
     return cudaGetLastError();
 }
 
@@ -573,9 +575,9 @@ cudaError_t nn_mlp_launch(const NNDevNet& net, const float* gt, int rows, float*
     return mlp_launch<false>(net, in, rows, E, u, status, num_sms, s);
 }
 
-cudaError_t nn_mlp_md_launch(const NNDevNet& net, const NNMD& q, const NNDescParams& dp, const PosPack* pack,
-                             const unsigned* nbr, const int* nnb, int* flag, int* count, float* E, float* u,
-                             unsigned* status, int num_sms, cudaStream_t s) {
+cudaError_t nn_mlp_md_launch(const NNDevNet& net, const NNMD& q, const NNDescParams& dp, bool std_ang,
+                             const PosPack* pack, const unsigned* nbr, const int* nnb, int* flag, int* count,
+                             float* E, float* u, unsigned* status, int num_sms, cudaStream_t s) {
     MLPInput in{};
     in.q = q;
     in.dp = dp;
@@ -584,7 +586,8 @@ cudaError_t nn_mlp_md_launch(const NNDevNet& net, const NNMD& q, const NNDescPar
     in.nnb = nnb;
     in.flag = flag;
     in.count = count;
-    return mlp_launch<true>(net, in, q.n, E, u, status, num_sms, s);
+    return std_ang ? mlp_launch<true, true>(net, in, q.n, E, u, status, num_sms, s)
+                   : mlp_launch<true, false>(net, in, q.n, E, u, status, num_sms, s);
 }
 
 }  // namespace omdg

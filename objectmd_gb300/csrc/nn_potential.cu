@@ -27,6 +27,8 @@ struct NNState {
     int fallback = -1;     // index of the Tersoff potential in ctx->pots
 };
 
+// STD: the default angular layout (zeta and lambda constants of the term loop)
+template <bool STD>
 __global__ void __launch_bounds__(128) k_nn_md_desc(NNMD q, NNDescParams p, const PosPack* __restrict__ pack,
                                                     const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                     float* __restrict__ Gt, int* __restrict__ flag, int* count,
@@ -34,7 +36,7 @@ __global__ void __launch_bounds__(128) k_nn_md_desc(NNMD q, NNDescParams p, cons
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= q.n) return;
     float g[NN_DESC];
-    nn_md_descriptors(q, p, i, pack, nbr, nnb[i], g, status);
+    nn_md_descriptors<STD>(q, p, i, pack, nbr, nnb[i], g, status);
     float4* dst = reinterpret_cast<float4*>(Gt + (size_t)i * NN_DESC);
 #pragma unroll
     for (int k = 0; k < NN_DESC; k += 4) {
@@ -50,7 +52,10 @@ __global__ void __launch_bounds__(128) k_nn_md_desc(NNMD q, NNDescParams p, cons
     if (out) atomicAdd(count, 1);
 }
 
-__global__ void __launch_bounds__(128) k_nn_md_force(NNMD q, NNDescParams p, const PosPack* __restrict__ pack,
+// STD holds the shared powers of both bases: 80 registers at six blocks per
+// SM, where unbounded it takes 96 (five blocks)
+template <bool STD>
+__global__ void __launch_bounds__(128, STD ? 6 : 7) k_nn_md_force(NNMD q, NNDescParams p, const PosPack* __restrict__ pack,
                                                      const unsigned* __restrict__ nbr, const int* __restrict__ nnb,
                                                      const float* __restrict__ E, const float* __restrict__ U,
                                                      const int* __restrict__ flag, float4* __restrict__ slot,
@@ -110,8 +115,8 @@ __global__ void __launch_bounds__(128) k_nn_md_force(NNMD q, NNDescParams p, con
 #pragma unroll
                 for (int mm = 0; mm < NN_ANG; mm++) {
                     float v, d_ra, d_rb, d_cs;
-                    nn_angular(p, mm, rr[a], rr[b], cs, fa, dfa, fb, dfb, ex.get(p.eta_a[mm], s2), v, d_ra, d_rb,
-                               d_cs);
+                    nn_angular<STD>(p, mm, rr[a], rr[b], cs, fa, dfa, fb, dfb, ex.get(p.eta_a[mm], s2), v, d_ra,
+                                    d_rb, d_cs);
                     const float w = u[NN_RAD + mm];
                     cra = fmaf(w, d_ra, cra);
                     crb = fmaf(w, d_rb, crb);
@@ -185,18 +190,19 @@ int nn_launch(Context* c, Potential& pot, bool first) {
     const unsigned grid = (unsigned)grid_for(c->n, 128);
     const unsigned* nbr = reinterpret_cast<const unsigned*>(c->nbr);
     cudaMemsetAsync(s.count, 0, sizeof(int), c->stream);
+    const bool std_ang = nn_std_angular(s.model.dp);
     cudaError_t e;
     if (c->nn_fused) {
         // descriptors computed by the network kernel's own threads
         prof_begin(c, "nn_desc_mlp");
-        e = nn_mlp_md_launch(s.net, q, s.model.dp, c->pack, nbr, c->nnb, s.flag, s.count, s.E, s.U, c->d_status,
-                             c->num_sms, c->stream);
+        e = nn_mlp_md_launch(s.net, q, s.model.dp, std_ang, c->pack, nbr, c->nnb, s.flag, s.count, s.E, s.U,
+                             c->d_status, c->num_sms, c->stream);
         prof_end(c);
         c->launches -= 1;
     } else {
         prof_begin(c, "nn_descriptors");
-        k_nn_md_desc<<<grid, 128, 0, c->stream>>>(q, s.model.dp, c->pack, nbr, c->nnb, s.Gt, s.flag, s.count,
-                                                  c->d_status);
+        auto desc = std_ang ? k_nn_md_desc<true> : k_nn_md_desc<false>;
+        desc<<<grid, 128, 0, c->stream>>>(q, s.model.dp, c->pack, nbr, c->nnb, s.Gt, s.flag, s.count, c->d_status);
         prof_end(c);
         prof_begin(c, "nn_mlp");
         e = nn_mlp_launch(s.net, s.Gt, c->n, s.E, s.U, c->d_status, c->num_sms, c->stream);
@@ -204,8 +210,9 @@ int nn_launch(Context* c, Potential& pot, bool first) {
     }
     if (e != cudaSuccess) return check_cuda(c, e, "surrogate network");
     prof_begin(c, "nn_force");
-    k_nn_md_force<<<grid, 128, 0, c->stream>>>(q, s.model.dp, c->pack, nbr, c->nnb, s.E, s.U, s.flag, c->slot_buf,
-                                               c->fx, c->fy, c->fz, c->pe, c->vir, c->d_status);
+    auto force = std_ang ? k_nn_md_force<true> : k_nn_md_force<false>;
+    force<<<grid, 128, 0, c->stream>>>(q, s.model.dp, c->pack, nbr, c->nnb, s.E, s.U, s.flag, c->slot_buf, c->fx,
+                                       c->fy, c->fz, c->pe, c->vir, c->d_status);
     prof_end(c);
     c->launches += 3;
     if ((rc = check_cuda(c, cudaGetLastError(), "surrogate"))) return rc;

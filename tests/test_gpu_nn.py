@@ -46,10 +46,12 @@ def dataset(oracle_lib):
     return confs
 
 
-def make_network(omdg, confs, seed=3):
+def make_network(omdg, confs, seed=3, desc=None):
     from oracle import nn_oracle as nn
 
     net = omdg.Network(0)
+    if desc is not None:
+        net.set_descriptors(*desc)
     net.set_dataset([len(c["x"]) for c in confs], np.concatenate([c["x"] for c in confs]),
                     [np.asarray(c["hi"]) - np.asarray(c["lo"]) for c in confs], [c["E"] for c in confs],
                     np.concatenate([c["F"] for c in confs]))
@@ -130,6 +132,28 @@ def surrogate_context(omdg, c, model, fallback):
 def test_md_path_matches_prediction(omdg_lib, dataset, tmp_path):
     net, w, norm = make_network(omdg_lib, dataset)
     model = str(tmp_path / "model.nn")
+    net.save(model)
+    E, F = net.predict(1, 1)
+    net.close()
+    with surrogate_context(omdg_lib, dataset[1], model, True) as ctx:
+        st = ctx.get_state()
+        assert ctx.nn_fallback_atoms() == 0
+    assert np.abs(st["pot"] - E).max() < 2e-3
+    assert np.linalg.norm(st["f"] - F) / np.linalg.norm(F) < 2e-3
+
+
+def test_md_path_with_another_angular_layout(omdg_lib, dataset, tmp_path):
+    """The MD kernels take zeta and lambda as constants when the angular set
+    has the default layout (zeta 1, 2, 4, 8 in pairs, lambda +1 then -1).
+    Here lambda comes -1 first and zeta 3 stands in for 4, so the MD path
+    runs its general kernels; they too equal the trainer's prediction."""
+    from oracle import nn_oracle as nn
+
+    p = nn.descriptor_params()
+    zeta = np.where(p["zeta"] == 4, 3, p["zeta"]).astype(np.int32)
+    desc = (p["rs"], p["eta_r"], zeta, -np.asarray(p["lam"]), p["eta_a"])
+    net, _, _ = make_network(omdg_lib, dataset, desc=desc)
+    model = str(tmp_path / "layout.nn")
     net.save(model)
     E, F = net.predict(1, 1)
     net.close()

@@ -216,7 +216,7 @@ int nn_launch(Context* c, Potential& pot, bool first) {
     prof_end(c);
     c->launches += 3;
     if ((rc = check_cuda(c, cudaGetLastError(), "surrogate"))) return rc;
-    if (s.fallback >= 0 && (rc = tersoff_centre(c, c->pots[s.fallback], false, s.flag))) return rc;
+    if (s.fallback >= 0 && (rc = tersoff_centre(c, c->pots[s.fallback], false, s.flag, s.count))) return rc;
     return gather_slots(c, false);
 }
 

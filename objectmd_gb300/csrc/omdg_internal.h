@@ -393,7 +393,9 @@ int zero_forces(Context* c);
 int upload_state(Context* c, const double* in_x, const double* in_v);
 int resolve_thermostat(Context* c);
 int gather_slots(Context* c, bool zero_virial);
-int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask);
+// mask: only centres i with mask[i] != 0; mask_count: device count of them
+// (0: the pass does no work)
+int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask, const int* mask_count = nullptr);
 int nn_launch(Context* c, Potential& pot, bool first);
 int replica_prepare(Context* c);  // per-replica cell grids and shifts (host, before a build)
 int thermo_detect(Context* c, bool after_step);  // local thermodynamics (ttm.cu); after_step: the step advanced the ledger row

@@ -584,7 +584,9 @@ __global__ void __launch_bounds__(128, TERS_CTAS_PER_SM) k_tersoff_a(TersDev p, 
                                                    float4* __restrict__ slot, float* __restrict__ fx,
                                                    float* __restrict__ fy, float* __restrict__ fz,
                                                    float* __restrict__ pe, float* __restrict__ vir, unsigned* status,
-                                                   const int* __restrict__ mask, int* __restrict__ wide) {
+                                                   const int* __restrict__ mask, int* __restrict__ wide,
+                                                   const int* __restrict__ nmask) {
+    if (nmask && *nmask == 0) return;  // a mask with no centre in it
     if (PERSISTENT) {
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x)
             ters_reg_centre(p, i, pack, nbr, nnb, slot, fx, fy, fz, pe, vir, mask, wide);
@@ -804,7 +806,7 @@ int tersoff_launch(Context* c, Potential& pot, bool first) {
 
 // Pass A of Tersoff: bond gradients of every centre (or of the centres with
 // mask[i] != 0) into the slot buffer; the caller gathers.
-int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask) {
+int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask, const int* mask_count) {
     if (!c->rev || !c->slot_buf) return set_error(c, OMDG_ESTATE, "three-body buffers missing");
     const TersoffParams& t = pot.ters;
     TersDev p;
@@ -833,14 +835,17 @@ int tersoff_centre(Context* c, Potential& pot, bool first, const int* mask) {
     p.first = first ? 1 : 0;
     prof_begin(c, mask ? "tersoff_fallback" : "tersoff_centre");
     cudaMemsetAsync(c->ters_wide, 0, sizeof(int), c->stream);
-    if (c->tb_persistent)
+    // a masked pass (the surrogate's fallback, usually for no centre at all)
+    // takes the strided form: one resident grid, each block gone after
+    // reading the count
+    if (c->tb_persistent || mask_count)
         k_tersoff_a<true><<<std::min(grid_for(c->n, 128), TERS_CTAS_PER_SM * c->num_sms), 128, 0, c->stream>>>(
             p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->slot_buf, c->fx, c->fy, c->fz, c->pe,
-            c->vir, c->d_status, mask, c->ters_wide);
+            c->vir, c->d_status, mask, c->ters_wide, mask_count);
     else
         k_tersoff_a<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(
             p, c->pack, reinterpret_cast<const unsigned*>(c->nbr), c->nnb, c->slot_buf, c->fx, c->fy, c->fz, c->pe,
-            c->vir, c->d_status, mask, c->ters_wide);
+            c->vir, c->d_status, mask, c->ters_wide, mask_count);
     k_tersoff_wide<<<2 * c->num_sms, 128, 0, c->stream>>>(p, c->pack, reinterpret_cast<const unsigned*>(c->nbr),
                                                           c->nnb, c->ters_wide, c->slot_buf, c->fx, c->fy, c->fz,
                                                           c->pe, c->vir, c->d_status);

@@ -286,7 +286,10 @@ int omdg_ttm_state(omdg_ctx* ctx, double* electron_temperature, double* int_een,
  * from the analytic gradient.  model_file is written by omdg_nn_save.  With
  * tersoff_fallback (a Tersoff parameter file, as for omdg_add_tersoff) every
  * atom whose descriptors leave the training range takes its energy and
- * forces from Tersoff instead; NULL disables the fallback.
+ * forces from Tersoff instead; NULL disables the fallback.  A model whose
+ * angular terms keep the default layout (zeta 1, 1, 2, 2, 4, 4, 8, 8 twice,
+ * lambda alternating +1, -1) runs descriptor and force kernels specialised
+ * for it; any other layout runs general kernels with the same results.
  */
 int omdg_add_nn(omdg_ctx* ctx, int type_a, int type_b, const char* model_file, const char* tersoff_fallback);
 /* Atoms handed to the Tersoff fallback in the last force evaluation. */

@@ -289,7 +289,8 @@ int omdg_ttm_state(omdg_ctx* ctx, double* electron_temperature, double* int_een,
  * forces from Tersoff instead; NULL disables the fallback.  A model whose
  * angular terms keep the default layout (zeta 1, 1, 2, 2, 4, 4, 8, 8 twice,
  * lambda alternating +1, -1) runs descriptor and force kernels specialised
- * for it; any other layout runs general kernels with the same results.
+ * for it; any other layout runs general kernels (the same terms, without
+ * the powers shared across terms).
  */
 int omdg_add_nn(omdg_ctx* ctx, int type_a, int type_b, const char* model_file, const char* tersoff_fallback);
 /* Atoms handed to the Tersoff fallback in the last force evaluation. */

@@ -65,3 +65,32 @@ def test_reference_arm_prints_on_rank_zero_only(monkeypatch):
     with contextlib.redirect_stdout(out):
         bench.run_reference(args)
     assert out.getvalue() == ""
+
+
+def test_reference_arm_line_keeps_the_contract(oracle_lib, monkeypatch):
+    """Rank 0 of the reference arm prints one JSON line with the base keys,
+    impl "reference", both rebuild policies, a cpu_baseline describing the
+    run and an e2e object with no host-device bytes (LJ Ar 4000, the oracle
+    port on this host)."""
+    import json
+
+    import bench
+
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    args = bench.argparse.Namespace(workload="lj_ar_4000", ncell=0, steps=1, warmup=0)
+    out = io.StringIO()
+    with contextlib.redirect_stdout(out):
+        bench.run_reference(args)
+    lines = [ln for ln in out.getvalue().splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == bench.UNIT and d["metric"] == bench.METRIC
+    assert set(d["rebuild_policies"]) == {"every_step", "refresh_10"}
+    assert d["value"] == max(p["value"] for p in d["rebuild_policies"].values())
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

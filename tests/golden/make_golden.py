@@ -382,6 +382,33 @@ def example_case():
     print("wrote example_pt_fcc111", len(start), "atoms", len(steps), "steps")
 
 
+def read_cluster(path):
+    """Positions (first three columns) of one of the reference's own silicon
+    test clusters (test/check-verlet-list: dimer, trimer, tetra, 1x1x1)."""
+    rows = []
+    with open(path) as fh:
+        for line in fh:
+            t = line.split()
+            if t and not line.startswith("#"):
+                rows.append([float(v) for v in t[:3]])
+    return np.array(rows)
+
+
+def clusters_case(tdir, work):
+    """SW Si on the reference's own test clusters, free boundaries: the
+    reference built without the sw.cpp:261 guard (every triplet) and as
+    shipped, with its full neighbour tuples."""
+    for name in ("dimer", "trimer", "tetra", "1x1x1"):
+        x = read_cluster(os.path.join(REF, "test", "check-verlet-list", name))
+        lo, hi = x.min(0) - 5.0, x.max(0) + 5.0
+        f = os.path.join(work, "sw_si_%s.dat" % name)
+        inputs.write_import(f, x, None, box=(lo, hi), periodic=(False, False, False), species=("silicon",))
+        res = oc.run_reference(f, "sw", "silicon", steps=0, dump_nbr=True, table_dir=tdir, swfix=True)
+        asis = oc.run_reference(f, "sw", "silicon", steps=0, table_dir=tdir, swfix=False)
+        save_case("sw_si_%s" % name, f, res, box_lo=lo, box_hi=hi, f_asis=asis["atoms"][:, 8:11],
+                  pot_asis=asis["atoms"][:, 11])
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not REF:
@@ -411,6 +438,9 @@ def main(only=None):
         return
     if only == "example":
         example_case()
+        return
+    if only == "clusters":
+        clusters_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
         return
     if only == "lj4000":
         lj4000_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))

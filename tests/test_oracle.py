@@ -78,10 +78,29 @@ def test_sw_oracle_matches_fixed_reference(oracle_lib, case):
     assert nbr_set(*nb) == set(map(tuple, d["nbr"].tolist()))
 
 
+@pytest.mark.parametrize("case", ["sw_si_dimer", "sw_si_trimer", "sw_si_tetra", "sw_si_1x1x1"])
+def test_sw_oracle_matches_reference_on_its_own_clusters(oracle_lib, case):
+    """The reference's own silicon test clusters (test/check-verlet-list),
+    free boundaries: forces, per-atom energies and the full neighbour tuples
+    equal the reference built with every triplet evaluated."""
+    oc = oracle_lib
+    d = load_case(case)
+    box = oc.make_box(d["box_lo"], d["box_hi"], (0, 0, 0))
+    x = d["x0"]
+    nb = oc.neighbors(box, x, 2.0951 * 1.8 + 0.3)
+    f, e, vir = oc.sw(box, x, nb, sw_params(oc))
+    assert np.abs(f - d["f"]).max() < 1e-11
+    assert np.abs(e - d["pot"]).max() < 1e-12
+    assert nbr_set(*nb) == set(map(tuple, d["nbr"].tolist()))
+
+
 def test_sw_reference_guard_drops_triplets(oracle_lib):
-    """The unmodified reference (sw.cpp:261) differs from the full triplet sum."""
+    """The unmodified reference (sw.cpp:261) differs from the full triplet sum,
+    already on its own three-atom test cluster."""
     d = load_case("sw_si_216")
     assert np.abs(d["f_asis"] - d["f"]).max() > 1e-3
+    d = load_case("sw_si_trimer")
+    assert np.abs(d["f_asis"] - d["f"]).max() > 1.0
 
 
 def test_sw_forces_are_energy_gradients(oracle_lib):

@@ -409,6 +409,36 @@ def clusters_case(tdir, work):
                   pot_asis=asis["atoms"][:, 11])
 
 
+def impact_replica_case(tdir, work):
+    """The reference's own impact replica (test/si-impact/atom.dat: a Si slab
+    of 10,648 atoms, periodic x/y, free z, and one Ar atom) with its
+    potentials (test/si-impact/main.cpp:70-71: SW between target atoms, the
+    Ar-Si table between projectile and target).  Static forces and energies
+    with the Ar atom over the aim point of test/si-impact/omd-parameter
+    (28.52, 31.27) at 0.5-2.0 A above the top layer."""
+    x, v, t, (lo, hi), per = inputs.read_import(os.path.join(REF, "test", "si-impact", "atom.dat"))
+    order = np.argsort(t, kind="stable")  # targets first: nid follows the containers' order
+    x, v, t = x[order], v[order], t[order]
+    top = x[t == 0, 2].max()
+    hs = [0.5, 1.4, 2.0]
+    fs, ps, xs = [], [], []
+    for k, h in enumerate(hs):
+        xk = x.copy()
+        xk[t == 1] = [28.52, 31.27, top + h]
+        f = os.path.join(work, "impact_replica%d.dat" % k)
+        inputs.write_import(f, xk, v, types=t, box=(lo, hi), periodic=per, species=("silicon", "argon"),
+                            names=("target", "projectile"))
+        res = oc.run_reference(f, "sw", "silicon", steps=0, table_dir=tdir, swfix=True, pair2="ar-si.zbl")
+        a = res["atoms"]
+        fs.append(a[:, 8:11])
+        ps.append(a[:, 11])
+        xs.append(xk[t == 1][0])
+    np.savez_compressed(os.path.join(GOLD, "impact_replica.npz"), x0=x, types=t, box_lo=lo, box_hi=hi,
+                        periodic=np.array(per), ar=np.array(xs), heights=np.array(hs), f=np.array(fs),
+                        pot=np.array(ps))
+    print("wrote impact_replica", len(x), "atoms")
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not REF:
@@ -438,6 +468,9 @@ def main(only=None):
         return
     if only == "example":
         example_case()
+        return
+    if only == "impact_replica":
+        impact_replica_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
         return
     if only == "clusters":
         clusters_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))

@@ -288,3 +288,31 @@ def test_oracle_sw_and_ar_si_table_match_the_reference_impact_slab(oracle_lib):
                             np.zeros(len(x)))
         assert np.abs(f - d["static_f"][k]).max() <= 1e-11 * np.abs(d["static_f"][k]).max()
         assert np.abs(e - d["static_pot"][k]).max() <= 1e-12
+
+
+def test_oracle_matches_the_reference_on_its_own_impact_replica(oracle_lib):
+    """The reference's own impact replica (test/si-impact/atom.dat: 10,648 Si
+    atoms, periodic x/y, free z, one Ar) with its potentials (SW between Si
+    atoms, the Ar-Si table between Ar and Si, test/si-impact/main.cpp:70-71)
+    and the Ar atom 0.5-2.0 A above the aim point of its parameter file:
+    forces and per-atom energies equal the reference's."""
+    oc = oracle_lib
+    d = dict(np.load(os.path.join(GOLD, "impact_replica.npz")))
+    phi = oc.Table.from_file(os.path.join(GOLD, "tables", "pair.ar-si.zbl"))
+    types = d["types"]
+    si = types == 0
+    box = oc.make_box(d["box_lo"], d["box_hi"], tuple(int(p) for p in d["periodic"]))
+    for k in range(len(d["heights"])):
+        x = d["x0"].copy()
+        x[types == 1] = d["ar"][k]
+        xs = oc.wrap(box, x[si])
+        fs, es, _ = oc.sw(box, xs, oc.neighbors(box, xs, 2.0951 * 1.8 + 0.3), sw_params(oc))
+        f = np.zeros_like(x)
+        e = np.zeros(len(x))
+        f[si], e[si] = fs, es
+        x[si] = xs
+        oc.pair_table_typed(box, x, types, 1, 0, oc.neighbors(box, x, phi.max_range() + 0.3), phi, f, e,
+                            np.zeros(len(x)))
+        assert np.abs(f - d["f"][k]).max() <= 1e-11 * np.abs(d["f"][k]).max()
+        assert np.abs(e - d["pot"][k]).max() <= 1e-12
+        assert np.abs(d["f"][k][types == 1]).max() > 1.0  # the Ar-Si term acts

@@ -439,6 +439,39 @@ def impact_replica_case(tdir, work):
     print("wrote impact_replica", len(x), "atoms")
 
 
+def ar_pt_case(tdir, work):
+    """Two atom types with EAM on one of them, as test/two_elements/two.cpp
+    combines them: EAM platinum between Pt atoms (type 0, "target") and the
+    reference's Ar-Pt table (tables/pair.ar-pt.zbl) between the Ar atom
+    (type 1, "projectile") and Pt.  An FCC Pt slab of 6 x 6 x 3 cells
+    (a = 3.924, periodic x/y, free z, Gaussian displacements 0.05 A) with the
+    Ar atom 1.2-2.8 A above a surface atom.  Static forces and energies."""
+    shutil.copy(os.path.join(REF, "tables", "pair.ar-pt.zbl"), os.path.join(TABLES, "pair.ar-pt.zbl"))
+    tdir = table_dir()  # with the table just written
+    a = 3.924
+    x, lo, hi = inputs.lattice(inputs.FCC_BASIS, (6, 6, 3), a, 0.25)
+    x = inputs.perturb(x, 0.05, 81, lo, hi, (True, True, False))
+    top = np.where(x[:, 2] > x[:, 2].max() - 0.5)[0]
+    s = top[np.argmin(np.sum((x[top, :2] - np.array([2.6 * a, 3.1 * a])) ** 2, axis=1))]
+    hi = np.array([hi[0], hi[1], x[:, 2].max() + 12.0])
+    types = np.concatenate([np.zeros(len(x), dtype=np.int32), [1]]).astype(np.int32)
+    hs = [1.2, 2.0, 2.8]
+    xs, fs, ps = [], [], []
+    for k, h in enumerate(hs):
+        xk = np.vstack([x, x[s] + np.array([0.3, -0.2, h])])
+        f = os.path.join(work, "ar_pt%d.dat" % k)
+        inputs.write_import(f, xk, None, types=types, box=(lo, hi), periodic=(True, True, False),
+                            species=("platinum", "argon"), names=("target", "projectile"))
+        res = oc.run_reference(f, "eam", "platinum", steps=0, table_dir=tdir, pair2="ar-pt.zbl")
+        at = res["atoms"]
+        xs.append(xk)
+        fs.append(at[:, 8:11])
+        ps.append(at[:, 11])
+    np.savez_compressed(os.path.join(GOLD, "ar_pt_slab.npz"), x0=np.array(xs), types=types, box_lo=lo, box_hi=hi,
+                        heights=np.array(hs), f=np.array(fs), pot=np.array(ps))
+    print("wrote ar_pt_slab", len(types), "atoms")
+
+
 def main(only=None):
     os.makedirs(TABLES, exist_ok=True)
     if not REF:
@@ -468,6 +501,9 @@ def main(only=None):
         return
     if only == "example":
         example_case()
+        return
+    if only == "ar_pt":
+        ar_pt_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))
         return
     if only == "impact_replica":
         impact_replica_case(table_dir(), tempfile.mkdtemp(prefix="omdgold_"))

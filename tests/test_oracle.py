@@ -316,3 +316,30 @@ def test_oracle_matches_the_reference_on_its_own_impact_replica(oracle_lib):
         assert np.abs(f - d["f"][k]).max() <= 1e-11 * np.abs(d["f"][k]).max()
         assert np.abs(e - d["pot"][k]).max() <= 1e-12
         assert np.abs(d["f"][k][types == 1]).max() > 1.0  # the Ar-Si term acts
+
+
+def test_oracle_matches_the_reference_with_two_atom_types(oracle_lib):
+    """EAM platinum between Pt atoms and the reference's Ar-Pt table between
+    an Ar atom and Pt (the combination of test/two_elements/two.cpp), Ar
+    1.2-2.8 A above a Pt slab (periodic x/y, free z): forces and per-atom
+    energies equal the reference's."""
+    oc = oracle_lib
+    d = dict(np.load(os.path.join(GOLD, "ar_pt_slab.npz")))
+    table = os.path.join(TABLES, "eam.platinum")
+    phi, ed, em = (oc.Table.from_file(table, sec) for sec in ("PAIR", "EDENS", "EMBED"))
+    zbl = oc.Table.from_file(os.path.join(TABLES, "pair.ar-pt.zbl"))
+    types = d["types"]
+    pt = types == 0
+    box = oc.make_box(d["box_lo"], d["box_hi"], (1, 1, 0))
+    for k in range(len(d["heights"])):
+        x = d["x0"][k].copy()
+        xp = oc.wrap(box, x[pt])
+        fp, ep, _, _ = oc.eam(box, xp, oc.neighbors(box, xp, phi.max_range() + 0.3), phi, ed, em)
+        f = np.zeros_like(x)
+        e = np.zeros(len(x))
+        f[pt], e[pt] = fp, ep
+        x[pt] = xp
+        oc.pair_table_typed(box, x, types, 1, 0, oc.neighbors(box, x, zbl.max_range() + 0.3), zbl, f, e,
+                            np.zeros(len(x)))
+        assert np.abs(f - d["f"][k]).max() <= 1e-11 * np.abs(d["f"][k]).max()
+        assert np.abs(e - d["pot"][k]).max() <= 1e-11

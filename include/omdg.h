@@ -223,7 +223,10 @@ int omdg_tile_counts(omdg_ctx* ctx, int* tiles, int* staged);
  * Launch shapes (no reference counterpart: the reference is scalar C++).
  * Keys: "eam_block", "eam_lanes" (threads per atom), "eam_stage" (spline
  * knots in shared memory), "eam_ctas_per_sm", "pair_block", "pair_lanes",
- * "tb_block", "tb_lanes", "nbr_hshift" (log2 of the neighbour slice height),
+ * "tb_lanes" (the three-body candidate's lanes, which set the neighbour slice
+ * height; its kernels run one thread per centre), "tb_block" (kept for
+ * callers that set it; the three-body kernels run 128-thread blocks),
+ * "nbr_hshift" (log2 of the neighbour slice height),
  * "build_lanes" (list build: 0 cell CTAs, else threads per atom), "io_blocks"
  * (blocks of omdg_step_io's downloads beside the step's kernels), "nbr_capacity"
  * (row capacity of the next first list build; 0 sizes it from the density;

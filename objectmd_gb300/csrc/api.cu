@@ -2004,10 +2004,11 @@ int omdg_autotune(omdg_ctx* c, int reps, double* best_ms) {
         for (int lanes : {2, 4, 8, 16})
             for (int block : {128, 256}) cands.push_back(Cand{lanes, block, 0, tile_on});
     } else if (tb) {
+        // lanes: the neighbour slice height the rows are laid out in (the
+        // three-body kernels run one thread per centre in 128-thread blocks);
         // stage: the Tersoff register pass as one resident grid (persistent)
         for (int lanes : {1, 2, 4})
-            for (int block : {64, 128, 256})
-                for (int stage : {0, 1}) cands.push_back(Cand{lanes, block, stage, tile_on});
+            for (int stage : {0, 1}) cands.push_back(Cand{lanes, 128, stage, tile_on});
     }
     int rc = OMDG_OK;
     // list build: cell-CTA, 8 or 4 lanes per atom, or one thread per atom

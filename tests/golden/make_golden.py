@@ -13,8 +13,15 @@ the GPU tests only read the committed outputs.  Steps:
    - sw.silicon and tersoff.silicon27 parameter files.
 3. Generate seeded atom configurations (objectmd_gb300.inputs) and run the
    reference on them: static forces, per-atom energies, virials and the
-   neighbour tuples, plus a short NVE trajectory.
+   neighbour tuples, plus a short NVE trajectory.  The reference's own test
+   inputs are run too: its silicon clusters (test/check-verlet-list), its
+   impact replica (test/si-impact/atom.dat) and the two-element combination
+   of test/two_elements/two.cpp on a generated Pt slab.
 4. Save each case as <case>.npz with its Import file.
+
+A single group of cases: python tests/golden/make_golden.py <name> with
+<name> one of ttm, checkpoint, output, thermo, modifies, impact, fdtd,
+example, lj4000, clusters, impact_replica, ar_pt.
 """
 from __future__ import annotations
 
